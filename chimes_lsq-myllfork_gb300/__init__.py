@@ -1,0 +1,247 @@
+"""GB300 design-matrix path of ChIMES-lsq: Python mirror of the C ABI.
+
+This package wraps ``libchimes_gb300.so`` (built in-tree by ``build.py``) with
+ctypes.  The names follow the reference's operator surface:
+
+* :class:`Model` parses ``fm_setup.in`` (INPUT::PARSE_INFILE_LSQ, src/input.C:172-225)
+  and exposes the ``params.header`` / ``ff_groups.map`` text
+  (print_param_header / print_map_file, src/chimes_lsq.C:562-716);
+* :class:`Frames` reads ``.xyzf`` trajectories (FRAME::READ_XYZF,
+  src/ClassDefs.C:2411-2683) or takes arrays;
+* :class:`Session` assembles the A matrix on one GPU (the frame loop of
+  src/chimes_lsq.C:292-328 calling ZCalc_Deriv, src/functions.C:755-804).
+
+Errors from the library raise :class:`ChimesError` with the library's message.
+There is no CPU fallback: without the compiled library every call fails.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libchimes_gb300.so")
+
+CG_FP64 = 0
+CG_FP32 = 1
+
+_lib = None
+
+
+class ChimesError(RuntimeError):
+    """A non-zero status from the C ABI."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def build(verbose=False):
+    """Compile the CUDA/C++ library in-tree (sm_103a)."""
+    from importlib import util
+    spec = util.spec_from_file_location("_chimes_gb300_build", os.path.join(_HERE, "build.py"))
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose)
+
+
+def lib():
+    """Load the compiled library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ChimesError(2, f"{LIB_PATH} is missing: run build() first (no CPU fallback exists)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, ip, i64p, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "cg_model_load": (ctypes.c_int, [ctypes.c_char_p, pp]),
+        "cg_model_free": (None, [vp]),
+        "cg_model_columns": (ctypes.c_int, [vp, ip, ip, ip, ip, ip]),
+        "cg_model_sizes": (ctypes.c_int, [vp, ip, ip]),
+        "cg_model_header_text": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "cg_model_map_text": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "cg_frames_read": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int, pp]),
+        "cg_frames_create": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, pp]),
+        "cg_frames_free": (None, [vp]),
+        "cg_frames_rows": (ctypes.c_int, [vp, i64p, i64p]),
+        "cg_frames_labels": (ctypes.c_int, [vp, dp]),
+        "cg_session_create": (ctypes.c_int, [vp, ctypes.c_int, pp]),
+        "cg_session_free": (None, [vp]),
+        "cg_session_stream": (ctypes.c_void_p, [vp]),
+        "cg_assemble": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, ctypes.c_int64]),
+        "cg_frames_upload": (ctypes.c_int, [vp, vp, pp]),
+        "cg_dframes_free": (None, [vp]),
+        "cg_assemble_device": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, ctypes.c_int64]),
+        "cg_session_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p, i64p]),
+        "cg_last_error": (ctypes.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise ChimesError(rc, lib().cg_last_error().decode(errors="replace"))
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class Model:
+    """Parsed fm_setup.in with its pair / cluster topology."""
+
+    def __init__(self, fm_setup_path):
+        h = ctypes.c_void_p()
+        _check(lib().cg_model_load(os.fspath(fm_setup_path).encode(), ctypes.byref(h)))
+        self._h = h
+        self.path = os.fspath(fm_setup_path)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cg_model_free(self._h)
+            self._h = None
+
+    def columns(self):
+        """dict with n2b, n3b, n4b, nener, ntotal (A columns)."""
+        v = [ctypes.c_int() for _ in range(5)]
+        _check(lib().cg_model_columns(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(["n2b", "n3b", "n4b", "nener", "ntotal"], [x.value for x in v]))
+
+    @property
+    def ncols(self):
+        return self.columns()["ntotal"]
+
+    def sizes(self):
+        nf, nt = ctypes.c_int(), ctypes.c_int()
+        _check(lib().cg_model_sizes(self._h, ctypes.byref(nf), ctypes.byref(nt)))
+        return nf.value, nt.value
+
+    def _text(self, fn):
+        need = ctypes.c_size_t()
+        _check(fn(self._h, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value + 1)
+        _check(fn(self._h, buf, need.value + 1, ctypes.byref(need)))
+        return buf.raw[: need.value].decode()
+
+    def params_header(self):
+        return self._text(lib().cg_model_header_text)
+
+    def ff_groups_map(self):
+        return self._text(lib().cg_model_map_text)
+
+
+class Frames:
+    """A batch of frames (one A-matrix row block each)."""
+
+    def __init__(self, handle, model):
+        self._h = handle
+        self.model = model
+
+    @classmethod
+    def read(cls, model, xyzf_path=None, nframes=0):
+        h = ctypes.c_void_p()
+        p = None if xyzf_path is None else os.fspath(xyzf_path).encode()
+        _check(lib().cg_frames_read(model._h, p, int(nframes), ctypes.byref(h)))
+        return cls(h, model)
+
+    @classmethod
+    def from_arrays(cls, model, natoms, types, xyz, cell, forces=None, stress=None, energy=None, first_index=0):
+        """natoms[F]; types[sum N] (TYPEIDX order); xyz[sum N,3] (A); cell[F,9]
+        (ax ay az bx by bz cx cy cz); forces[sum N,3] (Hartree/Bohr); stress[F,6]
+        (xx yy zz xy xz yz, GPa); energy[F]."""
+        natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        forces = None if forces is None else np.ascontiguousarray(forces, dtype=np.float64)
+        stress = None if stress is None else np.ascontiguousarray(stress, dtype=np.float64)
+        energy = None if energy is None else np.ascontiguousarray(energy, dtype=np.float64)
+        h = ctypes.c_void_p()
+        _check(lib().cg_frames_create(model._h, len(natoms), _ptr(natoms), _ptr(types), _ptr(xyz), _ptr(forces),
+                                      _ptr(cell), _ptr(stress), _ptr(energy), int(first_index), ctypes.byref(h)))
+        return cls(h, model)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cg_frames_free(self._h)
+            self._h = None
+
+    def rows(self):
+        r, a = ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().cg_frames_rows(self._h, ctypes.byref(r), ctypes.byref(a)))
+        return r.value, a.value
+
+    @property
+    def nrows(self):
+        return self.rows()[0]
+
+    def labels(self):
+        b = np.empty(self.nrows, dtype=np.float64)
+        _check(lib().cg_frames_labels(self._h, _ptr(b)))
+        return b
+
+
+class DeviceFrames:
+    """Frames resident on the GPU of a session."""
+
+    def __init__(self, handle, nrows):
+        self._h = handle
+        self.nrows = nrows
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cg_dframes_free(self._h)
+            self._h = None
+
+
+class Session:
+    """One GPU (device ordinal) with a CUDA stream, bound to a model."""
+
+    def __init__(self, model, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().cg_session_create(model._h, int(device), ctypes.byref(h)))
+        self._h = h
+        self.model = model
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cg_session_free(self._h)
+            self._h = None
+
+    @property
+    def stream(self):
+        """cudaStream_t of the session as an integer."""
+        return lib().cg_session_stream(self._h) or 0
+
+    def assemble(self, frames, precision=CG_FP64, out=None):
+        """A matrix of the frames in host memory (float64 or float32)."""
+        nrows = frames.nrows
+        ncols = self.model.ncols
+        dt = np.float64 if precision == CG_FP64 else np.float32
+        if out is None:
+            out = np.empty((nrows, ncols), dtype=dt)
+        assert out.dtype == dt and out.flags.c_contiguous and out.shape[0] == nrows
+        _check(lib().cg_assemble(self._h, frames._h, int(precision), _ptr(out), out.shape[1]))
+        return out
+
+    def upload(self, frames):
+        h = ctypes.c_void_p()
+        _check(lib().cg_frames_upload(self._h, frames._h, ctypes.byref(h)))
+        return DeviceFrames(h, frames.nrows)
+
+    def assemble_device(self, dframes, precision, a_device_ptr, lda):
+        """Assemble into a device buffer (asynchronous on the session stream)."""
+        _check(lib().cg_assemble_device(self._h, dframes._h, int(precision), ctypes.c_void_p(int(a_device_ptr)),
+                                        int(lda)))
+
+    def last_counts(self):
+        v = [ctypes.c_int64() for _ in range(5)]
+        _check(lib().cg_session_last_counts(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(["pairs", "triplets", "quads", "evals3", "evals4"], [x.value for x in v]))

@@ -1,0 +1,700 @@
+// Design-matrix (A-matrix) assembly kernels.
+//
+// Reference: Cheby::Deriv_2B / Deriv_3B / Deriv_4B (src/Cheby.C:709-1729) with
+// set_polys / set_polys_out_of_range (src/Cheby.C:207-443) and FCUT::get_fcut
+// (src/Fcut.C:17-72).  The reference loops, per cluster, over every allowed power
+// tuple p and scatters ~50-130 flops into the A rows of the cluster's atoms.
+//
+// GB300 formulation (same sums, different association):
+//  * Force rows are gathered by their owner atom (one CTA per real atom), so
+//    every A entry is written once, without atomics, in a fixed order.
+//  * For an owner at canonical position pi of a cluster, the slots split into the
+//    ones incident to it (I) and the rest (O).  The per-power derivative sum
+//        F_x[p] = sum_{s in I} w_s,x h_s[p_s] prod_{s' != s} g_s'[p_s']
+//    factorises as M_x[p_I] * Q[p_O]; M and Q are tabulated once per cluster in
+//    shared memory, so each (cluster, power) costs 3 FMAs instead of ~40.
+//  * Stress / energy rows are gathered per (frame, cluster type) with the split
+//    S1 = I(0), S2 = O(0):  W_ab[p] = A1_ab[p1] Q2[p2] + Q1[p1] A2_ab[p2],
+//    E[p] = Q1[p1] Q2[p2].
+//  * Powers that PARAM_INDICES maps to one column (permutations of identical
+//    atoms) are contiguous; they are summed in shared memory before the store.
+// g_s[n] = fcut_s T_n(x_s), h_s[n] = d g_s[n] / dr_s.
+#include <cstdio>
+#include "assemble.h"
+
+namespace cgd {
+
+static constexpr double PI_REF = 3.14159265359;   // src/functions.h:48
+
+// ---------------------------------------------------------------- basis
+// Cheby::set_polys (+ out-of-range branch) for one distance; fills T[0..snum], D[0..snum].
+__device__ void cheb_polys(const ModelDev& M, double lambda, double xavg, double xdiff, double smin, double r,
+                           int snum, double* T, double* D) {
+    const bool out = r < smin;
+    const double rr = out ? smin : r;
+    double x, ex = 0.0;
+    if (M.trans == 0) { ex = exp(-rr / lambda); x = (ex - xavg) / xdiff; }
+    else if (M.trans == 1) { x = (1.0 / rr - xavg) / xdiff; }
+    else { x = (rr - xavg) / xdiff; }
+    T[0] = 1.0; T[1] = x;
+    D[0] = 1.0; D[1] = 2.0 * x;
+    for (int i = 2; i <= snum; ++i) {
+        T[i] = 2.0 * x * T[i - 1] - T[i - 2];
+        D[i] = 2.0 * x * D[i - 1] - D[i - 2];
+    }
+    if (out && M.fix == 1) {   // ZERO_DERIV
+        for (int i = 0; i <= snum; ++i) D[i] = 0.0;
+        return;
+    }
+    double dxdr;
+    if (M.trans == 0) dxdr = (-ex / lambda) / xdiff;
+    else if (M.trans == 1) dxdr = -1.0 / (rr * rr * xdiff);
+    else dxdr = 1.0 / xdiff;
+    dxdr *= M.deriv_const;
+    for (int i = snum; i >= 1; --i) D[i] = i * dxdr * D[i - 1];
+    D[0] = 0.0;
+    if (!out) return;
+    if (M.fix == 2) {   // CONSTANT_DERIV
+        for (int i = 0; i <= snum; ++i) T[i] += D[i] * (r - smin);
+    } else {            // SMOOTH
+        const double damp = exp((r - smin) / M.smooth);
+        for (int i = 0; i <= snum; ++i) { T[i] += M.smooth * (damp - 1.0) * D[i]; D[i] *= damp; }
+    }
+}
+
+// FCUT::get_fcut src/Fcut.C:17-72
+__device__ __forceinline__ void fcut_eval(const ModelDev& M, double r, double rmax, double& f, double& fd) {
+    if (M.fcut == 0) {
+        double f0 = 1.0 - r / rmax;
+        f = f0 * f0 * f0;
+        fd = f0 * f0 * (-3.0 / rmax);
+    } else {
+        double th = rmax - M.fcut_offset * rmax;
+        if (r < th) { f = 1.0; fd = 0.0; }
+        else if (r > rmax) { f = 0.0; fd = 0.0; }
+        else {
+            double a = (r - th) / (rmax - th) * PI_REF + PI_REF / 2.0;
+            double ad = PI_REF / (rmax - th);
+            f = 0.5 + 0.5 * sin(a);
+            fd = 0.5 * cos(a) * ad;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- slot tables
+// Canonical slot lists: incident slots of canonical position pi, and the rest.
+__device__ __forceinline__ void role_slots(int NB, int pi, int* I, int* O) {
+    if (NB == 3) {
+        const int ti[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        const int to[3] = {2, 1, 0};
+        I[0] = ti[pi][0]; I[1] = ti[pi][1]; O[0] = to[pi];
+    } else {
+        const int ti[4][3] = {{0, 1, 2}, {0, 3, 4}, {1, 3, 5}, {2, 4, 5}};
+        const int to[4][3] = {{3, 4, 5}, {1, 2, 5}, {0, 2, 4}, {0, 1, 3}};
+        for (int k = 0; k < 3; ++k) { I[k] = ti[pi][k]; O[k] = to[pi][k]; }
+    }
+}
+
+__device__ __forceinline__ void edge_members(int NB, int e, int& a, int& b) {
+    if (NB == 3) { const int ea[3] = {0, 0, 1}, eb[3] = {1, 2, 2}; a = ea[e]; b = eb[e]; }
+    else { const int ea[6] = {0, 0, 0, 1, 1, 2}, eb[6] = {1, 2, 3, 2, 3, 3}; a = ea[e]; b = eb[e]; }
+}
+
+__device__ __forceinline__ int member(int4 m, int k) { return k == 0 ? m.x : (k == 1 ? m.y : (k == 2 ? m.z : m.w)); }
+
+// Basis of the edge that maps to canonical slot s of cluster q: g, h (ord values each),
+// the edge's unit vector oriented first->second actual member, and stress factors.
+struct SlotBasis {
+    int e, ma, mb;
+    double r, rab[3];
+};
+
+__device__ void slot_basis(const ModelDev& M, const FramesDev& F, int NB, int f, int4 mem, int id, int T,
+                           int s, int ord, double* g, double* h, SlotBasis& sb) {
+    const int np = NB == 3 ? 3 : 6;
+    const int8_t* pm = (NB == 3 ? M.pidx3 : M.pidx4) + id * np;
+    int e = 0;
+    for (int k = 0; k < np; ++k) if (pm[k] == s) e = k;
+    int a, b;
+    edge_members(NB, e, a, b);
+    const int N = F.natoms[f];
+    const int64_t gb = F.ghost_ofs[f];
+    const int ga = member(mem, a), gbm = member(mem, b);
+    const BoxDev& B = F.box[f];
+    sb.e = e; sb.ma = a; sb.mb = b;
+    sb.r = dist_exact(B.h, F.scaled + 3 * (gb + ga), F.scaled + 3 * (gb + gbm), sb.rab);
+    const ClusterTypeDev& CT = (NB == 3 ? M.types3 : M.types4)[T];
+    const int* typ = F.type + F.atom_ofs[f];
+    const int pt = M.int_pair_map[typ[ga % N] * M.natmtyp + typ[gbm % N]];
+    double Tn[MAXORD + 1], Dn[MAXORD + 1];
+    cheb_polys(M, M.pairs[pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], sb.r, ord, Tn, Dn);
+    double fc, fd;
+    fcut_eval(M, sb.r, CT.smax[s], fc, fd);
+    for (int n = 0; n < ord; ++n) { g[n] = fc * Tn[n]; h[n] = fc * Dn[n] + fd * Tn[n]; }
+}
+
+// ---------------------------------------------------------------- 2-body force rows
+// One CTA per real atom; threads over the 2-body columns (pair type, n).
+template <typename R>
+__global__ void k_force2(ModelDev M, FramesDev F, NeighDev NB, Buckets inc, const int64_t* key_frame_ofs, R* A,
+                         int64_t lda) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ord = M.order2;
+    const int ncol = M.npairs * ord;
+    R* sD = reinterpret_cast<R*>(smem_raw);            // [chunk][3*ord]
+    int* sPt = reinterpret_cast<int*>(sD + (size_t)blockDim.x * 3 * ord);
+    const int gatom = blockIdx.x;
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (F.atom_ofs[mid] <= gatom) lo = mid; else hi = mid - 1; }
+    const int f = lo;
+    const int a = gatom - (int)F.atom_ofs[f];
+    const BoxDev& B = F.box[f];
+    const int64_t kb = key_frame_ofs[f];
+    const int64_t e0 = inc.key_ofs[kb + a], e1 = inc.key_ofs[kb + a + 1];
+    const int64_t pbase = NB.ofs2[F.atom_ofs[f]];   // first 2B pair of the frame
+    constexpr int MAXC = 8;
+    R acc[MAXC][3];
+    for (int c = 0; c < MAXC; ++c) acc[c][0] = acc[c][1] = acc[c][2] = R(0);
+    for (int64_t c0 = e0; c0 < e1; c0 += blockDim.x) {
+        const int64_t ei = c0 + threadIdx.x;
+        if (ei < e1) {
+            const int v = inc.val[ei];
+            const int64_t p = pbase + (v >> 1);
+            const double sgn = (v & 1) ? -1.0 : 1.0;
+            const int pt = NB.pt2[p];
+            const double r = NB.r2[p];
+            const PairDev P = M.pairs[pt];
+            double Tn[MAXORD + 1], Dn[MAXORD + 1];
+            cheb_polys(M, P.lambda, P.xavg, P.xdiff, P.smin, r, ord, Tn, Dn);
+            double fc, fd;
+            fcut_eval(M, r, P.smax, fc, fd);
+            const double ux = NB.rab2[3 * p] / r, uy = NB.rab2[3 * p + 1] / r, uz = NB.rab2[3 * p + 2] / r;
+            R* d = sD + (size_t)threadIdx.x * 3 * ord;
+            for (int n = 0; n < ord; ++n) {
+                const double t = sgn * B.perm2 * (fc * Dn[n + 1] + fd * Tn[n + 1]);
+                d[3 * n] = R(t * ux); d[3 * n + 1] = R(t * uy); d[3 * n + 2] = R(t * uz);
+            }
+            sPt[threadIdx.x] = pt;
+        }
+        __syncthreads();
+        const int cnt = (int)min((int64_t)blockDim.x, e1 - c0);
+        for (int c = 0; c < MAXC; ++c) {
+            const int col = threadIdx.x + c * blockDim.x;
+            if (col >= ncol) break;
+            const int pt = col / ord, n = col % ord;
+            for (int k = 0; k < cnt; ++k) {
+                if (sPt[k] != pt) continue;
+                const R* d = sD + (size_t)k * 3 * ord + 3 * n;
+                acc[c][0] += d[0]; acc[c][1] += d[1]; acc[c][2] += d[2];
+            }
+        }
+        __syncthreads();
+    }
+    const int64_t row = F.row_ofs[f] + 3 * a;
+    for (int c = 0; c < MAXC; ++c) {
+        const int col = threadIdx.x + c * blockDim.x;
+        if (col >= ncol) break;
+        A[(row + 0) * lda + col] = acc[c][0];
+        A[(row + 1) * lda + col] = acc[c][1];
+        A[(row + 2) * lda + col] = acc[c][2];
+    }
+}
+
+// ---------------------------------------------------------------- 2-body stress/energy rows
+// One CTA per frame; threads over the 2-body columns.  comps: 0 E, 1 xx, 2 yy, 3 zz, 4 xy, 5 xz, 6 yz.
+template <typename R>
+__global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t lda) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ord = M.order2;
+    const int ncol = M.npairs * ord;
+    const int f = blockIdx.x;
+    const int srows = F.stress_rows[f], erows = F.energy_rows[f];
+    if (srows == 0 && erows == 0) return;
+    R* sGH = reinterpret_cast<R*>(smem_raw);                      // [chunk][2*ord]
+    R* sV = sGH + (size_t)blockDim.x * 2 * ord;                    // [chunk][6]
+    int* sPt = reinterpret_cast<int*>(sV + (size_t)blockDim.x * 6);
+    const BoxDev& B = F.box[f];
+    const int64_t p0 = NB.ofs2[F.atom_ofs[f]], p1 = NB.ofs2[F.atom_ofs[f + 1]];
+    constexpr int MAXC = 8;
+    R acc[MAXC][7];
+    for (int c = 0; c < MAXC; ++c) for (int k = 0; k < 7; ++k) acc[c][k] = R(0);
+    for (int64_t c0 = p0; c0 < p1; c0 += blockDim.x) {
+        const int64_t p = c0 + threadIdx.x;
+        if (p < p1) {
+            const int pt = NB.pt2[p];
+            const double r = NB.r2[p];
+            const PairDev P = M.pairs[pt];
+            double Tn[MAXORD + 1], Dn[MAXORD + 1];
+            cheb_polys(M, P.lambda, P.xavg, P.xdiff, P.smin, r, ord, Tn, Dn);
+            double fc, fd;
+            fcut_eval(M, r, P.smax, fc, fd);
+            R* gh = sGH + (size_t)threadIdx.x * 2 * ord;
+            for (int n = 0; n < ord; ++n) {
+                gh[2 * n] = R(B.perm2 * fc * Tn[n + 1]);
+                gh[2 * n + 1] = R(B.perm2 * (fc * Dn[n + 1] + fd * Tn[n + 1]));
+            }
+            const double* x = NB.rab2 + 3 * p;
+            R* v = sV + (size_t)threadIdx.x * 6;
+            v[0] = R(x[0] * x[0] / r); v[1] = R(x[1] * x[1] / r); v[2] = R(x[2] * x[2] / r);
+            v[3] = R(x[0] * x[1] / r); v[4] = R(x[0] * x[2] / r); v[5] = R(x[1] * x[2] / r);
+            sPt[threadIdx.x] = pt;
+        }
+        __syncthreads();
+        const int cnt = (int)min((int64_t)blockDim.x, p1 - c0);
+        for (int c = 0; c < MAXC; ++c) {
+            const int col = threadIdx.x + c * blockDim.x;
+            if (col >= ncol) break;
+            const int pt = col / ord, n = col % ord;
+            for (int k = 0; k < cnt; ++k) {
+                if (sPt[k] != pt) continue;
+                const R* gh = sGH + (size_t)k * 2 * ord + 2 * n;
+                const R* v = sV + (size_t)k * 6;
+                acc[c][0] += gh[0];
+                for (int q = 0; q < 6; ++q) acc[c][1 + q] -= gh[1] * v[q];
+            }
+        }
+        __syncthreads();
+    }
+    const double inv_vol = 1.0 / B.vol;
+    for (int c = 0; c < MAXC; ++c) {
+        const int col = threadIdx.x + c * blockDim.x;
+        if (col >= ncol) break;
+        write_virial_rows(F, f, col, acc[c], inv_vol, A, lda);
+    }
+}
+
+// ---------------------------------------------------------------- many-body force rows
+// One CTA per real (owner) atom.  PPT powers per thread cover every allowed power
+// tuple of the largest cluster type, so the accumulators stay in registers.
+template <int NBODY, typename R, int PPT>
+__global__ void __launch_bounds__(MB_THREADS) k_force_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
+                                                         const int64_t* key_frame_ofs, R* A, int64_t lda) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    constexpr int NI = NBODY - 1;
+    constexpr int NO = NP - NI;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ord = NBODY == 3 ? M.order3 : M.order4;
+    const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
+    const ClusterTypeDev* types = NBODY == 3 ? M.types3 : M.types4;
+    const uint8_t* pows = NBODY == 3 ? M.pow3 : M.pow4;
+    const int* grps = NBODY == 3 ? M.grp3 : M.grp4;
+    const int8_t* revs = NBODY == 3 ? M.rev3 : M.rev4;
+    int sizeI = 1, sizeO = 1;
+    for (int k = 0; k < NI; ++k) sizeI *= ord;
+    for (int k = 0; k < NO; ++k) sizeO *= ord;
+    const int per = 3 * sizeI + sizeO;
+    const int nkeys = ntypes * 4;
+    int max_allowed = 0;
+    for (int t = 0; t < ntypes; ++t) max_allowed = max(max_allowed, types[t].n_allowed);
+    const MbForceSmem L = mb_force_smem(NBODY, ord, nkeys, max_allowed, (int)sizeof(R));
+    int* sEnt = reinterpret_cast<int*>(smem_raw + L.ent);
+    int* sKey = reinterpret_cast<int*>(smem_raw + L.key);
+    int* sOrd = reinterpret_cast<int*>(smem_raw + L.ord);
+    int* sCnt = reinterpret_cast<int*>(smem_raw + L.cnt);
+    int* sQ = reinterpret_cast<int*>(smem_raw + L.q);
+    int* sPi = reinterpret_cast<int*>(smem_raw + L.pi);
+    double* sGH = reinterpret_cast<double*>(smem_raw + L.gh);
+    double* sW = reinterpret_cast<double*>(smem_raw + L.w);
+    R* sTab = reinterpret_cast<R*>(smem_raw + L.tab);
+
+    const int gatom = blockIdx.x;
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (F.atom_ofs[mid] <= gatom) lo = mid; else hi = mid - 1; }
+    const int f = lo;
+    const int a = gatom - (int)F.atom_ofs[f];
+    const int N = F.natoms[f];
+    const BoxDev& B = F.box[f];
+    const double perm = NBODY == 3 ? B.perm3 : B.perm4;
+    const int64_t kb = key_frame_ofs[f];
+    const int64_t e0 = inc.key_ofs[kb + a], e1 = inc.key_ofs[kb + a + 1];
+    const bool single_pass = (e1 - e0) <= MB_MAX_ENT;
+    const int64_t qbase = CS.ofs[F.atom_ofs[f]];
+    const int* typ = F.type + F.atom_ofs[f];
+    const int64_t row = F.row_ofs[f] + 3 * (int64_t)a;
+    const int lane = threadIdx.x & 31;
+
+    for (int64_t c0 = e0; c0 < e1; c0 += MB_MAX_ENT) {
+        const int nent = (int)min((int64_t)MB_MAX_ENT, e1 - c0);
+        for (int k = threadIdx.x; k <= nkeys; k += blockDim.x) sCnt[k] = 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < nent; k += blockDim.x) {
+            const int v = inc.val[c0 + k];
+            const int q = v >> 2, m = v & 3;
+            const int4 mm = CS.m[qbase + q];
+            const int T = CS.type[qbase + q];
+            int id = 0, w = 1;
+            for (int t = 0; t < NBODY; ++t) { id += w * (typ[member(mm, t) % N] + 1); w *= 10; }
+            const int pi = revs[id * NBODY + m];
+            sEnt[k] = v;
+            sKey[k] = T * 4 + pi;
+            atomicAdd(&sCnt[T * 4 + pi + 1], 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) for (int k = 1; k <= nkeys; ++k) sCnt[k] += sCnt[k - 1];
+        __syncthreads();
+        if (threadIdx.x < 32) {   // stable placement by (type, role), 32 entries at a time
+            for (int b = 0; b < nent; b += 32) {
+                const int k = b + lane;
+                const bool act = k < nent;
+                const int key = act ? sKey[k] : -1 - lane;
+                const unsigned peers = __match_any_sync(0xffffffffu, key);
+                const int leader = __ffs(peers) - 1;
+                const int rank = __popc(peers & ((1u << lane) - 1u));
+                int st = 0;
+                if (act && lane == leader) st = sCnt[key];
+                st = __shfl_sync(0xffffffffu, st, leader);
+                if (act) sOrd[st + rank] = k;
+                __syncwarp();
+                if (act && lane == leader) sCnt[key] = st + __popc(peers);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        // sCnt[key] now holds the end of each key; starts are the previous key's end
+        for (int T = 0; T < ntypes; ++T) {
+            const int gbeg = T == 0 ? 0 : sCnt[T * 4 - 1], gend = sCnt[T * 4 + 3];
+            if (gbeg == gend) continue;
+            const ClusterTypeDev& CT = types[T];
+            R acc[PPT][3];
+#pragma unroll
+            for (int k = 0; k < PPT; ++k) acc[k][0] = acc[k][1] = acc[k][2] = R(0);
+            for (int pi = 0; pi < NBODY; ++pi) {
+                const int key = T * 4 + pi;
+                const int rb = key == 0 ? 0 : sCnt[key - 1], re = sCnt[key];
+                if (rb == re) continue;
+                int I[3], O[3];
+                role_slots(NBODY, pi, I, O);
+                int idxI[PPT], idxO[PPT];
+#pragma unroll
+                for (int k = 0; k < PPT; ++k) {
+                    const int p = threadIdx.x + k * blockDim.x;
+                    idxI[k] = -1; idxO[k] = 0;
+                    if (p < CT.n_allowed) {
+                        const uint8_t* pw = pows + CT.pow_offset + (size_t)p * NP;
+                        int ii = 0, oo = 0;
+                        for (int t = NI - 1; t >= 0; --t) ii = ii * ord + pw[I[t]];
+                        for (int t = NO - 1; t >= 0; --t) oo = oo * ord + pw[O[t]];
+                        idxI[k] = ii; idxO[k] = oo;
+                    }
+                }
+                for (int b0 = rb; b0 < re; b0 += MB_CB) {
+                    const int nb = min(MB_CB, re - b0);
+                    if (threadIdx.x < nb) {
+                        const int v = sEnt[sOrd[b0 + threadIdx.x]];
+                        sQ[threadIdx.x] = v >> 2; sPi[threadIdx.x] = v & 3;
+                    }
+                    __syncthreads();
+                    // (1) per (cluster, slot): basis and the owner's weight vector
+                    for (int t = threadIdx.x; t < nb * NP; t += blockDim.x) {
+                        const int c = t / NP, s = t % NP;
+                        const int4 mm = CS.m[qbase + sQ[c]];
+                        int id = 0, w = 1;
+                        for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
+                        SlotBasis sb;
+                        double* g = sGH + ((size_t)c * NP + s) * 2 * ord;
+                        slot_basis(M, F, NBODY, f, mm, id, T, s, ord, g, g + ord, sb);
+                        const int m = sPi[c];
+                        const double sg = (m == sb.ma) ? 1.0 : ((m == sb.mb) ? -1.0 : 0.0);
+                        double* wv = sW + ((size_t)c * NP + s) * 3;
+                        wv[0] = sg * sb.rab[0] / sb.r; wv[1] = sg * sb.rab[1] / sb.r; wv[2] = sg * sb.rab[2] / sb.r;
+                    }
+                    __syncthreads();
+                    // (2) M_x,y,z over the incident-slot powers, Q over the others
+                    for (int t = threadIdx.x; t < nb * per; t += blockDim.x) {
+                        const int c = t / per, z = t % per;
+                        const double* GH = sGH + (size_t)c * NP * 2 * ord;
+                        const double* W = sW + (size_t)c * NP * 3;
+                        R* tab = sTab + (size_t)c * per;
+                        if (z < sizeI) {
+                            int pwr[3] = {0, 0, 0}, zz = z;
+                            for (int u = 0; u < NI; ++u) { pwr[u] = zz % ord; zz /= ord; }
+                            double mx = 0, my = 0, mz = 0;
+                            for (int u = 0; u < NI; ++u) {
+                                double prod = GH[(size_t)I[u] * 2 * ord + ord + pwr[u]];
+                                for (int v2 = 0; v2 < NI; ++v2)
+                                    if (v2 != u) prod *= GH[(size_t)I[v2] * 2 * ord + pwr[v2]];
+                                const double* wv = W + I[u] * 3;
+                                mx += prod * wv[0]; my += prod * wv[1]; mz += prod * wv[2];
+                            }
+                            tab[z] = R(mx); tab[sizeI + z] = R(my); tab[2 * sizeI + z] = R(mz);
+                        } else {
+                            int zz = z - sizeI;
+                            double prod = 1.0;
+                            for (int u = 0; u < NO; ++u) { prod *= GH[(size_t)O[u] * 2 * ord + zz % ord]; zz /= ord; }
+                            tab[z + 2 * sizeI] = R(prod);
+                        }
+                    }
+                    __syncthreads();
+                    // (3) 3 FMAs per (cluster, power)
+                    for (int c = 0; c < nb; ++c) {
+                        const R* tab = sTab + (size_t)c * per;
+#pragma unroll
+                        for (int k = 0; k < PPT; ++k) {
+                            if (idxI[k] < 0) continue;
+                            const R qv = tab[3 * sizeI + idxO[k]];
+                            acc[k][0] += tab[idxI[k]] * qv;
+                            acc[k][1] += tab[sizeI + idxI[k]] * qv;
+                            acc[k][2] += tab[2 * sizeI + idxI[k]] * qv;
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            // sum the powers that share a column, then store the owner's 3 rows
+#pragma unroll
+            for (int k = 0; k < PPT; ++k) {
+                const int p = threadIdx.x + k * blockDim.x;
+                if (p < CT.n_allowed) {
+                    sTab[3 * p] = acc[k][0]; sTab[3 * p + 1] = acc[k][1]; sTab[3 * p + 2] = acc[k][2];
+                }
+            }
+            __syncthreads();
+            const int* gp = grps + CT.grp_offset;
+            for (int col = threadIdx.x; col < CT.n_true; col += blockDim.x) {
+                R sx = 0, sy = 0, sz = 0;
+                for (int p = gp[col]; p < gp[col + 1]; ++p) { sx += sTab[3 * p]; sy += sTab[3 * p + 1]; sz += sTab[3 * p + 2]; }
+                const int64_t cc = CT.col_base + col;
+                R* a0 = A + (row + 0) * lda + cc;
+                R* a1 = A + (row + 1) * lda + cc;
+                R* a2 = A + (row + 2) * lda + cc;
+                if (single_pass) { *a0 = R(sx * perm); *a1 = R(sy * perm); *a2 = R(sz * perm); }
+                else { *a0 += R(sx * perm); *a1 += R(sy * perm); *a2 += R(sz * perm); }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- many-body stress/energy rows
+// grid: (frame, cluster type, group-aligned power chunk); comps as in k_virial2.
+template <int NBODY, typename R>
+__global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets bytype,
+                                                          const int64_t* key_frame_ofs, int ncomp, R* A, int64_t lda) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    constexpr int N1 = NBODY - 1;
+    constexpr int N2 = NP - N1;
+    constexpr int PPT = VIR_PPT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int f = blockIdx.x;
+    const int T = blockIdx.y;
+    const int srows = F.stress_rows[f], erows = F.energy_rows[f];
+    if (srows == 0 && erows == 0) return;
+    const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
+    if ((int)blockIdx.z >= CT.vir_nchunk) return;
+    const int pbeg = CT.vir_chunk[blockIdx.z], pend = CT.vir_chunk[blockIdx.z + 1];
+    const int64_t kb = key_frame_ofs[f];
+    const int64_t c0 = bytype.key_ofs[kb + T], c1 = bytype.key_ofs[kb + T + 1];
+    if (c0 == c1) return;
+    const int ord = NBODY == 3 ? M.order3 : M.order4;
+    const uint8_t* pows = NBODY == 3 ? M.pow3 : M.pow4;
+    const int* grps = NBODY == 3 ? M.grp3 : M.grp4;
+    const int N = F.natoms[f];
+    const BoxDev& B = F.box[f];
+    const double perm = NBODY == 3 ? B.perm3 : B.perm4;
+    const int64_t qbase = CS.ofs[F.atom_ofs[f]];
+    const int* typ = F.type + F.atom_ofs[f];
+    int size1 = 1, size2 = 1;
+    for (int k = 0; k < N1; ++k) size1 *= ord;
+    for (int k = 0; k < N2; ++k) size2 *= ord;
+    const int per = 7 * size1 + 7 * size2;   // [Q1 | A1 xx..yz | Q2 | A2 xx..yz]
+    int S1[3], S2[3];
+    role_slots(NBODY, 0, S1, S2);
+    const MbVirSmem L = mb_vir_smem(NBODY, ord, PPT * MB_THREADS, (int)sizeof(R));
+    int* sQ = reinterpret_cast<int*>(smem_raw + L.q);
+    double* sGH = reinterpret_cast<double*>(smem_raw + L.gh);
+    double* sV = reinterpret_cast<double*>(smem_raw + L.v);
+    R* sTab = reinterpret_cast<R*>(smem_raw + L.tab);
+
+    int i1[PPT], i2[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const int p = pbeg + threadIdx.x + k * blockDim.x;
+        i1[k] = -1; i2[k] = 0;
+        if (p < pend) {
+            const uint8_t* pw = pows + CT.pow_offset + (size_t)p * NP;
+            int x = 0, y = 0;
+            for (int t = N1 - 1; t >= 0; --t) x = x * ord + pw[S1[t]];
+            for (int t = N2 - 1; t >= 0; --t) y = y * ord + pw[S2[t]];
+            i1[k] = x; i2[k] = y;
+        }
+    }
+    R acc[PPT][7];
+#pragma unroll
+    for (int k = 0; k < PPT; ++k)
+        for (int c = 0; c < 7; ++c) acc[k][c] = R(0);
+    for (int64_t b0 = c0; b0 < c1; b0 += MB_CB) {
+        const int nb = (int)min((int64_t)MB_CB, c1 - b0);
+        if (threadIdx.x < nb) sQ[threadIdx.x] = bytype.val[b0 + threadIdx.x];
+        __syncthreads();
+        for (int t = threadIdx.x; t < nb * NP; t += blockDim.x) {
+            const int c = t / NP, s = t % NP;
+            const int4 mm = CS.m[qbase + sQ[c]];
+            int id = 0, w = 1;
+            for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
+            SlotBasis sb;
+            double* g = sGH + ((size_t)c * NP + s) * 2 * ord;
+            slot_basis(M, F, NBODY, f, mm, id, T, s, ord, g, g + ord, sb);
+            double* v = sV + ((size_t)c * NP + s) * 6;
+            const double* x = sb.rab;
+            v[0] = x[0] * x[0] / sb.r; v[1] = x[1] * x[1] / sb.r; v[2] = x[2] * x[2] / sb.r;
+            v[3] = x[0] * x[1] / sb.r; v[4] = x[0] * x[2] / sb.r; v[5] = x[1] * x[2] / sb.r;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < nb * (size1 + size2); t += blockDim.x) {
+            const int c = t / (size1 + size2);
+            int z = t % (size1 + size2);
+            const bool first = z < size1;
+            const int* S = first ? S1 : S2;
+            const int ns = first ? N1 : N2;
+            if (!first) z -= size1;
+            const double* GH = sGH + (size_t)c * NP * 2 * ord;
+            const double* V = sV + (size_t)c * NP * 6;
+            int pwr[3] = {0, 0, 0}, zz = z;
+            for (int u = 0; u < ns; ++u) { pwr[u] = zz % ord; zz /= ord; }
+            double q = 1.0, av[6] = {0, 0, 0, 0, 0, 0};
+            for (int u = 0; u < ns; ++u) q *= GH[(size_t)S[u] * 2 * ord + pwr[u]];
+            for (int u = 0; u < ns; ++u) {
+                double prod = GH[(size_t)S[u] * 2 * ord + ord + pwr[u]];
+                for (int v2 = 0; v2 < ns; ++v2) if (v2 != u) prod *= GH[(size_t)S[v2] * 2 * ord + pwr[v2]];
+                for (int k = 0; k < 6; ++k) av[k] += prod * V[S[u] * 6 + k];
+            }
+            R* tab = sTab + (size_t)c * per + (first ? 0 : 7 * size1);
+            const int sz = first ? size1 : size2;
+            tab[z] = R(q);
+            for (int k = 0; k < 6; ++k) tab[(1 + k) * sz + z] = R(av[k]);
+        }
+        __syncthreads();
+        for (int c = 0; c < nb; ++c) {
+            const R* t1 = sTab + (size_t)c * per;
+            const R* t2 = t1 + 7 * size1;
+#pragma unroll
+            for (int k = 0; k < PPT; ++k) {
+                if (i1[k] < 0) continue;
+                const R q1 = t1[i1[k]], q2 = t2[i2[k]];
+                acc[k][0] += q1 * q2;
+                for (int cc = 1; cc < ncomp; ++cc)
+                    acc[k][cc] -= t1[cc * size1 + i1[k]] * q2 + q1 * t2[cc * size2 + i2[k]];
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const int pl = threadIdx.x + k * blockDim.x;
+        if (pbeg + pl < pend)
+            for (int c = 0; c < 7; ++c) sTab[(size_t)pl * 7 + c] = acc[k][c];
+    }
+    __syncthreads();
+    const int* gp = grps + CT.grp_offset;
+    const double inv_vol = 1.0 / B.vol;
+    for (int col = threadIdx.x; col < CT.n_true; col += blockDim.x) {
+        const int pa = gp[col], pb = gp[col + 1];
+        if (pa < pbeg || pa >= pend) continue;
+        R sv[7] = {0, 0, 0, 0, 0, 0, 0};
+        for (int p = pa; p < pb; ++p)
+            for (int c = 0; c < 7; ++c) sv[c] += sTab[(size_t)(p - pbeg) * 7 + c];
+        for (int c = 0; c < 7; ++c) sv[c] = R(sv[c] * perm);
+        write_virial_rows(F, f, CT.col_base + col, sv, inv_vol, A, lda);
+    }
+}
+
+// ---------------------------------------------------------------- energy offset columns
+// One column per atom type holding that type's atom count on energy rows
+// (A_MAT::add_col_of_ones src/A_Matrix.C:155-175); force and stress rows keep 0.
+__global__ void k_energy_cols(ModelDev M, FramesDev F, void* A, int64_t lda, int is_double) {
+    const int f = blockIdx.x;
+    if (F.energy_rows[f] == 0 || M.fit_ener_cols == 0) return;
+    const int N = F.natoms[f];
+    const int* typ = F.type + F.atom_ofs[f];
+    const int64_t row = F.row_ofs[f] + 3 * (int64_t)N + F.stress_rows[f];
+    for (int t = threadIdx.x; t < M.fit_ener_cols; t += blockDim.x) {
+        int count = 0;
+        for (int k = 0; k < N; ++k) count += typ[k] == t;
+        for (int rr = 0; rr < F.energy_rows[f]; ++rr) {
+            const int64_t idx = (row + rr) * lda + M.tot_short + t;
+            if (is_double) reinterpret_cast<double*>(A)[idx] = (double)count;
+            else reinterpret_cast<float*>(A)[idx] = (float)count;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+template <typename K>
+static void set_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+void launch_force2(int prec, int nreal, const ModelDev& M, const FramesDev& F, const NeighDev& NB,
+                   const Buckets& inc, const int64_t* kfo, void* A, int64_t lda, cudaStream_t st) {
+    const size_t rs = prec == 0 ? 8 : 4;
+    const size_t sm = (size_t)F2_THREADS * 3 * M.order2 * rs + F2_THREADS * sizeof(int);
+    if (prec == 0) {
+        set_smem(k_force2<double>, sm);
+        k_force2<double><<<nreal, F2_THREADS, sm, st>>>(M, F, NB, inc, kfo, (double*)A, lda);
+    } else {
+        set_smem(k_force2<float>, sm);
+        k_force2<float><<<nreal, F2_THREADS, sm, st>>>(M, F, NB, inc, kfo, (float*)A, lda);
+    }
+}
+
+void launch_virial2(int prec, int nframes, const ModelDev& M, const FramesDev& F, const NeighDev& NB, void* A,
+                    int64_t lda, cudaStream_t st) {
+    const size_t rs = prec == 0 ? 8 : 4;
+    const size_t sm = (size_t)F2_THREADS * (2 * M.order2 + 6) * rs + F2_THREADS * sizeof(int);
+    if (prec == 0) {
+        set_smem(k_virial2<double>, sm);
+        k_virial2<double><<<nframes, F2_THREADS, sm, st>>>(M, F, NB, (double*)A, lda);
+    } else {
+        set_smem(k_virial2<float>, sm);
+        k_virial2<float><<<nframes, F2_THREADS, sm, st>>>(M, F, NB, (float*)A, lda);
+    }
+}
+
+template <int NBD, typename R>
+static void force_mb_ppt(int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS,
+                         const Buckets& inc, const int64_t* kfo, R* A, int64_t lda, cudaStream_t st) {
+    if (ppt <= 1) {
+        set_smem(k_force_mb<NBD, R, 1>, smem);
+        k_force_mb<NBD, R, 1><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, A, lda);
+    } else if (ppt <= 2) {
+        set_smem(k_force_mb<NBD, R, 2>, smem);
+        k_force_mb<NBD, R, 2><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, A, lda);
+    } else {
+        set_smem(k_force_mb<NBD, R, 8>, smem);
+        k_force_mb<NBD, R, 8><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, A, lda);
+    }
+}
+
+void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,
+                     const ClusterSet& CS, const Buckets& inc, const int64_t* kfo, void* A, int64_t lda,
+                     cudaStream_t st) {
+    if (nbody == 3 && prec == 0) force_mb_ppt<3, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (double*)A, lda, st);
+    else if (nbody == 3) force_mb_ppt<3, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (float*)A, lda, st);
+    else if (prec == 0) force_mb_ppt<4, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (double*)A, lda, st);
+    else force_mb_ppt<4, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (float*)A, lda, st);
+}
+
+void launch_virial_mb(int nbody, int prec, dim3 grid, size_t smem, const ModelDev& M, const FramesDev& F,
+                      const ClusterSet& CS, const Buckets& byt, const int64_t* kfo, int ncomp, void* A, int64_t lda,
+                      cudaStream_t st) {
+    if (nbody == 3 && prec == 0) {
+        set_smem(k_virial_mb<3, double>, smem);
+        k_virial_mb<3, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (double*)A, lda);
+    } else if (nbody == 3) {
+        set_smem(k_virial_mb<3, float>, smem);
+        k_virial_mb<3, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (float*)A, lda);
+    } else if (prec == 0) {
+        set_smem(k_virial_mb<4, double>, smem);
+        k_virial_mb<4, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (double*)A, lda);
+    } else {
+        set_smem(k_virial_mb<4, float>, smem);
+        k_virial_mb<4, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (float*)A, lda);
+    }
+}
+
+void launch_energy_cols(int prec, int nframes, const ModelDev& M, const FramesDev& F, void* A, int64_t lda,
+                        cudaStream_t st) {
+    k_energy_cols<<<nframes, 32, 0, st>>>(M, F, A, lda, prec == 0 ? 1 : 0);
+}
+
+}  // namespace cgd

@@ -1,0 +1,94 @@
+// Launch configuration and shared-memory layout of the assembly kernels.
+#pragma once
+#include "kernels.h"
+
+namespace cgd {
+
+constexpr int MB_THREADS = 512;     // threads of the many-body kernels
+constexpr int MB_CB = 16;           // clusters staged per shared-memory batch
+constexpr int MB_MAX_ENT = 1024;    // owner incidences handled per pass
+constexpr int VIR_PPT = 4;          // powers per thread in the stress/energy kernel
+constexpr int F2_THREADS = 128;     // 2-body kernels
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+struct MbForceSmem {
+    size_t ent, key, ord, cnt, q, pi, gh, w, tab, total;
+};
+__host__ __device__ inline MbForceSmem mb_force_smem(int nbody, int ord, int nkeys, int max_allowed, int rsize) {
+    const int np = nbody == 3 ? 3 : 6, ni = nbody - 1, no = np - ni;
+    int sizeI = 1, sizeO = 1;
+    for (int k = 0; k < ni; ++k) sizeI *= ord;
+    for (int k = 0; k < no; ++k) sizeO *= ord;
+    const size_t per = 3 * (size_t)sizeI + sizeO;
+    MbForceSmem s;
+    s.ent = 0;
+    s.key = align16(s.ent + MB_MAX_ENT * sizeof(int));
+    s.ord = align16(s.key + MB_MAX_ENT * sizeof(int));
+    s.cnt = align16(s.ord + MB_MAX_ENT * sizeof(int));
+    s.q = align16(s.cnt + (nkeys + 1) * sizeof(int));
+    s.pi = align16(s.q + MB_CB * sizeof(int));
+    s.gh = align16(s.pi + MB_CB * sizeof(int));
+    s.w = align16(s.gh + (size_t)MB_CB * np * 2 * ord * sizeof(double));
+    s.tab = align16(s.w + (size_t)MB_CB * np * 3 * sizeof(double));
+    size_t tab = (size_t)MB_CB * per;
+    if ((size_t)max_allowed * 3 > tab) tab = (size_t)max_allowed * 3;
+    s.total = align16(s.tab + tab * rsize);
+    return s;
+}
+
+struct MbVirSmem {
+    size_t q, gh, v, tab, total;
+};
+__host__ __device__ inline MbVirSmem mb_vir_smem(int nbody, int ord, int pchunk, int rsize) {
+    const int np = nbody == 3 ? 3 : 6, n1 = nbody - 1, n2 = np - n1;
+    int s1 = 1, s2 = 1;
+    for (int k = 0; k < n1; ++k) s1 *= ord;
+    for (int k = 0; k < n2; ++k) s2 *= ord;
+    const size_t per = 7 * (size_t)s1 + 7 * (size_t)s2;
+    MbVirSmem s;
+    s.q = 0;
+    s.gh = align16(MB_CB * sizeof(int));
+    s.v = align16(s.gh + (size_t)MB_CB * np * 2 * ord * sizeof(double));
+    s.tab = align16(s.v + (size_t)MB_CB * np * 6 * sizeof(double));
+    size_t tab = (size_t)MB_CB * per;
+    if ((size_t)pchunk * 7 > tab) tab = (size_t)pchunk * 7;
+    s.total = align16(s.tab + tab * rsize);
+    return s;
+}
+
+// Energy (comp 0) and stress (comps 1..6 = xx yy zz xy xz yz) rows of one column,
+// in the reference's row order (src/A_Matrix.C:309-553).
+template <typename R>
+__device__ __forceinline__ void write_virial_rows(const FramesDev& F, int f, int64_t col, const R* s, double inv_vol,
+                                                  R* A, int64_t lda) {
+    const int N = F.natoms[f];
+    const int sr = F.stress_rows[f], er = F.energy_rows[f];
+    int64_t row = F.row_ofs[f] + 3 * (int64_t)N;
+    if (sr == 3) {
+        A[(row + 0) * lda + col] = R(s[1] * inv_vol);
+        A[(row + 1) * lda + col] = R(s[2] * inv_vol);
+        A[(row + 2) * lda + col] = R(s[3] * inv_vol);
+    } else if (sr == 9) {
+        const int map9[9] = {1, 4, 5, 4, 2, 6, 5, 6, 3};
+        for (int k = 0; k < 9; ++k) A[(row + k) * lda + col] = R(s[map9[k]] * inv_vol);
+    }
+    row += sr;
+    for (int k = 0; k < er; ++k) A[(row + k) * lda + col] = s[0];
+}
+
+// Host launchers (kernels are defined in assemble.cu).  prec: 0 FP64, 1 FP32.
+void launch_force2(int prec, int nreal, const ModelDev& M, const FramesDev& F, const NeighDev& NB,
+                   const Buckets& inc, const int64_t* key_frame_ofs, void* A, int64_t lda, cudaStream_t st);
+void launch_virial2(int prec, int nframes, const ModelDev& M, const FramesDev& F, const NeighDev& NB, void* A,
+                    int64_t lda, cudaStream_t st);
+void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,
+                     const ClusterSet& CS, const Buckets& inc, const int64_t* key_frame_ofs, void* A, int64_t lda,
+                     cudaStream_t st);
+void launch_virial_mb(int nbody, int prec, dim3 grid, size_t smem, const ModelDev& M, const FramesDev& F,
+                      const ClusterSet& CS, const Buckets& bytype, const int64_t* key_frame_ofs, int ncomp, void* A,
+                      int64_t lda, cudaStream_t st);
+void launch_energy_cols(int prec, int nframes, const ModelDev& M, const FramesDev& F, void* A, int64_t lda,
+                        cudaStream_t st);
+
+}  // namespace cgd

@@ -1,0 +1,252 @@
+// extern "C" entry points declared in include/chimes_gb300.h.
+#include "../../include/chimes_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+
+#include "model.h"
+#include "session.h"
+
+struct cg_model {
+    cg::Model m;
+};
+struct cg_frames {
+    cg::FrameBatch fb;
+};
+struct cg_session {
+    std::unique_ptr<cg::Session> s;
+    cg::AssembleStats last;
+};
+struct cg_dframes {
+    std::unique_ptr<cg::DeviceFrames> d;
+    int64_t nrows = 0;
+};
+
+static thread_local std::string g_err;
+
+template <typename F>
+static int guarded(F&& fn) {
+    try {
+        g_err.clear();
+        fn();
+        return 0;
+    } catch (const cg::Error& e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_err = "out of host memory";
+        return 4;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return 2;
+    }
+}
+
+static void need(bool ok, const char* what) {
+    if (!ok) throw cg::Error(1, std::string("bad argument: ") + what);
+}
+
+extern "C" {
+
+const char* cg_last_error(void) { return g_err.c_str(); }
+
+int cg_model_load(const char* path, cg_model** out) {
+    return guarded([&] {
+        need(path && out, "path/out");
+        std::unique_ptr<cg_model> h(new cg_model());
+        h->m = cg::load_model(path);
+        *out = h.release();
+    });
+}
+
+void cg_model_free(cg_model* m) { delete m; }
+
+int cg_model_columns(const cg_model* h, int* n2b, int* n3b, int* n4b, int* nener, int* ntotal) {
+    return guarded([&] {
+        need(h, "model");
+        if (n2b) *n2b = h->m.tot_snum;
+        if (n3b) *n3b = h->m.num3;
+        if (n4b) *n4b = h->m.num4;
+        if (nener) *nener = h->m.tot_all - h->m.tot_short;
+        if (ntotal) *ntotal = h->m.tot_all;
+    });
+}
+
+int cg_model_sizes(const cg_model* h, int* nframes, int* natmtyp) {
+    return guarded([&] {
+        need(h, "model");
+        if (nframes) *nframes = h->m.ctl.nframes;
+        if (natmtyp) *natmtyp = h->m.ctl.natmtyp;
+    });
+}
+
+static void copy_text(const std::string& t, char* buf, size_t cap, size_t* needed) {
+    if (needed) *needed = t.size();
+    if (buf && cap) {
+        size_t n = t.size() < cap - 1 ? t.size() : cap - 1;
+        std::memcpy(buf, t.data(), n);
+        buf[n] = 0;
+    }
+}
+
+int cg_model_header_text(const cg_model* h, char* buf, size_t cap, size_t* needed) {
+    return guarded([&] {
+        need(h, "model");
+        copy_text(cg::params_header_text(h->m), buf, cap, needed);
+    });
+}
+
+int cg_model_map_text(const cg_model* h, char* buf, size_t cap, size_t* needed) {
+    return guarded([&] {
+        need(h, "model");
+        copy_text(cg::ff_groups_map_text(h->m), buf, cap, needed);
+    });
+}
+
+int cg_frames_read(const cg_model* h, const char* path, int nframes, cg_frames** out) {
+    return guarded([&] {
+        need(h && out, "model/out");
+        std::vector<cg::Frame> frames;
+        if (!path && nframes <= 0) {
+            frames = cg::read_frames(h->m);
+        } else {
+            std::string p = path ? std::string(path) : h->m.ctl.infile.at(0);
+            if (!path && !p.empty() && p[0] != '/') p = h->m.dir + "/" + p;
+            cg::Box box;
+            frames = cg::read_xyzf(h->m, p, nframes > 0 ? nframes : h->m.ctl.nframes, 0, box);
+        }
+        std::unique_ptr<cg_frames> f(new cg_frames());
+        f->fb = cg::make_batch(h->m, frames, 0);
+        *out = f.release();
+    });
+}
+
+int cg_frames_create(const cg_model* h, int nframes, const int* natoms, const int* types, const double* xyz,
+                     const double* forces, const double* cell, const double* stress, const double* energy,
+                     int first_index, cg_frames** out) {
+    return guarded([&] {
+        need(h && out && nframes >= 0 && natoms && types && xyz && cell, "frame arrays");
+        const double fconv = 627.50960803 * 1.889725989;
+        std::vector<cg::Frame> frames(nframes);
+        int64_t a0 = 0;
+        for (int f = 0; f < nframes; ++f) {
+            cg::Frame& fr = frames[f];
+            fr.natoms = natoms[f];
+            need(fr.natoms > 0, "natoms");
+            fr.type.assign(types + a0, types + a0 + fr.natoms);
+            for (int t : fr.type) need(t >= 0 && t < h->m.ctl.natmtyp, "atom type index");
+            fr.xyz.assign(xyz + 3 * a0, xyz + 3 * (a0 + fr.natoms));
+            fr.force.assign(3 * (size_t)fr.natoms, 0.0);
+            if (forces)
+                for (int k = 0; k < 3 * fr.natoms; ++k) fr.force[k] = forces[3 * a0 + k] * fconv;
+            const double* c = cell + 9 * (size_t)f;
+            cg::Box& b = fr.box;
+            b.ax = c[0]; b.ay = c[1]; b.az = c[2]; b.bx = c[3]; b.by = c[4]; b.bz = c[5];
+            b.cx = c[6]; b.cy = c[7]; b.cz = c[8];
+            b.update_cell();
+            if (b.ax <= 0.0 || b.by <= 0.0 || b.cz <= 0.0 || b.ay != 0.0 || b.az != 0.0 || b.bz != 0.0)
+                throw cg::Error(2, "cell must be upper triangular with a positive diagonal");
+            if (stress) {
+                for (int k = 0; k < 3; ++k) fr.stress_diag[k] = stress[6 * (size_t)f + k];
+                for (int k = 0; k < 3; ++k) fr.stress_off[k] = stress[6 * (size_t)f + 3 + k];
+            }
+            fr.energy = energy ? energy[f] : 0.0;
+            a0 += fr.natoms;
+        }
+        std::unique_ptr<cg_frames> fo(new cg_frames());
+        fo->fb = cg::make_batch(h->m, frames, first_index);
+        *out = fo.release();
+    });
+}
+
+void cg_frames_free(cg_frames* fr) { delete fr; }
+
+int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms) {
+    return guarded([&] {
+        need(fr, "frames");
+        if (nrows) *nrows = fr->fb.nrows;
+        if (natoms) *natoms = fr->fb.natoms_total;
+    });
+}
+
+int cg_frames_labels(const cg_frames* fr, double* b) {
+    return guarded([&] {
+        need(fr && b, "frames/b");
+        std::memcpy(b, fr->fb.b.data(), fr->fb.b.size() * sizeof(double));
+    });
+}
+
+int cg_session_create(const cg_model* h, int device, cg_session** out) {
+    return guarded([&] {
+        need(h && out, "model/out");
+        std::unique_ptr<cg_session> s(new cg_session());
+        s->s.reset(new cg::Session(h->m, device));
+        *out = s.release();
+    });
+}
+
+void cg_session_free(cg_session* s) { delete s; }
+
+void* cg_session_stream(cg_session* s) { return s ? (void*)s->s->stream() : nullptr; }
+
+int cg_frames_upload(cg_session* s, const cg_frames* fr, cg_dframes** out) {
+    return guarded([&] {
+        need(s && fr && out, "session/frames/out");
+        std::unique_ptr<cg_dframes> d(new cg_dframes());
+        d->d = s->s->upload(fr->fb);
+        d->nrows = fr->fb.nrows;
+        *out = d.release();
+    });
+}
+
+void cg_dframes_free(cg_dframes* d) { delete d; }
+
+int cg_assemble_device(cg_session* s, const cg_dframes* d, int precision, void* A, int64_t lda) {
+    return guarded([&] {
+        need(s && d && A, "session/frames/A");
+        need(precision == CG_FP64 || precision == CG_FP32, "precision");
+        s->s->assemble(*d->d, precision, A, lda, &s->last);
+    });
+}
+
+int cg_assemble(cg_session* s, const cg_frames* fr, int precision, void* A, int64_t lda) {
+    return guarded([&] {
+        need(s && fr && A, "session/frames/A");
+        need(precision == CG_FP64 || precision == CG_FP32, "precision");
+        const size_t rsz = precision == CG_FP64 ? 8 : 4;
+        std::unique_ptr<cg::DeviceFrames> d = s->s->upload(fr->fb);
+        void* dA = nullptr;
+        const size_t bytes = (size_t)std::max<int64_t>(1, fr->fb.nrows) * lda * rsz;
+        cg::cuda_check(cudaMallocAsync(&dA, bytes, s->s->stream()), "cudaMallocAsync(A)");
+        try {
+            s->s->assemble(*d, precision, dA, lda, &s->last);
+            cg::cuda_check(cudaMemcpyAsync(A, dA, (size_t)fr->fb.nrows * lda * rsz, cudaMemcpyDeviceToHost,
+                                           s->s->stream()),
+                           "cudaMemcpyAsync(A)");
+            cg::cuda_check(cudaFreeAsync(dA, s->s->stream()), "cudaFreeAsync(A)");
+            cg::cuda_check(cudaStreamSynchronize(s->s->stream()), "cudaStreamSynchronize");
+        } catch (...) {
+            cudaFreeAsync(dA, s->s->stream());
+            cudaStreamSynchronize(s->s->stream());
+            throw;
+        }
+    });
+}
+
+int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads, int64_t* evals3,
+                           int64_t* evals4) {
+    return guarded([&] {
+        need(s, "session");
+        if (pairs) *pairs = s->last.pairs2;
+        if (triplets) *triplets = s->last.triplets;
+        if (quads) *quads = s->last.quads;
+        if (evals3) *evals3 = s->last.power_evals3;
+        if (evals4) *evals4 = s->last.power_evals4;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,327 @@
+// Geometry, neighbour lists and cluster enumeration on the device.
+//
+// Reference behaviour reproduced here (all index sets are bit-exact):
+//   FRAME::build_layers / update_ghost  src/ClassDefs.C:2361-2409, 2685-2752
+//   BOX::WRAP_ATOM / LAYER_ATOM          src/ClassDefs.C:2064-2164
+//   NEIGHBORS::DO_UPDATE_BIG / _SMALL    src/ClassDefs.C:137-393
+//   triplet loops of Cheby::Deriv_3B     src/Cheby.C:981-1054
+//   quadruplet loops of Cheby::Deriv_4B  src/Cheby.C:1387-1500
+//   FCUT::PROCEED                        src/Fcut.C:125-140
+// The reference decides membership with FP64 distances; every candidate is first
+// screened with an FP32 distance (margin 1e-2 A, far above FP32 error) and only
+// candidates near a cut-off are re-decided with the exact FP64 sequence.
+#include "dev.cuh"
+#include "kernels.h"
+
+namespace cgd {
+
+static constexpr float MARGIN = 1.0e-2f;
+
+// ---------------------------------------------------------------- ghost set-up
+__global__ void k_frame_setup(FramesDev F, int64_t total_ghosts) {
+    int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= total_ghosts) return;
+    // frame lookup: binary search over ghost_ofs
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (F.ghost_ofs[mid] <= gid) lo = mid; else hi = mid - 1;
+    }
+    const int f = lo;
+    const int N = F.natoms[f];
+    const int g = (int)(gid - F.ghost_ofs[f]);
+    const int a = g % N;
+    const int k = g / N;   // 0 = real image
+    const BoxDev& B = F.box[f];
+    const double* x0 = F.xyz + 3 * (F.atom_ofs[f] + a);
+    double w[3];
+    // WRAP_ATOM (src/ClassDefs.C:2075-2119)
+    if (B.is_ortho) {
+        double L3[3] = {B.lx, B.ly, B.lz};
+        for (int q = 0; q < 3; ++q) {
+            int idx = (int)floor(__ddiv_rn(x0[q], L3[q]));
+            w[q] = subrn(x0[q], mulrn((double)idx, L3[q]));
+        }
+    } else {
+        double t[3];
+        for (int q = 0; q < 3; ++q) t[q] = dot3rn(B.inv[3 * q], B.inv[3 * q + 1], B.inv[3 * q + 2], x0[0], x0[1], x0[2]);
+        for (int q = 0; q < 3; ++q) { int idx = (int)floor(t[q]); t[q] = subrn(t[q], (double)idx); }
+        for (int q = 0; q < 3; ++q) w[q] = dot3rn(B.h[3 * q], B.h[3 * q + 1], B.h[3 * q + 2], t[0], t[1], t[2]);
+    }
+    double c[3] = {w[0], w[1], w[2]};
+    if (k > 0) {   // LAYER_ATOM (src/ClassDefs.C:2132-2164)
+        int n1, n2, n3;
+        layer_index(k - 1, F.nlayers, n1, n2, n3);
+        if (B.is_ortho) {
+            c[0] = addrn(w[0], mulrn((double)n1, B.h[0]));
+            c[1] = addrn(w[1], mulrn((double)n2, B.h[4]));
+            c[2] = addrn(w[2], mulrn((double)n3, B.h[8]));
+        } else {
+            double t[3];
+            for (int q = 0; q < 3; ++q) t[q] = dot3rn(B.inv[3 * q], B.inv[3 * q + 1], B.inv[3 * q + 2], w[0], w[1], w[2]);
+            t[0] = addrn(t[0], (double)n1); t[1] = addrn(t[1], (double)n2); t[2] = addrn(t[2], (double)n3);
+            for (int q = 0; q < 3; ++q) c[q] = dot3rn(B.h[3 * q], B.h[3 * q + 1], B.h[3 * q + 2], t[0], t[1], t[2]);
+        }
+    }
+    double* s = F.scaled + 3 * gid;
+    for (int q = 0; q < 3; ++q) s[q] = dot3rn(B.inv[3 * q], B.inv[3 * q + 1], B.inv[3 * q + 2], c[0], c[1], c[2]);
+    float4 c32 = make_float4((float)c[0], (float)c[1], (float)c[2], 0.f);
+    reinterpret_cast<float4*>(F.cart32)[gid] = c32;
+}
+
+// ---------------------------------------------------------------- neighbour lists
+// One warp per real atom.  Candidates are scanned in ghost-index order, so the
+// lists come out sorted and the fill pass is deterministic.
+__global__ void k_neigh(ModelDev M, FramesDev F, NeighDev NB, int fill) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= NB.n_real) return;
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (F.atom_ofs[mid] <= warp) lo = mid; else hi = mid - 1;
+    }
+    const int f = lo;
+    const int N = F.natoms[f];
+    const int i = warp - (int)F.atom_ofs[f];
+    const int G = N * F.nimg;
+    const int64_t gbase = F.ghost_ofs[f];
+    const BoxDev& B = F.box[f];
+    const int* typ = F.type + F.atom_ofs[f];
+    const int ti = typ[i];
+    const float4 ci = reinterpret_cast<const float4*>(F.cart32)[gbase + i];
+    const double* si = F.scaled + 3 * (gbase + i);
+    const float maxall = (float)fmax(fmax(M.maxcut2, M.order3 > 0 ? M.maxcut3 : 0.0), M.order4 > 0 ? M.maxcut4 : 0.0);
+    const float pre = maxall + MARGIN;
+    int64_t o2 = 0, o3 = 0, o4 = 0;
+    if (fill) { o2 = NB.ofs2[warp]; o3 = NB.ofs3[warp]; o4 = NB.ofs4[warp]; }
+    int c2 = 0, c3 = 0, c4 = 0;
+    for (int base = 0; base < G; base += 32) {
+        const int g = base + lane;
+        bool in2 = false, in3 = false, in4 = false;
+        double r = 0, rab[3] = {0, 0, 0};
+        int pt = 0;
+        if (g < G && g != i && (B.small || i <= g % N)) {
+            float4 cg = reinterpret_cast<const float4*>(F.cart32)[gbase + g];
+            float dx = cg.x - ci.x, dy = cg.y - ci.y, dz = cg.z - ci.z;
+            float r32 = sqrtf(dx * dx + dy * dy + dz * dz);
+            if (r32 < pre) {
+                r = dist_exact(B.h, si, F.scaled + 3 * (gbase + g), rab);
+                pt = M.int_pair_map[ti * M.natmtyp + typ[g % N]];
+                const PairDev P = M.pairs[pt];
+                in2 = M.order2 > 0 && r > P.smin && r < P.smax;
+                in3 = M.order3 > 0 && r < M.maxcut3;
+                in4 = M.order4 > 0 && r < M.maxcut4;
+            }
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        unsigned b2 = __ballot_sync(0xffffffffu, in2);
+        unsigned b3 = __ballot_sync(0xffffffffu, in3);
+        unsigned b4 = __ballot_sync(0xffffffffu, in4);
+        if (fill) {
+            if (in2) {
+                int64_t p = o2 + c2 + __popc(b2 & lt);
+                NB.i2[p] = i; NB.g2[p] = g; NB.pt2[p] = pt; NB.r2[p] = r;
+                NB.rab2[3 * p] = rab[0]; NB.rab2[3 * p + 1] = rab[1]; NB.rab2[3 * p + 2] = rab[2];
+            }
+            if (in3) { int64_t p = o3 + c3 + __popc(b3 & lt); NB.g3[p] = g; NB.r3[p] = r; }
+            if (in4) { int64_t p = o4 + c4 + __popc(b4 & lt); NB.g4[p] = g; NB.r4[p] = r; }
+        }
+        c2 += __popc(b2); c3 += __popc(b3); c4 += __popc(b4);
+    }
+    if (!fill && lane == 0) { NB.cnt2[warp] = c2; NB.cnt3[warp] = c3; NB.cnt4[warp] = c4; }
+}
+
+// ---------------------------------------------------------------- clusters
+__device__ __forceinline__ float dist32(const float4* c, int64_t a, int64_t b) {
+    float4 x = c[a], y = c[b];
+    float dx = y.x - x.x, dy = y.y - x.y, dz = y.z - x.z;
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
+// r(a,b) < smax decided exactly; FP32 settles all but the near-boundary cases.
+__device__ __forceinline__ bool within(const FramesDev& F, const BoxDev& B, int64_t gbase, int a, int b,
+                                       double smax, float r32) {
+    if (r32 < (float)smax - MARGIN) return true;
+    if (r32 > (float)smax + MARGIN) return false;
+    double rab[3];
+    double r = dist_exact(B.h, F.scaled + 3 * (gbase + a), F.scaled + 3 * (gbase + b), rab);
+    return r < smax;
+}
+
+template <int NB_>
+__global__ void k_clusters(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int fill) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= NB.n_real) return;
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (F.atom_ofs[mid] <= warp) lo = mid; else hi = mid - 1;
+    }
+    const int f = lo;
+    const int N = F.natoms[f];
+    const int i = warp - (int)F.atom_ofs[f];
+    const int64_t gbase = F.ghost_ofs[f];
+    const BoxDev& B = F.box[f];
+    const int* typ = F.type + F.atom_ofs[f];
+    const float4* c32 = reinterpret_cast<const float4*>(F.cart32);
+    const int* lg = NB_ == 3 ? NB.g3 + NB.ofs3[warp] : NB.g4 + NB.ofs4[warp];
+    const double* lr = NB_ == 3 ? NB.r3 + NB.ofs3[warp] : NB.r4 + NB.ofs4[warp];
+    const int n = NB_ == 3 ? NB.cnt3[warp] : NB.cnt4[warp];
+    const int* imap = NB_ == 3 ? M.int_map3 : M.int_map4;
+    const int8_t* pidx = NB_ == 3 ? M.pidx3 : M.pidx4;
+    const ClusterTypeDev* types = NB_ == 3 ? M.types3 : M.types4;
+    const bool ordered = !B.small;
+    const int ti = typ[i];
+    int64_t out = fill ? CS.ofs[warp] : 0;
+    int count = 0;
+    const int64_t total = NB_ == 3 ? (int64_t)n * n : (int64_t)n * n * n;
+    for (int64_t base = 0; base < total; base += 32) {
+        const int64_t t = base + lane;
+        bool ok = false;
+        int j = -1, k = -1, l = -1, T = -1;
+        if (t < total) {
+            int a, b, c = 0;
+            if (NB_ == 3) { a = (int)(t / n); b = (int)(t % n); }
+            else { a = (int)(t / ((int64_t)n * n)); b = (int)((t / n) % n); c = (int)(t % n); }
+            j = lg[a]; k = lg[b];
+            ok = (j != k) && !(ordered && (j % N) > (k % N));
+            if (ok && NB_ == 4) {
+                l = lg[c];
+                ok = (j != l) && (k != l) && !(ordered && (k % N) > (l % N));
+            }
+            if (ok) {
+                int id = (ti + 1) + 10 * (typ[j % N] + 1) + 100 * (typ[k % N] + 1) +
+                         (NB_ == 4 ? 1000 * (typ[l % N] + 1) : 0);
+                T = imap[id];
+                ok = T >= 0;
+                if (ok) {
+                    const ClusterTypeDev& CT = types[T];
+                    const int8_t* pm = pidx + id * (NB_ == 3 ? 3 : 6);
+                    if (NB_ == 3) {
+                        ok = lr[a] < CT.smax[pm[0]] && lr[b] < CT.smax[pm[1]] &&
+                             within(F, B, gbase, j, k, CT.smax[pm[2]], dist32(c32, gbase + j, gbase + k));
+                    } else {
+                        ok = lr[a] < CT.smax[pm[0]] && lr[b] < CT.smax[pm[1]] && lr[c] < CT.smax[pm[2]] &&
+                             within(F, B, gbase, j, k, CT.smax[pm[3]], dist32(c32, gbase + j, gbase + k)) &&
+                             within(F, B, gbase, j, l, CT.smax[pm[4]], dist32(c32, gbase + j, gbase + l)) &&
+                             within(F, B, gbase, k, l, CT.smax[pm[5]], dist32(c32, gbase + k, gbase + l));
+                    }
+                }
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+        if (fill && ok) {
+            int64_t p = out + count + __popc(bal & ((1u << lane) - 1u));
+            CS.m[p] = make_int4(i, j, k, l);
+            CS.type[p] = T;
+        }
+        count += __popc(bal);
+    }
+    if (!fill && lane == 0) CS.cnt[warp] = count;
+}
+
+// ---------------------------------------------------------------- bucketing
+// Stable counting sort of one frame's items by key, one CTA per frame.  Counting
+// and the scan are parallel; the fill walks the items in order, one warp, 32 at a
+// time, ranking equal keys with __match_any_sync so the result is deterministic.
+constexpr int BUCKET_THREADS = 256;
+constexpr int BUCKET_MAX_KEYS = 8192;
+
+__device__ __forceinline__ void bucket_item(const BucketSpec& S, int N, int64_t base, int64_t t, int& key, int& val) {
+    if (S.kind == 0) {
+        int64_t p = base + (t >> 1);
+        int e = (int)(t & 1);
+        key = e == 0 ? S.i2[p] : S.g2[p] % N;
+        val = (int)t;
+    } else if (S.kind == 1) {
+        int64_t q = base + t / S.nb;
+        int e = (int)(t % S.nb);
+        int4 mm = S.m[q];
+        int g = e == 0 ? mm.x : (e == 1 ? mm.y : (e == 2 ? mm.z : mm.w));
+        key = g % N;
+        val = (int)((t / S.nb) * 4 + e);
+    } else {
+        key = S.type[base + t];
+        val = (int)t;
+    }
+}
+
+__global__ void k_bucket(FramesDev F, BucketSpec S, Buckets out) {
+    __shared__ int cnt[BUCKET_MAX_KEYS];
+    __shared__ int part[BUCKET_THREADS];
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    // pair items live in the neighbour CSR, which is indexed by global real atom
+    const int64_t base = S.item_frame_ofs[f];
+    const int64_t nunits = S.item_frame_ofs[f + 1] - base;
+    const int mult = S.kind == 0 ? 2 : (S.kind == 1 ? S.nb : 1);
+    const int64_t nitems = nunits * mult;
+    const int64_t kbase = S.key_frame_ofs[f];
+    const int K = (int)(S.key_frame_ofs[f + 1] - kbase - 1);
+    const int64_t vbase = base * mult;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    for (int64_t t = threadIdx.x; t < nitems; t += blockDim.x) {
+        int key, val;
+        bucket_item(S, N, base, t, key, val);
+        atomicAdd(&cnt[key], 1);
+    }
+    __syncthreads();
+    // exclusive scan of cnt[0..K)
+    const int per = (K + blockDim.x - 1) / blockDim.x;
+    const int k0 = threadIdx.x * per, k1 = min(K, k0 + per);
+    int local = 0;
+    for (int k = k0; k < k1; ++k) local += cnt[k];
+    part[threadIdx.x] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int w = 0; w < (int)blockDim.x; ++w) { int v = part[w]; part[w] = run; run += v; }
+    }
+    __syncthreads();
+    int run = part[threadIdx.x];
+    for (int k = k0; k < k1; ++k) { int v = cnt[k]; cnt[k] = run; out.key_ofs[kbase + k] = vbase + run; run += v; }
+    if (threadIdx.x == 0) out.key_ofs[kbase + K] = vbase + nitems;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        for (int64_t c0 = 0; c0 < nitems; c0 += 32) {
+            int64_t t = c0 + lane;
+            bool act = t < nitems;
+            int key = -1 - lane, val = 0;
+            if (act) bucket_item(S, N, base, t, key, val);
+            unsigned peers = __match_any_sync(0xffffffffu, key);
+            int leader = __ffs(peers) - 1;
+            int rank = __popc(peers & ((1u << lane) - 1u));
+            int start = 0;
+            if (act && lane == leader) start = cnt[key];
+            start = __shfl_sync(0xffffffffu, start, leader);
+            if (act) out.val[vbase + start + rank] = val;
+            __syncwarp();
+            if (act && lane == leader) cnt[key] = start + __popc(peers);
+            __syncwarp();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+void launch_frame_setup(const FramesDev& F, int64_t n, cudaStream_t st) {
+    if (n > 0) k_frame_setup<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, n);
+}
+void launch_neigh(const ModelDev& M, const FramesDev& F, const NeighDev& NB, int fill, cudaStream_t st) {
+    if (NB.n_real > 0) k_neigh<<<(unsigned)((NB.n_real + 7) / 8), 256, 0, st>>>(M, F, NB, fill);
+}
+void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const NeighDev& NB, const ClusterSet& CS,
+                     int fill, cudaStream_t st) {
+    if (NB.n_real <= 0) return;
+    const unsigned g = (unsigned)((NB.n_real + 7) / 8);
+    if (nbody == 3) k_clusters<3><<<g, 256, 0, st>>>(M, F, NB, CS, fill);
+    else k_clusters<4><<<g, 256, 0, st>>>(M, F, NB, CS, fill);
+}
+void launch_bucket(int nframes, const FramesDev& F, const BucketSpec& S, const Buckets& out, cudaStream_t st) {
+    if (nframes > 0) k_bucket<<<nframes, BUCKET_THREADS, 0, st>>>(F, S, out);
+}
+
+}  // namespace cgd

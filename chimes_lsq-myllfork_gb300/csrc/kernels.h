@@ -1,0 +1,51 @@
+// Device work lists produced by the enumeration kernels and consumed by the
+// assembly kernels, plus the kernel entry points.
+#pragma once
+#include "dev.cuh"
+
+namespace cgd {
+
+struct NeighDev {
+    int n_real;                                   // real atoms in the batch (one list each)
+    int* cnt2; int* cnt3; int* cnt4;              // [n_real]
+    int64_t* ofs2; int64_t* ofs3; int64_t* ofs4;  // [n_real + 1] exclusive prefix
+    // 2-body pairs accepted by s_min < r < s_max (src/Cheby.C:772)
+    int* i2; int* g2; int* pt2; double* r2; double* rab2;
+    // 3-body / 4-body candidate lists: r < maximum cluster cut-off
+    int* g3; double* r3;
+    int* g4; double* r4;
+};
+
+struct ClusterSet {                               // triplets or quadruplets of a batch
+    int* cnt;                                     // [n_real] clusters centred on each real atom
+    int64_t* ofs;                                 // [n_real + 1]
+    int4* m;                                      // members (frame-local ghost indices), .w = -1 for 3B
+    int* type;                                    // cluster type index
+};
+
+// Stable per-frame bucketing (owner incidences and per-type lists).
+struct Buckets {
+    int64_t* key_ofs;                             // [sum_f K_f + nframes] global start of each (frame,key)
+    int* val;                                     // permuted item values
+};
+
+// Per-frame item ranges for a bucketing pass.
+struct BucketSpec {
+    int kind;                                     // 0: 2B pair ends, 1: cluster members, 2: cluster types
+    int nb;                                       // members per cluster (kind 1)
+    const int64_t* item_frame_ofs;                // [nframes+1] (in pairs / clusters)
+    const int64_t* key_frame_ofs;                 // [nframes+1] (in keys, incl. one sentinel per frame)
+    const int* i2;                                // kind 0
+    const int* g2;                                // kind 0
+    const int4* m;                                // kind 1
+    const int* type;                              // kind 2
+};
+
+// Host launchers (kernels are defined in geom.cu).
+void launch_frame_setup(const FramesDev& F, int64_t total_ghosts, cudaStream_t st);
+void launch_neigh(const ModelDev& M, const FramesDev& F, const NeighDev& NB, int fill, cudaStream_t st);
+void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const NeighDev& NB, const ClusterSet& CS,
+                     int fill, cudaStream_t st);
+void launch_bucket(int nframes, const FramesDev& F, const BucketSpec& S, const Buckets& out, cudaStream_t st);
+
+}  // namespace cgd

@@ -1,0 +1,437 @@
+// Host orchestration of the design-matrix path (see session.h).
+#include "session.h"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+#include "assemble.h"
+#include "kernels.h"
+
+namespace cg {
+
+static const double GPA = 6.9476955;   // src/functions.h:45
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw Error(3, std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+}
+#define CK(x) cuda_check((x), #x)
+
+template <typename T>
+static T* dev_upload(std::vector<void*>& allocs, const T* src, size_t n) {
+    T* p = nullptr;
+    size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    CK(cudaMalloc((void**)&p, bytes));
+    allocs.push_back(p);
+    if (n) CK(cudaMemcpy(p, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+}
+
+// ------------------------------------------------------------------ model tables
+static void rev_index(const ClusterType& ct, const int* types, int n, int8_t* out) {
+    std::vector<bool> used(n, false);   // greedy match of CLUSTER::map_indices_int src/Cluster.C:1813-1825
+    for (int m = 0; m < n; ++m) {
+        out[m] = -1;
+        for (int q = 0; q < n; ++q)
+            if (types[m] == ct.atom_indices[q] && !used[q]) { out[m] = (int8_t)q; used[q] = true; break; }
+    }
+}
+
+static void upload_list(const Model& m, const ClusterList& cl, int nb, int col_base, int pchunk, DeviceModel& D,
+                        const int** int_map, const int8_t** pidx, const int8_t** rev, const cgd::ClusterTypeDev** types,
+                        const uint8_t** pows, const int** grps, int& max_allowed) {
+    const int np = nb == 3 ? 3 : 6;
+    const int dim = nb == 3 ? 1000 : 10000;
+    std::vector<int> imap(dim, -1);
+    std::vector<int8_t> pi(dim * np, -1), rv(dim * nb, -1);
+    for (int id = 0; id < dim && id < (int)cl.int_map.size(); ++id) {
+        imap[id] = cl.int_map[id];
+        if (imap[id] < 0) continue;
+        for (int e = 0; e < np; ++e) pi[id * np + e] = (int8_t)cl.pair_indices[id][e];
+        int t[4], x = id;
+        for (int k = 0; k < nb; ++k) { t[k] = x % 10 - 1; x /= 10; }
+        rev_index(cl.vec[imap[id]], t, nb, &rv[id * nb]);
+    }
+    std::vector<cgd::ClusterTypeDev> tv(cl.vec.size());
+    std::vector<uint8_t> pw;
+    std::vector<int> gp;
+    int col = col_base;
+    max_allowed = 0;
+    for (size_t t = 0; t < cl.vec.size(); ++t) {
+        const ClusterType& ct = cl.vec[t];
+        cgd::ClusterTypeDev& d = tv[t];
+        std::memset(&d, 0, sizeof(d));
+        d.n_allowed = ct.excluded ? 0 : ct.n_allowed;
+        d.n_true = ct.excluded ? 0 : ct.n_true;
+        d.col_base = col;
+        col += d.n_true;
+        d.pow_offset = (int)pw.size();
+        d.grp_offset = (int)gp.size();
+        max_allowed = std::max(max_allowed, d.n_allowed);
+        for (int p = 0; p < d.n_allowed; ++p)
+            for (int s = 0; s < np; ++s) pw.push_back((uint8_t)ct.allowed_powers[p][s]);
+        // column groups: PARAM_INDICES is non-decreasing with contiguous groups
+        int c = 0;
+        for (int p = 0; p < d.n_allowed; ++p) {
+            if (p > 0 && ct.param_indices[p] < ct.param_indices[p - 1])
+                throw Error(2, "PARAM_INDICES not monotone; unsupported cluster layout");
+            while (c <= ct.param_indices[p]) { gp.push_back(p); ++c; }
+        }
+        while (c <= d.n_true) { gp.push_back(d.n_allowed); ++c; }
+        // group-aligned power chunks for the stress/energy kernel
+        int nch = 0;
+        d.vir_chunk[0] = 0;
+        int start = 0;
+        while (start < d.n_allowed) {
+            int end = std::min(d.n_allowed, start + pchunk);
+            if (end < d.n_allowed) {   // move back to a group start
+                int gstart = end;
+                while (gstart > start && ct.param_indices[gstart] == ct.param_indices[gstart - 1]) --gstart;
+                if (gstart == start) throw Error(2, "power group larger than a chunk");
+                end = gstart;
+            }
+            if (nch >= cgd::MAXCHUNK) throw Error(2, "too many power chunks for one cluster type");
+            d.vir_chunk[++nch] = end;
+            start = end;
+        }
+        d.vir_nchunk = nch;
+        for (int s = 0; s < np; ++s) {
+            d.smax[s] = ct.smax[s]; d.smin[s] = ct.smin[s]; d.xavg[s] = ct.xavg[s]; d.xdiff[s] = ct.xdiff[s];
+            size_t j = 0;
+            for (; j < m.pairs.size(); ++j) if (m.pairs[j].prpr == ct.pair_names[s]) break;
+            d.lambda[s] = j < m.pairs.size() ? m.pairs[j].lambda : 0.0;
+        }
+    }
+    *int_map = dev_upload(D.allocs, imap.data(), imap.size());
+    *pidx = dev_upload(D.allocs, pi.data(), pi.size());
+    *rev = dev_upload(D.allocs, rv.data(), rv.size());
+    *types = dev_upload(D.allocs, tv.data(), tv.size());
+    *pows = dev_upload(D.allocs, pw.data(), pw.size());
+    *grps = dev_upload(D.allocs, gp.data(), gp.size());
+}
+
+DeviceModel::DeviceModel(const Model& m, int vir_pchunk) {
+    const Controls& c = m.ctl;
+    if (c.cheby_order > cgd::MAXORD || c.cheby3 > cgd::MAXORD || c.cheby4 > cgd::MAXORD)
+        throw Error(2, "Chebyshev order above the device limit");
+    if (c.use4 && c.cheby4 > 4) throw Error(2, "4-body order above 4 is not supported on the device");
+    if (c.use3 && c.cheby3 > 16) throw Error(2, "3-body order above 16 is not supported on the device");
+    cgd::ModelDev& d = dev;
+    d.natmtyp = c.natmtyp;
+    d.npairs = (int)m.pairs.size();
+    d.order2 = c.cheby_order;
+    d.order3 = c.use3 ? c.cheby3 : 0;
+    d.order4 = c.use4 ? c.cheby4 : 0;
+    d.trans = c.trans; d.fix = c.fix; d.fcut = c.fcut;
+    d.smooth = c.smooth; d.deriv_const = m.deriv_const; d.fcut_offset = c.fcut_offset;
+    d.maxcut2 = m.max_cutoff_2b; d.maxcut3 = m.max_cutoff_3b; d.maxcut4 = m.max_cutoff_4b;
+    d.ntypes3 = c.use3 ? (int)m.trips.vec.size() : 0;
+    d.ntypes4 = c.use4 ? (int)m.quads.vec.size() : 0;
+    d.n2b = m.tot_snum; d.tot_short = m.tot_short; d.tot_all = m.tot_all;
+    d.col3 = m.tot_snum; d.col4 = m.tot_snum + m.num3;
+    d.fit_ener_cols = c.fit_ener ? c.natmtyp : 0;
+    d.int_pair_map = dev_upload(allocs, m.int_pair_map.data(), m.int_pair_map.size());
+    std::vector<cgd::PairDev> pv;
+    for (const auto& p : m.pairs) pv.push_back({p.smin, p.smax, p.lambda, p.xavg, p.xdiff});
+    d.pairs = dev_upload(allocs, pv.data(), pv.size());
+    if (c.use3)
+        upload_list(m, m.trips, 3, d.col3, vir_pchunk, *this, &d.int_map3, &d.pidx3, &d.rev3, &d.types3, &d.pow3,
+                    &d.grp3, max_allowed3);
+    if (c.use4)
+        upload_list(m, m.quads, 4, d.col4, vir_pchunk, *this, &d.int_map4, &d.pidx4, &d.rev4, &d.types4, &d.pow4,
+                    &d.grp4, max_allowed4);
+}
+
+DeviceModel::~DeviceModel() {
+    for (void* p : allocs) cudaFree(p);
+}
+
+// ------------------------------------------------------------------ frames
+FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int first_index) {
+    FrameBatch fb;
+    fb.nframes = (int)frames.size();
+    fb.first_index = first_index;
+    const int L = m.ctl.nlayers;
+    const int nimg = (2 * L + 1) * (2 * L + 1) * (2 * L + 1);
+    fb.atom_ofs.push_back(0); fb.ghost_ofs.push_back(0); fb.row_ofs.push_back(0);
+    bool small = false;
+    for (int k = 0; k < fb.nframes; ++k) {
+        const Frame& fr = frames[k];
+        const int fi = first_index + k;
+        if (fr.natoms <= 0) throw Error(2, "frame with no atoms");
+        if (fr.natoms > 8191) throw Error(2, "frames above 8191 atoms are not supported on the device");
+        RowLayout rl = frame_rows(m, fi, fr.natoms);
+        fb.natoms.push_back(fr.natoms);
+        fb.stress_rows.push_back(rl.stress_rows);
+        fb.energy_rows.push_back(rl.energy_rows);
+        fb.atom_ofs.push_back(fb.atom_ofs.back() + fr.natoms);
+        fb.ghost_ofs.push_back(fb.ghost_ofs.back() + (int64_t)nimg * fr.natoms);
+        fb.row_ofs.push_back(fb.row_ofs.back() + rl.total());
+        small = frame_is_small(m, fr.box, small);
+        cgd::BoxDev bd;
+        std::memset(&bd, 0, sizeof(bd));
+        for (int q = 0; q < 9; ++q) { bd.h[q] = fr.box.hmat[q]; bd.inv[q] = fr.box.invr[q]; }
+        bd.lx = fr.box.lx; bd.ly = fr.box.ly; bd.lz = fr.box.lz; bd.vol = fr.box.vol;
+        bd.is_ortho = fr.box.is_ortho ? 1 : 0;
+        bd.small = small ? 1 : 0;
+        // PERM_SCALE src/ClassDefs.C:146-152
+        bd.perm2 = small ? 0.5 : 1.0;
+        bd.perm3 = small ? 0.5 / 3.0 : 1.0;
+        bd.perm4 = small ? 0.5 / 3.0 / 4.0 : 1.0;
+        fb.box.push_back(bd);
+        fb.type.insert(fb.type.end(), fr.type.begin(), fr.type.end());
+        fb.xyz.insert(fb.xyz.end(), fr.xyz.begin(), fr.xyz.end());
+        for (int a = 0; a < fr.natoms; ++a)
+            for (int q = 0; q < 3; ++q) fb.b.push_back(fr.force[3 * a + q]);
+        if (rl.stress_rows == 3) {
+            for (int q = 0; q < 3; ++q) fb.b.push_back(fr.stress_diag[q] / GPA);
+        } else if (rl.stress_rows == 9) {
+            const double xx = fr.stress_diag[0], yy = fr.stress_diag[1], zz = fr.stress_diag[2];
+            const double xy = fr.stress_off[0], xz = fr.stress_off[1], yz = fr.stress_off[2];
+            const double v[9] = {xx, xy, xz, xy, yy, yz, xz, yz, zz};
+            for (double x : v) fb.b.push_back(x / GPA);
+        }
+        for (int q = 0; q < rl.energy_rows; ++q) fb.b.push_back(fr.energy);
+    }
+    fb.nrows = fb.row_ofs.back();
+    fb.natoms_total = fb.atom_ofs.back();
+    fb.nghosts = fb.ghost_ofs.back();
+    return fb;
+}
+
+DeviceFrames::~DeviceFrames() {
+    for (void* p : allocs) cudaFree(p);
+}
+
+}  // namespace cg
+
+namespace cgd {
+// ------------------------------------------------------------------ device helpers
+__global__ void k_scan_counts(const int* cnt, int n, int64_t* ofs) {
+    __shared__ int64_t part[1024];
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(n, b + per);
+    int64_t s = 0;
+    for (int i = b; i < e; ++i) s += cnt[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        int64_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int64_t run = part[threadIdx.x] - s;
+    for (int i = b; i < e; ++i) { ofs[i] = run; run += cnt[i]; }
+    if (threadIdx.x == blockDim.x - 1) ofs[n] = part[threadIdx.x];
+}
+
+__global__ void k_gather_frame_ofs(const int64_t* ofs, const int64_t* atom_ofs, int nframes, int64_t* out) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f <= nframes) out[f] = ofs[atom_ofs[f]];
+}
+
+__global__ void k_key_frame_ofs(const int64_t* atom_ofs, int nframes, int per_type, int64_t* out) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f > nframes) return;
+    out[f] = per_type > 0 ? (int64_t)f * (per_type + 1) : atom_ofs[f] + f;
+}
+}  // namespace cgd
+
+namespace cg {
+
+// ------------------------------------------------------------------ session
+Session::Session(const Model& m, int device) : model_(m), device_(device) {
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    dm_.reset(new DeviceModel(model_, cgd::VIR_PPT * cgd::MB_THREADS));
+}
+
+Session::~Session() {
+    dm_.reset();
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+std::unique_ptr<DeviceFrames> Session::upload(const FrameBatch& fb) {
+    CK(cudaSetDevice(device_));
+    std::unique_ptr<DeviceFrames> df(new DeviceFrames());
+    df->nframes = fb.nframes;
+    df->nrows = fb.nrows;
+    df->natoms_total = fb.natoms_total;
+    df->nghosts = fb.nghosts;
+    df->atom_ofs_host = fb.atom_ofs;
+    df->row_ofs_host = fb.row_ofs;
+    df->natoms_host = fb.natoms;
+    cgd::FramesDev& d = df->dev;
+    const int L = model_.ctl.nlayers;
+    d.nframes = fb.nframes;
+    d.nlayers = L;
+    d.nimg = (2 * L + 1) * (2 * L + 1) * (2 * L + 1);
+    d.natoms = dev_upload(df->allocs, fb.natoms.data(), fb.natoms.size());
+    d.atom_ofs = dev_upload(df->allocs, fb.atom_ofs.data(), fb.atom_ofs.size());
+    d.ghost_ofs = dev_upload(df->allocs, fb.ghost_ofs.data(), fb.ghost_ofs.size());
+    d.row_ofs = dev_upload(df->allocs, fb.row_ofs.data(), fb.row_ofs.size());
+    d.stress_rows = dev_upload(df->allocs, fb.stress_rows.data(), fb.stress_rows.size());
+    d.energy_rows = dev_upload(df->allocs, fb.energy_rows.data(), fb.energy_rows.size());
+    d.box = dev_upload(df->allocs, fb.box.data(), fb.box.size());
+    d.type = dev_upload(df->allocs, fb.type.data(), fb.type.size());
+    d.xyz = dev_upload(df->allocs, fb.xyz.data(), fb.xyz.size());
+    double* scaled = nullptr;
+    float* c32 = nullptr;
+    CK(cudaMalloc((void**)&scaled, std::max<int64_t>(1, fb.nghosts) * 3 * sizeof(double)));
+    df->allocs.push_back(scaled);
+    CK(cudaMalloc((void**)&c32, std::max<int64_t>(1, fb.nghosts) * 4 * sizeof(float)));
+    df->allocs.push_back(c32);
+    d.scaled = scaled;
+    d.cart32 = c32;
+    return df;
+}
+
+namespace {
+// stream-ordered scratch, released at the end of a call
+struct Scratch {
+    cudaStream_t s;
+    std::vector<void*> ptrs;
+    explicit Scratch(cudaStream_t st) : s(st) {}
+    template <typename T>
+    T* get(size_t n) {
+        void* p = nullptr;
+        CK(cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T), s));
+        ptrs.push_back(p);
+        return reinterpret_cast<T*>(p);
+    }
+    ~Scratch() {
+        for (void* p : ptrs) cudaFreeAsync(p, s);
+    }
+};
+
+void run_assembly(int prec, const cgd::ModelDev& M, const DeviceModel& dm, const Model& model, const DeviceFrames& df,
+                  cgd::NeighDev& NB, cgd::ClusterSet* CS3, cgd::ClusterSet* CS4, Scratch& S, cudaStream_t st, void* A,
+                  int64_t lda) {
+    const int rsize = prec == 0 ? 8 : 4;
+    const cgd::FramesDev& F = df.dev;
+    const int nf = df.nframes;
+    const int nreal = (int)df.natoms_total;
+    int64_t* kfo_atoms = S.get<int64_t>(nf + 1);
+    int64_t* kfo_t3 = S.get<int64_t>(nf + 1);
+    int64_t* kfo_t4 = S.get<int64_t>(nf + 1);
+    cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, 0, kfo_atoms);
+    if (M.order3 > 0) cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, M.ntypes3, kfo_t3);
+    if (M.order4 > 0) cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, M.ntypes4, kfo_t4);
+    // ---- 2-body
+    if (M.order2 > 0) {
+        int64_t* pfo = S.get<int64_t>(nf + 1);
+        cgd::k_gather_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(NB.ofs2, F.atom_ofs, nf, pfo);
+        int64_t npair = 0;
+        CK(cudaMemcpyAsync(&npair, NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        cgd::Buckets inc2{S.get<int64_t>(nreal + nf), S.get<int>(2 * npair)};
+        cgd::BucketSpec spec{0, 2, pfo, kfo_atoms, NB.i2, NB.g2, nullptr, nullptr};
+        cgd::launch_bucket(nf, F, spec, inc2, st);
+        const int ncol = M.npairs * M.order2;
+        if (ncol > 8 * cgd::F2_THREADS) throw Error(2, "too many 2-body columns for the device kernel");
+        cgd::launch_force2(prec, nreal, M, F, NB, inc2, kfo_atoms, A, lda, st);
+        if (model.ctl.fit_stress || model.ctl.fit_stress_all || model.ctl.fit_ener)
+            cgd::launch_virial2(prec, nf, M, F, NB, A, lda, st);
+        CK(cudaGetLastError());
+    }
+    const int ncomp = (model.ctl.fit_stress_all ? 7 : (model.ctl.fit_stress ? 4 : 1));
+    auto many_body = [&](int nbody, cgd::ClusterSet& CS, const int64_t* kfo_types, int ntypes, int ord,
+                         int max_allowed) {
+        int64_t* cfo = S.get<int64_t>(nf + 1);
+        cgd::k_gather_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(CS.ofs, F.atom_ofs, nf, cfo);
+        int64_t nq = 0;
+        CK(cudaMemcpyAsync(&nq, CS.ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (nq == 0) return;
+        cgd::Buckets inc{S.get<int64_t>(nreal + nf), S.get<int>(nbody * nq)};
+        cgd::BucketSpec spec{1, nbody, cfo, kfo_atoms, nullptr, nullptr, CS.m, nullptr};
+        cgd::launch_bucket(nf, F, spec, inc, st);
+        cgd::Buckets byt{S.get<int64_t>((int64_t)nf * (ntypes + 1)), S.get<int>(nq)};
+        cgd::BucketSpec spec2{2, 1, cfo, kfo_types, nullptr, nullptr, nullptr, CS.type};
+        cgd::launch_bucket(nf, F, spec2, byt, st);
+        const int ppt = (max_allowed + cgd::MB_THREADS - 1) / cgd::MB_THREADS;
+        if (ppt > 8) throw Error(2, "too many allowed powers for the device force kernel");
+        const int pp = ppt <= 1 ? 1 : (ppt <= 2 ? 2 : 8);
+        cgd::MbForceSmem L = cgd::mb_force_smem(nbody, ord, ntypes * 4, max_allowed, rsize);
+        cgd::launch_force_mb(nbody, prec, pp, nreal, L.total, M, F, CS, inc, kfo_atoms, A, lda, st);
+        CK(cudaGetLastError());
+        if (model.ctl.fit_stress || model.ctl.fit_stress_all || model.ctl.fit_ener) {
+            cgd::MbVirSmem V = cgd::mb_vir_smem(nbody, ord, cgd::VIR_PPT * cgd::MB_THREADS, rsize);
+            const int maxch = (max_allowed + cgd::VIR_PPT * cgd::MB_THREADS - 1) / (cgd::VIR_PPT * cgd::MB_THREADS) + 1;
+            dim3 grid(nf, ntypes, std::min(maxch, cgd::MAXCHUNK));
+            cgd::launch_virial_mb(nbody, prec, grid, V.total, M, F, CS, byt, kfo_types, ncomp, A, lda, st);
+            CK(cudaGetLastError());
+        }
+    };
+    if (CS3) many_body(3, *CS3, kfo_t3, M.ntypes3, M.order3, dm.max_allowed3);
+    if (CS4) many_body(4, *CS4, kfo_t4, M.ntypes4, M.order4, dm.max_allowed4);
+    if (M.fit_ener_cols > 0) {
+        cgd::launch_energy_cols(prec, nf, M, F, A, lda, st);
+        CK(cudaGetLastError());
+    }
+}
+}  // namespace
+
+void Session::assemble(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats) {
+    CK(cudaSetDevice(device_));
+    const cgd::ModelDev& M = dm_->dev;
+    const cgd::FramesDev& F = df.dev;
+    cudaStream_t st = stream_;
+    Scratch S(st);
+    const int nf = df.nframes;
+    const int nreal = (int)df.natoms_total;
+    if (lda < M.tot_all) throw Error(1, "lda smaller than the number of A columns");
+    // ghosts
+    cgd::launch_frame_setup(F, df.nghosts, st);
+    CK(cudaGetLastError());
+    // neighbour lists
+    cgd::NeighDev NB{};
+    NB.n_real = nreal;
+    NB.cnt2 = S.get<int>(nreal); NB.cnt3 = S.get<int>(nreal); NB.cnt4 = S.get<int>(nreal);
+    NB.ofs2 = S.get<int64_t>(nreal + 1); NB.ofs3 = S.get<int64_t>(nreal + 1); NB.ofs4 = S.get<int64_t>(nreal + 1);
+    cgd::launch_neigh(M, F, NB, 0, st);
+    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt2, nreal, NB.ofs2);
+    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt3, nreal, NB.ofs3);
+    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt4, nreal, NB.ofs4);
+    int64_t tot[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(&tot[0], NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&tot[1], NB.ofs3 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&tot[2], NB.ofs4 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    NB.i2 = S.get<int>(tot[0]); NB.g2 = S.get<int>(tot[0]); NB.pt2 = S.get<int>(tot[0]);
+    NB.r2 = S.get<double>(tot[0]); NB.rab2 = S.get<double>(3 * tot[0]);
+    NB.g3 = S.get<int>(tot[1]); NB.r3 = S.get<double>(tot[1]);
+    NB.g4 = S.get<int>(tot[2]); NB.r4 = S.get<double>(tot[2]);
+    cgd::launch_neigh(M, F, NB, 1, st);
+    CK(cudaGetLastError());
+    // clusters
+    cgd::ClusterSet CS3{}, CS4{};
+    auto clusters = [&](int nbody, cgd::ClusterSet& CS) -> int64_t {
+        CS.cnt = S.get<int>(nreal);
+        CS.ofs = S.get<int64_t>(nreal + 1);
+        cgd::launch_clusters(nbody, M, F, NB, CS, 0, st);
+        cgd::k_scan_counts<<<1, 1024, 0, st>>>(CS.cnt, nreal, CS.ofs);
+        int64_t n = 0;
+        CK(cudaMemcpyAsync(&n, CS.ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        CS.m = S.get<int4>(n);
+        CS.type = S.get<int>(n);
+        cgd::launch_clusters(nbody, M, F, NB, CS, 1, st);
+        CK(cudaGetLastError());
+        return n;
+    };
+    int64_t n3 = M.order3 > 0 ? clusters(3, CS3) : 0;
+    int64_t n4 = M.order4 > 0 ? clusters(4, CS4) : 0;
+    // zero the batch's rows, then write every non-zero block once
+    const size_t rsz = precision == 0 ? sizeof(double) : sizeof(float);
+    CK(cudaMemsetAsync(A, 0, (size_t)df.nrows * lda * rsz, st));
+    run_assembly(precision, M, *dm_, model_, df, NB, M.order3 > 0 ? &CS3 : nullptr, M.order4 > 0 ? &CS4 : nullptr, S,
+                 st, A, lda);
+    if (stats) {
+        stats->pairs2 = tot[0]; stats->list3 = tot[1]; stats->list4 = tot[2];
+        stats->triplets = n3; stats->quads = n4;
+    }
+}
+
+}  // namespace cg

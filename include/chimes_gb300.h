@@ -1,0 +1,101 @@
+/*
+ * chimes_gb300 — C ABI of the GB300 design-matrix path of ChIMES-lsq.
+ *
+ * The reference has no FFI: its operator surface is the `chimes_lsq` CLI and the
+ * in-process calls it makes.  Each entry point below replaces one step of that
+ * surface (reference file:line cited beside it).  All entry points return 0 on
+ * success and a non-zero status otherwise (1 bad argument, 2 bad input / unsupported
+ * option, 3 CUDA failure, 4 out of memory); cg_last_error() returns the message of
+ * the calling thread's last failure.  Handles are opaque; every buffer is owned by
+ * the caller.  A session owns one CUDA stream and may be used by one thread at a time.
+ */
+#ifndef CHIMES_GB300_H
+#define CHIMES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cg_model cg_model;
+typedef struct cg_frames cg_frames;
+typedef struct cg_session cg_session;
+typedef struct cg_dframes cg_dframes;
+
+/* Precision of the assembled A matrix. */
+enum { CG_FP64 = 0, CG_FP32 = 1 };
+
+/* Parse fm_setup.in and build the pair / cluster topology and coefficient map.
+ * Replaces INPUT::PARSE_INFILE_LSQ (src/input.C:172-225), build_clusters
+ * (src/chimes_lsq.C:533-560) and the column bookkeeping (src/chimes_lsq.C:198-248). */
+int cg_model_load(const char* fm_setup_path, cg_model** out);
+void cg_model_free(cg_model* m);
+
+/* Column counts: 2-body, 3-body, 4-body, energy-offset and total A columns
+ * (TOT_SNUM, NUM_3B_CHEBY, NUM_4B_CHEBY, TOT_ALL_PARAMS in src/chimes_lsq.C:198-248). */
+int cg_model_columns(const cg_model* m, int* n2b, int* n3b, int* n4b, int* nener, int* ntotal);
+
+/* Number of frames (NFRAMES) and atom types (NATMTYP) of the model. */
+int cg_model_sizes(const cg_model* m, int* nframes, int* natmtyp);
+
+/* Text of params.header / ff_groups.map.  Writes at most cap bytes (NUL terminated
+ * when room) and the full length to *needed.  Replaces print_param_header and
+ * print_map_file (src/chimes_lsq.C:562-716). */
+int cg_model_header_text(const cg_model* m, char* buf, size_t cap, size_t* needed);
+int cg_model_map_text(const cg_model* m, char* buf, size_t cap, size_t* needed);
+
+/* Read nframes frames of an .xyzf trajectory (path NULL: the model's TRJFILE,
+ * nframes <= 0: NFRAMES).  Replaces FRAME::READ_XYZF (src/ClassDefs.C:2411-2683). */
+int cg_frames_read(const cg_model* m, const char* xyzf_path, int nframes, cg_frames** out);
+
+/* Build frames from arrays (no text parsing).  Per frame f: natoms[f] atoms with
+ * types (index into the TYPEIDX order) and xyz (A), forces (Hartree/Bohr, as in
+ * .xyzf), cell[9*f..] = the 9 cell-vector components ax ay az bx by bz cx cy cz,
+ * stress[6*f..] = xx yy zz xy xz yz (GPa, may be NULL), energy[f] (may be NULL).
+ * first_index is the global index of the first frame (NSTRESS / NENER use it). */
+int cg_frames_create(const cg_model* m, int nframes, const int* natoms, const int* types, const double* xyz,
+                     const double* forces, const double* cell, const double* stress, const double* energy,
+                     int first_index, cg_frames** out);
+void cg_frames_free(cg_frames* fr);
+
+/* Rows of the A matrix for these frames and the total atom count. */
+int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms);
+
+/* Label vector b in A row order (src/A_Matrix.C:294-553), nrows doubles. */
+int cg_frames_labels(const cg_frames* fr, double* b);
+
+/* One GPU session (device ordinal) for a model; owns a CUDA stream. */
+int cg_session_create(const cg_model* m, int device, cg_session** out);
+void cg_session_free(cg_session* s);
+
+/* The session's CUDA stream (cudaStream_t), for callers that order their own work after it. */
+void* cg_session_stream(cg_session* s);
+
+/* Assemble the full A matrix of the frames into HOST memory A (row-major,
+ * nrows x lda, lda >= ntotal) in CG_FP64 (double) or CG_FP32 (float).  Host->device
+ * copies of the coordinates and the device->host copy of A happen inside.
+ * Replaces the per-frame loop process_frame -> ZCalc_Deriv -> Deriv_2B/3B/4B
+ * (src/chimes_lsq.C:292-328, 718-823; src/functions.C:755-804; src/Cheby.C:709-1729). */
+int cg_assemble(cg_session* s, const cg_frames* fr, int precision, void* A, int64_t lda);
+
+/* Device-resident variant: upload the frames once, then assemble into a DEVICE
+ * buffer A.  cg_assemble_device is asynchronous on the session stream. */
+int cg_frames_upload(cg_session* s, const cg_frames* fr, cg_dframes** out);
+void cg_dframes_free(cg_dframes* d);
+int cg_assemble_device(cg_session* s, const cg_dframes* d, int precision, void* A_device, int64_t lda);
+
+/* Work counters of the last assembly: accepted 2-body pairs, triplets, quadruplets,
+ * and (cluster, allowed-power) evaluations of the 3- and 4-body terms. */
+int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads,
+                           int64_t* evals3, int64_t* evals4);
+
+/* Message of the calling thread's last failure ("" if none). */
+const char* cg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHIMES_GB300_H */
