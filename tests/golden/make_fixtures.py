@@ -1,0 +1,57 @@
+"""Generate the golden fixtures of tests/golden/ with the reference's own chimes_lsq.
+
+Run in a container where the reference sources are available:
+    python oracle/build_ref.sh && python tests/golden/make_fixtures.py
+Each fixture directory holds the seeded synthetic inputs (fm_setup.in, traj.xyzf)
+and ref.npz with the reference's A matrix and b vector (read back from its
+A.txt / b.txt, written with %.16e, so the round trip is exact).
+"""
+import importlib
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+REF = os.path.join(ROOT, "oracle", "_ref", "chimes_lsq")
+
+# name -> (workload, overrides, nframes, seed)
+FIXTURES = {
+    # 2-body water, forces only (configs[0] basis)
+    "water2b": ("water-2b", {}, 2, 11),
+    # 2B16 + 3B8 water with full stress and energy rows (configs[1] basis), 32 molecules
+    "water3b": ("water-3b", dict(nmol=32, L=9.86), 1, 12),
+    # C/H triclinic with 2B8 / 3B4 / 4B3, stress and energy rows
+    "ch4b": ("chno-4b", dict(natoms=40, order=(8, 4, 3), triclinic=False, density=0.1, species2=True), 2, 13),
+    # small cubic cell (extent below the cut-off): unordered neighbour convention, PERM_SCALE 1/n!
+    "small4b": ("chno-4b", dict(natoms=12, order=(6, 3, 2), triclinic=False, density=0.1, species2=True,
+                                fitstrs=None, fitener=True), 1, 14),
+}
+
+
+def make(name):
+    wl, over, nframes, seed = FIXTURES[name]
+    d = os.path.join(HERE, name)
+    os.makedirs(d, exist_ok=True)
+    synth.make_workload(wl, d, nframes=nframes, seed=seed, **over)
+    with tempfile.TemporaryDirectory() as tmp:
+        shutil.copy(os.path.join(d, "fm_setup.in"), tmp)
+        shutil.copy(os.path.join(d, "traj.xyzf"), tmp)
+        subprocess.run([REF, "fm_setup.in"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+        A = np.loadtxt(os.path.join(tmp, "A.txt"), ndmin=2)
+        b = np.loadtxt(os.path.join(tmp, "b.txt"))
+        for f in ("params.header", "ff_groups.map"):
+            shutil.copy(os.path.join(tmp, f), os.path.join(d, f))
+    np.savez_compressed(os.path.join(d, "ref.npz"), A=A, b=b)
+    print(name, A.shape)
+
+
+if __name__ == "__main__":
+    for n in (sys.argv[1:] or FIXTURES):
+        make(n)
