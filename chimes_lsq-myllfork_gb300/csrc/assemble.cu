@@ -400,8 +400,9 @@ __global__ void __launch_bounds__(MB_THREADS) k_force_mb(ModelDev M, FramesDev F
                     }
                     __syncthreads();
                     // (2) M_x,y,z over the incident-slot powers, Q over the others
-                    for (int t = threadIdx.x; t < nb * per; t += blockDim.x) {
-                        const int c = t / per, z = t % per;
+                    const int nzt = sizeI + sizeO;   // M entries (x,y,z written together) + Q entries
+                    for (int t = threadIdx.x; t < nb * nzt; t += blockDim.x) {
+                        const int c = t / nzt, z = t % nzt;
                         const double* GH = sGH + (size_t)c * NP * 2 * ord;
                         const double* W = sW + (size_t)c * NP * 3;
                         R* tab = sTab + (size_t)c * per;
@@ -421,7 +422,7 @@ __global__ void __launch_bounds__(MB_THREADS) k_force_mb(ModelDev M, FramesDev F
                             int zz = z - sizeI;
                             double prod = 1.0;
                             for (int u = 0; u < NO; ++u) { prod *= GH[(size_t)O[u] * 2 * ord + zz % ord]; zz /= ord; }
-                            tab[z + 2 * sizeI] = R(prod);
+                            tab[3 * sizeI + (z - sizeI)] = R(prod);
                         }
                     }
                     __syncthreads();

@@ -354,10 +354,12 @@ void run_assembly(int prec, const cgd::ModelDev& M, const DeviceModel& dm, const
         if (ppt > 8) throw Error(2, "too many allowed powers for the device force kernel");
         const int pp = ppt <= 1 ? 1 : (ppt <= 2 ? 2 : 8);
         cgd::MbForceSmem L = cgd::mb_force_smem(nbody, ord, ntypes * 4, max_allowed, rsize);
+        if (L.total > 227 * 1024) throw Error(2, "cluster order too large for the device force kernel");
         cgd::launch_force_mb(nbody, prec, pp, nreal, L.total, M, F, CS, inc, kfo_atoms, A, lda, st);
         CK(cudaGetLastError());
         if (model.ctl.fit_stress || model.ctl.fit_stress_all || model.ctl.fit_ener) {
             cgd::MbVirSmem V = cgd::mb_vir_smem(nbody, ord, cgd::VIR_PPT * cgd::MB_THREADS, rsize);
+            if (V.total > 227 * 1024) throw Error(2, "cluster order too large for the device stress/energy kernel");
             const int maxch = (max_allowed + cgd::VIR_PPT * cgd::MB_THREADS - 1) / (cgd::VIR_PPT * cgd::MB_THREADS) + 1;
             dim3 grid(nf, ntypes, std::min(maxch, cgd::MAXCHUNK));
             cgd::launch_virial_mb(nbody, prec, grid, V.total, M, F, CS, byt, kfo_types, ncomp, A, lda, st);
