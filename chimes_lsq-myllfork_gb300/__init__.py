@@ -75,6 +75,10 @@ def lib():
         "cg_dframes_free": (None, [vp]),
         "cg_assemble_device": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, ctypes.c_int64]),
         "cg_session_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p, i64p]),
+        "cg_session_last_launches": (ctypes.c_int, [vp, i64p]),
+        "cg_session_profile": (ctypes.c_int, [vp, ctypes.c_int]),
+        "cg_session_stage_times": (ctypes.c_int, [vp, vp, vp]),
+        "cg_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
         "cg_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -240,6 +244,24 @@ class Session:
         """Assemble into a device buffer (asynchronous on the session stream)."""
         _check(lib().cg_assemble_device(self._h, dframes._h, int(precision), ctypes.c_void_p(int(a_device_ptr)),
                                         int(lda)))
+
+    NSTAGES = 11
+
+    def profile(self, enable=True):
+        """Turn per-stage CUDA-event timing on/off (clears the totals)."""
+        _check(lib().cg_session_profile(self._h, 1 if enable else 0))
+
+    def stage_times(self):
+        """{stage: (total_ms, calls)} accumulated since profile() was called."""
+        ms = np.zeros(self.NSTAGES, dtype=np.float64)
+        calls = np.zeros(self.NSTAGES, dtype=np.int64)
+        _check(lib().cg_session_stage_times(self._h, _ptr(ms), _ptr(calls)))
+        return {lib().cg_stage_name(k).decode(): (float(ms[k]), int(calls[k])) for k in range(self.NSTAGES)}
+
+    def last_launches(self):
+        v = ctypes.c_int64()
+        _check(lib().cg_session_last_launches(self._h, ctypes.byref(v)))
+        return v.value
 
     def last_counts(self):
         v = [ctypes.c_int64() for _ in range(5)]

@@ -249,4 +249,29 @@ int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplet
     });
 }
 
+int cg_session_last_launches(const cg_session* s, int64_t* launches) {
+    return guarded([&] {
+        need(s && launches, "session/launches");
+        *launches = s->last.launches;
+    });
+}
+
+int cg_session_profile(cg_session* s, int enable) {
+    return guarded([&] {
+        need(s, "session");
+        s->s->reset_stage_totals();
+        s->s->set_profiling(enable != 0);
+    });
+}
+
+int cg_session_stage_times(cg_session* s, double* ms, int64_t* calls) {
+    return guarded([&] {
+        need(s, "session");
+        static_assert(CG_NSTAGES == cg::ST_COUNT, "stage count");
+        s->s->stage_totals(ms, calls);
+    });
+}
+
+const char* cg_stage_name(int stage) { return cg::stage_name(stage); }
+
 }  // extern "C"

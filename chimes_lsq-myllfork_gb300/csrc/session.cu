@@ -240,6 +240,52 @@ __global__ void k_key_frame_ofs(const int64_t* atom_ofs, int nframes, int per_ty
 
 namespace cg {
 
+// ------------------------------------------------------------------ stage timing
+const char* stage_name(int s) {
+    static const char* names[ST_COUNT] = {"frame_setup", "neighbour_lists", "clusters", "buckets", "force_2b",
+                                          "virial_2b", "force_3b", "virial_3b", "force_4b", "virial_4b", "other"};
+    return s >= 0 && s < ST_COUNT ? names[s] : "?";
+}
+
+void Session::mark(int stage, bool begin) {
+    if (!profiling_) return;
+    auto get_event = [&]() {
+        cudaEvent_t e;
+        if (!event_pool_.empty()) { e = event_pool_.back(); event_pool_.pop_back(); }
+        else CK(cudaEventCreate(&e));
+        return e;
+    };
+    if (begin) {
+        open_event_ = get_event();
+        open_stage_ = stage;
+        CK(cudaEventRecord(open_event_, stream_));
+    } else if (open_stage_ == stage) {
+        cudaEvent_t e = get_event();
+        CK(cudaEventRecord(e, stream_));
+        pending_.push_back({stage, open_event_, e});
+        open_stage_ = -1;
+    }
+}
+
+void Session::stage_totals(double* ms, int64_t* calls) {
+    for (auto& p : pending_) {
+        CK(cudaEventSynchronize(p.b));
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, p.a, p.b));
+        stage_ms_[p.stage] += t;
+        stage_calls_[p.stage] += 1;
+        event_pool_.push_back(p.a);
+        event_pool_.push_back(p.b);
+    }
+    pending_.clear();
+    for (int k = 0; k < ST_COUNT; ++k) { if (ms) ms[k] = stage_ms_[k]; if (calls) calls[k] = stage_calls_[k]; }
+}
+
+void Session::reset_stage_totals() {
+    stage_totals(nullptr, nullptr);
+    for (int k = 0; k < ST_COUNT; ++k) { stage_ms_[k] = 0; stage_calls_[k] = 0; }
+}
+
 // ------------------------------------------------------------------ session
 Session::Session(const Model& m, int device) : model_(m), device_(device) {
     CK(cudaSetDevice(device));
@@ -248,6 +294,8 @@ Session::Session(const Model& m, int device) : model_(m), device_(device) {
 }
 
 Session::~Session() {
+    for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    for (auto e : event_pool_) cudaEventDestroy(e);
     dm_.reset();
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -305,73 +353,13 @@ struct Scratch {
     }
 };
 
-void run_assembly(int prec, const cgd::ModelDev& M, const DeviceModel& dm, const Model& model, const DeviceFrames& df,
-                  cgd::NeighDev& NB, cgd::ClusterSet* CS3, cgd::ClusterSet* CS4, Scratch& S, cudaStream_t st, void* A,
-                  int64_t lda) {
-    const int rsize = prec == 0 ? 8 : 4;
-    const cgd::FramesDev& F = df.dev;
-    const int nf = df.nframes;
-    const int nreal = (int)df.natoms_total;
-    int64_t* kfo_atoms = S.get<int64_t>(nf + 1);
-    int64_t* kfo_t3 = S.get<int64_t>(nf + 1);
-    int64_t* kfo_t4 = S.get<int64_t>(nf + 1);
-    cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, 0, kfo_atoms);
-    if (M.order3 > 0) cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, M.ntypes3, kfo_t3);
-    if (M.order4 > 0) cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, M.ntypes4, kfo_t4);
-    // ---- 2-body
-    if (M.order2 > 0) {
-        int64_t* pfo = S.get<int64_t>(nf + 1);
-        cgd::k_gather_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(NB.ofs2, F.atom_ofs, nf, pfo);
-        int64_t npair = 0;
-        CK(cudaMemcpyAsync(&npair, NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        cgd::Buckets inc2{S.get<int64_t>(nreal + nf), S.get<int>(2 * npair)};
-        cgd::BucketSpec spec{0, 2, pfo, kfo_atoms, NB.i2, NB.g2, nullptr, nullptr};
-        cgd::launch_bucket(nf, F, spec, inc2, st);
-        const int ncol = M.npairs * M.order2;
-        if (ncol > 8 * cgd::F2_THREADS) throw Error(2, "too many 2-body columns for the device kernel");
-        cgd::launch_force2(prec, nreal, M, F, NB, inc2, kfo_atoms, A, lda, st);
-        if (model.ctl.fit_stress || model.ctl.fit_stress_all || model.ctl.fit_ener)
-            cgd::launch_virial2(prec, nf, M, F, NB, A, lda, st);
-        CK(cudaGetLastError());
-    }
-    const int ncomp = (model.ctl.fit_stress_all ? 7 : (model.ctl.fit_stress ? 4 : 1));
-    auto many_body = [&](int nbody, cgd::ClusterSet& CS, const int64_t* kfo_types, int ntypes, int ord,
-                         int max_allowed) {
-        int64_t* cfo = S.get<int64_t>(nf + 1);
-        cgd::k_gather_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(CS.ofs, F.atom_ofs, nf, cfo);
-        int64_t nq = 0;
-        CK(cudaMemcpyAsync(&nq, CS.ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (nq == 0) return;
-        cgd::Buckets inc{S.get<int64_t>(nreal + nf), S.get<int>(nbody * nq)};
-        cgd::BucketSpec spec{1, nbody, cfo, kfo_atoms, nullptr, nullptr, CS.m, nullptr};
-        cgd::launch_bucket(nf, F, spec, inc, st);
-        cgd::Buckets byt{S.get<int64_t>((int64_t)nf * (ntypes + 1)), S.get<int>(nq)};
-        cgd::BucketSpec spec2{2, 1, cfo, kfo_types, nullptr, nullptr, nullptr, CS.type};
-        cgd::launch_bucket(nf, F, spec2, byt, st);
-        const int ppt = (max_allowed + cgd::MB_THREADS - 1) / cgd::MB_THREADS;
-        if (ppt > 8) throw Error(2, "too many allowed powers for the device force kernel");
-        const int pp = ppt <= 1 ? 1 : (ppt <= 2 ? 2 : 8);
-        cgd::MbForceSmem L = cgd::mb_force_smem(nbody, ord, ntypes * 4, max_allowed, rsize);
-        if (L.total > 227 * 1024) throw Error(2, "cluster order too large for the device force kernel");
-        cgd::launch_force_mb(nbody, prec, pp, nreal, L.total, M, F, CS, inc, kfo_atoms, A, lda, st);
-        CK(cudaGetLastError());
-        if (model.ctl.fit_stress || model.ctl.fit_stress_all || model.ctl.fit_ener) {
-            cgd::MbVirSmem V = cgd::mb_vir_smem(nbody, ord, cgd::VIR_PPT * cgd::MB_THREADS, rsize);
-            if (V.total > 227 * 1024) throw Error(2, "cluster order too large for the device stress/energy kernel");
-            const int maxch = (max_allowed + cgd::VIR_PPT * cgd::MB_THREADS - 1) / (cgd::VIR_PPT * cgd::MB_THREADS) + 1;
-            dim3 grid(nf, ntypes, std::min(maxch, cgd::MAXCHUNK));
-            cgd::launch_virial_mb(nbody, prec, grid, V.total, M, F, CS, byt, kfo_types, ncomp, A, lda, st);
-            CK(cudaGetLastError());
-        }
-    };
-    if (CS3) many_body(3, *CS3, kfo_t3, M.ntypes3, M.order3, dm.max_allowed3);
-    if (CS4) many_body(4, *CS4, kfo_t4, M.ntypes4, M.order4, dm.max_allowed4);
-    if (M.fit_ener_cols > 0) {
-        cgd::launch_energy_cols(prec, nf, M, F, A, lda, st);
-        CK(cudaGetLastError());
-    }
+__global__ void k_count_evals(const int* type, int64_t n, const cgd::ClusterTypeDev* types,
+                              unsigned long long* out) {
+    unsigned long long local = 0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        local += (unsigned long long)types[type[q]].n_allowed;
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(out, local);
 }
 }  // namespace
 
@@ -379,23 +367,32 @@ void Session::assemble(const DeviceFrames& df, int precision, void* A, int64_t l
     CK(cudaSetDevice(device_));
     const cgd::ModelDev& M = dm_->dev;
     const cgd::FramesDev& F = df.dev;
+    const Model& model = model_;
     cudaStream_t st = stream_;
     Scratch S(st);
     const int nf = df.nframes;
     const int nreal = (int)df.natoms_total;
+    const int prec = precision;
+    const int rsize = prec == 0 ? 8 : 4;
+    int64_t launches = 0;
     if (lda < M.tot_all) throw Error(1, "lda smaller than the number of A columns");
+    if (nf == 0) return;
+    auto L = [&](int n = 1) { launches += n; };
     // ghosts
-    cgd::launch_frame_setup(F, df.nghosts, st);
+    mark(ST_SETUP, true);
+    cgd::launch_frame_setup(F, df.nghosts, st); L();
     CK(cudaGetLastError());
+    mark(ST_SETUP, false);
     // neighbour lists
+    mark(ST_NEIGH, true);
     cgd::NeighDev NB{};
     NB.n_real = nreal;
     NB.cnt2 = S.get<int>(nreal); NB.cnt3 = S.get<int>(nreal); NB.cnt4 = S.get<int>(nreal);
     NB.ofs2 = S.get<int64_t>(nreal + 1); NB.ofs3 = S.get<int64_t>(nreal + 1); NB.ofs4 = S.get<int64_t>(nreal + 1);
-    cgd::launch_neigh(M, F, NB, 0, st);
-    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt2, nreal, NB.ofs2);
-    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt3, nreal, NB.ofs3);
-    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt4, nreal, NB.ofs4);
+    cgd::launch_neigh(M, F, NB, 0, st); L();
+    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt2, nreal, NB.ofs2); L();
+    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt3, nreal, NB.ofs3); L();
+    cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt4, nreal, NB.ofs4); L();
     int64_t tot[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(&tot[0], NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&tot[1], NB.ofs3 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -405,34 +402,115 @@ void Session::assemble(const DeviceFrames& df, int precision, void* A, int64_t l
     NB.r2 = S.get<double>(tot[0]); NB.rab2 = S.get<double>(3 * tot[0]);
     NB.g3 = S.get<int>(tot[1]); NB.r3 = S.get<double>(tot[1]);
     NB.g4 = S.get<int>(tot[2]); NB.r4 = S.get<double>(tot[2]);
-    cgd::launch_neigh(M, F, NB, 1, st);
+    cgd::launch_neigh(M, F, NB, 1, st); L();
     CK(cudaGetLastError());
+    mark(ST_NEIGH, false);
     // clusters
     cgd::ClusterSet CS3{}, CS4{};
+    unsigned long long* d_evals = S.get<unsigned long long>(2);
+    CK(cudaMemsetAsync(d_evals, 0, 2 * sizeof(unsigned long long), st));
     auto clusters = [&](int nbody, cgd::ClusterSet& CS) -> int64_t {
         CS.cnt = S.get<int>(nreal);
         CS.ofs = S.get<int64_t>(nreal + 1);
-        cgd::launch_clusters(nbody, M, F, NB, CS, 0, st);
-        cgd::k_scan_counts<<<1, 1024, 0, st>>>(CS.cnt, nreal, CS.ofs);
+        cgd::launch_clusters(nbody, M, F, NB, CS, 0, st); L();
+        cgd::k_scan_counts<<<1, 1024, 0, st>>>(CS.cnt, nreal, CS.ofs); L();
         int64_t n = 0;
         CK(cudaMemcpyAsync(&n, CS.ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         CS.m = S.get<int4>(n);
         CS.type = S.get<int>(n);
-        cgd::launch_clusters(nbody, M, F, NB, CS, 1, st);
+        cgd::launch_clusters(nbody, M, F, NB, CS, 1, st); L();
+        if (n > 0) {
+            k_count_evals<<<(unsigned)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, st>>>(
+                CS.type, n, nbody == 3 ? M.types3 : M.types4, d_evals + (nbody - 3)); L();
+        }
         CK(cudaGetLastError());
         return n;
     };
+    mark(ST_CLUSTERS, true);
     int64_t n3 = M.order3 > 0 ? clusters(3, CS3) : 0;
     int64_t n4 = M.order4 > 0 ? clusters(4, CS4) : 0;
+    mark(ST_CLUSTERS, false);
     // zero the batch's rows, then write every non-zero block once
-    const size_t rsz = precision == 0 ? sizeof(double) : sizeof(float);
-    CK(cudaMemsetAsync(A, 0, (size_t)df.nrows * lda * rsz, st));
-    run_assembly(precision, M, *dm_, model_, df, NB, M.order3 > 0 ? &CS3 : nullptr, M.order4 > 0 ? &CS4 : nullptr, S,
-                 st, A, lda);
+    mark(ST_OTHER, true);
+    CK(cudaMemsetAsync(A, 0, (size_t)df.nrows * lda * rsize, st));
+    int64_t* kfo_atoms = S.get<int64_t>(nf + 1);
+    int64_t* kfo_t3 = S.get<int64_t>(nf + 1);
+    int64_t* kfo_t4 = S.get<int64_t>(nf + 1);
+    cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, 0, kfo_atoms); L();
+    if (M.order3 > 0) { cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, M.ntypes3, kfo_t3); L(); }
+    if (M.order4 > 0) { cgd::k_key_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(F.atom_ofs, nf, M.ntypes4, kfo_t4); L(); }
+    mark(ST_OTHER, false);
+    const bool virial = model.ctl.fit_stress || model.ctl.fit_stress_all || model.ctl.fit_ener;
+    // ---- 2-body
+    if (M.order2 > 0) {
+        mark(ST_BUCKET, true);
+        int64_t* pfo = S.get<int64_t>(nf + 1);
+        cgd::k_gather_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(NB.ofs2, F.atom_ofs, nf, pfo); L();
+        cgd::Buckets inc2{S.get<int64_t>(nreal + nf), S.get<int>(2 * tot[0])};
+        cgd::BucketSpec spec{0, 2, pfo, kfo_atoms, NB.i2, NB.g2, nullptr, nullptr};
+        cgd::launch_bucket(nf, F, spec, inc2, st); L();
+        mark(ST_BUCKET, false);
+        const int ncol = M.npairs * M.order2;
+        if (ncol > 8 * cgd::F2_THREADS) throw Error(2, "too many 2-body columns for the device kernel");
+        mark(ST_FORCE2, true);
+        cgd::launch_force2(prec, nreal, M, F, NB, inc2, kfo_atoms, A, lda, st); L();
+        mark(ST_FORCE2, false);
+        if (virial) {
+            mark(ST_VIRIAL2, true);
+            cgd::launch_virial2(prec, nf, M, F, NB, A, lda, st); L();
+            mark(ST_VIRIAL2, false);
+        }
+        CK(cudaGetLastError());
+    }
+    const int ncomp = (model.ctl.fit_stress_all ? 7 : (model.ctl.fit_stress ? 4 : 1));
+    auto many_body = [&](int nbody, cgd::ClusterSet& CS, int64_t nq, const int64_t* kfo_types, int ntypes, int ord,
+                         int max_allowed) {
+        if (nq == 0) return;
+        mark(ST_BUCKET, true);
+        int64_t* cfo = S.get<int64_t>(nf + 1);
+        cgd::k_gather_frame_ofs<<<(nf + 128) / 128, 128, 0, st>>>(CS.ofs, F.atom_ofs, nf, cfo); L();
+        cgd::Buckets inc{S.get<int64_t>(nreal + nf), S.get<int>(nbody * nq)};
+        cgd::BucketSpec spec{1, nbody, cfo, kfo_atoms, nullptr, nullptr, CS.m, nullptr};
+        cgd::launch_bucket(nf, F, spec, inc, st); L();
+        cgd::Buckets byt{S.get<int64_t>((int64_t)nf * (ntypes + 1)), S.get<int>(nq)};
+        cgd::BucketSpec spec2{2, 1, cfo, kfo_types, nullptr, nullptr, nullptr, CS.type};
+        cgd::launch_bucket(nf, F, spec2, byt, st); L();
+        mark(ST_BUCKET, false);
+        const int ppt = (max_allowed + cgd::MB_THREADS - 1) / cgd::MB_THREADS;
+        if (ppt > 8) throw Error(2, "too many allowed powers for the device force kernel");
+        const int pp = ppt <= 1 ? 1 : (ppt <= 2 ? 2 : 8);
+        cgd::MbForceSmem Lf = cgd::mb_force_smem(nbody, ord, ntypes * 4, max_allowed, rsize);
+        if (Lf.total > 227 * 1024) throw Error(2, "cluster order too large for the device force kernel");
+        mark(nbody == 3 ? ST_FORCE3 : ST_FORCE4, true);
+        cgd::launch_force_mb(nbody, prec, pp, nreal, Lf.total, M, F, CS, inc, kfo_atoms, A, lda, st); L();
+        mark(nbody == 3 ? ST_FORCE3 : ST_FORCE4, false);
+        CK(cudaGetLastError());
+        if (virial) {
+            cgd::MbVirSmem V = cgd::mb_vir_smem(nbody, ord, cgd::VIR_PPT * cgd::MB_THREADS, rsize);
+            if (V.total > 227 * 1024) throw Error(2, "cluster order too large for the device stress/energy kernel");
+            const int maxch = (max_allowed + cgd::VIR_PPT * cgd::MB_THREADS - 1) / (cgd::VIR_PPT * cgd::MB_THREADS) + 1;
+            dim3 grid(nf, ntypes, std::min(maxch, cgd::MAXCHUNK));
+            mark(nbody == 3 ? ST_VIRIAL3 : ST_VIRIAL4, true);
+            cgd::launch_virial_mb(nbody, prec, grid, V.total, M, F, CS, byt, kfo_types, ncomp, A, lda, st); L();
+            mark(nbody == 3 ? ST_VIRIAL3 : ST_VIRIAL4, false);
+            CK(cudaGetLastError());
+        }
+    };
+    if (M.order3 > 0) many_body(3, CS3, n3, kfo_t3, M.ntypes3, M.order3, dm_->max_allowed3);
+    if (M.order4 > 0) many_body(4, CS4, n4, kfo_t4, M.ntypes4, M.order4, dm_->max_allowed4);
+    if (M.fit_ener_cols > 0) {
+        cgd::launch_energy_cols(prec, nf, M, F, A, lda, st); L();
+        CK(cudaGetLastError());
+    }
     if (stats) {
+        unsigned long long ev[2] = {0, 0};
+        CK(cudaMemcpyAsync(ev, d_evals, sizeof(ev), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
         stats->pairs2 = tot[0]; stats->list3 = tot[1]; stats->list4 = tot[2];
         stats->triplets = n3; stats->quads = n4;
+        stats->power_evals3 = (int64_t)ev[0]; stats->power_evals4 = (int64_t)ev[1];
+        stats->launches = launches;
     }
 }
 

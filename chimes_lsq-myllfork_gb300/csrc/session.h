@@ -54,7 +54,15 @@ struct DeviceFrames {
 struct AssembleStats {
     int64_t pairs2 = 0, list3 = 0, list4 = 0, triplets = 0, quads = 0;
     int64_t power_evals3 = 0, power_evals4 = 0;   // sum over clusters of n_allowed
+    int64_t launches = 0;                         // kernels launched by the last call
 };
+
+// Pipeline stages timed with CUDA events when profiling is on.
+enum Stage {
+    ST_SETUP = 0, ST_NEIGH, ST_CLUSTERS, ST_BUCKET, ST_FORCE2, ST_VIRIAL2, ST_FORCE3, ST_VIRIAL3, ST_FORCE4,
+    ST_VIRIAL4, ST_OTHER, ST_COUNT
+};
+const char* stage_name(int s);
 
 class Session {
    public:
@@ -66,8 +74,22 @@ class Session {
     // A (device pointer, row-major, lda >= tot_all) receives the batch's rows.
     void assemble(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats);
 
+    // Stage timing (CUDA events on the session stream).
+    void set_profiling(bool on) { profiling_ = on; }
+    void stage_totals(double* ms, int64_t* calls);   // syncs pending events, accumulates, returns totals
+    void reset_stage_totals();
+    void mark(int stage, bool begin);
+
    private:
     Model model_;
+    bool profiling_ = false;
+    struct Pending { int stage; cudaEvent_t a, b; };
+    std::vector<Pending> pending_;
+    std::vector<cudaEvent_t> event_pool_;
+    double stage_ms_[ST_COUNT] = {0};
+    int64_t stage_calls_[ST_COUNT] = {0};
+    cudaEvent_t open_event_ = nullptr;
+    int open_stage_ = -1;
     int device_;
     cudaStream_t stream_ = nullptr;
     std::unique_ptr<DeviceModel> dm_;

@@ -91,6 +91,18 @@ int cg_assemble_device(cg_session* s, const cg_dframes* d, int precision, void* 
 int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads,
                            int64_t* evals3, int64_t* evals4);
 
+/* Number of CUDA kernels the last assembly launched. */
+int cg_session_last_launches(const cg_session* s, int64_t* launches);
+
+/* Per-stage GPU time: with profiling on, the session records CUDA events around each
+ * stage of every assembly (on its own stream).  cg_session_stage_times waits for them
+ * and returns accumulated milliseconds and call counts for the CG_NSTAGES stages
+ * named by cg_stage_name; cg_session_profile(s, 1) also clears the totals. */
+#define CG_NSTAGES 11
+int cg_session_profile(cg_session* s, int enable);
+int cg_session_stage_times(cg_session* s, double* ms, int64_t* calls);
+const char* cg_stage_name(int stage);
+
 /* Message of the calling thread's last failure ("" if none). */
 const char* cg_last_error(void);
 
