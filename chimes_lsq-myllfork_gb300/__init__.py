@@ -75,6 +75,7 @@ def lib():
         "cg_dframes_free": (None, [vp]),
         "cg_assemble_device": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, ctypes.c_int64]),
         "cg_session_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p, i64p]),
+        "cg_assemble_device_noalloc": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, ctypes.c_int64]),
         "cg_session_last_launches": (ctypes.c_int, [vp, i64p]),
         "cg_session_profile": (ctypes.c_int, [vp, ctypes.c_int]),
         "cg_session_stage_times": (ctypes.c_int, [vp, vp, vp]),
@@ -262,6 +263,12 @@ class Session:
         v = ctypes.c_int64()
         _check(lib().cg_session_last_launches(self._h, ctypes.byref(v)))
         return v.value
+
+    def assemble_device_noalloc(self, dframes, precision, a_device_ptr, lda):
+        """Allocation-free variant of assemble_device (work buffers from a fixed
+        device array inside the library; see include/chimes_gb300.h)."""
+        _check(lib().cg_assemble_device_noalloc(self._h, dframes._h, int(precision),
+                                                ctypes.c_void_p(int(a_device_ptr)), int(lda)))
 
     def last_counts(self):
         v = [ctypes.c_int64() for _ in range(5)]

@@ -213,6 +213,14 @@ int cg_assemble_device(cg_session* s, const cg_dframes* d, int precision, void* 
     });
 }
 
+int cg_assemble_device_noalloc(cg_session* s, const cg_dframes* d, int precision, void* A, int64_t lda) {
+    return guarded([&] {
+        need(s && d && A, "session/frames/A");
+        need(precision == CG_FP64 || precision == CG_FP32, "precision");
+        s->s->assemble_noalloc(*d->d, precision, A, lda, &s->last);
+    });
+}
+
 int cg_assemble(cg_session* s, const cg_frames* fr, int precision, void* A, int64_t lda) {
     return guarded([&] {
         need(s && fr && A, "session/frames/A");

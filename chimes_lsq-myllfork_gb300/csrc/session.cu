@@ -3,8 +3,10 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 
+#include "../../include/chimes_gb300.h"
 #include "assemble.h"
 #include "kernels.h"
 
@@ -335,16 +337,30 @@ std::unique_ptr<DeviceFrames> Session::upload(const FrameBatch& fb) {
     return df;
 }
 
-namespace {
-// stream-ordered scratch, released at the end of a call
+// Per-call scratch: stream-ordered device allocations released at the end of the
+// call, or -- for the no-allocation entry point -- a bump allocator over the
+// static device array below (256-byte aligned sub-buffers, capacity checked).
 struct Scratch {
     cudaStream_t s;
+    unsigned char* base = nullptr;
+    size_t cap = 0, used = 0;
     std::vector<void*> ptrs;
     explicit Scratch(cudaStream_t st) : s(st) {}
+    Scratch(cudaStream_t st, void* static_base, size_t capacity)
+        : s(st), base(reinterpret_cast<unsigned char*>(static_base)), cap(capacity) {}
     template <typename T>
     T* get(size_t n) {
+        const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+        if (base) {
+            const size_t off = (used + 255) & ~size_t(255);
+            if (off + bytes > cap)
+                throw Error(4, "input exceeds the no-allocation scratch capacity of " +
+                                   std::to_string(cap >> 20) + " MiB; use cg_assemble_device");
+            used = off + bytes;
+            return reinterpret_cast<T*>(base + off);
+        }
         void* p = nullptr;
-        CK(cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T), s));
+        CK(cudaMallocAsync(&p, bytes, s));
         ptrs.push_back(p);
         return reinterpret_cast<T*>(p);
     }
@@ -352,6 +368,28 @@ struct Scratch {
         for (void* p : ptrs) cudaFreeAsync(p, s);
     }
 };
+
+namespace {
+// Scratch of the no-allocation entry point: one fixed array per device that loads
+// this library, held until the process exits.  Host code must not use the symbol
+// as an address; noalloc_scratch() obtains the device address once per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[CG_NOALLOC_SCRATCH_BYTES];
+
+void* noalloc_scratch(int device) {
+    static std::mutex mu;
+    static std::vector<void*> ptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)ptr.size() <= device) ptr.resize(device + 1, nullptr);
+    if (!ptr[device]) {
+        // the caller has made `device` current
+        void* p = nullptr;
+        cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (rc != cudaSuccess || p == nullptr)
+            throw Error(3, std::string("cudaGetSymbolAddress(no-allocation scratch): ") + cudaGetErrorString(rc));
+        ptr[device] = p;
+    }
+    return ptr[device];
+}
 
 __global__ void k_count_evals(const int* type, int64_t n, const cgd::ClusterTypeDev* types,
                               unsigned long long* out) {
@@ -365,11 +403,22 @@ __global__ void k_count_evals(const int* type, int64_t n, const cgd::ClusterType
 
 void Session::assemble(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats) {
     CK(cudaSetDevice(device_));
+    Scratch S(stream_);
+    run(df, precision, A, lda, stats, S);
+}
+
+void Session::assemble_noalloc(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats) {
+    CK(cudaSetDevice(device_));
+    if (profiling_) throw Error(1, "stage profiling is not available in the no-allocation call");
+    Scratch S(stream_, noalloc_scratch(device_), CG_NOALLOC_SCRATCH_BYTES);
+    run(df, precision, A, lda, stats, S);
+}
+
+void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats, Scratch& S) {
     const cgd::ModelDev& M = dm_->dev;
     const cgd::FramesDev& F = df.dev;
     const Model& model = model_;
     cudaStream_t st = stream_;
-    Scratch S(st);
     const int nf = df.nframes;
     const int nreal = (int)df.natoms_total;
     const int prec = precision;

@@ -13,6 +13,7 @@
 
 namespace cg {
 
+struct Scratch;
 void cuda_check(cudaError_t e, const char* what);
 
 // Model tables uploaded to the device (immutable after creation).
@@ -73,6 +74,9 @@ class Session {
     std::unique_ptr<DeviceFrames> upload(const FrameBatch& fb);
     // A (device pointer, row-major, lda >= tot_all) receives the batch's rows.
     void assemble(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats);
+    // Same pipeline with every per-call device buffer taken from a fixed static
+    // device array (no cudaMalloc / cudaMallocAsync / cudaFree in the call).
+    void assemble_noalloc(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats);
 
     // Stage timing (CUDA events on the session stream).
     void set_profiling(bool on) { profiling_ = on; }
@@ -81,6 +85,7 @@ class Session {
     void mark(int stage, bool begin);
 
    private:
+    void run(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats, struct Scratch& S);
     Model model_;
     bool profiling_ = false;
     struct Pending { int stage; cudaEvent_t a, b; };

@@ -86,6 +86,24 @@ int cg_frames_upload(cg_session* s, const cg_frames* fr, cg_dframes** out);
 void cg_dframes_free(cg_dframes* d);
 int cg_assemble_device(cg_session* s, const cg_dframes* d, int precision, void* A_device, int64_t lda);
 
+/* Allocation-free assembly (this entry point has no counterpart in the reference).
+ * For callers that cannot allocate device memory while they run -- an MD engine or
+ * serving loop that reserves its memory at start-up and forbids allocation inside a
+ * step, or a host application that manages the device heap through its own pool --
+ * this variant of cg_assemble_device takes every per-call work buffer (neighbour
+ * lists, cluster lists, owner buckets, counters) from one fixed device array of
+ * CG_NOALLOC_SCRATCH_BYTES compiled into the library, and calls no cudaMalloc,
+ * cudaMallocAsync or cudaFree.  The caller still provides the uploaded frames and the
+ * output A (device, row-major, lda >= ntotal).  Inputs whose work lists do not fit
+ * are rejected with status 4 and a message naming the capacity.  The array exists
+ * once per GPU that loads the library and stays allocated until the process exits.
+ * The first call on a device looks up the array's device address (make that first
+ * call before any stream capture).  Every call on a device shares the array and
+ * overwrites it, so calls that overlap on the GPU (other threads, other sessions'
+ * streams) race; serialise them.  Stage profiling is not available here. */
+#define CG_NOALLOC_SCRATCH_BYTES (32u << 20)
+int cg_assemble_device_noalloc(cg_session* s, const cg_dframes* d, int precision, void* A_device, int64_t lda);
+
 /* Work counters of the last assembly: accepted 2-body pairs, triplets, quadruplets,
  * and (cluster, allowed-power) evaluations of the 3- and 4-body terms. */
 int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads,
