@@ -144,6 +144,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--frames", type=int, default=200, help="frames per rank (200 = the full workload)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -162,7 +163,7 @@ def main():
     cg = importlib.import_module("chimes_lsq-myllfork_gb300")
     synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
     tmp = tempfile.mkdtemp(prefix="chimes_bench_")
-    fm = synth.make_workload(WORKLOAD, tmp, seed=1000 + rank)   # weak scaling: each rank its own 200 frames
+    fm = synth.make_workload(WORKLOAD, tmp, nframes=args.frames, seed=1000 + rank)   # weak scaling: own frames per rank
     model = cg.Model(fm)
     frames = cg.Frames.read(model)
     sess = cg.Session(model, local)
@@ -212,7 +213,7 @@ def main():
     dom = max(stages, key=lambda k: stages[k][0])
     dom_ms = stages[dom][0] / max(1, stages[dom][1])
     cols = model.columns()
-    frames_n = 200
+    frames_n = args.frames
     force_rows = 3 * natoms
     vir_rows = nrows - force_rows
     # algorithmic bytes written per launch (A entries the kernel owns) and FP64 work
