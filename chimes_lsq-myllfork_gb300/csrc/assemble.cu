@@ -27,47 +27,63 @@ namespace cgd {
 static constexpr double PI_REF = 3.14159265359;   // src/functions.h:48
 
 // ---------------------------------------------------------------- basis
-// Cheby::set_polys (+ out-of-range branch) for one distance; fills T[0..snum], D[0..snum].
-__device__ void cheb_polys(const ModelDev& M, double lambda, double xavg, double xdiff, double smin, double r,
-                           int snum, double* T, double* D) {
+// Cheby::set_polys and set_polys_out_of_range (src/Cheby.C:207-443) evaluated as one
+// forward recursion: T_n(x) and U_{n-1}(x) give T'_n = n (dx/dr) U_{n-1}.  Writes
+// g[k] = f T_{n0+k} and h[k] = f T'_{n0+k} + f' T_{n0+k} for k < count (stride apart),
+// so nothing is kept in local memory.
+template <typename Out>
+__device__ __forceinline__ void basis_gh(const ModelDev& M, double lambda, double xavg, double xdiff, double smin,
+                                         double r, int n0, int count, double fc, double fd, Out* g, Out* h,
+                                         int stride) {
     const bool out = r < smin;
     const double rr = out ? smin : r;
     double x, ex = 0.0;
-    if (M.trans == 0) { ex = exp(-rr / lambda); x = (ex - xavg) / xdiff; }
-    else if (M.trans == 1) { x = (1.0 / rr - xavg) / xdiff; }
-    else { x = (rr - xavg) / xdiff; }
-    T[0] = 1.0; T[1] = x;
-    D[0] = 1.0; D[1] = 2.0 * x;
-    for (int i = 2; i <= snum; ++i) {
-        T[i] = 2.0 * x * T[i - 1] - T[i - 2];
-        D[i] = 2.0 * x * D[i - 1] - D[i - 2];
-    }
-    if (out && M.fix == 1) {   // ZERO_DERIV
-        for (int i = 0; i <= snum; ++i) D[i] = 0.0;
-        return;
-    }
+    const double ixd = 1.0 / xdiff;
+    if (M.trans == 0) { ex = exp(-rr / lambda); x = (ex - xavg) * ixd; }
+    else if (M.trans == 1) { x = (1.0 / rr - xavg) * ixd; }
+    else { x = (rr - xavg) * ixd; }
     double dxdr;
-    if (M.trans == 0) dxdr = (-ex / lambda) / xdiff;
-    else if (M.trans == 1) dxdr = -1.0 / (rr * rr * xdiff);
-    else dxdr = 1.0 / xdiff;
+    if (M.trans == 0) dxdr = -ex / lambda * ixd;
+    else if (M.trans == 1) dxdr = -ixd / (rr * rr);
+    else dxdr = ixd;
     dxdr *= M.deriv_const;
-    for (int i = snum; i >= 1; --i) D[i] = i * dxdr * D[i - 1];
-    D[0] = 0.0;
-    if (!out) return;
-    if (M.fix == 2) {   // CONSTANT_DERIV
-        for (int i = 0; i <= snum; ++i) T[i] += D[i] * (r - smin);
-    } else {            // SMOOTH
-        const double damp = exp((r - smin) / M.smooth);
-        for (int i = 0; i <= snum; ++i) { T[i] += M.smooth * (damp - 1.0) * D[i]; D[i] *= damp; }
+    const bool zero_d = out && M.fix == 1;           // ZERO_DERIV
+    double damp = 1.0, shift = 0.0;                  // SMOOTH: T += s (damp-1) T', T' *= damp
+    if (out && M.fix == 0) { damp = exp((r - smin) / M.smooth); shift = M.smooth * (damp - 1.0); }
+    const double lin = (out && M.fix == 2) ? (r - smin) : 0.0;   // CONSTANT_DERIV: T += T' (r - smin)
+    double t_prev = 1.0, t_cur = x;          // T_0, T_1
+    double u_prev2 = 0.0, u_prev = 1.0;      // U_{-1} (unused), U_0
+    const int n1 = n0 + count;
+    for (int n = 0; n < n1; ++n) {
+        double tn, un_1;                     // T_n, U_{n-1}
+        if (n == 0) { tn = 1.0; un_1 = 0.0; }
+        else if (n == 1) { tn = x; un_1 = 1.0; }
+        else {
+            tn = 2.0 * x * t_cur - t_prev;
+            t_prev = t_cur; t_cur = tn;
+            const double un = (n - 1 == 1) ? 2.0 * x : 2.0 * x * u_prev - u_prev2;   // U_{n-1}
+            u_prev2 = u_prev; u_prev = un;
+            un_1 = un;
+        }
+        double td = (n == 0 || zero_d) ? 0.0 : n * dxdr * un_1;
+        if (out) {
+            if (M.fix == 0) { tn += shift * td; td *= damp; }
+            else if (M.fix == 2) tn += td * lin;
+        }
+        if (n >= n0) {
+            g[(n - n0) * stride] = Out(fc * tn);
+            h[(n - n0) * stride] = Out(fc * td + fd * tn);
+        }
     }
 }
 
 // FCUT::get_fcut src/Fcut.C:17-72
 __device__ __forceinline__ void fcut_eval(const ModelDev& M, double r, double rmax, double& f, double& fd) {
     if (M.fcut == 0) {
-        double f0 = 1.0 - r / rmax;
+        const double irm = 1.0 / rmax;
+        double f0 = 1.0 - r * irm;
         f = f0 * f0 * f0;
-        fd = f0 * f0 * (-3.0 / rmax);
+        fd = f0 * f0 * (-3.0 * irm);
     } else {
         double th = rmax - M.fcut_offset * rmax;
         if (r < th) { f = 1.0; fd = 0.0; }
@@ -126,11 +142,9 @@ __device__ void slot_basis(const ModelDev& M, const FramesDev& F, int NB, int f,
     const ClusterTypeDev& CT = (NB == 3 ? M.types3 : M.types4)[T];
     const int* typ = F.type + F.atom_ofs[f];
     const int pt = M.int_pair_map[typ[ga % N] * M.natmtyp + typ[gbm % N]];
-    double Tn[MAXORD + 1], Dn[MAXORD + 1];
-    cheb_polys(M, M.pairs[pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], sb.r, ord, Tn, Dn);
     double fc, fd;
     fcut_eval(M, sb.r, CT.smax[s], fc, fd);
-    for (int n = 0; n < ord; ++n) { g[n] = fc * Tn[n]; h[n] = fc * Dn[n] + fd * Tn[n]; }
+    basis_gh(M, M.pairs[pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], sb.r, 0, ord, fc, fd, g, h, 1);
 }
 
 // ---------------------------------------------------------------- 2-body force rows
@@ -164,14 +178,15 @@ __global__ void k_force2(ModelDev M, FramesDev F, NeighDev NB, Buckets inc, cons
             const int pt = NB.pt2[p];
             const double r = NB.r2[p];
             const PairDev P = M.pairs[pt];
-            double Tn[MAXORD + 1], Dn[MAXORD + 1];
-            cheb_polys(M, P.lambda, P.xavg, P.xdiff, P.smin, r, ord, Tn, Dn);
             double fc, fd;
             fcut_eval(M, r, P.smax, fc, fd);
-            const double ux = NB.rab2[3 * p] / r, uy = NB.rab2[3 * p + 1] / r, uz = NB.rab2[3 * p + 2] / r;
+            const double ir = sgn * B.perm2 / r;
+            const double ux = NB.rab2[3 * p] * ir, uy = NB.rab2[3 * p + 1] * ir, uz = NB.rab2[3 * p + 2] * ir;
             R* d = sD + (size_t)threadIdx.x * 3 * ord;
+            // h_n (n = 1..ord) into the x slot, then spread to y and z
+            basis_gh(M, P.lambda, P.xavg, P.xdiff, P.smin, r, 1, ord, fc, fd, d + 1, d, 3);
             for (int n = 0; n < ord; ++n) {
-                const double t = sgn * B.perm2 * (fc * Dn[n + 1] + fd * Tn[n + 1]);
+                const double t = (double)d[3 * n];
                 d[3 * n] = R(t * ux); d[3 * n + 1] = R(t * uy); d[3 * n + 2] = R(t * uz);
             }
             sPt[threadIdx.x] = pt;
@@ -224,15 +239,10 @@ __global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t ld
             const int pt = NB.pt2[p];
             const double r = NB.r2[p];
             const PairDev P = M.pairs[pt];
-            double Tn[MAXORD + 1], Dn[MAXORD + 1];
-            cheb_polys(M, P.lambda, P.xavg, P.xdiff, P.smin, r, ord, Tn, Dn);
             double fc, fd;
             fcut_eval(M, r, P.smax, fc, fd);
             R* gh = sGH + (size_t)threadIdx.x * 2 * ord;
-            for (int n = 0; n < ord; ++n) {
-                gh[2 * n] = R(B.perm2 * fc * Tn[n + 1]);
-                gh[2 * n + 1] = R(B.perm2 * (fc * Dn[n + 1] + fd * Tn[n + 1]));
-            }
+            basis_gh(M, P.lambda, P.xavg, P.xdiff, P.smin, r, 1, ord, B.perm2 * fc, B.perm2 * fd, gh, gh + 1, 2);
             const double* x = NB.rab2 + 3 * p;
             R* v = sV + (size_t)threadIdx.x * 6;
             v[0] = R(x[0] * x[0] / r); v[1] = R(x[1] * x[1] / r); v[2] = R(x[2] * x[2] / r);
@@ -267,7 +277,7 @@ __global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t ld
 // One CTA per real (owner) atom.  PPT powers per thread cover every allowed power
 // tuple of the largest cluster type, so the accumulators stay in registers.
 template <int NBODY, typename R, int PPT>
-__global__ void __launch_bounds__(MB_THREADS) k_force_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
+__global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
                                                          const int64_t* key_frame_ofs, R* A, int64_t lda) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
     constexpr int NI = NBODY - 1;
@@ -395,8 +405,11 @@ __global__ void __launch_bounds__(MB_THREADS) k_force_mb(ModelDev M, FramesDev F
                         slot_basis(M, F, NBODY, f, mm, id, T, s, ord, g, g + ord, sb);
                         const int m = sPi[c];
                         const double sg = (m == sb.ma) ? 1.0 : ((m == sb.mb) ? -1.0 : 0.0);
-                        double* wv = sW + ((size_t)c * NP + s) * 3;
-                        wv[0] = sg * sb.rab[0] / sb.r; wv[1] = sg * sb.rab[1] / sb.r; wv[2] = sg * sb.rab[2] / sb.r;
+                        const double ir = sg / sb.r;
+                        const double wx = sb.rab[0] * ir, wy = sb.rab[1] * ir, wz = sb.rab[2] * ir;
+                        double* hw = sW + ((size_t)c * NP + s) * 3 * ord;   // h_s[n] * w_s,{x,y,z}
+                        const double* h = g + ord;
+                        for (int n = 0; n < ord; ++n) { hw[n] = h[n] * wx; hw[ord + n] = h[n] * wy; hw[2 * ord + n] = h[n] * wz; }
                     }
                     __syncthreads();
                     // (2) M_x,y,z over the incident-slot powers, Q over the others
@@ -404,18 +417,20 @@ __global__ void __launch_bounds__(MB_THREADS) k_force_mb(ModelDev M, FramesDev F
                     for (int t = threadIdx.x; t < nb * nzt; t += blockDim.x) {
                         const int c = t / nzt, z = t % nzt;
                         const double* GH = sGH + (size_t)c * NP * 2 * ord;
-                        const double* W = sW + (size_t)c * NP * 3;
+                        const double* HW = sW + (size_t)c * NP * 3 * ord;
                         R* tab = sTab + (size_t)c * per;
                         if (z < sizeI) {
                             int pwr[3] = {0, 0, 0}, zz = z;
                             for (int u = 0; u < NI; ++u) { pwr[u] = zz % ord; zz /= ord; }
+                            double gs[3];
+                            for (int u = 0; u < NI; ++u) gs[u] = GH[(size_t)I[u] * 2 * ord + pwr[u]];
+                            double other[3];   // product of the other incident slots' g
+                            if (NI == 2) { other[0] = gs[1]; other[1] = gs[0]; }
+                            else { other[0] = gs[1] * gs[2]; other[1] = gs[0] * gs[2]; other[2] = gs[0] * gs[1]; }
                             double mx = 0, my = 0, mz = 0;
                             for (int u = 0; u < NI; ++u) {
-                                double prod = GH[(size_t)I[u] * 2 * ord + ord + pwr[u]];
-                                for (int v2 = 0; v2 < NI; ++v2)
-                                    if (v2 != u) prod *= GH[(size_t)I[v2] * 2 * ord + pwr[v2]];
-                                const double* wv = W + I[u] * 3;
-                                mx += prod * wv[0]; my += prod * wv[1]; mz += prod * wv[2];
+                                const double* hw = HW + (size_t)I[u] * 3 * ord + pwr[u];
+                                mx += hw[0] * other[u]; my += hw[ord] * other[u]; mz += hw[2 * ord] * other[u];
                             }
                             tab[z] = R(mx); tab[sizeI + z] = R(my); tab[2 * sizeI + z] = R(mz);
                         } else {
@@ -468,24 +483,31 @@ __global__ void __launch_bounds__(MB_THREADS) k_force_mb(ModelDev M, FramesDev F
 
 // ---------------------------------------------------------------- many-body stress/energy rows
 // grid: (frame, cluster type, group-aligned power chunk); comps as in k_virial2.
+// grid: x = frame * ntypes + type, y = group-aligned power chunk, z = cluster chunk.
+// Each CTA sums VIR_CLUSTERS clusters and stores its column partials (7 comps);
+// k_virial_reduce adds the chunks in order and writes the rows.
 template <int NBODY, typename R>
 __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets bytype,
-                                                          const int64_t* key_frame_ofs, int ncomp, R* A, int64_t lda) {
+                                                          const int64_t* key_frame_ofs, int ncomp, R* part,
+                                                          int ntrue_max, int nchunks_max) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
     constexpr int N1 = NBODY - 1;
     constexpr int N2 = NP - N1;
     constexpr int PPT = VIR_PPT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int f = blockIdx.x;
-    const int T = blockIdx.y;
+    const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
+    const int f = blockIdx.x / ntypes;
+    const int T = blockIdx.x % ntypes;
     const int srows = F.stress_rows[f], erows = F.energy_rows[f];
     if (srows == 0 && erows == 0) return;
     const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
-    if ((int)blockIdx.z >= CT.vir_nchunk) return;
-    const int pbeg = CT.vir_chunk[blockIdx.z], pend = CT.vir_chunk[blockIdx.z + 1];
+    if ((int)blockIdx.y >= CT.vir_nchunk) return;
+    const int pbeg = CT.vir_chunk[blockIdx.y], pend = CT.vir_chunk[blockIdx.y + 1];
     const int64_t kb = key_frame_ofs[f];
-    const int64_t c0 = bytype.key_ofs[kb + T], c1 = bytype.key_ofs[kb + T + 1];
-    if (c0 == c1) return;
+    const int64_t t0 = bytype.key_ofs[kb + T], t1 = bytype.key_ofs[kb + T + 1];
+    const int64_t c0 = t0 + (int64_t)blockIdx.z * VIR_CLUSTERS;
+    if (c0 >= t1) return;
+    const int64_t c1 = min(t1, c0 + (int64_t)VIR_CLUSTERS);
     const int ord = NBODY == 3 ? M.order3 : M.order4;
     const uint8_t* pows = NBODY == 3 ? M.pow3 : M.pow4;
     const int* grps = NBODY == 3 ? M.grp3 : M.grp4;
@@ -572,9 +594,14 @@ __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev 
             for (int k = 0; k < PPT; ++k) {
                 if (i1[k] < 0) continue;
                 const R q1 = t1[i1[k]], q2 = t2[i2[k]];
-                acc[k][0] += q1 * q2;
-                for (int cc = 1; cc < ncomp; ++cc)
-                    acc[k][cc] -= t1[cc * size1 + i1[k]] * q2 + q1 * t2[cc * size2 + i2[k]];
+                acc[k][0] = fma(q1, q2, acc[k][0]);
+#pragma unroll
+                for (int cc = 1; cc < 7; ++cc) {   // fully unrolled: accumulators stay in registers
+                    if (cc < ncomp) {
+                        acc[k][cc] = fma(-t1[cc * size1 + i1[k]], q2, acc[k][cc]);
+                        acc[k][cc] = fma(-q1, t2[cc * size2 + i2[k]], acc[k][cc]);
+                    }
+                }
             }
         }
         __syncthreads();
@@ -587,16 +614,52 @@ __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev 
     }
     __syncthreads();
     const int* gp = grps + CT.grp_offset;
-    const double inv_vol = 1.0 / B.vol;
+    R* out = part + ((size_t)blockIdx.x * nchunks_max + blockIdx.z) * 7 * ntrue_max;
     for (int col = threadIdx.x; col < CT.n_true; col += blockDim.x) {
         const int pa = gp[col], pb = gp[col + 1];
         if (pa < pbeg || pa >= pend) continue;
         R sv[7] = {0, 0, 0, 0, 0, 0, 0};
         for (int p = pa; p < pb; ++p)
             for (int c = 0; c < 7; ++c) sv[c] += sTab[(size_t)(p - pbeg) * 7 + c];
-        for (int c = 0; c < 7; ++c) sv[c] = R(sv[c] * perm);
+        for (int c = 0; c < 7; ++c) out[(size_t)c * ntrue_max + col] = sv[c];
+    }
+}
+
+// Sum the cluster-chunk partials of each (frame, type) in chunk order and write the
+// stress / energy rows (PERM_SCALE and 1/V applied once, at the end).
+template <int NBODY, typename R>
+__global__ void k_virial_reduce(ModelDev M, FramesDev F, Buckets bytype, const int64_t* key_frame_ofs,
+                                const R* part, int ntrue_max, int nchunks_max, R* A, int64_t lda) {
+    const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
+    const int f = blockIdx.x / ntypes;
+    const int T = blockIdx.x % ntypes;
+    if (F.stress_rows[f] == 0 && F.energy_rows[f] == 0) return;
+    const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
+    const int64_t kb = key_frame_ofs[f];
+    const int64_t n = bytype.key_ofs[kb + T + 1] - bytype.key_ofs[kb + T];
+    if (n == 0) return;
+    const int nch = (int)((n + VIR_CLUSTERS - 1) / VIR_CLUSTERS);
+    const BoxDev& B = F.box[f];
+    const double perm = NBODY == 3 ? B.perm3 : B.perm4;
+    const double inv_vol = 1.0 / B.vol;
+    const R* base = part + (size_t)blockIdx.x * nchunks_max * 7 * ntrue_max;
+    for (int col = threadIdx.x; col < CT.n_true; col += blockDim.x) {
+        R sv[7] = {0, 0, 0, 0, 0, 0, 0};
+        for (int c = 0; c < nch; ++c)
+            for (int k = 0; k < 7; ++k) sv[k] += base[((size_t)c * 7 + k) * ntrue_max + col];
+        for (int k = 0; k < 7; ++k) sv[k] = R(sv[k] * perm);
         write_virial_rows(F, f, CT.col_base + col, sv, inv_vol, A, lda);
     }
+}
+
+// Largest cluster count of any (frame, type) bucket.
+__global__ void k_max_bucket(const int64_t* key_ofs, const int64_t* key_frame_ofs, int nframes, int ntypes,
+                             int* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nframes * ntypes) return;
+    const int f = i / ntypes, T = i % ntypes;
+    const int64_t kb = key_frame_ofs[f];
+    atomicMax(out, (int)(key_ofs[kb + T + 1] - key_ofs[kb + T]));
 }
 
 // ---------------------------------------------------------------- energy offset columns
@@ -675,22 +738,42 @@ void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const
     else force_mb_ppt<4, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (float*)A, lda, st);
 }
 
-void launch_virial_mb(int nbody, int prec, dim3 grid, size_t smem, const ModelDev& M, const FramesDev& F,
-                      const ClusterSet& CS, const Buckets& byt, const int64_t* kfo, int ncomp, void* A, int64_t lda,
-                      cudaStream_t st) {
+void launch_virial_mb(int nbody, int prec, int nframes, int ntypes, int nzchunk, int nchunks_max, int ntrue_max,
+                      size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
+                      const int64_t* kfo, int ncomp, void* part, void* A, int64_t lda, cudaStream_t st) {
+    dim3 grid(nframes * ntypes, nzchunk, nchunks_max);
+    const unsigned rgrid = (unsigned)(nframes * ntypes);
     if (nbody == 3 && prec == 0) {
         set_smem(k_virial_mb<3, double>, smem);
-        k_virial_mb<3, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (double*)A, lda);
+        k_virial_mb<3, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (double*)part, ntrue_max,
+                                                                nchunks_max);
+        k_virial_reduce<3, double><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const double*)part, ntrue_max, nchunks_max,
+                                                          (double*)A, lda);
     } else if (nbody == 3) {
         set_smem(k_virial_mb<3, float>, smem);
-        k_virial_mb<3, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (float*)A, lda);
+        k_virial_mb<3, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (float*)part, ntrue_max,
+                                                               nchunks_max);
+        k_virial_reduce<3, float><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const float*)part, ntrue_max, nchunks_max,
+                                                         (float*)A, lda);
     } else if (prec == 0) {
         set_smem(k_virial_mb<4, double>, smem);
-        k_virial_mb<4, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (double*)A, lda);
+        k_virial_mb<4, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (double*)part, ntrue_max,
+                                                                nchunks_max);
+        k_virial_reduce<4, double><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const double*)part, ntrue_max, nchunks_max,
+                                                          (double*)A, lda);
     } else {
         set_smem(k_virial_mb<4, float>, smem);
-        k_virial_mb<4, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (float*)A, lda);
+        k_virial_mb<4, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (float*)part, ntrue_max,
+                                                               nchunks_max);
+        k_virial_reduce<4, float><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const float*)part, ntrue_max, nchunks_max,
+                                                         (float*)A, lda);
     }
+}
+
+void launch_max_bucket(const int64_t* key_ofs, const int64_t* kfo, int nframes, int ntypes, int* out,
+                       cudaStream_t st) {
+    const int n = nframes * ntypes;
+    if (n > 0) k_max_bucket<<<(n + 255) / 256, 256, 0, st>>>(key_ofs, kfo, nframes, ntypes, out);
 }
 
 void launch_energy_cols(int prec, int nframes, const ModelDev& M, const FramesDev& F, void* A, int64_t lda,

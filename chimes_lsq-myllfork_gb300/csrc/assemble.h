@@ -8,6 +8,7 @@ constexpr int MB_THREADS = 512;     // threads of the many-body kernels
 constexpr int MB_CB = 16;           // clusters staged per shared-memory batch
 constexpr int MB_MAX_ENT = 1024;    // owner incidences handled per pass
 constexpr int VIR_PPT = 4;          // powers per thread in the stress/energy kernel
+constexpr int VIR_CLUSTERS = 512;   // clusters per CTA in the stress/energy kernel
 constexpr int F2_THREADS = 128;     // 2-body kernels
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -30,7 +31,7 @@ __host__ __device__ inline MbForceSmem mb_force_smem(int nbody, int ord, int nke
     s.pi = align16(s.q + MB_CB * sizeof(int));
     s.gh = align16(s.pi + MB_CB * sizeof(int));
     s.w = align16(s.gh + (size_t)MB_CB * np * 2 * ord * sizeof(double));
-    s.tab = align16(s.w + (size_t)MB_CB * np * 3 * sizeof(double));
+    s.tab = align16(s.w + (size_t)MB_CB * np * 3 * ord * sizeof(double));
     size_t tab = (size_t)MB_CB * per;
     if ((size_t)max_allowed * 3 > tab) tab = (size_t)max_allowed * 3;
     s.total = align16(s.tab + tab * rsize);
@@ -85,9 +86,13 @@ void launch_virial2(int prec, int nframes, const ModelDev& M, const FramesDev& F
 void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,
                      const ClusterSet& CS, const Buckets& inc, const int64_t* key_frame_ofs, void* A, int64_t lda,
                      cudaStream_t st);
-void launch_virial_mb(int nbody, int prec, dim3 grid, size_t smem, const ModelDev& M, const FramesDev& F,
-                      const ClusterSet& CS, const Buckets& bytype, const int64_t* key_frame_ofs, int ncomp, void* A,
-                      int64_t lda, cudaStream_t st);
+// Stress/energy rows: nchunks_max cluster chunks of VIR_CLUSTERS per (frame, type);
+// part holds nframes*ntypes*nchunks_max*7*ntrue_max partial sums (R).
+void launch_virial_mb(int nbody, int prec, int nframes, int ntypes, int nzchunk, int nchunks_max, int ntrue_max,
+                      size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
+                      const int64_t* key_frame_ofs, int ncomp, void* part, void* A, int64_t lda, cudaStream_t st);
+void launch_max_bucket(const int64_t* key_ofs, const int64_t* key_frame_ofs, int nframes, int ntypes, int* out,
+                       cudaStream_t st);
 void launch_energy_cols(int prec, int nframes, const ModelDev& M, const FramesDev& F, void* A, int64_t lda,
                         cudaStream_t st);
 

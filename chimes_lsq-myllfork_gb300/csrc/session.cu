@@ -538,10 +538,22 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
         if (virial) {
             cgd::MbVirSmem V = cgd::mb_vir_smem(nbody, ord, cgd::VIR_PPT * cgd::MB_THREADS, rsize);
             if (V.total > 227 * 1024) throw Error(2, "cluster order too large for the device stress/energy kernel");
-            const int maxch = (max_allowed + cgd::VIR_PPT * cgd::MB_THREADS - 1) / (cgd::VIR_PPT * cgd::MB_THREADS) + 1;
-            dim3 grid(nf, ntypes, std::min(maxch, cgd::MAXCHUNK));
+            const int maxz = (max_allowed + cgd::VIR_PPT * cgd::MB_THREADS - 1) / (cgd::VIR_PPT * cgd::MB_THREADS) + 1;
+            int* d_max = S.get<int>(1);
+            CK(cudaMemsetAsync(d_max, 0, sizeof(int), st));
+            cgd::launch_max_bucket(byt.key_ofs, kfo_types, nf, ntypes, d_max, st); L();
+            int hmax = 0;
+            CK(cudaMemcpyAsync(&hmax, d_max, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            const int nch = std::max(1, (hmax + cgd::VIR_CLUSTERS - 1) / cgd::VIR_CLUSTERS);
+            const auto& cl = nbody == 3 ? model.trips : model.quads;
+            int ntrue_max = 1;
+            for (const auto& ct : cl.vec) ntrue_max = std::max(ntrue_max, ct.excluded ? 0 : ct.n_true);
+            void* part = prec == 0 ? (void*)S.get<double>((size_t)nf * ntypes * nch * 7 * ntrue_max)
+                                   : (void*)S.get<float>((size_t)nf * ntypes * nch * 7 * ntrue_max);
             mark(nbody == 3 ? ST_VIRIAL3 : ST_VIRIAL4, true);
-            cgd::launch_virial_mb(nbody, prec, grid, V.total, M, F, CS, byt, kfo_types, ncomp, A, lda, st); L();
+            cgd::launch_virial_mb(nbody, prec, nf, ntypes, std::min(maxz, cgd::MAXCHUNK), nch, ntrue_max, V.total, M, F,
+                                  CS, byt, kfo_types, ncomp, part, A, lda, st); L(2);
             mark(nbody == 3 ? ST_VIRIAL3 : ST_VIRIAL4, false);
             CK(cudaGetLastError());
         }
