@@ -79,7 +79,7 @@ def build(verbose=False, force=False):
                 if verbose and out.strip():
                     print(out)
     if force or jobs or not os.path.exists(LIB):
-        _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])
+        _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart", "-lcublas"])
     return LIB
 
 

@@ -257,6 +257,32 @@ int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplet
     });
 }
 
+int cg_gram(cg_session* s, int a_precision, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b,
+            int mode, double* G, double* h) {
+    return guarded([&] {
+        need(s && A && b && G && h && ncols > 0 && lda >= ncols && nrows >= 0, "gram arguments");
+        need(a_precision == CG_FP64 || a_precision == CG_FP32, "precision");
+        need(mode == CG_GRAM_FP64 || mode == CG_GRAM_BF16X3, "gram mode");
+        s->s->gram(a_precision, A, lda, nrows, ncols, b, mode, G, h);
+    });
+}
+
+int cg_gram_finish(cg_session* s, double* G, int ncols) {
+    return guarded([&] {
+        need(s && G && ncols > 0, "gram_finish arguments");
+        s->s->gram_finish(G, ncols);
+    });
+}
+
+int cg_solve(cg_session* s, const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda,
+             int64_t nrows, const double* b, int iters, double* x, double* info) {
+    return guarded([&] {
+        need(s && G && h && x && ncols > 0 && iters >= 0, "solve arguments");
+        need(iters == 0 || (A && b && lda >= ncols), "refinement needs A and b");
+        s->s->solve(G, h, ncols, ridge, A, lda, nrows, b, iters, x, info);
+    });
+}
+
 int cg_session_last_launches(const cg_session* s, int64_t* launches) {
     return guarded([&] {
         need(s && launches, "session/launches");

@@ -1,0 +1,374 @@
+// Normal equations of the fit: G = A^T A and h = A^T b, streamed over row blocks.
+//
+// The reference solves the least-squares problem with a truncated SVD of the full
+// A in numpy (src/chimes_lsq.py:169-214); this build forms the Gram instead, the
+// path's only dense contraction and its only tensor-core work:
+//  * mixed form: A is split into two BF16 planes (hi = bf16(a), lo = bf16(a - hi)),
+//    stored transposed (K = rows contiguous), and G += hi^T hi + hi^T lo + lo^T hi on
+//    tcgen05 (kind::f16, FP32 accumulation in TMEM).  Operands arrive by TMA with
+//    128-byte swizzle through a 3-stage mbarrier pipeline; one thread issues the
+//    MMAs; four warps drain TMEM with tcgen05.ld and add the split-K partial tile
+//    into an FP64 G.
+//  * plain form: FP64 G by the library SYRK (cuBLAS), a plain GEMM.
+//  * h = A^T b is an FP64 matrix-vector product (memory bound) in both forms.
+// Every wait on an mbarrier is bounded (about one second); on time-out the kernel
+// records an error code, skips its stores, frees its TMEM and returns.
+#include <cublas_v2.h>
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+
+#include "gram.h"
+
+namespace cgd {
+
+constexpr int GB_M = 128, GB_N = 128, GB_K = 64, GB_STAGES = 3, GB_THREADS = 128;
+constexpr uint32_t GB_TILE_BYTES = GB_M * GB_K * 2;         // one 128x64 bf16 operand tile (16 KB)
+constexpr uint32_t GB_STAGE_BYTES = 4 * GB_TILE_BYTES;      // A_hi, A_lo, B_hi, B_lo
+constexpr long long GB_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
+
+// ---------------------------------------------------------------- split + transpose
+// planes[p][c][k] (bf16, k contiguous) for rows [r0, r0+nr) of A (row-major, lda),
+// zero padded to (cpad, kpad).
+template <typename T>
+__global__ void k_split_transpose(const T* __restrict__ A, int64_t lda, int64_t r0, int64_t nr, int ncols,
+                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t kpad) {
+    __shared__ float tile[32][33];
+    const int64_t k0 = (int64_t)blockIdx.x * 32;   // rows of A -> K
+    const int c0 = blockIdx.y * 32;                // columns of A -> plane rows
+    for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+        const int64_t k = k0 + dy;
+        const int c = c0 + threadIdx.x;
+        float v = 0.f;
+        if (k < nr && c < ncols) v = (float)A[(r0 + k) * lda + c];
+        tile[dy][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+        const int c = c0 + dy;
+        const int64_t k = k0 + threadIdx.x;
+        const float v = tile[threadIdx.x][dy];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+        hi[(int64_t)c * kpad + k] = h;
+        lo[(int64_t)c * kpad + k] = l;
+    }
+}
+
+// h[c] += sum_r A[r][c] b[r] in FP64: partial[y][c] over row slices y (coalesced
+// along c), then an ordered sum over y, so the result is reproducible.
+constexpr int ATB_SLICES = 256;
+template <typename T>
+__global__ void k_atb_partial(const T* __restrict__ A, int64_t lda, int64_t nr, int ncols,
+                              const double* __restrict__ b, double* __restrict__ partial) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    const int64_t per = (nr + gridDim.y - 1) / gridDim.y;
+    const int64_t r0 = (int64_t)blockIdx.y * per, r1 = min(nr, r0 + per);
+    double s = 0.0;
+    for (int64_t r = r0; r < r1; ++r) s = fma((double)A[r * lda + c], b[r], s);
+    partial[(int64_t)blockIdx.y * ncols + c] = s;
+}
+__global__ void k_atb_reduce(const double* __restrict__ partial, int nslices, int ncols, double* __restrict__ h) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    double s = 0.0;
+    for (int y = 0; y < nslices; ++y) s += partial[(int64_t)y * ncols + c];
+    h[c] += s;
+}
+
+__global__ void k_symmetrize(double* G, int n) {
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && j < n && j < i) G[(int64_t)i * n + j] = G[(int64_t)j * n + i];
+}
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false (and an error code in *err) when the phase does not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > GB_WAIT_CYCLES) {
+            atomicCAS(err, 0, code);
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+// K-major operand with 128-byte swizzle: 8-row atoms of 1024 B (SBO), version 1.
+__device__ __forceinline__ uint64_t smem_desc(const void* p) {
+    const uint64_t addr = smem_u32(p);
+    return ((addr >> 4) & 0x3FFFull) | ((uint64_t)(16 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           (1ull << 46) | (2ull << 61);
+}
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// ---------------------------------------------------------------- tcgen05 Gram tile
+// grid.x: upper-triangular tile pair (i <= j), grid.y: K slice.
+__global__ void __launch_bounds__(GB_THREADS, 1)
+    k_gram_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo, int ntile,
+              int64_t kpad, int64_t kslice, int ncols, double* __restrict__ G, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + GB_STAGES * GB_STAGE_BYTES);
+    uint64_t* empty = full + GB_STAGES;
+    uint64_t* done = empty + GB_STAGES;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+
+    // tile pair from the linear upper-triangle index
+    int t = blockIdx.x, ti = 0;
+    while (t >= ntile - ti) { t -= ntile - ti; ++ti; }
+    const int tj = ti + t;
+    const int64_t kb = (int64_t)blockIdx.y * kslice;
+    const int64_t ke = min(kpad, kb + kslice);
+    const int nk = (int)((ke - kb) / GB_K);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < GB_STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {   // TMEM: 128 lanes x 128 FP32 columns
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(GB_N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0 && nk > 0) {   // producer
+        for (int it = 0; it < nk && ok; ++it) {
+            const int s = it % GB_STAGES;
+            const uint32_t ph = (uint32_t)(it / GB_STAGES) & 1u;
+            if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+            unsigned char* st = smem + s * GB_STAGE_BYTES;
+            mbar_expect_tx(&full[s], GB_STAGE_BYTES);
+            const int x = (int)(kb + (int64_t)it * GB_K);
+            tma_load_2d(st, &map_hi, &full[s], x, ti * GB_M);
+            tma_load_2d(st + GB_TILE_BYTES, &map_lo, &full[s], x, ti * GB_M);
+            tma_load_2d(st + 2 * GB_TILE_BYTES, &map_hi, &full[s], x, tj * GB_N);
+            tma_load_2d(st + 3 * GB_TILE_BYTES, &map_lo, &full[s], x, tj * GB_N);
+        }
+        // drain: wait for the copies still in flight before the CTA may exit
+        if (!ok)
+            for (int s = 0; s < GB_STAGES; ++s) mbar_try_wait(&full[s], 0);
+    } else if (warp == 1 && lane == 0 && nk > 0) {   // MMA issuer
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GB_N >> 3) << 17) |
+                               ((uint32_t)(GB_M >> 4) << 24);
+        for (int it = 0; it < nk && ok; ++it) {
+            const int s = it % GB_STAGES;
+            const uint32_t ph = (uint32_t)(it / GB_STAGES) & 1u;
+            if (!mbar_wait(&full[s], ph, err, 2)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            unsigned char* st = smem + s * GB_STAGE_BYTES;
+            const uint64_t ahi = smem_desc(st), alo = smem_desc(st + GB_TILE_BYTES);
+            const uint64_t bhi = smem_desc(st + 2 * GB_TILE_BYTES), blo = smem_desc(st + 3 * GB_TILE_BYTES);
+#pragma unroll
+            for (int kk = 0; kk < GB_K / 16; ++kk) {
+                const uint64_t adv = (uint64_t)((kk * 32) >> 4);   // 16 bf16 = 32 B along K
+                umma_bf16(tmem, ahi + adv, bhi + adv, idesc, (it > 0 || kk > 0) ? 1u : 0u);
+                umma_bf16(tmem, ahi + adv, blo + adv, idesc, 1u);
+                umma_bf16(tmem, alo + adv, bhi + adv, idesc, 1u);
+            }
+            umma_commit(&empty[s]);
+        }
+        umma_commit(done);
+    }
+    __syncwarp();
+    // epilogue: all four warps (TMEM lane quarter = warp)
+    bool have = nk > 0;
+    if (have) have = mbar_wait(done, 0, err, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (have && *err == 0) {
+        const int row = ti * GB_M + warp * 32 + lane;
+#pragma unroll 1
+        for (int c0 = 0; c0 < GB_N; c0 += 32) {
+            uint32_t v[32];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < ncols) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    const int col = tj * GB_N + c0 + c;
+                    if (col < ncols && (ti != tj || col >= row))
+                        atomicAdd(&G[(int64_t)row * ncols + col], (double)__uint_as_float(v[c]));
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GB_N) : "memory");
+    }
+}
+
+}  // namespace cgd
+
+// ================================================================ host side
+namespace cg {
+
+static void ck(cudaError_t e, const char* w) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error in ") + w + ": " + cudaGetErrorString(e));
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    if (!fn) throw std::runtime_error("cuTensorMapEncodeTiled is not available from the driver");
+    return fn;
+}
+
+static CUtensorMap plane_map(void* base, int64_t kpad, int64_t cpad) {
+    CUtensorMap m;
+    cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)cpad};
+    cuuint64_t strides[1] = {(cuuint64_t)(kpad * 2)};
+    cuuint32_t box[2] = {cgd::GB_K, cgd::GB_M};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return m;
+}
+
+size_t gram_plane_bytes(int64_t nrows_block, int ncols) {
+    const int64_t kpad = (nrows_block + cgd::GB_K - 1) / cgd::GB_K * cgd::GB_K;
+    const int64_t cpad = (ncols + cgd::GB_M - 1) / cgd::GB_M * cgd::GB_M;
+    return (size_t)(2 * cpad * kpad * 2);
+}
+
+void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
+                     double* G, double* h, void* planes, size_t planes_bytes, int* d_err, void* cublas,
+                     cudaStream_t st) {
+    if (nrows <= 0) return;
+    // h += A^T b (FP64), reproducible
+    {
+        const int ns = (int)std::min<int64_t>(nrows, cgd::ATB_SLICES);
+        double* partial = nullptr;
+        ck(cudaMallocAsync((void**)&partial, sizeof(double) * ns * ncols, st), "atb scratch");
+        dim3 grid((ncols + 127) / 128, ns);
+        if (prec_in == 0) cgd::k_atb_partial<double><<<grid, 128, 0, st>>>((const double*)A, lda, nrows, ncols, b, partial);
+        else cgd::k_atb_partial<float><<<grid, 128, 0, st>>>((const float*)A, lda, nrows, ncols, b, partial);
+        cgd::k_atb_reduce<<<(ncols + 127) / 128, 128, 0, st>>>(partial, ns, ncols, h);
+        ck(cudaGetLastError(), "k_atb");
+        ck(cudaFreeAsync(partial, st), "atb scratch free");
+    }
+    if (mode == 0) {   // FP64 library SYRK (upper triangle of the row-major G)
+        if (prec_in != 0) throw std::runtime_error("the FP64 Gram needs an FP64 A");
+        cublasHandle_t hnd = (cublasHandle_t)cublas;
+        cublasSetStream(hnd, st);
+        const double one = 1.0;
+        // row-major A (nrows x ncols) is column-major X = A^T (ncols x nrows); G = X X^T.
+        cublasStatus_t s = cublasDsyrk(hnd, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, ncols, (int)nrows, &one,
+                                       (const double*)A, (int)lda, &one, G, ncols);
+        if (s != CUBLAS_STATUS_SUCCESS) throw std::runtime_error("cublasDsyrk failed");
+        return;   // lower triangle of column-major G == upper triangle of row-major G
+    }
+    // split-BF16 3-term on tcgen05, in row blocks that fit the plane buffer
+    const int64_t cpad = (ncols + cgd::GB_M - 1) / cgd::GB_M * cgd::GB_M;
+    int64_t rblock = (int64_t)(planes_bytes / (size_t)(2 * cpad * 2)) / cgd::GB_K * cgd::GB_K;
+    if (rblock <= 0) throw std::runtime_error("Gram plane buffer too small");
+    const int ntile = (int)(cpad / cgd::GB_M);
+    const int npairs = ntile * (ntile + 1) / 2;
+    const size_t smem = (size_t)cgd::GB_STAGES * cgd::GB_STAGE_BYTES + 1024 + 256;
+    ck(cudaFuncSetAttribute(cgd::k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr");
+    for (int64_t r0 = 0; r0 < nrows; r0 += rblock) {
+        const int64_t nr = std::min(rblock, nrows - r0);
+        const int64_t kpad = (nr + cgd::GB_K - 1) / cgd::GB_K * cgd::GB_K;
+        __nv_bfloat16* hi = (__nv_bfloat16*)planes;
+        __nv_bfloat16* lo = hi + cpad * kpad;
+        dim3 tg((unsigned)(kpad / 32), (unsigned)(cpad / 32));
+        if (prec_in == 0)
+            cgd::k_split_transpose<double><<<tg, dim3(32, 8), 0, st>>>((const double*)A, lda, r0, nr, ncols, hi, lo, kpad);
+        else
+            cgd::k_split_transpose<float><<<tg, dim3(32, 8), 0, st>>>((const float*)A, lda, r0, nr, ncols, hi, lo, kpad);
+        ck(cudaGetLastError(), "k_split_transpose");
+        CUtensorMap mhi = plane_map(hi, kpad, cpad), mlo = plane_map(lo, kpad, cpad);
+        // K slices: about four CTAs per SM in total
+        const int64_t ksteps = kpad / cgd::GB_K;
+        int64_t nslice = std::max<int64_t>(1, std::min<int64_t>(ksteps, (608 + npairs - 1) / npairs));
+        const int64_t kslice = (ksteps + nslice - 1) / nslice * cgd::GB_K;
+        nslice = (kpad + kslice - 1) / kslice;
+        cgd::k_gram_tc<<<dim3(npairs, (unsigned)nslice), cgd::GB_THREADS, smem, st>>>(mhi, mlo, ntile, kpad, kslice,
+                                                                                      ncols, G, d_err);
+        ck(cudaGetLastError(), "k_gram_tc");
+    }
+}
+
+void gram_symmetrize(double* G, int n, bool from_upper, cudaStream_t st) {
+    (void)from_upper;
+    dim3 grid((n + 31) / 32, (n + 31) / 32);
+    cgd::k_symmetrize<<<grid, dim3(32, 32), 0, st>>>(G, n);
+    ck(cudaGetLastError(), "k_symmetrize");
+}
+
+}  // namespace cg

@@ -1,0 +1,32 @@
+// Normal equations and their FP64 solve (see gram.cu and solve.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace cg {
+
+// Bytes of the two BF16 planes for an A block of nrows_block rows.
+size_t gram_plane_bytes(int64_t nrows_block, int ncols);
+
+// G (row-major ncols x ncols FP64, upper triangle) += A^T A and h += A^T b for the
+// device A block (row-major, lda; prec_in 0 = FP64, 1 = FP32).  mode 0: FP64 library
+// SYRK; mode 1: split-BF16 3-product Gram on tcgen05 (planes: scratch of at least
+// gram_plane_bytes(64, ncols) bytes; larger buffers take larger row blocks).
+void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
+                     double* G, double* h, void* planes, size_t planes_bytes, int* d_err, void* cublas,
+                     cudaStream_t st);
+// Copy the upper triangle of G to the lower one.
+void gram_symmetrize(double* G, int n, bool from_upper, cudaStream_t st);
+
+// In-place Cholesky G = L L^T (lower, row-major storage of a symmetric matrix).
+// Returns false when a pivot is not positive.
+bool cholesky(double* G, int n, int* d_info, void* cublas, cudaStream_t st);
+// x = G^-1 h with the factor from cholesky().
+void cholesky_solve(const double* L, int n, const double* h, double* x, void* cublas, cudaStream_t st);
+// r = b - A x (FP64 A, row-major lda) and g = A^T r; returns ||r||_2 and ||g||_2.
+void residual(const double* A, int64_t lda, int64_t nrows, int ncols, const double* b, const double* x, double* r,
+              double* g, double* rnorm, double* gnorm, void* cublas, cudaStream_t st);
+
+}  // namespace cg

@@ -6,7 +6,10 @@
 #include <mutex>
 #include <numeric>
 
+#include <cublas_v2.h>
+
 #include "../../include/chimes_gb300.h"
+#include "gram.h"
 #include "assemble.h"
 #include "kernels.h"
 
@@ -293,11 +296,16 @@ Session::Session(const Model& m, int device) : model_(m), device_(device) {
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     dm_.reset(new DeviceModel(model_, cgd::VIR_PPT * cgd::MB_THREADS));
+    cublasHandle_t h = nullptr;
+    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) throw Error(3, "cublasCreate failed");
+    cublasSetStream(h, stream_);
+    cublas_ = h;
 }
 
 Session::~Session() {
     for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : event_pool_) cudaEventDestroy(e);
+    if (cublas_) cublasDestroy((cublasHandle_t)cublas_);
     dm_.reset();
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -572,6 +580,107 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
         stats->triplets = n3; stats->quads = n4;
         stats->power_evals3 = (int64_t)ev[0]; stats->power_evals4 = (int64_t)ev[1];
         stats->launches = launches;
+    }
+}
+
+// ------------------------------------------------------------------ normal equations
+void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
+                   double* G, double* h) {
+    CK(cudaSetDevice(device_));
+    Scratch S(stream_);
+    int* d_err = S.get<int>(1);
+    CK(cudaMemsetAsync(d_err, 0, sizeof(int), stream_));
+    void* planes = nullptr;
+    size_t pbytes = 0;
+    if (mode == 1) {
+        const int64_t cpad = (ncols + 127) / 128 * 128;
+        int64_t rb = std::min<int64_t>(nrows, std::max<int64_t>(64, (int64_t)(1ull << 30) / (4 * cpad)));
+        pbytes = gram_plane_bytes(rb, ncols);
+        planes = S.get<unsigned char>(pbytes);
+    }
+    try {
+        gram_accumulate(prec_in, A, lda, nrows, ncols, b, mode, G, h, planes, pbytes, d_err, cublas_, stream_);
+    } catch (const std::runtime_error& e) {
+        throw Error(3, e.what());
+    }
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    if (herr) throw Error(3, "tensor-core Gram kernel timed out waiting on its pipeline (code " + std::to_string(herr) + ")");
+}
+
+void Session::gram_finish(double* G, int ncols) {
+    CK(cudaSetDevice(device_));
+    gram_symmetrize(G, ncols, true, stream_);
+}
+
+__global__ void k_add_diag(double* G, int n, double v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) G[(int64_t)i * n + i] += v;
+}
+
+void Session::solve(const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda,
+                    int64_t nrows, const double* b, int iters, double* x, double* info) {
+    CK(cudaSetDevice(device_));
+    Scratch S(stream_);
+    double* L = S.get<double>((size_t)ncols * ncols);
+    int* d_info = S.get<int>(1);
+    cublasHandle_t hb = (cublasHandle_t)cublas_;
+    try {
+        // Cholesky of G + ridge I; the ridge grows tenfold (up to 8 times) until the
+        // factorisation succeeds (a mixed-precision G can be indefinite at tiny ridges).
+        double used = ridge;
+        bool ok = false;
+        for (int attempt = 0; attempt < 9 && !ok; ++attempt) {
+            CK(cudaMemcpyAsync(L, G, sizeof(double) * ncols * ncols, cudaMemcpyDeviceToDevice, stream_));
+            if (used != 0.0) k_add_diag<<<(ncols + 255) / 256, 256, 0, stream_>>>(L, ncols, used);
+            ok = cholesky(L, ncols, d_info, cublas_, stream_);
+            if (!ok) used = used > 0.0 ? used * 10.0 : 1e-12;
+        }
+        if (!ok) throw Error(2, "the normal-equations matrix is not positive definite even with a ridge");
+        cholesky_solve(L, ncols, h, x, cublas_, stream_);
+        double rn = 0, gn = 0;
+        if (iters > 0 && A && b) {
+            // preconditioned CG on the exact normal equations A^T A x = A^T b (FP64 products
+            // through A), preconditioner (L L^T)^-1
+            double* r = S.get<double>(ncols);   // normal-equation residual
+            double* z = S.get<double>(ncols);
+            double* pv = S.get<double>(ncols);
+            double* q = S.get<double>(ncols);
+            double* t = S.get<double>(nrows);
+            const double one = 1.0, zero = 0.0;
+            cublasSetStream(hb, stream_);
+            cublasSetPointerMode(hb, CUBLAS_POINTER_MODE_HOST);
+            residual(A, lda, nrows, ncols, b, x, t, r, &rn, &gn, cublas_, stream_);
+            cholesky_solve(L, ncols, r, z, cublas_, stream_);
+            CK(cudaMemcpyAsync(pv, z, sizeof(double) * ncols, cudaMemcpyDeviceToDevice, stream_));
+            double rz = 0;
+            cublasDdot(hb, ncols, r, 1, z, 1, &rz);
+            for (int it = 0; it < iters && rz > 0.0; ++it) {
+                // q = A^T (A p)
+                cublasDgemv(hb, CUBLAS_OP_T, ncols, (int)nrows, &one, A, (int)lda, pv, 1, &zero, t, 1);
+                cublasDgemv(hb, CUBLAS_OP_N, ncols, (int)nrows, &one, A, (int)lda, t, 1, &zero, q, 1);
+                double pq = 0;
+                cublasDdot(hb, ncols, pv, 1, q, 1, &pq);
+                if (!(pq > 0.0)) break;
+                const double alpha = rz / pq, malpha = -alpha;
+                cublasDaxpy(hb, ncols, &alpha, pv, 1, x, 1);
+                cublasDaxpy(hb, ncols, &malpha, q, 1, r, 1);
+                cholesky_solve(L, ncols, r, z, cublas_, stream_);
+                double rz_new = 0;
+                cublasDdot(hb, ncols, r, 1, z, 1, &rz_new);
+                const double beta = rz_new / rz;
+                cublasDscal(hb, ncols, &beta, pv, 1);
+                cublasDaxpy(hb, ncols, &one, z, 1, pv, 1);
+                rz = rz_new;
+            }
+            residual(A, lda, nrows, ncols, b, x, t, r, &rn, &gn, cublas_, stream_);
+        }
+        CK(cudaStreamSynchronize(stream_));
+        if (info) { info[0] = rn; info[1] = gn; info[2] = used; }
+    } catch (const std::runtime_error& e) {
+        if (dynamic_cast<const Error*>(&e)) throw;
+        throw Error(3, e.what());
     }
 }
 

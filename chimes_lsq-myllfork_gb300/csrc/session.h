@@ -78,6 +78,16 @@ class Session {
     // device array (no cudaMalloc / cudaMallocAsync / cudaFree in the call).
     void assemble_noalloc(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats);
 
+    // Normal equations (gram.cu / solve.cu) on the session stream.
+    void gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode, double* G,
+              double* h);
+    void gram_finish(double* G, int ncols);
+    // x = (G + ridge I)^-1 h, then `iters` preconditioned-CG steps on A^T A x = A^T b
+    // (A may be null when iters == 0).  info: [rnorm, gnorm, ridge used].
+    void solve(const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda, int64_t nrows,
+               const double* b, int iters, double* x, double* info);
+    void* cublas() const { return cublas_; }
+
     // Stage timing (CUDA events on the session stream).
     void set_profiling(bool on) { profiling_ = on; }
     void stage_totals(double* ms, int64_t* calls);   // syncs pending events, accumulates, returns totals
@@ -97,6 +107,7 @@ class Session {
     int open_stage_ = -1;
     int device_;
     cudaStream_t stream_ = nullptr;
+    void* cublas_ = nullptr;
     std::unique_ptr<DeviceModel> dm_;
 };
 

@@ -104,6 +104,26 @@ int cg_assemble_device(cg_session* s, const cg_dframes* d, int precision, void* 
 #define CG_NOALLOC_SCRATCH_BYTES (32u << 20)
 int cg_assemble_device_noalloc(cg_session* s, const cg_dframes* d, int precision, void* A_device, int64_t lda);
 
+/* Normal equations of the fit (replaces the SVD of chimes_lsq.py, src/chimes_lsq.py:169-214).
+ * cg_gram accumulates G += A^T A (row-major ncols x ncols FP64, upper triangle until
+ * cg_gram_finish mirrors it) and h += A^T b for a device A block (row-major, lda,
+ * a_precision CG_FP64 or CG_FP32).  mode CG_GRAM_FP64: FP64 library SYRK (FP64 A);
+ * CG_GRAM_BF16X3: A split into BF16 hi/lo planes, G from hi.hi + hi.lo + lo.hi on the
+ * tensor cores with FP32 accumulation.  The caller zeroes G and h before the first
+ * block.  All pointers are device pointers. */
+enum { CG_GRAM_FP64 = 0, CG_GRAM_BF16X3 = 1 };
+int cg_gram(cg_session* s, int a_precision, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b,
+            int mode, double* G, double* h);
+int cg_gram_finish(cg_session* s, double* G, int ncols);
+
+/* x = (G + ridge I)^-1 h by FP64 Cholesky (the ridge grows tenfold, at most 8 times,
+ * if G + ridge I is not positive definite), then `iters` iterations of conjugate
+ * gradients on the exact normal equations A^T A x = A^T b with FP64 products through A,
+ * preconditioned by that Cholesky factor (A: FP64 device matrix; may be NULL if
+ * iters == 0).  info (host, 3 doubles): ||b - A x||, ||A^T (b - A x)||, ridge used. */
+int cg_solve(cg_session* s, const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda,
+             int64_t nrows, const double* b, int iters, double* x, double* info);
+
 /* Work counters of the last assembly: accepted 2-body pairs, triplets, quadruplets,
  * and (cluster, allowed-power) evaluations of the 3- and 4-body terms. */
 int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads,

@@ -1,0 +1,113 @@
+"""GPU checks of the normal equations (G = A^T A, h = A^T b) and the FP64 solve.
+
+Tolerances: the FP64 library Gram matches numpy's A^T A to 1e-12 relative to
+sqrt(G_ii G_jj); the split-BF16 tensor-core Gram (hi.hi + hi.lo + lo.hi, FP32
+accumulation) to 1e-4 of sqrt(G_ii G_jj) (its products carry ~2^-16 relative error).
+The FP64 solve matches numpy's FP64 solve of the same ridge-regularised system
+within the system's conditioning; preconditioned CG with FP64 products through A
+brings the mixed form (tensor-core Gram) to the same least-squares fit as the FP64
+form (measured agreements are printed).
+"""
+import ctypes
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def system(cg, tmp_path_factory):
+    torch = pytest.importorskip("torch")
+    synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+    fm = synth.make_workload("water-3b", str(tmp_path_factory.mktemp("gram")), nframes=8, seed=404)
+    model = cg.Model(fm)
+    frames = cg.Frames.read(model)
+    sess = cg.Session(model, 0)
+    A = sess.assemble(frames, cg.CG_FP64)
+    b = frames.labels()
+    dA = torch.from_numpy(A).cuda()
+    db = torch.from_numpy(b).cuda()
+    return sess, A, b, dA, db, torch
+
+
+def _gram(cg, sess, dA, db, mode, torch, prec=0):
+    n = dA.shape[1]
+    G = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    h = torch.zeros(n, dtype=torch.float64, device="cuda")
+    src = dA if prec == 0 else dA.float()
+    lib = cg.lib()
+    rc = lib.cg_gram(sess._h, prec, ctypes.c_void_p(src.data_ptr()), src.shape[1], src.shape[0], n,
+                     ctypes.c_void_p(db.data_ptr()), mode, ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(h.data_ptr()))
+    assert rc == 0, lib.cg_last_error().decode()
+    assert lib.cg_gram_finish(sess._h, ctypes.c_void_p(G.data_ptr()), n) == 0
+    torch.cuda.synchronize()
+    return G, h
+
+
+def test_gram_fp64_and_tensor_core(cg, system):
+    sess, A, b, dA, db, torch = system
+    Gref = A.T @ A
+    href = A.T @ b
+    d = np.sqrt(np.maximum(np.diag(Gref), 1e-300))
+    scale = np.outer(d, d)
+    G64, h64 = _gram(cg, sess, dA, db, 0, torch)
+    assert np.all(np.abs(G64.cpu().numpy() - Gref) <= 1e-12 * scale + 1e-300)
+    assert np.allclose(h64.cpu().numpy(), href, rtol=1e-10, atol=1e-10 * np.abs(href).max())
+    Gtc, htc = _gram(cg, sess, dA, db, 1, torch)
+    err = np.abs(Gtc.cpu().numpy() - Gref)
+    assert np.all(err <= 1e-4 * scale + 1e-300), (err / (scale + 1e-300)).max()
+    assert np.array_equal(htc.cpu().numpy(), h64.cpu().numpy())
+    # FP32 A input gives the same tensor-core Gram (the split starts from FP32 values)
+    Gtc32, _ = _gram(cg, sess, dA, db, 1, torch, prec=1)
+    assert np.all(np.abs(Gtc32.cpu().numpy() - Gref) <= 1e-4 * scale + 1e-300)
+
+
+def _solve(cg, sess, G, h, dA, db, ridge, iters, torch):
+    n = G.shape[0]
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    info = (ctypes.c_double * 3)()
+    lib = cg.lib()
+    rc = lib.cg_solve(sess._h, ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(h.data_ptr()), n, ctypes.c_double(ridge),
+                      ctypes.c_void_p(dA.data_ptr()), dA.shape[1], dA.shape[0], ctypes.c_void_p(db.data_ptr()), iters,
+                      ctypes.c_void_p(x.data_ptr()), info)
+    assert rc == 0, lib.cg_last_error().decode()
+    torch.cuda.synchronize()
+    return x.cpu().numpy(), info[0], info[1]
+
+
+def test_solve_matches_numpy_and_mixed_refines(cg, system):
+    """FP64 Cholesky solve vs numpy on the same ridge system, and the mixed form
+    (tensor-core Gram + FP64 Cholesky + FP64-residual refinement) vs the FP64 form.
+    Agreement is bounded by the conditioning of G, so the checks are on the
+    normal-equation residuals and on relative differences measured against numpy's own
+    FP64 solve of the same system."""
+    sess, A, b, dA, db, torch = system
+    G64, h64 = _gram(cg, sess, dA, db, 0, torch)
+    Gn = A.T @ A
+    hn = A.T @ b
+    ridge = 1e-9 * np.abs(np.diag(Gn)).max()
+    Gr = Gn + ridge * np.eye(Gn.shape[0])
+    xref = np.linalg.solve(Gr, hn)
+    x64, _, _ = _solve(cg, sess, G64, h64, dA, db, ridge, 0, torch)
+    res_ref = np.linalg.norm(Gr @ xref - hn) / np.linalg.norm(hn)
+    res_64 = np.linalg.norm(Gr @ x64 - hn) / np.linalg.norm(hn)
+    assert res_64 <= max(10 * res_ref, 1e-10)
+    assert np.linalg.norm(x64 - xref) <= 1e-6 * np.linalg.norm(xref)
+    # refinement toward the least-squares solution
+    Gtc, htc = _gram(cg, sess, dA, db, 1, torch)
+    ridge_m = 1e-5 * np.abs(np.diag(Gn)).max()   # above the tensor-core Gram's error
+    x0, _, g0 = _solve(cg, sess, Gtc, htc, dA, db, ridge_m, 0, torch)
+    xm, rn_m, gn_m = _solve(cg, sess, Gtc, htc, dA, db, ridge_m, 60, torch)
+    x64r, rn_r, gn_r = _solve(cg, sess, G64, h64, dA, db, ridge, 60, torch)
+    rel_m = np.linalg.norm(xm - x64r) / np.linalg.norm(x64r)
+    rel_0 = np.linalg.norm(x0 - x64r) / np.linalg.norm(x64r)
+    print(f"\nmixed vs FP64 coefficients: before CG {rel_0:.3e}, after {rel_m:.3e}; "
+          f"||A^T r||/||A^T b||: mixed {gn_m / np.linalg.norm(hn):.3e}, FP64 {gn_r / np.linalg.norm(hn):.3e}; "
+          f"||r||: mixed {rn_m:.9e}, FP64 {rn_r:.9e}", flush=True)
+    assert rel_m < rel_0
+    g0_np = np.linalg.norm(A.T @ (b - A @ x0))
+    assert gn_m < g0_np
+    # the fits are equally good: residual norms agree to 1e-6 relative
+    assert abs(rn_m - rn_r) <= 1e-6 * rn_r
