@@ -62,6 +62,8 @@ def lib():
         "cg_model_sizes": (ctypes.c_int, [vp, ip, ip]),
         "cg_model_header_text": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "cg_model_map_text": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "cg_model_params_text": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t,
+                                                ctypes.POINTER(ctypes.c_size_t)]),
         "cg_frames_read": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int, pp]),
         "cg_frames_create": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, pp]),
         "cg_frames_free": (None, [vp]),
@@ -140,6 +142,17 @@ class Model:
 
     def ff_groups_map(self):
         return self._text(lib().cg_model_map_text)
+
+    def params_txt(self, x, preamble=""):
+        """params.txt text for the fitted coefficients x (one per A column)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        pre = preamble.encode()
+        fn = lib().cg_model_params_text
+        need = ctypes.c_size_t()
+        _check(fn(self._h, _ptr(x), x.size, pre, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value + 1)
+        _check(fn(self._h, _ptr(x), x.size, pre, buf, need.value + 1, ctypes.byref(need)))
+        return buf.raw[: need.value].decode()
 
 
 class Frames:

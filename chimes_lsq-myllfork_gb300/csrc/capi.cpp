@@ -107,6 +107,14 @@ int cg_model_map_text(const cg_model* h, char* buf, size_t cap, size_t* needed) 
     });
 }
 
+int cg_model_params_text(const cg_model* h, const double* x, int nx, const char* preamble, char* buf, size_t cap,
+                         size_t* needed) {
+    return guarded([&] {
+        need(h && x, "model/x");
+        copy_text(cg::params_txt_text(h->m, x, nx, preamble ? preamble : ""), buf, cap, needed);
+    });
+}
+
 int cg_frames_read(const cg_model* h, const char* path, int nframes, cg_frames** out) {
     return guarded([&] {
         need(h && out, "model/out");

@@ -6,7 +6,9 @@
 #include "model.h"
 
 #include <algorithm>
+#include <cctype>
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <fstream>
 #include <iomanip>
@@ -740,6 +742,147 @@ std::string ff_groups_map_text(const Model& m) {   // print_map_file src/chimes_
         o << std::endl << "QUADMAPS: " << m.quads.map.size() << std::endl;
         for (const auto& kv : m.quads.map) o << kv.second << " " << kv.first << std::endl;
     }
+    return o.str();
+}
+
+static std::string fmt(const char* f, ...) {
+    char buf[256];
+    va_list ap;
+    va_start(ap, f);
+    vsnprintf(buf, sizeof(buf), f, ap);
+    va_end(ap);
+    return buf;
+}
+
+static std::vector<std::string> split_lines(const std::string& t) {
+    std::vector<std::string> out;
+    std::stringstream ss(t);
+    std::string l;
+    while (std::getline(ss, l)) out.push_back(l);
+    return out;
+}
+
+static std::vector<std::string> ws_split(const std::string& l) {   // python str.split()
+    std::vector<std::string> t;
+    std::stringstream ss(l);
+    std::string w;
+    while (ss >> w) t.push_back(w);
+    return t;
+}
+
+static std::string rstrip_ws(std::string l) {
+    while (!l.empty() && std::isspace((unsigned char)l.back())) l.pop_back();
+    return l;
+}
+
+// The layout is driven by the params.header text, token by token, the way the
+// solver script reads it back (src/chimes_lsq.py:316-672): header echo up to the
+// TRIPLETS / QUADRUPLETS count lines, one "%3d %21.13e" line per 2-body power,
+// the header's cluster power lines each followed by " %21.13e" of the coefficient
+// named by its param-index column, ff_groups.map, then the energy offsets.
+std::string params_txt_text(const Model& m, const double* x, int nx, const std::string& preamble) {
+    if (nx != m.tot_all) throw Error(1, "coefficient count does not match the model's columns");
+    std::ostringstream o;
+    o << preamble;
+    const std::vector<std::string> hf = split_lines(params_header_text(m));
+    auto tok = [&](size_t line) {
+        if (line >= hf.size()) throw Error(2, "params.header is shorter than its own counts");
+        return ws_split(hf[line]);
+    };
+    auto at = [](const std::vector<std::string>& t, size_t i) -> const std::string& {
+        if (i >= t.size()) throw Error(2, "params.header line has too few fields");
+        return t[i];
+    };
+    size_t trip_line = 0, quad_line = 0;
+    int ntrips = 0, nquads = 0;
+    for (size_t i = 0; i < hf.size(); ++i) {
+        o << hf[i] << "\n";
+        const auto t = ws_split(hf[i]);
+        bool done = false;
+        if (t.size() > 3 && t[2] == "TRIPLETS:") {
+            ntrips = std::stoi(t[3]);
+            trip_line = i;
+            for (size_t j = i; j < hf.size(); ++j) {
+                const auto u = ws_split(hf[j]);
+                if (u.size() > 3 && u[2] == "QUADRUPLETS:") {
+                    o << hf[j] << "\n";
+                    nquads = std::stoi(u[3]);
+                    quad_line = j;
+                    done = true;
+                    break;
+                }
+            }
+        }
+        if (done) break;
+    }
+    const std::string potential = at(tok(7), 1);
+    o << "\n" << "PAIR " << potential << " PARAMS \n\n";
+    const auto pt = tok(7);
+    const int snum = pt.size() >= 4 ? std::stoi(pt[2]) : 0;
+    const size_t types_line = 9;
+    const int ntypes = std::stoi(at(tok(types_line), 2));
+    const size_t pairs_line = types_line + 2 + ntypes + 2;
+    const int npairs = std::stoi(at(tok(pairs_line), 2));
+    int eff = 0;
+    for (int i = 0; i < npairs; ++i) {
+        const auto a = tok(pairs_line + 2 + i + 1);
+        o << "PAIRTYPE PARAMS: " << i << " " << at(a, 1) << " " << at(a, 2) << "\n\n";
+        for (int j = 0; j < snum; ++j) o << fmt("%3d %21.13e", j, x[eff * snum + j]) << "\n";
+        ++eff;
+        o << " \n";
+    }
+    // natoms 3: pair names in fields 1-3, counts in 4 / 6, power lines carry the param
+    // index in column 5 (index, 3 powers, equiv, param);
+    // natoms 4: pair names in fields 1-6, counts in 7 / 9, param index in column 8.
+    int counted3 = 0, counted4 = 0;
+    auto cluster_block = [&](size_t line0, int ncl, int natoms, int base) {
+        const bool trip = natoms == 3;
+        const size_t npn = trip ? 3 : 6;
+        o << (trip ? "TRIPLET " : "QUADRUPLET ") << potential << " PARAMS \n\n";
+        int add = 0, par = 0;
+        for (int t = 0; t < ncl; ++t) {
+            o << (trip ? "TRIPLETTYPE PARAMS:" : "QUADRUPLETYPE PARAMS: ") << "\n";
+            o << "  " << rstrip_ws(hf.at(line0 + 2 + add)) << "\n";
+            const auto p1 = tok(line0 + 3 + add);
+            o << "   PAIRS:";
+            for (size_t k = 1; k <= npn; ++k) o << " " << at(p1, k);
+            if (at(p1, npn + 1) == "EXCLUDED:") {
+                o << (trip ? " EXCLUDED:" : " EXCLUDED: ") << "\n";
+                add += 1;
+            } else {
+                const int uniq = std::stoi(at(p1, npn + 1));
+                const int totl = std::stoi(at(p1, npn + 3));
+                o << " UNIQUE: " << at(p1, npn + 1) << " TOTAL: " << at(p1, npn + 3) << "\n";
+                o << "     index  |  powers  |  equiv index  |  param index  |       parameter       \n";
+                o << "   ----------------------------------------------------------------------------\n";
+                add += 3;
+                for (int p = 0; p < totl; ++p) {
+                    add += 1;
+                    const size_t ln = line0 + 2 + add;
+                    const int pidx = std::stoi(at(tok(ln), npn + 2));
+                    const int col = base + par + pidx;
+                    if (col < 0 || col >= nx) throw Error(2, "params.header names a coefficient out of range");
+                    o << hf[ln] << fmt(" %21.13e", x[col]) << "\n";
+                }
+                par += uniq;
+                (trip ? counted3 : counted4) += uniq;
+            }
+            o << "\n";
+            add += 2;
+        }
+    };
+    if (ntrips > 0) cluster_block(trip_line, ntrips, 3, eff * snum);
+    if (nquads > 0) cluster_block(quad_line, nquads, 4, eff * snum + counted3);
+    o << "\n";
+    for (const auto& l : split_lines(ff_groups_map_text(m))) o << l << "\n";
+    o << "\n";
+    const int total = eff * snum + counted3 + counted4;
+    if (total != nx && nx != total + ntypes) throw Error(2, "error in counting parameters");
+    if (nx == total + ntypes) {
+        o << "NO ENERGY OFFSETS:  " << ntypes << "\n";
+        for (int i = 0; i < ntypes; ++i) o << fmt("ENERGY OFFSET %d %21.13e", i + 1, x[total + i]) << "\n";
+    }
+    o << "ENDFILE\n";
     return o.str();
 }
 

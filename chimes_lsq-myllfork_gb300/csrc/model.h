@@ -116,6 +116,12 @@ int make_id_int(const int* types, int n);
 std::string params_header_text(const Model& m);
 std::string ff_groups_map_text(const Model& m);
 
+// params.txt (the force field file written by chimes_lsq.py, src/chimes_lsq.py:284-675)
+// for coefficients x (tot_all values): `preamble` is the "!"-comment block that the
+// solver prints first; the rest follows params.header, the coefficient blocks and
+// ff_groups.map exactly.
+std::string params_txt_text(const Model& m, const double* x, int nx, const std::string& preamble);
+
 // ---------------------------------------------------------------- frames
 
 struct Box {

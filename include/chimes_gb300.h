@@ -46,6 +46,14 @@ int cg_model_sizes(const cg_model* m, int* nframes, int* natmtyp);
 int cg_model_header_text(const cg_model* m, char* buf, size_t cap, size_t* needed);
 int cg_model_map_text(const cg_model* m, char* buf, size_t cap, size_t* needed);
 
+/* Text of params.txt, the fitted force-field file, for coefficients x[0..nx) (nx =
+ * the model's column count): `preamble` (the solver's "!" comment block, may be
+ * NULL), the params.header echo, the 2-body / cluster coefficient blocks, the
+ * ff_groups.map text and the energy offsets, then ENDFILE.  Same buffer rules as
+ * cg_model_header_text.  Replaces the output half of src/chimes_lsq.py:284-672. */
+int cg_model_params_text(const cg_model* m, const double* x, int nx, const char* preamble, char* buf, size_t cap,
+                         size_t* needed);
+
 /* Read nframes frames of an .xyzf trajectory (path NULL: the model's TRJFILE,
  * nframes <= 0: NFRAMES).  Replaces FRAME::READ_XYZF (src/ClassDefs.C:2411-2683). */
 int cg_frames_read(const cg_model* m, const char* xyzf_path, int nframes, cg_frames** out);

@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import FIXTURES, REFERENCE, ROOT, fixture_dir
+from conftest import FIXTURES, GOLDEN, REFERENCE, ROOT, fixture_dir
 
 HEADER = os.path.join(ROOT, "include", "chimes_gb300.h")
 
@@ -128,3 +128,33 @@ def test_oracle_matches_reference_suite_tail(oracle, tmp_path, case):
     assert (np.abs(tail - G) / scale).max() < 1e-10
     gb = np.loadtxt(os.path.join(gold, "b.txt"))
     assert np.allclose(b, gb, rtol=1e-12, atol=1e-12)
+
+
+PARAMS_CASES = ["fitstrs", "fitstrs3b", "h2o-invr", "nonorth2", "one-file-three-trajs", "special3b", "special4b",
+                "stress-and-ener-2b1", "stress-and-ener-2b2", "stress-and-ener-2b3", "stress-and-ener-4b",
+                "stress-and-ener-4b2", "test_4atoms", "test_4atoms.2"]
+
+
+@needs_ref
+@pytest.mark.parametrize("case", PARAMS_CASES)
+def test_params_txt_matches_reference_suite(cg, case):
+    """params.txt from the reference's fitted coefficients (test_suite_params.txt) and
+    its "!" solver preamble is byte-identical to the reference's params.txt."""
+    d = os.path.join(REF_LSQ, case, "correct_output")
+    m = cg.Model(os.path.join(REF_LSQ, case, "fm_setup.in"))
+    gold = open(os.path.join(d, "params.txt")).read()
+    lines = gold.splitlines(True)
+    k = 0
+    while k < len(lines) and lines[k].startswith("!"):
+        k += 1
+    x = np.array([float(ln.split()[1]) for ln in open(os.path.join(d, "test_suite_params.txt")) if ln.strip()])
+    assert x.size == m.ncols
+    assert m.params_txt(x, "".join(lines[:k])) == gold
+
+
+def test_params_txt_rejects_wrong_count(cg):
+    m = cg.Model(os.path.join(GOLDEN, "water3b", "fm_setup.in"))
+    with pytest.raises(cg.ChimesError):
+        m.params_txt(np.zeros(m.ncols + 1))
+    t = m.params_txt(np.arange(m.ncols, dtype=float))
+    assert t.startswith(m.params_header().splitlines()[0]) and t.endswith("ENDFILE\n")
