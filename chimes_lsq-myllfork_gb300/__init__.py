@@ -24,6 +24,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libchimes_gb300.so")
 
 CG_FP64 = 0
 CG_FP32 = 1
+MD_ENERGY_OFFSETS = 1
+MD_NSCALAR = 11   # energy, PRESSURE_XYZ/3V, virial tensor/V (3x3 row-major)
 
 _lib = None
 
@@ -69,6 +71,8 @@ def lib():
         "cg_frames_free": (None, [vp]),
         "cg_frames_rows": (ctypes.c_int, [vp, i64p, i64p]),
         "cg_frames_labels": (ctypes.c_int, [vp, dp]),
+        "cg_frames_count": (ctypes.c_int, [vp, ip]),
+        "cg_frames_independent": (ctypes.c_int, [vp]),
         "cg_session_create": (ctypes.c_int, [vp, ctypes.c_int, pp]),
         "cg_session_free": (None, [vp]),
         "cg_session_stream": (ctypes.c_void_p, [vp]),
@@ -83,6 +87,13 @@ def lib():
         "cg_session_stage_times": (ctypes.c_int, [vp, vp, vp]),
         "cg_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
         "cg_last_error": (ctypes.c_char_p, []),
+        "cg_md_setup": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double]),
+        "cg_md_force": (ctypes.c_int, [vp, vp, dp, dp]),
+        "cg_md_force_device": (ctypes.c_int, [vp, vp, vp, vp]),
+        "cg_md_nve": (ctypes.c_int, [vp, vp, dp, ctypes.c_double, ctypes.c_int, vp, vp, vp, vp]),
+        "cg_dframes_positions": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_void_p), i64p]),
+        "cg_md_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -191,6 +202,11 @@ class Frames:
             _lib.cg_frames_free(self._h)
             self._h = None
 
+    def independent(self):
+        """Each frame decides the small-cell convention alone (MD systems)."""
+        _check(lib().cg_frames_independent(self._h))
+        return self
+
     def rows(self):
         r, a = ctypes.c_int64(), ctypes.c_int64()
         _check(lib().cg_frames_rows(self._h, ctypes.byref(r), ctypes.byref(a)))
@@ -199,6 +215,16 @@ class Frames:
     @property
     def nrows(self):
         return self.rows()[0]
+
+    @property
+    def natoms_total(self):
+        return self.rows()[1]
+
+    @property
+    def nframes(self):
+        n = ctypes.c_int()
+        _check(lib().cg_frames_count(self._h, ctypes.byref(n)))
+        return n.value
 
     def labels(self):
         b = np.empty(self.nrows, dtype=np.float64)
@@ -217,6 +243,12 @@ class DeviceFrames:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.cg_dframes_free(self._h)
             self._h = None
+
+    def positions_ptr(self):
+        """(device pointer to the 3*natoms positions, natoms)."""
+        p, n = ctypes.c_void_p(), ctypes.c_int64()
+        _check(lib().cg_dframes_positions(self._h, ctypes.byref(p), ctypes.byref(n)))
+        return p.value, n.value
 
 
 class Session:
@@ -282,6 +314,37 @@ class Session:
         device array inside the library; see include/chimes_gb300.h)."""
         _check(lib().cg_assemble_device_noalloc(self._h, dframes._h, int(precision),
                                                 ctypes.c_void_p(int(a_device_ptr)), int(lda)))
+
+    # ---------------------------------------------------------------- MD force
+    def md_setup(self, x, precision=CG_FP64, energy_offsets=False, penalty_dist=0.01, penalty_scale=1.0e4):
+        """Coefficients x (one per A column) for the MD force (cg_md_setup)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        _check(lib().cg_md_setup(self._h, _ptr(x), x.size, int(precision), MD_ENERGY_OFFSETS if energy_offsets else 0,
+                                 float(penalty_dist), float(penalty_scale)))
+
+    def md_force(self, frames):
+        """(forces [natoms_total, 3], scalars [nframes, 11]) of host frames."""
+        nat = frames.natoms_total
+        F = np.zeros((nat, 3), dtype=np.float64)
+        S = np.zeros((frames.nframes, MD_NSCALAR), dtype=np.float64)
+        _check(lib().cg_md_force(self._h, frames._h, _ptr(F), _ptr(S)))
+        return F, S
+
+    def md_force_device(self, dframes, forces_ptr, scalars_ptr):
+        _check(lib().cg_md_force_device(self._h, dframes._h, ctypes.c_void_p(int(forces_ptr)),
+                                        ctypes.c_void_p(int(scalars_ptr))))
+
+    def md_nve(self, dframes, masses, dt_fs, nsteps, v_ptr, forces_ptr, scalars_ptr=0, ke_ptr=0):
+        """nsteps NVE steps of uploaded frames (device buffers, see cg_md_nve)."""
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        _check(lib().cg_md_nve(self._h, dframes._h, _ptr(m), float(dt_fs), int(nsteps), ctypes.c_void_p(int(v_ptr)),
+                               ctypes.c_void_p(int(forces_ptr)), ctypes.c_void_p(int(scalars_ptr) or None),
+                               ctypes.c_void_p(int(ke_ptr) or None)))
+
+    def md_last_counts(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        _check(lib().cg_md_last_counts(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(["pairs", "triplets", "quads", "launches"], [x.value for x in v]))
 
     def last_counts(self):
         v = [ctypes.c_int64() for _ in range(5)]

@@ -20,6 +20,7 @@ struct cg_frames {
 struct cg_session {
     std::unique_ptr<cg::Session> s;
     cg::AssembleStats last;
+    cg::MdCounts md_last;
 };
 struct cg_dframes {
     std::unique_ptr<cg::DeviceFrames> d;
@@ -181,6 +182,20 @@ int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms) {
     });
 }
 
+int cg_frames_independent(cg_frames* fr) {
+    return guarded([&] {
+        need(fr, "frames");
+        cg::make_independent(fr->fb);
+    });
+}
+
+int cg_frames_count(const cg_frames* fr, int* nframes) {
+    return guarded([&] {
+        need(fr && nframes, "frames/nframes");
+        *nframes = fr->fb.nframes;
+    });
+}
+
 int cg_frames_labels(const cg_frames* fr, double* b) {
     return guarded([&] {
         need(fr && b, "frames/b");
@@ -315,5 +330,76 @@ int cg_session_stage_times(cg_session* s, double* ms, int64_t* calls) {
 }
 
 const char* cg_stage_name(int stage) { return cg::stage_name(stage); }
+
+// ------------------------------------------------------------------ MD force
+int cg_md_setup(cg_session* s, const double* x, int nx, int precision, int flags, double penalty_dist,
+                double penalty_scale) {
+    return guarded([&] {
+        need(s && x, "session/x");
+        need(precision == CG_FP64 || precision == CG_FP32, "precision");
+        need((flags & ~CG_MD_ENERGY_OFFSETS) == 0, "flags");
+        s->s->md_setup(x, nx, precision, (flags & CG_MD_ENERGY_OFFSETS) != 0, penalty_dist, penalty_scale);
+    });
+}
+
+int cg_md_force_device(cg_session* s, const cg_dframes* d, double* forces, double* scalars) {
+    return guarded([&] {
+        need(s && d && forces && scalars, "session/frames/forces/scalars");
+        s->s->md_force(*d->d, forces, scalars, &s->md_last);
+    });
+}
+
+int cg_md_force(cg_session* s, const cg_frames* fr, double* forces, double* scalars) {
+    return guarded([&] {
+        need(s && fr && forces && scalars, "session/frames/forces/scalars");
+        cudaStream_t st = s->s->stream();
+        std::unique_ptr<cg::DeviceFrames> d = s->s->upload(fr->fb);
+        const size_t nf = (size_t)fr->fb.natoms_total * 3, ns = (size_t)fr->fb.nframes * cgd::MD_NSCALAR;
+        double* dF = nullptr;
+        cg::cuda_check(cudaMallocAsync((void**)&dF, std::max<size_t>(1, nf + ns) * sizeof(double), st),
+                       "cudaMallocAsync(forces)");
+        try {
+            s->s->md_force(*d, dF, dF + nf, &s->md_last);
+            cg::cuda_check(cudaMemcpyAsync(forces, dF, nf * sizeof(double), cudaMemcpyDeviceToHost, st),
+                           "cudaMemcpyAsync(forces)");
+            cg::cuda_check(cudaMemcpyAsync(scalars, dF + nf, ns * sizeof(double), cudaMemcpyDeviceToHost, st),
+                           "cudaMemcpyAsync(scalars)");
+            cg::cuda_check(cudaFreeAsync(dF, st), "cudaFreeAsync(forces)");
+            cg::cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        } catch (...) {
+            cudaFreeAsync(dF, st);
+            cudaStreamSynchronize(st);
+            throw;
+        }
+    });
+}
+
+int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, double* velocities,
+              double* forces, double* scalars_steps, double* ke_steps) {
+    return guarded([&] {
+        need(s && d && mass && velocities && forces, "session/frames/mass/velocities/forces");
+        need(dt_fs > 0.0 && nsteps >= 0, "dt/nsteps");
+        const double Tfs = 48.888;   // internal time unit in fs (src/functions.h:44)
+        s->s->md_nve(*d->d, mass, dt_fs / Tfs, nsteps, velocities, forces, scalars_steps, ke_steps);
+    });
+}
+
+int cg_dframes_positions(const cg_dframes* d, double** xyz, int64_t* natoms) {
+    return guarded([&] {
+        need(d && xyz && natoms, "frames/xyz/natoms");
+        *xyz = d->d->xyz;
+        *natoms = d->d->natoms_total;
+    });
+}
+
+int cg_md_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads, int64_t* launches) {
+    return guarded([&] {
+        need(s, "session");
+        if (pairs) *pairs = s->md_last.pairs2;
+        if (triplets) *triplets = s->md_last.triplets;
+        if (quads) *quads = s->md_last.quads;
+        if (launches) *launches = s->md_last.launches;
+    });
+}
 
 }  // extern "C"

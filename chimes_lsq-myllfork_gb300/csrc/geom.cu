@@ -109,7 +109,7 @@ __global__ void k_neigh(ModelDev M, FramesDev F, NeighDev NB, int fill) {
                 r = dist_exact(B.h, si, F.scaled + 3 * (gbase + g), rab);
                 pt = M.int_pair_map[ti * M.natmtyp + typ[g % N]];
                 const PairDev P = M.pairs[pt];
-                in2 = M.order2 > 0 && r > P.smin && r < P.smax;
+                in2 = M.order2 > 0 && r < P.smax && (NB.md || r > P.smin);
                 in3 = M.order3 > 0 && r < M.maxcut3;
                 in4 = M.order4 > 0 && r < M.maxcut4;
             }

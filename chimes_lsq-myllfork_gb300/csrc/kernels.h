@@ -14,6 +14,9 @@ struct NeighDev {
     // 3-body / 4-body candidate lists: r < maximum cluster cut-off
     int* g3; double* r3;
     int* g4; double* r4;
+    // 0: the fit's 2-body filter s_min < r < s_max; 1: the MD force's r < s_max
+    // (Cheby::Force_all src/Cheby.C:1834 also evaluates r <= s_min, smoothed)
+    int md;
 };
 
 struct ClusterSet {                               // triplets or quadruplets of a batch
@@ -47,5 +50,9 @@ void launch_neigh(const ModelDev& M, const FramesDev& F, const NeighDev& NB, int
 void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const NeighDev& NB, const ClusterSet& CS,
                      int fill, cudaStream_t st);
 void launch_bucket(int nframes, const FramesDev& F, const BucketSpec& S, const Buckets& out, cudaStream_t st);
+// Prefix sums and per-frame offsets (session.cu).
+void launch_scan_counts(const int* cnt, int n, int64_t* ofs, cudaStream_t st);
+void launch_gather_frame_ofs(const int64_t* ofs, const int64_t* atom_ofs, int nframes, int64_t* out, cudaStream_t st);
+void launch_key_frame_ofs(const int64_t* atom_ofs, int nframes, int per_type, int64_t* out, cudaStream_t st);
 
 }  // namespace cgd

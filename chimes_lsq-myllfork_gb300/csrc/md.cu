@@ -1,0 +1,571 @@
+// MD force kernels: 2-body pairs, dense-tensor triplet / quadruplet contraction,
+// the per-frame finish (ZCalc's /V scaling and energy offsets) and the
+// velocity-Verlet updates.
+//
+// Reference arithmetic per cluster (Cheby::Force_3B / Force_4B, src/Cheby.C:2024-2675):
+// for every allowed power tuple p with coefficient c_p,
+//   E   += perm c_p prod_e f_e T_e[p_e]
+//   F_e  = perm c_p (f_e T'_e + f'_e T_e)[p_e] prod_{e' != e} f_e' T_e'[p_e']
+// and F_e / r_e times the edge vector is added to the first member and taken
+// from the second; the virial collects -F_e r_e and -F_e r_a r_b / r_e.
+//
+// GB300 formulation: the coefficients of a cluster type are one dense tensor
+// C[p_0..p_{n-1}] over the canonical pair slots (zero where a tuple is not
+// allowed).  With u_s[k] = f_s T_k(r_s), one depth-first pass over C gives
+//   E = sum C prod_s u_s[p_s]   and   G_s[k] = dE / du_s[k]
+// (partial sums flow up, prefix products flow down: two FMAs per entry), and
+// F_e = perm sum_k G_s[k] (f T' + f' T)_s[k] for the edge e in slot s.  A
+// 4-body type of order 4 costs ~11k FMAs per quadruplet this way, against ~80k for
+// the power-tuple loop.  One thread owns one cluster; a block shares one
+// (frame, cluster type) bucket, so C sits in shared memory and every read of it
+// is a broadcast.
+#include <cstdio>
+
+#include "basis.cuh"
+#include "md.h"
+
+namespace cgd {
+
+constexpr int MDC_THREADS = 128;
+
+__device__ __forceinline__ int frame_of_atom(const FramesDev& F, int64_t a) {
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (F.atom_ofs[mid] <= a) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum 8 per-thread values over the block and add them to the frame's scalars:
+// v = [E, P, Wxx, Wxy, Wxz, Wyy, Wyz, Wzz].
+__device__ void block_scalars_add(double* v, double* So, int f) {
+    __shared__ double red[8][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        double s = warp_sum(v[k]);
+        if (lane == 0) red[k][w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double s = 0.0;
+        for (int i = 0; i < nw; ++i) s += red[threadIdx.x][i];
+        // tensor slots: xx=2 xy=3 xz=4 yx=5 yy=6 yz=7 zx=8 zy=9 zz=10 (symmetric)
+        const int k = threadIdx.x;
+        double* o = So + (size_t)f * MD_NSCALAR;
+        if (s != 0.0) {
+            if (k == 0) atomicAdd(o + 0, s);
+            else if (k == 1) atomicAdd(o + 1, s);
+            else if (k == 2) atomicAdd(o + 2, s);
+            else if (k == 3) { atomicAdd(o + 3, s); atomicAdd(o + 5, s); }
+            else if (k == 4) { atomicAdd(o + 4, s); atomicAdd(o + 8, s); }
+            else if (k == 5) atomicAdd(o + 6, s);
+            else if (k == 6) { atomicAdd(o + 7, s); atomicAdd(o + 9, s); }
+            else atomicAdd(o + 10, s);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ 2-body
+struct Dot2 {
+    const double* c;
+    double e = 0.0, g = 0.0;
+    __device__ void operator()(int k, double gk, double hk) {
+        e = fma(c[k], gk, e);
+        g = fma(c[k], hk, g);
+    }
+};
+
+// One warp per real atom over its 2-body list (pairs i <= PARENT[g] with r < s_max;
+// Cheby::Force_all src/Cheby.C:1812-1968).
+__global__ void __launch_bounds__(256) k_md2(ModelDev M, MdDev D, FramesDev F, NeighDev NB, double* Fo, double* So) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= NB.n_real) return;
+    const int f = frame_of_atom(F, warp);
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    const BoxDev& B = F.box[f];
+    const int64_t o = NB.ofs2[warp];
+    const int n = NB.cnt2[warp];
+    const int ord = M.order2;
+    double fi[3] = {0.0, 0.0, 0.0}, v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int t = lane; t < n; t += 32) {
+        const int64_t q = o + t;
+        const int g = NB.g2[q], pt = NB.pt2[q];
+        const double r = NB.r2[q];
+        const double R[3] = {NB.rab2[3 * q], NB.rab2[3 * q + 1], NB.rab2[3 * q + 2]};
+        const PairDev& P = M.pairs[pt];
+        double fc, fd;
+        fcut_eval(M, r, P.smax, fc, fd);
+        Dot2 acc{D.c2 + (size_t)pt * ord};
+        basis_visit(M, P.lambda, P.xavg, P.xdiff, P.smin, r, fc, fd, 1, ord, acc);
+        double es = B.perm2 * acc.e, gs = B.perm2 * acc.g;
+        if (r - D.pen_dist < P.smin) {   // cubic penalty below s_min + d (src/Cheby.C:1900-1968)
+            const double rp = P.smin + D.pen_dist - r;
+            if (rp > 0.0) {
+                gs += -3.0 * rp * rp * D.pen_scale;
+                es += rp * rp * rp * D.pen_scale;
+            }
+        }
+        const double wv = gs / r;
+        double* fo = Fo + 3 * (aofs + g % N);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            fi[c] = fma(wv, R[c], fi[c]);
+            atomicAdd(fo + c, -wv * R[c]);
+        }
+        v[0] += es;
+        v[1] -= gs * r;
+        v[2] -= wv * R[0] * R[0]; v[3] -= wv * R[0] * R[1]; v[4] -= wv * R[0] * R[2];
+        v[5] -= wv * R[1] * R[1]; v[6] -= wv * R[1] * R[2]; v[7] -= wv * R[2] * R[2];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fi[c] = warp_sum(fi[c]);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = warp_sum(v[k]);
+    if (lane == 0) {
+        const int i = warp - (int)aofs;
+        double* fo = Fo + 3 * (aofs + i);
+        if (n > 0) {
+            for (int c = 0; c < 3; ++c) atomicAdd(fo + c, fi[c]);
+            double* so = So + (size_t)f * MD_NSCALAR;
+            atomicAdd(so + 0, v[0]); atomicAdd(so + 1, v[1]);
+            atomicAdd(so + 2, v[2]); atomicAdd(so + 3, v[3]); atomicAdd(so + 4, v[4]);
+            atomicAdd(so + 5, v[3]); atomicAdd(so + 6, v[5]); atomicAdd(so + 7, v[6]);
+            atomicAdd(so + 8, v[4]); atomicAdd(so + 9, v[6]); atomicAdd(so + 10, v[7]);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ clusters
+template <int N_, int O>
+struct IPow { static constexpr int v = O * IPow<N_ - 1, O>::v; };
+template <int O>
+struct IPow<0, O> { static constexpr int v = 1; };
+
+template <int O, typename R>
+__device__ __forceinline__ R pick(const R (&a)[O], int i) {
+    R v = a[0];
+#pragma unroll
+    for (int k = 1; k < O; ++k) if (k == i) v = a[k];
+    return v;
+}
+template <int O, typename R>
+__device__ __forceinline__ void put(R (&a)[O], int i, R v) {
+#pragma unroll
+    for (int k = 0; k < O; ++k) if (k == i) a[k] = v;
+}
+
+// E and G_s[k] = dE/du_s[k] for one cluster: slot 0 is walked at run time, the
+// remaining slots fully unrolled (registers only).
+template <int O, typename R>
+__device__ __forceinline__ R contract3(const R* __restrict__ sC, const R (&u)[3][O], R (&G)[3][O]) {
+    R E = R(0);
+#pragma unroll 1
+    for (int a = 0; a < O; ++a) {
+        const R ua = pick<O>(u[0], a);
+        const R* Ca = sC + a * O * O;
+        R Sa = R(0);
+#pragma unroll
+        for (int b = 0; b < O; ++b) {
+            const R P = ua * u[1][b];
+            R Sab = R(0);
+#pragma unroll
+            for (int c = 0; c < O; ++c) {
+                const R cv = Ca[b * O + c];
+                Sab = fma(cv, u[2][c], Sab);
+                G[2][c] = fma(P, cv, G[2][c]);
+            }
+            G[1][b] = fma(ua, Sab, G[1][b]);
+            Sa = fma(u[1][b], Sab, Sa);
+        }
+        put<O>(G[0], a, Sa);
+        E = fma(ua, Sa, E);
+    }
+    return E;
+}
+
+template <int O, typename R>
+__device__ __forceinline__ R contract4(const R* __restrict__ sC, const R (&u)[6][O], R (&G)[6][O]) {
+    R E = R(0);
+#pragma unroll 1
+    for (int a = 0; a < O; ++a) {
+        const R ua = pick<O>(u[0], a);
+        const R* Ca = sC + a * IPow<5, O>::v;
+        R Sa = R(0);
+#pragma unroll
+        for (int b = 0; b < O; ++b) {
+            const R Pb = ua * u[1][b];
+            R Sb = R(0);
+#pragma unroll
+            for (int c = 0; c < O; ++c) {
+                const R Pc = Pb * u[2][c];
+                R Sc = R(0);
+#pragma unroll
+                for (int d = 0; d < O; ++d) {
+                    const R Pd = Pc * u[3][d];
+                    R Sd = R(0);
+#pragma unroll
+                    for (int e = 0; e < O; ++e) {
+                        const R Pe = Pd * u[4][e];
+                        const R* Cl = Ca + (((b * O + c) * O + d) * O + e) * O;
+                        R Se = R(0);
+#pragma unroll
+                        for (int g = 0; g < O; ++g) {
+                            const R cv = Cl[g];
+                            Se = fma(cv, u[5][g], Se);
+                            G[5][g] = fma(Pe, cv, G[5][g]);
+                        }
+                        G[4][e] = fma(Pd, Se, G[4][e]);
+                        Sd = fma(u[4][e], Se, Sd);
+                    }
+                    G[3][d] = fma(Pc, Sd, G[3][d]);
+                    Sc = fma(u[3][d], Sd, Sc);
+                }
+                G[2][c] = fma(Pb, Sc, G[2][c]);
+                Sb = fma(u[2][c], Sc, Sb);
+            }
+            G[1][b] = fma(ua, Sb, G[1][b]);
+            Sa = fma(u[1][b], Sb, Sa);
+        }
+        put<O>(G[0], a, Sa);
+        E = fma(ua, Sa, E);
+    }
+    return E;
+}
+
+__device__ __forceinline__ void edge_ab(int NBODY, int e, int& a, int& b) {
+    if (NBODY == 3) { a = e == 2 ? 1 : 0; b = e == 0 ? 1 : 2; }
+    else {
+        a = e < 3 ? 0 : (e < 5 ? 1 : 2);
+        b = e == 0 ? 1 : (e == 1 || e == 3) ? 2 : 3;
+    }
+}
+
+// Per-thread geometry of a cluster, slot by slot (canonical slot s <- actual edge e).
+struct SlotGeom {
+    double r, R[3];
+    int a, b, pt;
+};
+
+template <int NBODY>
+__device__ __forceinline__ void cluster_geom(const ModelDev& M, const FramesDev& F, int f, int4 mm, SlotGeom* sg) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    const int N = F.natoms[f];
+    const int64_t gb = F.ghost_ofs[f];
+    const int* typ = F.type + F.atom_ofs[f];
+    int id = 0, w = 1;
+#pragma unroll
+    for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
+    const int8_t* pm = (NBODY == 3 ? M.pidx3 : M.pidx4) + id * NP;
+    const BoxDev& B = F.box[f];
+#pragma unroll
+    for (int e = 0; e < NP; ++e) {
+        const int s = pm[e];
+        int a, b;
+        edge_ab(NBODY, e, a, b);
+        const int ga = member(mm, a), gbm = member(mm, b);
+        SlotGeom g;
+        g.a = a; g.b = b;
+        g.r = dist_exact(B.h, F.scaled + 3 * (gb + ga), F.scaled + 3 * (gb + gbm), g.R);
+        g.pt = M.int_pair_map[typ[ga % N] * M.natmtyp + typ[gbm % N]];
+        sg[s] = g;
+    }
+}
+
+template <int NBODY, int O, typename R>
+__global__ void __launch_bounds__(MDC_THREADS) k_mdc(ModelDev M, MdDev D, FramesDev F, ClusterSet CS, Buckets byt,
+                                                     const int64_t* kfo, double* Fo, double* So) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    constexpr int SZ = IPow<NP, O>::v;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sC = reinterpret_cast<R*>(smem_raw);
+    SlotGeom* sG = reinterpret_cast<SlotGeom*>(smem_raw + ((SZ * sizeof(R) + 15) & ~size_t(15)));
+    const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
+    const int f = blockIdx.x / ntypes;
+    const int T = blockIdx.x % ntypes;
+    const int64_t kb = kfo[f];
+    const int64_t t0 = byt.key_ofs[kb + T], t1 = byt.key_ofs[kb + T + 1];
+    const int64_t cb = t0 + (int64_t)blockIdx.y * blockDim.x;
+    if (cb >= t1) return;
+    const R* Cg = (NBODY == 3 ? (sizeof(R) == 8 ? (const R*)D.C3 : (const R*)D.C3f)
+                              : (sizeof(R) == 8 ? (const R*)D.C4 : (const R*)D.C4f)) + (size_t)T * SZ;
+    for (int i = threadIdx.x; i < SZ; i += blockDim.x) sC[i] = Cg[i];
+    __syncthreads();
+    const int64_t c = cb + threadIdx.x;
+    const bool active = c < t1;
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (active) {
+        const int N = F.natoms[f];
+        const int64_t aofs = F.atom_ofs[f];
+        const BoxDev& B = F.box[f];
+        const double perm = NBODY == 3 ? B.perm3 : B.perm4;
+        const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
+        const int64_t q = CS.ofs[aofs] + byt.val[c];
+        const int4 mm = CS.m[q];
+        SlotGeom* sg = sG + (size_t)threadIdx.x * NP;
+        cluster_geom<NBODY>(M, F, f, mm, sg);
+        R u[NP][O], G[NP][O];
+#pragma unroll
+        for (int s = 0; s < NP; ++s) {
+            const SlotGeom& g = sg[s];
+            double fc, fd;
+            fcut_eval(M, g.r, CT.smax[s], fc, fd);
+            basis_regs<O, true, false>(M, M.pairs[g.pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], g.r, fc, fd,
+                                       u[s], (R*)nullptr);
+#pragma unroll
+            for (int k = 0; k < O; ++k) G[s][k] = R(0);
+        }
+        R E;
+        if constexpr (NBODY == 3) E = contract3<O, R>(sC, u, G);
+        else E = contract4<O, R>(sC, u, G);
+        v[0] = perm * (double)E;
+        double fm[NBODY][3];
+#pragma unroll
+        for (int k = 0; k < NBODY; ++k) fm[k][0] = fm[k][1] = fm[k][2] = 0.0;
+#pragma unroll
+        for (int s = 0; s < NP; ++s) {
+            const SlotGeom& g = sg[s];
+            double fc, fd;
+            fcut_eval(M, g.r, CT.smax[s], fc, fd);
+            R h[O];
+            basis_regs<O, false, true>(M, M.pairs[g.pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], g.r, fc, fd,
+                                       (R*)nullptr, h);
+            R gs = R(0);
+#pragma unroll
+            for (int k = 0; k < O; ++k) gs = fma(G[s][k], h[k], gs);
+            const double ge = perm * (double)gs;
+            const double wv = ge / g.r;
+#pragma unroll
+            for (int k = 0; k < NBODY; ++k) {
+                if (k == g.a) { fm[k][0] += wv * g.R[0]; fm[k][1] += wv * g.R[1]; fm[k][2] += wv * g.R[2]; }
+                if (k == g.b) { fm[k][0] -= wv * g.R[0]; fm[k][1] -= wv * g.R[1]; fm[k][2] -= wv * g.R[2]; }
+            }
+            v[1] -= ge * g.r;
+            v[2] -= wv * g.R[0] * g.R[0]; v[3] -= wv * g.R[0] * g.R[1]; v[4] -= wv * g.R[0] * g.R[2];
+            v[5] -= wv * g.R[1] * g.R[1]; v[6] -= wv * g.R[1] * g.R[2]; v[7] -= wv * g.R[2] * g.R[2];
+        }
+#pragma unroll
+        for (int k = 0; k < NBODY; ++k) {
+            double* fo = Fo + 3 * (aofs + member(mm, k) % N);
+            atomicAdd(fo + 0, fm[k][0]);
+            atomicAdd(fo + 1, fm[k][1]);
+            atomicAdd(fo + 2, fm[k][2]);
+        }
+    }
+    block_scalars_add(v, So, f);
+}
+
+// Any order: the dense tensor read from global memory, digits decoded at run time,
+// leave-one-out products by prefix / suffix.  Used for orders without an unrolled
+// instantiation.
+constexpr int MDG_MAXO = 16;
+
+template <int NBODY>
+__global__ void __launch_bounds__(MDC_THREADS) k_mdc_generic(ModelDev M, MdDev D, FramesDev F, ClusterSet CS,
+                                                             Buckets byt, const int64_t* kfo, int O, double* Fo,
+                                                             double* So) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    __shared__ SlotGeom sG[MDC_THREADS * NP];
+    const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
+    const int f = blockIdx.x / ntypes;
+    const int T = blockIdx.x % ntypes;
+    const int64_t kb = kfo[f];
+    const int64_t t0 = byt.key_ofs[kb + T], t1 = byt.key_ofs[kb + T + 1];
+    const int64_t cb = t0 + (int64_t)blockIdx.y * blockDim.x;
+    if (cb >= t1) return;
+    int SZ = 1;
+    for (int k = 0; k < NP; ++k) SZ *= O;
+    const double* C = (NBODY == 3 ? D.C3 : D.C4) + (size_t)T * SZ;
+    const int64_t c = cb + threadIdx.x;
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (c < t1) {
+        const int N = F.natoms[f];
+        const int64_t aofs = F.atom_ofs[f];
+        const BoxDev& B = F.box[f];
+        const double perm = NBODY == 3 ? B.perm3 : B.perm4;
+        const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
+        const int64_t q = CS.ofs[aofs] + byt.val[c];
+        const int4 mm = CS.m[q];
+        SlotGeom* sg = sG + (size_t)threadIdx.x * NP;
+        cluster_geom<NBODY>(M, F, f, mm, sg);
+        double u[NP][MDG_MAXO], h[NP][MDG_MAXO], G[NP][MDG_MAXO];
+        for (int s = 0; s < NP; ++s) {
+            const SlotGeom& g = sg[s];
+            double fc, fd;
+            fcut_eval(M, g.r, CT.smax[s], fc, fd);
+            basis_gh(M, M.pairs[g.pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], g.r, 0, O, fc, fd, u[s], h[s], 1);
+            for (int k = 0; k < O; ++k) G[s][k] = 0.0;
+        }
+        double E = 0.0;
+        for (int idx = 0; idx < SZ; ++idx) {
+            const double cv = C[idx];
+            if (cv == 0.0) continue;
+            int p[NP];
+            int rem = idx;
+            for (int s = NP - 1; s >= 0; --s) { p[s] = rem % O; rem /= O; }
+            double pre[NP + 1], suf[NP + 1];
+            pre[0] = 1.0; suf[NP] = 1.0;
+            for (int s = 0; s < NP; ++s) pre[s + 1] = pre[s] * u[s][p[s]];
+            for (int s = NP - 1; s >= 0; --s) suf[s] = suf[s + 1] * u[s][p[s]];
+            E += cv * pre[NP];
+            for (int s = 0; s < NP; ++s) G[s][p[s]] += cv * pre[s] * suf[s + 1];
+        }
+        v[0] = perm * E;
+        for (int s = 0; s < NP; ++s) {
+            const SlotGeom& g = sg[s];
+            double gs = 0.0;
+            for (int k = 0; k < O; ++k) gs += G[s][k] * h[s][k];
+            const double ge = perm * gs;
+            const double wv = ge / g.r;
+            double* fa = Fo + 3 * (aofs + member(mm, g.a) % N);
+            double* fb = Fo + 3 * (aofs + member(mm, g.b) % N);
+            for (int k = 0; k < 3; ++k) { atomicAdd(fa + k, wv * g.R[k]); atomicAdd(fb + k, -wv * g.R[k]); }
+            v[1] -= ge * g.r;
+            v[2] -= wv * g.R[0] * g.R[0]; v[3] -= wv * g.R[0] * g.R[1]; v[4] -= wv * g.R[0] * g.R[2];
+            v[5] -= wv * g.R[1] * g.R[1]; v[6] -= wv * g.R[1] * g.R[2]; v[7] -= wv * g.R[2] * g.R[2];
+        }
+    }
+    block_scalars_add(v, So, f);
+}
+
+// ------------------------------------------------------------------ finish
+// ZCalc (src/functions.C:838-887): per-atom energy offsets, PRESSURE_XYZ / 3V,
+// tensor / V.
+__global__ void k_md_finalize(ModelDev M, MdDev D, FramesDev F, double* So) {
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    double e = 0.0;
+    if (D.eoff) {
+        const int* typ = F.type + F.atom_ofs[f];
+        for (int a = threadIdx.x; a < N; a += blockDim.x) e += D.eoff[typ[a]];
+    }
+    __shared__ double red[32];
+    e = warp_sum(e);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) s += red[i];
+        double* o = So + (size_t)f * MD_NSCALAR;
+        const double V = F.box[f].vol;
+        o[0] += s;
+        o[1] /= 3.0 * V;
+        for (int k = 2; k < MD_NSCALAR; ++k) o[k] /= V;
+    }
+}
+
+// ------------------------------------------------------------------ integration
+__global__ void k_md_drift(int64_t n3, double* x, double* v, const double* a, double dt) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n3) return;
+    x[i] += v[i] * dt + 0.5 * a[i] * dt * dt;
+    v[i] = v[i] + 0.5 * a[i] * dt;
+}
+
+__global__ void k_md_kick(FramesDev F, const double* Fo, const double* inv_mass_type, const double* mass_type,
+                          double* acc, double* v, double dt, int half, double* ke) {
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    double k = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const int t = F.type[aofs + i / 3];
+        const double a = Fo[g] * inv_mass_type[t];
+        acc[g] = a;
+        if (half) v[g] = v[g] + 0.5 * a * dt;
+        k += 0.5 * mass_type[t] * v[g] * v[g];
+    }
+    if (!ke) return;
+    __shared__ double red[32];
+    k = warp_sum(k);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = k;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) s += red[i];
+        ke[f] = s;
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+bool md_fast_order(int nbody, int order) {
+    if (nbody == 3) return order >= 2 && order <= 8;
+    return order >= 2 && order <= 4;
+}
+
+void launch_md2(const ModelDev& M, const MdDev& D, const FramesDev& F, const NeighDev& NB, double* Fo, double* So,
+                cudaStream_t st) {
+    if (NB.n_real == 0 || M.order2 == 0) return;
+    const int threads = 256;
+    const int64_t blocks = ((int64_t)NB.n_real * 32 + threads - 1) / threads;
+    k_md2<<<(unsigned)blocks, threads, 0, st>>>(M, D, F, NB, Fo, So);
+}
+
+template <int NBODY, int O, typename R>
+static void run_mdc(dim3 grid, const ModelDev& M, const MdDev& D, const FramesDev& F, const ClusterSet& CS,
+                    const Buckets& byt, const int64_t* kfo, double* Fo, double* So, cudaStream_t st) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    const size_t smem = ((IPow<NP, O>::v * sizeof(R) + 15) & ~size_t(15)) + sizeof(SlotGeom) * NP * MDC_THREADS;
+    cudaFuncSetAttribute(k_mdc<NBODY, O, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_mdc<NBODY, O, R><<<grid, MDC_THREADS, smem, st>>>(M, D, F, CS, byt, kfo, Fo, So);
+}
+
+template <int NBODY, typename R>
+static bool dispatch_mdc(int order, dim3 grid, const ModelDev& M, const MdDev& D, const FramesDev& F,
+                         const ClusterSet& CS, const Buckets& byt, const int64_t* kfo, double* Fo, double* So,
+                         cudaStream_t st) {
+#define MDC_CASE(O)                                                   \
+    case O:                                                           \
+        run_mdc<NBODY, O, R>(grid, M, D, F, CS, byt, kfo, Fo, So, st); \
+        return true;
+    if constexpr (NBODY == 3) {
+        switch (order) { MDC_CASE(2) MDC_CASE(3) MDC_CASE(4) MDC_CASE(5) MDC_CASE(6) MDC_CASE(7) MDC_CASE(8) }
+    } else {
+        switch (order) { MDC_CASE(2) MDC_CASE(3) MDC_CASE(4) }
+    }
+#undef MDC_CASE
+    return false;
+}
+
+void launch_mdc(int nbody, int prec, int nframes, int ntypes, int order, int max_bucket, const ModelDev& M,
+                const MdDev& D, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
+                const int64_t* key_frame_ofs, double* Fo, double* So, cudaStream_t st) {
+    if (max_bucket <= 0 || nframes * ntypes == 0) return;
+    dim3 grid((unsigned)(nframes * ntypes), (unsigned)((max_bucket + MDC_THREADS - 1) / MDC_THREADS));
+    bool done;
+    if (nbody == 3)
+        done = prec == 1 ? dispatch_mdc<3, float>(order, grid, M, D, F, CS, byt, key_frame_ofs, Fo, So, st)
+                         : dispatch_mdc<3, double>(order, grid, M, D, F, CS, byt, key_frame_ofs, Fo, So, st);
+    else
+        done = prec == 1 ? dispatch_mdc<4, float>(order, grid, M, D, F, CS, byt, key_frame_ofs, Fo, So, st)
+                         : dispatch_mdc<4, double>(order, grid, M, D, F, CS, byt, key_frame_ofs, Fo, So, st);
+    if (done) return;
+    if (nbody == 3) k_mdc_generic<3><<<grid, MDC_THREADS, 0, st>>>(M, D, F, CS, byt, key_frame_ofs, order, Fo, So);
+    else k_mdc_generic<4><<<grid, MDC_THREADS, 0, st>>>(M, D, F, CS, byt, key_frame_ofs, order, Fo, So);
+}
+
+void launch_md_finalize(int nframes, const ModelDev& M, const MdDev& D, const FramesDev& F, double* So,
+                        cudaStream_t st) {
+    if (nframes > 0) k_md_finalize<<<nframes, 256, 0, st>>>(M, D, F, So);
+}
+
+void launch_md_drift(int64_t natoms, double* xyz, double* v, const double* acc, double dt, cudaStream_t st) {
+    const int64_t n3 = 3 * natoms;
+    if (n3 > 0) k_md_drift<<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(n3, xyz, v, acc, dt);
+}
+
+void launch_md_kick(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
+                    const double* mass_type, double* acc, double* v, double dt, int half, double* ke, cudaStream_t st) {
+    if (nframes > 0) k_md_kick<<<nframes, 256, 0, st>>>(F, Fo, inv_mass_type, mass_type, acc, v, dt, half, ke);
+}
+
+}  // namespace cgd

@@ -1,0 +1,52 @@
+// MD force evaluation (the ZCalc / Cheby::Force_all path) on the device.
+//
+// Reference: ZCalc (src/functions.C:815-891), Cheby::Force_all (src/Cheby.C:1731-2021),
+// Force_3B (src/Cheby.C:2024-2300), Force_4B (src/Cheby.C:2303-2675).
+//
+// The clusters are the ones the design-matrix path enumerates (same neighbour
+// convention and cut-off tests); the 2-body list additionally keeps r <= s_min
+// (smoothed basis plus the cubic penalty).  Per cluster the coefficients are
+// contracted as one dense tensor over the canonical pair slots, so energy and all
+// edge derivatives come out of a single depth-first pass.
+#pragma once
+#include "kernels.h"
+
+namespace cgd {
+
+// Per-frame scalars written by the force pass:
+//   [0] potential energy, [1] scalar virial pressure term (PRESSURE_XYZ / 3V),
+//   [2..10] virial tensor / V, row-major xx xy xz yx yy yz zx zy zz.
+constexpr int MD_NSCALAR = 11;
+
+struct MdDev {
+    const double* c2;       // [npairs * order2]  coefficient of T_{n+1} of pair type
+    const double* C3;       // [ntypes3 * O3^3]   dense, canonical slots, slot 0 most significant
+    const double* C4;       // [ntypes4 * O4^6]
+    const float* C3f;       // FP32 copies (contraction precision 1)
+    const float* C4f;
+    const double* eoff;     // [natmtyp] per-atom energy offsets, or null
+    double pen_dist, pen_scale;   // 2-body penalty (src/chimes_md.C:1747-1748 defaults)
+};
+
+// Orders with an unrolled contraction kernel; others use the generic kernel.
+bool md_fast_order(int nbody, int order);
+
+void launch_md2(const ModelDev& M, const MdDev& D, const FramesDev& F, const NeighDev& NB, double* Fo, double* So,
+                cudaStream_t st);
+// Clusters of one body count, grouped by (frame, type) buckets; grid.y covers the
+// largest bucket.
+void launch_mdc(int nbody, int prec, int nframes, int ntypes, int order, int max_bucket, const ModelDev& M,
+                const MdDev& D, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
+                const int64_t* key_frame_ofs, double* Fo, double* So, cudaStream_t st);
+void launch_md_finalize(int nframes, const ModelDev& M, const MdDev& D, const FramesDev& F, double* So,
+                        cudaStream_t st);
+
+// Velocity Verlet (CONSTRAINT::UPDATE_COORDS / UPDATE_VELOCS_HALF_1 / _2,
+// src/ClassDefs.C:870-900, 1088-1157) over every real atom of the batch.
+// drift: x += v dt + a dt^2 / 2, v += a dt / 2.   kick: a = F / m, v += a dt / 2,
+// kinetic energy per frame into ke[f] (when ke is not null).
+void launch_md_drift(int64_t natoms, double* xyz, double* v, const double* acc, double dt, cudaStream_t st);
+void launch_md_kick(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
+                    const double* mass_type, double* acc, double* v, double dt, int half, double* ke, cudaStream_t st);
+
+}  // namespace cgd

@@ -12,6 +12,7 @@
 #include "gram.h"
 #include "assemble.h"
 #include "kernels.h"
+#include "scratch.h"
 
 namespace cg {
 
@@ -20,7 +21,6 @@ static const double GPA = 6.9476955;   // src/functions.h:45
 void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw Error(3, std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
 }
-#define CK(x) cuda_check((x), #x)
 
 template <typename T>
 static T* dev_upload(std::vector<void*>& allocs, const T* src, size_t n) {
@@ -152,6 +152,18 @@ DeviceModel::~DeviceModel() {
 }
 
 // ------------------------------------------------------------------ frames
+void set_small(cgd::BoxDev& bd, bool small) {
+    bd.small = small ? 1 : 0;
+    // PERM_SCALE src/ClassDefs.C:146-152
+    bd.perm2 = small ? 0.5 : 1.0;
+    bd.perm3 = small ? 0.5 / 3.0 : 1.0;
+    bd.perm4 = small ? 0.5 / 3.0 / 4.0 : 1.0;
+}
+
+void make_independent(FrameBatch& fb) {
+    for (int k = 0; k < fb.nframes; ++k) set_small(fb.box[k], fb.small_self[k] != 0);
+}
+
 FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int first_index) {
     FrameBatch fb;
     fb.nframes = (int)frames.size();
@@ -173,16 +185,14 @@ FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int firs
         fb.ghost_ofs.push_back(fb.ghost_ofs.back() + (int64_t)nimg * fr.natoms);
         fb.row_ofs.push_back(fb.row_ofs.back() + rl.total());
         small = frame_is_small(m, fr.box, small);
+        fb.small_self.push_back(frame_is_small(m, fr.box, false) ? 1 : 0);
         cgd::BoxDev bd;
         std::memset(&bd, 0, sizeof(bd));
         for (int q = 0; q < 9; ++q) { bd.h[q] = fr.box.hmat[q]; bd.inv[q] = fr.box.invr[q]; }
         bd.lx = fr.box.lx; bd.ly = fr.box.ly; bd.lz = fr.box.lz; bd.vol = fr.box.vol;
         bd.is_ortho = fr.box.is_ortho ? 1 : 0;
         bd.small = small ? 1 : 0;
-        // PERM_SCALE src/ClassDefs.C:146-152
-        bd.perm2 = small ? 0.5 : 1.0;
-        bd.perm3 = small ? 0.5 / 3.0 : 1.0;
-        bd.perm4 = small ? 0.5 / 3.0 / 4.0 : 1.0;
+        set_small(bd, small);
         fb.box.push_back(bd);
         fb.type.insert(fb.type.end(), fr.type.begin(), fr.type.end());
         fb.xyz.insert(fb.xyz.end(), fr.xyz.begin(), fr.xyz.end());
@@ -240,6 +250,16 @@ __global__ void k_key_frame_ofs(const int64_t* atom_ofs, int nframes, int per_ty
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f > nframes) return;
     out[f] = per_type > 0 ? (int64_t)f * (per_type + 1) : atom_ofs[f] + f;
+}
+
+void launch_scan_counts(const int* cnt, int n, int64_t* ofs, cudaStream_t st) {
+    k_scan_counts<<<1, 1024, 0, st>>>(cnt, n, ofs);
+}
+void launch_gather_frame_ofs(const int64_t* ofs, const int64_t* atom_ofs, int nframes, int64_t* out, cudaStream_t st) {
+    k_gather_frame_ofs<<<(nframes + 128) / 128, 128, 0, st>>>(ofs, atom_ofs, nframes, out);
+}
+void launch_key_frame_ofs(const int64_t* atom_ofs, int nframes, int per_type, int64_t* out, cudaStream_t st) {
+    k_key_frame_ofs<<<(nframes + 128) / 128, 128, 0, st>>>(atom_ofs, nframes, per_type, out);
 }
 }  // namespace cgd
 
@@ -306,6 +326,7 @@ Session::~Session() {
     for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : event_pool_) cudaEventDestroy(e);
     if (cublas_) cublasDestroy((cublasHandle_t)cublas_);
+    md_.reset();
     dm_.reset();
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -333,7 +354,8 @@ std::unique_ptr<DeviceFrames> Session::upload(const FrameBatch& fb) {
     d.energy_rows = dev_upload(df->allocs, fb.energy_rows.data(), fb.energy_rows.size());
     d.box = dev_upload(df->allocs, fb.box.data(), fb.box.size());
     d.type = dev_upload(df->allocs, fb.type.data(), fb.type.size());
-    d.xyz = dev_upload(df->allocs, fb.xyz.data(), fb.xyz.size());
+    df->xyz = dev_upload(df->allocs, fb.xyz.data(), fb.xyz.size());
+    d.xyz = df->xyz;
     double* scaled = nullptr;
     float* c32 = nullptr;
     CK(cudaMalloc((void**)&scaled, std::max<int64_t>(1, fb.nghosts) * 3 * sizeof(double)));
@@ -344,38 +366,6 @@ std::unique_ptr<DeviceFrames> Session::upload(const FrameBatch& fb) {
     d.cart32 = c32;
     return df;
 }
-
-// Per-call scratch: stream-ordered device allocations released at the end of the
-// call, or -- for the no-allocation entry point -- a bump allocator over the
-// static device array below (256-byte aligned sub-buffers, capacity checked).
-struct Scratch {
-    cudaStream_t s;
-    unsigned char* base = nullptr;
-    size_t cap = 0, used = 0;
-    std::vector<void*> ptrs;
-    explicit Scratch(cudaStream_t st) : s(st) {}
-    Scratch(cudaStream_t st, void* static_base, size_t capacity)
-        : s(st), base(reinterpret_cast<unsigned char*>(static_base)), cap(capacity) {}
-    template <typename T>
-    T* get(size_t n) {
-        const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
-        if (base) {
-            const size_t off = (used + 255) & ~size_t(255);
-            if (off + bytes > cap)
-                throw Error(4, "input exceeds the no-allocation scratch capacity of " +
-                                   std::to_string(cap >> 20) + " MiB; use cg_assemble_device");
-            used = off + bytes;
-            return reinterpret_cast<T*>(base + off);
-        }
-        void* p = nullptr;
-        CK(cudaMallocAsync(&p, bytes, s));
-        ptrs.push_back(p);
-        return reinterpret_cast<T*>(p);
-    }
-    ~Scratch() {
-        for (void* p : ptrs) cudaFreeAsync(p, s);
-    }
-};
 
 namespace {
 // Scratch of the no-allocation entry point: one fixed array per device that loads

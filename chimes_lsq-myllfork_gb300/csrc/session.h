@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "dev.cuh"
+#include "md.h"
 #include "model.h"
 
 namespace cg {
@@ -36,10 +37,15 @@ struct FrameBatch {
     std::vector<int> type;
     std::vector<double> xyz;
     std::vector<double> b;        // labels in A row order (src/A_Matrix.C:294-553)
+    std::vector<char> small_self; // each frame's own small-cell test (no carry-over)
     int64_t nrows = 0, natoms_total = 0, nghosts = 0;
 };
 
 FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int first_index);
+// The small-cell convention is sticky along a trajectory (the fit reads frames in
+// sequence); independent configurations (MD systems) each decide it alone.
+void make_independent(FrameBatch& fb);
+void set_small(cgd::BoxDev& bd, bool small);
 
 // The same batch resident in device memory.
 struct DeviceFrames {
@@ -49,6 +55,7 @@ struct DeviceFrames {
     std::vector<int64_t> atom_ofs_host, row_ofs_host;
     std::vector<int> natoms_host;
     std::vector<void*> allocs;
+    double* xyz = nullptr;          // the positions dev.xyz points to (the MD updates them)
     ~DeviceFrames();
 };
 
@@ -56,6 +63,18 @@ struct AssembleStats {
     int64_t pairs2 = 0, list3 = 0, list4 = 0, triplets = 0, quads = 0;
     int64_t power_evals3 = 0, power_evals4 = 0;   // sum over clusters of n_allowed
     int64_t launches = 0;                         // kernels launched by the last call
+};
+
+// Coefficient tables of the MD force (md.h), built from one fitted vector x.
+struct MdTables {
+    cgd::MdDev dev{};
+    int precision = 0;                 // 0: FP64 contraction, 1: FP32 contraction
+    std::vector<void*> allocs;
+    ~MdTables() { for (void* p : allocs) cudaFree(p); }
+};
+
+struct MdCounts {
+    int64_t pairs2 = 0, triplets = 0, quads = 0, launches = 0;
 };
 
 // Pipeline stages timed with CUDA events when profiling is on.
@@ -88,6 +107,20 @@ class Session {
                const double* b, int iters, double* x, double* info);
     void* cublas() const { return cublas_; }
 
+    // MD force (md.h / md_host.cu).  md_setup stores the coefficients x (one per A
+    // column): offsets adds the per-atom-type energy offsets of an energy fit.
+    void md_setup(const double* x, int nx, int precision, bool offsets, double pen_dist, double pen_scale);
+    bool md_ready() const { return (bool)md_; }
+    // Forces Fo [natoms_total*3] and per-frame scalars So [nframes*MD_NSCALAR]
+    // (device pointers) of the batch's current positions.
+    void md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts* counts);
+    // nsteps velocity-Verlet steps (NVE) of every frame of the batch; df's positions
+    // and v [natoms_total*3] (device) are advanced in place.  mass_type: host,
+    // natmtyp masses.  So_steps [(nsteps+1)*nframes*MD_NSCALAR] and ke_steps
+    // [(nsteps+1)*nframes] (device, may be null) receive step 0..nsteps.
+    void md_nve(DeviceFrames& df, const double* mass_type, double dt, int nsteps, double* v, double* Fo,
+                double* So_steps, double* ke_steps);
+
     // Stage timing (CUDA events on the session stream).
     void set_profiling(bool on) { profiling_ = on; }
     void stage_totals(double* ms, int64_t* calls);   // syncs pending events, accumulates, returns totals
@@ -109,6 +142,7 @@ class Session {
     cudaStream_t stream_ = nullptr;
     void* cublas_ = nullptr;
     std::unique_ptr<DeviceModel> dm_;
+    std::unique_ptr<MdTables> md_;
 };
 
 }  // namespace cg

@@ -71,6 +71,15 @@ void cg_frames_free(cg_frames* fr);
 /* Rows of the A matrix for these frames and the total atom count. */
 int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms);
 
+/* Number of frames in a batch. */
+int cg_frames_count(const cg_frames* fr, int* nframes);
+
+/* Treat the frames as independent configurations: each decides the small-cell
+ * neighbour convention (PERM_SCALE, src/ClassDefs.C:44-67) from its own box,
+ * instead of the fit's carry-over along a trajectory.  For MD batches; no
+ * counterpart in the reference, whose chimes_md runs one system. */
+int cg_frames_independent(cg_frames* fr);
+
 /* Label vector b in A row order (src/A_Matrix.C:294-553), nrows doubles. */
 int cg_frames_labels(const cg_frames* fr, double* b);
 
@@ -150,6 +159,46 @@ int cg_session_stage_times(cg_session* s, double* ms, int64_t* calls);
 const char* cg_stage_name(int stage);
 
 /* Message of the calling thread's last failure ("" if none). */
+/* ---------------------------------------------------------------- MD force
+ * The force-field evaluation of chimes_md for a batch of configurations:
+ * ZCalc (src/functions.C:815-891) with Cheby::Force_all / Force_3B / Force_4B
+ * (src/Cheby.C:1731-2675).  The coefficients are a fitted vector x with one value
+ * per A column (the order of params.txt's coefficients), and the basis, cut-offs and
+ * cluster map come from the model, as chimes_md takes them from params.txt. */
+#define CG_MD_ENERGY_OFFSETS 1   /* add x's per-atom-type energy offsets to the energy */
+
+/* Store the coefficients on the session's GPU.  precision: CG_FP64 (plain) or
+ * CG_FP32 (cluster contraction in FP32, geometry and accumulation in FP64).
+ * penalty_dist / penalty_scale: the 2-body penalty below s_min + dist (chimes_md
+ * defaults 0.01 and 1.0e4, src/chimes_md.C:1747-1748). */
+int cg_md_setup(cg_session* s, const double* x, int nx, int precision, int flags, double penalty_dist,
+                double penalty_scale);
+
+/* Forces (kcal/mol/A, 3 per atom in frame order; SYSTEM.ACCEL before the
+ * division by mass) and 11 scalars per frame: potential energy (kcal/mol), the
+ * pressure term PRESSURE_XYZ / (3V) and the 3x3 virial tensor / V (row-major,
+ * kcal/mol/A^3, PRESSURE_TENSORS_XYZ_ALL).  cg_md_force takes host frames and
+ * host outputs (copies included); cg_md_force_device works on uploaded frames and
+ * device outputs. */
+int cg_md_force(cg_session* s, const cg_frames* fr, double* forces, double* scalars);
+int cg_md_force_device(cg_session* s, const cg_dframes* d, double* forces, double* scalars);
+
+/* nsteps velocity-Verlet NVE steps of every uploaded frame (chimes_md with
+ * CONSRNT NVE: UPDATE_COORDS, UPDATE_VELOCS_HALF_1 / _2, src/ClassDefs.C:870-1157).
+ * mass: host, one per atom type (amu); dt_fs: time step in fs; velocities
+ * (device, A per internal time unit of 48.888 fs, advanced in place) and the
+ * positions of d are advanced; forces (device) holds the last step's forces.
+ * scalars_steps ((nsteps+1) * nframes * 11) and ke_steps ((nsteps+1) * nframes,
+ * kinetic energy) are device arrays receiving steps 0..nsteps, or NULL. */
+int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, double* velocities,
+              double* forces, double* scalars_steps, double* ke_steps);
+
+/* Device pointer to the positions of uploaded frames (3 per atom). */
+int cg_dframes_positions(const cg_dframes* d, double** xyz, int64_t* natoms);
+
+/* Pairs, triplets, quadruplets and kernel launches of the last MD force call. */
+int cg_md_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads, int64_t* launches);
+
 const char* cg_last_error(void);
 
 #ifdef __cplusplus

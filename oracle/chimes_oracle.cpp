@@ -15,6 +15,8 @@
 //   3-body rows     Cheby::Deriv_3B                src/Cheby.C:885-1277
 //   4-body rows     Cheby::Deriv_4B                src/Cheby.C:1279-1729
 //   row layout, b   A_MAT::PRINT_FRAME             src/A_Matrix.C:210-567
+//   MD force        ZCalc                          src/functions.C:815-891
+//                   Cheby::Force_all / 3B / 4B     src/Cheby.C:1731-2675
 // Parsing and the cluster topology come from the library's host model code
 // (model.cpp), whose params.header output is checked byte-for-byte against the
 // reference separately.
@@ -497,6 +499,222 @@ void frame_rows_out(const Model& m, const Frame& fr, int fi, bool small, double*
     }
 }
 
+// ---------------------------------------------------------------- MD force
+// ZCalc with Cheby::Force_all / Force_3B / Force_4B: the same lists and basis as
+// the fit, contracted with the coefficients x (one per A column).  F gets
+// SYSTEM.ACCEL (forces, kcal/mol/A); S gets [TOT_POT_ENER, PRESSURE_XYZ/(3V),
+// PRESSURE_TENSORS_XYZ_ALL/V (3x3 row-major)].
+struct MdOut {
+    std::vector<V3> F;
+    double E = 0, P = 0, W[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+};
+
+void md_tensor(MdOut& o, double fw, const V3& R) {   // fw already divided by r
+    o.W[0][0] -= fw * R.x * R.x; o.W[0][1] -= fw * R.x * R.y; o.W[0][2] -= fw * R.x * R.z;
+    o.W[1][1] -= fw * R.y * R.y; o.W[1][2] -= fw * R.y * R.z;
+    o.W[2][2] -= fw * R.z * R.z;
+    o.W[1][0] = o.W[0][1]; o.W[2][0] = o.W[0][2]; o.W[2][1] = o.W[1][2];
+}
+
+void md_force_2b(const Model& m, const OFrame& fr, const Lists& L, const double* x, double pd, double ps, MdOut& o) {
+    Basis B{m};
+    std::vector<double> Tn(m.ctl.cheby_order + 2), Tnd(m.ctl.cheby_order + 2);
+    V3 rab;
+    const double perm = L.perm[2];
+    for (int a1 = 0; a1 < fr.natoms; ++a1)
+        for (int a2 : L.l2[a1]) {
+            int pt = pair_index(m, fr, a1, a2);
+            const PairType& p = m.pairs[pt];
+            double r = get_dist(fr.box, fr.coords[a1], fr.coords[a2], rab);
+            if (!(r < p.smax)) continue;   // r < s_min included (src/Cheby.C:1834)
+            B.polys(pt, Tn.data(), Tnd.data(), r, p.xdiff, p.xavg, p.snum, p.smin);
+            double fc, fd;
+            B.fcut(fc, fd, r, p.smax);
+            int fa2 = fr.parent[a2];
+            for (int i = 0; i < p.snum; ++i) {
+                double coeff = perm * x[pt * p.snum + i];
+                o.E += coeff * fc * Tn[i + 1];
+                double deriv = fc * Tnd[i + 1] + fd * Tn[i + 1];
+                o.P -= coeff * deriv * r;
+                md_tensor(o, coeff * deriv / r, rab);
+                o.F[a1].x += coeff * deriv * rab.x / r; o.F[a1].y += coeff * deriv * rab.y / r;
+                o.F[a1].z += coeff * deriv * rab.z / r;
+                o.F[fa2].x -= coeff * deriv * rab.x / r; o.F[fa2].y -= coeff * deriv * rab.y / r;
+                o.F[fa2].z -= coeff * deriv * rab.z / r;
+            }
+            double rpen = (r - pd < p.smin) ? p.smin + pd - r : 0.0;   // src/Cheby.C:1900-1968
+            if (rpen > 0.0) {
+                double coeff = -3.0 * rpen * rpen * ps;
+                o.F[a1].x += coeff * rab.x / r; o.F[a1].y += coeff * rab.y / r; o.F[a1].z += coeff * rab.z / r;
+                o.F[fa2].x -= coeff * rab.x / r; o.F[fa2].y -= coeff * rab.y / r; o.F[fa2].z -= coeff * rab.z / r;
+                o.E += rpen * rpen * rpen * ps;
+                o.P -= coeff * r;
+                md_tensor(o, coeff / r, rab);
+            }
+        }
+}
+
+// Force_3B (src/Cheby.C:2024-2300) over the fit's triplet enumeration.
+void md_force_3b(const Model& m, const OFrame& fr, const Lists& L, const double* x, MdOut& o) {
+    Basis B{m};
+    const ClusterList& cl = m.trips;
+    const int ord = m.ctl.cheby3;
+    std::vector<double> T[3], D[3];
+    for (int e = 0; e < 3; ++e) { T[e].resize(ord + 2); D[e].resize(ord + 2); }
+    const double perm = L.perm[3];
+    V3 R[3];
+    double rl[3];
+    for (int a1 = 0; a1 < fr.natoms; ++a1)
+        for (int a2 : L.l3[a1])
+            for (int a3 : L.l3[a1]) {
+                if (a3 == a2) continue;
+                if (perm == 1.0 && fr.parent[a2] > fr.parent[a3]) continue;
+                int pts[3] = {pair_index(m, fr, a1, a2), pair_index(m, fr, a1, a3), pair_index(m, fr, a2, a3)};
+                int ti[3] = {fr.type[a1], fr.type[a2], fr.type[a3]};
+                int id = make_id_int(ti, 3);
+                int T3 = cl.int_map[id];
+                if (T3 < 0) continue;
+                const ClusterType& ct = cl.vec[T3];
+                const std::vector<int>& pi = cl.pair_indices[id];
+                rl[0] = get_dist(fr.box, fr.coords[a1], fr.coords[a2], R[0]);
+                rl[1] = get_dist(fr.box, fr.coords[a1], fr.coords[a3], R[1]);
+                rl[2] = get_dist(fr.box, fr.coords[a2], fr.coords[a3], R[2]);
+                bool ok = true;
+                for (int e = 0; e < 3; ++e) ok = ok && rl[e] < ct.smax[pi[e]];
+                if (!ok) continue;
+                double fc[3], fd[3];
+                for (int e = 0; e < 3; ++e)
+                    B.polys(pts[e], T[e].data(), D[e].data(), rl[e], ct.xdiff[pi[e]], ct.xavg[pi[e]], ord, ct.smin[pi[e]]);
+                for (int e = 0; e < 3; ++e) B.fcut(fc[e], fd[e], rl[e], ct.smax[pi[e]]);
+                int vstart = m.tot_snum;
+                for (int t = 0; t < T3; ++t) vstart += cl.vec[t].n_true;
+                int fid[3] = {a1, fr.parent[a2], fr.parent[a3]};
+                static const int ea[3] = {0, 0, 1}, eb[3] = {1, 2, 2};
+                for (int p = 0; p < ct.n_allowed; ++p) {
+                    double coeff = perm * x[vstart + ct.param_indices[p]];
+                    int pw[3] = {ct.allowed_powers[p][pi[0]], ct.allowed_powers[p][pi[1]], ct.allowed_powers[p][pi[2]]};
+                    o.E += coeff * fc[0] * fc[1] * fc[2] * T[0][pw[0]] * T[1][pw[1]] * T[2][pw[2]];
+                    double d[3], f[3];
+                    for (int e = 0; e < 3; ++e) d[e] = fc[e] * D[e][pw[e]] + fd[e] * T[e][pw[e]];
+                    f[0] = coeff * d[0] * fc[1] * fc[2] * T[1][pw[1]] * T[2][pw[2]];
+                    f[1] = coeff * d[1] * fc[0] * fc[2] * T[0][pw[0]] * T[2][pw[2]];
+                    f[2] = coeff * d[2] * fc[0] * fc[1] * T[0][pw[0]] * T[1][pw[1]];
+                    for (int e = 0; e < 3; ++e) {
+                        o.P -= f[e] * rl[e];
+                        double fw = f[e] / rl[e];
+                        md_tensor(o, fw, R[e]);
+                        V3& A = o.F[fid[ea[e]]];
+                        V3& Bv = o.F[fid[eb[e]]];
+                        A.x += fw * R[e].x; A.y += fw * R[e].y; A.z += fw * R[e].z;
+                        Bv.x -= fw * R[e].x; Bv.y -= fw * R[e].y; Bv.z -= fw * R[e].z;
+                    }
+                }
+            }
+}
+
+// Force_4B (src/Cheby.C:2303-2675) over the fit's quadruplet enumeration.
+void md_force_4b(const Model& m, const OFrame& fr, const Lists& L, const double* x, MdOut& o) {
+    Basis B{m};
+    const ClusterList& cl = m.quads;
+    const int ord = m.ctl.cheby4;
+    std::vector<double> T[6], D[6];
+    for (int e = 0; e < 6; ++e) { T[e].resize(ord + 2); D[e].resize(ord + 2); }
+    const double perm = L.perm[4];
+    V3 R[6];
+    double rl[6];
+    static const int ea[6] = {0, 0, 0, 1, 1, 2}, eb[6] = {1, 2, 3, 2, 3, 3};
+    for (int a1 = 0; a1 < fr.natoms; ++a1)
+        for (int a2 : L.l4[a1])
+            for (int a3 : L.l4[a1]) {
+                if (a3 == a2) continue;
+                if (perm == 1.0 && fr.parent[a2] > fr.parent[a3]) continue;
+                for (int a4 : L.l4[a1]) {
+                    if (a2 == a4 || a3 == a4) continue;
+                    if (perm == 1.0 && fr.parent[a3] > fr.parent[a4]) continue;
+                    int at[4] = {a1, a2, a3, a4};
+                    int pts[6];
+                    for (int e = 0; e < 6; ++e) pts[e] = pair_index(m, fr, at[ea[e]], at[eb[e]]);
+                    int ti[4] = {fr.type[a1], fr.type[a2], fr.type[a3], fr.type[a4]};
+                    int id = make_id_int(ti, 4);
+                    int Q = cl.int_map[id];
+                    if (Q < 0) continue;
+                    for (int e = 0; e < 6; ++e) rl[e] = get_dist(fr.box, fr.coords[at[ea[e]]], fr.coords[at[eb[e]]], R[e]);
+                    const ClusterType& ct = cl.vec[Q];
+                    const std::vector<int>& pm = cl.pair_indices[id];
+                    bool ok = true;
+                    for (int e = 0; e < 6 && ok; ++e) ok = rl[e] < ct.smax[pm[e]];
+                    if (!ok) continue;
+                    for (int e = 0; e < 6; ++e)
+                        B.polys(pts[e], T[e].data(), D[e].data(), rl[e], ct.xdiff[pm[e]], ct.xavg[pm[e]], ord, ct.smin[pm[e]]);
+                    double fc[6], fd[6];
+                    for (int e = 0; e < 6; ++e) B.fcut(fc[e], fd[e], rl[e], ct.smax[pm[e]]);
+                    int vstart = m.tot_snum + m.num3;
+                    for (int t = 0; t < Q; ++t) vstart += cl.vec[t].n_true;
+                    int fid[4] = {a1, fr.parent[a2], fr.parent[a3], fr.parent[a4]};
+                    for (int p = 0; p < ct.n_allowed; ++p) {
+                        double coeff = perm * x[vstart + ct.param_indices[p]];
+                        int pw[6];
+                        for (int e = 0; e < 6; ++e) pw[e] = ct.allowed_powers[p][pm[e]];
+                        double te = coeff;
+                        for (int e = 0; e < 6; ++e) te *= fc[e];
+                        for (int e = 0; e < 6; ++e) te *= T[e][pw[e]];
+                        o.E += te;
+                        for (int e = 0; e < 6; ++e) {
+                            double f = coeff * (fc[e] * D[e][pw[e]] + fd[e] * T[e][pw[e]]);
+                            for (int k = 0; k < 6; ++k) if (k != e) f *= fc[k];
+                            for (int k = 0; k < 6; ++k) if (k != e) f *= T[k][pw[k]];
+                            o.P -= f * rl[e];
+                            double fw = f / rl[e];
+                            md_tensor(o, fw, R[e]);
+                            V3& A = o.F[fid[ea[e]]];
+                            V3& Bv = o.F[fid[eb[e]]];
+                            A.x += fw * R[e].x; A.y += fw * R[e].y; A.z += fw * R[e].z;
+                            Bv.x -= fw * R[e].x; Bv.y -= fw * R[e].y; Bv.z -= fw * R[e].z;
+                        }
+                    }
+                }
+            }
+}
+
+void md_force_frame(const Model& m, const Frame& fr, bool small, const double* x, bool offsets, double pd, double ps,
+                    double* F, double* S) {
+    OFrame of = make_frame(m, fr);
+    Lists L = neighbours(m, of, small);
+    MdOut o;
+    o.F.assign(fr.natoms, V3{0, 0, 0});
+    if (offsets)
+        for (int a = 0; a < fr.natoms; ++a) o.E += x[m.tot_short + fr.type[a]];
+    if (m.ctl.cheby_order > 0) md_force_2b(m, of, L, x, pd, ps, o);
+    if (m.ctl.use3) md_force_3b(m, of, L, x, o);
+    if (m.ctl.use4) md_force_4b(m, of, L, x, o);
+    for (int a = 0; a < fr.natoms; ++a) { F[3 * a] = o.F[a].x; F[3 * a + 1] = o.F[a].y; F[3 * a + 2] = o.F[a].z; }
+    const double V = fr.box.vol;
+    S[0] = o.E;
+    S[1] = o.P / (3.0 * V);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) S[2 + 3 * i + j] = o.W[i][j] / V;
+}
+
+std::vector<Frame> frames_from_arrays(const Model& m, int nframes, const int* natoms, const int* types,
+                                      const double* xyz, const double* cell) {
+    std::vector<Frame> frames(nframes);
+    int64_t a0 = 0;
+    for (int f = 0; f < nframes; ++f) {
+        Frame& fr = frames[f];
+        fr.natoms = natoms[f];
+        fr.type.assign(types + a0, types + a0 + fr.natoms);
+        fr.xyz.assign(xyz + 3 * a0, xyz + 3 * (a0 + fr.natoms));
+        fr.force.assign(3 * (size_t)fr.natoms, 0.0);
+        const double* c = cell + 9 * (size_t)f;
+        Box& b = fr.box;
+        b.ax = c[0]; b.ay = c[1]; b.az = c[2]; b.bx = c[3]; b.by = c[4]; b.bz = c[5];
+        b.cx = c[6]; b.cy = c[7]; b.cz = c[8];
+        b.update_cell();
+        a0 += fr.natoms;
+    }
+    return frames;
+}
+
 thread_local std::string g_err;
 
 }  // namespace
@@ -546,6 +764,36 @@ int oracle_assemble(const char* fm_setup, const char* xyzf, int nframes, int fir
         for (int k = 0; k < count; ++k) {
             try {
                 frame_rows_out(m, fr[first + k], first + k, small[k], A + ofs[k] * lda, lda, b + ofs[k]);
+            } catch (const std::exception& e) {
+#pragma omp critical
+                err = e.what();
+            }
+        }
+        if (!err.empty()) throw Error(2, err);
+        return 0;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return 2;
+    }
+}
+
+// MD force of independent configurations (each decides the small-cell convention
+// alone): forces [3 * sum natoms] and 11 scalars per frame (see md_force_frame).
+int oracle_md_force(const char* fm_setup, int nframes, const int* natoms, const int* types, const double* xyz,
+                    const double* cell, const double* x, int nx, int offsets, double pen_dist, double pen_scale,
+                    int nthreads, double* F, double* S) {
+    try {
+        Model m = load_model(fm_setup);
+        if (nx != m.tot_all) throw Error(1, "coefficient count does not match the model");
+        std::vector<Frame> fr = frames_from_arrays(m, nframes, natoms, types, xyz, cell);
+        std::vector<int64_t> ofs(nframes + 1, 0);
+        for (int f = 0; f < nframes; ++f) ofs[f + 1] = ofs[f] + natoms[f];
+        std::string err;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
+        for (int f = 0; f < nframes; ++f) {
+            try {
+                bool small = frame_is_small(m, fr[f].box, false);
+                md_force_frame(m, fr[f], small, x, offsets != 0, pen_dist, pen_scale, F + 3 * ofs[f], S + 11 * f);
             } catch (const std::exception& e) {
 #pragma omp critical
                 err = e.what();

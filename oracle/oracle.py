@@ -37,6 +37,10 @@ def lib():
         L.oracle_assemble.restype = ctypes.c_int
         L.oracle_assemble.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+        L.oracle_md_force.restype = ctypes.c_int
+        L.oracle_md_force.argtypes = [ctypes.c_char_p, ctypes.c_int] + [ctypes.c_void_p] * 5 + [
+            ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p,
+            ctypes.c_void_p]
         L.oracle_last_error.restype = ctypes.c_char_p
         _lib = L
     return _lib
@@ -73,6 +77,24 @@ def assemble(fm_setup, xyzf=None, nframes=0, first=0, count=0, nthreads=1):
     if rc:
         raise RuntimeError(lib().oracle_last_error().decode())
     return A, b
+
+
+def md_force(fm_setup, natoms, types, xyz, cell, x, offsets=False, pen_dist=0.01, pen_scale=1.0e4, nthreads=1):
+    """MD forces [sum natoms, 3] and scalars [nframes, 11] of independent
+    configurations (ZCalc restated; see chimes_oracle.cpp)."""
+    natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+    types = np.ascontiguousarray(types, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    cell = np.ascontiguousarray(cell, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    F = np.zeros((int(natoms.sum()), 3), dtype=np.float64)
+    S = np.zeros((len(natoms), 11), dtype=np.float64)
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)
+    rc = lib().oracle_md_force(_enc(fm_setup), len(natoms), p(natoms), p(types), p(xyz), p(cell), p(x), x.size,
+                               1 if offsets else 0, float(pen_dist), float(pen_scale), int(nthreads), p(F), p(S))
+    if rc:
+        raise RuntimeError(lib().oracle_last_error().decode())
+    return F, S
 
 
 def run_reference(workdir):

@@ -1,0 +1,146 @@
+"""Generate the MD fixtures of tests/golden/md_*/ with the reference's own chimes_md.
+
+Run in a container where the reference sources are available:
+    oracle/build_ref.sh && python tests/golden/make_md_fixtures.py
+Per fixture: a seeded synthetic trajectory is fitted (numpy least squares on the
+oracle's A, only to obtain a physically shaped coefficient vector x), params.txt is
+written by the library's writer, and the reference chimes_md runs NVE from the
+first frame with seeded 300 K velocities.  md_ref.npz keeps the configuration, x,
+the velocities, the reference's forces of every step (forceout.txt, 15 digits) and
+its per-step table (Ktot/N, Vtot/N, Etot/N, T, P from run_md.out).
+"""
+import importlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+cg = importlib.import_module("chimes_lsq-myllfork_gb300")
+from oracle import oracle  # noqa: E402
+
+REF_MD = os.path.join(ROOT, "oracle", "_ref", "chimes_md")
+KB = 0.0019872067   # kcal/mol/K (src/functions.h:43)
+
+# name -> (workload, overrides, fit frames, seed, NVE steps)
+MD_FIXTURES = {
+    "md_water3b": ("water-3b", dict(nmol=32, L=9.86), 3, 31, 10),
+    "md_ch4b": ("chno-4b", dict(natoms=40, order=(8, 4, 3), triclinic=False, density=0.1, species2=True), 8, 32, 10),
+}
+
+RUN_MD = """# RNDSEED #
+	12357
+# TEMPERA #
+	300.0
+# CMPRFRC #
+	false
+# TIMESTP #
+	{dt}
+# N_MDSTP #
+	{steps}
+# NLAYERS #
+	1
+# USENEIG #
+	true
+# PRMFILE #
+	params.txt
+# CRDFILE #
+	input.xyzf
+# VELINIT #
+	READ
+# CONSRNT #
+	NVE
+# PRSCALC #
+	ANALYTICAL
+# WRPCRDS #
+	false
+# FRQDFTB #
+	1000
+# FRQENER #
+	1
+# PRNTFRC #
+	true 1
+# ENDFILE #
+"""
+
+
+def header_types(model):
+    lines = model.params_header().splitlines()
+    i = next(k for k, ln in enumerate(lines) if ln.startswith("# TYPEIDX #"))
+    n = int(next(ln for ln in lines if ln.startswith("ATOM TYPES:")).split()[2])
+    rows = [lines[i + 1 + k].split() for k in range(n)]
+    return [r[1] for r in rows], np.array([float(r[3]) for r in rows])
+
+
+def read_first_frame(path, names):
+    L = open(path).read().split("\n")
+    n = int(L[0].split()[0])
+    t = L[1].split()
+    if t[0] == "NON_ORTHO":
+        cell = [float(v) for v in t[1:10]]
+    else:
+        a, b, c = (float(v) for v in t[:3])
+        cell = [a, 0, 0, 0, b, 0, 0, 0, c]
+    types, xyz = [], []
+    for k in range(n):
+        w = L[2 + k].split()
+        types.append(names.index(w[0]))
+        xyz.append([float(v) for v in w[1:4]])
+    return n, np.array(types, dtype=np.int32), np.array(xyz), np.array(cell)
+
+
+def make(name):
+    wl, over, nfit, seed, steps = MD_FIXTURES[name]
+    d = os.path.join(HERE, name)
+    os.makedirs(d, exist_ok=True)
+    fm = synth.make_workload(wl, d, nframes=nfit, seed=seed, **over)
+    model = cg.Model(fm)
+    A, b = oracle.assemble(fm, nthreads=8)
+    lam = 1e-8 * np.abs(A).max() ** 2
+    x = np.linalg.solve(A.T @ A + lam * np.eye(A.shape[1]), A.T @ b)
+    names, masses = header_types(model)
+    n, types, xyz, cell = read_first_frame(os.path.join(d, "traj.xyzf"), names)
+    rng = np.random.default_rng(seed)
+    tfs = 48.888   # internal time unit in fs (src/functions.h:44)
+    v = rng.standard_normal((n, 3)) * np.sqrt(KB * 300.0 / masses[types])[:, None]
+    v -= (masses[types][:, None] * v).sum(0) / masses[types].sum()
+    dt = 0.2
+    with tempfile.TemporaryDirectory() as tmp:
+        open(os.path.join(tmp, "params.txt"), "w").write(model.params_txt(x, "! synthetic fit for MD fixtures\n!\n"))
+        with open(os.path.join(tmp, "input.xyzf"), "w") as f:
+            f.write(f"{n}\n")
+            if cell[1] == 0 and cell[2] == 0 and cell[3] == 0 and cell[5] == 0 and cell[6] == 0 and cell[7] == 0:
+                f.write(f"{cell[0]:.10f} {cell[4]:.10f} {cell[8]:.10f}\n")
+            else:
+                f.write("NON_ORTHO " + " ".join(f"{c:.10f}" for c in cell) + "\n")
+            for k in range(n):
+                f.write(f"{names[types[k]]} {xyz[k, 0]:.10f} {xyz[k, 1]:.10f} {xyz[k, 2]:.10f} "
+                        f"{v[k, 0]:.16e} {v[k, 1]:.16e} {v[k, 2]:.16e}\n")
+        open(os.path.join(tmp, "run_md.in"), "w").write(RUN_MD.format(dt=dt, steps=steps))
+        p = subprocess.run([REF_MD, "run_md.in"], cwd=tmp, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"chimes_md failed for {name}:\n{p.stdout[-2000:]}")
+        # read the positions / velocities back exactly as chimes_md parsed them
+        _, _, xyz_in, _ = read_first_frame(os.path.join(tmp, "input.xyzf"), names)
+        Fall = np.loadtxt(os.path.join(tmp, "forceout.txt")).reshape(-1, n, 3)
+        table = []
+        out = p.stdout.split("Ktot/N", 1)[1].split("END SIMULATION", 1)[0]
+        for ln in out.splitlines():
+            w = ln.split()
+            if len(w) == 7 and w[0].isdigit():   # Step Time Ktot/N Vtot/N Etot/N T P (NVE)
+                table.append([float(t) for t in w])
+    vin = np.array([[float(t) for t in f"{v[k, 0]:.16e} {v[k, 1]:.16e} {v[k, 2]:.16e}".split()] for k in range(n)])
+    np.savez_compressed(os.path.join(d, "md_ref.npz"), x=x, types=types, xyz=xyz_in, cell=cell, v=vin,
+                        masses=masses, dt=dt, steps=steps, forces=Fall, table=np.array(table))
+    os.remove(os.path.join(d, "traj.xyzf"))   # the fixture keeps its first frame in md_ref.npz
+    print(name, "atoms", n, "cols", x.size, "force blocks", Fall.shape[0], "table rows", len(table))
+
+
+if __name__ == "__main__":
+    for nm in (sys.argv[1:] or MD_FIXTURES):
+        make(nm)

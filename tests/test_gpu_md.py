@@ -1,0 +1,159 @@
+"""GPU MD force (cg_md_force*, cg_md_nve) against the oracle and the reference's
+own chimes_md outputs (tests/golden/md_*/md_ref.npz).
+
+Tolerances (FP64): forces within 1e-10 of the largest component, energy and
+virial within 1e-10 relative.  FP32 contraction: forces within 2e-5 of the
+largest component, energy within 2e-6 relative.  NVE against the reference's
+10-step run: per-atom kinetic / potential energy to the printed 7 decimals
+(5e-8), pressure to the printed 8 decimals, forces of every step within 1e-8.
+"""
+import importlib
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+GPA = 6.9476955
+MD_FIXTURES = ["md_water3b", "md_ch4b"]
+
+
+def load_md(name):
+    d = np.load(os.path.join(GOLDEN, name, "md_ref.npz"))
+    return os.path.join(GOLDEN, name, "fm_setup.in"), {k: d[k] for k in d.files}
+
+
+def gpu_force(cg, fm, natoms, types, xyz, cell, x, precision=0, offsets=False):
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.md_setup(x, precision=precision, energy_offsets=offsets)
+    fr = cg.Frames.from_arrays(model, natoms, types, xyz, cell).independent()
+    F, S = sess.md_force(fr)
+    return F, S, sess
+
+
+def close(a, b, rel):
+    return np.abs(a - b).max() <= rel * max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name", MD_FIXTURES)
+def test_md_force_fp64_matches_reference_and_oracle(cg, oracle, name):
+    fm, d = load_md(name)
+    n = len(d["types"])
+    F, S, sess = gpu_force(cg, fm, [n], d["types"], d["xyz"], d["cell"][None], d["x"], offsets=True)
+    Fo, So = oracle.md_force(fm, [n], d["types"], d["xyz"], d["cell"][None], d["x"], offsets=True, nthreads=8)
+    assert close(F, d["forces"][0], 1e-10)
+    assert close(F, Fo, 1e-10)
+    assert abs(S[0, 0] - So[0, 0]) <= 1e-10 * abs(So[0, 0])
+    assert close(S[0, 1:], So[0, 1:], 1e-10)
+    c = sess.md_last_counts()
+    assert c["pairs"] > 0 and c["launches"] > 0
+
+
+def _chno_batch(cg, tmp_path, sizes, triclinic, seed):
+    synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+    fm = synth.make_workload("chno-4b", str(tmp_path), nframes=len(sizes), seed=seed, order=(8, 4, 3),
+                             sizes=list(sizes), triclinic=triclinic, density=0.1)
+    model = cg.Model(fm)
+    nat, types, xyz, cell = synth.frames_arrays(os.path.join(str(tmp_path), "traj.xyzf"), len(sizes),
+                                                ["C", "H", "N", "O"])[:4]
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(model.ncols) * 0.05
+    return fm, model, (nat, types, xyz, cell), x
+
+
+@pytest.mark.parametrize("triclinic", [False, True])
+def test_md_force_batch_matches_oracle_and_each_alone(cg, oracle, tmp_path, triclinic):
+    """Frames of different sizes in one batch: each result equals the oracle's and
+    the same frame evaluated alone (atomics reorder sums: 1e-12 relative)."""
+    sizes = [24, 60, 33] if not triclinic else [150, 90]
+    fm, model, (nat, types, xyz, cell), x = _chno_batch(cg, tmp_path, sizes, triclinic, 71 + triclinic)
+    F, S, _ = gpu_force(cg, fm, nat, types, xyz, cell, x)
+    Fo, So = oracle.md_force(fm, nat, types, xyz, cell, x, nthreads=8)
+    assert close(F, Fo, 1e-10)
+    assert close(S, So, 1e-10)
+    ofs = np.concatenate([[0], np.cumsum(nat)])
+    for f in range(len(nat)):
+        a, b = ofs[f], ofs[f + 1]
+        F1, S1, _ = gpu_force(cg, fm, [nat[f]], types[a:b], xyz[a:b], cell[f:f + 1], x)
+        assert close(F1, F[a:b], 1e-12)
+        assert close(S1[0], S[f], 1e-12)
+
+
+def test_md_force_small_cell_convention(cg, oracle):
+    """Cell extent below the cut-off: unordered lists with PERM_SCALE 1/n!."""
+    fm = os.path.join(GOLDEN, "small4b", "fm_setup.in")
+    model = cg.Model(fm)
+    synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+    nat, types, xyz, cell = synth.frames_arrays(os.path.join(GOLDEN, "small4b", "traj.xyzf"), 1, ["C", "H"])[:4]
+    x = np.random.default_rng(5).standard_normal(model.ncols) * 0.05
+    F, S, _ = gpu_force(cg, fm, nat, types, xyz, cell, x)
+    Fo, So = oracle.md_force(fm, nat, types, xyz, cell, x, nthreads=4)
+    assert close(F, Fo, 1e-10)
+    assert close(S, So, 1e-10)
+
+
+def test_md_force_equals_design_matrix_times_coefficients(cg):
+    """The reference's verify-lsq-forces identity: MD forces = A x on the force rows
+    (and energy / stress rows against the MD energy and virial) when no pair is
+    inside s_min + 0.01 (the fit's 2-body rows skip r <= s_min)."""
+    fm, d = load_md("md_ch4b")
+    n = len(d["types"])
+    model = cg.Model(fm)
+    fr = cg.Frames.from_arrays(model, [n], d["types"], d["xyz"], d["cell"][None])
+    sess = cg.Session(model, 0)
+    A = sess.assemble(fr, cg.CG_FP64)
+    sess.md_setup(d["x"], energy_offsets=True, penalty_scale=0.0)
+    F, S = sess.md_force(fr)
+    y = A @ d["x"]
+    assert close(F.reshape(-1), y[:3 * n], 1e-10)
+    rows = A.shape[0] - 3 * n
+    if rows >= 12:   # 9 stress rows (xx xy xz yx yy yz zx zy zz) then 3 energy rows
+        assert close(S[0, 2:11], y[3 * n:3 * n + 9], 1e-10)
+        assert abs(y[-1] - S[0, 0]) <= 1e-10 * abs(S[0, 0])
+
+
+@pytest.mark.parametrize("name", MD_FIXTURES)
+def test_md_force_fp32_contraction_tolerance(cg, name):
+    fm, d = load_md(name)
+    n = len(d["types"])
+    F64, S64, _ = gpu_force(cg, fm, [n], d["types"], d["xyz"], d["cell"][None], d["x"])
+    F32, S32, _ = gpu_force(cg, fm, [n], d["types"], d["xyz"], d["cell"][None], d["x"], precision=1)
+    err = np.abs(F32 - F64).max() / np.abs(F64).max()
+    print(f"\n{name}: FP32-contraction force error {err:.3e} of max |F|", flush=True)
+    assert err <= 2e-5
+    assert abs(S32[0, 0] - S64[0, 0]) <= 2e-6 * abs(S64[0, 0])
+
+
+@pytest.mark.parametrize("name", MD_FIXTURES)
+def test_md_nve_matches_reference_run(cg, name):
+    torch = pytest.importorskip("torch")
+    fm, d = load_md(name)
+    n = len(d["types"])
+    steps = int(d["steps"]) - 1          # the reference prints steps 0..N_MDSTP-1
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.md_setup(d["x"], energy_offsets=True)
+    fr = cg.Frames.from_arrays(model, [n], d["types"], d["xyz"], d["cell"][None]).independent()
+    F0, _ = sess.md_force(fr)
+    dfr = sess.upload(fr)
+    v = torch.from_numpy(d["v"].reshape(-1).copy()).cuda()
+    Fd = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    So = torch.zeros((steps + 1, 11), dtype=torch.float64, device="cuda")
+    ke = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    sess.md_nve(dfr, d["masses"], float(d["dt"]), steps, v.data_ptr(), Fd.data_ptr(), So.data_ptr(), ke.data_ptr())
+    torch.cuda.synchronize()
+    So_h, ke_h = So.cpu().numpy(), ke.cpu().numpy()
+    V = abs(np.linalg.det(d["cell"].reshape(3, 3)))
+    tab = d["table"]
+    assert close(F0, d["forces"][0], 1e-10)
+    assert close(Fd.cpu().numpy().reshape(n, 3), d["forces"][steps], 1e-8)
+    for s in range(steps + 1):
+        kn = ke_h[s] / n
+        vn = So_h[s, 0] / n
+        p = (So_h[s, 1] + 2.0 * ke_h[s] / (3.0 * V)) * GPA
+        assert abs(kn - tab[s, 2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, tab[s, 2])
+        assert abs(vn - tab[s, 3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, tab[s, 3])
+        assert abs(p - tab[s, 6]) <= 5e-9 * max(1.0, abs(p)) + 1e-12, (s, p, tab[s, 6])
