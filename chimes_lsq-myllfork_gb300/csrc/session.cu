@@ -631,25 +631,28 @@ void Session::solve(const double* G, const double* h, int ncols, double ridge, c
         cholesky_solve(L, ncols, h, x, cublas_, stream_);
         double rn = 0, gn = 0;
         if (iters > 0 && A && b) {
-            // preconditioned CG on the exact normal equations A^T A x = A^T b (FP64 products
-            // through A), preconditioner (L L^T)^-1
+            // preconditioned CG on the FP64 ridge normal equations (A^T A + ridge I) x = A^T b,
+            // products through A; preconditioner (L L^T)^-1 from the (possibly mixed-precision,
+            // possibly more strongly ridged) Gram factor
             double* r = S.get<double>(ncols);   // normal-equation residual
             double* z = S.get<double>(ncols);
             double* pv = S.get<double>(ncols);
             double* q = S.get<double>(ncols);
             double* t = S.get<double>(nrows);
-            const double one = 1.0, zero = 0.0;
+            const double one = 1.0, zero = 0.0, mridge = -ridge;
             cublasSetStream(hb, stream_);
             cublasSetPointerMode(hb, CUBLAS_POINTER_MODE_HOST);
             residual(A, lda, nrows, ncols, b, x, t, r, &rn, &gn, cublas_, stream_);
+            if (ridge != 0.0) cublasDaxpy(hb, ncols, &mridge, x, 1, r, 1);
             cholesky_solve(L, ncols, r, z, cublas_, stream_);
             CK(cudaMemcpyAsync(pv, z, sizeof(double) * ncols, cudaMemcpyDeviceToDevice, stream_));
             double rz = 0;
             cublasDdot(hb, ncols, r, 1, z, 1, &rz);
             for (int it = 0; it < iters && rz > 0.0; ++it) {
-                // q = A^T (A p)
+                // q = A^T (A p) + ridge p
                 cublasDgemv(hb, CUBLAS_OP_T, ncols, (int)nrows, &one, A, (int)lda, pv, 1, &zero, t, 1);
                 cublasDgemv(hb, CUBLAS_OP_N, ncols, (int)nrows, &one, A, (int)lda, t, 1, &zero, q, 1);
+                if (ridge != 0.0) cublasDaxpy(hb, ncols, &ridge, pv, 1, q, 1);
                 double pq = 0;
                 cublasDdot(hb, ncols, pv, 1, q, 1, &pq);
                 if (!(pq > 0.0)) break;
@@ -665,6 +668,10 @@ void Session::solve(const double* G, const double* h, int ncols, double ridge, c
                 rz = rz_new;
             }
             residual(A, lda, nrows, ncols, b, x, t, r, &rn, &gn, cublas_, stream_);
+            if (ridge != 0.0) {
+                cublasDaxpy(hb, ncols, &mridge, x, 1, r, 1);
+                cublasDnrm2(hb, ncols, r, 1, &gn);
+            }
         }
         CK(cudaStreamSynchronize(stream_));
         if (info) { info[0] = rn; info[1] = gn; info[2] = used; }

@@ -133,11 +133,14 @@ int cg_gram(cg_session* s, int a_precision, const void* A, int64_t lda, int64_t 
             int mode, double* G, double* h);
 int cg_gram_finish(cg_session* s, double* G, int ncols);
 
-/* x = (G + ridge I)^-1 h by FP64 Cholesky (the ridge grows tenfold, at most 8 times,
- * if G + ridge I is not positive definite), then `iters` iterations of conjugate
- * gradients on the exact normal equations A^T A x = A^T b with FP64 products through A,
- * preconditioned by that Cholesky factor (A: FP64 device matrix; may be NULL if
- * iters == 0).  info (host, 3 doubles): ||b - A x||, ||A^T (b - A x)||, ridge used. */
+/* Ridge least squares (A^T A + ridge I) x = A^T b.  First x = (G + r I)^-1 h by FP64
+ * Cholesky with r = ridge (r grows tenfold, at most 8 times, while G + r I is not
+ * positive definite, as a mixed-precision G can be), then `iters` iterations of
+ * conjugate gradients on the FP64 system (A^T A + ridge I) x = A^T b with products
+ * through A, preconditioned by that factor -- so a tensor-core G converges to the
+ * FP64 solution of the same system (A: FP64 device matrix; may be NULL if iters == 0).
+ * info (host, 3 doubles): ||b - A x||, ||A^T (b - A x) - ridge x|| (0 when iters == 0),
+ * and the r of the factorisation. */
 int cg_solve(cg_session* s, const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda,
              int64_t nrows, const double* b, int iters, double* x, double* info);
 
