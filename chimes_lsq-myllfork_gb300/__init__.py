@@ -93,7 +93,10 @@ def lib():
         "cg_md_force_device": (ctypes.c_int, [vp, vp, vp, vp]),
         "cg_md_nve": (ctypes.c_int, [vp, vp, dp, ctypes.c_double, ctypes.c_int, vp, vp, vp, vp]),
         "cg_dframes_positions": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_void_p), i64p]),
+        "cg_dframes_read_positions": (ctypes.c_int, [vp, dp]),
         "cg_md_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
+        "cg_md_serve": (ctypes.c_int, [vp, ctypes.c_int, vp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
+                                       ctypes.c_int, vp, vp, i64p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -101,6 +104,17 @@ def lib():
         fn.argtypes = args
     _lib = L
     return L
+
+
+class MdRequest(ctypes.Structure):
+    _fields_ = [("natoms", ctypes.c_int), ("nsteps", ctypes.c_int), ("arrival", ctypes.c_double),
+                ("types", ctypes.c_void_p), ("xyz", ctypes.c_void_p), ("cell", ctypes.c_void_p),
+                ("v", ctypes.c_void_p), ("xyz_out", ctypes.c_void_p)]
+
+
+class MdResult(ctypes.Structure):
+    _fields_ = [("admitted", ctypes.c_double), ("finished", ctypes.c_double), ("step_ms_sum", ctypes.c_double),
+                ("step_ms_max", ctypes.c_double)]
 
 
 def _check(rc):
@@ -244,6 +258,13 @@ class DeviceFrames:
             _lib.cg_dframes_free(self._h)
             self._h = None
 
+    def read_positions(self):
+        """Current positions (host copy, [natoms, 3])."""
+        _, n = self.positions_ptr()
+        x = np.empty((n, 3), dtype=np.float64)
+        _check(lib().cg_dframes_read_positions(self._h, _ptr(x)))
+        return x
+
     def positions_ptr(self):
         """(device pointer to the 3*natoms positions, natoms)."""
         p, n = ctypes.c_void_p(), ctypes.c_int64()
@@ -340,6 +361,36 @@ class Session:
         _check(lib().cg_md_nve(self._h, dframes._h, _ptr(m), float(dt_fs), int(nsteps), ctypes.c_void_p(int(v_ptr)),
                                ctypes.c_void_p(int(forces_ptr)), ctypes.c_void_p(int(scalars_ptr) or None),
                                ctypes.c_void_p(int(ke_ptr) or None)))
+
+    def md_serve(self, requests, masses, dt_fs=0.2, hbm_budget=150e9, max_batch_atoms=1 << 16,
+                 max_batch_frames=1024, want_step_ms=True):
+        """Continuous-batching NVE serving (cg_md_serve).  requests: list of dicts with
+        types, xyz [n,3], cell [9], v [n,3], nsteps, arrival (s).  Returns (final xyz
+        list, results structured array, step_ms [nreq, max nsteps] or None, batched steps)."""
+        keep = []
+        arr = (MdRequest * len(requests))()
+        outs = []
+        for k, q in enumerate(requests):
+            t = np.ascontiguousarray(q["types"], dtype=np.int32)
+            x = np.ascontiguousarray(q["xyz"], dtype=np.float64)
+            c = np.ascontiguousarray(q["cell"], dtype=np.float64).reshape(9)
+            v = np.ascontiguousarray(q["v"], dtype=np.float64)
+            o = np.zeros_like(x)
+            keep += [t, x, c, v]
+            outs.append(o)
+            arr[k] = MdRequest(len(t), int(q["nsteps"]), float(q.get("arrival", 0.0)), t.ctypes.data, x.ctypes.data,
+                               c.ctypes.data, v.ctypes.data, o.ctypes.data)
+        res = (MdResult * len(requests))()
+        smax = max([int(q["nsteps"]) for q in requests] + [1])
+        step_ms = np.zeros((len(requests), smax)) if want_step_ms else None
+        nb = ctypes.c_int64()
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        _check(lib().cg_md_serve(self._h, len(requests), ctypes.cast(arr, ctypes.c_void_p), _ptr(m), float(dt_fs),
+                                 float(hbm_budget), int(max_batch_atoms), int(max_batch_frames),
+                                 ctypes.cast(res, ctypes.c_void_p), _ptr(step_ms), ctypes.byref(nb)))
+        r = np.array([(x.admitted, x.finished, x.step_ms_sum, x.step_ms_max) for x in res],
+                     dtype=[("admitted", "f8"), ("finished", "f8"), ("step_ms_sum", "f8"), ("step_ms_max", "f8")])
+        return outs, r, step_ms, nb.value
 
     def md_last_counts(self):
         v = [ctypes.c_int64() for _ in range(4)]

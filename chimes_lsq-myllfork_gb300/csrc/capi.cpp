@@ -384,11 +384,46 @@ int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
     });
 }
 
+int cg_md_serve(cg_session* s, int nreq, const cg_md_request* req, const double* mass, double dt_fs,
+                double hbm_budget_bytes, int64_t max_batch_atoms, int max_batch_frames, cg_md_result* results,
+                double* step_ms, int64_t* batch_steps) {
+    return guarded([&] {
+        need(s && (req || nreq == 0) && mass && results && nreq >= 0, "session/requests/mass/results");
+        need(dt_fs > 0.0 && max_batch_atoms > 0 && max_batch_frames > 0 && hbm_budget_bytes > 0.0, "limits");
+        std::vector<cg::MdRequest> rq(nreq);
+        for (int r = 0; r < nreq; ++r) {
+            rq[r].natoms = req[r].natoms; rq[r].nsteps = req[r].nsteps; rq[r].arrival = req[r].arrival;
+            rq[r].types = req[r].types; rq[r].xyz = req[r].xyz; rq[r].cell = req[r].cell; rq[r].v = req[r].v;
+            rq[r].xyz_out = req[r].xyz_out;
+        }
+        cg::MdServeOptions opt;
+        opt.dt = dt_fs / 48.888;   // internal time unit in fs (src/functions.h:44)
+        opt.hbm_budget = hbm_budget_bytes;
+        opt.max_batch_atoms = max_batch_atoms;
+        opt.max_batch_frames = max_batch_frames;
+        std::vector<cg::MdResult> out(nreq);
+        const int64_t nb = s->s->md_serve(rq, mass, opt, out.data(), step_ms);
+        for (int r = 0; r < nreq; ++r) {
+            results[r].admitted = out[r].admitted; results[r].finished = out[r].finished;
+            results[r].step_ms_sum = out[r].step_ms_sum; results[r].step_ms_max = out[r].step_ms_max;
+        }
+        if (batch_steps) *batch_steps = nb;
+    });
+}
+
 int cg_dframes_positions(const cg_dframes* d, double** xyz, int64_t* natoms) {
     return guarded([&] {
         need(d && xyz && natoms, "frames/xyz/natoms");
         *xyz = d->d->xyz;
         *natoms = d->d->natoms_total;
+    });
+}
+
+int cg_dframes_read_positions(const cg_dframes* d, double* xyz_host) {
+    return guarded([&] {
+        need(d && xyz_host, "frames/xyz");
+        cg::cuda_check(cudaMemcpy(xyz_host, d->d->xyz, 3 * d->d->natoms_total * sizeof(double), cudaMemcpyDeviceToHost),
+                       "cudaMemcpy(positions)");
     });
 }
 

@@ -70,20 +70,26 @@ __global__ void k_frame_setup(FramesDev F, int64_t total_ghosts) {
 }
 
 // ---------------------------------------------------------------- neighbour lists
-// One warp per real atom.  Candidates are scanned in ghost-index order, so the
-// lists come out sorted and the fill pass is deterministic.
-__global__ void k_neigh(ModelDev M, FramesDev F, NeighDev NB, int fill) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// One block of NEIGH_WARPS warps per real atom; warp w scans the w-th contiguous
+// slice of the ghost indices, so the concatenated lists come out in ghost-index
+// order and the fill pass is deterministic.  The fill pass recounts each slice to
+// place it after the slices before it.
+constexpr int NEIGH_WARPS = 8;
+
+__global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDev F, NeighDev NB, int fill) {
+    __shared__ int sc[3][NEIGH_WARPS];
+    const int atom = blockIdx.x;
+    const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    if (warp >= NB.n_real) return;
+    if (atom >= NB.n_real) return;
     int lo = 0, hi = F.nframes - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        if (F.atom_ofs[mid] <= warp) lo = mid; else hi = mid - 1;
+        if (F.atom_ofs[mid] <= atom) lo = mid; else hi = mid - 1;
     }
     const int f = lo;
     const int N = F.natoms[f];
-    const int i = warp - (int)F.atom_ofs[f];
+    const int i = atom - (int)F.atom_ofs[f];
     const int G = N * F.nimg;
     const int64_t gbase = F.ghost_ofs[f];
     const BoxDev& B = F.box[f];
@@ -93,43 +99,59 @@ __global__ void k_neigh(ModelDev M, FramesDev F, NeighDev NB, int fill) {
     const double* si = F.scaled + 3 * (gbase + i);
     const float maxall = (float)fmax(fmax(M.maxcut2, M.order3 > 0 ? M.maxcut3 : 0.0), M.order4 > 0 ? M.maxcut4 : 0.0);
     const float pre = maxall + MARGIN;
-    int64_t o2 = 0, o3 = 0, o4 = 0;
-    if (fill) { o2 = NB.ofs2[warp]; o3 = NB.ofs3[warp]; o4 = NB.ofs4[warp]; }
+    const int per = ((G + NEIGH_WARPS - 1) / NEIGH_WARPS + 31) & ~31;
+    const int g0 = w * per, g1 = min(G, g0 + per);
+    const unsigned lt = (1u << lane) - 1u;
+    auto sweep = [&](bool write, int64_t o2, int64_t o3, int64_t o4, int& c2, int& c3, int& c4) {
+        for (int base = g0; base < g1; base += 32) {
+            const int g = base + lane;
+            bool in2 = false, in3 = false, in4 = false;
+            double r = 0, rab[3] = {0, 0, 0};
+            int pt = 0;
+            if (g < g1 && g != i && (B.small || i <= g % N)) {
+                float4 cg = reinterpret_cast<const float4*>(F.cart32)[gbase + g];
+                float dx = cg.x - ci.x, dy = cg.y - ci.y, dz = cg.z - ci.z;
+                float r32 = sqrtf(dx * dx + dy * dy + dz * dz);
+                if (r32 < pre) {
+                    r = dist_exact(B.h, si, F.scaled + 3 * (gbase + g), rab);
+                    pt = M.int_pair_map[ti * M.natmtyp + typ[g % N]];
+                    const PairDev P = M.pairs[pt];
+                    in2 = M.order2 > 0 && r < P.smax && (NB.md || r > P.smin);
+                    in3 = M.order3 > 0 && r < M.maxcut3;
+                    in4 = M.order4 > 0 && r < M.maxcut4;
+                }
+            }
+            const unsigned b2 = __ballot_sync(0xffffffffu, in2);
+            const unsigned b3 = __ballot_sync(0xffffffffu, in3);
+            const unsigned b4 = __ballot_sync(0xffffffffu, in4);
+            if (write) {
+                if (in2) {
+                    const int64_t p = o2 + c2 + __popc(b2 & lt);
+                    NB.i2[p] = i; NB.g2[p] = g; NB.pt2[p] = pt; NB.r2[p] = r;
+                    NB.rab2[3 * p] = rab[0]; NB.rab2[3 * p + 1] = rab[1]; NB.rab2[3 * p + 2] = rab[2];
+                }
+                if (in3) { const int64_t p = o3 + c3 + __popc(b3 & lt); NB.g3[p] = g; NB.r3[p] = r; }
+                if (in4) { const int64_t p = o4 + c4 + __popc(b4 & lt); NB.g4[p] = g; NB.r4[p] = r; }
+            }
+            c2 += __popc(b2); c3 += __popc(b3); c4 += __popc(b4);
+        }
+    };
     int c2 = 0, c3 = 0, c4 = 0;
-    for (int base = 0; base < G; base += 32) {
-        const int g = base + lane;
-        bool in2 = false, in3 = false, in4 = false;
-        double r = 0, rab[3] = {0, 0, 0};
-        int pt = 0;
-        if (g < G && g != i && (B.small || i <= g % N)) {
-            float4 cg = reinterpret_cast<const float4*>(F.cart32)[gbase + g];
-            float dx = cg.x - ci.x, dy = cg.y - ci.y, dz = cg.z - ci.z;
-            float r32 = sqrtf(dx * dx + dy * dy + dz * dz);
-            if (r32 < pre) {
-                r = dist_exact(B.h, si, F.scaled + 3 * (gbase + g), rab);
-                pt = M.int_pair_map[ti * M.natmtyp + typ[g % N]];
-                const PairDev P = M.pairs[pt];
-                in2 = M.order2 > 0 && r < P.smax && (NB.md || r > P.smin);
-                in3 = M.order3 > 0 && r < M.maxcut3;
-                in4 = M.order4 > 0 && r < M.maxcut4;
-            }
+    sweep(false, 0, 0, 0, c2, c3, c4);
+    if (lane == 0) { sc[0][w] = c2; sc[1][w] = c3; sc[2][w] = c4; }
+    __syncthreads();
+    if (!fill) {
+        if (threadIdx.x == 0) {
+            int t2 = 0, t3 = 0, t4 = 0;
+            for (int k = 0; k < NEIGH_WARPS; ++k) { t2 += sc[0][k]; t3 += sc[1][k]; t4 += sc[2][k]; }
+            NB.cnt2[atom] = t2; NB.cnt3[atom] = t3; NB.cnt4[atom] = t4;
         }
-        const unsigned lt = (1u << lane) - 1u;
-        unsigned b2 = __ballot_sync(0xffffffffu, in2);
-        unsigned b3 = __ballot_sync(0xffffffffu, in3);
-        unsigned b4 = __ballot_sync(0xffffffffu, in4);
-        if (fill) {
-            if (in2) {
-                int64_t p = o2 + c2 + __popc(b2 & lt);
-                NB.i2[p] = i; NB.g2[p] = g; NB.pt2[p] = pt; NB.r2[p] = r;
-                NB.rab2[3 * p] = rab[0]; NB.rab2[3 * p + 1] = rab[1]; NB.rab2[3 * p + 2] = rab[2];
-            }
-            if (in3) { int64_t p = o3 + c3 + __popc(b3 & lt); NB.g3[p] = g; NB.r3[p] = r; }
-            if (in4) { int64_t p = o4 + c4 + __popc(b4 & lt); NB.g4[p] = g; NB.r4[p] = r; }
-        }
-        c2 += __popc(b2); c3 += __popc(b3); c4 += __popc(b4);
+        return;
     }
-    if (!fill && lane == 0) { NB.cnt2[warp] = c2; NB.cnt3[warp] = c3; NB.cnt4[warp] = c4; }
+    int64_t o2 = NB.ofs2[atom], o3 = NB.ofs3[atom], o4 = NB.ofs4[atom];
+    for (int k = 0; k < w; ++k) { o2 += sc[0][k]; o3 += sc[1][k]; o4 += sc[2][k]; }
+    int d2 = 0, d3 = 0, d4 = 0;
+    sweep(true, o2, o3, o4, d2, d3, d4);
 }
 
 // ---------------------------------------------------------------- clusters
@@ -218,6 +240,87 @@ __global__ void k_clusters(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, 
             CS.type[p] = T;
         }
         count += __popc(bal);
+    }
+    if (!fill && lane == 0) CS.cnt[warp] = count;
+}
+
+// Quadruplets in two stages (same accepted set as k_clusters<4>, different but fixed
+// order): the lanes first test (j, k) pairs -- distinct, parent-ordered, r_jk under
+// the largest 4-body cut-off -- and the surviving pairs of each chunk of 32 are then
+// crossed with every l, flattened over the lanes, with the full per-slot tests.
+__global__ void k_quads(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int fill) {
+    __shared__ int2 sPair[8][32];
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int wib = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= NB.n_real) return;
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (F.atom_ofs[mid] <= warp) lo = mid; else hi = mid - 1;
+    }
+    const int f = lo;
+    const int N = F.natoms[f];
+    const int i = warp - (int)F.atom_ofs[f];
+    const int64_t gbase = F.ghost_ofs[f];
+    const BoxDev& B = F.box[f];
+    const int* typ = F.type + F.atom_ofs[f];
+    const float4* c32 = reinterpret_cast<const float4*>(F.cart32);
+    const int* lg = NB.g4 + NB.ofs4[warp];
+    const double* lr = NB.r4 + NB.ofs4[warp];
+    const int n = NB.cnt4[warp];
+    const bool ordered = !B.small;
+    const int ti = typ[i];
+    const float cut = (float)M.maxcut4 + MARGIN;
+    int64_t out = fill ? CS.ofs[warp] : 0;
+    int count = 0;
+    const int npairs = n * n;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int pb = 0; pb < npairs; pb += 32) {
+        const int p = pb + lane;
+        bool pv = false;
+        int a = 0, b = 0;
+        if (p < npairs) {
+            a = p / n; b = p - a * n;
+            const int j = lg[a], k = lg[b];
+            pv = (j != k) && !(ordered && (j % N) > (k % N)) && dist32(c32, gbase + j, gbase + k) < cut;
+        }
+        const unsigned pbal = __ballot_sync(0xffffffffu, pv);
+        if (pv) sPair[wib][__popc(pbal & lt)] = make_int2(a, b);
+        __syncwarp();
+        const int work = __popc(pbal) * n;
+        for (int tb = 0; tb < work; tb += 32) {
+            const int t = tb + lane;
+            bool ok = false;
+            int j = -1, k = -1, l = -1, T = -1;
+            if (t < work) {
+                const int pi = t / n, c = t - pi * n;
+                const int2 ab = sPair[wib][pi];
+                j = lg[ab.x]; k = lg[ab.y]; l = lg[c];
+                ok = (j != l) && (k != l) && !(ordered && (k % N) > (l % N));
+                if (ok) {
+                    const int id = (ti + 1) + 10 * (typ[j % N] + 1) + 100 * (typ[k % N] + 1) + 1000 * (typ[l % N] + 1);
+                    T = M.int_map4[id];
+                    ok = T >= 0;
+                    if (ok) {
+                        const ClusterTypeDev& CT = M.types4[T];
+                        const int8_t* pm = M.pidx4 + id * 6;
+                        ok = lr[ab.x] < CT.smax[pm[0]] && lr[ab.y] < CT.smax[pm[1]] && lr[c] < CT.smax[pm[2]] &&
+                             within(F, B, gbase, j, k, CT.smax[pm[3]], dist32(c32, gbase + j, gbase + k)) &&
+                             within(F, B, gbase, j, l, CT.smax[pm[4]], dist32(c32, gbase + j, gbase + l)) &&
+                             within(F, B, gbase, k, l, CT.smax[pm[5]], dist32(c32, gbase + k, gbase + l));
+                    }
+                }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, ok);
+            if (fill && ok) {
+                const int64_t q = out + count + __popc(bal & lt);
+                CS.m[q] = make_int4(i, j, k, l);
+                CS.type[q] = T;
+            }
+            count += __popc(bal);
+        }
+        __syncwarp();
     }
     if (!fill && lane == 0) CS.cnt[warp] = count;
 }
@@ -311,14 +414,14 @@ void launch_frame_setup(const FramesDev& F, int64_t n, cudaStream_t st) {
     if (n > 0) k_frame_setup<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, n);
 }
 void launch_neigh(const ModelDev& M, const FramesDev& F, const NeighDev& NB, int fill, cudaStream_t st) {
-    if (NB.n_real > 0) k_neigh<<<(unsigned)((NB.n_real + 7) / 8), 256, 0, st>>>(M, F, NB, fill);
+    if (NB.n_real > 0) k_neigh<<<(unsigned)NB.n_real, 32 * NEIGH_WARPS, 0, st>>>(M, F, NB, fill);
 }
 void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const NeighDev& NB, const ClusterSet& CS,
                      int fill, cudaStream_t st) {
     if (NB.n_real <= 0) return;
     const unsigned g = (unsigned)((NB.n_real + 7) / 8);
     if (nbody == 3) k_clusters<3><<<g, 256, 0, st>>>(M, F, NB, CS, fill);
-    else k_clusters<4><<<g, 256, 0, st>>>(M, F, NB, CS, fill);
+    else k_quads<<<g, 256, 0, st>>>(M, F, NB, CS, fill);
 }
 void launch_bucket(int nframes, const FramesDev& F, const BucketSpec& S, const Buckets& out, cudaStream_t st) {
     if (nframes > 0) k_bucket<<<nframes, BUCKET_THREADS, 0, st>>>(F, S, out);

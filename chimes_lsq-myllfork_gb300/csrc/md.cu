@@ -19,6 +19,7 @@
 // the power-tuple loop.  One thread owns one cluster; a block shares one
 // (frame, cluster type) bucket, so C sits in shared memory and every read of it
 // is a broadcast.
+#include <algorithm>
 #include <cstdio>
 
 #include "basis.cuh"
@@ -26,7 +27,7 @@
 
 namespace cgd {
 
-constexpr int MDC_THREADS = 128;
+constexpr int MDC_THREADS = MDC_TILE;
 
 __device__ __forceinline__ int frame_of_atom(const FramesDev& F, int64_t a) {
     int lo = 0, hi = F.nframes - 1;
@@ -142,6 +143,98 @@ __global__ void __launch_bounds__(256) k_md2(ModelDev M, MdDev D, FramesDev F, N
             atomicAdd(so + 8, v[4]); atomicAdd(so + 9, v[6]); atomicAdd(so + 10, v[7]);
         }
     }
+}
+
+// ------------------------------------------------------------------ grouping
+__device__ __forceinline__ int frame_of_cluster(const int64_t* cfo, int nframes, int64_t q) {
+    int lo = 0, hi = nframes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (cfo[mid] <= q) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Warp-aggregated increment: one atomic per distinct key in the warp; returns the
+// slot of this lane (order among equal keys within the warp by lane).
+__device__ __forceinline__ int warp_agg_inc(int* ctr, int key, bool active) {
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    int slot = 0;
+    if (active) {
+        const unsigned peers = __match_any_sync(act, key);
+        const int leader = __ffs(peers) - 1;
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(ctr + key, __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        slot = base + __popc(peers & ((1u << lane) - 1u));
+    }
+    return slot;
+}
+
+__global__ void k_md_bucket_count(int64_t n, int nframes, const int64_t* cfo, const int* type, int ntypes,
+                                  int* cnt) {
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = base + threadIdx.x;
+        const bool ok = q < n;
+        const int key = ok ? frame_of_cluster(cfo, nframes, q) * ntypes + type[q] : 0;
+        warp_agg_inc(cnt, key, ok);
+    }
+}
+
+// Single block: start[] = exclusive scan of the counts, tile_ofs[] = exclusive scan
+// of ceil(count / MDC_TILE).
+__global__ void k_md_bucket_scan(const int* cnt, int nkeys, int64_t* start, int* tile_ofs) {
+    __shared__ int64_t ps[1024];
+    __shared__ int pt[1024];
+    const int per = (nkeys + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(nkeys, b + per);
+    int64_t s = 0;
+    int t = 0;
+    for (int i = b; i < e; ++i) { s += cnt[i]; t += (cnt[i] + MDC_TILE - 1) / MDC_TILE; }
+    ps[threadIdx.x] = s;
+    pt[threadIdx.x] = t;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        int64_t vs = threadIdx.x >= (unsigned)off ? ps[threadIdx.x - off] : 0;
+        int vt = threadIdx.x >= (unsigned)off ? pt[threadIdx.x - off] : 0;
+        __syncthreads();
+        ps[threadIdx.x] += vs;
+        pt[threadIdx.x] += vt;
+        __syncthreads();
+    }
+    int64_t rs = ps[threadIdx.x] - s;
+    int rt = pt[threadIdx.x] - t;
+    for (int i = b; i < e; ++i) {
+        start[i] = rs; tile_ofs[i] = rt;
+        rs += cnt[i]; rt += (cnt[i] + MDC_TILE - 1) / MDC_TILE;
+    }
+    if (threadIdx.x == blockDim.x - 1) { start[nkeys] = ps[threadIdx.x]; tile_ofs[nkeys] = pt[threadIdx.x]; }
+}
+
+__global__ void k_md_bucket_fill(int64_t n, int nframes, const int64_t* cfo, const int* type, int ntypes,
+                                 const int64_t* start, int* cursor, int* val) {
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = base + threadIdx.x;
+        const bool ok = q < n;
+        const int key = ok ? frame_of_cluster(cfo, nframes, q) * ntypes + type[q] : 0;
+        const int slot = warp_agg_inc(cursor, key, ok);
+        if (ok) val[start[key] + slot] = (int)q;
+    }
+}
+
+// Tile -> (key, first grouped cluster); false when the tile is past the last one.
+__device__ __forceinline__ bool tile_lookup(const MdBuckets& B, int tile, int& key, int64_t& c0, int64_t& c1) {
+    if (tile >= B.tile_ofs[B.nkeys]) return false;
+    int lo = 0, hi = B.nkeys - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (B.tile_ofs[mid] <= tile) lo = mid; else hi = mid - 1;
+    }
+    key = lo;
+    c0 = B.start[key] + (int64_t)(tile - B.tile_ofs[key]) * MDC_TILE;
+    c1 = B.start[key + 1];
+    return c0 < c1;
 }
 
 // ------------------------------------------------------------------ clusters
@@ -281,20 +374,18 @@ __device__ __forceinline__ void cluster_geom(const ModelDev& M, const FramesDev&
 }
 
 template <int NBODY, int O, typename R>
-__global__ void __launch_bounds__(MDC_THREADS) k_mdc(ModelDev M, MdDev D, FramesDev F, ClusterSet CS, Buckets byt,
-                                                     const int64_t* kfo, double* Fo, double* So) {
+__global__ void __launch_bounds__(MDC_THREADS) k_mdc(ModelDev M, MdDev D, FramesDev F, ClusterSet CS, MdBuckets MB,
+                                                     double* Fo, double* So) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
     constexpr int SZ = IPow<NP, O>::v;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* sC = reinterpret_cast<R*>(smem_raw);
     SlotGeom* sG = reinterpret_cast<SlotGeom*>(smem_raw + ((SZ * sizeof(R) + 15) & ~size_t(15)));
-    const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
-    const int f = blockIdx.x / ntypes;
-    const int T = blockIdx.x % ntypes;
-    const int64_t kb = kfo[f];
-    const int64_t t0 = byt.key_ofs[kb + T], t1 = byt.key_ofs[kb + T + 1];
-    const int64_t cb = t0 + (int64_t)blockIdx.y * blockDim.x;
-    if (cb >= t1) return;
+    int key;
+    int64_t cb, t1;
+    if (!tile_lookup(MB, blockIdx.x, key, cb, t1)) return;
+    const int f = key / MB.ntypes;
+    const int T = key % MB.ntypes;
     const R* Cg = (NBODY == 3 ? (sizeof(R) == 8 ? (const R*)D.C3 : (const R*)D.C3f)
                               : (sizeof(R) == 8 ? (const R*)D.C4 : (const R*)D.C4f)) + (size_t)T * SZ;
     for (int i = threadIdx.x; i < SZ; i += blockDim.x) sC[i] = Cg[i];
@@ -308,8 +399,7 @@ __global__ void __launch_bounds__(MDC_THREADS) k_mdc(ModelDev M, MdDev D, Frames
         const BoxDev& B = F.box[f];
         const double perm = NBODY == 3 ? B.perm3 : B.perm4;
         const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
-        const int64_t q = CS.ofs[aofs] + byt.val[c];
-        const int4 mm = CS.m[q];
+        const int4 mm = CS.m[MB.val[c]];
         SlotGeom* sg = sG + (size_t)threadIdx.x * NP;
         cluster_geom<NBODY>(M, F, f, mm, sg);
         R u[NP][O], G[NP][O];
@@ -370,17 +460,14 @@ constexpr int MDG_MAXO = 16;
 
 template <int NBODY>
 __global__ void __launch_bounds__(MDC_THREADS) k_mdc_generic(ModelDev M, MdDev D, FramesDev F, ClusterSet CS,
-                                                             Buckets byt, const int64_t* kfo, int O, double* Fo,
-                                                             double* So) {
+                                                             MdBuckets MB, int O, double* Fo, double* So) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
     __shared__ SlotGeom sG[MDC_THREADS * NP];
-    const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
-    const int f = blockIdx.x / ntypes;
-    const int T = blockIdx.x % ntypes;
-    const int64_t kb = kfo[f];
-    const int64_t t0 = byt.key_ofs[kb + T], t1 = byt.key_ofs[kb + T + 1];
-    const int64_t cb = t0 + (int64_t)blockIdx.y * blockDim.x;
-    if (cb >= t1) return;
+    int key;
+    int64_t cb, t1;
+    if (!tile_lookup(MB, blockIdx.x, key, cb, t1)) return;
+    const int f = key / MB.ntypes;
+    const int T = key % MB.ntypes;
     int SZ = 1;
     for (int k = 0; k < NP; ++k) SZ *= O;
     const double* C = (NBODY == 3 ? D.C3 : D.C4) + (size_t)T * SZ;
@@ -392,8 +479,7 @@ __global__ void __launch_bounds__(MDC_THREADS) k_mdc_generic(ModelDev M, MdDev D
         const BoxDev& B = F.box[f];
         const double perm = NBODY == 3 ? B.perm3 : B.perm4;
         const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
-        const int64_t q = CS.ofs[aofs] + byt.val[c];
-        const int4 mm = CS.m[q];
+        const int4 mm = CS.m[MB.val[c]];
         SlotGeom* sg = sG + (size_t)threadIdx.x * NP;
         cluster_geom<NBODY>(M, F, f, mm, sg);
         double u[NP][MDG_MAXO], h[NP][MDG_MAXO], G[NP][MDG_MAXO];
@@ -463,16 +549,19 @@ __global__ void k_md_finalize(ModelDev M, MdDev D, FramesDev F, double* So) {
 }
 
 // ------------------------------------------------------------------ integration
-__global__ void k_md_drift(int64_t n3, double* x, double* v, const double* a, double dt) {
+__global__ void k_md_drift(FramesDev F, const unsigned char* first, int64_t n3, double* x, double* v, const double* a,
+                           double dt) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n3) return;
+    if (first && first[frame_of_atom(F, i / 3)]) return;   // a frame's step 0 only evaluates forces
     x[i] += v[i] * dt + 0.5 * a[i] * dt * dt;
     v[i] = v[i] + 0.5 * a[i] * dt;
 }
 
 __global__ void k_md_kick(FramesDev F, const double* Fo, const double* inv_mass_type, const double* mass_type,
-                          double* acc, double* v, double dt, int half, double* ke) {
+                          double* acc, double* v, double dt, int half, const unsigned char* first, double* ke) {
     const int f = blockIdx.x;
+    if (first && first[f]) half = 0;
     const int N = F.natoms[f];
     const int64_t aofs = F.atom_ofs[f];
     double k = 0.0;
@@ -510,22 +599,39 @@ void launch_md2(const ModelDev& M, const MdDev& D, const FramesDev& F, const Nei
     k_md2<<<(unsigned)blocks, threads, 0, st>>>(M, D, F, NB, Fo, So);
 }
 
+void launch_md_bucket(int64_t n, int nframes, const int64_t* cfo, const int* type, const MdBuckets& B,
+                      cudaStream_t st) {
+    if (n <= 0) return;
+    int* cnt = B.cursor;   // counts first, then reused as fill cursors
+    cudaMemsetAsync(cnt, 0, sizeof(int) * B.nkeys, st);
+    const int blocks = (int)std::min<int64_t>(4 * 152, (n + 255) / 256);
+    k_md_bucket_count<<<blocks, 256, 0, st>>>(n, nframes, cfo, type, B.ntypes, cnt);
+    k_md_bucket_scan<<<1, 1024, 0, st>>>(cnt, B.nkeys, B.start, B.tile_ofs);
+    cudaMemsetAsync(B.cursor, 0, sizeof(int) * B.nkeys, st);
+    k_md_bucket_fill<<<blocks, 256, 0, st>>>(n, nframes, cfo, type, B.ntypes, B.start, B.cursor, B.val);
+}
+
 template <int NBODY, int O, typename R>
-static void run_mdc(dim3 grid, const ModelDev& M, const MdDev& D, const FramesDev& F, const ClusterSet& CS,
-                    const Buckets& byt, const int64_t* kfo, double* Fo, double* So, cudaStream_t st) {
+static void run_mdc(unsigned grid, const ModelDev& M, const MdDev& D, const FramesDev& F, const ClusterSet& CS,
+                    const MdBuckets& B, double* Fo, double* So, cudaStream_t st) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
     const size_t smem = ((IPow<NP, O>::v * sizeof(R) + 15) & ~size_t(15)) + sizeof(SlotGeom) * NP * MDC_THREADS;
-    cudaFuncSetAttribute(k_mdc<NBODY, O, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_mdc<NBODY, O, R><<<grid, MDC_THREADS, smem, st>>>(M, D, F, CS, byt, kfo, Fo, So);
+    static thread_local int attr_dev = -1;   // the attribute is per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (attr_dev != dev) {
+        cudaFuncSetAttribute(k_mdc<NBODY, O, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_dev = dev;
+    }
+    k_mdc<NBODY, O, R><<<grid, MDC_THREADS, smem, st>>>(M, D, F, CS, B, Fo, So);
 }
 
 template <int NBODY, typename R>
-static bool dispatch_mdc(int order, dim3 grid, const ModelDev& M, const MdDev& D, const FramesDev& F,
-                         const ClusterSet& CS, const Buckets& byt, const int64_t* kfo, double* Fo, double* So,
-                         cudaStream_t st) {
-#define MDC_CASE(O)                                                   \
-    case O:                                                           \
-        run_mdc<NBODY, O, R>(grid, M, D, F, CS, byt, kfo, Fo, So, st); \
+static bool dispatch_mdc(int order, unsigned grid, const ModelDev& M, const MdDev& D, const FramesDev& F,
+                         const ClusterSet& CS, const MdBuckets& B, double* Fo, double* So, cudaStream_t st) {
+#define MDC_CASE(O)                                          \
+    case O:                                                  \
+        run_mdc<NBODY, O, R>(grid, M, D, F, CS, B, Fo, So, st); \
         return true;
     if constexpr (NBODY == 3) {
         switch (order) { MDC_CASE(2) MDC_CASE(3) MDC_CASE(4) MDC_CASE(5) MDC_CASE(6) MDC_CASE(7) MDC_CASE(8) }
@@ -536,21 +642,21 @@ static bool dispatch_mdc(int order, dim3 grid, const ModelDev& M, const MdDev& D
     return false;
 }
 
-void launch_mdc(int nbody, int prec, int nframes, int ntypes, int order, int max_bucket, const ModelDev& M,
-                const MdDev& D, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
-                const int64_t* key_frame_ofs, double* Fo, double* So, cudaStream_t st) {
-    if (max_bucket <= 0 || nframes * ntypes == 0) return;
-    dim3 grid((unsigned)(nframes * ntypes), (unsigned)((max_bucket + MDC_THREADS - 1) / MDC_THREADS));
+void launch_mdc(int nbody, int prec, int order, int64_t max_tiles, const ModelDev& M, const MdDev& D,
+                const FramesDev& F, const ClusterSet& CS, const MdBuckets& B, double* Fo, double* So,
+                cudaStream_t st) {
+    if (max_tiles <= 0) return;
+    const unsigned grid = (unsigned)max_tiles;
     bool done;
     if (nbody == 3)
-        done = prec == 1 ? dispatch_mdc<3, float>(order, grid, M, D, F, CS, byt, key_frame_ofs, Fo, So, st)
-                         : dispatch_mdc<3, double>(order, grid, M, D, F, CS, byt, key_frame_ofs, Fo, So, st);
+        done = prec == 1 ? dispatch_mdc<3, float>(order, grid, M, D, F, CS, B, Fo, So, st)
+                         : dispatch_mdc<3, double>(order, grid, M, D, F, CS, B, Fo, So, st);
     else
-        done = prec == 1 ? dispatch_mdc<4, float>(order, grid, M, D, F, CS, byt, key_frame_ofs, Fo, So, st)
-                         : dispatch_mdc<4, double>(order, grid, M, D, F, CS, byt, key_frame_ofs, Fo, So, st);
+        done = prec == 1 ? dispatch_mdc<4, float>(order, grid, M, D, F, CS, B, Fo, So, st)
+                         : dispatch_mdc<4, double>(order, grid, M, D, F, CS, B, Fo, So, st);
     if (done) return;
-    if (nbody == 3) k_mdc_generic<3><<<grid, MDC_THREADS, 0, st>>>(M, D, F, CS, byt, key_frame_ofs, order, Fo, So);
-    else k_mdc_generic<4><<<grid, MDC_THREADS, 0, st>>>(M, D, F, CS, byt, key_frame_ofs, order, Fo, So);
+    if (nbody == 3) k_mdc_generic<3><<<grid, MDC_THREADS, 0, st>>>(M, D, F, CS, B, order, Fo, So);
+    else k_mdc_generic<4><<<grid, MDC_THREADS, 0, st>>>(M, D, F, CS, B, order, Fo, So);
 }
 
 void launch_md_finalize(int nframes, const ModelDev& M, const MdDev& D, const FramesDev& F, double* So,
@@ -558,14 +664,17 @@ void launch_md_finalize(int nframes, const ModelDev& M, const MdDev& D, const Fr
     if (nframes > 0) k_md_finalize<<<nframes, 256, 0, st>>>(M, D, F, So);
 }
 
-void launch_md_drift(int64_t natoms, double* xyz, double* v, const double* acc, double dt, cudaStream_t st) {
+void launch_md_drift(int64_t natoms, const FramesDev& F, const unsigned char* first, double* xyz, double* v,
+                     const double* acc, double dt, cudaStream_t st) {
     const int64_t n3 = 3 * natoms;
-    if (n3 > 0) k_md_drift<<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(n3, xyz, v, acc, dt);
+    if (n3 > 0) k_md_drift<<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(F, first, n3, xyz, v, acc, dt);
 }
 
 void launch_md_kick(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
-                    const double* mass_type, double* acc, double* v, double dt, int half, double* ke, cudaStream_t st) {
-    if (nframes > 0) k_md_kick<<<nframes, 256, 0, st>>>(F, Fo, inv_mass_type, mass_type, acc, v, dt, half, ke);
+                    const double* mass_type, double* acc, double* v, double dt, int half, const unsigned char* first,
+                    double* ke, cudaStream_t st) {
+    if (nframes > 0)
+        k_md_kick<<<nframes, 256, 0, st>>>(F, Fo, inv_mass_type, mass_type, acc, v, dt, half, first, ke);
 }
 
 }  // namespace cgd

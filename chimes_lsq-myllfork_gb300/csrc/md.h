@@ -28,25 +28,43 @@ struct MdDev {
     double pen_dist, pen_scale;   // 2-body penalty (src/chimes_md.C:1747-1748 defaults)
 };
 
+// Clusters grouped by key = frame * ntypes + type for the contraction kernels: the
+// order inside a group is not fixed (the forces are accumulated with atomics).
+struct MdBuckets {
+    int nkeys, ntypes;
+    int64_t* start;       // [nkeys + 1] first grouped cluster of each key
+    int* tile_ofs;        // [nkeys + 1] first MDC tile (block) of each key
+    int* cursor;          // [nkeys] fill cursors
+    int* val;             // [n] global cluster indices, grouped
+};
+constexpr int MDC_TILE = 128;   // clusters per contraction block
+
+// Group n clusters of a batch (cluster frame offsets cfo) by (frame, type).
+void launch_md_bucket(int64_t n, int nframes, const int64_t* cfo, const int* type, const MdBuckets& B,
+                      cudaStream_t st);
+
 // Orders with an unrolled contraction kernel; others use the generic kernel.
 bool md_fast_order(int nbody, int order);
 
 void launch_md2(const ModelDev& M, const MdDev& D, const FramesDev& F, const NeighDev& NB, double* Fo, double* So,
                 cudaStream_t st);
-// Clusters of one body count, grouped by (frame, type) buckets; grid.y covers the
-// largest bucket.
-void launch_mdc(int nbody, int prec, int nframes, int ntypes, int order, int max_bucket, const ModelDev& M,
-                const MdDev& D, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
-                const int64_t* key_frame_ofs, double* Fo, double* So, cudaStream_t st);
+// Clusters of one body count, one block per tile of a (frame, type) group; max_tiles
+// bounds the number of tiles (n / MDC_TILE + nkeys).
+void launch_mdc(int nbody, int prec, int order, int64_t max_tiles, const ModelDev& M, const MdDev& D,
+                const FramesDev& F, const ClusterSet& CS, const MdBuckets& B, double* Fo, double* So,
+                cudaStream_t st);
 void launch_md_finalize(int nframes, const ModelDev& M, const MdDev& D, const FramesDev& F, double* So,
                         cudaStream_t st);
 
 // Velocity Verlet (CONSTRAINT::UPDATE_COORDS / UPDATE_VELOCS_HALF_1 / _2,
 // src/ClassDefs.C:870-900, 1088-1157) over every real atom of the batch.
 // drift: x += v dt + a dt^2 / 2, v += a dt / 2.   kick: a = F / m, v += a dt / 2,
-// kinetic energy per frame into ke[f] (when ke is not null).
-void launch_md_drift(int64_t natoms, double* xyz, double* v, const double* acc, double dt, cudaStream_t st);
+// kinetic energy per frame into ke[f] (when ke is not null).  first (per frame, may
+// be null): frames at their step 0, which neither drift nor kick.
+void launch_md_drift(int64_t natoms, const FramesDev& F, const unsigned char* first, double* xyz, double* v,
+                     const double* acc, double dt, cudaStream_t st);
 void launch_md_kick(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
-                    const double* mass_type, double* acc, double* v, double dt, int half, double* ke, cudaStream_t st);
+                    const double* mass_type, double* acc, double* v, double dt, int half, const unsigned char* first,
+                    double* ke, cudaStream_t st);
 
 }  // namespace cgd

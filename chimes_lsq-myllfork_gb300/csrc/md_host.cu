@@ -7,7 +7,10 @@
 // neighbour lists, clusters, per-(frame, type) buckets) followed by the force
 // kernels of md.cu.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstring>
+#include <thread>
 #include <vector>
 
 #include "assemble.h"
@@ -115,40 +118,46 @@ void Session::md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts*
     c.pairs2 = tot[0];
     cgd::launch_md2(M, D, F, NB, Fo, So, st); L();
     CK(cudaGetLastError());
-    int64_t* kfo_atoms = S.get<int64_t>(nf + 1);
-    cgd::launch_key_frame_ofs(F.atom_ofs, nf, 0, kfo_atoms, st); L();
-    auto many = [&](int nbody, int ntypes, int ord) {
-        cgd::ClusterSet CS{};
-        CS.cnt = S.get<int>(nreal);
-        CS.ofs = S.get<int64_t>(nreal + 1);
-        cgd::launch_clusters(nbody, M, F, NB, CS, 0, st); L();
-        cgd::launch_scan_counts(CS.cnt, nreal, CS.ofs, st); L();
-        int64_t n = 0;
-        CK(cudaMemcpyAsync(&n, CS.ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        (nbody == 3 ? c.triplets : c.quads) = n;
-        if (n == 0) return;
+    // clusters: count both body counts, then one host read of the totals
+    cgd::ClusterSet CS3{}, CS4{};
+    int64_t ncl[2] = {0, 0};
+    const bool use[2] = {M.order3 > 0, M.order4 > 0};
+    cgd::ClusterSet* css[2] = {&CS3, &CS4};
+    for (int k = 0; k < 2; ++k) {
+        if (!use[k]) continue;
+        css[k]->cnt = S.get<int>(nreal);
+        css[k]->ofs = S.get<int64_t>(nreal + 1);
+        cgd::launch_clusters(3 + k, M, F, NB, *css[k], 0, st); L();
+        cgd::launch_scan_counts(css[k]->cnt, nreal, css[k]->ofs, st); L();
+        CK(cudaMemcpyAsync(&ncl[k], css[k]->ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    }
+    if (use[0] || use[1]) CK(cudaStreamSynchronize(st));
+    c.triplets = ncl[0];
+    c.quads = ncl[1];
+    for (int k = 0; k < 2; ++k) {
+        const int64_t n = ncl[k];
+        if (!use[k] || n == 0) continue;
+        const int nbody = 3 + k;
+        const int ntypes = k == 0 ? M.ntypes3 : M.ntypes4;
+        cgd::ClusterSet& CS = *css[k];
         CS.m = S.get<int4>(n);
         CS.type = S.get<int>(n);
         cgd::launch_clusters(nbody, M, F, NB, CS, 1, st); L();
         int64_t* cfo = S.get<int64_t>(nf + 1);
         cgd::launch_gather_frame_ofs(CS.ofs, F.atom_ofs, nf, cfo, st); L();
-        int64_t* kfo = S.get<int64_t>(nf + 1);
-        cgd::launch_key_frame_ofs(F.atom_ofs, nf, ntypes, kfo, st); L();
-        cgd::Buckets byt{S.get<int64_t>((int64_t)nf * (ntypes + 1)), S.get<int>(n)};
-        cgd::BucketSpec spec{2, 1, cfo, kfo, nullptr, nullptr, nullptr, CS.type};
-        cgd::launch_bucket(nf, F, spec, byt, st); L();
-        int* dmax = S.get<int>(1);
-        CK(cudaMemsetAsync(dmax, 0, sizeof(int), st));
-        cgd::launch_max_bucket(byt.key_ofs, kfo, nf, ntypes, dmax, st); L();
-        int hmax = 0;
-        CK(cudaMemcpyAsync(&hmax, dmax, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        cgd::launch_mdc(nbody, md_->precision, nf, ntypes, ord, hmax, M, D, F, CS, byt, kfo, Fo, So, st); L();
+        cgd::MdBuckets B{};
+        B.ntypes = ntypes;
+        B.nkeys = nf * ntypes;
+        B.start = S.get<int64_t>(B.nkeys + 1);
+        B.tile_ofs = S.get<int>(B.nkeys + 1);
+        B.cursor = S.get<int>(B.nkeys);
+        B.val = S.get<int>(n);
+        cgd::launch_md_bucket(n, nf, cfo, CS.type, B, st); L(3);
+        const int64_t max_tiles = (n + cgd::MDC_TILE - 1) / cgd::MDC_TILE + B.nkeys;
+        cgd::launch_mdc(nbody, md_->precision, k == 0 ? M.order3 : M.order4, max_tiles, M, D, F, CS, B, Fo, So, st);
+        L();
         CK(cudaGetLastError());
-    };
-    if (M.order3 > 0) many(3, M.ntypes3, M.order3);
-    if (M.order4 > 0) many(4, M.ntypes4, M.order4);
+    }
     cgd::launch_md_finalize(nf, M, D, F, So, st); L();
     CK(cudaGetLastError());
     if (counts) *counts = c;
@@ -177,13 +186,260 @@ void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int n
     CK(cudaMemcpyAsync(dim, im.data(), nt * sizeof(double), cudaMemcpyHostToDevice, st));
     const cgd::FramesDev& F = df.dev;
     for (int step = 0; step <= nsteps; ++step) {
-        if (step > 0) cgd::launch_md_drift(n, df.xyz, v, acc, dt, st);   // UPDATE_COORDS + VELOCS_HALF_1
+        if (step > 0) cgd::launch_md_drift(n, F, nullptr, df.xyz, v, acc, dt, st);   // UPDATE_COORDS + VELOCS_HALF_1
         double* sout = So_steps ? So_steps + (size_t)step * nf * cgd::MD_NSCALAR : so;
         md_force(df, Fo, sout, nullptr);
-        cgd::launch_md_kick(nf, F, Fo, dim, dm, acc, v, dt, step > 0 ? 1 : 0,
+        cgd::launch_md_kick(nf, F, Fo, dim, dm, acc, v, dt, step > 0 ? 1 : 0, nullptr,
                             ke_steps ? ke_steps + (size_t)step * nf : nullptr, st);   // a = F/m, VELOCS_HALF_2
         CK(cudaGetLastError());
     }
+}
+
+}  // namespace cg
+
+// ------------------------------------------------------------------ serving loop
+namespace cg {
+namespace {
+
+// Device arrays of one batch composition, sized for the largest batch.
+struct ServeArena {
+    std::vector<void*> allocs;
+    int* natoms = nullptr;
+    int64_t *atom_ofs = nullptr, *ghost_ofs = nullptr, *row_ofs = nullptr;
+    int *stress_rows = nullptr, *energy_rows = nullptr, *type = nullptr;
+    cgd::BoxDev* box = nullptr;
+    double *xyz = nullptr, *v = nullptr, *acc = nullptr, *scaled = nullptr, *Fo = nullptr, *So = nullptr;
+    float* cart32 = nullptr;
+    unsigned char* first = nullptr;
+    template <typename T>
+    T* get(size_t n) {
+        void* p = nullptr;
+        CK(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+        allocs.push_back(p);
+        CK(cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T)));
+        return reinterpret_cast<T*>(p);
+    }
+    void init(int64_t atoms, int frames, int nimg) {
+        natoms = get<int>(frames);
+        atom_ofs = get<int64_t>(frames + 1);
+        ghost_ofs = get<int64_t>(frames + 1);
+        row_ofs = get<int64_t>(frames + 1);
+        stress_rows = get<int>(frames);
+        energy_rows = get<int>(frames);
+        box = get<cgd::BoxDev>(frames);
+        type = get<int>(atoms);
+        xyz = get<double>(3 * atoms);
+        v = get<double>(3 * atoms);
+        acc = get<double>(3 * atoms);
+        Fo = get<double>(3 * atoms);
+        So = get<double>((size_t)frames * cgd::MD_NSCALAR);
+        scaled = get<double>(3 * atoms * nimg);
+        cart32 = get<float>(4 * atoms * nimg);
+        first = get<unsigned char>(frames);
+    }
+    ~ServeArena() { for (void* p : allocs) cudaFree(p); }
+};
+
+template <typename T>
+struct Pinned {
+    T* p = nullptr;
+    size_t n = 0;
+    void reserve(size_t m) {
+        if (m <= n) return;
+        if (p) cudaFreeHost(p);
+        CK(cudaMallocHost((void**)&p, std::max<size_t>(m, 1) * sizeof(T)));
+        n = m;
+    }
+    ~Pinned() { if (p) cudaFreeHost(p); }
+};
+
+double now_s(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_type, const MdServeOptions& opt,
+                          MdResult* res, double* step_ms) {
+    CK(cudaSetDevice(device_));
+    if (!md_) throw Error(1, "MD coefficients are not set (cg_md_setup)");
+    const Model& m = model_;
+    const int nt = m.ctl.natmtyp;
+    const int nreq = (int)req.size();
+    const int L = m.ctl.nlayers;
+    const int nimg = (2 * L + 1) * (2 * L + 1) * (2 * L + 1);
+    int stride = 0;
+    std::vector<cgd::BoxDev> boxes(nreq);
+    for (int r = 0; r < nreq; ++r) {
+        const MdRequest& q = req[r];
+        if (q.natoms <= 0 || q.nsteps <= 0 || !q.types || !q.xyz || !q.cell || !q.v)
+            throw Error(1, "request " + std::to_string(r) + ": empty or incomplete");
+        if (q.natoms > opt.max_batch_atoms) throw Error(1, "request larger than the batch capacity");
+        if (q.natoms > 8191) throw Error(2, "frames above 8191 atoms are not supported on the device");
+        for (int a = 0; a < q.natoms; ++a)
+            if (q.types[a] < 0 || q.types[a] >= nt) throw Error(1, "atom type index out of range");
+        stride = std::max(stride, q.nsteps);
+        Box b;
+        b.ax = q.cell[0]; b.ay = q.cell[1]; b.az = q.cell[2]; b.bx = q.cell[3]; b.by = q.cell[4]; b.bz = q.cell[5];
+        b.cx = q.cell[6]; b.cy = q.cell[7]; b.cz = q.cell[8];
+        b.update_cell();
+        if (b.ax <= 0.0 || b.by <= 0.0 || b.cz <= 0.0 || b.ay != 0.0 || b.az != 0.0 || b.bz != 0.0)
+            throw Error(2, "cell must be upper triangular with a positive diagonal");
+        cgd::BoxDev& bd = boxes[r];
+        std::memset(&bd, 0, sizeof(bd));
+        for (int k = 0; k < 9; ++k) { bd.h[k] = b.hmat[k]; bd.inv[k] = b.invr[k]; }
+        bd.lx = b.lx; bd.ly = b.ly; bd.lz = b.lz; bd.vol = b.vol;
+        bd.is_ortho = b.is_ortho ? 1 : 0;
+        set_small(bd, frame_is_small(m, b, false));
+    }
+    std::vector<double> mv(mass_type, mass_type + nt), im(nt);
+    for (int i = 0; i < nt; ++i) {
+        if (!(mv[i] > 0.0)) throw Error(1, "atom masses must be positive");
+        im[i] = 1.0 / mv[i];
+    }
+    cudaStream_t st = stream_;
+    const int64_t cap_atoms = opt.max_batch_atoms;
+    const int cap_frames = std::max(1, opt.max_batch_frames);
+    ServeArena arena[2];
+    arena[0].init(cap_atoms, cap_frames, nimg);
+    arena[1].init(cap_atoms, cap_frames, nimg);
+    double *dm = nullptr, *dim = nullptr;
+    CK(cudaMalloc((void**)&dm, nt * sizeof(double)));
+    CK(cudaMalloc((void**)&dim, nt * sizeof(double)));
+    std::unique_ptr<double, void (*)(double*)> g1(dm, [](double* p) { cudaFree(p); });
+    std::unique_ptr<double, void (*)(double*)> g2(dim, [](double* p) { cudaFree(p); });
+    CK(cudaMemcpy(dm, mv.data(), nt * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dim, im.data(), nt * sizeof(double), cudaMemcpyHostToDevice));
+    Pinned<int> h_nat, h_type;
+    Pinned<int64_t> h_aofs, h_gofs;
+    Pinned<cgd::BoxDev> h_box;
+    Pinned<unsigned char> h_first;
+    h_nat.reserve(cap_frames); h_aofs.reserve(cap_frames + 1); h_gofs.reserve(cap_frames + 1);
+    h_box.reserve(cap_frames); h_first.reserve(cap_frames); h_type.reserve(cap_atoms);
+
+    std::vector<int> order(nreq);
+    for (int r = 0; r < nreq; ++r) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return req[a].arrival < req[b].arrival; });
+    const double per_atom_bytes = 8192.0, per_req_bytes = 65536.0;   // resident estimate per request
+    std::vector<int> active, steps_done(nreq, 0);
+    std::vector<int64_t> pos(nreq, -1);      // atom offset of each active request in the current arena
+    std::vector<char> first(nreq, 0);
+    int cur = 0, next_pending = 0, finished = 0;
+    int64_t active_atoms = 0, nbatch = 0;
+    double mem = 0.0;
+    bool changed = false;
+    const auto t0 = std::chrono::steady_clock::now();
+    while (finished < nreq) {
+        // admit every arrived request that fits
+        double t = now_s(t0);
+        while (next_pending < nreq) {
+            const MdRequest& q = req[order[next_pending]];
+            const double need = per_atom_bytes * q.natoms + per_req_bytes;
+            if (q.arrival > t || active_atoms + q.natoms > cap_atoms || (int)active.size() >= cap_frames ||
+                mem + need > opt.hbm_budget)
+                break;
+            const int r = order[next_pending++];
+            active.push_back(r);
+            active_atoms += q.natoms;
+            mem += need;
+            first[r] = 1;
+            res[r].admitted = t;
+            changed = true;
+        }
+        if (active.empty()) {
+            if (next_pending < nreq) {
+                const double wait = req[order[next_pending]].arrival - now_s(t0);
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
+            }
+            continue;
+        }
+        ServeArena& A = arena[cur];
+        ServeArena& B = arena[cur ^ 1];
+        const int nf = (int)active.size();
+        if (changed) {
+            // new composition in the other arena: carried-over state copied on the device
+            int64_t ofs = 0;
+            h_aofs.p[0] = 0; h_gofs.p[0] = 0;
+            for (int k = 0; k < nf; ++k) {
+                const int r = active[k];
+                const int n = req[r].natoms;
+                h_nat.p[k] = n;
+                h_box.p[k] = boxes[r];
+                std::memcpy(h_type.p + ofs, req[r].types, n * sizeof(int));
+                if (first[r]) {
+                    CK(cudaMemcpyAsync(B.xyz + 3 * ofs, req[r].xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+                    CK(cudaMemcpyAsync(B.v + 3 * ofs, req[r].v, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+                    CK(cudaMemsetAsync(B.acc + 3 * ofs, 0, 3 * n * sizeof(double), st));
+                } else {
+                    const size_t bytes = 3 * n * sizeof(double);
+                    CK(cudaMemcpyAsync(B.xyz + 3 * ofs, A.xyz + 3 * pos[r], bytes, cudaMemcpyDeviceToDevice, st));
+                    CK(cudaMemcpyAsync(B.v + 3 * ofs, A.v + 3 * pos[r], bytes, cudaMemcpyDeviceToDevice, st));
+                    CK(cudaMemcpyAsync(B.acc + 3 * ofs, A.acc + 3 * pos[r], bytes, cudaMemcpyDeviceToDevice, st));
+                }
+                ofs += n;
+                h_aofs.p[k + 1] = ofs;
+                h_gofs.p[k + 1] = ofs * nimg;
+            }
+            for (int k = 0; k < nf; ++k) pos[active[k]] = h_aofs.p[k];
+            CK(cudaMemcpyAsync(B.natoms, h_nat.p, nf * sizeof(int), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.atom_ofs, h_aofs.p, (nf + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.ghost_ofs, h_gofs.p, (nf + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.box, h_box.p, nf * sizeof(cgd::BoxDev), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.type, h_type.p, ofs * sizeof(int), cudaMemcpyHostToDevice, st));
+            cur ^= 1;
+            changed = false;
+        }
+        ServeArena& C = arena[cur];
+        for (int k = 0; k < nf; ++k) h_first.p[k] = first[active[k]] ? 1 : 0;
+        CK(cudaMemcpyAsync(C.first, h_first.p, nf, cudaMemcpyHostToDevice, st));
+        DeviceFrames df;
+        df.nframes = nf;
+        df.natoms_total = active_atoms;
+        df.nghosts = active_atoms * nimg;
+        df.xyz = C.xyz;
+        cgd::FramesDev& F = df.dev;
+        F.nframes = nf; F.nlayers = L; F.nimg = nimg;
+        F.natoms = C.natoms; F.atom_ofs = C.atom_ofs; F.ghost_ofs = C.ghost_ofs; F.row_ofs = C.row_ofs;
+        F.stress_rows = C.stress_rows; F.energy_rows = C.energy_rows; F.box = C.box; F.type = C.type;
+        F.xyz = C.xyz; F.scaled = C.scaled; F.cart32 = C.cart32;
+        // one batched step
+        const auto s0 = std::chrono::steady_clock::now();
+        cgd::launch_md_drift(active_atoms, F, C.first, C.xyz, C.v, C.acc, opt.dt, st);
+        md_force(df, C.Fo, C.So, nullptr);
+        cgd::launch_md_kick(nf, F, C.Fo, dim, dm, C.acc, C.v, opt.dt, 1, C.first, nullptr, st);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - s0).count();
+        ++nbatch;
+        // bookkeeping, retire finished requests
+        std::vector<int> keep;
+        keep.reserve(active.size());
+        for (int r : active) {
+            if (step_ms) step_ms[(size_t)r * stride + steps_done[r]] = ms;
+            res[r].step_ms_sum += ms;
+            res[r].step_ms_max = std::max(res[r].step_ms_max, ms);
+            first[r] = 0;
+            if (++steps_done[r] == req[r].nsteps) {
+                if (req[r].xyz_out)
+                    CK(cudaMemcpyAsync(req[r].xyz_out, C.xyz + 3 * pos[r], 3 * req[r].natoms * sizeof(double),
+                                       cudaMemcpyDeviceToHost, st));
+                active_atoms -= req[r].natoms;
+                mem -= per_atom_bytes * req[r].natoms + per_req_bytes;
+                ++finished;
+                changed = true;
+            } else {
+                keep.push_back(r);
+            }
+        }
+        if (changed) {
+            CK(cudaStreamSynchronize(st));
+            const double tf = now_s(t0);
+            for (int r : active)
+                if (steps_done[r] == req[r].nsteps && res[r].finished == 0.0) res[r].finished = tf;
+        }
+        active.swap(keep);
+    }
+    return nbatch;
 }
 
 }  // namespace cg

@@ -77,6 +77,27 @@ struct MdCounts {
     int64_t pairs2 = 0, triplets = 0, quads = 0, launches = 0;
 };
 
+// One MD request of the serving loop (host arrays owned by the caller).
+struct MdRequest {
+    int natoms = 0, nsteps = 0;
+    double arrival = 0.0;             // seconds after the start of the run
+    const int* types = nullptr;
+    const double* xyz = nullptr;
+    const double* cell = nullptr;     // ax ay az bx by bz cx cy cz
+    const double* v = nullptr;        // A per internal time unit
+    double* xyz_out = nullptr;        // final positions (may be null)
+};
+struct MdResult {
+    double admitted = 0, finished = 0;    // seconds after the start of the run
+    double step_ms_sum = 0, step_ms_max = 0;
+};
+struct MdServeOptions {
+    double dt = 0;                        // internal time units
+    double hbm_budget = 150e9;            // bytes of device memory requests may hold
+    int64_t max_batch_atoms = 1 << 16;
+    int max_batch_frames = 1024;
+};
+
 // Pipeline stages timed with CUDA events when profiling is on.
 enum Stage {
     ST_SETUP = 0, ST_NEIGH, ST_CLUSTERS, ST_BUCKET, ST_FORCE2, ST_VIRIAL2, ST_FORCE3, ST_VIRIAL3, ST_FORCE4,
@@ -120,6 +141,13 @@ class Session {
     // [(nsteps+1)*nframes] (device, may be null) receive step 0..nsteps.
     void md_nve(DeviceFrames& df, const double* mass_type, double dt, int nsteps, double* v, double* Fo,
                 double* So_steps, double* ke_steps);
+    // Continuous-batching serving loop: requests are admitted on arrival while the
+    // batch has room (atoms, frames, memory budget), every batched step advances all
+    // admitted requests by one velocity-Verlet step, finished requests leave at once.
+    // step_ms (may be null): per (request, step) wall time of the batched step, stride
+    // = largest nsteps.  Returns the number of batched steps.
+    int64_t md_serve(const std::vector<MdRequest>& req, const double* mass_type, const MdServeOptions& opt,
+                     MdResult* res, double* step_ms);
 
     // Stage timing (CUDA events on the session stream).
     void set_profiling(bool on) { profiling_ = on; }

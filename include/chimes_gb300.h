@@ -196,8 +196,37 @@ int cg_md_force_device(cg_session* s, const cg_dframes* d, double* forces, doubl
 int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, double* velocities,
               double* forces, double* scalars_steps, double* ke_steps);
 
-/* Device pointer to the positions of uploaded frames (3 per atom). */
+/* Continuous-batching MD serving (no counterpart in the reference, whose chimes_md
+ * runs one system).  Each request runs nsteps velocity-Verlet NVE steps (step 0
+ * evaluates forces only, as chimes_md's first step) from its own positions and
+ * velocities; it is admitted once its arrival time (seconds after the call starts)
+ * has passed and the batch has room -- at most max_batch_atoms atoms and
+ * max_batch_frames requests, and hbm_budget_bytes of estimated resident memory --
+ * and every batched step advances all admitted requests together; a request leaves
+ * the batch as soon as it finishes and its final positions are copied to xyz_out.
+ * results[r]: admission / finish times (seconds), sum and maximum of its step times
+ * (ms).  step_ms (may be NULL): nreq * max(nsteps) wall times (ms) of the batched
+ * step that advanced request r at step s.  *batch_steps: number of batched steps. */
+typedef struct {
+    int natoms, nsteps;
+    double arrival;
+    const int* types;
+    const double* xyz;
+    const double* cell;
+    const double* v;
+    double* xyz_out;
+} cg_md_request;
+typedef struct {
+    double admitted, finished, step_ms_sum, step_ms_max;
+} cg_md_result;
+int cg_md_serve(cg_session* s, int nreq, const cg_md_request* req, const double* mass, double dt_fs,
+                double hbm_budget_bytes, int64_t max_batch_atoms, int max_batch_frames, cg_md_result* results,
+                double* step_ms, int64_t* batch_steps);
+
+/* Device pointer to the positions of uploaded frames (3 per atom), and a copy of
+ * them into host memory. */
 int cg_dframes_positions(const cg_dframes* d, double** xyz, int64_t* natoms);
+int cg_dframes_read_positions(const cg_dframes* d, double* xyz_host);
 
 /* Pairs, triplets, quadruplets and kernel launches of the last MD force call. */
 int cg_md_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads, int64_t* launches);

@@ -157,3 +157,38 @@ def test_md_nve_matches_reference_run(cg, name):
         assert abs(kn - tab[s, 2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, tab[s, 2])
         assert abs(vn - tab[s, 3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, tab[s, 3])
         assert abs(p - tab[s, 6]) <= 5e-9 * max(1.0, abs(p)) + 1e-12, (s, p, tab[s, 6])
+
+
+def test_md_serving_results_same_alone_and_in_the_mix(cg, tmp_path):
+    """Continuous batching: requests of different sizes arriving while others run
+    give the same final positions as each request alone (one-at-a-time serving) and
+    as the plain NVE call, within 1e-9 A after 6 steps (atomics reorder FP64 sums)."""
+    torch = pytest.importorskip("torch")
+    sizes = [40, 96, 64, 150, 33, 80]
+    fm, model, (nat, types, xyz, cell), x = _chno_batch(cg, tmp_path, sizes, False, 91)
+    x *= 0.02
+    masses = np.array([12.011, 1.0079, 14.007, 15.9994])
+    rng = np.random.default_rng(3)
+    ofs = np.concatenate([[0], np.cumsum(nat)])
+    reqs = []
+    for k in range(len(sizes)):
+        a, b = ofs[k], ofs[k + 1]
+        v = rng.standard_normal((b - a, 3)) * 0.01
+        reqs.append(dict(types=types[a:b], xyz=xyz[a:b], cell=cell[k], v=v, nsteps=6, arrival=0.0005 * k))
+    sess = cg.Session(model, 0)
+    sess.md_setup(x)
+    mix, res, step_ms, nb = sess.md_serve(reqs, masses, dt_fs=0.2, max_batch_atoms=300, max_batch_frames=3)
+    alone, res1, _, nb1 = sess.md_serve(reqs, masses, dt_fs=0.2, max_batch_frames=1)
+    assert nb1 == 6 * len(sizes) and nb < nb1
+    assert np.all(res["finished"] >= res["admitted"]) and np.all(step_ms > 0)
+    for k, q in enumerate(reqs):
+        assert np.abs(mix[k] - alone[k]).max() <= 1e-9
+        # the plain NVE call on the same request
+        fr = cg.Frames.from_arrays(model, [sizes[k]], q["types"], q["xyz"], q["cell"][None]).independent()
+        dfr = sess.upload(fr)
+        vd = torch.from_numpy(q["v"].reshape(-1).copy()).cuda()
+        Fd = torch.zeros(3 * sizes[k], dtype=torch.float64, device="cuda")
+        sess.md_nve(dfr, masses, 0.2, 5, vd.data_ptr(), Fd.data_ptr())
+        torch.cuda.synchronize()
+        pos = dfr.read_positions()
+        assert np.abs(pos.reshape(-1, 3) - mix[k]).max() <= 1e-9
