@@ -136,6 +136,143 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("bf16_tflops", 1900.0), "measured"
+    return 1900.0, "fallback"
+
+
+def gram_bench(cg, sess, model, A64, b, steps, torch):
+    """Normal equations of the step's A: the plain form (FP64 A, FP64 library Gram)
+    against the mixed form (FP32 A, split-BF16 tcgen05 Gram, FP32 accumulate), and
+    the FP64 solve of both against each other."""
+    nrows, ncols = A64.shape
+    stream = torch.cuda.ExternalStream(sess.stream)
+    A32 = A64.float()
+    G = torch.zeros((ncols, ncols), dtype=torch.float64, device="cuda")
+    h = torch.zeros(ncols, dtype=torch.float64, device="cuda")
+    flops = nrows * ncols * (ncols + 1) + 2 * nrows * ncols   # SYRK lower triangle + A^T b
+    out = {}
+    for name, prec, src, mode in (("fp64", 0, A64, 0), ("bf16x3", 1, A32, 1)):
+        def one():
+            G.zero_(); h.zero_()
+            sess.gram(prec, src.data_ptr(), ncols, nrows, ncols, b.data_ptr(), mode, G.data_ptr(), h.data_ptr())
+        for _ in range(3):
+            one()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            one()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        sess.gram_finish(G.data_ptr(), ncols)
+        torch.cuda.synchronize()
+        out[name] = {"ms": ms, "tflops": flops / (ms / 1e3) / 1e12, "G": G.clone()}
+    pk, kind = bf16_peak()
+    tc = out["bf16x3"]
+    roof = {"bound": "tensor", "kernel": "k_gram_tc (split-BF16 3-term, tcgen05)", "achieved": tc["tflops"],
+            "peak": pk / 3.0, "unit": "TFLOP/s", "frac": tc["tflops"] / (pk / 3.0), "traffic": None,
+            "peak_source": f"{kind} bf16 dense burst / 3 (three BF16 products per FP32-accurate product)",
+            "flops_per_launch": flops}
+    # the solve of both forms on one ridge system (coefficients and RMSE agreement)
+    Gd = torch.diagonal(out["fp64"]["G"])
+    lam = 1e-6 * float(Gd.abs().max())
+    h64 = (A64.T @ b).contiguous()
+    res = {}
+    for name, it in (("fp64", 20), ("bf16x3", 400)):
+        x = torch.zeros(ncols, dtype=torch.float64, device="cuda")
+        t0 = time.perf_counter()
+        info = sess.solve(out[name]["G"].data_ptr(), h64.data_ptr(), ncols, lam, A64.data_ptr(), ncols, nrows,
+                          b.data_ptr(), it, x.data_ptr())
+        torch.cuda.synchronize()
+        res[name] = (x, time.perf_counter() - t0, info)
+    xf, xm = res["fp64"][0], res["bf16x3"][0]
+    rel = float(torch.linalg.norm(xm - xf) / torch.linalg.norm(xf))
+    rm = lambda x: float(torch.sqrt(torch.mean((A64 @ x - b) ** 2)))
+    return {
+        "rows": nrows, "cols": ncols, "fp64_ms": out["fp64"]["ms"], "fp64_tflops": out["fp64"]["tflops"],
+        "bf16x3_ms": tc["ms"], "bf16x3_tflops": tc["tflops"], "speedup_mixed_vs_fp64": out["fp64"]["ms"] / tc["ms"],
+        "solve": {"ridge": lam, "fp64_s": res["fp64"][1], "mixed_s": res["bf16x3"][1],
+                  "coef_rel_diff_mixed_vs_fp64": rel, "rmse_fp64": rm(xf), "rmse_mixed": rm(xm),
+                  "unit_rmse": "kcal/mol/A over all rows"},
+    }, roof
+
+
+def md_bench(cg, local):
+    """MD serving on the Poisson-arrival, 64-4096-atom, 4-species, 4-body workload:
+    a bounded arrival window, 100 NVE steps per request, batched FP64 and
+    FP32-contraction serving against one request at a time in FP64."""
+    synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+    import numpy as np
+    KB = 0.0019872067
+    window, nsteps, rate = 0.02, 100, 2000.0
+    rng = np.random.default_rng(7)
+    arr = np.cumsum(rng.exponential(1 / rate, size=10000))
+    arr = arr[arr < window]
+    nreq = len(arr)
+    sizes = np.exp(rng.uniform(np.log(64), np.log(4096), size=nreq)).astype(int)
+    tmp = tempfile.mkdtemp(prefix="chimes_md_")
+    fm = synth.make_workload("chno-4b", tmp, nframes=nreq, seed=9, sizes=list(sizes), triclinic=False, density=0.1,
+                             labels=False)
+    model = cg.Model(fm)
+    nat, types, xyz, cell = synth.frames_arrays(os.path.join(tmp, "traj.xyzf"), nreq, ["C", "H", "N", "O"])[:4]
+    masses = np.array([12.011, 1.0079, 14.007, 15.9994])
+    x = np.random.default_rng(1).standard_normal(model.ncols) * 1e-4
+    ofs = np.concatenate([[0], np.cumsum(nat)])
+    reqs = []
+    for k in range(nreq):
+        a, b = ofs[k], ofs[k + 1]
+        v = rng.standard_normal((b - a, 3)) * np.sqrt(KB * 300.0 / masses[types[a:b]])[:, None]
+        reqs.append(dict(types=types[a:b], xyz=xyz[a:b], cell=cell[k], v=v, nsteps=nsteps, arrival=float(arr[k])))
+    out = {"workload": f"{nreq} Poisson arrivals at {rate:.0f}/s over {window} s, N log-uniform in [64, 4096] "
+                       f"(mean {sizes.mean():.0f}), 4 species, density 0.1/A^3, 2B16@5.0 / 3B8@4.0 / 4B4@3.5 "
+                       f"({model.ncols} coefficients, seeded), {nsteps} NVE steps at 0.2 fs each",
+           "unit": "atom-steps/s"}
+    sel = (sizes >= 768) & (sizes <= 1280)
+    for name, prec, cap, frames_cap, sub in (("batched_fp64", 0, 16384, 1024, None),
+                                             ("batched_fp32", 1, 16384, 1024, None),
+                                             ("one_at_a_time_fp64", 0, 1 << 16, 1, 6)):
+        sess = cg.Session(model, local)
+        sess.md_setup(x, precision=prec)
+        rq = reqs if sub is None else [dict(r, arrival=0.0) for r in reqs[:sub]]
+        sz = sizes if sub is None else sizes[:sub]
+        outs, res, step_ms, nb = sess.md_serve(rq, masses, dt_fs=0.2, max_batch_atoms=cap,
+                                               max_batch_frames=frames_cap)
+        t_first = min(r["arrival"] for r in rq)
+        span = float(res["finished"].max() - t_first)
+        sm = step_ms.reshape(-1)
+        d = {"value": float(sz.sum() * nsteps / span), "batched_steps": int(nb), "requests": len(rq),
+             "max_batch_atoms": cap if frames_cap > 1 else "one request",
+             "step_ms_p50": float(np.percentile(sm, 50)), "step_ms_p99": float(np.percentile(sm, 99)),
+             "request_latency_s_p50": float(np.percentile(res["finished"] - np.array([r["arrival"] for r in rq]), 50)),
+             "request_latency_s_p99": float(np.percentile(res["finished"] - np.array([r["arrival"] for r in rq]), 99))}
+        s1 = sel[: len(rq)]
+        if s1.any():
+            d["step_ms_p50_1024atom"] = float(np.percentile(step_ms[s1].reshape(-1), 50))
+            d["step_ms_p99_1024atom"] = float(np.percentile(step_ms[s1].reshape(-1), 99))
+        out[name] = d
+    # one 1024-atom request alone: per-step latency of the plain and the FP32 form
+    for name, prec in (("single_1024_fp64", 0), ("single_1024_fp32", 1)):
+        tmp2 = tempfile.mkdtemp(prefix="chimes_md1_")
+        fm2 = synth.make_workload("chno-4b", tmp2, nframes=1, seed=21, sizes=[1024], triclinic=False, density=0.1,
+                                  labels=False)
+        m2 = cg.Model(fm2)
+        n2, t2, x2, c2 = synth.frames_arrays(os.path.join(tmp2, "traj.xyzf"), 1, ["C", "H", "N", "O"])[:4]
+        v2 = rng.standard_normal((1024, 3)) * np.sqrt(KB * 300.0 / masses[t2])[:, None]
+        sess = cg.Session(m2, local)
+        sess.md_setup(x, precision=prec)
+        _, res, step_ms, _ = sess.md_serve([dict(types=t2, xyz=x2, cell=c2[0], v=v2, nsteps=nsteps, arrival=0.0)],
+                                           masses, dt_fs=0.2)
+        sm = step_ms.reshape(-1)[1:]
+        out[name] = {"step_ms_p50": float(np.percentile(sm, 50)), "step_ms_p99": float(np.percentile(sm, 99)),
+                     "value": float(1024 / (np.mean(sm) / 1e3))}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -145,6 +282,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--frames", type=int, default=200, help="frames per rank (200 = the full workload)")
+    ap.add_argument("--no-gram", action="store_true")
+    ap.add_argument("--no-md", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -247,6 +386,19 @@ def main():
            "h2d_bytes_per_step": int(natoms * (3 * 8 + 4) + frames_n * (4 + 3 * 8 + 2 * 4 + 208) + 3 * 8),
            "d2h_bytes_per_step": int(nrows * ncols * esz)}
 
+    gram, gram_roof = None, None
+    if rank == 0 and not args.no_gram:
+        b = torch.from_numpy(frames.labels()).cuda()
+        A64 = A if esz == 8 else A.double()
+        sess.assemble_device(dfr, cg.CG_FP64, A64.data_ptr(), ncols) if esz != 8 else None
+        torch.cuda.synchronize()
+        gram, gram_roof = gram_bench(cg, sess, model, A64, b, max(3, args.steps // 2), torch)
+    md = None
+    if rank == 0 and not args.no_md:
+        del A
+        torch.cuda.empty_cache()
+        md = md_bench(cg, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         th = cpu_threads()
@@ -263,7 +415,7 @@ def main():
                        "parallelism": f"frames sharded, {world} rank(s), no collective"},
             "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "fp64": fp64,
             "stages_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in stages.items() if v[1]},
-            "work": counts, "cpu_baseline": cpu,
+            "work": counts, "cpu_baseline": cpu, "gram": gram, "roofline_gram": gram_roof, "md": md,
         }
         print(json.dumps(line), flush=True)
     if dist:

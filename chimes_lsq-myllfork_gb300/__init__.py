@@ -87,6 +87,11 @@ def lib():
         "cg_session_stage_times": (ctypes.c_int, [vp, vp, vp]),
         "cg_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
         "cg_last_error": (ctypes.c_char_p, []),
+        "cg_gram": (ctypes.c_int, [vp, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, vp, ctypes.c_int,
+                                   vp, vp]),
+        "cg_gram_finish": (ctypes.c_int, [vp, vp, ctypes.c_int]),
+        "cg_solve": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_double, vp, ctypes.c_int64, ctypes.c_int64, vp,
+                                    ctypes.c_int, vp, vp]),
         "cg_md_setup": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double]),
         "cg_md_force": (ctypes.c_int, [vp, vp, dp, dp]),
@@ -335,6 +340,25 @@ class Session:
         device array inside the library; see include/chimes_gb300.h)."""
         _check(lib().cg_assemble_device_noalloc(self._h, dframes._h, int(precision),
                                                 ctypes.c_void_p(int(a_device_ptr)), int(lda)))
+
+    # ---------------------------------------------------------------- normal equations
+    def gram(self, a_precision, a_ptr, lda, nrows, ncols, b_ptr, mode, g_ptr, h_ptr):
+        """Accumulate G += A^T A (upper triangle), h += A^T b on the device (cg_gram)."""
+        _check(lib().cg_gram(self._h, int(a_precision), ctypes.c_void_p(int(a_ptr)), ctypes.c_int64(int(lda)),
+                             ctypes.c_int64(int(nrows)), int(ncols), ctypes.c_void_p(int(b_ptr)), int(mode),
+                             ctypes.c_void_p(int(g_ptr)), ctypes.c_void_p(int(h_ptr))))
+
+    def gram_finish(self, g_ptr, ncols):
+        _check(lib().cg_gram_finish(self._h, ctypes.c_void_p(int(g_ptr)), int(ncols)))
+
+    def solve(self, g_ptr, h_ptr, ncols, ridge, a_ptr, lda, nrows, b_ptr, iters, x_ptr):
+        """Ridge least squares (cg_solve); returns (||b - A x||, ||A^T r - ridge x||, ridge used)."""
+        info = (ctypes.c_double * 3)()
+        _check(lib().cg_solve(self._h, ctypes.c_void_p(int(g_ptr)), ctypes.c_void_p(int(h_ptr)), int(ncols),
+                              ctypes.c_double(ridge), ctypes.c_void_p(int(a_ptr) or None), ctypes.c_int64(int(lda)),
+                              ctypes.c_int64(int(nrows)), ctypes.c_void_p(int(b_ptr) or None), int(iters),
+                              ctypes.c_void_p(int(x_ptr)), info))
+        return info[0], info[1], info[2]
 
     # ---------------------------------------------------------------- MD force
     def md_setup(self, x, precision=CG_FP64, energy_offsets=False, penalty_dist=0.01, penalty_scale=1.0e4):

@@ -106,22 +106,24 @@ def _finish(xyz, cell, i, j, d, r, dEdr, E):
 
 def chno_frame(rng, natoms, cell, min_sep=0.9, ntypes=4):
     inv = np.linalg.inv(cell)
-    pts = []
+    pts = np.empty((natoms, 3))
+    n = 0
     tries = 0
-    while len(pts) < natoms:
+    while n < natoms:
         tries += 1
         if tries > 500000:
             raise RuntimeError("could not place atoms")
         p = rng.uniform(0, 1, size=3) @ cell
-        if pts:
-            d = np.array(pts) - p
+        if n:
+            d = pts[:n] - p
             f = d @ inv
             f -= np.round(f)
             if np.min(np.linalg.norm(f @ cell, axis=1)) < min_sep:
                 continue
-        pts.append(p)
+        pts[n] = p
+        n += 1
     types = rng.integers(0, ntypes, size=natoms).astype(np.int32)
-    return np.array(pts), types
+    return pts, types
 
 
 def triclinic_cell(rng, lo=12.0, hi=16.0, alo=80.0, ahi=100.0):
