@@ -70,16 +70,18 @@ __global__ void k_frame_setup(FramesDev F, int64_t total_ghosts) {
 }
 
 // ---------------------------------------------------------------- neighbour lists
-// One block of NEIGH_WARPS warps per real atom; warp w scans the w-th contiguous
-// slice of the ghost indices, so the concatenated lists come out in ghost-index
-// order and the fill pass is deterministic.  The fill pass recounts each slice to
-// place it after the slices before it.
+// One block of nw warps per real atom (nw = blockDim.x / 32, at most NEIGH_WARPS);
+// warp w scans the w-th contiguous slice of the ghost indices, so the concatenated
+// lists come out in ghost-index order and the fill pass is deterministic.  With
+// several warps the fill pass recounts each slice to place it after the slices
+// before it; batches with many atoms use one warp per atom and skip that.
 constexpr int NEIGH_WARPS = 8;
 
-__global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDev F, NeighDev NB, int fill) {
+__global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDev F, NeighDev NB, int fill, int nw) {
     __shared__ int sc[3][NEIGH_WARPS];
-    const int atom = blockIdx.x;
-    const int w = threadIdx.x >> 5;
+    // nw > 1: one atom per block, nw warps on it; nw == 1: one atom per warp
+    const int atom = nw > 1 ? blockIdx.x : blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int w = nw > 1 ? threadIdx.x >> 5 : 0;
     const int lane = threadIdx.x & 31;
     if (atom >= NB.n_real) return;
     int lo = 0, hi = F.nframes - 1;
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDe
     const double* si = F.scaled + 3 * (gbase + i);
     const float maxall = (float)fmax(fmax(M.maxcut2, M.order3 > 0 ? M.maxcut3 : 0.0), M.order4 > 0 ? M.maxcut4 : 0.0);
     const float pre = maxall + MARGIN;
-    const int per = ((G + NEIGH_WARPS - 1) / NEIGH_WARPS + 31) & ~31;
+    const int per = ((G + nw - 1) / nw + 31) & ~31;
     const int g0 = w * per, g1 = min(G, g0 + per);
     const unsigned lt = (1u << lane) - 1u;
     auto sweep = [&](bool write, int64_t o2, int64_t o3, int64_t o4, int& c2, int& c3, int& c4) {
@@ -137,13 +139,22 @@ __global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDe
         }
     };
     int c2 = 0, c3 = 0, c4 = 0;
+    if (nw == 1) {   // single slice per atom: no block-level bookkeeping
+        if (fill) {
+            sweep(true, NB.ofs2[atom], NB.ofs3[atom], NB.ofs4[atom], c2, c3, c4);
+        } else {
+            sweep(false, 0, 0, 0, c2, c3, c4);
+            if (lane == 0) { NB.cnt2[atom] = c2; NB.cnt3[atom] = c3; NB.cnt4[atom] = c4; }
+        }
+        return;
+    }
     sweep(false, 0, 0, 0, c2, c3, c4);
     if (lane == 0) { sc[0][w] = c2; sc[1][w] = c3; sc[2][w] = c4; }
     __syncthreads();
     if (!fill) {
         if (threadIdx.x == 0) {
             int t2 = 0, t3 = 0, t4 = 0;
-            for (int k = 0; k < NEIGH_WARPS; ++k) { t2 += sc[0][k]; t3 += sc[1][k]; t4 += sc[2][k]; }
+            for (int k = 0; k < nw; ++k) { t2 += sc[0][k]; t3 += sc[1][k]; t4 += sc[2][k]; }
             NB.cnt2[atom] = t2; NB.cnt3[atom] = t3; NB.cnt4[atom] = t4;
         }
         return;
@@ -414,7 +425,12 @@ void launch_frame_setup(const FramesDev& F, int64_t n, cudaStream_t st) {
     if (n > 0) k_frame_setup<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, n);
 }
 void launch_neigh(const ModelDev& M, const FramesDev& F, const NeighDev& NB, int fill, cudaStream_t st) {
-    if (NB.n_real > 0) k_neigh<<<(unsigned)NB.n_real, 32 * NEIGH_WARPS, 0, st>>>(M, F, NB, fill);
+    // enough atoms to fill the GPU with one warp each: one warp per atom
+    if (NB.n_real <= 0) return;
+    if (NB.n_real >= 32768)
+        k_neigh<<<(unsigned)((NB.n_real + NEIGH_WARPS - 1) / NEIGH_WARPS), 32 * NEIGH_WARPS, 0, st>>>(M, F, NB, fill, 1);
+    else
+        k_neigh<<<(unsigned)NB.n_real, 32 * NEIGH_WARPS, 0, st>>>(M, F, NB, fill, NEIGH_WARPS);
 }
 void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const NeighDev& NB, const ClusterSet& CS,
                      int fill, cudaStream_t st) {

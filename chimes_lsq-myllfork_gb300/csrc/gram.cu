@@ -308,17 +308,21 @@ size_t gram_plane_bytes(int64_t nrows_block, int ncols) {
 
 void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
                      double* G, double* h, void* planes, size_t planes_bytes, int* d_err, void* cublas,
-                     cudaStream_t st) {
+                     cudaStream_t st, const std::function<void(int, bool)>& mark) {
     if (nrows <= 0) return;
+    // stage ids (session.h): ST_GRAM_ATB 11, ST_GRAM_SPLIT 12, ST_GRAM_TC 13, ST_GRAM_SYRK 14
+    enum { S_ATB = 11, S_SPLIT = 12, S_TC = 13, S_SYRK = 14 };
     // h += A^T b (FP64), reproducible
     {
         const int ns = (int)std::min<int64_t>(nrows, cgd::ATB_SLICES);
         double* partial = nullptr;
         ck(cudaMallocAsync((void**)&partial, sizeof(double) * ns * ncols, st), "atb scratch");
+        mark(S_ATB, true);
         dim3 grid((ncols + 127) / 128, ns);
         if (prec_in == 0) cgd::k_atb_partial<double><<<grid, 128, 0, st>>>((const double*)A, lda, nrows, ncols, b, partial);
         else cgd::k_atb_partial<float><<<grid, 128, 0, st>>>((const float*)A, lda, nrows, ncols, b, partial);
         cgd::k_atb_reduce<<<(ncols + 127) / 128, 128, 0, st>>>(partial, ns, ncols, h);
+        mark(S_ATB, false);
         ck(cudaGetLastError(), "k_atb");
         ck(cudaFreeAsync(partial, st), "atb scratch free");
     }
@@ -328,8 +332,10 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         cublasSetStream(hnd, st);
         const double one = 1.0;
         // row-major A (nrows x ncols) is column-major X = A^T (ncols x nrows); G = X X^T.
+        mark(S_SYRK, true);
         cublasStatus_t s = cublasDsyrk(hnd, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, ncols, (int)nrows, &one,
                                        (const double*)A, (int)lda, &one, G, ncols);
+        mark(S_SYRK, false);
         if (s != CUBLAS_STATUS_SUCCESS) throw std::runtime_error("cublasDsyrk failed");
         return;   // lower triangle of column-major G == upper triangle of row-major G
     }
@@ -347,10 +353,12 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         __nv_bfloat16* hi = (__nv_bfloat16*)planes;
         __nv_bfloat16* lo = hi + cpad * kpad;
         dim3 tg((unsigned)(kpad / 32), (unsigned)(cpad / 32));
+        mark(S_SPLIT, true);
         if (prec_in == 0)
             cgd::k_split_transpose<double><<<tg, dim3(32, 8), 0, st>>>((const double*)A, lda, r0, nr, ncols, hi, lo, kpad);
         else
             cgd::k_split_transpose<float><<<tg, dim3(32, 8), 0, st>>>((const float*)A, lda, r0, nr, ncols, hi, lo, kpad);
+        mark(S_SPLIT, false);
         ck(cudaGetLastError(), "k_split_transpose");
         CUtensorMap mhi = plane_map(hi, kpad, cpad), mlo = plane_map(lo, kpad, cpad);
         // K slices: about four CTAs per SM in total
@@ -358,8 +366,10 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         int64_t nslice = std::max<int64_t>(1, std::min<int64_t>(ksteps, (608 + npairs - 1) / npairs));
         const int64_t kslice = (ksteps + nslice - 1) / nslice * cgd::GB_K;
         nslice = (kpad + kslice - 1) / kslice;
+        mark(S_TC, true);
         cgd::k_gram_tc<<<dim3(npairs, (unsigned)nslice), cgd::GB_THREADS, smem, st>>>(mhi, mlo, ntile, kpad, kslice,
                                                                                       ncols, G, d_err);
+        mark(S_TC, false);
         ck(cudaGetLastError(), "k_gram_tc");
     }
 }

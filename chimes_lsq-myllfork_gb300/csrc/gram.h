@@ -4,6 +4,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 
 namespace cg {
 
@@ -14,9 +15,11 @@ size_t gram_plane_bytes(int64_t nrows_block, int ncols);
 // device A block (row-major, lda; prec_in 0 = FP64, 1 = FP32).  mode 0: FP64 library
 // SYRK; mode 1: split-BF16 3-product Gram on tcgen05 (planes: scratch of at least
 // gram_plane_bytes(64, ncols) bytes; larger buffers take larger row blocks).
+// mark(stage, begin) brackets the A^T b, split, tensor and FP64 SYRK launches
+// (stage ids of session.h) for the optional CUDA-event timing.
 void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
                      double* G, double* h, void* planes, size_t planes_bytes, int* d_err, void* cublas,
-                     cudaStream_t st);
+                     cudaStream_t st, const std::function<void(int, bool)>& mark);
 // Copy the upper triangle of G to the lower one.
 void gram_symmetrize(double* G, int n, bool from_upper, cudaStream_t st);
 

@@ -37,7 +37,7 @@ struct MdBuckets {
     int* cursor;          // [nkeys] fill cursors
     int* val;             // [n] global cluster indices, grouped
 };
-constexpr int MDC_TILE = 128;   // clusters per contraction block
+constexpr int MDC_TILE = 64;    // clusters per contraction block
 
 // Group n clusters of a batch (cluster frame offsets cfo) by (frame, type).
 void launch_md_bucket(int64_t n, int nframes, const int64_t* cfo, const int* type, const MdBuckets& B,

@@ -266,9 +266,12 @@ void launch_key_frame_ofs(const int64_t* atom_ofs, int nframes, int per_type, in
 namespace cg {
 
 // ------------------------------------------------------------------ stage timing
+static_assert(ST_GRAM_ATB == 11 && ST_GRAM_SPLIT == 12 && ST_GRAM_TC == 13 && ST_GRAM_SYRK == 14,
+              "gram.cu brackets its launches with these stage ids");
+
 const char* stage_name(int s) {
     static const char* names[ST_COUNT] = {"frame_setup", "neighbour_lists", "clusters", "buckets", "force_2b",
-                                          "virial_2b", "force_3b", "virial_3b", "force_4b", "virial_4b", "other"};
+                                          "virial_2b", "force_3b", "virial_3b", "force_4b", "virial_4b", "other", "gram_atb", "gram_split", "gram_tensor", "gram_fp64_syrk"};
     return s >= 0 && s < ST_COUNT ? names[s] : "?";
 }
 
@@ -589,7 +592,8 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
         planes = S.get<unsigned char>(pbytes);
     }
     try {
-        gram_accumulate(prec_in, A, lda, nrows, ncols, b, mode, G, h, planes, pbytes, d_err, cublas_, stream_);
+        gram_accumulate(prec_in, A, lda, nrows, ncols, b, mode, G, h, planes, pbytes, d_err, cublas_, stream_,
+                        [this](int stage, bool begin) { mark(stage, begin); });
     } catch (const std::runtime_error& e) {
         throw Error(3, e.what());
     }
