@@ -285,6 +285,88 @@ def md_bench(cg, local):
     return out
 
 
+def fit4b_bench(cg, local, nframes, block, solve):
+    """The 4-body fit (256-atom C/H/N/O triclinic frames, 2B16 / 3B8 / 4B4, force +
+    stress + energy rows, 51,209 columns) in blocks of frames: the plain form (FP64
+    assembly + FP64 library Gram) against the mixed form (FP32 assembly + split-BF16
+    tcgen05 Gram).  The FP64 Gram runs about 0.4 TFLOP/s on this GPU, so it is timed
+    on one frame's rows and scaled per row (linear in rows)."""
+    import numpy as np
+    import torch
+    synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+    tmp = tempfile.mkdtemp(prefix="chimes_4b_")
+    fm = synth.make_workload("chno-4b", tmp, nframes=nframes, seed=2024)
+    model = cg.Model(fm)
+    C = model.ncols
+    nat, types, xyz, cell, frc, st, en = synth.frames_arrays(os.path.join(tmp, "traj.xyzf"), nframes,
+                                                             ["C", "H", "N", "O"])
+    sess = cg.Session(model, local)
+    stream = torch.cuda.ExternalStream(sess.stream)
+    ofs = np.concatenate([[0], np.cumsum(nat)])
+    blocks = []
+    for f0 in range(0, nframes, block):
+        f1 = min(nframes, f0 + block)
+        a, b = ofs[f0], ofs[f1]
+        fr = cg.Frames.from_arrays(model, nat[f0:f1], types[a:b], xyz[a:b], cell[f0:f1], forces=frc[a:b],
+                                   stress=st[f0:f1], energy=en[f0:f1], first_index=f0)
+        blocks.append((fr, sess.upload(fr), torch.from_numpy(fr.labels()).cuda()))
+    rows = sum(bl[0].nrows for bl in blocks)
+    maxr = max(bl[0].nrows for bl in blocks)
+    G = torch.zeros((C, C), dtype=torch.float64, device="cuda")
+    h = torch.zeros(C, dtype=torch.float64, device="cuda")
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    out = {"workload": f"chno-4b: {nframes} frames x 256 atoms (triclinic, Morse + Axilrod-Teller labels), "
+                       f"2B16@5.0 / 3B8@4.0 / 4B4@3.5, {rows} rows x {C} columns, blocks of {block} frames"}
+    for name, prec in (("fp64", cg.CG_FP64), ("fp32", cg.CG_FP32)):
+        A = torch.empty((maxr, C), dtype=torch.float64 if prec == cg.CG_FP64 else torch.float32, device="cuda")
+        sess.assemble_device(blocks[0][1], prec, A.data_ptr(), C)   # warm-up
+        t_asm, t_gram = 0.0, 0.0
+        G.zero_(); h.zero_()
+        for fr, dfr, bvec in blocks:
+            t_asm += timed(lambda: sess.assemble_device(dfr, prec, A.data_ptr(), C))
+            if prec == cg.CG_FP32:
+                t_gram += timed(lambda: sess.gram(1, A.data_ptr(), C, fr.nrows, C, bvec.data_ptr(), 1, G.data_ptr(),
+                                                  h.data_ptr()))
+        if prec == cg.CG_FP64:
+            # FP64 Gram on the first frame's rows, scaled per row
+            r1 = 780
+            Gs = torch.zeros((C, C), dtype=torch.float64, device="cuda")
+            hs = torch.zeros(C, dtype=torch.float64, device="cuda")
+            fr0, dfr0, b0 = blocks[0]
+            sess.assemble_device(dfr0, prec, A.data_ptr(), C)
+            t1 = timed(lambda: sess.gram(0, A.data_ptr(), C, r1, C, b0.data_ptr(), 0, Gs.data_ptr(), hs.data_ptr()))
+            t_gram = t1 * rows / r1
+            del Gs, hs
+        out[name] = {"assembly_rows_per_s": rows / t_asm, "assembly_s": t_asm, "gram_s": t_gram,
+                     "gram_timing": "measured over all rows" if prec == cg.CG_FP32 else
+                     "measured on 780 rows, scaled per row",
+                     "assembly_plus_gram_rows_per_s": rows / (t_asm + t_gram)}
+        del A
+        torch.cuda.empty_cache()
+    out["speedup_mixed_vs_plain"] = (out["fp64"]["assembly_s"] + out["fp64"]["gram_s"]) / (
+        out["fp32"]["assembly_s"] + out["fp32"]["gram_s"])
+    out["speedup_assembly_fp32_vs_fp64"] = out["fp64"]["assembly_s"] / out["fp32"]["assembly_s"]
+    if solve:
+        sess.gram_finish(G.data_ptr(), C)
+        lam = 1e-6 * float(torch.diagonal(G).abs().max())
+        x = torch.zeros(C, dtype=torch.float64, device="cuda")
+        t = time.perf_counter()
+        info = sess.solve(G.data_ptr(), h.data_ptr(), C, lam, 0, C, 0, 0, 0, x.data_ptr())
+        torch.cuda.synchronize()
+        out["solve_fp64_cholesky_s"] = time.perf_counter() - t
+        out["solve_ridge"] = info[2]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -296,6 +378,9 @@ def main():
     ap.add_argument("--frames", type=int, default=200, help="frames per rank (200 = the full workload)")
     ap.add_argument("--no-gram", action="store_true")
     ap.add_argument("--no-md", action="store_true")
+    ap.add_argument("--fit4b", type=int, default=0, metavar="FRAMES",
+                    help="also measure the 4-body fit (assembly + Gram, plain vs mixed) on FRAMES frames")
+    ap.add_argument("--fit4b-solve", action="store_true", help="with --fit4b: time the FP64 Cholesky of its Gram")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -411,6 +496,10 @@ def main():
         torch.cuda.empty_cache()
         md = md_bench(cg, local)
 
+    fit4b = None
+    if rank == 0 and args.fit4b > 0:
+        fit4b = fit4b_bench(cg, local, args.fit4b, 8, args.fit4b_solve)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         th = cpu_threads()
@@ -427,7 +516,7 @@ def main():
                        "parallelism": f"frames sharded, {world} rank(s), no collective"},
             "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "fp64": fp64,
             "stages_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in stages.items() if v[1]},
-            "work": counts, "cpu_baseline": cpu, "gram": gram, "roofline_gram": gram_roof, "md": md,
+            "work": counts, "cpu_baseline": cpu, "gram": gram, "roofline_gram": gram_roof, "md": md, "fit4b": fit4b,
         }
         print(json.dumps(line), flush=True)
     if dist:

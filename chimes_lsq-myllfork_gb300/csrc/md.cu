@@ -343,13 +343,17 @@ __device__ __forceinline__ void edge_ab(int NBODY, int e, int& a, int& b) {
 }
 
 // Per-thread geometry of a cluster, slot by slot (canonical slot s <- actual edge e).
-struct SlotGeom {
-    double r, R[3];
+// FP64: the exact H (s_b - s_a) distance of the enumeration; FP32 form: the FP32
+// Cartesian copy of the ghosts (the cluster set itself was decided exactly).
+template <typename R>
+struct SlotGeomT {
+    R r, R3[3];
     int a, b, pt;
 };
 
-template <int NBODY>
-__device__ __forceinline__ void cluster_geom(const ModelDev& M, const FramesDev& F, int f, int4 mm, SlotGeom* sg) {
+template <int NBODY, typename R>
+__device__ __forceinline__ void cluster_geom(const ModelDev& M, const FramesDev& F, int f, int4 mm,
+                                             SlotGeomT<R>* sg) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
     const int N = F.natoms[f];
     const int64_t gb = F.ghost_ofs[f];
@@ -365,12 +369,96 @@ __device__ __forceinline__ void cluster_geom(const ModelDev& M, const FramesDev&
         int a, b;
         edge_ab(NBODY, e, a, b);
         const int ga = member(mm, a), gbm = member(mm, b);
-        SlotGeom g;
+        SlotGeomT<R> g;
         g.a = a; g.b = b;
-        g.r = dist_exact(B.h, F.scaled + 3 * (gb + ga), F.scaled + 3 * (gb + gbm), g.R);
+        if constexpr (sizeof(R) == 8) {
+            g.r = dist_exact(B.h, F.scaled + 3 * (gb + ga), F.scaled + 3 * (gb + gbm), g.R3);
+        } else {
+            const float4* c32 = reinterpret_cast<const float4*>(F.cart32);
+            const float4 x = c32[gb + ga], y = c32[gb + gbm];
+            g.R3[0] = y.x - x.x; g.R3[1] = y.y - x.y; g.R3[2] = y.z - x.z;
+            g.r = sqrtf(g.R3[0] * g.R3[0] + g.R3[1] * g.R3[1] + g.R3[2] * g.R3[2]);
+        }
         g.pt = M.int_pair_map[typ[ga % N] * M.natmtyp + typ[gbm % N]];
         sg[s] = g;
     }
+}
+
+// FCUT::get_fcut (src/Fcut.C:17-72) in the contraction precision.
+template <typename R>
+__device__ __forceinline__ void fcut_r(const ModelDev& M, R r, R rmax, R& f, R& fd) {
+    if constexpr (sizeof(R) == 8) {
+        fcut_eval(M, r, rmax, f, fd);
+    } else {
+        if (M.fcut == 0) {
+            const float irm = 1.0f / rmax;
+            const float f0 = 1.0f - r * irm;
+            f = f0 * f0 * f0;
+            fd = f0 * f0 * (-3.0f * irm);
+        } else {
+            const float th = rmax - (float)M.fcut_offset * rmax;
+            if (r < th) { f = 1.0f; fd = 0.0f; }
+            else if (r > rmax) { f = 0.0f; fd = 0.0f; }
+            else {
+                const float a = (r - th) / (rmax - th) * (float)PI_REF + (float)PI_REF / 2.0f;
+                const float ad = (float)PI_REF / (rmax - th);
+                f = 0.5f + 0.5f * sinf(a);
+                fd = 0.5f * cosf(a) * ad;
+            }
+        }
+    }
+}
+
+// basis_regs in FP32 arithmetic (the FP32 form); FP64 uses basis_regs itself.
+template <int O, bool WANT_G, bool WANT_H>
+__device__ __forceinline__ void basis_regs_f(const ModelDev& M, float lambda, float xavg, float xdiff, float smin,
+                                             float r, float fc, float fd, float* g, float* h) {
+    const bool out = r < smin;
+    const float rr = out ? smin : r;
+    float x, ex = 0.0f;
+    const float ixd = 1.0f / xdiff;
+    if (M.trans == 0) { ex = expf(-rr / lambda); x = (ex - xavg) * ixd; }
+    else if (M.trans == 1) { x = (1.0f / rr - xavg) * ixd; }
+    else { x = (rr - xavg) * ixd; }
+    float dxdr;
+    if (M.trans == 0) dxdr = -ex / lambda * ixd;
+    else if (M.trans == 1) dxdr = -ixd / (rr * rr);
+    else dxdr = ixd;
+    dxdr *= (float)M.deriv_const;
+    const bool zero_d = out && M.fix == 1;
+    float damp = 1.0f, shift = 0.0f;
+    if (out && M.fix == 0) { damp = expf((r - smin) / (float)M.smooth); shift = (float)M.smooth * (damp - 1.0f); }
+    const float lin = (out && M.fix == 2) ? (r - smin) : 0.0f;
+    float t_prev = 1.0f, t_cur = x, u_prev2 = 0.0f, u_prev = 1.0f;
+#pragma unroll
+    for (int n = 0; n < O; ++n) {
+        float tn, un_1;
+        if (n == 0) { tn = 1.0f; un_1 = 0.0f; }
+        else if (n == 1) { tn = x; un_1 = 1.0f; }
+        else {
+            tn = 2.0f * x * t_cur - t_prev;
+            t_prev = t_cur; t_cur = tn;
+            const float un = (n - 1 == 1) ? 2.0f * x : 2.0f * x * u_prev - u_prev2;
+            u_prev2 = u_prev; u_prev = un;
+            un_1 = un;
+        }
+        float td = (n == 0 || zero_d) ? 0.0f : n * dxdr * un_1;
+        if (out) {
+            if (M.fix == 0) { tn += shift * td; td *= damp; }
+            else if (M.fix == 2) tn += td * lin;
+        }
+        if (WANT_G) g[n] = fc * tn;
+        if (WANT_H) h[n] = fc * td + fd * tn;
+    }
+}
+
+template <int O, bool WANT_G, bool WANT_H, typename R>
+__device__ __forceinline__ void basis_r(const ModelDev& M, double lambda, double xavg, double xdiff, double smin, R r,
+                                        R fc, R fd, R* g, R* h) {
+    if constexpr (sizeof(R) == 8)
+        basis_regs<O, WANT_G, WANT_H>(M, lambda, xavg, xdiff, smin, r, fc, fd, g, h);
+    else
+        basis_regs_f<O, WANT_G, WANT_H>(M, (float)lambda, (float)xavg, (float)xdiff, (float)smin, r, fc, fd, g, h);
 }
 
 template <int NBODY, int O, typename R>
@@ -380,7 +468,7 @@ __global__ void __launch_bounds__(MDC_THREADS) k_mdc(ModelDev M, MdDev D, Frames
     constexpr int SZ = IPow<NP, O>::v;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* sC = reinterpret_cast<R*>(smem_raw);
-    SlotGeom* sG = reinterpret_cast<SlotGeom*>(smem_raw + ((SZ * sizeof(R) + 15) & ~size_t(15)));
+    SlotGeomT<R>* sG = reinterpret_cast<SlotGeomT<R>*>(smem_raw + ((SZ * sizeof(R) + 15) & ~size_t(15)));
     int key;
     int64_t cb, t1;
     if (!tile_lookup(MB, blockIdx.x, key, cb, t1)) return;
@@ -397,57 +485,60 @@ __global__ void __launch_bounds__(MDC_THREADS) k_mdc(ModelDev M, MdDev D, Frames
         const int N = F.natoms[f];
         const int64_t aofs = F.atom_ofs[f];
         const BoxDev& B = F.box[f];
-        const double perm = NBODY == 3 ? B.perm3 : B.perm4;
+        const R perm = (R)(NBODY == 3 ? B.perm3 : B.perm4);
         const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
         const int4 mm = CS.m[MB.val[c]];
-        SlotGeom* sg = sG + (size_t)threadIdx.x * NP;
-        cluster_geom<NBODY>(M, F, f, mm, sg);
+        SlotGeomT<R>* sg = sG + (size_t)threadIdx.x * NP;
+        cluster_geom<NBODY, R>(M, F, f, mm, sg);
         R u[NP][O], G[NP][O];
 #pragma unroll
         for (int s = 0; s < NP; ++s) {
-            const SlotGeom& g = sg[s];
-            double fc, fd;
-            fcut_eval(M, g.r, CT.smax[s], fc, fd);
-            basis_regs<O, true, false>(M, M.pairs[g.pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], g.r, fc, fd,
-                                       u[s], (R*)nullptr);
+            const SlotGeomT<R>& g = sg[s];
+            R fc, fd;
+            fcut_r<R>(M, g.r, (R)CT.smax[s], fc, fd);
+            basis_r<O, true, false, R>(M, M.pairs[g.pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], g.r, fc, fd, u[s],
+                                       (R*)nullptr);
 #pragma unroll
             for (int k = 0; k < O; ++k) G[s][k] = R(0);
         }
         R E;
         if constexpr (NBODY == 3) E = contract3<O, R>(sC, u, G);
         else E = contract4<O, R>(sC, u, G);
-        v[0] = perm * (double)E;
-        double fm[NBODY][3];
+        v[0] = (double)(perm * E);
+        R fm[NBODY][3];
+        R w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-        for (int k = 0; k < NBODY; ++k) fm[k][0] = fm[k][1] = fm[k][2] = 0.0;
+        for (int k = 0; k < NBODY; ++k) fm[k][0] = fm[k][1] = fm[k][2] = R(0);
 #pragma unroll
         for (int s = 0; s < NP; ++s) {
-            const SlotGeom& g = sg[s];
-            double fc, fd;
-            fcut_eval(M, g.r, CT.smax[s], fc, fd);
+            const SlotGeomT<R>& g = sg[s];
+            R fc, fd;
+            fcut_r<R>(M, g.r, (R)CT.smax[s], fc, fd);
             R h[O];
-            basis_regs<O, false, true>(M, M.pairs[g.pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], g.r, fc, fd,
+            basis_r<O, false, true, R>(M, M.pairs[g.pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], g.r, fc, fd,
                                        (R*)nullptr, h);
             R gs = R(0);
 #pragma unroll
             for (int k = 0; k < O; ++k) gs = fma(G[s][k], h[k], gs);
-            const double ge = perm * (double)gs;
-            const double wv = ge / g.r;
+            const R ge = perm * gs;
+            const R wv = ge / g.r;
 #pragma unroll
             for (int k = 0; k < NBODY; ++k) {
-                if (k == g.a) { fm[k][0] += wv * g.R[0]; fm[k][1] += wv * g.R[1]; fm[k][2] += wv * g.R[2]; }
-                if (k == g.b) { fm[k][0] -= wv * g.R[0]; fm[k][1] -= wv * g.R[1]; fm[k][2] -= wv * g.R[2]; }
+                if (k == g.a) { fm[k][0] += wv * g.R3[0]; fm[k][1] += wv * g.R3[1]; fm[k][2] += wv * g.R3[2]; }
+                if (k == g.b) { fm[k][0] -= wv * g.R3[0]; fm[k][1] -= wv * g.R3[1]; fm[k][2] -= wv * g.R3[2]; }
             }
-            v[1] -= ge * g.r;
-            v[2] -= wv * g.R[0] * g.R[0]; v[3] -= wv * g.R[0] * g.R[1]; v[4] -= wv * g.R[0] * g.R[2];
-            v[5] -= wv * g.R[1] * g.R[1]; v[6] -= wv * g.R[1] * g.R[2]; v[7] -= wv * g.R[2] * g.R[2];
+            w[1] -= ge * g.r;
+            w[2] -= wv * g.R3[0] * g.R3[0]; w[3] -= wv * g.R3[0] * g.R3[1]; w[4] -= wv * g.R3[0] * g.R3[2];
+            w[5] -= wv * g.R3[1] * g.R3[1]; w[6] -= wv * g.R3[1] * g.R3[2]; w[7] -= wv * g.R3[2] * g.R3[2];
         }
+#pragma unroll
+        for (int k = 1; k < 8; ++k) v[k] = (double)w[k];
 #pragma unroll
         for (int k = 0; k < NBODY; ++k) {
             double* fo = Fo + 3 * (aofs + member(mm, k) % N);
-            atomicAdd(fo + 0, fm[k][0]);
-            atomicAdd(fo + 1, fm[k][1]);
-            atomicAdd(fo + 2, fm[k][2]);
+            atomicAdd(fo + 0, (double)fm[k][0]);
+            atomicAdd(fo + 1, (double)fm[k][1]);
+            atomicAdd(fo + 2, (double)fm[k][2]);
         }
     }
     block_scalars_add(v, So, f);
@@ -462,7 +553,7 @@ template <int NBODY>
 __global__ void __launch_bounds__(MDC_THREADS) k_mdc_generic(ModelDev M, MdDev D, FramesDev F, ClusterSet CS,
                                                              MdBuckets MB, int O, double* Fo, double* So) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
-    __shared__ SlotGeom sG[MDC_THREADS * NP];
+    __shared__ SlotGeomT<double> sG[MDC_THREADS * NP];
     int key;
     int64_t cb, t1;
     if (!tile_lookup(MB, blockIdx.x, key, cb, t1)) return;
@@ -480,11 +571,11 @@ __global__ void __launch_bounds__(MDC_THREADS) k_mdc_generic(ModelDev M, MdDev D
         const double perm = NBODY == 3 ? B.perm3 : B.perm4;
         const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
         const int4 mm = CS.m[MB.val[c]];
-        SlotGeom* sg = sG + (size_t)threadIdx.x * NP;
-        cluster_geom<NBODY>(M, F, f, mm, sg);
+        SlotGeomT<double>* sg = sG + (size_t)threadIdx.x * NP;
+        cluster_geom<NBODY, double>(M, F, f, mm, sg);
         double u[NP][MDG_MAXO], h[NP][MDG_MAXO], G[NP][MDG_MAXO];
         for (int s = 0; s < NP; ++s) {
-            const SlotGeom& g = sg[s];
+            const SlotGeomT<double>& g = sg[s];
             double fc, fd;
             fcut_eval(M, g.r, CT.smax[s], fc, fd);
             basis_gh(M, M.pairs[g.pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], g.r, 0, O, fc, fd, u[s], h[s], 1);
@@ -506,17 +597,17 @@ __global__ void __launch_bounds__(MDC_THREADS) k_mdc_generic(ModelDev M, MdDev D
         }
         v[0] = perm * E;
         for (int s = 0; s < NP; ++s) {
-            const SlotGeom& g = sg[s];
+            const SlotGeomT<double>& g = sg[s];
             double gs = 0.0;
             for (int k = 0; k < O; ++k) gs += G[s][k] * h[s][k];
             const double ge = perm * gs;
             const double wv = ge / g.r;
             double* fa = Fo + 3 * (aofs + member(mm, g.a) % N);
             double* fb = Fo + 3 * (aofs + member(mm, g.b) % N);
-            for (int k = 0; k < 3; ++k) { atomicAdd(fa + k, wv * g.R[k]); atomicAdd(fb + k, -wv * g.R[k]); }
+            for (int k = 0; k < 3; ++k) { atomicAdd(fa + k, wv * g.R3[k]); atomicAdd(fb + k, -wv * g.R3[k]); }
             v[1] -= ge * g.r;
-            v[2] -= wv * g.R[0] * g.R[0]; v[3] -= wv * g.R[0] * g.R[1]; v[4] -= wv * g.R[0] * g.R[2];
-            v[5] -= wv * g.R[1] * g.R[1]; v[6] -= wv * g.R[1] * g.R[2]; v[7] -= wv * g.R[2] * g.R[2];
+            v[2] -= wv * g.R3[0] * g.R3[0]; v[3] -= wv * g.R3[0] * g.R3[1]; v[4] -= wv * g.R3[0] * g.R3[2];
+            v[5] -= wv * g.R3[1] * g.R3[1]; v[6] -= wv * g.R3[1] * g.R3[2]; v[7] -= wv * g.R3[2] * g.R3[2];
         }
     }
     block_scalars_add(v, So, f);
@@ -615,7 +706,7 @@ template <int NBODY, int O, typename R>
 static void run_mdc(unsigned grid, const ModelDev& M, const MdDev& D, const FramesDev& F, const ClusterSet& CS,
                     const MdBuckets& B, double* Fo, double* So, cudaStream_t st) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
-    const size_t smem = ((IPow<NP, O>::v * sizeof(R) + 15) & ~size_t(15)) + sizeof(SlotGeom) * NP * MDC_THREADS;
+    const size_t smem = ((IPow<NP, O>::v * sizeof(R) + 15) & ~size_t(15)) + sizeof(SlotGeomT<R>) * NP * MDC_THREADS;
     static thread_local int attr_dev = -1;   // the attribute is per device
     int dev = 0;
     cudaGetDevice(&dev);
