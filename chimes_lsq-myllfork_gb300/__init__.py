@@ -92,6 +92,7 @@ def lib():
         "cg_gram_finish": (ctypes.c_int, [vp, vp, ctypes.c_int]),
         "cg_solve": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_double, vp, ctypes.c_int64, ctypes.c_int64, vp,
                                     ctypes.c_int, vp, vp]),
+        "cg_lars": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_int, vp, vp]),
         "cg_md_setup": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double]),
         "cg_md_force": (ctypes.c_int, [vp, vp, dp, dp]),
@@ -359,6 +360,13 @@ class Session:
                               ctypes.c_int64(int(nrows)), ctypes.c_void_p(int(b_ptr) or None), int(iters),
                               ctypes.c_void_p(int(x_ptr)), info))
         return info[0], info[1], info[2]
+
+    def lars(self, g_ptr, h_ptr, ncols, nsamples, alpha, x_ptr, max_iter=100000):
+        """LARS-lasso on the normal equations (cg_lars); returns (steps, active, final C/n)."""
+        info = (ctypes.c_double * 3)()
+        _check(lib().cg_lars(self._h, ctypes.c_void_p(int(g_ptr)), ctypes.c_void_p(int(h_ptr)), int(ncols),
+                             int(nsamples), float(alpha), int(max_iter), ctypes.c_void_p(int(x_ptr)), info))
+        return int(info[0]), int(info[1]), info[2]
 
     # ---------------------------------------------------------------- MD force
     def md_setup(self, x, precision=CG_FP64, energy_offsets=False, penalty_dist=0.01, penalty_scale=1.0e4):

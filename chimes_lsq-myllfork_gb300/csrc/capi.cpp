@@ -306,6 +306,14 @@ int cg_solve(cg_session* s, const double* G, const double* h, int ncols, double 
     });
 }
 
+int cg_lars(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter,
+            double* x, double* info) {
+    return guarded([&] {
+        need(s && G && h && x && ncols > 0 && nsamples > 0 && alpha >= 0.0 && max_iter > 0, "lars arguments");
+        s->s->lars(G, h, ncols, nsamples, alpha, max_iter, x, info);
+    });
+}
+
 int cg_session_last_launches(const cg_session* s, int64_t* launches) {
     return guarded([&] {
         need(s && launches, "session/launches");

@@ -32,4 +32,9 @@ void cholesky_solve(const double* L, int n, const double* h, double* x, void* cu
 void residual(const double* A, int64_t lda, int64_t nrows, int ncols, const double* b, const double* x, double* r,
               double* g, double* rnorm, double* gnorm, void* cublas, cudaStream_t st);
 
+// LARS with the lasso modification on G (full symmetric, FP64, device) and h:
+// coefficients into x (device); info: [steps, active variables, final C / n].
+void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
+                double* info, void* cublas, cudaStream_t st);
+
 }  // namespace cg

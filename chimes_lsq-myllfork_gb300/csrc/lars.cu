@@ -1,0 +1,347 @@
+// LARS with the lasso modification on the normal equations, FP64 on the device.
+//
+// Reference: `chimes_lsq.py --algorithm lassolars` (scikit-learn LassoLars,
+// src/chimes_lsq.py:248-263) and the DLARS code's active-set Cholesky updates
+// (contrib/dlars/src/dlars.C:1101-1329, Matrix::cholesky_add_row /
+// cholesky_remove_row contrib/dlars/src/Matrix.C:152, 215).  Published algorithm:
+// Efron, Hastie, Johnstone, Tibshirani, "Least angle regression" (2004), sec. 2-3.
+// Objective (1 / 2n) ||y - X w||^2 + alpha ||w||_1 with G = X^T X, h = X^T y.
+//
+// Device state: correlations c = h - G w, coefficients, the active list and the
+// lower Cholesky factor of G_AA (row-major, leading dimension kmax).  Per step:
+// the largest inactive |c| (block reduction), the factor's new row (cuBLAS DTRSV
+// on the stored factor, then one small kernel), the equiangular direction (two
+// DTRSV), a = sum_k w_k G[active_k, :] over contiguous rows of G, the step length
+// (block reductions over inactive crossings and active zero crossings), and on a
+// zero crossing the deletion of the variable from the factor by Givens rotations.
+#include <cublas_v2.h>
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace cgd {
+
+constexpr int LARS_THREADS = 1024;
+
+struct ArgMax {
+    double v;
+    int i;
+};
+
+__device__ __forceinline__ ArgMax amax(ArgMax a, ArgMax b) { return (b.v > a.v || (b.v == a.v && b.i < a.i)) ? b : a; }
+
+// max |c_j| over inactive j (flag 0); single block, lowest index wins ties
+__global__ void k_lars_argmax(const double* c, const int* flag, int n, ArgMax* out) {
+    __shared__ ArgMax sm[32];
+    ArgMax best{-1.0, -1};
+    for (int j = threadIdx.x; j < n; j += blockDim.x)
+        if (flag[j] == 0) best = amax(best, ArgMax{fabs(c[j]), j});
+    for (int o = 16; o > 0; o >>= 1) {
+        ArgMax other{__shfl_down_sync(0xffffffffu, best.v, o), __shfl_down_sync(0xffffffffu, best.i, o)};
+        best = amax(best, other);
+    }
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ArgMax b = sm[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = amax(b, sm[w]);
+        *out = b;
+    }
+}
+
+// v[k] = G[active_k, j]
+__global__ void k_lars_gather(const double* G, int n, const int* active, int na, int j, double* v) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < na) v[k] = G[(size_t)active[k] * n + j];
+}
+
+// d2 = G_jj - l.l (single block); out[0] = d2
+__global__ void k_lars_dot_rest(const double* l, int na, double gjj, double* out) {
+    __shared__ double sm[32];
+    double s = 0.0;
+    for (int k = threadIdx.x; k < na; k += blockDim.x) s += l[k] * l[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+        out[0] = gjj - t;
+    }
+}
+
+// row na of L: l (na entries) then sqrt(d2)
+__global__ void k_lars_put_row(double* L, int ld, int na, const double* l, double d2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < na) L[(size_t)na * ld + k] = l[k];
+    if (k == na) L[(size_t)na * ld + na] = sqrt(d2);
+}
+
+// s_k = sign(c[active_k])
+__global__ void k_lars_signs(const double* c, const int* active, int na, double* s) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < na) s[k] = c[active[k]] >= 0.0 ? 1.0 : -1.0;
+}
+
+// w <- w * AA with AA = (s.w)^-1/2 (single block); out[0] = AA
+__global__ void k_lars_scale(const double* s, double* w, int na, double* out) {
+    __shared__ double sm[32];
+    __shared__ double aa;
+    double t = 0.0;
+    for (int k = threadIdx.x; k < na; k += blockDim.x) t += s[k] * w[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double u = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) u += sm[q];
+        aa = 1.0 / sqrt(u);
+        out[0] = aa;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < na; k += blockDim.x) w[k] *= aa;
+}
+
+// a_j = sum_k w_k G[active_k, j]  (rows of the symmetric G: coalesced over j)
+__global__ void k_lars_direction(const double* G, int n, const int* active, const double* w, int na, double* a) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double s = 0.0;
+    for (int k = 0; k < na; ++k) s = fma(w[k], G[(size_t)active[k] * n + j], s);
+    a[j] = s;
+}
+
+struct MinPos {
+    double v;
+    int i;
+};
+__device__ __forceinline__ MinPos mmin(MinPos a, MinPos b) { return (b.v < a.v || (b.v == a.v && b.i < a.i)) ? b : a; }
+
+// out[0]: smallest positive inactive crossing (g1 or g2), out[1]: smallest positive
+// zero crossing -beta_k / w_k over the active list (index k).  `dropped`: the
+// variable that just left (its same-sign root is the current point).
+__global__ void k_lars_steps(const double* c, const double* a, const int* flag, int n, double C, double AA,
+                             int dropped, const double* beta, const int* active, const double* w, int na,
+                             MinPos* out) {
+    __shared__ MinPos s1[32], s2[32];
+    MinPos b1{INFINITY, -1}, b2{INFINITY, -1};
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        if (flag[j] != 0) continue;
+        const double g1 = (C - c[j]) / (AA - a[j]);
+        const double g2 = (C + c[j]) / (AA + a[j]);
+        const bool skip1 = j == dropped && c[j] > 0.0, skip2 = j == dropped && c[j] <= 0.0;
+        if (!skip1 && g1 > 0.0 && isfinite(g1)) b1 = mmin(b1, MinPos{g1, j});
+        if (!skip2 && g2 > 0.0 && isfinite(g2)) b1 = mmin(b1, MinPos{g2, j});
+    }
+    for (int k = threadIdx.x; k < na; k += blockDim.x) {
+        const double z = -beta[active[k]] / w[k];
+        if (z > 0.0 && isfinite(z)) b2 = mmin(b2, MinPos{z, k});
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        MinPos t1{__shfl_down_sync(0xffffffffu, b1.v, o), __shfl_down_sync(0xffffffffu, b1.i, o)};
+        MinPos t2{__shfl_down_sync(0xffffffffu, b2.v, o), __shfl_down_sync(0xffffffffu, b2.i, o)};
+        b1 = mmin(b1, t1);
+        b2 = mmin(b2, t2);
+    }
+    if ((threadIdx.x & 31) == 0) { s1[threadIdx.x >> 5] = b1; s2[threadIdx.x >> 5] = b2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        MinPos r1 = s1[0], r2 = s2[0];
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) { r1 = mmin(r1, s1[q]); r2 = mmin(r2, s2[q]); }
+        out[0] = r1;
+        out[1] = r2;
+    }
+}
+
+// beta[active] += gamma w; c -= gamma a
+__global__ void k_lars_update(double* beta, double* c, const double* a, const int* active, const double* w, int na,
+                              int n, double gamma) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < na) beta[active[j]] += gamma * w[j];
+    if (j < n) c[j] -= gamma * a[j];
+}
+
+// Delete variable k from the lower factor L (na x na, row-major, leading dim ld):
+// rows k+1.. move up one, then Givens rotations on columns (j, j+1), j = k..na-2,
+// restore the lower triangle (single block).
+__global__ void k_lars_chol_delete(double* L, int ld, int na, int k) {
+    for (int i = k; i < na - 1; ++i) {
+        for (int q = threadIdx.x; q <= i + 1; q += blockDim.x) L[(size_t)i * ld + q] = L[(size_t)(i + 1) * ld + q];
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < na; q += blockDim.x) L[(size_t)(na - 1) * ld + q] = 0.0;
+    __syncthreads();
+    __shared__ double cs, sn;
+    for (int j = k; j < na - 1; ++j) {
+        if (threadIdx.x == 0) {
+            const double a = L[(size_t)j * ld + j], b = L[(size_t)j * ld + j + 1];
+            const double r = hypot(a, b);
+            cs = a / r;
+            sn = b / r;
+        }
+        __syncthreads();
+        for (int i = j + threadIdx.x; i < na - 1; i += blockDim.x) {
+            const double x = L[(size_t)i * ld + j], y = L[(size_t)i * ld + j + 1];
+            L[(size_t)i * ld + j] = cs * x + sn * y;
+            L[(size_t)i * ld + j + 1] = -sn * x + cs * y;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace cgd
+
+namespace cg {
+
+static void ckl(cudaError_t e, const char* w) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error in ") + w + ": " + cudaGetErrorString(e));
+}
+static void cbl(cublasStatus_t s, const char* w) {
+    if (s != CUBLAS_STATUS_SUCCESS) throw std::runtime_error(std::string("cuBLAS error in ") + w);
+}
+
+// Returns [steps, active variables, final C / n]; x (device, n values) receives
+// the coefficients.  G: full symmetric FP64 (row-major), h: X^T y (device).
+void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
+                double* info, void* cublas, cudaStream_t st) {
+    cublasHandle_t hb = (cublasHandle_t)cublas;
+    cbl(cublasSetStream(hb, st), "setStream");
+    const int kmax = (int)std::min<int64_t>(n, std::max<int64_t>(nsamples, 1));
+    std::vector<void*> mem;
+    auto get = [&](size_t bytes) {
+        void* p = nullptr;
+        ckl(cudaMallocAsync(&p, std::max<size_t>(bytes, 8), st), "lars scratch");
+        mem.push_back(p);
+        return p;
+    };
+    try {
+        double* c = (double*)get(sizeof(double) * n);
+        double* a = (double*)get(sizeof(double) * n);
+        int* flag = (int*)get(sizeof(int) * n);
+        int* dact = (int*)get(sizeof(int) * kmax);
+        double* L = (double*)get(sizeof(double) * (size_t)kmax * kmax);
+        double* w = (double*)get(sizeof(double) * kmax);
+        double* sv = (double*)get(sizeof(double) * kmax);
+        double* scal = (double*)get(sizeof(double) * 4);
+        cgd::ArgMax* am = (cgd::ArgMax*)get(sizeof(cgd::ArgMax));
+        cgd::MinPos* mp = (cgd::MinPos*)get(sizeof(cgd::MinPos) * 2);
+        ckl(cudaMemcpyAsync(c, h, sizeof(double) * n, cudaMemcpyDeviceToDevice, st), "c = h");
+        ckl(cudaMemsetAsync(x, 0, sizeof(double) * n, st), "x = 0");
+        ckl(cudaMemsetAsync(flag, 0, sizeof(int) * n, st), "flags");
+        std::vector<int> active;
+        std::vector<int> hflag(n, 0);
+        const double target = (double)nsamples * alpha;
+        double C = 0.0;
+        bool drop = false;
+        int dropped = -1, steps = 0;
+        // C = max |h|
+        cgd::k_lars_argmax<<<1, cgd::LARS_THREADS, 0, st>>>(c, flag, n, am);
+        cgd::ArgMax hm{};
+        ckl(cudaMemcpyAsync(&hm, am, sizeof(hm), cudaMemcpyDeviceToHost, st), "argmax");
+        ckl(cudaStreamSynchronize(st), "sync");
+        C = hm.v;
+        const int tb = 256;
+        while (steps < max_iter && C > target) {
+            if (!drop) {
+                cgd::k_lars_argmax<<<1, cgd::LARS_THREADS, 0, st>>>(c, flag, n, am);
+                ckl(cudaMemcpyAsync(&hm, am, sizeof(hm), cudaMemcpyDeviceToHost, st), "argmax");
+                ckl(cudaStreamSynchronize(st), "sync");
+                if (hm.i < 0) break;
+                const int j = hm.i;
+                const int na = (int)active.size();
+                double gjj = 0.0;
+                ckl(cudaMemcpyAsync(&gjj, G + (size_t)j * n + j, sizeof(double), cudaMemcpyDeviceToHost, st), "Gjj");
+                double d2 = 0.0;
+                if (na == 0) {
+                    ckl(cudaStreamSynchronize(st), "sync");
+                    d2 = gjj;
+                } else {
+                    // L l = G[A, j]: the stored row-major lower factor is column-major upper U = L^T
+                    cgd::k_lars_gather<<<(na + tb - 1) / tb, tb, 0, st>>>(G, n, dact, na, j, sv);
+                    cbl(cublasDtrsv(hb, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, na, L, kmax, sv, 1),
+                        "trsv add");
+                    cgd::k_lars_dot_rest<<<1, cgd::LARS_THREADS, 0, st>>>(sv, na, gjj, scal);
+                    ckl(cudaMemcpyAsync(&d2, scal, sizeof(double), cudaMemcpyDeviceToHost, st), "d2");
+                    ckl(cudaStreamSynchronize(st), "sync");
+                }
+                const int one = 1, two = 2;
+                if (!(d2 > 1e-13 * gjj) || na >= kmax) {   // dependent on the active set: leave it out
+                    hflag[j] = 2;
+                    ckl(cudaMemcpyAsync(flag + j, &two, sizeof(int), cudaMemcpyHostToDevice, st), "flag");
+                    ckl(cudaStreamSynchronize(st), "sync");
+                    continue;
+                }
+                cgd::k_lars_put_row<<<(na + 1 + tb - 1) / tb, tb, 0, st>>>(L, kmax, na, sv, d2);
+                active.push_back(j);
+                hflag[j] = 1;
+                ckl(cudaMemcpyAsync(flag + j, &one, sizeof(int), cudaMemcpyHostToDevice, st), "flag");
+                ckl(cudaMemcpyAsync(dact + na, &active.back(), sizeof(int), cudaMemcpyHostToDevice, st), "active");
+                C = std::max(C, hm.v);
+                ckl(cudaStreamSynchronize(st), "sync");
+            }
+            drop = false;
+            const int na = (int)active.size();
+            // equiangular direction: L L^T w = s, w *= AA
+            cgd::k_lars_signs<<<(na + tb - 1) / tb, tb, 0, st>>>(c, dact, na, sv);
+            ckl(cudaMemcpyAsync(w, sv, sizeof(double) * na, cudaMemcpyDeviceToDevice, st), "w = s");
+            cbl(cublasDtrsv(hb, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, na, L, kmax, w, 1), "trsv 1");
+            cbl(cublasDtrsv(hb, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, na, L, kmax, w, 1), "trsv 2");
+            cgd::k_lars_scale<<<1, cgd::LARS_THREADS, 0, st>>>(sv, w, na, scal + 1);
+            cgd::k_lars_direction<<<(n + tb - 1) / tb, tb, 0, st>>>(G, n, dact, w, na, a);
+            double AA = 0.0;
+            ckl(cudaMemcpyAsync(&AA, scal + 1, sizeof(double), cudaMemcpyDeviceToHost, st), "AA");
+            ckl(cudaStreamSynchronize(st), "sync");
+            cgd::k_lars_steps<<<1, cgd::LARS_THREADS, 0, st>>>(c, a, flag, n, C, AA, dropped, x, dact, w, na, mp);
+            cgd::MinPos hp[2];
+            ckl(cudaMemcpyAsync(hp, mp, sizeof(hp), cudaMemcpyDeviceToHost, st), "steps");
+            ckl(cudaStreamSynchronize(st), "sync");
+            dropped = -1;
+            double gamma = std::min(C / AA, hp[0].v);
+            int kz = -1;
+            if (hp[1].i >= 0 && hp[1].v < gamma) {
+                gamma = hp[1].v;
+                kz = hp[1].i;
+                drop = true;
+            }
+            bool last = false;
+            if (C - gamma * AA < target) {   // land exactly on C / n = alpha
+                gamma = (C - target) / AA;
+                drop = false;
+                kz = -1;
+                last = true;
+            }
+            cgd::k_lars_update<<<(std::max(n, na) + tb - 1) / tb, tb, 0, st>>>(x, c, a, dact, w, na, n, gamma);
+            C -= gamma * AA;
+            ++steps;
+            if (last) break;
+            if (drop) {
+                const int var = active[kz];
+                const double zero = 0.0;
+                const int z0 = 0;
+                ckl(cudaMemcpyAsync(x + var, &zero, sizeof(double), cudaMemcpyHostToDevice, st), "beta = 0");
+                ckl(cudaMemcpyAsync(flag + var, &z0, sizeof(int), cudaMemcpyHostToDevice, st), "flag");
+                hflag[var] = 0;
+                cgd::k_lars_chol_delete<<<1, cgd::LARS_THREADS, 0, st>>>(L, kmax, na, kz);
+                active.erase(active.begin() + kz);
+                if (!active.empty())
+                    ckl(cudaMemcpyAsync(dact, active.data(), sizeof(int) * active.size(), cudaMemcpyHostToDevice, st),
+                        "active");
+                dropped = var;
+                ckl(cudaStreamSynchronize(st), "sync");
+            }
+            ckl(cudaGetLastError(), "lars step");
+        }
+        ckl(cudaStreamSynchronize(st), "sync");
+        if (info) { info[0] = steps; info[1] = (double)active.size(); info[2] = C / (double)nsamples; }
+    } catch (...) {
+        for (void* p : mem) cudaFreeAsync(p, st);
+        cudaStreamSynchronize(st);
+        throw;
+    }
+    for (void* p : mem) cudaFreeAsync(p, st);
+}
+
+}  // namespace cg

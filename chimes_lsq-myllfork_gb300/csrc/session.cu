@@ -603,6 +603,16 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
     if (herr) throw Error(3, "tensor-core Gram kernel timed out waiting on its pipeline (code " + std::to_string(herr) + ")");
 }
 
+void Session::lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter,
+                   double* x, double* info) {
+    CK(cudaSetDevice(device_));
+    try {
+        lars_lasso(G, h, ncols, nsamples, alpha, max_iter, x, info, cublas_, stream_);
+    } catch (const std::runtime_error& e) {
+        throw Error(3, e.what());
+    }
+}
+
 void Session::gram_finish(double* G, int ncols) {
     CK(cudaSetDevice(device_));
     gram_symmetrize(G, ncols, true, stream_);

@@ -127,6 +127,9 @@ class Session {
     void solve(const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda, int64_t nrows,
                const double* b, int iters, double* x, double* info);
     void* cublas() const { return cublas_; }
+    // LARS-lasso on the normal equations (lars.cu).
+    void lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter, double* x,
+              double* info);
 
     // MD force (md.h / md_host.cu).  md_setup stores the coefficients x (one per A
     // column): offsets adds the per-atom-type energy offsets of an energy fit.

@@ -144,6 +144,18 @@ int cg_gram_finish(cg_session* s, double* G, int ncols);
 int cg_solve(cg_session* s, const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda,
              int64_t nrows, const double* b, int iters, double* x, double* info);
 
+/* LARS with the lasso modification (the reference's `--algorithm lassolars`,
+ * scikit-learn LassoLars with fit_intercept=False, src/chimes_lsq.py:248-263; the
+ * active-set Cholesky updates of contrib/dlars/src/dlars.C:1101-1329) on the
+ * normal equations: G (full symmetric after cg_gram_finish) and h = A^T b, device
+ * FP64; nsamples = rows of A.  Minimises (1/2n)||b - A x||^2 + alpha ||x||_1 by
+ * following the path to C / n = alpha exactly; x (device) receives the
+ * coefficients.  info (host, 3 doubles, may be NULL): steps, active variables,
+ * final C / n.  The active-set factor is updated by rank-1 additions and Givens
+ * deletions in FP64. */
+int cg_lars(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter,
+            double* x, double* info);
+
 /* Work counters of the last assembly: accepted 2-body pairs, triplets, quadruplets,
  * and (cluster, allowed-power) evaluations of the 3- and 4-body terms. */
 int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads,
