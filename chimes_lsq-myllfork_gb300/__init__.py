@@ -73,6 +73,9 @@ def lib():
         "cg_frames_labels": (ctypes.c_int, [vp, dp]),
         "cg_frames_count": (ctypes.c_int, [vp, ip]),
         "cg_frames_independent": (ctypes.c_int, [vp]),
+        "cg_frames_slice": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, pp]),
+        "cg_model_params_read": (ctypes.c_int, [vp, ctypes.c_char_p, dp, ctypes.c_int]),
+        "cg_write_lsq_files": (ctypes.c_int, [vp, vp, dp, ctypes.c_int64, ctypes.c_char_p]),
         "cg_session_create": (ctypes.c_int, [vp, ctypes.c_int, pp]),
         "cg_session_free": (None, [vp]),
         "cg_session_stream": (ctypes.c_void_p, [vp]),
@@ -174,6 +177,12 @@ class Model:
     def ff_groups_map(self):
         return self._text(lib().cg_model_map_text)
 
+    def params_read(self, text):
+        """Coefficient vector of a params.txt text written for this model."""
+        x = np.zeros(self.ncols, dtype=np.float64)
+        _check(lib().cg_model_params_read(self._h, text.encode(), _ptr(x), x.size))
+        return x
+
     def params_txt(self, x, preamble=""):
         """params.txt text for the fitted coefficients x (one per A column)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -221,6 +230,17 @@ class Frames:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.cg_frames_free(self._h)
             self._h = None
+
+    def slice(self, first, count):
+        """Frames [first, first + count) as a new batch."""
+        h = ctypes.c_void_p()
+        _check(lib().cg_frames_slice(self._h, int(first), int(count), ctypes.byref(h)))
+        return Frames(h, self.model)
+
+    def write_lsq_files(self, A, directory):
+        """A.txt / b.txt / b-labeled.txt / natoms.txt / dim.txt for these frames (A: host FP64)."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        _check(lib().cg_write_lsq_files(self.model._h, self._h, _ptr(A), A.shape[1], os.fspath(directory).encode()))
 
     def independent(self):
         """Each frame decides the small-cell convention alone (MD systems)."""

@@ -10,6 +10,7 @@
 
 #include "model.h"
 #include "session.h"
+#include "textio.h"
 
 struct cg_model {
     cg::Model m;
@@ -116,6 +117,15 @@ int cg_model_params_text(const cg_model* h, const double* x, int nx, const char*
     });
 }
 
+int cg_model_params_read(const cg_model* h, const char* text, double* x, int nx) {
+    return guarded([&] {
+        need(h && text && x, "model/text/x");
+        need(nx == h->m.tot_all, "coefficient count");
+        std::vector<double> v = cg::params_txt_coefficients(h->m, text);
+        std::copy(v.begin(), v.end(), x);
+    });
+}
+
 int cg_frames_read(const cg_model* h, const char* path, int nframes, cg_frames** out) {
     return guarded([&] {
         need(h && out, "model/out");
@@ -182,10 +192,27 @@ int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms) {
     });
 }
 
+int cg_write_lsq_files(const cg_model* h, const cg_frames* fr, const double* A, int64_t lda, const char* dir) {
+    return guarded([&] {
+        need(h && fr && A && dir, "model/frames/A/dir");
+        need(lda >= h->m.tot_all, "lda");
+        cg::write_lsq_files(h->m, fr->fb, A, lda, dir);
+    });
+}
+
 int cg_frames_independent(cg_frames* fr) {
     return guarded([&] {
         need(fr, "frames");
         cg::make_independent(fr->fb);
+    });
+}
+
+int cg_frames_slice(const cg_frames* fr, int first, int count, cg_frames** out) {
+    return guarded([&] {
+        need(fr && out, "frames/out");
+        std::unique_ptr<cg_frames> o(new cg_frames());
+        o->fb = cg::slice_batch(fr->fb, first, count);
+        *out = o.release();
     });
 }
 

@@ -160,6 +160,34 @@ void set_small(cgd::BoxDev& bd, bool small) {
     bd.perm4 = small ? 0.5 / 3.0 / 4.0 : 1.0;
 }
 
+FrameBatch slice_batch(const FrameBatch& fb, int first, int count) {
+    if (first < 0 || count < 0 || first + count > fb.nframes) throw Error(1, "frame range outside the batch");
+    FrameBatch o;
+    o.nframes = count;
+    o.first_index = fb.first_index + first;
+    o.atom_ofs.push_back(0); o.ghost_ofs.push_back(0); o.row_ofs.push_back(0);
+    const int64_t nimg = fb.natoms.empty() ? 1 : (fb.ghost_ofs[1] - fb.ghost_ofs[0]) / std::max(1, fb.natoms[0]);
+    for (int k = first; k < first + count; ++k) {
+        const int n = fb.natoms[k];
+        o.natoms.push_back(n);
+        o.stress_rows.push_back(fb.stress_rows[k]);
+        o.energy_rows.push_back(fb.energy_rows[k]);
+        o.box.push_back(fb.box[k]);
+        o.small_self.push_back(fb.small_self[k]);
+        o.atom_ofs.push_back(o.atom_ofs.back() + n);
+        o.ghost_ofs.push_back(o.ghost_ofs.back() + nimg * n);
+        const int64_t rows = fb.row_ofs[k + 1] - fb.row_ofs[k];
+        o.row_ofs.push_back(o.row_ofs.back() + rows);
+        o.type.insert(o.type.end(), fb.type.begin() + fb.atom_ofs[k], fb.type.begin() + fb.atom_ofs[k + 1]);
+        o.xyz.insert(o.xyz.end(), fb.xyz.begin() + 3 * fb.atom_ofs[k], fb.xyz.begin() + 3 * fb.atom_ofs[k + 1]);
+        o.b.insert(o.b.end(), fb.b.begin() + fb.row_ofs[k], fb.b.begin() + fb.row_ofs[k + 1]);
+    }
+    o.nrows = o.row_ofs.back();
+    o.natoms_total = o.atom_ofs.back();
+    o.nghosts = o.ghost_ofs.back();
+    return o;
+}
+
 void make_independent(FrameBatch& fb) {
     for (int k = 0; k < fb.nframes; ++k) set_small(fb.box[k], fb.small_self[k] != 0);
 }

@@ -45,6 +45,8 @@ FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int firs
 // The small-cell convention is sticky along a trajectory (the fit reads frames in
 // sequence); independent configurations (MD systems) each decide it alone.
 void make_independent(FrameBatch& fb);
+// Frames [first, first + count) of a batch (their carried-over small-cell state kept).
+FrameBatch slice_batch(const FrameBatch& fb, int first, int count);
 void set_small(cgd::BoxDev& bd, bool small);
 
 // The same batch resident in device memory.

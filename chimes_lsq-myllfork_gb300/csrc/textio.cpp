@@ -1,0 +1,152 @@
+// Text files of the fit: A.txt / b.txt / b-labeled.txt / natoms.txt / dim.txt
+// (A_MAT::PRINT_FRAME and CLEANUP_FILES, src/A_Matrix.C:210-720) and the
+// coefficient reader of params.txt (the inverse of params_txt_text).
+#include "textio.h"
+
+#include <cstdio>
+#include <fstream>
+#include <sstream>
+#include <vector>
+
+namespace cg {
+
+namespace {
+
+struct Out {
+    std::FILE* f = nullptr;
+    explicit Out(const std::string& path) : f(std::fopen(path.c_str(), "w")) {
+        if (!f) throw Error(2, "cannot open " + path + " for writing");
+    }
+    ~Out() { if (f) std::fclose(f); }
+    void num(double v) { std::fprintf(f, "%.16e", v); }
+    void lab(double v) { std::fprintf(f, "%g", v); }   // default ostream format (6 significant digits)
+    void s(const char* t) { std::fputs(t, f); }
+};
+
+}  // namespace
+
+// Row order and separators follow PRINT_FRAME: force rows "%.16e   " per column,
+// b-labeled.txt values in the default stream format (%g),
+// stress and energy rows "%.16e " per column; with energy fitting each row ends in
+// " 0.0" per atom type (force / stress rows) or " <count of that type>" (energy rows).
+// natoms.txt has the frame's atom count per row; dim.txt "columns rows".
+void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int64_t lda, const std::string& dir) {
+    const int C = m.tot_short;
+    const int nener = m.tot_all - m.tot_short;
+    const bool do_ener = nener > 0;
+    Out fa(dir + "/A.txt"), fbv(dir + "/b.txt"), fbl(dir + "/b-labeled.txt"), fna(dir + "/natoms.txt");
+    int64_t row = 0;
+    for (int f = 0; f < fb.nframes; ++f) {
+        const int N = fb.natoms[f];
+        const int64_t a0 = fb.atom_ofs[f];
+        std::vector<int> count(m.ctl.natmtyp, 0);
+        for (int a = 0; a < N; ++a) count[fb.type[a0 + a]]++;
+        auto tail = [&](bool energy) {
+            if (do_ener)
+                for (int t = 0; t < m.ctl.natmtyp; ++t) {
+                    if (energy) std::fprintf(fa.f, " %d", count[t]);
+                    else fa.s(" 0.0");
+                }
+            std::fprintf(fna.f, "%d\n", N);
+            fa.s("\n");
+        };
+        const int64_t r0 = fb.row_ofs[f];
+        for (int a = 0; a < N; ++a) {
+            for (int q = 0; q < 3; ++q, ++row) {
+                const double* Ar = A + (r0 + 3 * a + q) * lda;
+                for (int c = 0; c < C; ++c) { fa.num(Ar[c]); fa.s("   "); }
+                tail(false);
+                const double bv = fb.b[r0 + 3 * a + q];
+                fbv.num(bv); fbv.s("\n");
+                fbl.s(m.atom_types[fb.type[a0 + a]].c_str()); fbl.s(" "); fbl.lab(bv); fbl.s("\n");
+            }
+        }
+        const int srows = fb.stress_rows[f], erows = fb.energy_rows[f];
+        static const char* l3[3] = {"s_xx ", "s_yy ", "s_zz "};
+        static const char* l9[9] = {"s_xx ", "s_xy ", "s_xz ", "s_yx ", "s_yy ", "s_yz ", "s_zx ", "s_zy ", "s_zz "};
+        for (int k = 0; k < srows; ++k, ++row) {
+            const int64_t r = r0 + 3 * N + k;
+            const double* Ar = A + r * lda;
+            for (int c = 0; c < C; ++c) { fa.num(Ar[c]); fa.s(" "); }
+            tail(false);
+            fbv.num(fb.b[r]); fbv.s("\n");
+            fbl.s(srows == 3 ? l3[k] : l9[k]); fbl.lab(fb.b[r]); fbl.s("\n");
+        }
+        for (int k = 0; k < erows; ++k, ++row) {
+            const int64_t r = r0 + 3 * N + srows + k;
+            const double* Ar = A + r * lda;
+            for (int c = 0; c < C; ++c) { fa.num(Ar[c]); fa.s(" "); }
+            tail(true);
+            fbv.num(fb.b[r]); fbv.s("\n");
+            fbl.s("+1 "); fbl.lab(fb.b[r]); fbl.s("\n");
+        }
+    }
+    Out fd(dir + "/dim.txt");
+    std::fprintf(fd.f, "%d %lld\n", m.tot_all, (long long)row);
+}
+
+// Coefficients from params.txt text: the 2-body blocks ("%3d %21.13e" lines after
+// "PAIRTYPE PARAMS:"), the cluster power lines (last field, param-index column) and
+// the energy offsets, placed in A-column order (src/chimes_lsq.py:462-672).
+std::vector<double> params_txt_coefficients(const Model& m, const std::string& text) {
+    std::vector<double> x(m.tot_all, 0.0);
+    std::vector<char> seen(m.tot_all, 0);
+    std::istringstream in(text);
+    std::string line;
+    std::vector<std::string> lines;
+    while (std::getline(in, line)) lines.push_back(line);
+    auto toks = [](const std::string& l) {
+        std::vector<std::string> t;
+        std::istringstream ss(l);
+        std::string w;
+        while (ss >> w) t.push_back(w);
+        return t;
+    };
+    const int snum = m.ctl.cheby_order;
+    int section = 0, pair = -1, ctype = -1, base = 0, tpar = 0;
+    const ClusterList* cl = nullptr;
+    auto put = [&](int col, double v) {
+        if (col < 0 || col >= m.tot_all) throw Error(2, "params.txt names a coefficient outside the model");
+        x[col] = v;
+        seen[col] = 1;
+    };
+    for (const std::string& l : lines) {
+        const auto t = toks(l);
+        if (t.empty() || t[0][0] == '!') continue;
+        if (t[0] == "PAIRMAPS:" || t[0] == "ENDFILE") { section = 0; continue; }   // ff_groups.map echo
+        if (t.size() >= 3 && t[2] == "PARAMS" && (t[0] == "PAIR" || t[0] == "TRIPLET" || t[0] == "QUADRUPLET")) {
+            section = t[0] == "PAIR" ? 2 : (t[0] == "TRIPLET" ? 3 : 4);
+            cl = section == 3 ? &m.trips : (section == 4 ? &m.quads : nullptr);
+            base = section == 3 ? m.tot_snum : m.tot_snum + m.num3;
+            ctype = -1;
+            tpar = 0;
+            continue;
+        }
+        if (section == 2 && t.size() >= 3 && t[0] == "PAIRTYPE" && t[1] == "PARAMS:") { pair = std::stoi(t[2]); continue; }
+        if ((section == 3 || section == 4) && t[0].rfind(section == 3 ? "TRIPLETTYPE" : "QUADRUPLETYPE", 0) == 0) {
+            if (ctype >= 0) tpar += cl->vec[ctype].n_true;
+            ++ctype;
+            continue;
+        }
+        if (t.size() >= 4 && t[0] == "ENERGY" && t[1] == "OFFSET") { put(m.tot_short + std::stoi(t[2]) - 1, std::stod(t[3])); continue; }
+        if (section == 2 && pair >= 0 && t.size() == 2 && snum > 0 && t[0].find_first_not_of("0123456789") == std::string::npos) {
+            const int k = std::stoi(t[0]);
+            if (k < snum) put(pair * snum + k, std::stod(t[1]));
+            continue;
+        }
+        if ((section == 3 || section == 4) && ctype >= 0 && ctype < (int)cl->vec.size()) {
+            const int npw = section == 3 ? 3 : 6;
+            if ((int)t.size() == npw + 4) {   // index, powers, equiv index, param index, value
+                bool numeric = true;
+                for (int k = 0; k < npw + 3 && numeric; ++k)
+                    numeric = t[k].find_first_not_of("0123456789") == std::string::npos;
+                if (numeric) put(base + tpar + std::stoi(t[npw + 2]), std::stod(t[npw + 3]));
+            }
+        }
+    }
+    for (int c = 0; c < m.tot_all; ++c)
+        if (!seen[c]) throw Error(2, "params.txt has no value for coefficient " + std::to_string(c));
+    return x;
+}
+
+}  // namespace cg

@@ -1,0 +1,135 @@
+"""Fit a ChIMES force field on the GPU: the drop-in for `chimes_lsq fm_setup.in`
+followed by `python chimes_lsq.py --algorithm ...` (src/chimes_lsq.C:108-424,
+src/chimes_lsq.py:1-675).
+
+    python chimes_lsq-myllfork_gb300/fit.py fm_setup.in [--algorithm ridge|lassolars]
+        [--alpha A] [--precision fp64|mixed] [--block-frames K] [--refine N] [--write-a] [--out DIR]
+
+Writes params.header, ff_groups.map, params.txt and force.txt (and, with
+--write-a, A.txt / b.txt / b-labeled.txt / natoms.txt / dim.txt) in the reference's
+formats.  The design matrix is assembled on the GPU in blocks of frames and folded
+into the normal equations G = A^T A, h = A^T b:
+  fp64   FP64 assembly, FP64 library Gram, FP64 Cholesky (ridge) or LARS;
+  mixed  FP32 assembly, split-BF16 tensor-core Gram; ridge is then refined by
+         conjugate gradients with FP64 products through an FP64 A (--refine N
+         iterations, when the FP64 A fits on the device).
+ridge solves (A^T A + alpha I) x = A^T b (scikit-learn Ridge(alpha,
+fit_intercept=False), the reference's --algorithm ridge); lassolars follows the
+LARS-lasso path to (1/2n)||b - A x||^2 + alpha ||x||_1 (the reference's
+--algorithm lassolars).  The reference's default truncated SVD is not offered:
+ridge with a small alpha replaces it.
+"""
+import argparse
+import datetime
+import importlib
+import math
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("fm_setup")
+    ap.add_argument("--algorithm", default="ridge", choices=["ridge", "lassolars"])
+    ap.add_argument("--alpha", type=float, default=1.0e-3)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--block-frames", type=int, default=64)
+    ap.add_argument("--refine", type=int, default=50, help="CG iterations of the mixed ridge solve")
+    ap.add_argument("--write-a", action="store_true", help="also write A.txt, b.txt, ... (slow for large A)")
+    ap.add_argument("--out", default=None, help="output directory (default: the fm_setup.in directory)")
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args(argv)
+
+    import numpy as np
+    import torch
+    cg = importlib.import_module("chimes_lsq-myllfork_gb300")
+    out = args.out or os.path.dirname(os.path.abspath(args.fm_setup))
+    os.makedirs(out, exist_ok=True)
+    model = cg.Model(args.fm_setup)
+    open(os.path.join(out, "params.header"), "w").write(model.params_header())
+    open(os.path.join(out, "ff_groups.map"), "w").write(model.ff_groups_map())
+    frames = cg.Frames.read(model)
+    torch.cuda.set_device(args.device)
+    sess = cg.Session(model, args.device)
+    C = model.ncols
+    nf = frames.nframes
+    mixed = args.precision == "mixed"
+    G = torch.zeros((C, C), dtype=torch.float64, device="cuda")
+    h = torch.zeros(C, dtype=torch.float64, device="cuda")
+    blocks = [frames.slice(f0, min(args.block_frames, nf - f0)) for f0 in range(0, nf, args.block_frames)]
+    nrows = sum(b.nrows for b in blocks)
+    fits = nrows * C * 8 < 0.5 * torch.cuda.mem_get_info()[0]
+    keep64 = fits and (not mixed or (args.algorithm == "ridge" and args.refine > 0))
+    A64_all = torch.empty((nrows, C), dtype=torch.float64, device="cuda") if keep64 else None
+    b_all = torch.empty(nrows, dtype=torch.float64, device="cuda")
+    r0 = 0
+    for blk in blocks:
+        dfr = sess.upload(blk)
+        n = blk.nrows
+        b_all[r0:r0 + n] = torch.from_numpy(blk.labels())
+        if mixed:
+            A32 = torch.empty((n, C), dtype=torch.float32, device="cuda")
+            sess.assemble_device(dfr, cg.CG_FP32, A32.data_ptr(), C)
+            sess.gram(1, A32.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 1, G.data_ptr(), h.data_ptr())
+            del A32
+        if keep64 or not mixed:
+            dst = A64_all[r0:r0 + n] if keep64 else torch.empty((n, C), dtype=torch.float64, device="cuda")
+            sess.assemble_device(dfr, cg.CG_FP64, dst.data_ptr(), C)
+            if not mixed:
+                sess.gram(0, dst.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr())
+            del dst
+        r0 += n
+    sess.gram_finish(G.data_ptr(), C)
+    x = torch.zeros(C, dtype=torch.float64, device="cuda")
+    lines = [f"! Date  {datetime.date.today()}", "!", f"! Number of variables            =  {C}",
+             f"! Number of equations            =  {nrows}"]
+    if args.algorithm == "ridge":
+        iters = args.refine if (mixed and keep64) else 0
+        sess.solve(G.data_ptr(), h.data_ptr(), C, args.alpha, A64_all.data_ptr() if iters else 0, C, nrows,
+                   b_all.data_ptr() if iters else 0, iters, x.data_ptr())
+        lines += ["! ridge regression used", "! Ridge alpha = %11.4e" % args.alpha]
+        if mixed:
+            lines += [f"! split-BF16 tensor-core Gram, FP64 Cholesky, {iters} FP64-product CG iterations"]
+    else:
+        sess.lars(G.data_ptr(), h.data_ptr(), C, nrows, args.alpha, x.data_ptr())
+        lines += ["! LARS implementation of LASSO used", "! LASSO alpha = %11.4e" % args.alpha]
+    torch.cuda.synchronize()
+    xh = x.cpu().numpy()
+    # predicted labels y = A x (force.txt) and the fit statistics
+    if keep64:
+        y = (A64_all @ x).cpu().numpy()
+    else:
+        ys = []
+        for blk in blocks:
+            dfr = sess.upload(blk)
+            A = torch.empty((blk.nrows, C), dtype=torch.float64, device="cuda")
+            sess.assemble_device(dfr, cg.CG_FP64, A.data_ptr(), C)
+            ys.append((A @ x).cpu().numpy())
+            del A
+        y = np.concatenate(ys)
+    b = b_all.cpu().numpy()
+    Z = float(((y - b) ** 2).sum())
+    nvars = C if args.algorithm == "ridge" else int(np.count_nonzero(xh))
+    bic = nrows * math.log(Z / nrows) + nvars * math.log(nrows)
+    lines += ["! RMS force error                = %11.4e" % math.sqrt(Z / nrows),
+              "! max abs variable               = %11.4e" % float(np.abs(xh).max()),
+              f"! number of fitting vars         =  {nvars}",
+              "! Bayesian Information Criterion = %11.4e" % bic, "!"]
+    with open(os.path.join(out, "force.txt"), "w") as f:
+        f.write("".join("%13.6e\n" % v for v in y))
+    open(os.path.join(out, "params.txt"), "w").write(model.params_txt(xh, "\n".join(lines) + "\n"))
+    if args.write_a:
+        A = A64_all.cpu().numpy() if keep64 else None
+        if A is None:
+            A = np.concatenate([sess.assemble(blk, cg.CG_FP64) for blk in blocks])
+        frames.write_lsq_files(A, out)
+    print(f"fit: {nrows} rows x {C} columns, {args.algorithm} alpha {args.alpha:g}, {args.precision}; "
+          f"RMS {math.sqrt(Z / nrows):.4e}; wrote {out}/params.txt")
+    return xh, y
+
+
+if __name__ == "__main__":
+    main()

@@ -54,6 +54,11 @@ int cg_model_map_text(const cg_model* m, char* buf, size_t cap, size_t* needed);
 int cg_model_params_text(const cg_model* m, const double* x, int nx, const char* preamble, char* buf, size_t cap,
                          size_t* needed);
 
+/* The coefficient vector (A-column order, nx = the model's column count) of a
+ * params.txt text written for this model: the inverse of cg_model_params_text,
+ * as chimes_md reads its PRMFILE (src/chimes_md.C:1700-2300). */
+int cg_model_params_read(const cg_model* m, const char* params_txt, double* x, int nx);
+
 /* Read nframes frames of an .xyzf trajectory (path NULL: the model's TRJFILE,
  * nframes <= 0: NFRAMES).  Replaces FRAME::READ_XYZF (src/ClassDefs.C:2411-2683). */
 int cg_frames_read(const cg_model* m, const char* xyzf_path, int nframes, cg_frames** out);
@@ -71,8 +76,19 @@ void cg_frames_free(cg_frames* fr);
 /* Rows of the A matrix for these frames and the total atom count. */
 int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms);
 
+/* A.txt, b.txt, b-labeled.txt, natoms.txt and dim.txt of the frames in directory
+ * dir, with A (host, row-major, lda >= columns) as assembled for them: the files of
+ * `chimes_lsq fm_setup.in` (A_MAT::PRINT_FRAME / CLEANUP_FILES,
+ * src/A_Matrix.C:210-720; %.16e, three spaces after force-row entries, one after
+ * stress / energy entries). */
+int cg_write_lsq_files(const cg_model* m, const cg_frames* fr, const double* A, int64_t lda, const char* dir);
+
 /* Number of frames in a batch. */
 int cg_frames_count(const cg_frames* fr, int* nframes);
+
+/* Frames [first, first + count) of a batch as a new batch (rows, labels and the
+ * small-cell state of the trajectory kept): for assembling a fit in row blocks. */
+int cg_frames_slice(const cg_frames* fr, int first, int count, cg_frames** out);
 
 /* Treat the frames as independent configurations: each decides the small-cell
  * neighbour convention (PERM_SCALE, src/ClassDefs.C:44-67) from its own box,

@@ -1,6 +1,7 @@
-"""Golden LARS-lasso coefficients from scikit-learn, the solver the reference's
-`chimes_lsq.py --algorithm lassolars` calls (src/chimes_lsq.py:248-263):
-`linear_model.LassoLars(alpha, fit_intercept=False, fit_path=False, max_iter=100000)`.
+"""Golden LARS-lasso and ridge coefficients from scikit-learn, the solvers the
+reference's `chimes_lsq.py --algorithm lassolars / ridge` call (src/chimes_lsq.py:
+216-263): `linear_model.LassoLars(alpha, fit_intercept=False, fit_path=False,
+max_iter=100000)` and `linear_model.Ridge(alpha, fit_intercept=False)`.
 
 Run where scikit-learn is installed (here: 1.9.0):
     python tests/golden/make_lars_fixtures.py
@@ -28,6 +29,12 @@ def main():
         out[key + "_coef"] = np.asarray(reg.coef_).ravel()
         out[key + "_steps"] = np.array(int(np.ravel(reg.n_iter_)[0]))
         print(key, "steps", int(np.ravel(reg.n_iter_)[0]), "nonzero", np.count_nonzero(out[key + "_coef"]))
+    # the reference's --algorithm ridge: Ridge(alpha, fit_intercept=False)
+    for name, alpha in (("water2b", 1e-3), ("ch4b", 1e-3)):
+        d = np.load(os.path.join(HERE, name, "ref.npz"))
+        reg = linear_model.Ridge(alpha=alpha, fit_intercept=False)
+        reg.fit(d["A"], d["b"])
+        out[f"{name}_ridge_{alpha:.0e}_coef"] = np.asarray(reg.coef_).ravel()
     np.savez_compressed(os.path.join(HERE, "lars", "sklearn_lassolars.npz"), **out)
 
 

@@ -158,3 +158,32 @@ def test_params_txt_rejects_wrong_count(cg):
         m.params_txt(np.zeros(m.ncols + 1))
     t = m.params_txt(np.arange(m.ncols, dtype=float))
     assert t.startswith(m.params_header().splitlines()[0]) and t.endswith("ENDFILE\n")
+
+
+@needs_ref
+@pytest.mark.parametrize("case", PARAMS_CASES)
+def test_params_txt_reader_matches_reference_coefficients(cg, case):
+    """params.txt -> coefficient vector equals the reference's test_suite_params.txt."""
+    d = os.path.join(REF_LSQ, case, "correct_output")
+    m = cg.Model(os.path.join(REF_LSQ, case, "fm_setup.in"))
+    x = np.array([float(ln.split()[1]) for ln in open(os.path.join(d, "test_suite_params.txt")) if ln.strip()])
+    assert np.array_equal(m.params_read(open(os.path.join(d, "params.txt")).read()), x)
+
+
+@needs_ref
+def test_lsq_text_files_match_reference_nonorth2(cg, tmp_path):
+    """A.txt / b.txt / b-labeled.txt / natoms.txt / dim.txt byte-identical to the
+    reference's for its own A values (the golden A.txt read back exactly)."""
+    src = os.path.join(REF_LSQ, "nonorth2")
+    for f in ("fm_setup.in", "input.xyzf"):
+        shutil.copy(os.path.join(src, f), tmp_path)
+    m = cg.Model(str(tmp_path / "fm_setup.in"))
+    frames = cg.Frames.read(m)
+    gold = os.path.join(src, "correct_output")
+    A = np.loadtxt(os.path.join(gold, "A.txt.aa"))
+    out = tmp_path / "out"
+    out.mkdir()
+    frames.write_lsq_files(A, out)
+    for f in ("A.txt", "b.txt", "b-labeled.txt", "natoms.txt", "dim.txt"):
+        ref = os.path.join(gold, "A.txt.aa" if f == "A.txt" else f)
+        assert open(out / f).read() == open(ref).read(), f
