@@ -95,6 +95,11 @@ def lib():
         "cg_gram_finish": (ctypes.c_int, [vp, vp, ctypes.c_int]),
         "cg_solve": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_double, vp, ctypes.c_int64, ctypes.c_int64, vp,
                                     ctypes.c_int, vp, vp]),
+        "cg_batch_fit_create": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int64, vp, vp, pp]),
+        "cg_batch_fit_launch": (ctypes.c_int, [vp, vp]),
+        "cg_batch_fit_nodes": (ctypes.c_int, [vp, i64p]),
+        "cg_batch_fit_free": (None, [vp]),
+        "cg_session_tune": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int]),
         "cg_lars": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_int, vp, vp]),
         "cg_md_setup": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double]),
@@ -298,6 +303,29 @@ class DeviceFrames:
         return p.value, n.value
 
 
+class BatchFit:
+    """A batched fit captured as one CUDA graph (cg_batch_fit_*)."""
+
+    def __init__(self, handle, session, keep):
+        self._h = handle
+        self.session = session
+        self._keep = keep
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cg_batch_fit_free(self._h)
+            self._h = None
+
+    def launch(self):
+        _check(lib().cg_batch_fit_launch(self.session._h, self._h))
+
+    @property
+    def nodes(self):
+        v = ctypes.c_int64()
+        _check(lib().cg_batch_fit_nodes(self._h, ctypes.byref(v)))
+        return v.value
+
+
 class Session:
     """One GPU (device ordinal) with a CUDA stream, bound to a model."""
 
@@ -380,6 +408,21 @@ class Session:
                               ctypes.c_int64(int(nrows)), ctypes.c_void_p(int(b_ptr) or None), int(iters),
                               ctypes.c_void_p(int(x_ptr)), info))
         return info[0], info[1], info[2]
+
+    def tune(self, key, value):
+        _check(lib().cg_session_tune(self._h, key.encode(), int(value)))
+
+    def batch_fit(self, dframes, label_ptrs, a_precision, a_ptr, lda, g_ptr, h_ptr):
+        """Capture the blocks' assembly + tensor-core Gram as one CUDA graph."""
+        n = len(dframes)
+        blocks = (ctypes.c_void_p * n)(*[d._h.value if isinstance(d._h, ctypes.c_void_p) else d._h for d in dframes])
+        labels = (ctypes.c_void_p * n)(*[int(p) for p in label_ptrs])
+        h = ctypes.c_void_p()
+        _check(lib().cg_batch_fit_create(self._h, n, ctypes.cast(blocks, ctypes.c_void_p),
+                                         ctypes.cast(labels, ctypes.c_void_p), int(a_precision),
+                                         ctypes.c_void_p(int(a_ptr)), int(lda), ctypes.c_void_p(int(g_ptr)),
+                                         ctypes.c_void_p(int(h_ptr)), ctypes.byref(h)))
+        return BatchFit(h, self, (dframes, blocks, labels))
 
     def lars(self, g_ptr, h_ptr, ncols, nsamples, alpha, x_ptr, max_iter=100000):
         """LARS-lasso on the normal equations (cg_lars); returns (steps, active, final C/n)."""

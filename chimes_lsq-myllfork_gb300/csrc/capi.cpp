@@ -23,6 +23,9 @@ struct cg_session {
     cg::AssembleStats last;
     cg::MdCounts md_last;
 };
+struct cg_batch_fit {
+    std::unique_ptr<cg::BatchFit> b;
+};
 struct cg_dframes {
     std::unique_ptr<cg::DeviceFrames> d;
     int64_t nrows = 0;
@@ -469,6 +472,52 @@ int cg_md_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, in
         if (triplets) *triplets = s->md_last.triplets;
         if (quads) *quads = s->md_last.quads;
         if (launches) *launches = s->md_last.launches;
+    });
+}
+
+// ------------------------------------------------------------------ batched fit
+int cg_batch_fit_create(cg_session* s, int nblocks, cg_dframes* const* blocks, const double* const* labels,
+                        int a_precision, void* A, int64_t lda, double* G, double* h, cg_batch_fit** out) {
+    return guarded([&] {
+        need(s && blocks && labels && A && G && h && out && nblocks > 0, "batch fit arguments");
+        need(a_precision == CG_FP64 || a_precision == CG_FP32, "precision");
+        std::vector<const cg::DeviceFrames*> bl(nblocks);
+        std::vector<const double*> lb(nblocks);
+        std::vector<cg::RunPlan> plans(nblocks);
+        for (int k = 0; k < nblocks; ++k) {
+            need(blocks[k] && labels[k], "block");
+            bl[k] = blocks[k]->d.get();
+            lb[k] = labels[k];
+            plans[k] = s->s->plan(*bl[k], a_precision, A, lda);   // sizing pass
+        }
+        std::unique_ptr<cg_batch_fit> o(new cg_batch_fit());
+        o->b = s->s->batch_fit_graph(bl, plans, lb, a_precision, A, lda, G, h);
+        *out = o.release();
+    });
+}
+
+int cg_batch_fit_launch(cg_session* s, cg_batch_fit* b) {
+    return guarded([&] {
+        need(s && b, "session/batch");
+        s->s->batch_fit_launch(*b->b);
+    });
+}
+
+int cg_batch_fit_nodes(const cg_batch_fit* b, int64_t* nodes) {
+    return guarded([&] {
+        need(b && nodes, "batch/nodes");
+        *nodes = b->b->nodes;
+    });
+}
+
+void cg_batch_fit_free(cg_batch_fit* b) { delete b; }
+
+int cg_session_tune(cg_session* s, const char* key, int value) {
+    return guarded([&] {
+        need(s && key, "session/key");
+        const std::string k(key);
+        if (k == "gram_ctas_per_sm") s->s->set_gram_ctas_per_sm(value);
+        else throw cg::Error(1, "unknown tuning key: " + k);
     });
 }
 

@@ -308,7 +308,7 @@ size_t gram_plane_bytes(int64_t nrows_block, int ncols) {
 
 void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
                      double* G, double* h, void* planes, size_t planes_bytes, int* d_err, void* cublas,
-                     cudaStream_t st, const std::function<void(int, bool)>& mark) {
+                     cudaStream_t st, const std::function<void(int, bool)>& mark, int ctas_per_sm) {
     if (nrows <= 0) return;
     // stage ids (session.h): ST_GRAM_ATB 11, ST_GRAM_SPLIT 12, ST_GRAM_TC 13, ST_GRAM_SYRK 14
     enum { S_ATB = 11, S_SPLIT = 12, S_TC = 13, S_SYRK = 14 };
@@ -361,9 +361,10 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         mark(S_SPLIT, false);
         ck(cudaGetLastError(), "k_split_transpose");
         CUtensorMap mhi = plane_map(hi, kpad, cpad), mlo = plane_map(lo, kpad, cpad);
-        // K slices: about four CTAs per SM in total
+        // K slices: about ctas_per_sm CTAs per SM in total (152 SMs)
         const int64_t ksteps = kpad / cgd::GB_K;
-        int64_t nslice = std::max<int64_t>(1, std::min<int64_t>(ksteps, (608 + npairs - 1) / npairs));
+        const int64_t target = 152 * (int64_t)std::max(1, ctas_per_sm);
+        int64_t nslice = std::max<int64_t>(1, std::min<int64_t>(ksteps, (target + npairs - 1) / npairs));
         const int64_t kslice = (ksteps + nslice - 1) / nslice * cgd::GB_K;
         nslice = (kpad + kslice - 1) / kslice;
         mark(S_TC, true);

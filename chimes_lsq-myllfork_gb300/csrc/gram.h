@@ -17,9 +17,10 @@ size_t gram_plane_bytes(int64_t nrows_block, int ncols);
 // gram_plane_bytes(64, ncols) bytes; larger buffers take larger row blocks).
 // mark(stage, begin) brackets the A^T b, split, tensor and FP64 SYRK launches
 // (stage ids of session.h) for the optional CUDA-event timing.
+// ctas_per_sm: target CTAs per SM when the K dimension is sliced (tunable).
 void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
                      double* G, double* h, void* planes, size_t planes_bytes, int* d_err, void* cublas,
-                     cudaStream_t st, const std::function<void(int, bool)>& mark);
+                     cudaStream_t st, const std::function<void(int, bool)>& mark, int ctas_per_sm = 4);
 // Copy the upper triangle of G to the lower one.
 void gram_symmetrize(double* G, int n, bool from_upper, cudaStream_t st);
 

@@ -433,17 +433,18 @@ __global__ void k_count_evals(const int* type, int64_t n, const cgd::ClusterType
 void Session::assemble(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats) {
     CK(cudaSetDevice(device_));
     Scratch S(stream_);
-    run(df, precision, A, lda, stats, S);
+    run(df, precision, A, lda, stats, S, nullptr, nullptr);
 }
 
 void Session::assemble_noalloc(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats) {
     CK(cudaSetDevice(device_));
     if (profiling_) throw Error(1, "stage profiling is not available in the no-allocation call");
     Scratch S(stream_, noalloc_scratch(device_), CG_NOALLOC_SCRATCH_BYTES);
-    run(df, precision, A, lda, stats, S);
+    run(df, precision, A, lda, stats, S, nullptr, nullptr);
 }
 
-void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats, Scratch& S) {
+void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats, Scratch& S,
+                  const RunPlan* plan_in, RunPlan* plan_out) {
     const cgd::ModelDev& M = dm_->dev;
     const cgd::FramesDev& F = df.dev;
     const Model& model = model_;
@@ -472,10 +473,15 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
     cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt3, nreal, NB.ofs3); L();
     cgd::k_scan_counts<<<1, 1024, 0, st>>>(NB.cnt4, nreal, NB.ofs4); L();
     int64_t tot[3] = {0, 0, 0};
-    CK(cudaMemcpyAsync(&tot[0], NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&tot[1], NB.ofs3 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&tot[2], NB.ofs4 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    if (plan_in) {   // sizes known from an earlier pass: no host synchronisation (capturable)
+        for (int k = 0; k < 3; ++k) tot[k] = plan_in->tot[k];
+    } else {
+        CK(cudaMemcpyAsync(&tot[0], NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&tot[1], NB.ofs3 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&tot[2], NB.ofs4 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    if (plan_out) for (int k = 0; k < 3; ++k) plan_out->tot[k] = tot[k];
     NB.i2 = S.get<int>(tot[0]); NB.g2 = S.get<int>(tot[0]); NB.pt2 = S.get<int>(tot[0]);
     NB.r2 = S.get<double>(tot[0]); NB.rab2 = S.get<double>(3 * tot[0]);
     NB.g3 = S.get<int>(tot[1]); NB.r3 = S.get<double>(tot[1]);
@@ -493,8 +499,13 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
         cgd::launch_clusters(nbody, M, F, NB, CS, 0, st); L();
         cgd::k_scan_counts<<<1, 1024, 0, st>>>(CS.cnt, nreal, CS.ofs); L();
         int64_t n = 0;
-        CK(cudaMemcpyAsync(&n, CS.ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        if (plan_in) {
+            n = plan_in->ncl[nbody - 3];
+        } else {
+            CK(cudaMemcpyAsync(&n, CS.ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+        if (plan_out) plan_out->ncl[nbody - 3] = n;
         CS.m = S.get<int4>(n);
         CS.type = S.get<int>(n);
         cgd::launch_clusters(nbody, M, F, NB, CS, 1, st); L();
@@ -572,8 +583,13 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
             CK(cudaMemsetAsync(d_max, 0, sizeof(int), st));
             cgd::launch_max_bucket(byt.key_ofs, kfo_types, nf, ntypes, d_max, st); L();
             int hmax = 0;
-            CK(cudaMemcpyAsync(&hmax, d_max, sizeof(int), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
+            if (plan_in) {
+                hmax = plan_in->hmax[nbody - 3];
+            } else {
+                CK(cudaMemcpyAsync(&hmax, d_max, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+            }
+            if (plan_out) plan_out->hmax[nbody - 3] = hmax;
             const int nch = std::max(1, (hmax + cgd::VIR_CLUSTERS - 1) / cgd::VIR_CLUSTERS);
             const auto& cl = nbody == 3 ? model.trips : model.quads;
             int ntrue_max = 1;
@@ -593,7 +609,7 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
         cgd::launch_energy_cols(prec, nf, M, F, A, lda, st); L();
         CK(cudaGetLastError());
     }
-    if (stats) {
+    if (stats && !plan_in) {
         unsigned long long ev[2] = {0, 0};
         CK(cudaMemcpyAsync(ev, d_evals, sizeof(ev), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -621,7 +637,7 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
     }
     try {
         gram_accumulate(prec_in, A, lda, nrows, ncols, b, mode, G, h, planes, pbytes, d_err, cublas_, stream_,
-                        [this](int stage, bool begin) { mark(stage, begin); });
+                        [this](int stage, bool begin) { mark(stage, begin); }, gram_ctas_per_sm_);
     } catch (const std::runtime_error& e) {
         throw Error(3, e.what());
     }
@@ -721,6 +737,71 @@ void Session::solve(const double* G, const double* h, int ncols, double ridge, c
         if (dynamic_cast<const Error*>(&e)) throw;
         throw Error(3, e.what());
     }
+}
+
+// ------------------------------------------------------------------ batched fit as one graph
+RunPlan Session::plan(const DeviceFrames& df, int precision, void* A, int64_t lda) {
+    CK(cudaSetDevice(device_));
+    RunPlan p;
+    Scratch S(stream_);
+    run(df, precision, A, lda, nullptr, S, nullptr, &p);
+    CK(cudaStreamSynchronize(stream_));
+    return p;
+}
+
+BatchFit::~BatchFit() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (d_err) cudaFree(d_err);
+}
+
+std::unique_ptr<BatchFit> Session::batch_fit_graph(const std::vector<const DeviceFrames*>& blocks,
+                                                   const std::vector<RunPlan>& plans,
+                                                   const std::vector<const double*>& labels, int precision,
+                                                   void* Abuf, int64_t lda, double* G, double* h) {
+    CK(cudaSetDevice(device_));
+    if (blocks.size() != plans.size() || blocks.size() != labels.size()) throw Error(1, "blocks / plans / labels");
+    if (profiling_) throw Error(1, "stage profiling is not available while capturing a graph");
+    const Model& m = model_;
+    std::unique_ptr<BatchFit> bf(new BatchFit());
+    CK(cudaMalloc((void**)&bf->d_err, sizeof(int)));
+    CK(cudaMemset(bf->d_err, 0, sizeof(int)));
+    const int ncols = m.tot_all;
+    int64_t maxrows = 1;
+    for (const DeviceFrames* d : blocks) maxrows = std::max<int64_t>(maxrows, d->nrows);
+    const int64_t cpad = (ncols + 127) / 128 * 128;
+    const int64_t rb = std::min<int64_t>(maxrows, std::max<int64_t>(64, (int64_t)(1ull << 30) / (4 * cpad)));
+    const size_t pbytes = gram_plane_bytes(rb, ncols);
+    CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
+    try {
+        for (size_t k = 0; k < blocks.size(); ++k) {
+            Scratch S(stream_);
+            run(*blocks[k], precision, Abuf, lda, nullptr, S, &plans[k], nullptr);
+            void* planes = S.get<unsigned char>(pbytes);
+            gram_accumulate(precision, Abuf, lda, blocks[k]->nrows, ncols, labels[k], 1, G, h, planes, pbytes,
+                            bf->d_err, cublas_, stream_, [](int, bool) {}, gram_ctas_per_sm_);
+        }
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(stream_, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    CK(cudaStreamEndCapture(stream_, &bf->graph));
+    CK(cudaGraphInstantiate(&bf->exec, bf->graph, 0));
+    size_t nodes = 0;
+    CK(cudaGraphGetNodes(bf->graph, nullptr, &nodes));
+    bf->nodes = (int64_t)nodes;
+    return bf;
+}
+
+void Session::batch_fit_launch(BatchFit& bf) {
+    CK(cudaSetDevice(device_));
+    CK(cudaGraphLaunch(bf.exec, stream_));
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, bf.d_err, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    if (herr) throw Error(3, "tensor-core Gram kernel timed out waiting on its pipeline (code " + std::to_string(herr) + ")");
 }
 
 }  // namespace cg

@@ -100,6 +100,24 @@ struct MdServeOptions {
     int max_batch_frames = 1024;
 };
 
+// Sizes of one batch's work lists, recorded by a sizing pass so that later passes
+// over the same batch need no host synchronisation (CUDA-graph capture).
+struct RunPlan {
+    int64_t tot[3] = {0, 0, 0};   // 2-body pairs, 3-body and 4-body candidate lists
+    int64_t ncl[2] = {0, 0};      // triplets, quadruplets
+    int hmax[2] = {0, 0};         // largest (frame, type) group of each
+};
+
+// A batched fit captured as one CUDA graph: every block's assembly and its
+// tensor-core Gram accumulation, replayed by one launch.
+struct BatchFit {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int* d_err = nullptr;
+    int64_t nodes = 0;
+    ~BatchFit();
+};
+
 // Pipeline stages timed with CUDA events when profiling is on.
 enum Stage {
     ST_SETUP = 0, ST_NEIGH, ST_CLUSTERS, ST_BUCKET, ST_FORCE2, ST_VIRIAL2, ST_FORCE3, ST_VIRIAL3, ST_FORCE4,
@@ -129,6 +147,17 @@ class Session {
     void solve(const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda, int64_t nrows,
                const double* b, int iters, double* x, double* info);
     void* cublas() const { return cublas_; }
+    // Sizing pass of a batch (a full assembly into A) recording its list sizes.
+    RunPlan plan(const DeviceFrames& df, int precision, void* A, int64_t lda);
+    // Capture the assembly of every block into Abuf (lda) and the split-BF16 Gram
+    // accumulation into G, h (labels: each block's b on the device) as one graph.
+    std::unique_ptr<BatchFit> batch_fit_graph(const std::vector<const DeviceFrames*>& blocks,
+                                              const std::vector<RunPlan>& plans,
+                                              const std::vector<const double*>& labels, int precision, void* Abuf,
+                                              int64_t lda, double* G, double* h);
+    void batch_fit_launch(BatchFit& bf);
+    void set_gram_ctas_per_sm(int v) { gram_ctas_per_sm_ = v > 0 ? v : 4; }
+    int gram_ctas_per_sm() const { return gram_ctas_per_sm_; }
     // LARS-lasso on the normal equations (lars.cu).
     void lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter, double* x,
               double* info);
@@ -161,7 +190,8 @@ class Session {
     void mark(int stage, bool begin);
 
    private:
-    void run(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats, struct Scratch& S);
+    void run(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats, struct Scratch& S,
+             const struct RunPlan* plan_in, struct RunPlan* plan_out);
     Model model_;
     bool profiling_ = false;
     struct Pending { int stage; cudaEvent_t a, b; };
@@ -176,6 +206,7 @@ class Session {
     void* cublas_ = nullptr;
     std::unique_ptr<DeviceModel> dm_;
     std::unique_ptr<MdTables> md_;
+    int gram_ctas_per_sm_ = 4;
 };
 
 }  // namespace cg

@@ -259,6 +259,27 @@ int cg_dframes_read_positions(const cg_dframes* d, double* xyz_host);
 /* Pairs, triplets, quadruplets and kernel launches of the last MD force call. */
 int cg_md_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads, int64_t* launches);
 
+/* ---------------------------------------------------------------- batched fit
+ * Thousands of frames in row blocks (uploaded with cg_frames_upload), each block
+ * assembled into the caller's A buffer (a_precision, lda >= columns, rows >= the
+ * largest block) and folded into G, h with the split-BF16 tensor-core Gram
+ * (caller zeroes G and h; labels[k]: block k's b, device).  Create runs one sizing
+ * pass per block (which also assembles it), then captures every block's launches
+ * -- assembly and Gram, no host synchronisation -- as one CUDA graph; launch
+ * replays the whole fit with one cudaGraphLaunch.  No counterpart in the reference
+ * (its frames are processed one at a time, src/chimes_lsq.C:292-328). */
+typedef struct cg_batch_fit cg_batch_fit;
+int cg_batch_fit_create(cg_session* s, int nblocks, cg_dframes* const* blocks, const double* const* labels,
+                        int a_precision, void* A, int64_t lda, double* G, double* h, cg_batch_fit** out);
+int cg_batch_fit_launch(cg_session* s, cg_batch_fit* b);
+int cg_batch_fit_nodes(const cg_batch_fit* b, int64_t* nodes);
+void cg_batch_fit_free(cg_batch_fit* b);
+
+/* Tunable launch parameters of a session (chosen by the autotuner,
+ * chimes_lsq-myllfork_gb300/autotune.py): "gram_ctas_per_sm" (CTAs per SM the
+ * tensor-core Gram aims for when it slices K; default 4). */
+int cg_session_tune(cg_session* s, const char* key, int value);
+
 const char* cg_last_error(void);
 
 #ifdef __cplusplus
