@@ -367,6 +367,85 @@ def fit4b_bench(cg, local, nframes, block, solve):
     return out
 
 
+def batched_bench(cg, local, nframes, per_frame_sample=24):
+    """Batched assembly streamed into the FP32-accumulated tensor-core Gram: frames
+    with log-uniform 32-1024 atoms, 4 species, cubic boxes at 0.1 atoms/A^3, the
+    4-body basis (2B16 / 3B8 / 4B4, 51,209 columns).  One CUDA graph replays every
+    block's assembly (FP32) and Gram; block size from the autotuner.  Against: the
+    same frames one at a time (per-frame assembly + Gram calls, host-synchronised)."""
+    import numpy as np
+    import torch
+    synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+    autotune = importlib.import_module("chimes_lsq-myllfork_gb300.autotune")
+    rng = np.random.default_rng(33)
+    sizes = np.exp(rng.uniform(np.log(32), np.log(1024), size=nframes)).astype(int)
+    tmp = tempfile.mkdtemp(prefix="chimes_batch_")
+    fm = synth.make_workload("chno-4b", tmp, nframes=nframes, seed=34, sizes=list(sizes), triclinic=False,
+                             density=0.1, labels=False)
+    model = cg.Model(fm)
+    frames = cg.Frames.read(model)
+    sess = cg.Session(model, local)
+    C = model.ncols
+    stream = torch.cuda.ExternalStream(sess.stream)
+    t0 = time.perf_counter()
+    choice, trials = autotune.tune_batch(cg, sess, frames, sizes, block_candidates=(16, 32, 64), sample_frames=64,
+                                         repeats=1, torch=torch)
+    tune_s = time.perf_counter() - t0
+    sess.tune("gram_ctas_per_sm", choice["gram_ctas_per_sm"])
+    bf = choice["block_frames"]
+    blocks = [frames.slice(f0, min(bf, nframes - f0)) for f0 in range(0, nframes, bf)]
+    rows = sum(b.nrows for b in blocks)
+    maxrows = max(b.nrows for b in blocks)
+    A = torch.empty((maxrows, C), dtype=torch.float32, device="cuda")
+    G = torch.zeros((C, C), dtype=torch.float64, device="cuda")
+    h = torch.zeros(C, dtype=torch.float64, device="cuda")
+    dfs = [sess.upload(b) for b in blocks]
+    labels = [torch.from_numpy(b.labels()).cuda() for b in blocks]
+    t0 = time.perf_counter()
+    g = sess.batch_fit(dfs, [l.data_ptr() for l in labels], cg.CG_FP32, A.data_ptr(), C, G.data_ptr(), h.data_ptr())
+    build_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    G.zero_(); h.zero_()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    graph_s = e0.elapsed_time(e1) / 1e3
+    # per-frame launches on a sample of the same frames
+    nper = min(per_frame_sample, nframes)
+    single = [frames.slice(f, 1) for f in range(nper)]
+    A1 = torch.empty((max(x.nrows for x in single), C), dtype=torch.float32, device="cuda")
+    d1 = [sess.upload(x) for x in single]
+    l1 = [torch.from_numpy(x.labels()).cuda() for x in single]
+    sess.assemble_device(d1[0], cg.CG_FP32, A1.data_ptr(), C)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for x, dfx, lx in zip(single, d1, l1):
+        sess.assemble_device(dfx, cg.CG_FP32, A1.data_ptr(), C)
+        sess.gram(1, A1.data_ptr(), C, x.nrows, C, lx.data_ptr(), 1, G.data_ptr(), h.data_ptr())
+    torch.cuda.synchronize()
+    per_s = time.perf_counter() - t0
+    rows_per = sum(x.nrows for x in single)
+    hbm, kind = peaks()
+    cpad = (C + 127) // 128 * 128
+    bytes_per_row = 4 * C + 4 * C + 4 * cpad + 4 * cpad   # A write, A read by the split, planes write + read
+    flops = rows * C * (C + 1)
+    pk, bkind = bf16_peak()
+    return {
+        "workload": f"{nframes} frames, N log-uniform in [32, 1024] (mean {sizes.mean():.0f}), 4 species, cubic "
+                    f"0.1/A^3, 2B16@5.0 / 3B8@4.0 / 4B4@3.5, {rows} rows x {C} columns",
+        "graph": {"rows_per_s": rows / graph_s, "seconds": graph_s, "blocks": len(blocks), "block_frames": bf,
+                  "graph_nodes": g.nodes, "capture_and_sizing_s": build_s,
+                  "hbm_gbs_algorithmic": rows * bytes_per_row / graph_s / 1e9, "hbm_peak_gbs": hbm,
+                  "gram_tflops_algorithmic": flops / graph_s / 1e12, "bf16_peak_over_3": pk / 3.0},
+        "per_frame": {"rows_per_s": rows_per / per_s, "frames": nper, "seconds": per_s},
+        "speedup_graph_vs_per_frame": (rows / graph_s) / (rows_per / per_s),
+        "autotune": {"choice": choice, "seconds": tune_s, "trials": trials},
+        "note": "bytes per row: FP32 A write + read by the BF16 split + BF16 hi/lo planes write + read",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -381,6 +460,8 @@ def main():
     ap.add_argument("--fit4b", type=int, default=0, metavar="FRAMES",
                     help="also measure the 4-body fit (assembly + Gram, plain vs mixed) on FRAMES frames")
     ap.add_argument("--fit4b-solve", action="store_true", help="with --fit4b: time the FP64 Cholesky of its Gram")
+    ap.add_argument("--batched", type=int, default=0, metavar="FRAMES",
+                    help="also measure the batched graph fit on FRAMES uneven 4-body frames")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -500,6 +581,10 @@ def main():
     if rank == 0 and args.fit4b > 0:
         fit4b = fit4b_bench(cg, local, args.fit4b, 8, args.fit4b_solve)
 
+    batched = None
+    if rank == 0 and args.batched > 0:
+        batched = batched_bench(cg, local, args.batched)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         th = cpu_threads()
@@ -516,7 +601,7 @@ def main():
                        "parallelism": f"frames sharded, {world} rank(s), no collective"},
             "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "fp64": fp64,
             "stages_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in stages.items() if v[1]},
-            "work": counts, "cpu_baseline": cpu, "gram": gram, "roofline_gram": gram_roof, "md": md, "fit4b": fit4b,
+            "work": counts, "cpu_baseline": cpu, "gram": gram, "roofline_gram": gram_roof, "md": md, "fit4b": fit4b, "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if dist:
