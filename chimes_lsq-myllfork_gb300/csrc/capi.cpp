@@ -517,6 +517,7 @@ int cg_session_tune(cg_session* s, const char* key, int value) {
         need(s && key, "session/key");
         const std::string k(key);
         if (k == "gram_ctas_per_sm") s->s->set_gram_ctas_per_sm(value);
+        else if (k == "md_skin_milli") s->s->set_md_skin(value * 1e-3);
         else throw cg::Error(1, "unknown tuning key: " + k);
     });
 }

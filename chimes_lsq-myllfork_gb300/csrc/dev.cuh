@@ -78,6 +78,11 @@ struct FramesDev {
     // derived by k_frame_setup
     double* scaled;                      // [ghosts*3] H^-1 x of every real and ghost atom
     float* cart32;                       // [ghosts*4] FP32 Cartesian copy for the pre-filter
+    // MD list reuse: the lattice shift that wraps each atom, computed when the lists
+    // are built (shift_mode 1) and reused until the next build (shift_mode 2), so a
+    // ghost index names the same image while atoms move.  null / 0: wrap each call.
+    int* shift;                          // [atoms*3]
+    int shift_mode;
 };
 
 // ---------------------------------------------------------------- exact FP64

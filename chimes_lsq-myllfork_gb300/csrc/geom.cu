@@ -35,17 +35,26 @@ __global__ void k_frame_setup(FramesDev F, int64_t total_ghosts) {
     const BoxDev& B = F.box[f];
     const double* x0 = F.xyz + 3 * (F.atom_ofs[f] + a);
     double w[3];
-    // WRAP_ATOM (src/ClassDefs.C:2075-2119)
+    // WRAP_ATOM (src/ClassDefs.C:2075-2119); with stored shifts (MD list reuse) the
+    // shift of the last list build is applied instead of a fresh floor
+    int* sh = (F.shift && F.shift_mode) ? F.shift + 3 * (F.atom_ofs[f] + a) : nullptr;
+    const bool use_stored = sh && F.shift_mode == 2;
+    const bool store = sh && F.shift_mode == 1 && k == 0;
     if (B.is_ortho) {
         double L3[3] = {B.lx, B.ly, B.lz};
         for (int q = 0; q < 3; ++q) {
-            int idx = (int)floor(__ddiv_rn(x0[q], L3[q]));
+            int idx = use_stored ? sh[q] : (int)floor(__ddiv_rn(x0[q], L3[q]));
+            if (store) sh[q] = idx;
             w[q] = subrn(x0[q], mulrn((double)idx, L3[q]));
         }
     } else {
         double t[3];
         for (int q = 0; q < 3; ++q) t[q] = dot3rn(B.inv[3 * q], B.inv[3 * q + 1], B.inv[3 * q + 2], x0[0], x0[1], x0[2]);
-        for (int q = 0; q < 3; ++q) { int idx = (int)floor(t[q]); t[q] = subrn(t[q], (double)idx); }
+        for (int q = 0; q < 3; ++q) {
+            int idx = use_stored ? sh[q] : (int)floor(t[q]);
+            if (store) sh[q] = idx;
+            t[q] = subrn(t[q], (double)idx);
+        }
         for (int q = 0; q < 3; ++q) w[q] = dot3rn(B.h[3 * q], B.h[3 * q + 1], B.h[3 * q + 2], t[0], t[1], t[2]);
     }
     double c[3] = {w[0], w[1], w[2]};
@@ -100,7 +109,7 @@ __global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDe
     const float4 ci = reinterpret_cast<const float4*>(F.cart32)[gbase + i];
     const double* si = F.scaled + 3 * (gbase + i);
     const float maxall = (float)fmax(fmax(M.maxcut2, M.order3 > 0 ? M.maxcut3 : 0.0), M.order4 > 0 ? M.maxcut4 : 0.0);
-    const float pre = maxall + MARGIN;
+    const float pre = maxall + MARGIN + (float)NB.skin;
     const int per = ((G + nw - 1) / nw + 31) & ~31;
     const int g0 = w * per, g1 = min(G, g0 + per);
     const unsigned lt = (1u << lane) - 1u;
@@ -118,9 +127,9 @@ __global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDe
                     r = dist_exact(B.h, si, F.scaled + 3 * (gbase + g), rab);
                     pt = M.int_pair_map[ti * M.natmtyp + typ[g % N]];
                     const PairDev P = M.pairs[pt];
-                    in2 = M.order2 > 0 && r < P.smax && (NB.md || r > P.smin);
-                    in3 = M.order3 > 0 && r < M.maxcut3;
-                    in4 = M.order4 > 0 && r < M.maxcut4;
+                    in2 = M.order2 > 0 && r < P.smax + NB.skin && (NB.md || r > P.smin);
+                    in3 = M.order3 > 0 && r < M.maxcut3 + NB.skin;
+                    in4 = M.order4 > 0 && r < M.maxcut4 + NB.skin;
                 }
             }
             const unsigned b2 = __ballot_sync(0xffffffffu, in2);
@@ -233,13 +242,15 @@ __global__ void k_clusters(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, 
                     const ClusterTypeDev& CT = types[T];
                     const int8_t* pm = pidx + id * (NB_ == 3 ? 3 : 6);
                     if (NB_ == 3) {
-                        ok = lr[a] < CT.smax[pm[0]] && lr[b] < CT.smax[pm[1]] &&
-                             within(F, B, gbase, j, k, CT.smax[pm[2]], dist32(c32, gbase + j, gbase + k));
+                        const double sk = NB.skin;
+                        ok = lr[a] < CT.smax[pm[0]] + sk && lr[b] < CT.smax[pm[1]] + sk &&
+                             within(F, B, gbase, j, k, CT.smax[pm[2]] + sk, dist32(c32, gbase + j, gbase + k));
                     } else {
-                        ok = lr[a] < CT.smax[pm[0]] && lr[b] < CT.smax[pm[1]] && lr[c] < CT.smax[pm[2]] &&
-                             within(F, B, gbase, j, k, CT.smax[pm[3]], dist32(c32, gbase + j, gbase + k)) &&
-                             within(F, B, gbase, j, l, CT.smax[pm[4]], dist32(c32, gbase + j, gbase + l)) &&
-                             within(F, B, gbase, k, l, CT.smax[pm[5]], dist32(c32, gbase + k, gbase + l));
+                        const double sk = NB.skin;
+                        ok = lr[a] < CT.smax[pm[0]] + sk && lr[b] < CT.smax[pm[1]] + sk && lr[c] < CT.smax[pm[2]] + sk &&
+                             within(F, B, gbase, j, k, CT.smax[pm[3]] + sk, dist32(c32, gbase + j, gbase + k)) &&
+                             within(F, B, gbase, j, l, CT.smax[pm[4]] + sk, dist32(c32, gbase + j, gbase + l)) &&
+                             within(F, B, gbase, k, l, CT.smax[pm[5]] + sk, dist32(c32, gbase + k, gbase + l));
                     }
                 }
             }
@@ -282,7 +293,7 @@ __global__ void k_quads(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int
     const int n = NB.cnt4[warp];
     const bool ordered = !B.small;
     const int ti = typ[i];
-    const float cut = (float)M.maxcut4 + MARGIN;
+    const float cut = (float)(M.maxcut4 + NB.skin) + MARGIN;
     int64_t out = fill ? CS.ofs[warp] : 0;
     int count = 0;
     const int npairs = n * n;
@@ -316,10 +327,12 @@ __global__ void k_quads(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int
                     if (ok) {
                         const ClusterTypeDev& CT = M.types4[T];
                         const int8_t* pm = M.pidx4 + id * 6;
-                        ok = lr[ab.x] < CT.smax[pm[0]] && lr[ab.y] < CT.smax[pm[1]] && lr[c] < CT.smax[pm[2]] &&
-                             within(F, B, gbase, j, k, CT.smax[pm[3]], dist32(c32, gbase + j, gbase + k)) &&
-                             within(F, B, gbase, j, l, CT.smax[pm[4]], dist32(c32, gbase + j, gbase + l)) &&
-                             within(F, B, gbase, k, l, CT.smax[pm[5]], dist32(c32, gbase + k, gbase + l));
+                        const double sk = NB.skin;
+                        ok = lr[ab.x] < CT.smax[pm[0]] + sk && lr[ab.y] < CT.smax[pm[1]] + sk &&
+                             lr[c] < CT.smax[pm[2]] + sk &&
+                             within(F, B, gbase, j, k, CT.smax[pm[3]] + sk, dist32(c32, gbase + j, gbase + k)) &&
+                             within(F, B, gbase, j, l, CT.smax[pm[4]] + sk, dist32(c32, gbase + j, gbase + l)) &&
+                             within(F, B, gbase, k, l, CT.smax[pm[5]] + sk, dist32(c32, gbase + k, gbase + l));
                     }
                 }
             }

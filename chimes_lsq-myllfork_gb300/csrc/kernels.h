@@ -15,8 +15,11 @@ struct NeighDev {
     int* g3; double* r3;
     int* g4; double* r4;
     // 0: the fit's 2-body filter s_min < r < s_max; 1: the MD force's r < s_max
-    // (Cheby::Force_all src/Cheby.C:1834 also evaluates r <= s_min, smoothed)
+    // (Cheby::Force_all src/Cheby.C:1834 also evaluates r <= s_min, smoothed);
+    // 2: MD lists reused over steps (pair distances recomputed, r < s_max tested)
     int md;
+    // MD list reuse: every cut-off of the enumeration widened by this skin (0: exact)
+    double skin;
 };
 
 struct ClusterSet {                               // triplets or quadruplets of a batch

@@ -100,9 +100,16 @@ __global__ void __launch_bounds__(256) k_md2(ModelDev M, MdDev D, FramesDev F, N
     for (int t = lane; t < n; t += 32) {
         const int64_t q = o + t;
         const int g = NB.g2[q], pt = NB.pt2[q];
-        const double r = NB.r2[q];
-        const double R[3] = {NB.rab2[3 * q], NB.rab2[3 * q + 1], NB.rab2[3 * q + 2]};
+        double r, R[3];
         const PairDev& P = M.pairs[pt];
+        if (NB.md == 2) {   // lists reused over steps: this step's distance, exact r < s_max
+            const int64_t gb = F.ghost_ofs[f];
+            r = dist_exact(B.h, F.scaled + 3 * (gb + (warp - aofs)), F.scaled + 3 * (gb + g), R);
+            if (!(r < P.smax)) continue;
+        } else {
+            r = NB.r2[q];
+            R[0] = NB.rab2[3 * q]; R[1] = NB.rab2[3 * q + 1]; R[2] = NB.rab2[3 * q + 2];
+        }
         double fc, fd;
         fcut_eval(M, r, P.smax, fc, fd);
         Dot2 acc{D.c2 + (size_t)pt * ord};
@@ -176,7 +183,7 @@ __global__ void k_md_bucket_count(int64_t n, int nframes, const int64_t* cfo, co
                                   int* cnt) {
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t q = base + threadIdx.x;
-        const bool ok = q < n;
+        const bool ok = q < n && type[q] >= 0;   // -1: filtered out this step
         const int key = ok ? frame_of_cluster(cfo, nframes, q) * ntypes + type[q] : 0;
         warp_agg_inc(cnt, key, ok);
     }
@@ -216,7 +223,7 @@ __global__ void k_md_bucket_fill(int64_t n, int nframes, const int64_t* cfo, con
                                  const int64_t* start, int* cursor, int* val) {
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t q = base + threadIdx.x;
-        const bool ok = q < n;
+        const bool ok = q < n && type[q] >= 0;
         const int key = ok ? frame_of_cluster(cfo, nframes, q) * ntypes + type[q] : 0;
         const int slot = warp_agg_inc(cursor, key, ok);
         if (ok) val[start[key] + slot] = (int)q;
@@ -613,6 +620,60 @@ __global__ void __launch_bounds__(MDC_THREADS) k_mdc_generic(ModelDev M, MdDev D
     block_scalars_add(v, So, f);
 }
 
+// ------------------------------------------------------------------ list reuse
+// Clusters of lists enumerated with a skin: keep a cluster this step iff every edge
+// is inside its slot's s_max (the same FP32-then-exact test as the enumeration);
+// type_out[q] = its type or -1.
+__device__ __forceinline__ bool within_md(const FramesDev& F, const BoxDev& B, int64_t gb, int a, int b, double smax) {
+    const float4* c32 = reinterpret_cast<const float4*>(F.cart32);
+    const float4 x = c32[gb + a], y = c32[gb + b];
+    const float dx = y.x - x.x, dy = y.y - x.y, dz = y.z - x.z;
+    const float r32 = sqrtf(dx * dx + dy * dy + dz * dz);
+    if (r32 < (float)smax - 1.0e-2f) return true;
+    if (r32 > (float)smax + 1.0e-2f) return false;
+    double rab[3];
+    return dist_exact(B.h, F.scaled + 3 * (gb + a), F.scaled + 3 * (gb + b), rab) < smax;
+}
+
+template <int NBODY>
+__global__ void k_md_filter(ModelDev M, FramesDev F, ClusterSet CS, const int64_t* cfo, int64_t n, int* type_out) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int f = frame_of_cluster(cfo, F.nframes, q);
+    const int4 mm = CS.m[q];
+    const int T = CS.type[q];
+    const int N = F.natoms[f];
+    const int64_t gb = F.ghost_ofs[f];
+    const int* typ = F.type + F.atom_ofs[f];
+    int id = 0, w = 1;
+#pragma unroll
+    for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
+    const int8_t* pm = (NBODY == 3 ? M.pidx3 : M.pidx4) + id * NP;
+    const ClusterTypeDev& CT = (NBODY == 3 ? M.types3 : M.types4)[T];
+    const BoxDev& B = F.box[f];
+    bool ok = true;
+#pragma unroll
+    for (int e = 0; e < NP; ++e) {
+        int a, b;
+        edge_ab(NBODY, e, a, b);
+        ok = ok && within_md(F, B, gb, member(mm, a), member(mm, b), CT.smax[pm[e]]);
+    }
+    type_out[q] = ok ? T : -1;
+}
+
+// Largest squared displacement since the lists were built (as ordered bits of a
+// non-negative double).
+__global__ void k_md_maxdisp(const double* x, const double* xref, int64_t n, unsigned long long* out) {
+    double m = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double dx = x[3 * i] - xref[3 * i], dy = x[3 * i + 1] - xref[3 * i + 1], dz = x[3 * i + 2] - xref[3 * i + 2];
+        m = fmax(m, dx * dx + dy * dy + dz * dz);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
 // ------------------------------------------------------------------ finish
 // ZCalc (src/functions.C:838-887): per-atom energy offsets, PRESSURE_XYZ / 3V,
 // tensor / V.
@@ -748,6 +809,18 @@ void launch_mdc(int nbody, int prec, int order, int64_t max_tiles, const ModelDe
     if (done) return;
     if (nbody == 3) k_mdc_generic<3><<<grid, MDC_THREADS, 0, st>>>(M, D, F, CS, B, order, Fo, So);
     else k_mdc_generic<4><<<grid, MDC_THREADS, 0, st>>>(M, D, F, CS, B, order, Fo, So);
+}
+
+void launch_md_filter(int nbody, const ModelDev& M, const FramesDev& F, const ClusterSet& CS, const int64_t* cfo,
+                      int64_t n, int* type_out, cudaStream_t st) {
+    if (n <= 0) return;
+    const unsigned g = (unsigned)((n + 255) / 256);
+    if (nbody == 3) k_md_filter<3><<<g, 256, 0, st>>>(M, F, CS, cfo, n, type_out);
+    else k_md_filter<4><<<g, 256, 0, st>>>(M, F, CS, cfo, n, type_out);
+}
+
+void launch_md_maxdisp(const double* x, const double* xref, int64_t n, unsigned long long* out, cudaStream_t st) {
+    if (n > 0) k_md_maxdisp<<<(unsigned)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, st>>>(x, xref, n, out);
 }
 
 void launch_md_finalize(int nframes, const ModelDev& M, const MdDev& D, const FramesDev& F, double* So,

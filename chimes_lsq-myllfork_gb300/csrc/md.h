@@ -55,6 +55,11 @@ void launch_mdc(int nbody, int prec, int order, int64_t max_tiles, const ModelDe
                 cudaStream_t st);
 void launch_md_finalize(int nframes, const ModelDev& M, const MdDev& D, const FramesDev& F, double* So,
                         cudaStream_t st);
+// List reuse: per-step exact filter of skin-enumerated clusters (type_out -1 when
+// out of range), and the largest squared displacement since the lists were built.
+void launch_md_filter(int nbody, const ModelDev& M, const FramesDev& F, const ClusterSet& CS, const int64_t* cfo,
+                      int64_t n, int* type_out, cudaStream_t st);
+void launch_md_maxdisp(const double* x, const double* xref, int64_t n, unsigned long long* out, cudaStream_t st);
 
 // Velocity Verlet (CONSTRAINT::UPDATE_COORDS / UPDATE_VELOCS_HALF_1 / _2,
 // src/ClassDefs.C:870-900, 1088-1157) over every real atom of the batch.

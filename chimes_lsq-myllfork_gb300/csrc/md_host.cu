@@ -163,6 +163,137 @@ void Session::md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts*
     if (counts) *counts = c;
 }
 
+void MdLists::release() {
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+    valid = false;
+}
+
+void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
+    CK(cudaSetDevice(device_));
+    const cgd::ModelDev& M = dm_->dev;
+    cudaStream_t st = stream_;
+    const int nf = df.nframes;
+    const int nreal = (int)df.natoms_total;
+    L.release();
+    L.skin = skin;
+    L.natoms = nreal;
+    auto get = [&](size_t bytes) {
+        void* p = nullptr;
+        CK(cudaMalloc(&p, std::max<size_t>(bytes, 8)));
+        L.allocs.push_back(p);
+        return p;
+    };
+    L.shift = (int*)get(sizeof(int) * 3 * std::max(nreal, 1));
+    L.xref = (double*)get(sizeof(double) * 3 * std::max(nreal, 1));
+    L.dmax = (unsigned long long*)get(sizeof(unsigned long long));
+    CK(cudaMemcpyAsync(L.xref, df.xyz, sizeof(double) * 3 * nreal, cudaMemcpyDeviceToDevice, st));
+    cgd::FramesDev F = df.dev;
+    F.shift = L.shift;
+    F.shift_mode = 1;   // wrap now and remember the shifts
+    cgd::launch_frame_setup(F, df.nghosts, st);
+    cgd::NeighDev& NB = L.NB;
+    NB = cgd::NeighDev{};
+    NB.n_real = nreal;
+    NB.md = 2;
+    NB.skin = skin;
+    NB.cnt2 = (int*)get(sizeof(int) * nreal); NB.cnt3 = (int*)get(sizeof(int) * nreal);
+    NB.cnt4 = (int*)get(sizeof(int) * nreal);
+    NB.ofs2 = (int64_t*)get(sizeof(int64_t) * (nreal + 1)); NB.ofs3 = (int64_t*)get(sizeof(int64_t) * (nreal + 1));
+    NB.ofs4 = (int64_t*)get(sizeof(int64_t) * (nreal + 1));
+    cgd::launch_neigh(M, F, NB, 0, st);
+    cgd::launch_scan_counts(NB.cnt2, nreal, NB.ofs2, st);
+    cgd::launch_scan_counts(NB.cnt3, nreal, NB.ofs3, st);
+    cgd::launch_scan_counts(NB.cnt4, nreal, NB.ofs4, st);
+    int64_t tot[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(&tot[0], NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&tot[1], NB.ofs3 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&tot[2], NB.ofs4 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    NB.i2 = (int*)get(sizeof(int) * tot[0]); NB.g2 = (int*)get(sizeof(int) * tot[0]);
+    NB.pt2 = (int*)get(sizeof(int) * tot[0]); NB.r2 = (double*)get(sizeof(double) * tot[0]);
+    NB.rab2 = (double*)get(sizeof(double) * 3 * tot[0]);
+    NB.g3 = (int*)get(sizeof(int) * tot[1]); NB.r3 = (double*)get(sizeof(double) * tot[1]);
+    NB.g4 = (int*)get(sizeof(int) * tot[2]); NB.r4 = (double*)get(sizeof(double) * tot[2]);
+    cgd::launch_neigh(M, F, NB, 1, st);
+    const bool use[2] = {M.order3 > 0, M.order4 > 0};
+    for (int k = 0; k < 2; ++k) {
+        if (!use[k]) continue;
+        L.CS[k].cnt = (int*)get(sizeof(int) * nreal);
+        L.CS[k].ofs = (int64_t*)get(sizeof(int64_t) * (nreal + 1));
+        cgd::launch_clusters(3 + k, M, F, NB, L.CS[k], 0, st);
+        cgd::launch_scan_counts(L.CS[k].cnt, nreal, L.CS[k].ofs, st);
+        CK(cudaMemcpyAsync(&L.ncl[k], L.CS[k].ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    for (int k = 0; k < 2; ++k) {
+        if (!use[k] || L.ncl[k] == 0) continue;
+        const int64_t n = L.ncl[k];
+        const int ntypes = k == 0 ? M.ntypes3 : M.ntypes4;
+        L.CS[k].m = (int4*)get(sizeof(int4) * n);
+        L.CS[k].type = (int*)get(sizeof(int) * n);
+        cgd::launch_clusters(3 + k, M, F, NB, L.CS[k], 1, st);
+        L.cfo[k] = (int64_t*)get(sizeof(int64_t) * (nf + 1));
+        cgd::launch_gather_frame_ofs(L.CS[k].ofs, F.atom_ofs, nf, L.cfo[k], st);
+        L.tstep[k] = (int*)get(sizeof(int) * n);
+        cgd::MdBuckets& B = L.B[k];
+        B.ntypes = ntypes;
+        B.nkeys = nf * ntypes;
+        B.start = (int64_t*)get(sizeof(int64_t) * (B.nkeys + 1));
+        B.tile_ofs = (int*)get(sizeof(int) * (B.nkeys + 1));
+        B.cursor = (int*)get(sizeof(int) * B.nkeys);
+        B.val = (int*)get(sizeof(int) * n);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    L.valid = true;
+    ++L.builds;
+}
+
+void Session::md_force_lists(DeviceFrames& df, MdLists& L, double* Fo, double* So) {
+    CK(cudaSetDevice(device_));
+    if (!md_) throw Error(1, "MD coefficients are not set (cg_md_setup)");
+    if (!L.valid) throw Error(1, "MD lists are not built");
+    const cgd::ModelDev& M = dm_->dev;
+    const cgd::MdDev& D = md_->dev;
+    cudaStream_t st = stream_;
+    const int nf = df.nframes;
+    const int nreal = (int)df.natoms_total;
+    CK(cudaMemsetAsync(Fo, 0, std::max<size_t>(1, (size_t)nreal * 3) * sizeof(double), st));
+    CK(cudaMemsetAsync(So, 0, std::max<size_t>(1, (size_t)nf * cgd::MD_NSCALAR) * sizeof(double), st));
+    cgd::FramesDev F = df.dev;
+    F.shift = L.shift;
+    F.shift_mode = 2;   // the build's images
+    cgd::launch_frame_setup(F, df.nghosts, st);
+    cgd::launch_md2(M, D, F, L.NB, Fo, So, st);
+    for (int k = 0; k < 2; ++k) {
+        const int64_t n = L.ncl[k];
+        if (n == 0 || !L.tstep[k]) continue;
+        cgd::ClusterSet CS = L.CS[k];
+        cgd::launch_md_filter(3 + k, M, F, CS, L.cfo[k], n, L.tstep[k], st);
+        CS.type = L.tstep[k];
+        cgd::launch_md_bucket(n, nf, L.cfo[k], L.tstep[k], L.B[k], st);
+        const int64_t max_tiles = (n + cgd::MDC_TILE - 1) / cgd::MDC_TILE + L.B[k].nkeys;
+        cgd::launch_mdc(3 + k, md_->precision, k == 0 ? M.order3 : M.order4, max_tiles, M, D, F, CS, L.B[k], Fo, So,
+                        st);
+    }
+    cgd::launch_md_finalize(nf, M, D, F, So, st);
+    CK(cudaGetLastError());
+}
+
+bool Session::md_lists_stale(const DeviceFrames& df, MdLists& L) {
+    if (!L.valid || L.natoms != df.natoms_total) return true;
+    cudaStream_t st = stream_;
+    CK(cudaMemsetAsync(L.dmax, 0, sizeof(unsigned long long), st));
+    cgd::launch_md_maxdisp(df.xyz, L.xref, L.natoms, L.dmax, st);
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, L.dmax, sizeof(bits), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double d2;
+    std::memcpy(&d2, &bits, sizeof(d2));
+    return d2 > 0.25 * L.skin * L.skin;
+}
+
 void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int nsteps, double* v, double* Fo,
                      double* So_steps, double* ke_steps) {
     CK(cudaSetDevice(device_));
@@ -185,10 +316,16 @@ void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int n
     CK(cudaMemcpyAsync(dm, m.data(), nt * sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dim, im.data(), nt * sizeof(double), cudaMemcpyHostToDevice, st));
     const cgd::FramesDev& F = df.dev;
+    MdLists lists;
     for (int step = 0; step <= nsteps; ++step) {
         if (step > 0) cgd::launch_md_drift(n, F, nullptr, df.xyz, v, acc, dt, st);   // UPDATE_COORDS + VELOCS_HALF_1
         double* sout = So_steps ? So_steps + (size_t)step * nf * cgd::MD_NSCALAR : so;
-        md_force(df, Fo, sout, nullptr);
+        if (md_skin_ > 0.0) {
+            if (md_lists_stale(df, lists)) md_lists_build(df, md_skin_, lists);
+            md_force_lists(df, lists, Fo, sout);
+        } else {
+            md_force(df, Fo, sout, nullptr);
+        }
         cgd::launch_md_kick(nf, F, Fo, dim, dm, acc, v, dt, step > 0 ? 1 : 0, nullptr,
                             ke_steps ? ke_steps + (size_t)step * nf : nullptr, st);   // a = F/m, VELOCS_HALF_2
         CK(cudaGetLastError());
@@ -326,6 +463,7 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
     std::vector<char> first(nreq, 0);
     int cur = 0, next_pending = 0, finished = 0;
     int64_t active_atoms = 0, nbatch = 0;
+    MdLists lists;   // skin lists of the current composition
     double mem = 0.0;
     bool changed = false;
     const auto t0 = std::chrono::steady_clock::now();
@@ -388,6 +526,7 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
             CK(cudaMemcpyAsync(B.type, h_type.p, ofs * sizeof(int), cudaMemcpyHostToDevice, st));
             cur ^= 1;
             changed = false;
+            lists.release();
         }
         ServeArena& C = arena[cur];
         for (int k = 0; k < nf; ++k) h_first.p[k] = first[active[k]] ? 1 : 0;
@@ -405,7 +544,12 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
         // one batched step
         const auto s0 = std::chrono::steady_clock::now();
         cgd::launch_md_drift(active_atoms, F, C.first, C.xyz, C.v, C.acc, opt.dt, st);
-        md_force(df, C.Fo, C.So, nullptr);
+        if (md_skin_ > 0.0) {
+            if (md_lists_stale(df, lists)) md_lists_build(df, md_skin_, lists);
+            md_force_lists(df, lists, C.Fo, C.So);
+        } else {
+            md_force(df, C.Fo, C.So, nullptr);
+        }
         cgd::launch_md_kick(nf, F, C.Fo, dim, dm, C.acc, C.v, opt.dt, 1, C.first, nullptr, st);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(st));

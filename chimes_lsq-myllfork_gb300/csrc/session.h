@@ -79,6 +79,28 @@ struct MdCounts {
     int64_t pairs2 = 0, triplets = 0, quads = 0, launches = 0;
 };
 
+// MD neighbour / cluster lists enumerated with a skin and reused over steps until
+// an atom has moved more than skin / 2 (the cluster set of each step is still
+// exact: a per-step filter keeps the clusters inside their cut-offs).
+struct MdLists {
+    std::vector<void*> allocs;
+    cgd::NeighDev NB{};
+    cgd::ClusterSet CS[2]{};
+    int64_t ncl[2] = {0, 0};
+    int* tstep[2] = {nullptr, nullptr};   // per-step type (-1: out of range)
+    int64_t* cfo[2] = {nullptr, nullptr};
+    cgd::MdBuckets B[2]{};
+    double* xref = nullptr;               // positions at the build
+    int* shift = nullptr;                 // wrap shifts at the build
+    unsigned long long* dmax = nullptr;
+    int64_t natoms = 0;
+    double skin = 0.0;
+    bool valid = false;
+    int64_t builds = 0;
+    void release();
+    ~MdLists() { release(); }
+};
+
 // One MD request of the serving loop (host arrays owned by the caller).
 struct MdRequest {
     int natoms = 0, nsteps = 0;
@@ -169,6 +191,13 @@ class Session {
     // Forces Fo [natoms_total*3] and per-frame scalars So [nframes*MD_NSCALAR]
     // (device pointers) of the batch's current positions.
     void md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts* counts);
+    // Skin lists: build, force with the lists (no host synchronisation), and the
+    // rebuild test (reads the largest displacement since the build).
+    void md_lists_build(DeviceFrames& df, double skin, MdLists& L);
+    void md_force_lists(DeviceFrames& df, MdLists& L, double* Fo, double* So);
+    bool md_lists_stale(const DeviceFrames& df, MdLists& L);
+    double md_skin() const { return md_skin_; }
+    void set_md_skin(double s) { md_skin_ = s >= 0.0 ? s : 0.0; }
     // nsteps velocity-Verlet steps (NVE) of every frame of the batch; df's positions
     // and v [natoms_total*3] (device) are advanced in place.  mass_type: host,
     // natmtyp masses.  So_steps [(nsteps+1)*nframes*MD_NSCALAR] and ke_steps
@@ -207,6 +236,7 @@ class Session {
     std::unique_ptr<DeviceModel> dm_;
     std::unique_ptr<MdTables> md_;
     int gram_ctas_per_sm_ = 4;
+    double md_skin_ = 0.5;   // Angstrom; 0: enumerate every step
 };
 
 }  // namespace cg

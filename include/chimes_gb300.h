@@ -277,7 +277,9 @@ void cg_batch_fit_free(cg_batch_fit* b);
 
 /* Tunable launch parameters of a session (chosen by the autotuner,
  * chimes_lsq-myllfork_gb300/autotune.py): "gram_ctas_per_sm" (CTAs per SM the
- * tensor-core Gram aims for when it slices K; default 4). */
+ * tensor-core Gram aims for when it slices K; default 4); "md_skin_milli" (the
+ * neighbour-list skin of cg_md_nve / cg_md_serve in 1e-3 A, default 500; 0 =
+ * enumerate every step; lists are rebuilt when an atom has moved half the skin). */
 int cg_session_tune(cg_session* s, const char* key, int value);
 
 const char* cg_last_error(void);
