@@ -163,10 +163,21 @@ void Session::md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts*
     if (counts) *counts = c;
 }
 
-void MdLists::release() {
-    for (void* p : allocs) cudaFree(p);
-    allocs.clear();
-    valid = false;
+void* MdLists::buffer(int slot, size_t bytes) {
+    bytes = std::max<size_t>(bytes, 8);
+    if ((int)allocs.size() <= slot) { allocs.resize(slot + 1, nullptr); caps.resize(slot + 1, 0); }
+    if (caps[slot] < bytes) {
+        if (allocs[slot]) CK(cudaFree(allocs[slot]));
+        allocs[slot] = nullptr;
+        const size_t grown = bytes + bytes / 4;   // room for the next build
+        CK(cudaMalloc(&allocs[slot], grown));
+        caps[slot] = grown;
+    }
+    return allocs[slot];
+}
+
+MdLists::~MdLists() {
+    for (void* p : allocs) if (p) cudaFree(p);
 }
 
 void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
@@ -178,12 +189,8 @@ void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
     L.release();
     L.skin = skin;
     L.natoms = nreal;
-    auto get = [&](size_t bytes) {
-        void* p = nullptr;
-        CK(cudaMalloc(&p, std::max<size_t>(bytes, 8)));
-        L.allocs.push_back(p);
-        return p;
-    };
+    int slot = 0;
+    auto get = [&](size_t bytes) { return L.buffer(slot++, bytes); };
     L.shift = (int*)get(sizeof(int) * 3 * std::max(nreal, 1));
     L.xref = (double*)get(sizeof(double) * 3 * std::max(nreal, 1));
     L.dmax = (unsigned long long*)get(sizeof(unsigned long long));

@@ -83,7 +83,8 @@ struct MdCounts {
 // an atom has moved more than skin / 2 (the cluster set of each step is still
 // exact: a per-step filter keeps the clusters inside their cut-offs).
 struct MdLists {
-    std::vector<void*> allocs;
+    std::vector<void*> allocs;            // grow-only buffers, one per slot, kept across rebuilds
+    std::vector<size_t> caps;
     cgd::NeighDev NB{};
     cgd::ClusterSet CS[2]{};
     int64_t ncl[2] = {0, 0};
@@ -97,8 +98,9 @@ struct MdLists {
     double skin = 0.0;
     bool valid = false;
     int64_t builds = 0;
-    void release();
-    ~MdLists() { release(); }
+    void release() { valid = false; }     // the buffers stay for the next build
+    void* buffer(int slot, size_t bytes);
+    ~MdLists();
 };
 
 // One MD request of the serving loop (host arrays owned by the caller).
