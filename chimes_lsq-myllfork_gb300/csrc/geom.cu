@@ -174,6 +174,125 @@ __global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDe
     sweep(true, o2, o3, o4, d2, d3, d4);
 }
 
+// ---------------------------------------------------------------- binned neighbour lists
+__device__ __forceinline__ int ghost_frame(const FramesDev& F, int64_t gid) {
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (F.ghost_ofs[mid] <= gid) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int bin_coord(double s, int L, int nb) {
+    // s spans [-L, L + 1) over the (2L+1) cell images
+    int b = (int)floor((s + L) / (2 * L + 1) * nb);
+    return b < 0 ? 0 : (b >= nb ? nb - 1 : b);
+}
+
+__device__ __forceinline__ int64_t bin_of(const FramesDev& F, const BinGrid& g, int64_t gid) {
+    const double* s = F.scaled + 3 * gid;
+    const int L = F.nlayers;
+    const int bx = bin_coord(s[0], L, g.nb[0]), by = bin_coord(s[1], L, g.nb[1]), bz = bin_coord(s[2], L, g.nb[2]);
+    return g.ofs + ((int64_t)bz * g.nb[1] + by) * g.nb[0] + bx;
+}
+
+__global__ void k_bin_count(FramesDev F, int64_t n, Bins B) {
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= n) return;
+    atomicAdd(B.count + bin_of(F, B.grid[ghost_frame(F, gid)], gid), 1);
+}
+
+__global__ void k_bin_fill(FramesDev F, int64_t n, Bins B) {
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= n) return;
+    const int f = ghost_frame(F, gid);
+    const int64_t bin = bin_of(F, B.grid[f], gid);
+    const int slot = atomicAdd(B.count + bin, 1);
+    B.atoms[B.start[bin] + slot] = (int)(gid - F.ghost_ofs[f]);
+}
+
+// One warp per real atom over the ghosts of the 27 bins around it; the per-ghost
+// tests are those of k_neigh.
+__global__ void __launch_bounds__(256) k_neigh_binned(ModelDev M, FramesDev F, NeighDev NB, Bins BN, int fill) {
+    const int atom = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (atom >= NB.n_real) return;
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (F.atom_ofs[mid] <= atom) lo = mid; else hi = mid - 1;
+    }
+    const int f = lo;
+    const int N = F.natoms[f];
+    const int i = atom - (int)F.atom_ofs[f];
+    const int64_t gbase = F.ghost_ofs[f];
+    const BoxDev& B = F.box[f];
+    const int* typ = F.type + F.atom_ofs[f];
+    const int ti = typ[i];
+    const float4 ci = reinterpret_cast<const float4*>(F.cart32)[gbase + i];
+    const double* si = F.scaled + 3 * (gbase + i);
+    const float maxall = (float)fmax(fmax(M.maxcut2, M.order3 > 0 ? M.maxcut3 : 0.0), M.order4 > 0 ? M.maxcut4 : 0.0);
+    const float pre = maxall + MARGIN + (float)NB.skin;
+    const BinGrid g = BN.grid[f];
+    const int L = F.nlayers;
+    const int cx = bin_coord(si[0], L, g.nb[0]), cy = bin_coord(si[1], L, g.nb[1]), cz = bin_coord(si[2], L, g.nb[2]);
+    int64_t o2 = 0, o3 = 0, o4 = 0;
+    if (fill) { o2 = NB.ofs2[atom]; o3 = NB.ofs3[atom]; o4 = NB.ofs4[atom]; }
+    int c2 = 0, c3 = 0, c4 = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int z = cz + dz;
+        if (z < 0 || z >= g.nb[2]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = cy + dy;
+            if (y < 0 || y >= g.nb[1]) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int x = cx + dx;
+                if (x < 0 || x >= g.nb[0]) continue;
+                const int64_t bin = g.ofs + ((int64_t)z * g.nb[1] + y) * g.nb[0] + x;
+                const int64_t b0 = BN.start[bin], b1 = BN.start[bin + 1];
+                for (int64_t base = b0; base < b1; base += 32) {
+                    const int64_t t = base + lane;
+                    bool in2 = false, in3 = false, in4 = false;
+                    double r = 0, rab[3] = {0, 0, 0};
+                    int pt = 0, gg = -1;
+                    if (t < b1) {
+                        gg = BN.atoms[t];
+                        if (gg != i && (B.small || i <= gg % N)) {
+                            const float4 cg = reinterpret_cast<const float4*>(F.cart32)[gbase + gg];
+                            const float ddx = cg.x - ci.x, ddy = cg.y - ci.y, ddz = cg.z - ci.z;
+                            const float r32 = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
+                            if (r32 < pre) {
+                                r = dist_exact(B.h, si, F.scaled + 3 * (gbase + gg), rab);
+                                pt = M.int_pair_map[ti * M.natmtyp + typ[gg % N]];
+                                const PairDev P = M.pairs[pt];
+                                in2 = M.order2 > 0 && r < P.smax + NB.skin && (NB.md || r > P.smin);
+                                in3 = M.order3 > 0 && r < M.maxcut3 + NB.skin;
+                                in4 = M.order4 > 0 && r < M.maxcut4 + NB.skin;
+                            }
+                        }
+                    }
+                    const unsigned b2 = __ballot_sync(0xffffffffu, in2);
+                    const unsigned b3 = __ballot_sync(0xffffffffu, in3);
+                    const unsigned b4 = __ballot_sync(0xffffffffu, in4);
+                    if (fill) {
+                        if (in2) {
+                            const int64_t p = o2 + c2 + __popc(b2 & lt);
+                            NB.i2[p] = i; NB.g2[p] = gg; NB.pt2[p] = pt; NB.r2[p] = r;
+                            NB.rab2[3 * p] = rab[0]; NB.rab2[3 * p + 1] = rab[1]; NB.rab2[3 * p + 2] = rab[2];
+                        }
+                        if (in3) { const int64_t p = o3 + c3 + __popc(b3 & lt); NB.g3[p] = gg; NB.r3[p] = r; }
+                        if (in4) { const int64_t p = o4 + c4 + __popc(b4 & lt); NB.g4[p] = gg; NB.r4[p] = r; }
+                    }
+                    c2 += __popc(b2); c3 += __popc(b3); c4 += __popc(b4);
+                }
+            }
+        }
+    }
+    if (!fill && lane == 0) { NB.cnt2[atom] = c2; NB.cnt3[atom] = c3; NB.cnt4[atom] = c4; }
+}
+
 // ---------------------------------------------------------------- clusters
 __device__ __forceinline__ float dist32(const float4* c, int64_t a, int64_t b) {
     float4 x = c[a], y = c[b];
@@ -445,6 +564,20 @@ void launch_neigh(const ModelDev& M, const FramesDev& F, const NeighDev& NB, int
     else
         k_neigh<<<(unsigned)NB.n_real, 32 * NEIGH_WARPS, 0, st>>>(M, F, NB, fill, NEIGH_WARPS);
 }
+void launch_bins(const FramesDev& F, int64_t n, const Bins& B, cudaStream_t st) {
+    if (n <= 0) return;
+    cudaMemsetAsync(B.count, 0, sizeof(int) * B.nbins, st);
+    k_bin_count<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, n, B);
+    launch_scan_counts(B.count, (int)B.nbins, B.start, st);
+    cudaMemsetAsync(B.count, 0, sizeof(int) * B.nbins, st);
+    k_bin_fill<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, n, B);
+}
+
+void launch_neigh_binned(const ModelDev& M, const FramesDev& F, const NeighDev& NB, const Bins& B, int fill,
+                         cudaStream_t st) {
+    if (NB.n_real > 0) k_neigh_binned<<<(unsigned)((NB.n_real + 7) / 8), 256, 0, st>>>(M, F, NB, B, fill);
+}
+
 void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const NeighDev& NB, const ClusterSet& CS,
                      int fill, cudaStream_t st) {
     if (NB.n_real <= 0) return;

@@ -71,9 +71,15 @@ __global__ void k_atb_partial(const T* __restrict__ A, int64_t lda, int64_t nr, 
     if (c >= ncols) return;
     const int64_t per = (nr + gridDim.y - 1) / gridDim.y;
     const int64_t r0 = (int64_t)blockIdx.y * per, r1 = min(nr, r0 + per);
-    double s = 0.0;
-    for (int64_t r = r0; r < r1; ++r) s = fma((double)A[r * lda + c], b[r], s);
-    partial[(int64_t)blockIdx.y * ncols + c] = s;
+    // eight independent chains keep eight row loads in flight per thread
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int64_t r = r0;
+    for (; r + 8 <= r1; r += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s[u] = fma((double)A[(r + u) * lda + c], b[r + u], s[u]);
+    }
+    for (int u = 0; r < r1; ++r, ++u) s[u] = fma((double)A[r * lda + c], b[r], s[u]);
+    partial[(int64_t)blockIdx.y * ncols + c] = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
 }
 __global__ void k_atb_reduce(const double* __restrict__ partial, int nslices, int ncols, double* __restrict__ h) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;

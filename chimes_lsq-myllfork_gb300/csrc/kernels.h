@@ -47,12 +47,33 @@ struct BucketSpec {
     const int* type;                              // kind 2
 };
 
+// Cell grid of one frame for the binned neighbour search: bins in fractional
+// coordinates over the ghost-extended cell, each at least the search radius wide
+// along its reciprocal direction, so neighbours lie in adjacent bins.
+struct BinGrid {
+    int nb[3];
+    int64_t ofs;                                  // first bin of the frame in the batch
+};
+struct Bins {
+    const BinGrid* grid;                          // [nframes]
+    int64_t nbins;
+    int* count;                                   // [nbins] then fill cursors
+    int64_t* start;                               // [nbins + 1]
+    int* atoms;                                   // [ghosts] frame-local ghost indices, grouped by bin
+};
+
 // Host launchers (kernels are defined in geom.cu).
 void launch_frame_setup(const FramesDev& F, int64_t total_ghosts, cudaStream_t st);
 void launch_neigh(const ModelDev& M, const FramesDev& F, const NeighDev& NB, int fill, cudaStream_t st);
 void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const NeighDev& NB, const ClusterSet& CS,
                      int fill, cudaStream_t st);
 void launch_bucket(int nframes, const FramesDev& F, const BucketSpec& S, const Buckets& out, cudaStream_t st);
+// Binned neighbour lists (MD list builds): bin every ghost, then the same count /
+// fill passes as launch_neigh over the 27 bins around each real atom (list order
+// follows the bins, not the ghost index).
+void launch_bins(const FramesDev& F, int64_t total_ghosts, const Bins& B, cudaStream_t st);
+void launch_neigh_binned(const ModelDev& M, const FramesDev& F, const NeighDev& NB, const Bins& B, int fill,
+                         cudaStream_t st);
 // Prefix sums and per-frame offsets (session.cu).
 void launch_scan_counts(const int* cnt, int n, int64_t* ofs, cudaStream_t st);
 void launch_gather_frame_ofs(const int64_t* ofs, const int64_t* atom_ofs, int nframes, int64_t* out, cudaStream_t st);

@@ -208,7 +208,36 @@ void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
     NB.cnt4 = (int*)get(sizeof(int) * nreal);
     NB.ofs2 = (int64_t*)get(sizeof(int64_t) * (nreal + 1)); NB.ofs3 = (int64_t*)get(sizeof(int64_t) * (nreal + 1));
     NB.ofs4 = (int64_t*)get(sizeof(int64_t) * (nreal + 1));
-    cgd::launch_neigh(M, F, NB, 0, st);
+    // binned search: fractional bins at least the search radius wide along each
+    // reciprocal direction (width_d = 1 / |row d of H^-1|)
+    const Model& mod = model_;
+    double rc = mod.max_cutoff_2b;
+    if (M.order3 > 0) rc = std::max(rc, mod.max_cutoff_3b);
+    if (M.order4 > 0) rc = std::max(rc, mod.max_cutoff_4b);
+    rc += skin + 0.02;
+    const int Lr = df.dev.nlayers;
+    std::vector<cgd::BinGrid> grid(nf);
+    int64_t nbins = 0;
+    for (int f = 0; f < nf; ++f) {
+        const cgd::BoxDev& bx = df.box_host.at(f);
+        for (int d = 0; d < 3; ++d) {
+            const double* row = bx.inv + 3 * d;
+            const double width = 1.0 / std::sqrt(row[0] * row[0] + row[1] * row[1] + row[2] * row[2]);
+            grid[f].nb[d] = std::max(1, std::min(256, (int)std::floor((2 * Lr + 1) * width / rc)));
+        }
+        grid[f].ofs = nbins;
+        nbins += (int64_t)grid[f].nb[0] * grid[f].nb[1] * grid[f].nb[2];
+    }
+    cgd::Bins BN{};
+    BN.nbins = nbins;
+    cgd::BinGrid* dgrid = (cgd::BinGrid*)get(sizeof(cgd::BinGrid) * nf);
+    CK(cudaMemcpyAsync(dgrid, grid.data(), sizeof(cgd::BinGrid) * nf, cudaMemcpyHostToDevice, st));
+    BN.grid = dgrid;
+    BN.count = (int*)get(sizeof(int) * nbins);
+    BN.start = (int64_t*)get(sizeof(int64_t) * (nbins + 1));
+    BN.atoms = (int*)get(sizeof(int) * df.nghosts);
+    cgd::launch_bins(F, df.nghosts, BN, st);
+    cgd::launch_neigh_binned(M, F, NB, BN, 0, st);
     cgd::launch_scan_counts(NB.cnt2, nreal, NB.ofs2, st);
     cgd::launch_scan_counts(NB.cnt3, nreal, NB.ofs3, st);
     cgd::launch_scan_counts(NB.cnt4, nreal, NB.ofs4, st);
@@ -222,7 +251,7 @@ void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
     NB.rab2 = (double*)get(sizeof(double) * 3 * tot[0]);
     NB.g3 = (int*)get(sizeof(int) * tot[1]); NB.r3 = (double*)get(sizeof(double) * tot[1]);
     NB.g4 = (int*)get(sizeof(int) * tot[2]); NB.r4 = (double*)get(sizeof(double) * tot[2]);
-    cgd::launch_neigh(M, F, NB, 1, st);
+    cgd::launch_neigh_binned(M, F, NB, BN, 1, st);
     const bool use[2] = {M.order3 > 0, M.order4 > 0};
     for (int k = 0; k < 2; ++k) {
         if (!use[k]) continue;
@@ -540,6 +569,7 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
         CK(cudaMemcpyAsync(C.first, h_first.p, nf, cudaMemcpyHostToDevice, st));
         DeviceFrames df;
         df.nframes = nf;
+        df.box_host.assign(h_box.p, h_box.p + nf);
         df.natoms_total = active_atoms;
         df.nghosts = active_atoms * nimg;
         df.xyz = C.xyz;

@@ -371,6 +371,7 @@ std::unique_ptr<DeviceFrames> Session::upload(const FrameBatch& fb) {
     df->nghosts = fb.nghosts;
     df->atom_ofs_host = fb.atom_ofs;
     df->row_ofs_host = fb.row_ofs;
+    df->box_host = fb.box;
     df->natoms_host = fb.natoms;
     cgd::FramesDev& d = df->dev;
     const int L = model_.ctl.nlayers;

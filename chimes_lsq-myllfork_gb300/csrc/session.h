@@ -58,6 +58,7 @@ struct DeviceFrames {
     std::vector<int> natoms_host;
     std::vector<void*> allocs;
     double* xyz = nullptr;          // the positions dev.xyz points to (the MD updates them)
+    std::vector<cgd::BoxDev> box_host;   // host copy of the boxes (binned neighbour search)
     ~DeviceFrames();
 };
 
