@@ -311,9 +311,10 @@ __device__ __forceinline__ bool within(const FramesDev& F, const BoxDev& B, int6
 }
 
 template <int NB_>
-__global__ void k_clusters(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int fill) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void k_clusters(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int fill, int parts) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
+    const int warp = gw / parts, part = gw - warp * parts;
     if (warp >= NB.n_real) return;
     int lo = 0, hi = F.nframes - 1;
     while (lo < hi) {
@@ -336,9 +337,13 @@ __global__ void k_clusters(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, 
     const bool ordered = !B.small;
     const int ti = typ[i];
     int64_t out = fill ? CS.ofs[warp] : 0;
+    if (fill)
+        for (int q = 0; q < part; ++q) out += CS.pcnt[(int64_t)warp * parts + q];
     int count = 0;
     const int64_t total = NB_ == 3 ? (int64_t)n * n : (int64_t)n * n * n;
-    for (int64_t base = 0; base < total; base += 32) {
+    const int64_t nbat = (total + 31) / 32;
+    const int64_t b0 = nbat * part / parts * 32, b1 = min(total, nbat * (part + 1) / parts * 32);
+    for (int64_t base = b0; base < b1; base += 32) {
         const int64_t t = base + lane;
         bool ok = false;
         int j = -1, k = -1, l = -1, T = -1;
@@ -382,18 +387,26 @@ __global__ void k_clusters(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, 
         }
         count += __popc(bal);
     }
-    if (!fill && lane == 0) CS.cnt[warp] = count;
+    if (!fill && lane == 0) {
+        if (parts == 1) {
+            CS.cnt[warp] = count;
+        } else {
+            CS.pcnt[(int64_t)warp * parts + part] = count;
+            atomicAdd(CS.cnt + warp, count);
+        }
+    }
 }
 
 // Quadruplets in two stages (same accepted set as k_clusters<4>, different but fixed
 // order): the lanes first test (j, k) pairs -- distinct, parent-ordered, r_jk under
 // the largest 4-body cut-off -- and the surviving pairs of each chunk of 32 are then
 // crossed with every l, flattened over the lanes, with the full per-slot tests.
-__global__ void k_quads(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int fill) {
+__global__ void k_quads(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int fill, int parts) {
     __shared__ int2 sPair[8][32];
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int wib = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
+    const int warp = gw / parts, part = gw - warp * parts;
     if (warp >= NB.n_real) return;
     int lo = 0, hi = F.nframes - 1;
     while (lo < hi) {
@@ -414,10 +427,14 @@ __global__ void k_quads(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int
     const int ti = typ[i];
     const float cut = (float)(M.maxcut4 + NB.skin) + MARGIN;
     int64_t out = fill ? CS.ofs[warp] : 0;
+    if (fill)
+        for (int q = 0; q < part; ++q) out += CS.pcnt[(int64_t)warp * parts + q];
     int count = 0;
     const int npairs = n * n;
     const unsigned lt = (1u << lane) - 1u;
-    for (int pb = 0; pb < npairs; pb += 32) {
+    const int nbat = (npairs + 31) / 32;
+    const int pb0 = nbat * part / parts * 32, pb1 = min(npairs, nbat * (part + 1) / parts * 32);
+    for (int pb = pb0; pb < pb1; pb += 32) {
         const int p = pb + lane;
         bool pv = false;
         int a = 0, b = 0;
@@ -465,7 +482,14 @@ __global__ void k_quads(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int
         }
         __syncwarp();
     }
-    if (!fill && lane == 0) CS.cnt[warp] = count;
+    if (!fill && lane == 0) {
+        if (parts == 1) {
+            CS.cnt[warp] = count;
+        } else {
+            CS.pcnt[(int64_t)warp * parts + part] = count;
+            atomicAdd(CS.cnt + warp, count);
+        }
+    }
 }
 
 // ---------------------------------------------------------------- bucketing
@@ -578,12 +602,18 @@ void launch_neigh_binned(const ModelDev& M, const FramesDev& F, const NeighDev& 
     if (NB.n_real > 0) k_neigh_binned<<<(unsigned)((NB.n_real + 7) / 8), 256, 0, st>>>(M, F, NB, B, fill);
 }
 
+int cluster_parts(int n_real) {
+    return n_real >= 32768 ? 1 : n_real >= 16384 ? 2 : n_real >= 8192 ? 4 : 8;
+}
+
 void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const NeighDev& NB, const ClusterSet& CS,
                      int fill, cudaStream_t st) {
     if (NB.n_real <= 0) return;
-    const unsigned g = (unsigned)((NB.n_real + 7) / 8);
-    if (nbody == 3) k_clusters<3><<<g, 256, 0, st>>>(M, F, NB, CS, fill);
-    else k_quads<<<g, 256, 0, st>>>(M, F, NB, CS, fill);
+    const int parts = CS.pcnt ? cluster_parts(NB.n_real) : 1;
+    if (parts > 1 && !fill) cudaMemsetAsync(CS.cnt, 0, sizeof(int) * NB.n_real, st);
+    const unsigned g = (unsigned)(((int64_t)NB.n_real * parts + 7) / 8);
+    if (nbody == 3) k_clusters<3><<<g, 256, 0, st>>>(M, F, NB, CS, fill, parts);
+    else k_quads<<<g, 256, 0, st>>>(M, F, NB, CS, fill, parts);
 }
 void launch_bucket(int nframes, const FramesDev& F, const BucketSpec& S, const Buckets& out, cudaStream_t st) {
     if (nframes > 0) k_bucket<<<nframes, BUCKET_THREADS, 0, st>>>(F, S, out);

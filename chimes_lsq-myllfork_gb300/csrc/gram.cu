@@ -35,51 +35,156 @@ constexpr long long GB_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
 
 // ---------------------------------------------------------------- split + transpose
 // planes[p][c][k] (bf16, k contiguous) for rows [r0, r0+nr) of A (row-major, lda),
-// zero padded to (cpad, kpad).
-template <typename T>
-__global__ void k_split_transpose(const T* __restrict__ A, int64_t lda, int64_t r0, int64_t nr, int ncols,
-                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t kpad) {
-    __shared__ float tile[32][33];
-    const int64_t k0 = (int64_t)blockIdx.x * 32;   // rows of A -> K
-    const int c0 = blockIdx.y * 32;                // columns of A -> plane rows
-    for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
-        const int64_t k = k0 + dy;
-        const int c = c0 + threadIdx.x;
-        float v = 0.f;
-        if (k < nr && c < ncols) v = (float)A[(r0 + k) * lda + c];
-        tile[dy][threadIdx.x] = v;
+// zero padded to (cpad, kpad), fused with h = A^T b so that A is read once.  A block owns a strip of
+// 32 columns and the 64-row K tiles kt = blockIdx.x, blockIdx.x + gridDim.x, ...;
+// each thread keeps one column's running sum over the rows it loads.  FP64 input
+// sums in FP64.  FP32 input sums in float-float: each product a*b (b split into
+// two floats) is formed exactly by an FMA, added by an error-free two-sum, and the
+// pair renormalised after every tile, so the sum carries about 44 significant bits
+// while the FP64 pipe (a small fraction of the FP32 rate on this GPU) stays idle.
+// partial[blockIdx.x][c] = the block's sum, combined in order by k_atb_reduce.
+constexpr int SPA_K = 64, SPA_C = 32, SPA_THREADS = 256;
+struct FloatFloat {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add_prod(float a, float bh, float bl) {
+        const float p = __fmul_rn(a, bh);
+        float e = __fmaf_rn(a, bh, -p);      // a*bh - p exactly
+        e = __fmaf_rn(a, bl, e);
+        const float s = __fadd_rn(hi, p);    // two-sum(hi, p)
+        const float bb = __fsub_rn(s, hi);
+        const float t = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+        hi = s;
+        lo = __fadd_rn(lo, __fadd_rn(t, e));
     }
+    __device__ __forceinline__ void renorm() {   // two-sum(hi, lo)
+        const float s = __fadd_rn(hi, lo);
+        const float bb = __fsub_rn(s, hi);
+        lo = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(lo, bb));
+        hi = s;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// b of the rows [r0, r0+nr) as two floats (bh + bl carries 48 bits), zero up to kpad
+__global__ void k_split_b(const double* __restrict__ b, int64_t r0, int64_t nr, int64_t kpad, float2* __restrict__ bs) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kpad) return;
+    const double v = k < nr ? b[r0 + k] : 0.0;
+    const float bh = __double2float_rn(v);
+    bs[k] = make_float2(bh, __double2float_rn(v - (double)bh));
+}
+
+// FP64 input reads b (rows r0..); FP32 input reads bsplit (k_split_b of the block).
+template <typename T>
+__global__ void __launch_bounds__(SPA_THREADS, 5) k_split_atb(const T* __restrict__ A, int64_t lda, int64_t r0,
+                                                          int64_t nr, int ncols, const double* __restrict__ b,
+                                                          const float2* __restrict__ bsplit,
+                                                          __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                                                          int64_t kpad, double* __restrict__ partial) {
+    __shared__ float tile[SPA_K][SPA_C + 1];
+    __shared__ double bd[SPA_K];
+    __shared__ float2 bs[SPA_K];
+    __shared__ double red[SPA_THREADS / 32][SPA_C];
+    const int tx = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int c0 = blockIdx.y * SPA_C;
+    const int c = c0 + tx;
+    const int64_t ntk = kpad / SPA_K;
+    double accd = 0.0;
+    FloatFloat accf;
+    for (int64_t kt = blockIdx.x; kt < ntk; kt += gridDim.x) {
+        const int64_t k0 = kt * SPA_K;
+        T v[SPA_K / 8];
+#pragma unroll
+        for (int i = 0; i < SPA_K / 8; ++i) {
+            const int64_t k = k0 + w + 8 * i;
+            v[i] = (k < nr && c < ncols) ? A[(r0 + k) * lda + c] : T(0);
+        }
+        if (threadIdx.x < SPA_K) {
+            const int64_t k = k0 + threadIdx.x;
+            if constexpr (sizeof(T) == 8) bd[threadIdx.x] = k < nr ? b[r0 + k] : 0.0;
+            else bs[threadIdx.x] = bsplit[k];
+        }
+#pragma unroll
+        for (int i = 0; i < SPA_K / 8; ++i) tile[w + 8 * i][tx] = (float)v[i];
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < SPA_K / 8; ++i) {
+            if constexpr (sizeof(T) == 8) {
+                accd = fma((double)v[i], bd[w + 8 * i], accd);
+            } else {
+                const float2 bb = bs[w + 8 * i];
+                accf.add_prod((float)v[i], bb.x, bb.y);
+            }
+        }
+        if constexpr (sizeof(T) != 8) accf.renorm();
+        // planes: column c0+cl gets 64 contiguous K values; a warp stores 32 bf16 pairs
+#pragma unroll
+        for (int j = 0; j < SPA_C / 8; ++j) {
+            const int cl = w + 8 * j;
+            const float f0 = tile[2 * tx][cl], f1 = tile[2 * tx + 1][cl];
+            const __nv_bfloat162 hp = __floats2bfloat162_rn(f0, f1);
+            const float2 hf = __bfloat1622float2(hp);
+            const __nv_bfloat162 lp = __floats2bfloat162_rn(f0 - hf.x, f1 - hf.y);
+            const int64_t o = (int64_t)(c0 + cl) * kpad + k0 + 2 * tx;
+            *reinterpret_cast<__nv_bfloat162*>(hi + o) = hp;
+            *reinterpret_cast<__nv_bfloat162*>(lo + o) = lp;
+        }
+        __syncthreads();
+    }
+    if constexpr (sizeof(T) == 8) red[w][tx] = accd;
+    else red[w][tx] = accf.value();
     __syncthreads();
-    for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
-        const int c = c0 + dy;
-        const int64_t k = k0 + threadIdx.x;
-        const float v = tile[threadIdx.x][dy];
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-        hi[(int64_t)c * kpad + k] = h;
-        lo[(int64_t)c * kpad + k] = l;
+    if (w == 0 && c < ncols) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < SPA_THREADS / 32; ++q) s += red[q][tx];
+        partial[(int64_t)blockIdx.x * ncols + c] = s;
     }
 }
 
-// h[c] += sum_r A[r][c] b[r] in FP64: partial[y][c] over row slices y (coalesced
-// along c), then an ordered sum over y, so the result is reproducible.
-constexpr int ATB_SLICES = 256;
-template <typename T>
-__global__ void k_atb_partial(const T* __restrict__ A, int64_t lda, int64_t nr, int ncols,
-                              const double* __restrict__ b, double* __restrict__ partial) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncols) return;
+// h[c] += sum_r A[r][c] b[r] in FP64: partial[y][c] over row slices y, then an
+// ordered sum over y, so the result is reproducible.  A block walks its slice's
+// rows with its threads across the columns (whole rows read contiguously), four
+// columns per thread and four rows per step.
+constexpr int ATB_SLICES = 1024;
+constexpr int ATB_THREADS = 256;
+__global__ void __launch_bounds__(ATB_THREADS) k_atb_partial(const double* __restrict__ A, int64_t lda, int64_t nr,
+                                                             int ncols, const double* __restrict__ b,
+                                                             double* __restrict__ partial) {
     const int64_t per = (nr + gridDim.y - 1) / gridDim.y;
     const int64_t r0 = (int64_t)blockIdx.y * per, r1 = min(nr, r0 + per);
-    // eight independent chains keep eight row loads in flight per thread
-    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int64_t r = r0;
-    for (; r + 8 <= r1; r += 8) {
+    for (int c0 = 0; c0 < ncols; c0 += 4 * ATB_THREADS) {
+        double s[4] = {0, 0, 0, 0};
+        int cc[4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) s[u] = fma((double)A[(r + u) * lda + c], b[r + u], s[u]);
+        for (int u = 0; u < 4; ++u) cc[u] = c0 + u * ATB_THREADS + threadIdx.x;
+        int64_t r = r0;
+        for (; r + 4 <= r1; r += 4) {   // 16 loads in flight per thread
+            double v[4][4];
+            double br[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                br[q] = b[r + q];
+                const double* row = A + (r + q) * lda;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[q][u] = cc[u] < ncols ? row[cc[u]] : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) s[u] = fma(v[q][u], br[q], s[u]);
+        }
+        for (; r < r1; ++r) {
+            const double br = b[r];
+            const double* row = A + r * lda;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (cc[u] < ncols) s[u] = fma(row[cc[u]], br, s[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (cc[u] < ncols) partial[(int64_t)blockIdx.y * ncols + cc[u]] = s[u];
     }
-    for (int u = 0; r < r1; ++r, ++u) s[u] = fma((double)A[r * lda + c], b[r], s[u]);
-    partial[(int64_t)blockIdx.y * ncols + c] = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
 }
 __global__ void k_atb_reduce(const double* __restrict__ partial, int nslices, int ncols, double* __restrict__ h) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -306,6 +411,23 @@ static CUtensorMap plane_map(void* base, int64_t kpad, int64_t cpad) {
     return m;
 }
 
+// Blocks of k_split_atb<T> resident on the current device at once (cached per device).
+template <typename T>
+static int split_atb_resident() {
+    static thread_local int dev_cached = -1, cached = 0;
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev != dev_cached) {
+        int per_sm = 0, sms = 0;
+        ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cgd::k_split_atb<T>, cgd::SPA_THREADS, 0),
+           "occupancy");
+        ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        cached = std::max(1, per_sm) * std::max(1, sms);
+        dev_cached = dev;
+    }
+    return cached;
+}
+
 size_t gram_plane_bytes(int64_t nrows_block, int ncols) {
     const int64_t kpad = (nrows_block + cgd::GB_K - 1) / cgd::GB_K * cgd::GB_K;
     const int64_t cpad = (ncols + cgd::GB_M - 1) / cgd::GB_M * cgd::GB_M;
@@ -318,22 +440,18 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
     if (nrows <= 0) return;
     // stage ids (session.h): ST_GRAM_ATB 11, ST_GRAM_SPLIT 12, ST_GRAM_TC 13, ST_GRAM_SYRK 14
     enum { S_ATB = 11, S_SPLIT = 12, S_TC = 13, S_SYRK = 14 };
-    // h += A^T b (FP64), reproducible
-    {
+    if (mode == 0) {   // h += A^T b (FP64), reproducible
+        if (prec_in != 0) throw std::runtime_error("the FP64 Gram needs an FP64 A");
         const int ns = (int)std::min<int64_t>(nrows, cgd::ATB_SLICES);
         double* partial = nullptr;
         ck(cudaMallocAsync((void**)&partial, sizeof(double) * ns * ncols, st), "atb scratch");
         mark(S_ATB, true);
-        dim3 grid((ncols + 127) / 128, ns);
-        if (prec_in == 0) cgd::k_atb_partial<double><<<grid, 128, 0, st>>>((const double*)A, lda, nrows, ncols, b, partial);
-        else cgd::k_atb_partial<float><<<grid, 128, 0, st>>>((const float*)A, lda, nrows, ncols, b, partial);
+        cgd::k_atb_partial<<<dim3(1, ns), cgd::ATB_THREADS, 0, st>>>((const double*)A, lda, nrows, ncols, b, partial);
         cgd::k_atb_reduce<<<(ncols + 127) / 128, 128, 0, st>>>(partial, ns, ncols, h);
         mark(S_ATB, false);
         ck(cudaGetLastError(), "k_atb");
         ck(cudaFreeAsync(partial, st), "atb scratch free");
-    }
-    if (mode == 0) {   // FP64 library SYRK (upper triangle of the row-major G)
-        if (prec_in != 0) throw std::runtime_error("the FP64 Gram needs an FP64 A");
+        // FP64 library SYRK (upper triangle of the row-major G)
         cublasHandle_t hnd = (cublasHandle_t)cublas;
         cublasSetStream(hnd, st);
         const double one = 1.0;
@@ -353,19 +471,39 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
     const int npairs = ntile * (ntile + 1) / 2;
     const size_t smem = (size_t)cgd::GB_STAGES * cgd::GB_STAGE_BYTES + 1024 + 256;
     ck(cudaFuncSetAttribute(cgd::k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr");
+    // split + A^T b: one wave of resident blocks over the column strips (a second,
+    // partial wave would double the pass)
+    const int nstrip = (int)(cpad / cgd::SPA_C);
+    const int64_t ktiles_max = (std::min(rblock, nrows) + cgd::SPA_K - 1) / cgd::SPA_K;
+    const int resident = prec_in == 0 ? split_atb_resident<double>() : split_atb_resident<float>();
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(ktiles_max, resident / nstrip));
+    double* partial = nullptr;
+    float2* bsplit = nullptr;
+    ck(cudaMallocAsync((void**)&partial, sizeof(double) * gx * ncols, st), "atb scratch");
+    const int64_t kpad_max = (std::min(rblock, nrows) + cgd::GB_K - 1) / cgd::GB_K * cgd::GB_K;
+    if (prec_in != 0) ck(cudaMallocAsync((void**)&bsplit, sizeof(float2) * kpad_max, st), "b split scratch");
     for (int64_t r0 = 0; r0 < nrows; r0 += rblock) {
         const int64_t nr = std::min(rblock, nrows - r0);
         const int64_t kpad = (nr + cgd::GB_K - 1) / cgd::GB_K * cgd::GB_K;
         __nv_bfloat16* hi = (__nv_bfloat16*)planes;
         __nv_bfloat16* lo = hi + cpad * kpad;
-        dim3 tg((unsigned)(kpad / 32), (unsigned)(cpad / 32));
+        const int gxb = (int)std::min<int64_t>(gx, kpad / cgd::SPA_K);
+        dim3 tg((unsigned)gxb, (unsigned)nstrip);
         mark(S_SPLIT, true);
-        if (prec_in == 0)
-            cgd::k_split_transpose<double><<<tg, dim3(32, 8), 0, st>>>((const double*)A, lda, r0, nr, ncols, hi, lo, kpad);
-        else
-            cgd::k_split_transpose<float><<<tg, dim3(32, 8), 0, st>>>((const float*)A, lda, r0, nr, ncols, hi, lo, kpad);
+        if (prec_in == 0) {
+            cgd::k_split_atb<double><<<tg, cgd::SPA_THREADS, 0, st>>>((const double*)A, lda, r0, nr, ncols, b, nullptr,
+                                                                     hi, lo, kpad, partial);
+        } else {
+            cgd::k_split_b<<<(unsigned)((kpad + 255) / 256), 256, 0, st>>>(b, r0, nr, kpad, bsplit);
+            cgd::k_split_atb<float><<<tg, cgd::SPA_THREADS, 0, st>>>((const float*)A, lda, r0, nr, ncols, nullptr,
+                                                                    bsplit, hi, lo, kpad, partial);
+        }
         mark(S_SPLIT, false);
-        ck(cudaGetLastError(), "k_split_transpose");
+        ck(cudaGetLastError(), "k_split_atb");
+        mark(S_ATB, true);
+        cgd::k_atb_reduce<<<(ncols + 127) / 128, 128, 0, st>>>(partial, gxb, ncols, h);
+        mark(S_ATB, false);
+        ck(cudaGetLastError(), "k_atb_reduce");
         CUtensorMap mhi = plane_map(hi, kpad, cpad), mlo = plane_map(lo, kpad, cpad);
         // K slices: about ctas_per_sm CTAs per SM in total (152 SMs)
         const int64_t ksteps = kpad / cgd::GB_K;
@@ -379,6 +517,8 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         mark(S_TC, false);
         ck(cudaGetLastError(), "k_gram_tc");
     }
+    ck(cudaFreeAsync(partial, st), "atb scratch free");
+    if (bsplit) ck(cudaFreeAsync(bsplit, st), "b split scratch free");
 }
 
 void gram_symmetrize(double* G, int n, bool from_upper, cudaStream_t st) {

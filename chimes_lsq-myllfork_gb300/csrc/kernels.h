@@ -27,7 +27,13 @@ struct ClusterSet {                               // triplets or quadruplets of 
     int64_t* ofs;                                 // [n_real + 1]
     int4* m;                                      // members (frame-local ghost indices), .w = -1 for 3B
     int* type;                                    // cluster type index
+    int* pcnt = nullptr;                          // [n_real * cluster_parts(n_real)] when that is > 1
 };
+
+// Warps that share one centre atom's enumeration (1, 2, 4 or 8): small batches
+// split each atom's candidate range so the GPU has enough warps; the clusters
+// keep the order of a single warp's walk.
+int cluster_parts(int n_real);
 
 // Stable per-frame bucketing (owner incidences and per-type lists).
 struct Buckets {

@@ -635,6 +635,112 @@ __device__ __forceinline__ bool within_md(const FramesDev& F, const BoxDev& B, i
     return dist_exact(B.h, F.scaled + 3 * (gb + a), F.scaled + 3 * (gb + b), rab) < smax;
 }
 
+// The FP32 form of k_md2: geometry from the FP32 Cartesian copy, basis, cut-off,
+// penalty and products in FP32; which pairs count (r < s_max) is decided as in
+// the FP64 form (FP32 with a margin, exact FP64 near s_max); FP64 accumulation.
+__global__ void __launch_bounds__(256) k_md2f(ModelDev M, MdDev D, FramesDev F, NeighDev NB, double* Fo, double* So) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= NB.n_real) return;
+    const int f = frame_of_atom(F, warp);
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    const BoxDev& B = F.box[f];
+    const int64_t o = NB.ofs2[warp];
+    const int n = NB.cnt2[warp];
+    const int ord = M.order2;
+    const float4* c32 = reinterpret_cast<const float4*>(F.cart32);
+    const int64_t gb = F.ghost_ofs[f];
+    const float4 xi = c32[gb + (warp - aofs)];
+    float fi[3] = {0.f, 0.f, 0.f}, v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int t = lane; t < n; t += 32) {
+        const int64_t q = o + t;
+        const int g = NB.g2[q], pt = NB.pt2[q];
+        const PairDev& P = M.pairs[pt];
+        float r, R[3];
+        if (NB.md == 2) {   // lists reused over steps: this step's geometry
+            const float4 xg = c32[gb + g];
+            R[0] = xg.x - xi.x; R[1] = xg.y - xi.y; R[2] = xg.z - xi.z;
+            r = sqrtf(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+            if (!within_md(F, B, gb, (int)(warp - aofs), g, P.smax)) continue;
+        } else {
+            r = (float)NB.r2[q];
+            R[0] = (float)NB.rab2[3 * q]; R[1] = (float)NB.rab2[3 * q + 1]; R[2] = (float)NB.rab2[3 * q + 2];
+        }
+        float fc, fd;
+        fcut_r<float>(M, r, (float)P.smax, fc, fd);
+        // Chebyshev basis with a run-time order (as basis_regs_f)
+        const float smin = (float)P.smin, lam = (float)P.lambda;
+        const bool out = r < smin;
+        const float rr = out ? smin : r;
+        const float ixd = 1.0f / (float)P.xdiff;
+        float x, ex = 0.0f, dxdr;
+        if (M.trans == 0) { ex = expf(-rr / lam); x = (ex - (float)P.xavg) * ixd; dxdr = -ex / lam * ixd; }
+        else if (M.trans == 1) { x = (1.0f / rr - (float)P.xavg) * ixd; dxdr = -ixd / (rr * rr); }
+        else { x = (rr - (float)P.xavg) * ixd; dxdr = ixd; }
+        dxdr *= (float)M.deriv_const;
+        const bool zero_d = out && M.fix == 1;
+        float damp = 1.0f, shift = 0.0f;
+        if (out && M.fix == 0) { damp = expf((r - smin) / (float)M.smooth); shift = (float)M.smooth * (damp - 1.0f); }
+        const float lin = (out && M.fix == 2) ? (r - smin) : 0.0f;
+        const double* c = D.c2 + (size_t)pt * ord;
+        float t_prev = 1.0f, t_cur = x, u_prev2 = 0.0f, u_prev = 1.0f, e = 0.0f, gsum = 0.0f;
+        for (int k = 1; k <= ord; ++k) {   // 2-body columns use T_1 .. T_order
+            float tn, un_1;
+            if (k == 1) { tn = x; un_1 = 1.0f; }
+            else {
+                tn = 2.0f * x * t_cur - t_prev;
+                t_prev = t_cur; t_cur = tn;
+                const float un = (k - 1 == 1) ? 2.0f * x : 2.0f * x * u_prev - u_prev2;
+                u_prev2 = u_prev; u_prev = un;
+                un_1 = un;
+            }
+            float td = zero_d ? 0.0f : k * dxdr * un_1;
+            if (out) {
+                if (M.fix == 0) { tn += shift * td; td *= damp; }
+                else if (M.fix == 2) tn += td * lin;
+            }
+            const float ck = (float)c[k - 1];
+            e = fmaf(ck, fc * tn, e);
+            gsum = fmaf(ck, fc * td + fd * tn, gsum);
+        }
+        const float perm = (float)B.perm2;
+        float es = perm * e, gs = perm * gsum;
+        if (r - (float)D.pen_dist < smin) {   // cubic penalty below s_min + d (src/Cheby.C:1900-1968)
+            const float rp = smin + (float)D.pen_dist - r;
+            if (rp > 0.0f) {
+                gs += -3.0f * rp * rp * (float)D.pen_scale;
+                es += rp * rp * rp * (float)D.pen_scale;
+            }
+        }
+        const float wv = gs / r;
+        double* fo = Fo + 3 * (aofs + g % N);
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) {
+            fi[cc] = fmaf(wv, R[cc], fi[cc]);
+            atomicAdd(fo + cc, (double)(-wv * R[cc]));
+        }
+        v[0] += es;
+        v[1] -= gs * r;
+        v[2] -= wv * R[0] * R[0]; v[3] -= wv * R[0] * R[1]; v[4] -= wv * R[0] * R[2];
+        v[5] -= wv * R[1] * R[1]; v[6] -= wv * R[1] * R[2]; v[7] -= wv * R[2] * R[2];
+    }
+    double fd3[3], vd[8];
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) fd3[cc] = warp_sum((double)fi[cc]);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) vd[k] = warp_sum((double)v[k]);
+    if (lane == 0 && n > 0) {
+        double* fo = Fo + 3 * warp;
+        for (int cc = 0; cc < 3; ++cc) atomicAdd(fo + cc, fd3[cc]);
+        double* so = So + (size_t)f * MD_NSCALAR;
+        atomicAdd(so + 0, vd[0]); atomicAdd(so + 1, vd[1]);
+        atomicAdd(so + 2, vd[2]); atomicAdd(so + 3, vd[3]); atomicAdd(so + 4, vd[4]);
+        atomicAdd(so + 5, vd[3]); atomicAdd(so + 6, vd[5]); atomicAdd(so + 7, vd[6]);
+        atomicAdd(so + 8, vd[4]); atomicAdd(so + 9, vd[6]); atomicAdd(so + 10, vd[7]);
+    }
+}
+
 template <int NBODY>
 __global__ void k_md_filter(ModelDev M, FramesDev F, ClusterSet CS, const int64_t* cfo, int64_t n, int* type_out) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
@@ -744,11 +850,12 @@ bool md_fast_order(int nbody, int order) {
 }
 
 void launch_md2(const ModelDev& M, const MdDev& D, const FramesDev& F, const NeighDev& NB, double* Fo, double* So,
-                cudaStream_t st) {
+                cudaStream_t st, int prec) {
     if (NB.n_real == 0 || M.order2 == 0) return;
     const int threads = 256;
     const int64_t blocks = ((int64_t)NB.n_real * 32 + threads - 1) / threads;
-    k_md2<<<(unsigned)blocks, threads, 0, st>>>(M, D, F, NB, Fo, So);
+    if (prec == 1) k_md2f<<<(unsigned)blocks, threads, 0, st>>>(M, D, F, NB, Fo, So);
+    else k_md2<<<(unsigned)blocks, threads, 0, st>>>(M, D, F, NB, Fo, So);
 }
 
 void launch_md_bucket(int64_t n, int nframes, const int64_t* cfo, const int* type, const MdBuckets& B,

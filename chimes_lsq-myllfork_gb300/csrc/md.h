@@ -47,7 +47,7 @@ void launch_md_bucket(int64_t n, int nframes, const int64_t* cfo, const int* typ
 bool md_fast_order(int nbody, int order);
 
 void launch_md2(const ModelDev& M, const MdDev& D, const FramesDev& F, const NeighDev& NB, double* Fo, double* So,
-                cudaStream_t st);
+                cudaStream_t st, int prec = 0);
 // Clusters of one body count, one block per tile of a (frame, type) group; max_tiles
 // bounds the number of tiles (n / MDC_TILE + nkeys).
 void launch_mdc(int nbody, int prec, int order, int64_t max_tiles, const ModelDev& M, const MdDev& D,

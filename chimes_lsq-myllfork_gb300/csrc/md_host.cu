@@ -109,14 +109,16 @@ void Session::md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts*
     CK(cudaMemcpyAsync(&tot[0], NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&tot[1], NB.ofs3 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&tot[2], NB.ofs4 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    mark(ST_NEIGH, false);
     CK(cudaStreamSynchronize(st));
+    mark(ST_NEIGH, true);
     NB.i2 = S.get<int>(tot[0]); NB.g2 = S.get<int>(tot[0]); NB.pt2 = S.get<int>(tot[0]);
     NB.r2 = S.get<double>(tot[0]); NB.rab2 = S.get<double>(3 * tot[0]);
     NB.g3 = S.get<int>(tot[1]); NB.r3 = S.get<double>(tot[1]);
     NB.g4 = S.get<int>(tot[2]); NB.r4 = S.get<double>(tot[2]);
     cgd::launch_neigh(M, F, NB, 1, st); L();
     c.pairs2 = tot[0];
-    cgd::launch_md2(M, D, F, NB, Fo, So, st); L();
+    cgd::launch_md2(M, D, F, NB, Fo, So, st, md_->precision); L();
     CK(cudaGetLastError());
     // clusters: count both body counts, then one host read of the totals
     cgd::ClusterSet CS3{}, CS4{};
@@ -127,6 +129,7 @@ void Session::md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts*
         if (!use[k]) continue;
         css[k]->cnt = S.get<int>(nreal);
         css[k]->ofs = S.get<int64_t>(nreal + 1);
+        if (cgd::cluster_parts(nreal) > 1) css[k]->pcnt = S.get<int>((size_t)nreal * cgd::cluster_parts(nreal));
         cgd::launch_clusters(3 + k, M, F, NB, *css[k], 0, st); L();
         cgd::launch_scan_counts(css[k]->cnt, nreal, css[k]->ofs, st); L();
         CK(cudaMemcpyAsync(&ncl[k], css[k]->ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -180,10 +183,11 @@ MdLists::~MdLists() {
     for (void* p : allocs) if (p) cudaFree(p);
 }
 
-void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
+void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L, cudaStream_t st) {
     CK(cudaSetDevice(device_));
     const cgd::ModelDev& M = dm_->dev;
-    cudaStream_t st = stream_;
+    const bool timed = st == stream_;   // stage marks time the main stream only
+    auto mark = [&](int stage, bool begin) { if (timed) this->mark(stage, begin); };
     const int nf = df.nframes;
     const int nreal = (int)df.natoms_total;
     L.release();
@@ -194,10 +198,15 @@ void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
     L.shift = (int*)get(sizeof(int) * 3 * std::max(nreal, 1));
     L.xref = (double*)get(sizeof(double) * 3 * std::max(nreal, 1));
     L.dmax = (unsigned long long*)get(sizeof(unsigned long long));
+    L.scaled = (double*)get(sizeof(double) * 3 * std::max<int64_t>(df.nghosts, 1));
+    L.cart32 = (float*)get(sizeof(float) * 4 * std::max<int64_t>(df.nghosts, 1));
     CK(cudaMemcpyAsync(L.xref, df.xyz, sizeof(double) * 3 * nreal, cudaMemcpyDeviceToDevice, st));
     cgd::FramesDev F = df.dev;
     F.shift = L.shift;
     F.shift_mode = 1;   // wrap now and remember the shifts
+    F.scaled = L.scaled;
+    F.cart32 = L.cart32;
+    mark(ST_NEIGH, true);
     cgd::launch_frame_setup(F, df.nghosts, st);
     cgd::NeighDev& NB = L.NB;
     NB = cgd::NeighDev{};
@@ -245,23 +254,30 @@ void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
     CK(cudaMemcpyAsync(&tot[0], NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&tot[1], NB.ofs3 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&tot[2], NB.ofs4 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    mark(ST_NEIGH, false);
     CK(cudaStreamSynchronize(st));
+    mark(ST_NEIGH, true);
     NB.i2 = (int*)get(sizeof(int) * tot[0]); NB.g2 = (int*)get(sizeof(int) * tot[0]);
     NB.pt2 = (int*)get(sizeof(int) * tot[0]); NB.r2 = (double*)get(sizeof(double) * tot[0]);
     NB.rab2 = (double*)get(sizeof(double) * 3 * tot[0]);
     NB.g3 = (int*)get(sizeof(int) * tot[1]); NB.r3 = (double*)get(sizeof(double) * tot[1]);
     NB.g4 = (int*)get(sizeof(int) * tot[2]); NB.r4 = (double*)get(sizeof(double) * tot[2]);
     cgd::launch_neigh_binned(M, F, NB, BN, 1, st);
+    mark(ST_NEIGH, false);
+    mark(ST_CLUSTERS, true);
     const bool use[2] = {M.order3 > 0, M.order4 > 0};
     for (int k = 0; k < 2; ++k) {
         if (!use[k]) continue;
         L.CS[k].cnt = (int*)get(sizeof(int) * nreal);
         L.CS[k].ofs = (int64_t*)get(sizeof(int64_t) * (nreal + 1));
+        L.CS[k].pcnt = (int*)get(sizeof(int) * (size_t)nreal * cgd::cluster_parts(nreal));
         cgd::launch_clusters(3 + k, M, F, NB, L.CS[k], 0, st);
         cgd::launch_scan_counts(L.CS[k].cnt, nreal, L.CS[k].ofs, st);
         CK(cudaMemcpyAsync(&L.ncl[k], L.CS[k].ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     }
+    mark(ST_CLUSTERS, false);
     CK(cudaStreamSynchronize(st));
+    mark(ST_CLUSTERS, true);
     for (int k = 0; k < 2; ++k) {
         if (!use[k] || L.ncl[k] == 0) continue;
         const int64_t n = L.ncl[k];
@@ -280,6 +296,7 @@ void Session::md_lists_build(DeviceFrames& df, double skin, MdLists& L) {
         B.cursor = (int*)get(sizeof(int) * B.nkeys);
         B.val = (int*)get(sizeof(int) * n);
     }
+    mark(ST_CLUSTERS, false);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     L.valid = true;
@@ -300,25 +317,33 @@ void Session::md_force_lists(DeviceFrames& df, MdLists& L, double* Fo, double* S
     cgd::FramesDev F = df.dev;
     F.shift = L.shift;
     F.shift_mode = 2;   // the build's images
+    mark(ST_SETUP, true);
     cgd::launch_frame_setup(F, df.nghosts, st);
-    cgd::launch_md2(M, D, F, L.NB, Fo, So, st);
+    mark(ST_SETUP, false);
+    mark(ST_FORCE2, true);
+    cgd::launch_md2(M, D, F, L.NB, Fo, So, st, md_->precision);
+    mark(ST_FORCE2, false);
     for (int k = 0; k < 2; ++k) {
         const int64_t n = L.ncl[k];
         if (n == 0 || !L.tstep[k]) continue;
         cgd::ClusterSet CS = L.CS[k];
+        mark(ST_BUCKET, true);
         cgd::launch_md_filter(3 + k, M, F, CS, L.cfo[k], n, L.tstep[k], st);
         CS.type = L.tstep[k];
         cgd::launch_md_bucket(n, nf, L.cfo[k], L.tstep[k], L.B[k], st);
+        mark(ST_BUCKET, false);
         const int64_t max_tiles = (n + cgd::MDC_TILE - 1) / cgd::MDC_TILE + L.B[k].nkeys;
+        mark(k == 0 ? ST_FORCE3 : ST_FORCE4, true);
         cgd::launch_mdc(3 + k, md_->precision, k == 0 ? M.order3 : M.order4, max_tiles, M, D, F, CS, L.B[k], Fo, So,
                         st);
+        mark(k == 0 ? ST_FORCE3 : ST_FORCE4, false);
     }
     cgd::launch_md_finalize(nf, M, D, F, So, st);
     CK(cudaGetLastError());
 }
 
-bool Session::md_lists_stale(const DeviceFrames& df, MdLists& L) {
-    if (!L.valid || L.natoms != df.natoms_total) return true;
+double Session::md_lists_disp2(const DeviceFrames& df, MdLists& L) {
+    if (!L.valid || L.natoms != df.natoms_total) return HUGE_VAL;
     cudaStream_t st = stream_;
     CK(cudaMemsetAsync(L.dmax, 0, sizeof(unsigned long long), st));
     cgd::launch_md_maxdisp(df.xyz, L.xref, L.natoms, L.dmax, st);
@@ -327,7 +352,36 @@ bool Session::md_lists_stale(const DeviceFrames& df, MdLists& L) {
     CK(cudaStreamSynchronize(st));
     double d2;
     std::memcpy(&d2, &bits, sizeof(d2));
-    return d2 > 0.25 * L.skin * L.skin;
+    return d2;
+}
+
+void Session::md_force_step(DeviceFrames& df, MdListSet& LS, double* Fo, double* So) {
+    if (LS.next_ready) {   // built ahead during the previous step (that build has completed)
+        LS.cur ^= 1;
+        LS.next_ready = false;
+    }
+    MdLists& L = LS.current();
+    const double half2 = 0.25 * md_skin_ * md_skin_;
+    double d2 = md_lists_disp2(df, L);
+    if (!(d2 <= half2) || L.skin != md_skin_) {
+        md_lists_build(df, md_skin_, L, stream_);
+        d2 = 0.0;
+    }
+    const bool ahead = d2 > (0.75 * 0.75) * half2;   // 3/8 of the skin
+    if (ahead) {
+        if (!side_stream_) {
+            CK(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&side_event_, cudaEventDisableTiming));
+        }
+        CK(cudaEventRecord(side_event_, stream_));   // this step's positions
+        CK(cudaStreamWaitEvent(side_stream_, side_event_, 0));
+    }
+    md_force_lists(df, L, Fo, So);
+    if (ahead) {   // overlaps the force kernels just queued on the main stream
+        md_lists_build(df, md_skin_, LS.lists[LS.cur ^ 1], side_stream_);
+        LS.next_ready = true;
+        ++LS.early_builds;
+    }
 }
 
 void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int nsteps, double* v, double* Fo,
@@ -352,13 +406,12 @@ void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int n
     CK(cudaMemcpyAsync(dm, m.data(), nt * sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dim, im.data(), nt * sizeof(double), cudaMemcpyHostToDevice, st));
     const cgd::FramesDev& F = df.dev;
-    MdLists lists;
+    MdListSet lists;
     for (int step = 0; step <= nsteps; ++step) {
         if (step > 0) cgd::launch_md_drift(n, F, nullptr, df.xyz, v, acc, dt, st);   // UPDATE_COORDS + VELOCS_HALF_1
         double* sout = So_steps ? So_steps + (size_t)step * nf * cgd::MD_NSCALAR : so;
         if (md_skin_ > 0.0) {
-            if (md_lists_stale(df, lists)) md_lists_build(df, md_skin_, lists);
-            md_force_lists(df, lists, Fo, sout);
+            md_force_step(df, lists, Fo, sout);
         } else {
             md_force(df, Fo, sout, nullptr);
         }
@@ -493,13 +546,13 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
     std::vector<int> order(nreq);
     for (int r = 0; r < nreq; ++r) order[r] = r;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return req[a].arrival < req[b].arrival; });
-    const double per_atom_bytes = 8192.0, per_req_bytes = 65536.0;   // resident estimate per request
+    const double per_atom_bytes = 12288.0, per_req_bytes = 65536.0;   // resident estimate per request
     std::vector<int> active, steps_done(nreq, 0);
     std::vector<int64_t> pos(nreq, -1);      // atom offset of each active request in the current arena
     std::vector<char> first(nreq, 0);
     int cur = 0, next_pending = 0, finished = 0;
     int64_t active_atoms = 0, nbatch = 0;
-    MdLists lists;   // skin lists of the current composition
+    MdListSet lists;   // skin lists of the current composition
     double mem = 0.0;
     bool changed = false;
     const auto t0 = std::chrono::steady_clock::now();
@@ -582,8 +635,7 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
         const auto s0 = std::chrono::steady_clock::now();
         cgd::launch_md_drift(active_atoms, F, C.first, C.xyz, C.v, C.acc, opt.dt, st);
         if (md_skin_ > 0.0) {
-            if (md_lists_stale(df, lists)) md_lists_build(df, md_skin_, lists);
-            md_force_lists(df, lists, C.Fo, C.So);
+            md_force_step(df, lists, C.Fo, C.So);
         } else {
             md_force(df, C.Fo, C.So, nullptr);
         }

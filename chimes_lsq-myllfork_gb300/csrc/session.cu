@@ -359,6 +359,8 @@ Session::~Session() {
     if (cublas_) cublasDestroy((cublasHandle_t)cublas_);
     md_.reset();
     dm_.reset();
+    if (side_event_) cudaEventDestroy(side_event_);
+    if (side_stream_) cudaStreamDestroy(side_stream_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -497,6 +499,7 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
     auto clusters = [&](int nbody, cgd::ClusterSet& CS) -> int64_t {
         CS.cnt = S.get<int>(nreal);
         CS.ofs = S.get<int64_t>(nreal + 1);
+        if (cgd::cluster_parts(nreal) > 1) CS.pcnt = S.get<int>((size_t)nreal * cgd::cluster_parts(nreal));
         cgd::launch_clusters(nbody, M, F, NB, CS, 0, st); L();
         cgd::k_scan_counts<<<1, 1024, 0, st>>>(CS.cnt, nreal, CS.ofs); L();
         int64_t n = 0;

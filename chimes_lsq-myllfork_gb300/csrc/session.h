@@ -94,6 +94,8 @@ struct MdLists {
     cgd::MdBuckets B[2]{};
     double* xref = nullptr;               // positions at the build
     int* shift = nullptr;                 // wrap shifts at the build
+    double* scaled = nullptr;             // the build's own ghost coordinates, so that a
+    float* cart32 = nullptr;              // build can run beside a force evaluation
     unsigned long long* dmax = nullptr;
     int64_t natoms = 0;
     double skin = 0.0;
@@ -102,6 +104,19 @@ struct MdLists {
     void release() { valid = false; }     // the buffers stay for the next build
     void* buffer(int slot, size_t bytes);
     ~MdLists();
+};
+
+// The lists of a running MD batch and a second set built ahead of need: once an
+// atom has moved 3/8 of the skin (lists stay valid up to 1/2), the next lists are
+// built on a side stream while the current step's forces run on the main stream,
+// and the following step switches to them; a rebuild then costs no step time.
+struct MdListSet {
+    MdLists lists[2];
+    int cur = 0;
+    bool next_ready = false;
+    int64_t early_builds = 0;
+    MdLists& current() { return lists[cur]; }
+    void release() { lists[0].release(); lists[1].release(); next_ready = false; }
 };
 
 // One MD request of the serving loop (host arrays owned by the caller).
@@ -196,9 +211,11 @@ class Session {
     void md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts* counts);
     // Skin lists: build, force with the lists (no host synchronisation), and the
     // rebuild test (reads the largest displacement since the build).
-    void md_lists_build(DeviceFrames& df, double skin, MdLists& L);
+    void md_lists_build(DeviceFrames& df, double skin, MdLists& L, cudaStream_t st);
     void md_force_lists(DeviceFrames& df, MdLists& L, double* Fo, double* So);
-    bool md_lists_stale(const DeviceFrames& df, MdLists& L);
+    double md_lists_disp2(const DeviceFrames& df, MdLists& L);   // largest squared displacement
+    // One step's forces through a list set (rebuilds, look-ahead builds, switch).
+    void md_force_step(DeviceFrames& df, MdListSet& LS, double* Fo, double* So);
     double md_skin() const { return md_skin_; }
     void set_md_skin(double s) { md_skin_ = s >= 0.0 ? s : 0.0; }
     // nsteps velocity-Verlet steps (NVE) of every frame of the batch; df's positions
@@ -235,6 +252,8 @@ class Session {
     int open_stage_ = -1;
     int device_;
     cudaStream_t stream_ = nullptr;
+    cudaStream_t side_stream_ = nullptr;   // look-ahead MD list builds
+    cudaEvent_t side_event_ = nullptr;
     void* cublas_ = nullptr;
     std::unique_ptr<DeviceModel> dm_;
     std::unique_ptr<MdTables> md_;

@@ -3,6 +3,7 @@
     python chimes_lsq-myllfork_gb300/profile_cases.py gram [nframes]        # split-BF16 Gram of water-3b A
     python chimes_lsq-myllfork_gb300/profile_cases.py md NATOMS PRECISION   # MD force of one 4-body system
     python chimes_lsq-myllfork_gb300/profile_cases.py assemble [nframes]    # FP64 A of water-3b frames
+    python chimes_lsq-myllfork_gb300/profile_cases.py serve NATOMS PRECISION NSTEPS  # one NVE request, stage times
 
 Each case runs its launch twice after the set-up, so `ncu -k regex:<kernel> -c 1`
 captures a warm launch; the synthetic inputs are seeded.
@@ -47,6 +48,8 @@ def main(argv):
         return
     n = int(argv[1]) if len(argv) > 1 else 1024
     prec = int(argv[2]) if len(argv) > 2 else 0
+    if case == "serve":   # one request through the serving loop (list reuse, rebuilds)
+        return serve_case(cg, synth, np, torch, tmp, n, prec, int(argv[3]) if len(argv) > 3 else 100)
     fm = synth.make_workload("chno-4b", tmp, nframes=1, seed=5, sizes=[n], triclinic=False, density=0.1, labels=False)
     model = cg.Model(fm)
     nat, types, xyz, cell = synth.frames_arrays(os.path.join(tmp, "traj.xyzf"), 1, ["C", "H", "N", "O"])[:4]
@@ -61,6 +64,33 @@ def main(argv):
         sess.md_force_device(dfr, F.data_ptr(), S.data_ptr())
     torch.cuda.synchronize()
     print("ok", case, sess.md_last_counts())
+
+
+def serve_case(cg, synth, np, torch, tmp, n, prec, nsteps):
+    KB = 0.0019872067
+    masses = np.array([12.011, 1.008, 14.007, 15.999])
+    fm = synth.make_workload("chno-4b", tmp, nframes=1, seed=21, sizes=[n], triclinic=False, density=0.1, labels=False)
+    model = cg.Model(fm)
+    nat, types, xyz, cell = synth.frames_arrays(os.path.join(tmp, "traj.xyzf"), 1, ["C", "H", "N", "O"])[:4]
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(model.ncols) * 1e-3
+    v = rng.standard_normal((n, 3)) * np.sqrt(KB * 300.0 / masses[types])[:, None]
+    sess = cg.Session(model, 0)
+    sess.md_setup(x, precision=prec)
+    req = [dict(types=types, xyz=xyz, cell=cell[0], v=v, nsteps=nsteps, arrival=0.0)]
+    sess.md_serve(req, masses, dt_fs=0.2)   # warm (allocations, attributes)
+    sess.profile(True)
+    _, _, step_ms, _ = sess.md_serve(req, masses, dt_fs=0.2)
+    st = sess.stage_times()
+    sess.profile(False)
+    sm = step_ms.reshape(-1)
+    torch.cuda.synchronize()
+    print("ok serve", n, prec, "steps", nsteps, "p50 %.3f p90 %.3f p99 %.3f max %.3f ms" % (
+        np.percentile(sm, 50), np.percentile(sm, 90), np.percentile(sm, 99), sm.max()))
+    print("slowest steps (index, ms):", sorted(enumerate(np.round(sm, 3).tolist()), key=lambda t: -t[1])[:12])
+    for k, (ms, calls) in st.items():
+        if calls:
+            print(f"  {k:16s} {ms:9.3f} ms  {calls:5d} calls  {ms / calls * 1e3:8.1f} us/call")
 
 
 if __name__ == "__main__":

@@ -58,10 +58,16 @@ def test_gram_fp64_and_tensor_core(cg, system):
     Gtc, htc = _gram(cg, sess, dA, db, 1, torch)
     err = np.abs(Gtc.cpu().numpy() - Gref)
     assert np.all(err <= 1e-4 * scale + 1e-300), (err / (scale + 1e-300)).max()
-    assert np.array_equal(htc.cpu().numpy(), h64.cpu().numpy())
-    # FP32 A input gives the same tensor-core Gram (the split starts from FP32 values)
-    Gtc32, _ = _gram(cg, sess, dA, db, 1, torch, prec=1)
+    # h of the mixed form: FP64 sums in another order (fused into the split pass)
+    habs = np.abs(A).T @ np.abs(b)
+    assert np.all(np.abs(htc.cpu().numpy() - href) <= 1e-13 * habs)
+    # FP32 A input gives the same tensor-core Gram (the split starts from FP32 values);
+    # its h is the float-float sum of the FP32 A's products (about 44 bits), checked
+    # against the FP64 product of that same FP32 A
+    Gtc32, htc32 = _gram(cg, sess, dA, db, 1, torch, prec=1)
     assert np.all(np.abs(Gtc32.cpu().numpy() - Gref) <= 1e-4 * scale + 1e-300)
+    A32 = A.astype(np.float32).astype(np.float64)
+    assert np.all(np.abs(htc32.cpu().numpy() - A32.T @ b) <= 1e-11 * habs)
 
 
 def _solve(cg, sess, G, h, dA, db, ridge, iters, torch):
