@@ -36,14 +36,14 @@ constexpr long long GB_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
 // ---------------------------------------------------------------- split + transpose
 // planes[p][c][k] (bf16, k contiguous) for rows [r0, r0+nr) of A (row-major, lda),
 // zero padded to (cpad, kpad), fused with h = A^T b so that A is read once.  A block owns a strip of
-// 32 columns and the 64-row K tiles kt = blockIdx.x, blockIdx.x + gridDim.x, ...;
+// 32 columns and the 128-row K tiles kt = blockIdx.x, blockIdx.x + gridDim.x, ...;
 // each thread keeps one column's running sum over the rows it loads.  FP64 input
 // sums in FP64.  FP32 input sums in float-float: each product a*b (b split into
 // two floats) is formed exactly by an FMA, added by an error-free two-sum, and the
 // pair renormalised after every tile, so the sum carries about 44 significant bits
 // while the FP64 pipe (a small fraction of the FP32 rate on this GPU) stays idle.
 // partial[blockIdx.x][c] = the block's sum, combined in order by k_atb_reduce.
-constexpr int SPA_K = 64, SPA_C = 32, SPA_THREADS = 256;
+constexpr int SPA_K = 128, SPA_C = 32, SPA_THREADS = 256;
 struct FloatFloat {
     float hi = 0.f, lo = 0.f;
     __device__ __forceinline__ void add_prod(float a, float bh, float bl) {
@@ -76,7 +76,7 @@ __global__ void k_split_b(const double* __restrict__ b, int64_t r0, int64_t nr, 
 
 // FP64 input reads b (rows r0..); FP32 input reads bsplit (k_split_b of the block).
 template <typename T>
-__global__ void __launch_bounds__(SPA_THREADS, 5) k_split_atb(const T* __restrict__ A, int64_t lda, int64_t r0,
+__global__ void __launch_bounds__(SPA_THREADS, 4) k_split_atb(const T* __restrict__ A, int64_t lda, int64_t r0,
                                                           int64_t nr, int ncols, const double* __restrict__ b,
                                                           const float2* __restrict__ bsplit,
                                                           __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
@@ -88,21 +88,25 @@ __global__ void __launch_bounds__(SPA_THREADS, 5) k_split_atb(const T* __restric
     const int tx = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int c0 = blockIdx.y * SPA_C;
     const int c = c0 + tx;
-    const int64_t ntk = kpad / SPA_K;
+    const int64_t ntk = (kpad + SPA_K - 1) / SPA_K;   // kpad is a multiple of 64
     double accd = 0.0;
     FloatFloat accf;
     for (int64_t kt = blockIdx.x; kt < ntk; kt += gridDim.x) {
         const int64_t k0 = kt * SPA_K;
         T v[SPA_K / 8];
+        const T* p = A + (r0 + k0 + w) * lda + c;
+        if (k0 + SPA_K <= nr && c < ncols) {   // interior tile: no per-row checks
 #pragma unroll
-        for (int i = 0; i < SPA_K / 8; ++i) {
-            const int64_t k = k0 + w + 8 * i;
-            v[i] = (k < nr && c < ncols) ? A[(r0 + k) * lda + c] : T(0);
+            for (int i = 0; i < SPA_K / 8; ++i) v[i] = p[(int64_t)i * 8 * lda];
+        } else {
+#pragma unroll
+            for (int i = 0; i < SPA_K / 8; ++i)
+                v[i] = (k0 + w + 8 * i < nr && c < ncols) ? p[(int64_t)i * 8 * lda] : T(0);
         }
         if (threadIdx.x < SPA_K) {
             const int64_t k = k0 + threadIdx.x;
             if constexpr (sizeof(T) == 8) bd[threadIdx.x] = k < nr ? b[r0 + k] : 0.0;
-            else bs[threadIdx.x] = bsplit[k];
+            else bs[threadIdx.x] = k < kpad ? bsplit[k] : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int i = 0; i < SPA_K / 8; ++i) tile[w + 8 * i][tx] = (float)v[i];
@@ -117,17 +121,22 @@ __global__ void __launch_bounds__(SPA_THREADS, 5) k_split_atb(const T* __restric
             }
         }
         if constexpr (sizeof(T) != 8) accf.renorm();
-        // planes: column c0+cl gets 64 contiguous K values; a warp stores 32 bf16 pairs
+        // planes: column c0+cl gets SPA_K contiguous K values (up to kpad); a warp
+        // stores 32 bf16 pairs = 128 bytes per instruction
 #pragma unroll
         for (int j = 0; j < SPA_C / 8; ++j) {
             const int cl = w + 8 * j;
-            const float f0 = tile[2 * tx][cl], f1 = tile[2 * tx + 1][cl];
-            const __nv_bfloat162 hp = __floats2bfloat162_rn(f0, f1);
-            const float2 hf = __bfloat1622float2(hp);
-            const __nv_bfloat162 lp = __floats2bfloat162_rn(f0 - hf.x, f1 - hf.y);
-            const int64_t o = (int64_t)(c0 + cl) * kpad + k0 + 2 * tx;
-            *reinterpret_cast<__nv_bfloat162*>(hi + o) = hp;
-            *reinterpret_cast<__nv_bfloat162*>(lo + o) = lp;
+#pragma unroll
+            for (int hk = 0; hk < SPA_K; hk += 64) {
+                if (k0 + hk >= kpad) break;
+                const float f0 = tile[hk + 2 * tx][cl], f1 = tile[hk + 2 * tx + 1][cl];
+                const __nv_bfloat162 hp = __floats2bfloat162_rn(f0, f1);
+                const float2 hf = __bfloat1622float2(hp);
+                const __nv_bfloat162 lp = __floats2bfloat162_rn(f0 - hf.x, f1 - hf.y);
+                const int64_t o = (int64_t)(c0 + cl) * kpad + k0 + hk + 2 * tx;
+                *reinterpret_cast<__nv_bfloat162*>(hi + o) = hp;
+                *reinterpret_cast<__nv_bfloat162*>(lo + o) = lp;
+            }
         }
         __syncthreads();
     }
@@ -487,7 +496,7 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         const int64_t kpad = (nr + cgd::GB_K - 1) / cgd::GB_K * cgd::GB_K;
         __nv_bfloat16* hi = (__nv_bfloat16*)planes;
         __nv_bfloat16* lo = hi + cpad * kpad;
-        const int gxb = (int)std::min<int64_t>(gx, kpad / cgd::SPA_K);
+        const int gxb = (int)std::min<int64_t>(gx, (kpad + cgd::SPA_K - 1) / cgd::SPA_K);
         dim3 tg((unsigned)gxb, (unsigned)nstrip);
         mark(S_SPLIT, true);
         if (prec_in == 0) {
