@@ -61,6 +61,8 @@ def lib():
         "cg_model_load": (ctypes.c_int, [ctypes.c_char_p, pp]),
         "cg_model_free": (None, [vp]),
         "cg_model_columns": (ctypes.c_int, [vp, ip, ip, ip, ip, ip]),
+        "cg_model_charge_columns": (ctypes.c_int, [vp, ip, ip]),
+        "cg_model_constraint_rows": (ctypes.c_int, [vp, dp, ctypes.c_int64, dp]),
         "cg_model_sizes": (ctypes.c_int, [vp, ip, ip]),
         "cg_model_header_text": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "cg_model_map_text": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
@@ -163,6 +165,21 @@ class Model:
     @property
     def ncols(self):
         return self.columns()["ntotal"]
+
+    def charge_columns(self):
+        """(ncoul, nconstraints): FITCOUL charge columns and charge-constraint rows."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _check(lib().cg_model_charge_columns(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def constraint_rows(self):
+        """(A rows, b) of the charge constraints that follow the last frame of a fit."""
+        _, n = self.charge_columns()
+        A = np.zeros((n, self.ncols), dtype=np.float64)
+        b = np.zeros(n, dtype=np.float64)
+        if n:
+            _check(lib().cg_model_constraint_rows(self._h, _ptr(A), A.shape[1], _ptr(b)))
+        return A, b
 
     def sizes(self):
         nf, nt = ctypes.c_int(), ctypes.c_int()

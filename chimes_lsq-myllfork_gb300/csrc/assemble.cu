@@ -596,7 +596,7 @@ __global__ void k_energy_cols(ModelDev M, FramesDev F, void* A, int64_t lda, int
         int count = 0;
         for (int k = 0; k < N; ++k) count += typ[k] == t;
         for (int rr = 0; rr < F.energy_rows[f]; ++rr) {
-            const int64_t idx = (row + rr) * lda + M.tot_short + t;
+            const int64_t idx = (row + rr) * lda + M.tot_short + M.ncoul + t;
             if (is_double) reinterpret_cast<double*>(A)[idx] = (double)count;
             else reinterpret_cast<float*>(A)[idx] = (float)count;
         }

@@ -95,5 +95,10 @@ void launch_max_bucket(const int64_t* key_ofs, const int64_t* key_frame_ofs, int
                        cudaStream_t st);
 void launch_energy_cols(int prec, int nframes, const ModelDev& M, const FramesDev& F, void* A, int64_t lda,
                         cudaStream_t st);
+// FITCOUL charge columns of the force rows (ewald.cu): real space, structure
+// factors, k space; S holds ewald_scratch_bytes(nframes, natmtyp).
+size_t ewald_scratch_bytes(int nframes, int natmtyp);
+void launch_ewald(int prec, int nframes, int nreal, const ModelDev& M, const FramesDev& F, void* S, void* A,
+                  int64_t lda, cudaStream_t st);
 
 }  // namespace cgd

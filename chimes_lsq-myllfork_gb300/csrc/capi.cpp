@@ -76,8 +76,24 @@ int cg_model_columns(const cg_model* h, int* n2b, int* n3b, int* n4b, int* nener
         if (n2b) *n2b = h->m.tot_snum;
         if (n3b) *n3b = h->m.num3;
         if (n4b) *n4b = h->m.num4;
-        if (nener) *nener = h->m.tot_all - h->m.tot_short;
+        if (nener) *nener = h->m.tot_all - h->m.tot_short - h->m.ncoul;
         if (ntotal) *ntotal = h->m.tot_all;
+    });
+}
+
+int cg_model_charge_columns(const cg_model* h, int* ncoul, int* nconstraints) {
+    return guarded([&] {
+        need(h, "model");
+        if (ncoul) *ncoul = h->m.ncoul;
+        if (nconstraints) *nconstraints = (int)h->m.charge_constraints.size();
+    });
+}
+
+int cg_model_constraint_rows(const cg_model* h, double* A, int64_t lda, double* b) {
+    return guarded([&] {
+        need(h && (h->m.charge_constraints.empty() || (A && b)), "model/A/b");
+        need(lda >= h->m.tot_all, "lda");
+        cg::constraint_rows(h->m, A, lda, b);
     });
 }
 

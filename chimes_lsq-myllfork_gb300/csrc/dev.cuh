@@ -40,6 +40,7 @@ struct ModelDev {
     int n2b, tot_short, tot_all;         // column counts
     int col3, col4;                      // first 3B / 4B column
     int fit_ener_cols;                   // number of energy-offset columns (0 or natmtyp)
+    int ncoul;                           // FITCOUL charge columns (one per pair type), after tot_short
     const int* int_pair_map;             // natmtyp^2
     const PairDev* pairs;
     const int* int_map3;                 // 1000 entries
@@ -62,6 +63,8 @@ struct BoxDev {
     double lx, ly, lz, vol;
     int is_ortho, small;                 // small = unordered neighbour convention
     double perm2, perm3, perm4;          // PERM_SCALE[n]
+    double ew_alpha, ew_rc;              // Ewald splitting and real-space cut-off (FITCOUL)
+    int ew_kmax;                         // Ewald integer k cut-off
 };
 
 struct FramesDev {

@@ -516,6 +516,26 @@ static void parse_topology(const Listing& L, Model& m) {
                     (m.pairs[j].atm1 == pk.atm1 && m.pairs[i].atm1 == pk.atm2))
                     m.pair_map.emplace(m.pairs[i].atm1 + m.pairs[j].atm2, k);
             }
+    // CHARGE CONSTRAINTS  INPUT::PARSE_TOPOLOGY_CHGCONS src/input.C:1148-1200: npair-1 lines of
+    // npair pair names, npair values and the force (last token)
+    if (c.fit_coul) {
+        for (size_t i = 0; i < N; ++i) {
+            if (L.size(i) < 2 || L.at(i, 0) + " " + L.at(i, 1) != "CHARGE CONSTRAINTS:") continue;
+            for (int n = 0; n < npair - 1; ++n) {
+                const size_t li = i + 1 + n;
+                ChargeConstraint cc;
+                for (int j = 0; j < npair; ++j) {
+                    auto it = m.pair_map.find(L.at(li, j));
+                    if (it == m.pair_map.end()) fail("unknown pair in CHARGE CONSTRAINTS: " + L.at(li, j));
+                    cc.pair.push_back(it->second);
+                }
+                for (int j = 0; j < npair; ++j) cc.value.push_back(to_double(L.at(li, npair + j)));
+                cc.force = to_double(L.at(li, L.size(li) - 1));
+                m.charge_constraints.push_back(cc);
+            }
+            break;
+        }
+    }
     // EXCLUDE nB INTERACTION  src/input.C:753-874, CLUSTER_LIST::read_exclude src/Cluster.C:1508-1526
     auto read_exclude = [&](const char* tag, std::vector<std::vector<std::string>>& ex, int natoms) {
         for (size_t i = 0; i < N; ++i) {
@@ -606,7 +626,8 @@ Model load_model(const std::string& path) {
     Controls& c = m.ctl;
     // RUN_SANITY_LSQ src/input.C:1306-1338
     if (c.wrap && c.nlayers > 0) c.wrap = false;
-    if (c.fit_coul) fail("FITCOUL (Ewald charge columns) is outside this build's design-matrix path");
+    if (c.fit_coul && (c.fit_stress || c.fit_stress_all || c.fit_ener))
+        fail("FITCOUL with stress or energy rows: the reference prints no charge columns on those rows");
     if (c.use_partial_charges) fail("fixed partial charges (Ewald subtraction) are outside this build's path");
     if (c.nlayers < 1) fail("NLAYERS must be >= 1 (ghost-atom images); NLAYERS 0 is not supported by this build");
     // main: src/chimes_lsq.C:198-248
@@ -625,7 +646,8 @@ Model load_model(const std::string& path) {
     if (c.use3) for (auto& ct : m.trips.vec) m.num3 += ct.n_true;
     if (c.use4) for (auto& ct : m.quads.vec) m.num4 += ct.n_true;
     m.tot_short = m.tot_snum + m.num3 + m.num4;
-    m.tot_all = m.tot_short + (c.fit_ener ? c.natmtyp : 0);
+    m.ncoul = c.fit_coul ? (int)m.pairs.size() : 0;
+    m.tot_all = m.tot_short + m.ncoul + (c.fit_ener ? c.natmtyp : 0);
     // JOB_CONTROL::LSQ_SETUP src/ClassDefs.C:2761-2785
     if ((c.fit_stress || c.fit_stress_all) && c.nstress == -1) c.nstress = c.nframes;
     if (c.fit_ener && c.nener == -1) c.nener = c.nframes;
@@ -708,8 +730,12 @@ std::string params_header_text(const Model& m) {   // print_param_header src/chi
     h << " " << p0.snum << " " << p0.snum3 << " " << p0.snum4 << " " << p0.range_low << " " << p0.range_high << std::endl;
     h << std::endl << "ATOM TYPES: " << c.natmtyp << std::endl << std::endl;
     h << "# TYPEIDX #\t# ATM_TYP #\t# ATMCHRG #\t# ATMMASS #" << std::endl;
-    for (int i = 0; i < c.natmtyp; ++i)
-        h << i << "\t\t" << m.pairs[i].atm1 << "\t\t" << m.pairs[i].chg1 << "\t\t" << m.pairs[i].mass1 << std::endl;
+    for (int i = 0; i < c.natmtyp; ++i) {   // FITCOUL prints the charge sign instead of the charge
+        h << i << "\t\t" << m.pairs[i].atm1 << "\t\t";
+        if (c.fit_coul) h << m.pairs[i].chrgsgn;
+        else h << m.pairs[i].chg1;
+        h << "\t\t" << m.pairs[i].mass1 << std::endl;
+    }
     h << std::endl << "ATOM PAIRS: " << m.pairs.size() << std::endl << std::endl;
     h << "# PAIRIDX #\t# ATM_TY1 #\t# ATM_TY1 #\t# S_MINIM #\t# S_MAXIM #\t# CHBDIST #\t# MORSE_LAMBDA #" << std::endl;
     for (const auto& p : m.pairs) {
@@ -823,12 +849,38 @@ std::string params_txt_text(const Model& m, const double* x, int nx, const std::
     const int ntypes = std::stoi(at(tok(types_line), 2));
     const size_t pairs_line = types_line + 2 + ntypes + 2;
     const int npairs = std::stoi(at(tok(pairs_line), 2));
+    // FITCOUL: one "q_A x q_B" coefficient per pair after the short-range ones; the
+    // short-range counts are read from the header as the solver script does
+    // (src/chimes_lsq.py:394-458)
+    const bool fit_coul = at(tok(1), 1) == "true";
+    int snum3 = 0, snum4 = 0, counted_coul = 0;
+    if (fit_coul) {
+        auto count_unique = [&](size_t line0, int ncl, size_t uq, size_t tl) {
+            int sum = 0, add = 0;
+            for (int t = 0; t < ncl; ++t) {
+                const auto p1 = tok(line0 + 3 + add);
+                if (at(p1, uq) != "EXCLUDED:") {
+                    sum += std::stoi(at(p1, uq));
+                    add += 5 + std::stoi(at(p1, tl));
+                }
+            }
+            return sum;
+        };
+        if (ntrips > 0) snum3 = count_unique(trip_line, ntrips, 4, 6);
+        if (nquads > 0) snum4 = count_unique(quad_line, nquads, 7, 9);
+    }
     int eff = 0;
     for (int i = 0; i < npairs; ++i) {
         const auto a = tok(pairs_line + 2 + i + 1);
         o << "PAIRTYPE PARAMS: " << i << " " << at(a, 1) << " " << at(a, 2) << "\n\n";
         for (int j = 0; j < snum; ++j) o << fmt("%3d %21.13e", j, x[eff * snum + j]) << "\n";
         ++eff;
+        if (fit_coul) {
+            const int col = npairs * snum + snum3 + snum4 + i;
+            if (col >= nx) throw Error(2, "params.header names a charge coefficient out of range");
+            o << "q_" << at(a, 1) << " x q_" << at(a, 2) << fmt(" %21.13e", x[col]) << "\n";
+            ++counted_coul;
+        }
         o << " \n";
     }
     // natoms 3: pair names in fields 1-3, counts in 4 / 6, power lines carry the param
@@ -876,7 +928,7 @@ std::string params_txt_text(const Model& m, const double* x, int nx, const std::
     o << "\n";
     for (const auto& l : split_lines(ff_groups_map_text(m))) o << l << "\n";
     o << "\n";
-    const int total = eff * snum + counted3 + counted4;
+    const int total = eff * snum + counted3 + counted4 + counted_coul;
     if (total != nx && nx != total + ntypes) throw Error(2, "error in counting parameters");
     if (nx == total + ntypes) {
         o << "NO ENERGY OFFSETS:  " << ntypes << "\n";
@@ -899,6 +951,38 @@ static double vec_angle(double a0, double a1, double a2, double b0, double b1, d
     ang /= vec_mag(a0, a1, a2);
     ang /= vec_mag(b0, b1, b2);
     return std::acos(ang);
+}
+
+void constraint_rows(const Model& m, double* A, int64_t lda, double* b) {
+    for (size_t i = 0; i < m.charge_constraints.size(); ++i) {
+        const ChargeConstraint& cc = m.charge_constraints[i];
+        double* row = A + (int64_t)i * lda;
+        for (int c = 0; c < m.tot_all; ++c) row[c] = 0.0;
+        for (size_t k = 0; k < cc.pair.size(); ++k) row[m.tot_short + cc.pair[k]] = cc.value[k];
+        b[i] = cc.force;
+    }
+}
+
+EwaldParams ewald_params(int natoms, const Box& box) {
+    // Fincham, Mol. Sim. 1, 1-9 (1994): balance the real- and k-space errors at the
+    // target accuracy; the same operations and constants as src/Ewald.C:428-475.
+    const double accuracy = 1.0e-06, effort_ratio = 5.5, balance_factor = 1.1, accuracy_factor = 0.8;
+    double min_boxdim = box.ax;
+    if (box.by < min_boxdim) min_boxdim = box.by;
+    if (box.cz < min_boxdim) min_boxdim = box.cz;
+    const double V = box.ax * box.by * box.cz;
+    const double p = -std::log(accuracy) * accuracy_factor;
+    EwaldParams e;
+    e.alpha = std::sqrt(M_PI) * std::pow(effort_ratio * natoms / (V * V), 1.0 / 6.0);
+    e.rc = balance_factor * std::sqrt(p) / e.alpha;
+    if (e.rc > 0.5 * min_boxdim) {
+        e.rc = 0.5 * min_boxdim;
+        e.alpha = std::sqrt(p) / e.rc;
+    }
+    const double rkc = 2.0 * e.alpha * std::sqrt(p) / balance_factor;
+    const double lavg = std::pow(V, 1.0 / 3.0);
+    e.kmax = (int)std::ceil(rkc * lavg / (2.0 * M_PI));
+    return e;
 }
 
 void Box::update_cell() {   // BOX::UPDATE_CELL src/ClassDefs.C:1940-1971 (and the functions it calls)

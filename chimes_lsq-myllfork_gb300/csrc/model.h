@@ -92,6 +92,14 @@ struct Controls {
     bool use_partial_charges = false;
 };
 
+// One CHARGE CONSTRAINTS line (src/input.C:1148-1200): sum_k value[k] * (q q)_pair[k]
+// = force, appended to the fit as one row after all frames.
+struct ChargeConstraint {
+    std::vector<int> pair;
+    std::vector<double> value;
+    double force = 0.0;
+};
+
 struct Model {
     std::string dir;   // directory of fm_setup.in (trajectory paths are relative to it)
     Controls ctl;
@@ -102,6 +110,8 @@ struct Model {
     std::vector<int> atom_type_idx;
     ClusterList trips, quads;
     int tot_snum = 0, num3 = 0, num4 = 0, tot_short = 0, tot_all = 0;
+    int ncoul = 0;                                   // FITCOUL: one q_i q_j column per pair type
+    std::vector<ChargeConstraint> charge_constraints;
     double max_cutoff_2b = 0, max_cutoff_3b = 0, max_cutoff_4b = 0;
     double deriv_const = 1.0;
 };
@@ -122,6 +132,17 @@ std::string ff_groups_map_text(const Model& m);
 // ff_groups.map exactly.
 std::string params_txt_text(const Model& m, const double* x, int nx, const std::string& preamble);
 
+// The charge-constraint rows of a FITCOUL fit (A_MAT::PRINT_CONSTRAINTS
+// src/A_Matrix.C:569-625): row i is zero in the short-range columns and holds the
+// constraint's value of each pair type in the charge columns; b[i] = its force.
+// A is row-major with lda >= tot_all; writes charge_constraints.size() rows.
+void constraint_rows(const Model& m, double* A, int64_t lda, double* b);
+
+// Ewald parameters of one frame (optimal_ewald_params src/Ewald.C:428-475, with
+// the accuracy 1e-6 of ZCalc_Ewald_Deriv): splitting alpha, real-space cut-off and
+// integer k cut-off.
+struct EwaldParams { double alpha = 0, rc = 0; int kmax = 0; };
+
 // ---------------------------------------------------------------- frames
 
 struct Box {
@@ -134,6 +155,8 @@ struct Box {
     double extent_x = 0, extent_y = 0, extent_z = 0, vol = 0;
     void update_cell();   // BOX::UPDATE_CELL
 };
+
+EwaldParams ewald_params(int natoms, const Box& box);
 
 struct Frame {
     int natoms = 0;

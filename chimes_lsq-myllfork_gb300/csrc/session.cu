@@ -135,6 +135,7 @@ DeviceModel::DeviceModel(const Model& m, int vir_pchunk) {
     d.n2b = m.tot_snum; d.tot_short = m.tot_short; d.tot_all = m.tot_all;
     d.col3 = m.tot_snum; d.col4 = m.tot_snum + m.num3;
     d.fit_ener_cols = c.fit_ener ? c.natmtyp : 0;
+    d.ncoul = m.ncoul;
     d.int_pair_map = dev_upload(allocs, m.int_pair_map.data(), m.int_pair_map.size());
     std::vector<cgd::PairDev> pv;
     for (const auto& p : m.pairs) pv.push_back({p.smin, p.smax, p.lambda, p.xavg, p.xdiff});
@@ -221,6 +222,11 @@ FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int firs
         bd.is_ortho = fr.box.is_ortho ? 1 : 0;
         bd.small = small ? 1 : 0;
         set_small(bd, small);
+        if (m.ncoul > 0) {   // ZCalc_Ewald_Deriv src/Ewald.C:518-550 (orthorhombic cells only)
+            if (!fr.box.is_ortho) throw Error(2, "the Ewald charge columns need an orthorhombic cell");
+            const EwaldParams ep = ewald_params(fr.natoms, fr.box);
+            bd.ew_alpha = ep.alpha; bd.ew_rc = ep.rc; bd.ew_kmax = ep.kmax;
+        }
         fb.box.push_back(bd);
         fb.type.insert(fb.type.end(), fr.type.begin(), fr.type.end());
         fb.xyz.insert(fb.xyz.end(), fr.xyz.begin(), fr.xyz.end());
@@ -611,6 +617,13 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
     if (M.order4 > 0) many_body(4, CS4, n4, kfo_t4, M.ntypes4, M.order4, dm_->max_allowed4);
     if (M.fit_ener_cols > 0) {
         cgd::launch_energy_cols(prec, nf, M, F, A, lda, st); L();
+        CK(cudaGetLastError());
+    }
+    if (M.ncoul > 0) {   // Ewald charge columns (ZCalc_Ewald_Deriv)
+        void* ews = S.get<unsigned char>(cgd::ewald_scratch_bytes(nf, model.ctl.natmtyp));
+        mark(ST_OTHER, true);
+        cgd::launch_ewald(prec, nf, nreal, M, F, ews, A, lda, st); L(3);
+        mark(ST_OTHER, false);
         CK(cudaGetLastError());
     }
     if (stats && !plan_in) {

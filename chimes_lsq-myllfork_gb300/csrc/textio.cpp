@@ -29,10 +29,13 @@ struct Out {
 // b-labeled.txt values in the default stream format (%g),
 // stress and energy rows "%.16e " per column; with energy fitting each row ends in
 // " 0.0" per atom type (force / stress rows) or " <count of that type>" (energy rows).
+// FITCOUL: force rows carry the charge columns after the short-range ones, and the
+// charge-constraint rows follow the last frame ("0.0 " short-range, then the values).
 // natoms.txt has the frame's atom count per row; dim.txt "columns rows".
-void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int64_t lda, const std::string& dir) {
+void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int64_t lda, const std::string& dir,
+                     bool with_constraints) {
     const int C = m.tot_short;
-    const int nener = m.tot_all - m.tot_short;
+    const int nener = m.tot_all - m.tot_short - m.ncoul;
     const bool do_ener = nener > 0;
     Out fa(dir + "/A.txt"), fbv(dir + "/b.txt"), fbl(dir + "/b-labeled.txt"), fna(dir + "/natoms.txt");
     int64_t row = 0;
@@ -54,7 +57,7 @@ void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int6
         for (int a = 0; a < N; ++a) {
             for (int q = 0; q < 3; ++q, ++row) {
                 const double* Ar = A + (r0 + 3 * a + q) * lda;
-                for (int c = 0; c < C; ++c) { fa.num(Ar[c]); fa.s("   "); }
+                for (int c = 0; c < C + m.ncoul; ++c) { fa.num(Ar[c]); fa.s("   "); }   // + charge columns
                 tail(false);
                 const double bv = fb.b[r0 + 3 * a + q];
                 fbv.num(bv); fbv.s("\n");
@@ -79,6 +82,18 @@ void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int6
             tail(true);
             fbv.num(fb.b[r]); fbv.s("\n");
             fbl.s("+1 "); fbl.lab(fb.b[r]); fbl.s("\n");
+        }
+    }
+    if (with_constraints && !m.charge_constraints.empty()) {   // A_MAT::PRINT_CONSTRAINTS src/A_Matrix.C:606-623
+        const int np = (int)m.pairs.size();
+        for (const ChargeConstraint& cc : m.charge_constraints) {
+            for (int c = 0; c < C; ++c) fa.s("0.0 ");
+            for (int j = 0; j < np; ++j)
+                for (size_t k = 0; k < cc.pair.size(); ++k)
+                    if (cc.pair[k] == j) { fa.num(cc.value[k]); fa.s(" "); }
+            fa.s("\n");
+            fbv.num(cc.force); fbv.s("\n");
+            ++row;
         }
     }
     Out fd(dir + "/dim.txt");
@@ -128,7 +143,14 @@ std::vector<double> params_txt_coefficients(const Model& m, const std::string& t
             ++ctype;
             continue;
         }
-        if (t.size() >= 4 && t[0] == "ENERGY" && t[1] == "OFFSET") { put(m.tot_short + std::stoi(t[2]) - 1, std::stod(t[3])); continue; }
+        if (t.size() >= 4 && t[0] == "ENERGY" && t[1] == "OFFSET") {
+            put(m.tot_short + m.ncoul + std::stoi(t[2]) - 1, std::stod(t[3]));
+            continue;
+        }
+        if (section == 2 && pair >= 0 && m.ncoul > 0 && t.size() == 4 && t[1] == "x" && t[0].rfind("q_", 0) == 0) {
+            put(m.tot_short + pair, std::stod(t[3]));   // charge product of the pair (FITCOUL)
+            continue;
+        }
         if (section == 2 && pair >= 0 && t.size() == 2 && snum > 0 && t[0].find_first_not_of("0123456789") == std::string::npos) {
             const int k = std::stoi(t[0]);
             if (k < snum) put(pair * snum + k, std::stod(t[1]));

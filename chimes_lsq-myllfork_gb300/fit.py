@@ -60,7 +60,9 @@ def main(argv=None):
     G = torch.zeros((C, C), dtype=torch.float64, device="cuda")
     h = torch.zeros(C, dtype=torch.float64, device="cuda")
     blocks = [frames.slice(f0, min(args.block_frames, nf - f0)) for f0 in range(0, nf, args.block_frames)]
-    nrows = sum(b.nrows for b in blocks)
+    Acon, bcon = model.constraint_rows()   # FITCOUL charge constraints, after the last frame
+    nfr_rows = sum(b.nrows for b in blocks)
+    nrows = nfr_rows + Acon.shape[0]
     fits = nrows * C * 8 < 0.5 * torch.cuda.mem_get_info()[0]
     keep64 = fits and (not mixed or (args.algorithm == "ridge" and args.refine > 0))
     A64_all = torch.empty((nrows, C), dtype=torch.float64, device="cuda") if keep64 else None
@@ -82,6 +84,12 @@ def main(argv=None):
                 sess.gram(0, dst.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr())
             del dst
         r0 += n
+    if Acon.shape[0]:   # the constraint rows join the normal equations like any row block
+        dAc = torch.from_numpy(Acon).cuda()
+        b_all[r0:] = torch.from_numpy(bcon)
+        sess.gram(0, dAc.data_ptr(), C, Acon.shape[0], C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr())
+        if keep64:
+            A64_all[r0:] = dAc
     sess.gram_finish(G.data_ptr(), C)
     x = torch.zeros(C, dtype=torch.float64, device="cuda")
     lines = [f"! Date  {datetime.date.today()}", "!", f"! Number of variables            =  {C}",
@@ -109,6 +117,7 @@ def main(argv=None):
             sess.assemble_device(dfr, cg.CG_FP64, A.data_ptr(), C)
             ys.append((A @ x).cpu().numpy())
             del A
+        ys.append(Acon @ xh)
         y = np.concatenate(ys)
     b = b_all.cpu().numpy()
     Z = float(((y - b) ** 2).sum())
@@ -122,10 +131,10 @@ def main(argv=None):
         f.write("".join("%13.6e\n" % v for v in y))
     open(os.path.join(out, "params.txt"), "w").write(model.params_txt(xh, "\n".join(lines) + "\n"))
     if args.write_a:
-        A = A64_all.cpu().numpy() if keep64 else None
+        A = A64_all[:nfr_rows].cpu().numpy() if keep64 else None
         if A is None:
             A = np.concatenate([sess.assemble(blk, cg.CG_FP64) for blk in blocks])
-        frames.write_lsq_files(A, out)
+        frames.write_lsq_files(A, out)   # (appends the constraint rows)
     print(f"fit: {nrows} rows x {C} columns, {args.algorithm} alpha {args.alpha:g}, {args.precision}; "
           f"RMS {math.sqrt(Z / nrows):.4e}; wrote {out}/params.txt")
     return xh, y

@@ -234,9 +234,12 @@ def write_xyzf(path, frames, species):
 
 
 def write_fm_setup(path, xyzf_name, nframes, species, masses, order2, order3, order4, smin, smax2, lam,
-                   smax3=None, smax4=None, fitstrs=None, fitener=False, nlayers=1):
+                   smax3=None, smax4=None, fitstrs=None, fitener=False, nlayers=1, fitcoul=False):
+    """fitcoul: fit the Ewald charge products (FITCOUL true, charge signs instead of
+    charges, npairs-1 CHARGE CONSTRAINTS lines tying the products together)."""
     lines = ["####### CONTROL VARIABLES #######", "", "# TRJFILE #", f"\t{xyzf_name}", "# WRAPTRJ #", "\ttrue",
-             "# NFRAMES #", f"\t{nframes}", "# NLAYERS #", f"\t{nlayers}", "# FITCOUL #", "\tfalse"]
+             "# NFRAMES #", f"\t{nframes}", "# NLAYERS #", f"\t{nlayers}", "# FITCOUL #",
+             "\ttrue" if fitcoul else "\tfalse"]
     if fitstrs:
         lines += ["# FITSTRS #", f"\t{fitstrs}"]
     if fitener:
@@ -245,7 +248,8 @@ def write_fm_setup(path, xyzf_name, nframes, species, masses, order2, order3, or
               "####### TOPOLOGY VARIABLES #######", "", "# NATMTYP # ", f"\t{len(species)}", "",
               "# TYPEIDX #\t# ATM_TYP #\t# ATMCHRG #\t# ATMMASS #"]
     for k, (s, m) in enumerate(zip(species, masses)):
-        lines.append(f"{k + 1}\t\t{s}\t\t0.0\t\t{m}")
+        chg = ("-" if k == 0 else "+") if fitcoul else "0.0"
+        lines.append(f"{k + 1}\t\t{s}\t\t{chg}\t\t{m}")
     lines += ["", "# PAIRIDX #\t# ATM_TY1 #\t# ATM_TY1 #\t# S_MINIM #\t# S_MAXIM #\t# S_DELTA #\t# MORSE_LAMBDA #"]
     k = 1
     n = len(species)
@@ -253,6 +257,12 @@ def write_fm_setup(path, xyzf_name, nframes, species, masses, order2, order3, or
     for a, b in pairs:
         lines.append(f"{k}\t\t{species[a]}\t\t{species[b]}\t\t{smin}\t\t{smax2}\t\t0.01\t\t{lam}")
         k += 1
+    if fitcoul:   # npairs-1 constraints: names, one weight per pair, force
+        names = [species[a] + species[b] for a, b in pairs]
+        lines.append("CHARGE CONSTRAINTS:")
+        for c in range(len(pairs) - 1):
+            w = [10000.0 * (1 + ((c + i) % 3)) * (-1 if (c + i) % 2 else 1) for i in range(len(pairs))]
+            lines.append("\t".join(names + [f"{v:.1f}" for v in w] + ["0.0"]))
     if order3 and smax3 is not None:
         lines += ["", f"SPECIAL 3B S_MAXIM: ALL {smax3}"]
     if order4 and smax4 is not None:
@@ -319,7 +329,8 @@ def make_workload(name, outdir, nframes=None, seed=1234, labels=True, **over):
     s2, s3, s4 = cfg["smax"]
     p = os.path.join(outdir, "fm_setup.in")
     write_fm_setup(p, "traj.xyzf", cfg["nframes"], species, masses, o2, o3, o4, cfg["smin"], s2, cfg["lam"],
-                   smax3=s3, smax4=s4, fitstrs=cfg["fitstrs"], fitener=cfg["fitener"])
+                   smax3=s3, smax4=s4, fitstrs=cfg["fitstrs"], fitener=cfg["fitener"],
+                   fitcoul=cfg.get("fitcoul", False))
     return p
 
 

@@ -37,6 +37,16 @@ void cg_model_free(cg_model* m);
  * (TOT_SNUM, NUM_3B_CHEBY, NUM_4B_CHEBY, TOT_ALL_PARAMS in src/chimes_lsq.C:198-248). */
 int cg_model_columns(const cg_model* m, int* n2b, int* n3b, int* n4b, int* nener, int* ntotal);
 
+/* FITCOUL (src/Ewald.C:477-750, src/A_Matrix.C:249-288): ncoul charge columns (one
+ * q_i q_j product per pair type, after the short-range columns, before the energy
+ * columns) and the number of CHARGE CONSTRAINTS rows (src/input.C:1148-1200). */
+int cg_model_charge_columns(const cg_model* m, int* ncoul, int* nconstraints);
+
+/* The charge-constraint rows that follow the last frame of a FITCOUL fit
+ * (A_MAT::PRINT_CONSTRAINTS src/A_Matrix.C:569-625): nconstraints rows of A
+ * (row-major, lda >= total columns) and their b values. */
+int cg_model_constraint_rows(const cg_model* m, double* A, int64_t lda, double* b);
+
 /* Number of frames (NFRAMES) and atom types (NATMTYP) of the model. */
 int cg_model_sizes(const cg_model* m, int* nframes, int* natmtyp);
 
@@ -82,6 +92,8 @@ int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms);
  * src/A_Matrix.C:210-720; %.16e, three spaces after force-row entries, one after
  * stress / energy entries). */
 int cg_write_lsq_files(const cg_model* m, const cg_frames* fr, const double* A, int64_t lda, const char* dir);
+/* (FITCOUL models: A holds the frames' rows; the charge-constraint rows are appended
+ * to A.txt and b.txt after them, as the reference writes them.) */
 
 /* Number of frames in a batch. */
 int cg_frames_count(const cg_frames* fr, int* nframes);

@@ -14,6 +14,7 @@
 //   2-body rows     Cheby::Deriv_2B                src/Cheby.C:709-883
 //   3-body rows     Cheby::Deriv_3B                src/Cheby.C:885-1277
 //   4-body rows     Cheby::Deriv_4B                src/Cheby.C:1279-1729
+//   charge columns  ZCalc_Ewald_Deriv              src/Ewald.C:477-825 (FITCOUL)
 //   row layout, b   A_MAT::PRINT_FRAME             src/A_Matrix.C:210-567
 //   MD force        ZCalc                          src/functions.C:815-891
 //                   Cheby::Force_all / 3B / 4B     src/Cheby.C:1731-2675
@@ -130,7 +131,7 @@ OFrame make_frame(const Model& m, const Frame& fr) {
 }
 
 struct Lists {
-    std::vector<std::vector<int>> l2, l3, l4;
+    std::vector<std::vector<int>> l2, l3, l4, lew;   // lew: LIST_EWALD (FITCOUL)
     double perm[5] = {1, 1, 1, 1, 1};
 };
 
@@ -143,11 +144,12 @@ double max_all_cutoffs(const Model& m) {
 }
 
 // NEIGHBORS::DO_UPDATE_BIG (pad 0.3) / DO_UPDATE_SMALL
-Lists neighbours(const Model& m, const OFrame& fr, bool small) {
+Lists neighbours(const Model& m, const OFrame& fr, bool small, double ewald_cut = 0.0) {
     Lists L;
-    L.l2.resize(fr.natoms); L.l3.resize(fr.natoms); L.l4.resize(fr.natoms);
+    L.l2.resize(fr.natoms); L.l3.resize(fr.natoms); L.l4.resize(fr.natoms); L.lew.resize(fr.natoms);
     const double pad = m.ctl.use_neigh ? 0.3 : 1.0e10;
     const double c2 = m.max_cutoff_2b + pad, c3 = m.max_cutoff_3b + pad, c4 = m.max_cutoff_4b + pad;
+    const double cew = ewald_cut + pad;
     V3 rab;
     if (small) {
         for (int j = 2; j < 5; ++j) L.perm[j] = L.perm[j - 1] / j;
@@ -158,6 +160,7 @@ Lists neighbours(const Model& m, const OFrame& fr, bool small) {
                 if (r < c2) L.l2[a1].push_back(a2);
                 if (r < c3) L.l3[a1].push_back(a2);
                 if (r < c4) L.l4[a1].push_back(a2);
+                if (r < cew) L.lew[a1].push_back(a2);
             }
         return L;
     }
@@ -166,6 +169,7 @@ Lists neighbours(const Model& m, const OFrame& fr, bool small) {
     double search = m.max_cutoff_2b;
     if (m.max_cutoff_3b > search) search = m.max_cutoff_3b;
     if (m.max_cutoff_4b > search) search = m.max_cutoff_4b;
+    if (ewald_cut > search) search = ewald_cut;   // SEARCH_DIST includes EWALD_CUTOFF
     search += pad;
     int nx = (int)std::ceil((2 * NL + 1) * b.extent_x / search) + 2;
     int ny = (int)std::ceil((2 * NL + 1) * b.extent_y / search) + 2;
@@ -195,6 +199,7 @@ Lists neighbours(const Model& m, const OFrame& fr, bool small) {
                         double r = get_dist(b, fr.coords[a1], fr.coords[a2], rab);
                         if (a1 <= fr.parent[a2]) {
                             if (r < c2) L.l2[a1].push_back(a2);
+                            if (r < cew) L.lew[a1].push_back(a2);
                             if (r < c3) L.l3[a1].push_back(a2);
                             if (r < c4) L.l4[a1].push_back(a2);
                         }
@@ -454,10 +459,125 @@ void deriv_4b(const Model& m, const OFrame& fr, const Lists& L, Acc& A, bool fs,
             }
 }
 
+// ZCalc_Ewald_Deriv src/Ewald.C:477-750 (orthorhombic): Q[(p * N + a) * 3 + x], the
+// charge-column force of atom a per unit q_i q_j of pair type p.  Real space over
+// LIST_EWALD, k space over every atom pair with the per-pair sine tables of
+// generate_trig / add_sines (src/Ewald.C:752-825), then the sign flip.
+void ewald_add_sines(int kx, int ky, int kz, const std::vector<V3>& S, const std::vector<V3>& C, double& out) {
+    V3 sk, ck;
+    if (kx >= 0) { sk.x = S[kx].x; ck.x = C[kx].x; } else { sk.x = -S[-kx].x; ck.x = C[-kx].x; }
+    if (ky >= 0) { sk.y = S[ky].y; ck.y = C[ky].y; } else { sk.y = -S[-ky].y; ck.y = C[-ky].y; }
+    if (kz >= 0) { sk.z = S[kz].z; ck.z = C[kz].z; } else { sk.z = -S[-kz].z; ck.z = C[-kz].z; }
+    const double syz = sk.y * ck.z + ck.y * sk.z;
+    const double cyz = ck.y * ck.z - sk.y * sk.z;
+    out = sk.x * cyz + ck.x * syz;
+}
+
+void ewald_deriv(const Model& m, const OFrame& fr, const Frame& raw, const Lists& L, const EwaldParams& ep,
+                 std::vector<double>& Q) {
+    const int N = fr.natoms, np = (int)m.pairs.size();
+    Q.assign((size_t)np * N * 3, 0.0);
+    auto q = [&](int p, int a) { return &Q[((size_t)p * N + a) * 3]; };
+    const double PI = 3.14159265359, ke = 1.0;
+    const double alpha = ep.alpha, alphasq = alpha * alpha, r_cut = ep.rc;
+    const int kmax = ep.kmax, ksqmax = 50;
+    const Box& b = fr.box;
+    const double Volume = b.vol;
+    std::vector<int> kv;   // kx, ky, kz triples
+    std::vector<double> kfac;
+    for (int kx = 0; kx <= kmax; kx++)
+        for (int ky = 0; ky <= kmax; ky++)
+            for (int kz = 0; kz <= kmax; kz++) {
+                const int ksq = kx * kx + ky * ky + kz * kz;
+                if (ksq != 0 && ksq < ksqmax) {
+                    const double rx = (2.0 * PI / b.ax) * kx, ry = (2.0 * PI / b.by) * ky, rz = (2.0 * PI / b.cz) * kz;
+                    const double rksq = rx * rx + ry * ry + rz * rz;
+                    kv.push_back(kx); kv.push_back(ky); kv.push_back(kz);
+                    kfac.push_back(std::exp(-rksq / (4.0 * alphasq)) / rksq);
+                }
+            }
+    const double perm_scale = L.perm[2];
+    V3 R;
+    for (int a1 = 0; a1 < N; a1++)
+        for (int a2 : L.lew[a1]) {
+            const int fidx = fr.parent[a2];
+            const int p = pair_index(m, fr, a1, a2);
+            const double rl = get_dist(b, fr.coords[a1], fr.coords[a2], R);
+            if (rl < r_cut) {
+                double t = ((-2.0 / std::sqrt(PI)) * std::exp(-1 * alpha * alpha * rl * rl) * rl * alpha -
+                            std::erfc(alpha * rl)) / (rl * rl);
+                t *= -1.0; t *= 2.0; t *= ke; t *= 0.5 / rl; t *= perm_scale;
+                double* qa = q(p, a1);
+                double* qb = q(p, fidx);
+                qa[0] += t * R.x; qa[1] += t * R.y; qa[2] += t * R.z;
+                qb[0] -= t * R.x; qb[1] -= t * R.y; qb[2] -= t * R.z;
+            }
+        }
+    std::vector<V3> S(kmax + 1), C(kmax + 1);
+    const int totk = (int)kfac.size();
+    for (int a1 = 0; a1 < N; a1++)
+        for (int a2 = 0; a2 < a1; a2++) {
+            const int p = pair_index(m, fr, a1, a2);
+            V3 rv{raw.xyz[3 * a2] - raw.xyz[3 * a1], raw.xyz[3 * a2 + 1] - raw.xyz[3 * a1 + 1],
+                  raw.xyz[3 * a2 + 2] - raw.xyz[3 * a1 + 2]};
+            S[0] = {0.0, 0.0, 0.0};
+            C[0] = {1.0, 1.0, 1.0};
+            if (kmax >= 1) {
+                S[1] = {std::sin(2.0 * M_PI * rv.x / b.ax), std::sin(2.0 * M_PI * rv.y / b.by),
+                        std::sin(2.0 * M_PI * rv.z / b.cz)};
+                C[1] = {std::cos(2.0 * M_PI * rv.x / b.ax), std::cos(2.0 * M_PI * rv.y / b.by),
+                        std::cos(2.0 * M_PI * rv.z / b.cz)};
+            }
+            for (int ik = 2; ik <= kmax; ik++) {
+                S[ik].x = S[ik - 1].x * C[1].x + C[ik - 1].x * S[1].x;
+                S[ik].y = S[ik - 1].y * C[1].y + C[ik - 1].y * S[1].y;
+                S[ik].z = S[ik - 1].z * C[1].z + C[ik - 1].z * S[1].z;
+                C[ik].x = C[ik - 1].x * C[1].x - S[ik - 1].x * S[1].x;
+                C[ik].y = C[ik - 1].y * C[1].y - S[ik - 1].y * S[1].y;
+                C[ik].z = C[ik - 1].z * C[1].z - S[ik - 1].z * S[1].z;
+            }
+            double* qa = q(p, a1);
+            double* qb = q(p, a2);
+            for (int ik = 0; ik < totk; ik++) {
+                const int kx = kv[3 * ik], ky = kv[3 * ik + 1], kz = kv[3 * ik + 2];
+                const double rkx = (2.0 * PI / b.ax) * kx, rky = (2.0 * PI / b.by) * ky, rkz = (2.0 * PI / b.cz) * kz;
+                const double Kfac = kfac[ik];
+                double t1, t2 = 0.0, t3 = 0.0, t4 = 0.0;
+                ewald_add_sines(kx, ky, kz, S, C, t1);
+                t1 *= ke; t1 *= 2.0; t1 *= Kfac * 0.5 * (4 * PI / Volume);
+                if (ky > 0) {
+                    ewald_add_sines(kx, -ky, kz, S, C, t2);
+                    t2 *= ke; t2 *= 2.0; t2 *= Kfac * 0.5 * (4 * PI / Volume);
+                    if (kz > 0) {
+                        ewald_add_sines(kx, -ky, -kz, S, C, t3);
+                        t3 *= ke; t3 *= 2.0; t3 *= Kfac * 0.5 * (4 * PI / Volume);
+                    }
+                }
+                if (kz > 0) {
+                    ewald_add_sines(kx, ky, -kz, S, C, t4);
+                    t4 *= ke; t4 *= 2.0; t4 *= Kfac * 0.5 * (4 * PI / Volume);
+                }
+                if (kx > 0) { t1 *= 2.0; t2 *= 2.0; t3 *= 2.0; t4 *= 2.0; }
+                qa[0] += (t1 + t2 + t3 + t4) * rkx;
+                qa[1] += (t1 - t2 - t3 + t4) * rky;
+                qa[2] += (t1 + t2 - t3 - t4) * rkz;
+                qb[0] -= (t1 + t2 + t3 + t4) * rkx;
+                qb[1] -= (t1 - t2 - t3 + t4) * rky;
+                qb[2] -= (t1 + t2 - t3 - t4) * rkz;
+            }
+        }
+    for (double& v : Q) v *= -1.0;
+}
+
 // One frame's A rows (dense, lda >= tot_all) and b values.
 void frame_rows_out(const Model& m, const Frame& fr, int fi, bool small, double* out, int64_t lda, double* b) {
     OFrame of = make_frame(m, fr);
-    Lists L = neighbours(m, of, small);
+    EwaldParams ep;
+    if (m.ncoul > 0) {
+        if (!fr.box.is_ortho) throw Error(2, "oracle: Ewald needs an orthorhombic cell");
+        ep = ewald_params(fr.natoms, fr.box);
+    }
+    Lists L = neighbours(m, of, small, m.ncoul > 0 ? ep.rc : 0.0);
     RowLayout rl = frame_rows(m, fi, fr.natoms);
     const bool fs = rl.stress_rows == 3, fsa = rl.stress_rows == 9, fe = rl.energy_rows > 0;
     Acc A(fr.natoms, m.tot_short);
@@ -472,11 +592,14 @@ void frame_rows_out(const Model& m, const Frame& fr, int fi, bool small, double*
     auto put = [&](int64_t r, int c, double v) { out[r * lda + c] = v; };
     std::vector<int> count(m.ctl.natmtyp, 0);
     for (int a = 0; a < fr.natoms; ++a) count[fr.type[a]]++;
-    const int nener = m.tot_all - m.tot_short;
+    const int nener = m.tot_all - m.tot_short - m.ncoul;
+    std::vector<double> Q;
+    if (m.ncoul > 0) ewald_deriv(m, of, fr, L, ep, Q);
     for (int a = 0; a < fr.natoms; ++a)
         for (int x = 0; x < 3; ++x, ++row) {
             for (int c = 0; c < m.tot_short; ++c) put(row, c, A.f(a, c)[x]);
-            for (int t = 0; t < nener; ++t) put(row, m.tot_short + t, 0.0);
+            for (int p = 0; p < m.ncoul; ++p) put(row, m.tot_short + p, Q[((size_t)p * fr.natoms + a) * 3 + x]);
+            for (int t = 0; t < nener; ++t) put(row, m.tot_short + m.ncoul + t, 0.0);
             b[row] = fr.force[3 * a + x];
         }
     if (rl.stress_rows) {

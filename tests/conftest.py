@@ -35,4 +35,13 @@ def fixture_dir(name):
     return os.path.join(GOLDEN, name)
 
 
-FIXTURES = ["water2b", "water3b", "ch4b", "small4b"]
+FIXTURES = ["water2b", "water3b", "ch4b", "small4b", "watercoul"]
+
+
+def frame_part(model, ref):
+    """(A, b) of a reference fixture without the charge-constraint rows that a
+    FITCOUL fit appends after its last frame, and those rows (A, b)."""
+    _, nc = model.charge_columns()
+    A, b = ref["A"], ref["b"]
+    n = A.shape[0] - nc
+    return A[:n], b[:n], A[n:], b[n:]

@@ -4,7 +4,8 @@ Run in a container where the reference sources are available:
     python oracle/build_ref.sh && python tests/golden/make_fixtures.py
 Each fixture directory holds the seeded synthetic inputs (fm_setup.in, traj.xyzf)
 and ref.npz with the reference's A matrix and b vector (read back from its
-A.txt / b.txt, written with %.16e, so the round trip is exact).
+A.txt / b.txt, written with %.16e, so the round trip is exact); a FITCOUL fixture's
+A ends with the charge-constraint rows, as the reference writes them.
 """
 import importlib
 import os
@@ -32,6 +33,9 @@ FIXTURES = {
     # small cubic cell (extent below the cut-off): unordered neighbour convention, PERM_SCALE 1/n!
     "small4b": ("chno-4b", dict(natoms=12, order=(6, 3, 2), triclinic=False, density=0.1, species2=True,
                                 fitstrs=None, fitener=True), 1, 14),
+    # 32 water molecules with the Ewald charge columns and charge constraints (FITCOUL)
+    "watercoul": ("water-2b", dict(nmol=32, L=9.86, order=(8, 4, 0), smax=(5.0, 4.0, None), fitcoul=True,
+                                   disp=0.1), 2, 15),
 }
 
 

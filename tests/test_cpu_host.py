@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import FIXTURES, GOLDEN, REFERENCE, ROOT, fixture_dir
+from conftest import FIXTURES, GOLDEN, REFERENCE, ROOT, fixture_dir, frame_part
 
 HEADER = os.path.join(ROOT, "include", "chimes_gb300.h")
 
@@ -40,28 +40,34 @@ def test_labels_and_rows_match_reference(cg, name):
     ref = np.load(os.path.join(d, "ref.npz"))
     m = cg.Model(os.path.join(d, "fm_setup.in"))
     fr = cg.Frames.read(m)
-    assert fr.nrows == ref["A"].shape[0]
+    A, b, Ac, bc = frame_part(m, ref)
+    assert fr.nrows == A.shape[0]
     assert m.ncols == ref["A"].shape[1]
-    assert np.array_equal(fr.labels(), ref["b"])
+    assert np.array_equal(fr.labels(), b)
+    Cc, cb = m.constraint_rows()   # FITCOUL charge-constraint rows (none otherwise)
+    assert np.array_equal(Cc, Ac) and np.array_equal(cb, bc)
 
 
 @pytest.mark.parametrize("name", FIXTURES)
-def test_oracle_matches_reference_fixture(oracle, name):
+def test_oracle_matches_reference_fixture(cg, oracle, name):
     d = fixture_dir(name)
     A, b = oracle.assemble(os.path.join(d, "fm_setup.in"), nthreads=4)
     ref = np.load(os.path.join(d, "ref.npz"))
-    R = ref["A"]
+    R, rb, _, _ = frame_part(cg.Model(os.path.join(d, "fm_setup.in")), ref)
     colmax = np.abs(R).max(axis=0)
     assert np.all(np.abs(A - R) <= 4e-16 * np.abs(R) + 1e-15 * colmax[None, :])
-    assert np.array_equal(b, ref["b"])
+    assert np.array_equal(b, rb)
 
 
 def test_model_errors_are_reported(cg, tmp_path):
     with pytest.raises(cg.ChimesError) as e:
         cg.Model(str(tmp_path / "missing.in"))
     assert e.value.code == 2
-    src = open(os.path.join(fixture_dir("water2b"), "fm_setup.in")).read()
+    # charge columns with stress / energy rows: the reference prints no charge
+    # columns there, so the combination is refused
+    src = open(os.path.join(fixture_dir("water3b"), "fm_setup.in")).read()
     bad = src.replace("# FITCOUL #\n\tfalse", "# FITCOUL #\n\ttrue")
+    assert bad != src
     p = tmp_path / "fm_setup.in"
     p.write_text(bad)
     with pytest.raises(cg.ChimesError, match="FITCOUL"):
@@ -187,3 +193,75 @@ def test_lsq_text_files_match_reference_nonorth2(cg, tmp_path):
     for f in ("A.txt", "b.txt", "b-labeled.txt", "natoms.txt", "dim.txt"):
         ref = os.path.join(gold, "A.txt.aa" if f == "A.txt" else f)
         assert open(out / f).read() == open(ref).read(), f
+
+
+# ---------------------------------------------------------------- FITCOUL (Ewald charge columns)
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", "chimes_lsq")
+needs_bin = pytest.mark.skipif(not os.path.isfile(REF_BIN), reason="reference binary not built here")
+LSQ2_PARAMS = ["params.ridge.1.0e-03.txt", "params.lassolars.1.0e-04.txt", "params.dlars.1.0e-04.txt",
+               "params.dlasso.1.0e-04.txt", "params.svd.1.0e-04.txt"]
+
+
+@needs_ref
+def test_lsq2_fitcoul_header_and_map(cg, tmp_path):
+    """The reference's lsq2 case (FITCOUL, charge constraints, 2B10 / 3B6 / 4B2)."""
+    src = os.path.join(REF_LSQ, "lsq2")
+    m = cg.Model(os.path.join(src, "fm_setup.in"))
+    assert m.charge_columns() == (3, 2)
+    assert m.ncols == 419
+    assert m.params_header() == open(os.path.join(src, "correct_output", "params.header")).read()
+
+
+@needs_ref
+@pytest.mark.parametrize("name", LSQ2_PARAMS)
+def test_lsq2_params_txt_round_trip(cg, name):
+    """The reference's lsq2 solver outputs (charge products "q_A x q_B" after each
+    pair's coefficients): params.txt -> coefficients -> params.txt is byte-identical."""
+    src = os.path.join(REF_LSQ, "lsq2")
+    m = cg.Model(os.path.join(src, "fm_setup.in"))
+    gold = open(os.path.join(src, "correct_output", name)).read()
+    head = gold.index("USECOUL:")   # the solver's preamble ("!" lines, blank lines of the DLARS runs)
+    pre = gold[:head]
+    x = m.params_read(gold)
+    assert m.params_txt(x, pre) == gold
+
+
+@needs_ref
+@needs_bin
+def test_oracle_matches_reference_binary_lsq2(oracle, cg, tmp_path):
+    """The oracle's Ewald restatement against the reference binary on the first two
+    frames of lsq2 (real- and k-space charge columns, constraint rows, labels)."""
+    src = os.path.join(REF_LSQ, "lsq2")
+    shutil.copy(os.path.join(src, "input.xyzf"), tmp_path)
+    fm = open(os.path.join(src, "fm_setup.in")).read()
+    fm = re.sub(r"(# NFRAMES #[^\n]*\n\s*)33", r"\g<1>2", fm)
+    (tmp_path / "fm_setup.in").write_text(fm)
+    subprocess.run([REF_BIN, "fm_setup.in"], cwd=tmp_path, check=True, stdout=subprocess.DEVNULL)
+    R = np.loadtxt(tmp_path / "A.txt")
+    rb = np.loadtxt(tmp_path / "b.txt")
+    A, b = oracle.assemble(str(tmp_path / "fm_setup.in"), nthreads=4)
+    m = cg.Model(str(tmp_path / "fm_setup.in"))
+    Cc, cb = m.constraint_rows()
+    assert R.shape[0] == A.shape[0] + Cc.shape[0]
+    colmax = np.abs(R).max(axis=0)
+    assert np.all(np.abs(A - R[:A.shape[0]]) <= 1e-15 * np.abs(R[:A.shape[0]]) + 1e-15 * colmax[None, :])
+    assert np.array_equal(Cc, R[A.shape[0]:]) and np.array_equal(cb, rb[A.shape[0]:])
+    assert np.array_equal(b, rb[:A.shape[0]])
+
+
+@needs_bin
+def test_lsq_text_files_match_reference_fitcoul(cg, tmp_path):
+    """A.txt (charge columns, constraint rows), b.txt, b-labeled.txt, natoms.txt and
+    dim.txt byte-identical to the reference's on the FITCOUL fixture."""
+    d = fixture_dir("watercoul")
+    for f in ("fm_setup.in", "traj.xyzf"):
+        shutil.copy(os.path.join(d, f), tmp_path)
+    subprocess.run([REF_BIN, "fm_setup.in"], cwd=tmp_path, check=True, stdout=subprocess.DEVNULL)
+    m = cg.Model(str(tmp_path / "fm_setup.in"))
+    frames = cg.Frames.read(m)
+    A = np.loadtxt(tmp_path / "A.txt")[: frames.nrows]
+    out = tmp_path / "out"
+    out.mkdir()
+    frames.write_lsq_files(A, out)
+    for f in ("A.txt", "b.txt", "b-labeled.txt", "natoms.txt", "dim.txt"):
+        assert open(out / f).read() == open(tmp_path / f).read(), f

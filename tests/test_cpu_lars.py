@@ -42,3 +42,20 @@ def test_cholesky_delete_matches_refactorisation():
         Ld = lars._chol_delete(L, k)
         keep = [i for i in range(12) if i != k]
         assert np.allclose(Ld @ Ld.T, G[np.ix_(keep, keep)], rtol=1e-12, atol=1e-12)
+
+
+def test_oracle_lars_matches_reference_lsq2_output():
+    """The LARS oracle on the normal equations of the reference's lsq2 case reproduces
+    the coefficients of the reference's params.lassolars.1.0e-04.txt (its
+    chimes_lsq.py --algorithm lassolars output): same support, 1e-6 of max|x|."""
+    import lars
+    d = np.load(os.path.join(GOLDEN, "lsq2", "normal.npz"))
+    n = int(d["ncols"])
+    G = np.zeros((n, n))
+    G[np.triu_indices(n)] = d["G_upper"]
+    G = G + np.triu(G, 1).T
+    out = lars.lars_lasso(G, d["h"], int(d["nrows"]), 1e-4)
+    x = out[0] if isinstance(out, tuple) else out
+    ref = d["x_lassolars_1e-4"]
+    assert np.array_equal(x != 0, ref != 0)
+    assert np.abs(x - ref).max() <= 1e-6 * np.abs(ref).max()
