@@ -35,7 +35,9 @@ void residual(const double* A, int64_t lda, int64_t nrows, int ncols, const doub
 
 // LARS with the lasso modification on G (full symmetric, FP64, device) and h:
 // coefficients into x (device); info: [steps, active variables, final C / n].
+// mode 0: scikit-learn LassoLars; mode 1 / 2: the reference's DLARS `lars` /
+// `lasso` (needs btb = b^T b; info[2] is then the objective of the last vertex).
 void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
-                double* info, void* cublas, cudaStream_t st);
+                double* info, void* cublas, cudaStream_t st, int mode = 0, double btb = 0.0);
 
 }  // namespace cg

@@ -33,12 +33,13 @@ struct ArgMax {
 
 __device__ __forceinline__ ArgMax amax(ArgMax a, ArgMax b) { return (b.v > a.v || (b.v == a.v && b.i < a.i)) ? b : a; }
 
-// max |c_j| over inactive j (flag 0); single block, lowest index wins ties
-__global__ void k_lars_argmax(const double* c, const int* flag, int n, ArgMax* out) {
+// max |c_j| over j with flag <= maxflag (0: inactive only, 1: inactive and
+// active); single block, lowest index wins ties
+__global__ void k_lars_argmax(const double* c, const int* flag, int n, ArgMax* out, int maxflag = 0) {
     __shared__ ArgMax sm[32];
     ArgMax best{-1.0, -1};
     for (int j = threadIdx.x; j < n; j += blockDim.x)
-        if (flag[j] == 0) best = amax(best, ArgMax{fabs(c[j]), j});
+        if (flag[j] <= maxflag) best = amax(best, ArgMax{fabs(c[j]), j});
     for (int o = 16; o > 0; o >>= 1) {
         ArgMax other{__shfl_down_sync(0xffffffffu, best.v, o), __shfl_down_sync(0xffffffffu, best.i, o)};
         best = amax(best, other);
@@ -125,7 +126,7 @@ __device__ __forceinline__ MinPos mmin(MinPos a, MinPos b) { return (b.v < a.v |
 // variable that just left (its same-sign root is the current point).
 __global__ void k_lars_steps(const double* c, const double* a, const int* flag, int n, double C, double AA,
                              int dropped, const double* beta, const int* active, const double* w, int na,
-                             MinPos* out) {
+                             MinPos* out, double zmin = 0.0) {
     __shared__ MinPos s1[32], s2[32];
     MinPos b1{INFINITY, -1}, b2{INFINITY, -1};
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -138,7 +139,7 @@ __global__ void k_lars_steps(const double* c, const double* a, const int* flag, 
     }
     for (int k = threadIdx.x; k < na; k += blockDim.x) {
         const double z = -beta[active[k]] / w[k];
-        if (z > 0.0 && isfinite(z)) b2 = mmin(b2, MinPos{z, k});
+        if (z > zmin && isfinite(z)) b2 = mmin(b2, MinPos{z, k});
     }
     for (int o = 16; o > 0; o >>= 1) {
         MinPos t1{__shfl_down_sync(0xffffffffu, b1.v, o), __shfl_down_sync(0xffffffffu, b1.i, o)};
@@ -153,6 +154,29 @@ __global__ void k_lars_steps(const double* c, const double* a, const int* flag, 
         for (int q = 1; q < (int)(blockDim.x >> 5); ++q) { r1 = mmin(r1, s1[q]); r2 = mmin(r2, s2[q]); }
         out[0] = r1;
         out[1] = r2;
+    }
+}
+
+// DLARS objective 0.5 ||b - A x||^2 / n + lambda ||x||_1 from the normal equations:
+// ||b - A x||^2 = b^T b - x^T h - x^T c with c = h - G x (single block; out[0])
+__global__ void k_lars_objective(const double* x, const double* h, const double* c, int n, double btb,
+                                 double nsamples, double lambda, double* out) {
+    __shared__ double s1[32], s2[32];
+    double q = 0.0, l1 = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        q += x[j] * (h[j] + c[j]);
+        l1 += fabs(x[j]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        q += __shfl_down_sync(0xffffffffu, q, o);
+        l1 += __shfl_down_sync(0xffffffffu, l1, o);
+    }
+    if ((threadIdx.x & 31) == 0) { s1[threadIdx.x >> 5] = q; s2[threadIdx.x >> 5] = l1; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double Q = 0.0, L1 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { Q += s1[w]; L1 += s2[w]; }
+        out[0] = 0.5 * (btb - Q) / nsamples + lambda * L1;
     }
 }
 
@@ -206,7 +230,15 @@ static void cbl(cublasStatus_t s, const char* w) {
 // Returns [steps, active variables, final C / n]; x (device, n values) receives
 // the coefficients.  G: full symmetric FP64 (row-major), h: X^T y (device).
 void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
-                double* info, void* cublas, cudaStream_t st) {
+                double* info, void* cublas, cudaStream_t st, int mode, double btb) {
+    // mode 0: scikit-learn LassoLars (exact landing on C/n = alpha).  mode 1 / 2: the
+    // reference's DLARS `lars` / `lasso` (contrib/dlars/src/dlars.C): the variable
+    // named by the last step enters, C = max |c| over every variable, lasso
+    // crossings above 1e-12, no re-entry bar, and the walk stops at the first
+    // vertex whose objective 0.5 ||b - A x||^2 / n + alpha ||x||_1 exceeds the
+    // previous vertex's by more than 1e-10, returning that vertex (the driver,
+    // :376-420).
+    const bool dl = mode != 0, dlasso = mode == 2;
     cublasHandle_t hb = (cublasHandle_t)cublas;
     cbl(cublasSetStream(hb, st), "setStream");
     const int kmax = (int)std::min<int64_t>(n, std::max<int64_t>(nsamples, 1));
@@ -236,7 +268,8 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
         const double target = (double)nsamples * alpha;
         double C = 0.0;
         bool drop = false;
-        int dropped = -1, steps = 0;
+        int dropped = -1, steps = 0, next_add = -1;
+        double last_obj = 1.0e50, obj = 0.0;
         // C = max |h|
         cgd::k_lars_argmax<<<1, cgd::LARS_THREADS, 0, st>>>(c, flag, n, am);
         cgd::ArgMax hm{};
@@ -244,11 +277,27 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
         ckl(cudaStreamSynchronize(st), "sync");
         C = hm.v;
         const int tb = 256;
-        while (steps < max_iter && C > target) {
-            if (!drop) {
-                cgd::k_lars_argmax<<<1, cgd::LARS_THREADS, 0, st>>>(c, flag, n, am);
-                ckl(cudaMemcpyAsync(&hm, am, sizeof(hm), cudaMemcpyDeviceToHost, st), "argmax");
+        while (steps < max_iter && (dl || C > target)) {
+            if (dl) {
+                if ((int)active.size() >= n) break;   // no more iterations possible
+                cgd::k_lars_objective<<<1, cgd::LARS_THREADS, 0, st>>>(x, h, c, n, btb, (double)nsamples, alpha,
+                                                                      scal + 2);
+                cgd::k_lars_argmax<<<1, cgd::LARS_THREADS, 0, st>>>(c, flag, n, am, 1);   // C over every variable
+                ckl(cudaMemcpyAsync(&obj, scal + 2, sizeof(double), cudaMemcpyDeviceToHost, st), "objective");
+                ckl(cudaMemcpyAsync(&hm, am, sizeof(hm), cudaMemcpyDeviceToHost, st), "C");
                 ckl(cudaStreamSynchronize(st), "sync");
+                if (obj > last_obj + 1.0e-10) break;   // this vertex is the answer
+                last_obj = obj;
+                C = hm.v;
+            }
+            if (!drop) {
+                if (dl && next_add >= 0) {
+                    hm.i = next_add;
+                } else {
+                    cgd::k_lars_argmax<<<1, cgd::LARS_THREADS, 0, st>>>(c, flag, n, am);
+                    ckl(cudaMemcpyAsync(&hm, am, sizeof(hm), cudaMemcpyDeviceToHost, st), "argmax");
+                    ckl(cudaStreamSynchronize(st), "sync");
+                }
                 if (hm.i < 0) break;
                 const int j = hm.i;
                 const int na = (int)active.size();
@@ -272,6 +321,8 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
                     hflag[j] = 2;
                     ckl(cudaMemcpyAsync(flag + j, &two, sizeof(int), cudaMemcpyHostToDevice, st), "flag");
                     ckl(cudaStreamSynchronize(st), "sync");
+                    next_add = -1;
+                    if (dl) last_obj = 1.0e50;   // re-evaluate at the same vertex
                     continue;
                 }
                 cgd::k_lars_put_row<<<(na + 1 + tb - 1) / tb, tb, 0, st>>>(L, kmax, na, sv, d2);
@@ -279,7 +330,7 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
                 hflag[j] = 1;
                 ckl(cudaMemcpyAsync(flag + j, &one, sizeof(int), cudaMemcpyHostToDevice, st), "flag");
                 ckl(cudaMemcpyAsync(dact + na, &active.back(), sizeof(int), cudaMemcpyHostToDevice, st), "active");
-                C = std::max(C, hm.v);
+                if (!dl) C = std::max(C, hm.v);
                 ckl(cudaStreamSynchronize(st), "sync");
             }
             drop = false;
@@ -294,27 +345,29 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
             double AA = 0.0;
             ckl(cudaMemcpyAsync(&AA, scal + 1, sizeof(double), cudaMemcpyDeviceToHost, st), "AA");
             ckl(cudaStreamSynchronize(st), "sync");
-            cgd::k_lars_steps<<<1, cgd::LARS_THREADS, 0, st>>>(c, a, flag, n, C, AA, dropped, x, dact, w, na, mp);
+            cgd::k_lars_steps<<<1, cgd::LARS_THREADS, 0, st>>>(c, a, flag, n, C, AA, dl ? -1 : dropped, x, dact, w, na,
+                                                               mp, dl ? 1.0e-12 : 0.0);
             cgd::MinPos hp[2];
             ckl(cudaMemcpyAsync(hp, mp, sizeof(hp), cudaMemcpyDeviceToHost, st), "steps");
             ckl(cudaStreamSynchronize(st), "sync");
             dropped = -1;
-            double gamma = std::min(C / AA, hp[0].v);
+            double gamma = dl ? (na < n ? (hp[0].i >= 0 ? hp[0].v : 1.0e20) : C / AA) : std::min(C / AA, hp[0].v);
+            next_add = dl ? hp[0].i : -1;
             int kz = -1;
-            if (hp[1].i >= 0 && hp[1].v < gamma) {
+            if ((!dl || dlasso) && hp[1].i >= 0 && hp[1].v < gamma) {
                 gamma = hp[1].v;
                 kz = hp[1].i;
                 drop = true;
             }
             bool last = false;
-            if (C - gamma * AA < target) {   // land exactly on C / n = alpha
+            if (!dl && C - gamma * AA < target) {   // land exactly on C / n = alpha
                 gamma = (C - target) / AA;
                 drop = false;
                 kz = -1;
                 last = true;
             }
             cgd::k_lars_update<<<(std::max(n, na) + tb - 1) / tb, tb, 0, st>>>(x, c, a, dact, w, na, n, gamma);
-            C -= gamma * AA;
+            if (!dl) C -= gamma * AA;
             ++steps;
             if (last) break;
             if (drop) {
@@ -335,7 +388,7 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
             ckl(cudaGetLastError(), "lars step");
         }
         ckl(cudaStreamSynchronize(st), "sync");
-        if (info) { info[0] = steps; info[1] = (double)active.size(); info[2] = C / (double)nsamples; }
+        if (info) { info[0] = steps; info[1] = (double)active.size(); info[2] = dl ? last_obj : C / (double)nsamples; }
     } catch (...) {
         for (void* p : mem) cudaFreeAsync(p, st);
         cudaStreamSynchronize(st);

@@ -665,10 +665,10 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
 }
 
 void Session::lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter,
-                   double* x, double* info) {
+                   double* x, double* info, int mode, double btb) {
     CK(cudaSetDevice(device_));
     try {
-        lars_lasso(G, h, ncols, nsamples, alpha, max_iter, x, info, cublas_, stream_);
+        lars_lasso(G, h, ncols, nsamples, alpha, max_iter, x, info, cublas_, stream_, mode, btb);
     } catch (const std::runtime_error& e) {
         throw Error(3, e.what());
     }

@@ -200,7 +200,7 @@ class Session {
     int gram_ctas_per_sm() const { return gram_ctas_per_sm_; }
     // LARS-lasso on the normal equations (lars.cu).
     void lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter, double* x,
-              double* info);
+              double* info, int mode = 0, double btb = 0.0);
 
     // MD force (md.h / md_host.cu).  md_setup stores the coefficients x (one per A
     // column): offsets adds the per-atom-type energy offsets of an energy fit.

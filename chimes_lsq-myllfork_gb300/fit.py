@@ -2,7 +2,7 @@
 followed by `python chimes_lsq.py --algorithm ...` (src/chimes_lsq.C:108-424,
 src/chimes_lsq.py:1-675).
 
-    python chimes_lsq-myllfork_gb300/fit.py fm_setup.in [--algorithm ridge|lassolars]
+    python chimes_lsq-myllfork_gb300/fit.py fm_setup.in [--algorithm ridge|lassolars|dlars|dlasso]
         [--alpha A] [--precision fp64|mixed] [--block-frames K] [--refine N] [--write-a] [--out DIR]
 
 Writes params.header, ff_groups.map, params.txt and force.txt (and, with
@@ -16,8 +16,11 @@ into the normal equations G = A^T A, h = A^T b:
 ridge solves (A^T A + alpha I) x = A^T b (scikit-learn Ridge(alpha,
 fit_intercept=False), the reference's --algorithm ridge); lassolars follows the
 LARS-lasso path to (1/2n)||b - A x||^2 + alpha ||x||_1 (the reference's
---algorithm lassolars).  The reference's default truncated SVD is not offered:
-ridge with a small alpha replaces it.
+--algorithm lassolars); dlars / dlasso follow the reference's DLARS solver
+(contrib/dlars, --algorithm dlars / dlasso without --normalize): LARS or LASSO
+steps stopped at the first vertex where the objective with lambda = alpha rises.
+The reference's default truncated SVD is not offered: ridge with a small alpha
+replaces it.
 """
 import argparse
 import datetime
@@ -33,7 +36,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("fm_setup")
-    ap.add_argument("--algorithm", default="ridge", choices=["ridge", "lassolars"])
+    ap.add_argument("--algorithm", default="ridge", choices=["ridge", "lassolars", "dlars", "dlasso"])
     ap.add_argument("--alpha", type=float, default=1.0e-3)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--block-frames", type=int, default=64)
@@ -101,9 +104,16 @@ def main(argv=None):
         lines += ["! ridge regression used", "! Ridge alpha = %11.4e" % args.alpha]
         if mixed:
             lines += [f"! split-BF16 tensor-core Gram, FP64 Cholesky, {iters} FP64-product CG iterations"]
-    else:
+    elif args.algorithm == "lassolars":
         sess.lars(G.data_ptr(), h.data_ptr(), C, nrows, args.alpha, x.data_ptr())
         lines += ["! LARS implementation of LASSO used", "! LASSO alpha = %11.4e" % args.alpha]
+    else:   # fit_dlars src/chimes_lsq.py:714-790
+        lasso = args.algorithm == "dlasso"
+        btb = float(b_all @ b_all)
+        sess.dlars(G.data_ptr(), h.data_ptr(), C, nrows, btb, args.alpha, lasso, x.data_ptr())
+        lines += ["! DLARS code for %s used" % ("LASSO" if lasso else "LARS"), "! DLARS alpha = %10.4e" % args.alpha,
+                  "! DLARS run: cg_dlars (device, normal equations) --lambda=%s --algorithm=%s --normalize=n"
+                  % (args.alpha, "lasso" if lasso else "lars"), ""]
     torch.cuda.synchronize()
     xh = x.cpu().numpy()
     # predicted labels y = A x (force.txt) and the fit statistics

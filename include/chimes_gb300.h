@@ -184,6 +184,17 @@ int cg_solve(cg_session* s, const double* G, const double* h, int ncols, double 
 int cg_lars(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter,
             double* x, double* info);
 
+/* The reference's DLARS solver (contrib/dlars/src/dlars.C; chimes_lsq.py
+ * --algorithm dlars | dlasso, src/chimes_lsq.py:714-790, without --normalize) on the
+ * normal equations: LARS (lasso = 0) or LASSO (lasso = 1) steps from x = 0, the
+ * variable named by each step entering next, stopping at the first path vertex
+ * whose objective 0.5 ||b - A x||^2 / nsamples + lambda ||x||_1 exceeds the
+ * previous vertex's by more than 1e-10 and returning that vertex, as the
+ * reference's driver does.  btb = b^T b.  info (may be NULL): iterations, active
+ * variables, objective of the previous vertex. */
+int cg_dlars(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double btb, double lambda,
+             int lasso, int max_iter, double* x, double* info);
+
 /* Work counters of the last assembly: accepted 2-body pairs, triplets, quadruplets,
  * and (cluster, allowed-power) evaluations of the 3- and 4-body terms. */
 int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads,

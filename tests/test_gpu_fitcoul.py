@@ -8,6 +8,9 @@
   augmented system lands 9.7e-9 from the published answer, LAPACK's Cholesky 1.4e-10,
   the device Cholesky 9.5e-8: tolerance 2e-7 of max|x|.  LARS: the same support and 1e-6 of max|x| (the
   numpy LARS oracle lands 8.6e-8 from it).
+* device DLARS (lars and lasso) against the reference's published DLARS outputs
+  (same support, objective 1e-7, coefficients 1e-4 of max|x|: the path is
+  ill-conditioned and its vertices move with the arithmetic route).
 * the fit driver on the FITCOUL fixture (charge columns assembled on the device,
   constraint rows appended) on the reference's own A: the ridge objective within
   1e-12 of the QR optimum; the coefficients within 1e-5 of LAPACK's Cholesky (the
@@ -70,6 +73,34 @@ def test_lsq2_lassolars_matches_reference_output(cg, lsq2):
     print(f"\nlsq2 lassolars: device vs the reference's params.lassolars.1.0e-04.txt {err:.2e}", flush=True)
     assert np.array_equal(xs != 0, ref != 0)
     assert err <= 1e-6
+
+
+@pytest.mark.parametrize("algorithm", ["dlars", "dlasso"])
+def test_lsq2_dlars_matches_reference_output(cg, lsq2, algorithm):
+    """Device DLARS (cg_dlars) on lsq2's normal equations against the reference's
+    params.dlars / params.dlasso.1.0e-04.txt: the same support, objective within 1e-7,
+    RMS within 1e-6, coefficients within 1e-4 of max|x| (the CPU restatement lands
+    1.0e-6 / 2.7e-5 from the published coefficients; see test_cpu_lars.py)."""
+    torch = pytest.importorskip("torch")
+    G, h, nrows, d = lsq2
+    n = G.shape[0]
+    btb = float(d["btb"])
+    sess = _session(cg)
+    dG, dh = torch.from_numpy(G).cuda(), torch.from_numpy(h).cuda()
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    it, nact, _ = sess.dlars(dG.data_ptr(), dh.data_ptr(), n, nrows, btb, 1e-4, algorithm == "dlasso", x.data_ptr())
+    torch.cuda.synchronize()
+    xs = x.cpu().numpy()
+    ref = d[f"x_{algorithm}_1e-4"]
+    sq = lambda v: btb - 2 * v @ h + v @ G @ v
+    obj = lambda v: 0.5 * sq(v) / nrows + 1e-4 * np.abs(v).sum()
+    err = np.abs(xs - ref).max() / np.abs(ref).max()
+    print(f"\nlsq2 {algorithm}: {it} iterations; device vs the reference's output {err:.2e}, objective "
+          f"{abs(obj(xs) - obj(ref)) / obj(ref):.2e}", flush=True)
+    assert np.array_equal(xs != 0, ref != 0)
+    assert abs(obj(xs) - obj(ref)) <= 1e-7 * obj(ref)
+    assert abs(np.sqrt(sq(xs) / nrows) - np.sqrt(sq(ref) / nrows)) <= 1e-6 * np.sqrt(sq(ref) / nrows)
+    assert err <= 1e-4
 
 
 def test_fitcoul_fit_driver_matches_fp64_ridge(cg, tmp_path):
