@@ -361,10 +361,13 @@ int cg_lars(cg_session* s, const double* G, const double* h, int ncols, int64_t 
 }
 
 int cg_dlars(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double btb, double lambda,
-             int lasso, int max_iter, double* x, double* info) {
+             int lasso, const double* colsum, double bsum, int max_iter, double* x, double* info) {
     return guarded([&] {
         need(s && G && h && x && ncols > 0 && nsamples > 0 && lambda >= 0.0 && max_iter > 0, "dlars arguments");
-        s->s->lars(G, h, ncols, nsamples, lambda, max_iter, x, info, lasso ? 2 : 1, btb);
+        if (colsum)
+            s->s->dlars_normalized(G, h, colsum, bsum, ncols, nsamples, btb, lambda, lasso, max_iter, x, info);
+        else
+            s->s->lars(G, h, ncols, nsamples, lambda, max_iter, x, info, lasso ? 2 : 1, btb);
     });
 }
 

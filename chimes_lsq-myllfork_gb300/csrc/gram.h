@@ -39,5 +39,10 @@ void residual(const double* A, int64_t lda, int64_t nrows, int ncols, const doub
 // `lasso` (needs btb = b^T b; info[2] is then the objective of the last vertex).
 void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
                 double* info, void* cublas, cudaStream_t st, int mode = 0, double btb = 0.0);
+// DLARS with --normalize: columns centred and scaled, b centred (colsum = A^T 1 on
+// the device, bsum = sum b), coefficients returned in unscaled units.
+void dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int n, int64_t nsamples,
+                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, void* cublas,
+                      cudaStream_t st);
 
 }  // namespace cg

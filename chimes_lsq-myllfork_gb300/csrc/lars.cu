@@ -180,6 +180,33 @@ __global__ void k_lars_objective(const double* x, const double* h, const double*
     }
 }
 
+// DLARS --normalize on the normal equations (Matrix::normalize, Vector::normalize
+// contrib/dlars/src/Matrix.h:614-660, Vector.h:140-150): columns centred on their
+// means mu = colsum / n and scaled to unit norm sigma_j = sqrt(G_jj - n mu_j^2), b
+// centred on its mean ybar:  Gc = (G - n mu mu^T) / (sigma sigma^T),
+// hc = (h - ybar colsum) / sigma.
+__global__ void k_dlars_sigma(const double* G, const double* colsum, int n, double nsamples, double* sigma, int* bad) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double mu = colsum[j] / nsamples;
+    const double s2 = G[(size_t)j * n + j] - nsamples * mu * mu;
+    sigma[j] = s2 > 0.0 ? sqrt(s2) : 0.0;
+    if (!(s2 > 0.0)) atomicExch(bad, 1);
+}
+__global__ void k_dlars_center(const double* G, const double* h, const double* colsum, const double* sigma, int n,
+                               double nsamples, double ybar, double* Gc, double* hc) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    const int i = (int)(idx / n), j = (int)(idx % n);
+    const double mi = colsum[i] / nsamples, mj = colsum[j] / nsamples;
+    Gc[idx] = (G[idx] - nsamples * mi * mj) / (sigma[i] * sigma[j]);
+    if (j == 0) hc[i] = (h[i] - ybar * colsum[i]) / sigma[i];
+}
+__global__ void k_dlars_unscale(double* x, const double* sigma, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) x[j] /= sigma[j];   // DLARS::print_unscaled (dlars.C:2073-2097)
+}
+
 // beta[active] += gamma w; c -= gamma a
 __global__ void k_lars_update(double* beta, double* c, const double* a, const int* active, const double* w, int na,
                               int n, double gamma) {
@@ -395,6 +422,39 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
         throw;
     }
     for (void* p : mem) cudaFreeAsync(p, st);
+}
+
+void dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int n, int64_t nsamples,
+                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, void* cublas,
+                      cudaStream_t st) {
+    double *Gc = nullptr, *hc = nullptr, *sigma = nullptr;
+    int* bad = nullptr;
+    ckl(cudaMallocAsync((void**)&Gc, sizeof(double) * (size_t)n * n, st), "normalised G");
+    ckl(cudaMallocAsync((void**)&hc, sizeof(double) * n, st), "normalised h");
+    ckl(cudaMallocAsync((void**)&sigma, sizeof(double) * n, st), "column scales");
+    ckl(cudaMallocAsync((void**)&bad, sizeof(int), st), "flag");
+    auto release = [&]() {
+        cudaFreeAsync(Gc, st); cudaFreeAsync(hc, st); cudaFreeAsync(sigma, st); cudaFreeAsync(bad, st);
+    };
+    try {
+        const double N = (double)nsamples, ybar = bsum / N;
+        ckl(cudaMemsetAsync(bad, 0, sizeof(int), st), "flag");
+        cgd::k_dlars_sigma<<<(n + 255) / 256, 256, 0, st>>>(G, colsum, n, N, sigma, bad);
+        int hbad = 0;
+        ckl(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st), "flag");
+        ckl(cudaStreamSynchronize(st), "sync");
+        if (hbad) throw std::runtime_error("a column of A is constant: its normalisation scale is 0");
+        const int64_t nn = (int64_t)n * n;
+        cgd::k_dlars_center<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(G, h, colsum, sigma, n, N, ybar, Gc, hc);
+        ckl(cudaGetLastError(), "normalise");
+        lars_lasso(Gc, hc, n, nsamples, lambda, max_iter, x, info, cublas, st, lasso ? 2 : 1, btb - N * ybar * ybar);
+        cgd::k_dlars_unscale<<<(n + 255) / 256, 256, 0, st>>>(x, sigma, n);
+        ckl(cudaGetLastError(), "unscale");
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
 }
 
 }  // namespace cg

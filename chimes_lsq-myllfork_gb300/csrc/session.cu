@@ -674,6 +674,18 @@ void Session::lars(const double* G, const double* h, int ncols, int64_t nsamples
     }
 }
 
+void Session::dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int ncols,
+                               int64_t nsamples, double btb, double lambda, int lasso, int max_iter, double* x,
+                               double* info) {
+    CK(cudaSetDevice(device_));
+    try {
+        cg::dlars_normalized(G, h, colsum, bsum, ncols, nsamples, btb, lambda, lasso, max_iter, x, info, cublas_,
+                             stream_);
+    } catch (const std::runtime_error& e) {
+        throw Error(2, e.what());
+    }
+}
+
 void Session::gram_finish(double* G, int ncols) {
     CK(cudaSetDevice(device_));
     gram_symmetrize(G, ncols, true, stream_);

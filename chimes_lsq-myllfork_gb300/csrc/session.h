@@ -201,6 +201,9 @@ class Session {
     // LARS-lasso on the normal equations (lars.cu).
     void lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter, double* x,
               double* info, int mode = 0, double btb = 0.0);
+    // DLARS with column normalisation (colsum = A^T 1 on the device, bsum = sum b).
+    void dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int ncols,
+                          int64_t nsamples, double btb, double lambda, int lasso, int max_iter, double* x, double* info);
 
     // MD force (md.h / md_host.cu).  md_setup stores the coefficients x (one per A
     // column): offsets adds the per-atom-type energy offsets of an energy fit.

@@ -17,8 +17,9 @@ ridge solves (A^T A + alpha I) x = A^T b (scikit-learn Ridge(alpha,
 fit_intercept=False), the reference's --algorithm ridge); lassolars follows the
 LARS-lasso path to (1/2n)||b - A x||^2 + alpha ||x||_1 (the reference's
 --algorithm lassolars); dlars / dlasso follow the reference's DLARS solver
-(contrib/dlars, --algorithm dlars / dlasso without --normalize): LARS or LASSO
-steps stopped at the first vertex where the objective with lambda = alpha rises.
+(contrib/dlars, --algorithm dlars / dlasso, --normalize as its --normalize=y):
+LARS or LASSO steps stopped at the first vertex where the objective with
+lambda = alpha rises.
 The reference's default truncated SVD is not offered: ridge with a small alpha
 replaces it.
 """
@@ -41,6 +42,8 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--block-frames", type=int, default=64)
     ap.add_argument("--refine", type=int, default=50, help="CG iterations of the mixed ridge solve")
+    ap.add_argument("--normalize", action="store_true",
+                    help="dlars / dlasso: centre and scale the columns and centre b (DLARS --normalize=y)")
     ap.add_argument("--write-a", action="store_true", help="also write A.txt, b.txt, ... (slow for large A)")
     ap.add_argument("--out", default=None, help="output directory (default: the fm_setup.in directory)")
     ap.add_argument("--device", type=int, default=0)
@@ -70,6 +73,7 @@ def main(argv=None):
     keep64 = fits and (not mixed or (args.algorithm == "ridge" and args.refine > 0))
     A64_all = torch.empty((nrows, C), dtype=torch.float64, device="cuda") if keep64 else None
     b_all = torch.empty(nrows, dtype=torch.float64, device="cuda")
+    colsum = torch.zeros(C, dtype=torch.float64, device="cuda")   # A^T 1 (DLARS --normalize)
     r0 = 0
     for blk in blocks:
         dfr = sess.upload(blk)
@@ -79,18 +83,21 @@ def main(argv=None):
             A32 = torch.empty((n, C), dtype=torch.float32, device="cuda")
             sess.assemble_device(dfr, cg.CG_FP32, A32.data_ptr(), C)
             sess.gram(1, A32.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 1, G.data_ptr(), h.data_ptr())
+            colsum += A32.sum(0, dtype=torch.float64)
             del A32
         if keep64 or not mixed:
             dst = A64_all[r0:r0 + n] if keep64 else torch.empty((n, C), dtype=torch.float64, device="cuda")
             sess.assemble_device(dfr, cg.CG_FP64, dst.data_ptr(), C)
             if not mixed:
                 sess.gram(0, dst.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr())
+                colsum += dst.sum(0)
             del dst
         r0 += n
     if Acon.shape[0]:   # the constraint rows join the normal equations like any row block
         dAc = torch.from_numpy(Acon).cuda()
         b_all[r0:] = torch.from_numpy(bcon)
         sess.gram(0, dAc.data_ptr(), C, Acon.shape[0], C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr())
+        colsum += dAc.sum(0)
         if keep64:
             A64_all[r0:] = dAc
     sess.gram_finish(G.data_ptr(), C)
@@ -110,10 +117,12 @@ def main(argv=None):
     else:   # fit_dlars src/chimes_lsq.py:714-790
         lasso = args.algorithm == "dlasso"
         btb = float(b_all @ b_all)
-        sess.dlars(G.data_ptr(), h.data_ptr(), C, nrows, btb, args.alpha, lasso, x.data_ptr())
+        bsum = float(b_all.sum())
+        sess.dlars(G.data_ptr(), h.data_ptr(), C, nrows, btb, args.alpha, lasso, x.data_ptr(),
+                   colsum_ptr=colsum.data_ptr() if args.normalize else 0, bsum=bsum)
         lines += ["! DLARS code for %s used" % ("LASSO" if lasso else "LARS"), "! DLARS alpha = %10.4e" % args.alpha,
-                  "! DLARS run: cg_dlars (device, normal equations) --lambda=%s --algorithm=%s --normalize=n"
-                  % (args.alpha, "lasso" if lasso else "lars"), ""]
+                  "! DLARS run: cg_dlars (device, normal equations) --lambda=%s --algorithm=%s --normalize=%s"
+                  % (args.alpha, "lasso" if lasso else "lars", "y" if args.normalize else "n"), ""]
     torch.cuda.synchronize()
     xh = x.cpu().numpy()
     # predicted labels y = A x (force.txt) and the fit statistics
@@ -130,6 +139,8 @@ def main(argv=None):
         ys.append(Acon @ xh)
         y = np.concatenate(ys)
     b = b_all.cpu().numpy()
+    if args.normalize and args.algorithm in ("dlars", "dlasso"):   # print_unshifted_mu: the centring comes back
+        y = y - float((colsum @ x).item()) / nrows + float(b.sum()) / nrows
     Z = float(((y - b) ** 2).sum())
     nvars = C if args.algorithm == "ridge" else int(np.count_nonzero(xh))
     bic = nrows * math.log(Z / nrows) + nvars * math.log(nrows)

@@ -185,15 +185,18 @@ int cg_lars(cg_session* s, const double* G, const double* h, int ncols, int64_t 
             double* x, double* info);
 
 /* The reference's DLARS solver (contrib/dlars/src/dlars.C; chimes_lsq.py
- * --algorithm dlars | dlasso, src/chimes_lsq.py:714-790, without --normalize) on the
- * normal equations: LARS (lasso = 0) or LASSO (lasso = 1) steps from x = 0, the
- * variable named by each step entering next, stopping at the first path vertex
- * whose objective 0.5 ||b - A x||^2 / nsamples + lambda ||x||_1 exceeds the
- * previous vertex's by more than 1e-10 and returning that vertex, as the
- * reference's driver does.  btb = b^T b.  info (may be NULL): iterations, active
- * variables, objective of the previous vertex. */
+ * --algorithm dlars | dlasso, src/chimes_lsq.py:714-790) on the normal equations:
+ * LARS (lasso = 0) or LASSO (lasso = 1) steps from x = 0, the variable named by
+ * each step entering next, stopping at the first path vertex whose objective
+ * 0.5 ||b - A x||^2 / nsamples + lambda ||x||_1 exceeds the previous vertex's by
+ * more than 1e-10 and returning that vertex, as the reference's driver does.
+ * btb = b^T b.  colsum (device, ncols; NULL = no normalisation) = A^T 1 and bsum
+ * = sum of b select --normalize=y: columns centred and scaled to unit norm, b
+ * centred, coefficients returned unscaled (the fit's predictions are then
+ * A x - (colsum / nsamples) . x + bsum / nsamples).  info (may be NULL):
+ * iterations, active variables, objective of the previous vertex. */
 int cg_dlars(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double btb, double lambda,
-             int lasso, int max_iter, double* x, double* info);
+             int lasso, const double* colsum, double bsum, int max_iter, double* x, double* info);
 
 /* Work counters of the last assembly: accepted 2-body pairs, triplets, quadruplets,
  * and (cluster, allowed-power) evaluations of the 3- and 4-body terms. */

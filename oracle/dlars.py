@@ -100,3 +100,20 @@ def dlars(G, h, btb, n, lam, lasso, max_iter=10000000):
         last_beta = beta.copy()
         last_obj = obj
     return last_beta, it, stop
+
+
+def dlars_normalized(G, h, colsum, bsum, btb, n, lam, lasso, max_iter=10000000):
+    """DLARS with --normalize=y (Matrix::normalize / Vector::normalize,
+    contrib/dlars/src/Matrix.h:614-660, Vector.h:140-150; print_unscaled
+    dlars.C:2073-2097): columns centred and scaled to unit norm, b centred;
+    returns the unscaled coefficients (beta / scale), iterations, stop reason."""
+    G = np.asarray(G, dtype=np.float64)
+    mu = np.asarray(colsum, dtype=np.float64) / n
+    ybar = bsum / n
+    sig = np.sqrt(np.diag(G) - n * mu * mu)
+    if np.any(~(sig > 0.0)):
+        raise ValueError("a column of A is constant: its normalisation scale is 0")
+    Gc = (G - n * np.outer(mu, mu)) / np.outer(sig, sig)
+    hc = (np.asarray(h) - ybar * np.asarray(colsum)) / sig
+    beta, it, stop = dlars(Gc, hc, btb - n * ybar * ybar, n, lam, lasso, max_iter)
+    return beta / sig, it, stop

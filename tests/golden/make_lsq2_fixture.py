@@ -6,8 +6,9 @@ suite uses for its solvers.  This script runs the reference's chimes_lsq
 (oracle/_ref) on it, forms G = A^T A (upper triangle), h = A^T b and b^T b, and
 reads the coefficients of the reference's committed outputs
 params.ridge.1.0e-03.txt, params.lassolars.1.0e-04.txt, params.dlars.1.0e-04.txt
-and params.dlasso.1.0e-04.txt (chimes_lsq.py --algorithm ridge / lassolars /
-dlars / dlasso) with this package's params.txt reader.
+params.dlasso.1.0e-04.txt and params.dlasso.norm.txt (chimes_lsq.py --algorithm
+ridge / lassolars / dlars / dlasso, the last with --normalize) with this
+package's params.txt reader; A^T 1 and the sum of b serve the normalisation.
 
 Run where the reference sources are present:
     sh oracle/build_ref.sh && python tests/golden/make_lsq2_fixture.py
@@ -43,10 +44,11 @@ def main():
     iu = np.triu_indices(G.shape[0])
     gold = {}
     for key, name in (("x_ridge_1e-3", "params.ridge.1.0e-03.txt"), ("x_lassolars_1e-4", "params.lassolars.1.0e-04.txt"),
-                      ("x_dlars_1e-4", "params.dlars.1.0e-04.txt"), ("x_dlasso_1e-4", "params.dlasso.1.0e-04.txt")):
+                      ("x_dlars_1e-4", "params.dlars.1.0e-04.txt"), ("x_dlasso_1e-4", "params.dlasso.1.0e-04.txt"),
+                      ("x_dlasso_norm_1e-4", "params.dlasso.norm.txt")):
         gold[key] = m.params_read(open(os.path.join(CASE, "correct_output", name)).read())
     np.savez_compressed(os.path.join(out, "normal.npz"), G_upper=G[iu], h=A.T @ b, btb=float(b @ b),
-                        nrows=A.shape[0], ncols=A.shape[1], **gold)
+                        colsum=A.sum(axis=0), bsum=float(b.sum()), nrows=A.shape[0], ncols=A.shape[1], **gold)
     print("lsq2", A.shape, {k: float(np.abs(v).max()) for k, v in gold.items()})
 
 

@@ -86,3 +86,21 @@ def test_oracle_dlars_matches_reference_lsq2_output(algorithm):
     assert abs(obj(x) - obj(ref)) <= 1e-7 * obj(ref)
     assert abs(np.sqrt(sq(x) / N) - np.sqrt(sq(ref) / N)) <= 1e-6 * np.sqrt(sq(ref) / N)
     assert np.abs(x - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_oracle_dlars_normalized_matches_reference_lsq2_output():
+    """DLARS --normalize=y (columns centred and scaled, b centred) on lsq2 against the
+    reference's params.dlasso.norm.txt: well conditioned after the scaling, the
+    coefficients agree to 1e-9 of max|x| (5.7e-12 measured)."""
+    import dlars
+    d = np.load(os.path.join(GOLDEN, "lsq2", "normal.npz"))
+    n = int(d["ncols"])
+    G = np.zeros((n, n))
+    G[np.triu_indices(n)] = d["G_upper"]
+    G = G + np.triu(G, 1).T
+    x, it, stop = dlars.dlars_normalized(G, d["h"], d["colsum"], float(d["bsum"]), float(d["btb"]), int(d["nrows"]),
+                                         1e-4, True)
+    ref = d["x_dlasso_norm_1e-4"]
+    assert stop == "objective increased"
+    assert np.array_equal(x != 0, ref != 0)
+    assert np.abs(x - ref).max() <= 1e-9 * np.abs(ref).max()

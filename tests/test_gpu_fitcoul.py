@@ -103,6 +103,28 @@ def test_lsq2_dlars_matches_reference_output(cg, lsq2, algorithm):
     assert err <= 1e-4
 
 
+def test_lsq2_dlasso_normalized_matches_reference_output(cg, lsq2):
+    """Device DLARS --normalize=y (columns centred and scaled on the device) against
+    the reference's params.dlasso.norm.txt: same support, 1e-8 of max|x| (the
+    scaled problem is well conditioned; the CPU restatement lands 5.7e-12 away)."""
+    torch = pytest.importorskip("torch")
+    G, h, nrows, d = lsq2
+    n = G.shape[0]
+    sess = _session(cg)
+    dG, dh = torch.from_numpy(G).cuda(), torch.from_numpy(h).cuda()
+    dcs = torch.from_numpy(d["colsum"]).cuda()
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    it, _, _ = sess.dlars(dG.data_ptr(), dh.data_ptr(), n, nrows, float(d["btb"]), 1e-4, True, x.data_ptr(),
+                          colsum_ptr=dcs.data_ptr(), bsum=float(d["bsum"]))
+    torch.cuda.synchronize()
+    xs = x.cpu().numpy()
+    ref = d["x_dlasso_norm_1e-4"]
+    err = np.abs(xs - ref).max() / np.abs(ref).max()
+    print(f"\nlsq2 dlasso --normalize: {it} iterations; device vs the reference's output {err:.2e}", flush=True)
+    assert np.array_equal(xs != 0, ref != 0)
+    assert err <= 1e-8
+
+
 def test_fitcoul_fit_driver_matches_fp64_ridge(cg, tmp_path):
     sl = pytest.importorskip("scipy.linalg")
     for f in ("fm_setup.in", "traj.xyzf"):
