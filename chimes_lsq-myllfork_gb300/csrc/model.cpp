@@ -122,15 +122,49 @@ static const char* trans_string(int t) {
 
 // ------------------------------------------------------------ control parse
 
-static void parse_controls(const Listing& L, Controls& c) {
+static void parse_controls(const Listing& L, Controls& c, const std::string& dir) {
     const size_t N = L.lines.size();
     for (size_t i = 0; i < N; ++i) {   // TRJFILE  src/input.C:290-430
         if (L.size(i) > 1 && L.at(i, 1) == "TRJFILE") {
             if (L.size(i + 1) == 1) {
                 c.infile.push_back(L.at(i + 1, 0));
                 c.force_flags.push_back(""); c.stress_flags.push_back(""); c.energy_flags.push_back("");
+            } else if (L.size(i + 1) == 2) {
+                // "MULTI <list>": <nfiles>, then per file <nframes> <file> [T] [F S E flags]
+                std::string lp = L.at(i + 1, 1);
+                if (!lp.empty() && lp[0] != '/') lp = dir + "/" + lp;
+                std::ifstream multi(lp);
+                if (!multi.is_open()) fail("Cannot open MULTI file: " + L.at(i + 1, 1));
+                std::string line;
+                std::vector<std::string> t;
+                std::getline(multi, line);
+                if (parse_space(line, t) != 1) fail("Expected to read <nfiles>, got: " + line);
+                const int nfiles = to_int(t[0]);
+                for (int j = 0; j < nfiles; ++j) {
+                    std::getline(multi, line);
+                    const int n = parse_space(line, t);
+                    if (n != 2 && n != 3 && n != 5 && n != 6)
+                        fail("Expected <nframes> <filename> [temperature] [F_flag S_flag E_flag], got: " + line);
+                    c.infile_frames.push_back(to_int(t[0]));
+                    c.infile.push_back(t[1]);
+                    if (n >= 5) {
+                        c.force_flags.push_back(t[n - 3] != "None" ? t[n - 3] : "");
+                        c.stress_flags.push_back(t[n - 2] != "None" ? t[n - 2] : "");
+                        c.energy_flags.push_back(t[n - 1] != "None" ? t[n - 1] : "");
+                    } else {
+                        c.force_flags.push_back(""); c.stress_flags.push_back(""); c.energy_flags.push_back("");
+                    }
+                }
+                for (int k = (int)c.infile_frames.size() - 1; k >= 0; --k)   // files with no frames are dropped
+                    if (c.infile_frames[k] < 1) {
+                        c.infile.erase(c.infile.begin() + k);
+                        c.infile_frames.erase(c.infile_frames.begin() + k);
+                        c.force_flags.erase(c.force_flags.begin() + k);
+                        c.stress_flags.erase(c.stress_flags.begin() + k);
+                        c.energy_flags.erase(c.energy_flags.begin() + k);
+                    }
             } else {
-                fail("only a single TRJFILE trajectory is supported by this build");
+                fail("TRJFILE expects one file name or MULTI <list>");
             }
             break;
         }
@@ -621,7 +655,7 @@ Model load_model(const std::string& path) {
     size_t slash = path.find_last_of('/');
     m.dir = slash == std::string::npos ? std::string(".") : path.substr(0, slash);
     Listing L = read_listing(path);
-    parse_controls(L, m.ctl);
+    parse_controls(L, m.ctl, m.dir);
     parse_topology(L, m);
     Controls& c = m.ctl;
     // RUN_SANITY_LSQ src/input.C:1306-1338
@@ -651,7 +685,7 @@ Model load_model(const std::string& path) {
     // JOB_CONTROL::LSQ_SETUP src/ClassDefs.C:2761-2785
     if ((c.fit_stress || c.fit_stress_all) && c.nstress == -1) c.nstress = c.nframes;
     if (c.fit_ener && c.nener == -1) c.nener = c.nframes;
-    if (c.infile.size() == 1) c.infile_frames.push_back(c.nframes);
+    if (c.infile.size() == 1 && c.infile_frames.empty()) c.infile_frames.push_back(c.nframes);
     return m;
 }
 
@@ -1139,11 +1173,23 @@ std::vector<Frame> read_xyzf(const Model& m, const std::string& path, int nframe
 }
 
 std::vector<Frame> read_frames(const Model& m) {
-    if (m.ctl.infile.empty()) throw Error(2, "no TRJFILE given");
-    std::string p = m.ctl.infile[0];
-    if (!p.empty() && p[0] != '/') p = m.dir + "/" + p;
+    // NFRAMES frames in file order (chimes_lsq.C:263-300: the next file opens when
+    // a file's INFILE_FRAMES are used up); one SYSTEM box carries across files
+    const Controls& c = m.ctl;
+    if (c.infile.empty()) throw Error(2, "no TRJFILE given");
     Box box;
-    return read_xyzf(m, p, m.ctl.nframes, 0, box);
+    std::vector<Frame> all;
+    int done = 0;
+    for (size_t k = 0; k < c.infile.size() && done < c.nframes; ++k) {
+        std::string p = c.infile[k];
+        if (!p.empty() && p[0] != '/') p = m.dir + "/" + p;
+        const int n = std::min(c.nframes - done, k < c.infile_frames.size() ? c.infile_frames[k] : c.nframes - done);
+        std::vector<Frame> part = read_xyzf(m, p, n, done, box);
+        for (Frame& f : part) { f.file = (int)k; all.push_back(std::move(f)); }
+        done += n;
+    }
+    if (done < c.nframes) throw Error(2, "the trajectory files hold fewer than NFRAMES frames");
+    return all;
 }
 
 RowLayout frame_rows(const Model& m, int fi, int natoms) {

@@ -167,6 +167,7 @@ struct Frame {
     double stress_diag[3] = {0, 0, 0};   // xx yy zz (GPa, as read)
     double stress_off[3] = {0, 0, 0};    // xy xz yz (GPa, as read)
     double energy = 0.0;
+    int file = 0;                     // index of the TRJFILE the frame came from (label flags)
 };
 
 // Read all NFRAMES frames of the model's trajectory file(s).

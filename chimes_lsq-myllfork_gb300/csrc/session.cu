@@ -175,6 +175,7 @@ FrameBatch slice_batch(const FrameBatch& fb, int first, int count) {
         o.energy_rows.push_back(fb.energy_rows[k]);
         o.box.push_back(fb.box[k]);
         o.small_self.push_back(fb.small_self[k]);
+        o.file.push_back(k < (int)fb.file.size() ? fb.file[k] : 0);
         o.atom_ofs.push_back(o.atom_ofs.back() + n);
         o.ghost_ofs.push_back(o.ghost_ofs.back() + nimg * n);
         const int64_t rows = fb.row_ofs[k + 1] - fb.row_ofs[k];
@@ -215,6 +216,7 @@ FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int firs
         fb.row_ofs.push_back(fb.row_ofs.back() + rl.total());
         small = frame_is_small(m, fr.box, small);
         fb.small_self.push_back(frame_is_small(m, fr.box, false) ? 1 : 0);
+        fb.file.push_back(fr.file);
         cgd::BoxDev bd;
         std::memset(&bd, 0, sizeof(bd));
         for (int q = 0; q < 9; ++q) { bd.h[q] = fr.box.hmat[q]; bd.inv[q] = fr.box.invr[q]; }

@@ -38,6 +38,7 @@ struct FrameBatch {
     std::vector<double> xyz;
     std::vector<double> b;        // labels in A row order (src/A_Matrix.C:294-553)
     std::vector<char> small_self; // each frame's own small-cell test (no carry-over)
+    std::vector<int> file;        // trajectory file of each frame (b-labeled.txt flags)
     int64_t nrows = 0, natoms_total = 0, nghosts = 0;
 };
 

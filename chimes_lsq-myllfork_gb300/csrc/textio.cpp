@@ -39,6 +39,10 @@ void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int6
     const bool do_ener = nener > 0;
     Out fa(dir + "/A.txt"), fbv(dir + "/b.txt"), fbl(dir + "/b-labeled.txt"), fna(dir + "/natoms.txt");
     int64_t row = 0;
+    auto flag = [&](const std::vector<std::string>& v, int f) -> const char* {   // INFILE_*_FLAGS[my_file]
+        const int k = f < (int)fb.file.size() ? fb.file[f] : 0;
+        return k < (int)v.size() ? v[k].c_str() : "";
+    };
     for (int f = 0; f < fb.nframes; ++f) {
         const int N = fb.natoms[f];
         const int64_t a0 = fb.atom_ofs[f];
@@ -61,7 +65,8 @@ void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int6
                 tail(false);
                 const double bv = fb.b[r0 + 3 * a + q];
                 fbv.num(bv); fbv.s("\n");
-                fbl.s(m.atom_types[fb.type[a0 + a]].c_str()); fbl.s(" "); fbl.lab(bv); fbl.s("\n");
+                fbl.s(flag(m.ctl.force_flags, f)); fbl.s(m.atom_types[fb.type[a0 + a]].c_str()); fbl.s(" ");
+                fbl.lab(bv); fbl.s("\n");
             }
         }
         const int srows = fb.stress_rows[f], erows = fb.energy_rows[f];
@@ -73,7 +78,7 @@ void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int6
             for (int c = 0; c < C; ++c) { fa.num(Ar[c]); fa.s(" "); }
             tail(false);
             fbv.num(fb.b[r]); fbv.s("\n");
-            fbl.s(srows == 3 ? l3[k] : l9[k]); fbl.lab(fb.b[r]); fbl.s("\n");
+            fbl.s(flag(m.ctl.stress_flags, f)); fbl.s(srows == 3 ? l3[k] : l9[k]); fbl.lab(fb.b[r]); fbl.s("\n");
         }
         for (int k = 0; k < erows; ++k, ++row) {
             const int64_t r = r0 + 3 * N + srows + k;
@@ -81,7 +86,7 @@ void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int6
             for (int c = 0; c < C; ++c) { fa.num(Ar[c]); fa.s(" "); }
             tail(true);
             fbv.num(fb.b[r]); fbv.s("\n");
-            fbl.s("+1 "); fbl.lab(fb.b[r]); fbl.s("\n");
+            fbl.s(flag(m.ctl.energy_flags, f)); fbl.s("+1 "); fbl.lab(fb.b[r]); fbl.s("\n");
         }
     }
     if (with_constraints && !m.charge_constraints.empty()) {   // A_MAT::PRINT_CONSTRAINTS src/A_Matrix.C:606-623

@@ -850,9 +850,9 @@ const char* oracle_last_error() { return g_err.c_str(); }
 int oracle_sizes(const char* fm_setup, const char* xyzf, int nframes, int64_t* nrows, int* ncols) {
     try {
         Model m = load_model(fm_setup);
-        std::string p = xyzf ? xyzf : m.dir + "/" + m.ctl.infile.at(0);
         Box box;
-        std::vector<Frame> fr = read_xyzf(m, p, nframes > 0 ? nframes : m.ctl.nframes, 0, box);
+        std::vector<Frame> fr = xyzf ? read_xyzf(m, xyzf, nframes > 0 ? nframes : m.ctl.nframes, 0, box)
+                                     : read_frames(m);
         int64_t r = 0;
         for (size_t f = 0; f < fr.size(); ++f) r += frame_rows(m, (int)f, fr[f].natoms).total();
         *nrows = r;
@@ -870,9 +870,9 @@ int oracle_assemble(const char* fm_setup, const char* xyzf, int nframes, int fir
                     double* A, int64_t lda, double* b) {
     try {
         Model m = load_model(fm_setup);
-        std::string p = xyzf ? xyzf : m.dir + "/" + m.ctl.infile.at(0);
         Box box;
-        std::vector<Frame> fr = read_xyzf(m, p, nframes > 0 ? nframes : m.ctl.nframes, 0, box);
+        std::vector<Frame> fr = xyzf ? read_xyzf(m, xyzf, nframes > 0 ? nframes : m.ctl.nframes, 0, box)
+                                     : read_frames(m);
         if (count <= 0) count = (int)fr.size() - first;
         std::vector<int64_t> ofs(count + 1, 0);
         std::vector<char> small(count, 0);

@@ -36,22 +36,49 @@ FIXTURES = {
     # 32 water molecules with the Ewald charge columns and charge constraints (FITCOUL)
     "watercoul": ("water-2b", dict(nmol=32, L=9.86, order=(8, 4, 0), smax=(5.0, 4.0, None), fitcoul=True,
                                    disp=0.1), 2, 15),
+    # two trajectory files of different sizes behind TRJFILE MULTI, label flags on the second
+    "multifile": ("multi", {}, 3, 16),
 }
+
+
+def make_multifile(d):
+    """Two trajectory files (32 and 24 water molecules) behind a MULTI list, with
+    label flags on the second file: TRJFILE MULTI traj_list.dat."""
+    with tempfile.TemporaryDirectory() as t1, tempfile.TemporaryDirectory() as t2:
+        synth.make_workload("water-3b", t1, nframes=2, seed=16, nmol=32, L=9.86, order=(8, 4, 0), fitstrs="ALL",
+                            fitener=True)
+        synth.make_workload("water-3b", t2, nframes=1, seed=17, nmol=24, L=8.96, order=(8, 4, 0), fitstrs="ALL",
+                            fitener=True)
+        shutil.copy(os.path.join(t1, "traj.xyzf"), os.path.join(d, "part_a.xyzf"))
+        shutil.copy(os.path.join(t2, "traj.xyzf"), os.path.join(d, "part_b.xyzf"))
+        fm = open(os.path.join(t1, "fm_setup.in")).read()
+    fm = fm.replace("# TRJFILE #\n\ttraj.xyzf", "# TRJFILE #\n\tMULTI traj_list.dat")
+    fm = fm.replace("# NFRAMES #\n\t2", "# NFRAMES #\n\t3")
+    open(os.path.join(d, "fm_setup.in"), "w").write(fm)
+    open(os.path.join(d, "traj_list.dat"), "w").write("2\n2 part_a.xyzf\n1 part_b.xyzf 300.0 fa_ sb_ eb_\n")
+    return ["part_a.xyzf", "part_b.xyzf", "traj_list.dat"]
 
 
 def make(name):
     wl, over, nframes, seed = FIXTURES[name]
     d = os.path.join(HERE, name)
     os.makedirs(d, exist_ok=True)
-    synth.make_workload(wl, d, nframes=nframes, seed=seed, **over)
+    inputs = ["traj.xyzf"]
+    if wl == "multi":
+        inputs = make_multifile(d)
+    else:
+        synth.make_workload(wl, d, nframes=nframes, seed=seed, **over)
     with tempfile.TemporaryDirectory() as tmp:
         shutil.copy(os.path.join(d, "fm_setup.in"), tmp)
-        shutil.copy(os.path.join(d, "traj.xyzf"), tmp)
+        for f in inputs:
+            shutil.copy(os.path.join(d, f), tmp)
         subprocess.run([REF, "fm_setup.in"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
         A = np.loadtxt(os.path.join(tmp, "A.txt"), ndmin=2)
         b = np.loadtxt(os.path.join(tmp, "b.txt"))
         for f in ("params.header", "ff_groups.map"):
             shutil.copy(os.path.join(tmp, f), os.path.join(d, f))
+        if wl == "multi":   # the labels file carries the per-file flags
+            shutil.copy(os.path.join(tmp, "b-labeled.txt"), os.path.join(d, "b-labeled.txt"))
     np.savez_compressed(os.path.join(d, "ref.npz"), A=A, b=b)
     print(name, A.shape)
 

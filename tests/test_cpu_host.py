@@ -265,3 +265,32 @@ def test_lsq_text_files_match_reference_fitcoul(cg, tmp_path):
     frames.write_lsq_files(A, out)
     for f in ("A.txt", "b.txt", "b-labeled.txt", "natoms.txt", "dim.txt"):
         assert open(out / f).read() == open(tmp_path / f).read(), f
+
+
+# ---------------------------------------------------------------- TRJFILE MULTI
+def test_multifile_labels_carry_the_file_flags(cg, tmp_path):
+    """b-labeled.txt of the two-file fixture (flags fa_ / sb_ / eb_ on the second
+    file's force / stress / energy rows) byte-identical to the reference's."""
+    d = fixture_dir("multifile")
+    m = cg.Model(os.path.join(d, "fm_setup.in"))
+    fr = cg.Frames.read(m)
+    assert fr.nframes == 3
+    A = np.zeros((fr.nrows, m.ncols))
+    fr.write_lsq_files(A, tmp_path)
+    assert open(tmp_path / "b-labeled.txt").read() == open(os.path.join(d, "b-labeled.txt")).read()
+
+
+@needs_ref
+def test_two_traj_files_match_reference_suite(cg, tmp_path):
+    """The reference's two-traj-files case (TRJFILE MULTI, 64- and 128-atom files):
+    labels, b.txt and b-labeled.txt as its golden output."""
+    src = os.path.join(REF_LSQ, "two-traj-files")
+    m = cg.Model(os.path.join(src, "fm_setup.in"))
+    fr = cg.Frames.read(m)
+    gold = os.path.join(src, "correct_output")
+    assert np.array_equal(fr.labels(), np.loadtxt(os.path.join(gold, "b.txt")))
+    A = np.zeros((fr.nrows, m.ncols))
+    fr.write_lsq_files(A, tmp_path)
+    for f in ("b.txt", "b-labeled.txt"):
+        assert open(tmp_path / f).read() == open(os.path.join(gold, f)).read(), f
+    assert m.params_header() == open(os.path.join(gold, "params.header")).read()
