@@ -449,6 +449,23 @@ int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
     });
 }
 
+int cg_md_nvt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, int style,
+              double temperature, double tau_fs, double* velocities, double* forces, double* scalars_steps,
+              double* ke_steps, double* conserved_steps) {
+    return guarded([&] {
+        need(s && d && mass && velocities && forces, "session/frames/mass/velocities/forces");
+        need(dt_fs > 0.0 && nsteps >= 0, "dt/nsteps");
+        need(style == CG_NVT_MTK || style == CG_NVT_BEREND, "thermostat style");
+        const double Tfs = 48.888;   // internal time unit in fs (src/functions.h:44)
+        cg::MdThermostat th;
+        th.style = style == CG_NVT_MTK ? 1 : 2;
+        th.temperature = temperature;
+        th.tau_fs = tau_fs;
+        s->s->md_run(*d->d, mass, dt_fs / Tfs, nsteps, th, velocities, forces, scalars_steps, ke_steps,
+                     conserved_steps);
+    });
+}
+
 int cg_md_serve(cg_session* s, int nreq, const cg_md_request* req, const double* mass, double dt_fs,
                 double hbm_budget_bytes, int64_t max_batch_atoms, int max_batch_frames, cg_md_result* results,
                 double* step_ms, int64_t* batch_steps) {

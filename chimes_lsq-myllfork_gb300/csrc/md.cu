@@ -843,6 +843,133 @@ __global__ void k_md_kick(FramesDev F, const double* Fo, const double* inv_mass_
     }
 }
 
+// ------------------------------------------------------------------ thermostats
+// Per-frame thermostat state th[f * MD_TH_STRIDE + ...]: zeta (THERM_VELOC), its
+// force (THERM_FORCE), position (THERM_POSIT), inertia Q, N_DOF kB T, the kinetic
+// energy of the step's incoming velocities, zeta0 / force0 of the step.
+// CONSTRAINT::UPDATE_COORDS / UPDATE_VELOCS_HALF_1 / _2, src/ClassDefs.C:867-1352.
+enum { TH_ZETA = 0, TH_FORCE, TH_POSIT, TH_Q, TH_NDOFKT, TH_KCUR, TH_ZETA0, TH_FORCE0 };
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+    v = warp_sum(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) s += red[i];
+    return s;
+}
+
+// NVT-MTK first half (one block per frame): the kinetic energy of v(t), then
+// x += v dt + a dt^2 / 2 - zeta0 v dt^2 / 2 and v_iter = v + a dt / 2 - zeta0 v dt / 2,
+// and the thermostat position.
+__global__ void k_md_mtk_half1(FramesDev F, const double* mass_type, double* x, double* v, const double* a, double dt,
+                               double* th) {
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    double* t = th + (size_t)f * MD_TH_STRIDE;
+    double k = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        k += 0.5 * mass_type[F.type[aofs + i / 3]] * v[g] * v[g];
+    }
+    k = block_sum(k, red);
+    const double z0 = t[TH_ZETA], f0 = t[TH_FORCE];
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const double vi = v[g], ai = a[g];
+        double xi = x[g] + (vi * dt + 0.5 * ai * dt * dt);
+        xi -= 0.5 * z0 * vi * dt * dt;
+        x[g] = xi;
+        double vn = vi + 0.5 * ai * dt;
+        vn -= 0.5 * z0 * vi * dt;
+        v[g] = vn;
+    }
+    if (threadIdx.x == 0) {
+        t[TH_KCUR] = k;
+        t[TH_ZETA0] = z0;
+        t[TH_FORCE0] = f0;
+        t[TH_POSIT] = t[TH_POSIT] + z0 * dt + 0.5 * dt * dt * f0;
+    }
+}
+
+// NVT-MTK second half (one block per frame): a = F/m; the thermostat velocity and
+// the velocity scale by the reference's 10-step fixed point (Martyna, Tobias, Klein
+// 1994, appendix D), the kinetic energy of (v_iter + a dt/2) / s being that of
+// v_iter + a dt/2 over s^2; then v = (v_iter + a dt / 2) / s.
+__global__ void k_md_mtk_half2(FramesDev F, const double* Fo, const double* inv_mass_type, const double* mass_type,
+                               double* acc, double* v, double dt, double* th, double* ke) {
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    double* t = th + (size_t)f * MD_TH_STRIDE;
+    double k0 = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const int ty = F.type[aofs + i / 3];
+        const double ai = Fo[g] * inv_mass_type[ty];
+        acc[g] = ai;
+        const double u = v[g] + 0.5 * ai * dt;
+        k0 += 0.5 * mass_type[ty] * u * u;
+    }
+    k0 = block_sum(k0, red);
+    const double Q = t[TH_Q], nkt = t[TH_NDOFKT], z0 = t[TH_ZETA0], f0 = t[TH_FORCE0];
+    double fT = (2.0 * t[TH_KCUR] - nkt) / Q;
+    double zT = z0, s = 1.0;
+    for (int itr = 0; itr < 10; ++itr) {
+        zT = z0 + (f0 + fT) * 0.5 * dt;
+        s = 1.0 + 0.5 * dt * zT;
+        fT = (2.0 * (k0 / (s * s)) - nkt) / Q;
+    }
+    double k = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const double vn = (v[g] + 0.5 * acc[g] * dt) / s;
+        v[g] = vn;
+        k += 0.5 * mass_type[F.type[aofs + i / 3]] * vn * vn;
+    }
+    k = block_sum(k, red);
+    if (threadIdx.x == 0) {
+        t[TH_ZETA] = zT;
+        t[TH_FORCE] = fT;
+        if (ke) ke[f] = k;
+    }
+}
+
+// NVT-BEREND: after the plain second half, v *= sqrt(1 + dt/tau (T0/T - 1)) with T
+// from the current kinetic energy and N_DOF = 3N - 3 (one block per frame).
+__global__ void k_md_berend(FramesDev F, const double* mass_type, double* v, double dt, double tau, double T0,
+                            double kb, double* ke, int* bad) {
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    double k = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        k += 0.5 * mass_type[F.type[aofs + i / 3]] * v[g] * v[g];
+    }
+    k = block_sum(k, red);
+    const double T = 2.0 * k / ((3.0 * N - 3.0) * kb);
+    const double fac = 1.0 + dt / tau * (T0 / T - 1.0);
+    if (!(fac > 0.0)) {
+        if (threadIdx.x == 0) atomicExch(bad, 1);
+        return;
+    }
+    const double eta = pow(fac, 0.5);
+    double k2 = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        v[g] *= eta;
+        k2 += 0.5 * mass_type[F.type[aofs + i / 3]] * v[g] * v[g];
+    }
+    k2 = block_sum(k2, red);
+    if (threadIdx.x == 0 && ke) ke[f] = k2;
+}
+
 // ------------------------------------------------------------------ launchers
 bool md_fast_order(int nbody, int order) {
     if (nbody == 3) return order >= 2 && order <= 8;
@@ -946,6 +1073,33 @@ void launch_md_kick(int nframes, const FramesDev& F, const double* Fo, const dou
                     double* ke, cudaStream_t st) {
     if (nframes > 0)
         k_md_kick<<<nframes, 256, 0, st>>>(F, Fo, inv_mass_type, mass_type, acc, v, dt, half, first, ke);
+}
+
+void launch_md_mtk_half1(int nframes, const FramesDev& F, const double* mass_type, double* x, double* v,
+                         const double* acc, double dt, double* th, cudaStream_t st) {
+    if (nframes > 0) k_md_mtk_half1<<<nframes, 256, 0, st>>>(F, mass_type, x, v, acc, dt, th);
+}
+
+void launch_md_mtk_half2(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
+                         const double* mass_type, double* acc, double* v, double dt, double* th, double* ke,
+                         cudaStream_t st) {
+    if (nframes > 0) k_md_mtk_half2<<<nframes, 256, 0, st>>>(F, Fo, inv_mass_type, mass_type, acc, v, dt, th, ke);
+}
+
+void launch_md_berend(int nframes, const FramesDev& F, const double* mass_type, double* v, double dt, double tau,
+                      double T0, double kb, double* ke, int* bad, cudaStream_t st) {
+    if (nframes > 0) k_md_berend<<<nframes, 256, 0, st>>>(F, mass_type, v, dt, tau, T0, kb, ke, bad);
+}
+
+__global__ void k_md_conserved(int nframes, const double* th, int mtk, double* out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nframes) return;
+    const double* t = th + (size_t)f * MD_TH_STRIDE;
+    out[f] = mtk ? 0.5 * t[TH_ZETA] * t[TH_ZETA] * t[TH_Q] + t[TH_NDOFKT] * t[TH_POSIT] : 0.0;
+}
+
+void launch_md_conserved(int nframes, const double* th, int mtk, double* out, cudaStream_t st) {
+    if (nframes > 0) k_md_conserved<<<(nframes + 127) / 128, 128, 0, st>>>(nframes, th, mtk, out);
 }
 
 }  // namespace cgd

@@ -71,5 +71,15 @@ void launch_md_drift(int64_t natoms, const FramesDev& F, const unsigned char* fi
 void launch_md_kick(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
                     const double* mass_type, double* acc, double* v, double dt, int half, const unsigned char* first,
                     double* ke, cudaStream_t st);
+// Thermostats (NVT-MTK, NVT-BEREND): per-frame state of MD_TH_STRIDE doubles.
+constexpr int MD_TH_STRIDE = 8;
+void launch_md_mtk_half1(int nframes, const FramesDev& F, const double* mass_type, double* x, double* v,
+                         const double* acc, double dt, double* th, cudaStream_t st);
+void launch_md_mtk_half2(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
+                         const double* mass_type, double* acc, double* v, double dt, double* th, double* ke,
+                         cudaStream_t st);
+void launch_md_berend(int nframes, const FramesDev& F, const double* mass_type, double* v, double dt, double tau,
+                      double T0, double kb, double* ke, int* bad, cudaStream_t st);
+void launch_md_conserved(int nframes, const double* th, int mtk, double* out, cudaStream_t st);
 
 }  // namespace cgd

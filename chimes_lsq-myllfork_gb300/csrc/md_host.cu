@@ -386,6 +386,11 @@ void Session::md_force_step(DeviceFrames& df, MdListSet& LS, double* Fo, double*
 
 void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int nsteps, double* v, double* Fo,
                      double* So_steps, double* ke_steps) {
+    md_run(df, mass_type, dt, nsteps, MdThermostat{}, v, Fo, So_steps, ke_steps, nullptr);
+}
+
+void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int nsteps, const MdThermostat& th, double* v,
+                     double* Fo, double* So_steps, double* ke_steps, double* cons_steps) {
     CK(cudaSetDevice(device_));
     if (!md_) throw Error(1, "MD coefficients are not set (cg_md_setup)");
     if (nsteps < 0) throw Error(1, "negative step count");
@@ -406,18 +411,56 @@ void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int n
     CK(cudaMemcpyAsync(dm, m.data(), nt * sizeof(double), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dim, im.data(), nt * sizeof(double), cudaMemcpyHostToDevice, st));
     const cgd::FramesDev& F = df.dev;
+    // thermostat state per frame (CONSTRAINT::INITIALIZE src/ClassDefs.C:525-585):
+    // N_DOF = 3N - 3, Q = N_DOF kB T tau^2 / Tfs^2 (tau in fs), Berendsen tau / Tfs
+    const double kb = 0.0019872067, tfs = 48.888;   // src/functions.h:43-44
+    double* thd = nullptr;
+    int* bad = nullptr;
+    if (th.style != 0) {
+        if (!(th.temperature > 0.0) || !(th.tau_fs > 0.0))
+            throw Error(1, "the thermostat needs a positive temperature and time constant");
+        std::vector<double> h((size_t)nf * cgd::MD_TH_STRIDE, 0.0);
+        for (int f = 0; f < nf; ++f) {
+            const double ndof = 3.0 * df.natoms_host.at(f) - 3.0;
+            h[(size_t)f * cgd::MD_TH_STRIDE + 3] = ndof * kb * th.temperature * th.tau_fs * th.tau_fs / tfs / tfs;
+            h[(size_t)f * cgd::MD_TH_STRIDE + 4] = ndof * kb * th.temperature;
+        }
+        thd = S.get<double>(h.size());
+        bad = S.get<int>(1);
+        CK(cudaMemcpyAsync(thd, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
+    }
     MdListSet lists;
     for (int step = 0; step <= nsteps; ++step) {
-        if (step > 0) cgd::launch_md_drift(n, F, nullptr, df.xyz, v, acc, dt, st);   // UPDATE_COORDS + VELOCS_HALF_1
+        if (step > 0) {   // UPDATE_COORDS + VELOCS_HALF_1
+            if (th.style == 1) cgd::launch_md_mtk_half1(nf, F, dm, df.xyz, v, acc, dt, thd, st);
+            else cgd::launch_md_drift(n, F, nullptr, df.xyz, v, acc, dt, st);
+        }
         double* sout = So_steps ? So_steps + (size_t)step * nf * cgd::MD_NSCALAR : so;
         if (md_skin_ > 0.0) {
             md_force_step(df, lists, Fo, sout);
         } else {
             md_force(df, Fo, sout, nullptr);
         }
-        cgd::launch_md_kick(nf, F, Fo, dim, dm, acc, v, dt, step > 0 ? 1 : 0, nullptr,
-                            ke_steps ? ke_steps + (size_t)step * nf : nullptr, st);   // a = F/m, VELOCS_HALF_2
+        double* ke = ke_steps ? ke_steps + (size_t)step * nf : nullptr;
+        if (th.style == 1 && step > 0) {   // a = F/m, VELOCS_HALF_2 with the MTK iteration
+            cgd::launch_md_mtk_half2(nf, F, Fo, dim, dm, acc, v, dt, thd, ke, st);
+        } else {
+            cgd::launch_md_kick(nf, F, Fo, dim, dm, acc, v, dt, step > 0 ? 1 : 0, nullptr, ke, st);
+            if (th.style == 2 && step > 0)
+                cgd::launch_md_berend(nf, F, dm, v, dt, th.tau_fs / tfs, th.temperature, kb, ke, bad, st);
+        }
+        if (cons_steps && thd) {   // CONSERVED_QUANT: Q zeta^2 / 2 + N_DOF kB T posit (NVT-MTK)
+            cgd::launch_md_conserved(nf, thd, th.style == 1, cons_steps + (size_t)step * nf, st);
+        }
         CK(cudaGetLastError());
+    }
+    if (bad) {
+        int hb = 0;
+        CK(cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hb) throw Error(2, "Berendsen temperature scale became negative: decrease the time step or increase the "
+                               "thermostat time");
     }
 }
 

@@ -120,6 +120,13 @@ struct MdListSet {
     void release() { lists[0].release(); lists[1].release(); next_ready = false; }
 };
 
+// Thermostat of an MD run: style 0 NVE, 1 NVT-MTK (Nose-Hoover chain of one, MTK
+// integration), 2 NVT-BEREND; temperature in K, time constant in fs.
+struct MdThermostat {
+    int style = 0;
+    double temperature = 0.0, tau_fs = 0.0;
+};
+
 // One MD request of the serving loop (host arrays owned by the caller).
 struct MdRequest {
     int natoms = 0, nsteps = 0;
@@ -228,6 +235,11 @@ class Session {
     // [(nsteps+1)*nframes] (device, may be null) receive step 0..nsteps.
     void md_nve(DeviceFrames& df, const double* mass_type, double dt, int nsteps, double* v, double* Fo,
                 double* So_steps, double* ke_steps);
+    // The same loop with a thermostat (CONSRNT NVT-MTK HOOVER tau / NVT-BEREND tau);
+    // cons_steps ((nsteps+1) * nframes, device, may be null) receives the
+    // thermostat's conserved-quantity term (NVT-MTK).
+    void md_run(DeviceFrames& df, const double* mass_type, double dt, int nsteps, const MdThermostat& th, double* v,
+                double* Fo, double* So_steps, double* ke_steps, double* cons_steps);
     // Continuous-batching serving loop: requests are admitted on arrival while the
     // batch has room (atoms, frames, memory budget), every batched step advances all
     // admitted requests by one velocity-Verlet step, finished requests leave at once.

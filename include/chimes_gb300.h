@@ -250,6 +250,19 @@ int cg_md_force_device(cg_session* s, const cg_dframes* d, double* forces, doubl
 int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, double* velocities,
               double* forces, double* scalars_steps, double* ke_steps);
 
+/* The same steps under a thermostat (chimes_md CONSRNT, src/ClassDefs.C:525-1460):
+ * CG_NVT_MTK = NVT-MTK HOOVER tau (a Nose-Hoover thermostat integrated as Martyna,
+ * Tobias and Klein, with the reference's 10-step velocity iteration), CG_NVT_BEREND
+ * = NVT-BEREND tau (Berendsen velocity rescaling).  temperature in K, tau in fs;
+ * every frame is its own system (N_DOF = 3N - 3).  conserved_steps
+ * ((nsteps+1) * nframes, device, may be NULL) receives the thermostat's part of the
+ * conserved quantity (CONSERVED_QUANT: Q zeta^2 / 2 + N_DOF kB T s; 0 for
+ * Berendsen): the run's Econs = kinetic + potential + this term. */
+enum { CG_NVT_MTK = 1, CG_NVT_BEREND = 2 };
+int cg_md_nvt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, int style,
+              double temperature, double tau_fs, double* velocities, double* forces, double* scalars_steps,
+              double* ke_steps, double* conserved_steps);
+
 /* Continuous-batching MD serving (no counterpart in the reference, whose chimes_md
  * runs one system).  Each request runs nsteps velocity-Verlet NVE steps (step 0
  * evaluates forces only, as chimes_md's first step) from its own positions and

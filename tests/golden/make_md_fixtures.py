@@ -7,7 +7,9 @@ oracle's A, only to obtain a physically shaped coefficient vector x), params.txt
 written by the library's writer, and the reference chimes_md runs NVE from the
 first frame with seeded 300 K velocities.  md_ref.npz keeps the configuration, x,
 the velocities, the reference's forces of every step (forceout.txt, 15 digits) and
-its per-step table (Ktot/N, Vtot/N, Etot/N, T, P from run_md.out).
+its per-step table (Ktot/N, Vtot/N, Etot/N, T, P from run_md.out).  md_nvt.npz (the
+4-body fixture) keeps the same from CONSRNT NVT-MTK HOOVER 10 (plus Econs/N) and
+NVT-BEREND 50 runs of 20 steps on the same inputs.
 """
 import importlib
 import os
@@ -141,6 +143,47 @@ def make(name):
     print(name, "atoms", n, "cols", x.size, "force blocks", Fall.shape[0], "table rows", len(table))
 
 
+def write_inputs(tmp, model, names, d, consrnt, steps):
+    n = len(d["types"])
+    cell, xyz, v, types = d["cell"], d["xyz"], d["v"], d["types"]
+    open(os.path.join(tmp, "params.txt"), "w").write(model.params_txt(d["x"], "! synthetic fit for MD fixtures\n!\n"))
+    with open(os.path.join(tmp, "input.xyzf"), "w") as f:
+        f.write(f"{n}\n{cell[0]:.10f} {cell[4]:.10f} {cell[8]:.10f}\n")
+        for k in range(n):
+            f.write(f"{names[types[k]]} {xyz[k, 0]:.10f} {xyz[k, 1]:.10f} {xyz[k, 2]:.10f} "
+                    f"{v[k, 0]:.16e} {v[k, 1]:.16e} {v[k, 2]:.16e}\n")
+    open(os.path.join(tmp, "run_md.in"), "w").write(RUN_MD.format(dt=float(d["dt"]), steps=steps).replace("NVE", consrnt))
+
+
+def make_nvt(name="md_ch4b", steps=20):
+    d = np.load(os.path.join(HERE, name, "md_ref.npz"))
+    model = cg.Model(os.path.join(HERE, name, "fm_setup.in"))
+    names, _ = header_types(model)
+    n = len(d["types"])
+    out = {}
+    for key, consrnt, ncol in (("mtk", "NVT-MTK HOOVER 10", 8), ("berend", "NVT-BEREND 50", 7)):
+        with tempfile.TemporaryDirectory() as tmp:
+            write_inputs(tmp, model, names, d, consrnt, steps)
+            p = subprocess.run([REF_MD, "run_md.in"], cwd=tmp, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                               text=True)
+            if p.returncode != 0:
+                raise RuntimeError(f"chimes_md failed ({consrnt}):\n{p.stdout[-2000:]}")
+            table = []
+            body = p.stdout.split("Ktot/N", 1)[1].split("END SIMULATION", 1)[0]
+            for ln in body.splitlines():
+                w = ln.split()
+                if len(w) == ncol and w[0].isdigit():
+                    table.append([float(t) for t in w])
+            out[f"table_{key}"] = np.array(table)
+            out[f"forces_{key}"] = np.loadtxt(os.path.join(tmp, "forceout.txt")).reshape(-1, n, 3)
+    np.savez_compressed(os.path.join(HERE, name, "md_nvt.npz"), steps=steps, tau_mtk=10.0, tau_berend=50.0,
+                        temperature=300.0, **out)
+    print(name, "nvt", {k: v.shape for k, v in out.items()})
+
+
 if __name__ == "__main__":
-    for nm in (sys.argv[1:] or MD_FIXTURES):
-        make(nm)
+    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt"]):
+        if nm == "nvt":
+            make_nvt()
+        else:
+            make(nm)

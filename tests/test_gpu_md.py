@@ -218,3 +218,44 @@ def test_md_skin_lists_match_per_step_enumeration(cg, tmp_path):
         out.append((dfr.read_positions(), Fd.cpu().numpy()))
     assert np.abs(out[0][0] - out[1][0]).max() <= 1e-9
     assert close(out[0][1], out[1][1], 1e-8)
+
+
+@pytest.mark.parametrize("style", ["mtk", "berend"])
+def test_md_nvt_matches_reference_run(cg, style):
+    """CONSRNT NVT-MTK HOOVER 10 and NVT-BEREND 50 against the reference chimes_md on
+    the 4-body fixture (tests/golden/md_ch4b/md_nvt.npz, 20 steps): per-step Ktot/N,
+    Vtot/N and P to the printed digits, Econs/N for MTK (kinetic + potential + the
+    thermostat's Q zeta^2 / 2 + N_DOF kB T s), and the last step's forces (1e-8)."""
+    torch = pytest.importorskip("torch")
+    fm, d = load_md("md_ch4b")
+    t = np.load(os.path.join(GOLDEN, "md_ch4b", "md_nvt.npz"))
+    tab = t[f"table_{style}"]
+    n = len(d["types"])
+    steps = int(t["steps"]) - 1
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.md_setup(d["x"], energy_offsets=True)
+    fr = cg.Frames.from_arrays(model, [n], d["types"], d["xyz"], d["cell"][None]).independent()
+    dfr = sess.upload(fr)
+    v = torch.from_numpy(d["v"].reshape(-1).copy()).cuda()
+    Fd = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    So = torch.zeros((steps + 1, 11), dtype=torch.float64, device="cuda")
+    ke = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    cons = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    st = cg.CG_NVT_MTK if style == "mtk" else cg.CG_NVT_BEREND
+    tau = float(t["tau_mtk"] if style == "mtk" else t["tau_berend"])
+    sess.md_nvt(dfr, d["masses"], float(d["dt"]), steps, st, float(t["temperature"]), tau, v.data_ptr(),
+                Fd.data_ptr(), So.data_ptr(), ke.data_ptr(), cons.data_ptr())
+    torch.cuda.synchronize()
+    So_h, ke_h, c_h = So.cpu().numpy(), ke.cpu().numpy(), cons.cpu().numpy()
+    V = abs(np.linalg.det(d["cell"].reshape(3, 3)))
+    assert close(Fd.cpu().numpy().reshape(n, 3), t[f"forces_{style}"][steps], 1e-8)
+    for s in range(steps + 1):
+        kn, vn = ke_h[s] / n, So_h[s, 0] / n
+        p = (So_h[s, 1] + 2.0 * ke_h[s] / (3.0 * V)) * GPA
+        assert abs(kn - tab[s, 2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, tab[s, 2])
+        assert abs(vn - tab[s, 3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, tab[s, 3])
+        assert abs(p - tab[s, 6]) <= 5e-9 * max(1.0, abs(p)) + 1e-12, (s, p, tab[s, 6])
+        if style == "mtk":
+            en = (ke_h[s] + So_h[s, 0] + c_h[s]) / n
+            assert abs(en - tab[s, 7]) <= 5e-8 * max(1.0, abs(en)) + 1e-12, (s, en, tab[s, 7])
