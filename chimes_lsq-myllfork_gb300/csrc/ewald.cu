@@ -21,6 +21,7 @@
 #include <cstdint>
 
 #include "kernels.h"
+#include "md.h"
 
 namespace cgd {
 
@@ -214,6 +215,208 @@ __global__ void __launch_bounds__(256) k_ewald_kspace(ModelDev M, FramesDev F, i
             }
         }
     }
+}
+
+// ---------------------------------------------------------------- MD (fixed charges)
+// ZCalc_Ewald / Ewald_K_Space_New (src/Ewald.C:28-426) with ke = 332.0637157615209
+// (src/functions.h:40).  Real space: each atom gathers the pair force of every image
+// g != a within r_c (the reference's half-list updates of both atoms sum to that);
+// energy and virial take the half list's entries, i.e. the images with parent >= a
+// (big cells) or all images with PERM_SCALE 1/2 (small cells).  k space over the full
+// sphere |k|^2 < k_cut^2 of integer k in [-k_cut, k_cut]^3: S(k) = sum_b q_b exp(i k.r_b),
+// energy ke (2 pi / V) sum_k Kfac |S|^2 - ke alpha / sqrt(pi) sum q^2, the Heyes
+// virial tensor, forces -4 pi ke Kfac q_a (C sin - S cos) / V k.  The pressure term is
+// the Coulomb energy (Hummer et al.).
+constexpr double MD_KE = 332.0637157615209;
+
+__global__ void __launch_bounds__(256) k_md_ewald_real(MdDev D, FramesDev F, int nreal, double* Fo, double* So) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nreal) return;
+    const int f = ew_frame_of_atom(F, warp);
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    const int i = warp - (int)aofs;
+    const int64_t gb = F.ghost_ofs[f];
+    const BoxDev& B = F.box[f];
+    const double alpha = B.ew_alpha, rc = B.ew_rc;
+    const float4* c32 = reinterpret_cast<const float4*>(F.cart32);
+    const float4 xi = c32[gb + i];
+    const int* typ = F.type + aofs;
+    const double qi = D.qtype[typ[i]];
+    const bool small = B.small != 0;
+    const double perm = B.perm2;
+    double fx = 0, fy = 0, fz = 0, u = 0, w[6] = {0, 0, 0, 0, 0, 0};
+    const int nimg_n = F.nimg * N;
+    for (int j = lane; j < nimg_n; j += 32) {
+        if (j == i) continue;
+        const float4 xj = c32[gb + j];
+        const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+        if (sqrtf(dx * dx + dy * dy + dz * dz) > (float)rc + 1.0e-2f) continue;
+        double R[3];
+        const double r = dist_exact(B.h, F.scaled + 3 * (gb + i), F.scaled + 3 * (gb + j), R);
+        if (!(r < rc)) continue;
+        const double qq = qi * D.qtype[typ[j % N]];
+        const double ef = erfc(alpha * r);
+        const double td = ((-2.0 / sqrt(M_PI)) * exp(-1.0 * alpha * alpha * r * r) * r * alpha - ef) / (r * r * r);
+        const double tx = -td * qq * MD_KE;   // the pair force on a is R * tx (R = r_g - r_a) with a minus sign
+        fx -= R[0] * tx; fy -= R[1] * tx; fz -= R[2] * tx;
+        const bool listed = small || (j % N) >= i;   // the reference's half list
+        if (listed) {
+            const double wgt = small ? perm : 1.0;
+            u += MD_KE * qq * (ef / r) * wgt;
+            const double t = tx * wgt;
+            w[0] += t * R[0] * R[0]; w[1] += t * R[0] * R[1]; w[2] += t * R[0] * R[2];
+            w[3] += t * R[1] * R[1]; w[4] += t * R[1] * R[2]; w[5] += t * R[2] * R[2];
+        }
+    }
+    fx = ew_warp_sum(fx); fy = ew_warp_sum(fy); fz = ew_warp_sum(fz); u = ew_warp_sum(u);
+    for (int k = 0; k < 6; ++k) w[k] = ew_warp_sum(w[k]);
+    if (lane == 0) {
+        double* fo = Fo + 3 * (aofs + i);
+        fo[0] += fx; fo[1] += fy; fo[2] += fz;   // one warp owns atom a
+        double* so = So + (size_t)f * MD_NSCALAR;
+        atomicAdd(so + 0, u);
+        atomicAdd(so + 1, u);
+        atomicAdd(so + 2, w[0]); atomicAdd(so + 3, w[1]); atomicAdd(so + 4, w[2]);
+        atomicAdd(so + 5, w[1]); atomicAdd(so + 6, w[3]); atomicAdd(so + 7, w[4]);
+        atomicAdd(so + 8, w[2]); atomicAdd(so + 9, w[4]); atomicAdd(so + 10, w[5]);
+    }
+}
+
+__device__ __forceinline__ bool md_kvec(int q, int kmax, int& kx, int& ky, int& kz) {
+    const int side = 2 * kmax + 1;
+    kx = q / (side * side) - kmax; ky = (q / side) % side - kmax; kz = q % side - kmax;
+    const int ksq = kx * kx + ky * ky + kz * kz;
+    return ksq != 0 && ksq < kmax * kmax;
+}
+
+// Per frame and k: S(k) (cos and sin sums); energy and virial of that k.
+__global__ void __launch_bounds__(128) k_md_ewald_sfac(MdDev D, FramesDev F, int kmax_max, double2* Sk, double* So) {
+    const int f = blockIdx.y;
+    const BoxDev& B = F.box[f];
+    const int kmax = B.ew_kmax;
+    const int side = 2 * kmax + 1, nq = side * side * side;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int side_max = 2 * kmax_max + 1;
+    double e = 0, w[6] = {0, 0, 0, 0, 0, 0};
+    int kx, ky, kz;
+    if (q < nq && md_kvec(q, kmax, kx, ky, kz)) {
+        const int N = F.natoms[f];
+        const int64_t aofs = F.atom_ofs[f];
+        const double L[3] = {B.h[0], B.h[4], B.h[8]};
+        const double kv[3] = {(2.0 * M_PI / L[0]) * kx, (2.0 * M_PI / L[1]) * ky, (2.0 * M_PI / L[2]) * kz};
+        const double alphasq = B.ew_alpha * B.ew_alpha;
+        const double rksq = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+        const double kfac = exp(-rksq / (4.0 * alphasq)) / rksq;
+        double cs = 0.0, sn = 0.0;
+        for (int b = 0; b < N; ++b) {
+            const double* x = F.xyz + 3 * (aofs + b);
+            const double kr = x[0] * kv[0] + x[1] * kv[1] + x[2] * kv[2];
+            double sv, cv;
+            sincos(kr, &sv, &cv);
+            const double qb = D.qtype[F.type[aofs + b]];
+            cs += qb * cv;
+            sn += qb * sv;
+        }
+        Sk[(size_t)f * side_max * side_max * side_max + q] = make_double2(cs, sn);
+        const double kw = kfac * (cs * cs + sn * sn);
+        const double V = (B.h[0] * B.h[4] * B.h[8]);
+        const double pre = 2 * M_PI * MD_KE / V;
+        e = kw;
+        w[0] = pre * kw * (1.0 - 2.0 * kv[0] * kv[0] / rksq - 0.5 * kv[0] * kv[0] / alphasq);
+        w[3] = pre * kw * (1.0 - 2.0 * kv[1] * kv[1] / rksq - 0.5 * kv[1] * kv[1] / alphasq);
+        w[5] = pre * kw * (1.0 - 2.0 * kv[2] * kv[2] / rksq - 0.5 * kv[2] * kv[2] / alphasq);
+        w[1] = pre * kw * (-2.0 * kv[0] * kv[1] / rksq - 0.5 * kv[0] * kv[1] / alphasq);
+        w[2] = pre * kw * (-2.0 * kv[0] * kv[2] / rksq - 0.5 * kv[0] * kv[2] / alphasq);
+        w[4] = pre * kw * (-2.0 * kv[1] * kv[2] / rksq - 0.5 * kv[1] * kv[2] / alphasq);
+    } else if (q < side_max * side_max * side_max) {
+        Sk[(size_t)f * side_max * side_max * side_max + q] = make_double2(0.0, 0.0);
+    }
+    // block sums -> frame scalars: energy ke (2 pi / V) sum kw (pressure term the same)
+    __shared__ double red[7][4];
+    double vals[7] = {e, w[0], w[1], w[2], w[3], w[4], w[5]};
+    for (int k = 0; k < 7; ++k) {
+        double v = ew_warp_sum(vals[k]);
+        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        double s = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[threadIdx.x][i];
+        double* so = So + (size_t)f * MD_NSCALAR;
+        if (s != 0.0) {
+            const int k = threadIdx.x;
+            if (k == 0) {
+                const double uk = MD_KE * (2 * M_PI / (F.box[f].h[0] * F.box[f].h[4] * F.box[f].h[8])) * s;
+                atomicAdd(so + 0, uk);
+                atomicAdd(so + 1, uk);
+            } else if (k == 1) atomicAdd(so + 2, s);
+            else if (k == 2) { atomicAdd(so + 3, s); atomicAdd(so + 5, s); }
+            else if (k == 3) { atomicAdd(so + 4, s); atomicAdd(so + 8, s); }
+            else if (k == 4) atomicAdd(so + 6, s);
+            else if (k == 5) { atomicAdd(so + 7, s); atomicAdd(so + 9, s); }
+            else atomicAdd(so + 10, s);
+        }
+    }
+}
+
+// Per atom: the k-space force, and the self-energy term (one warp per atom).
+__global__ void __launch_bounds__(256) k_md_ewald_kforce(MdDev D, FramesDev F, int nreal, int kmax_max,
+                                                         const double2* Sk, double* Fo, double* So) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nreal) return;
+    const int f = ew_frame_of_atom(F, warp);
+    const int64_t aofs = F.atom_ofs[f];
+    const int i = warp - (int)aofs;
+    const BoxDev& B = F.box[f];
+    const int kmax = B.ew_kmax;
+    const int side = 2 * kmax + 1, nq = side * side * side;
+    const int side_max = 2 * kmax_max + 1;
+    const double L[3] = {B.h[0], B.h[4], B.h[8]};
+    const double alphasq = B.ew_alpha * B.ew_alpha;
+    const double V = (B.h[0] * B.h[4] * B.h[8]);
+    const double* x = F.xyz + 3 * (aofs + i);
+    const double qa = D.qtype[F.type[aofs + i]];
+    double fx = 0, fy = 0, fz = 0;
+    for (int q = lane; q < nq; q += 32) {
+        int kx, ky, kz;
+        if (!md_kvec(q, kmax, kx, ky, kz)) continue;
+        const double kv[3] = {(2.0 * M_PI / L[0]) * kx, (2.0 * M_PI / L[1]) * ky, (2.0 * M_PI / L[2]) * kz};
+        const double rksq = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+        const double kfac = exp(-rksq / (4.0 * alphasq)) / rksq;
+        const double2 s = Sk[(size_t)f * side_max * side_max * side_max + q];
+        double sv, cv;
+        sincos(x[0] * kv[0] + x[1] * kv[1] + x[2] * kv[2], &sv, &cv);
+        const double td = -4.0 * M_PI * kfac * MD_KE * qa * (s.x * sv - s.y * cv) / V;
+        fx -= kv[0] * td; fy -= kv[1] * td; fz -= kv[2] * td;   // ACCEL -= TMP_EWALD
+    }
+    fx = ew_warp_sum(fx); fy = ew_warp_sum(fy); fz = ew_warp_sum(fz);
+    if (lane == 0) {
+        double* fo = Fo + 3 * (aofs + i);
+        fo[0] += fx; fo[1] += fy; fo[2] += fz;
+        const double self = -MD_KE * B.ew_alpha / sqrt(M_PI) * qa * qa;
+        double* so = So + (size_t)f * MD_NSCALAR;
+        atomicAdd(so + 0, self);
+        atomicAdd(so + 1, self);
+    }
+}
+
+size_t md_ewald_scratch_bytes(int nframes, int kmax_max) {
+    const size_t side = 2 * (size_t)kmax_max + 1;
+    return sizeof(double2) * (size_t)nframes * side * side * side;
+}
+
+void launch_md_ewald(int nframes, int nreal, int kmax_max, const ModelDev& M, const MdDev& D, const FramesDev& F,
+                     void* S, double* Fo, double* So, cudaStream_t st) {
+    (void)M;
+    if (!D.coulomb || nreal == 0) return;
+    const unsigned wb = (unsigned)(((int64_t)nreal * 32 + 255) / 256);
+    k_md_ewald_real<<<wb, 256, 0, st>>>(D, F, nreal, Fo, So);
+    const int side = 2 * kmax_max + 1, nq = side * side * side;
+    k_md_ewald_sfac<<<dim3((nq + 127) / 128, (unsigned)nframes), 128, 0, st>>>(D, F, kmax_max, (double2*)S, So);
+    k_md_ewald_kforce<<<wb, 256, 0, st>>>(D, F, nreal, kmax_max, (const double2*)S, Fo, So);
 }
 
 size_t ewald_scratch_bytes(int nframes, int natmtyp) {

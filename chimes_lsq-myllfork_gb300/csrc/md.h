@@ -26,7 +26,15 @@ struct MdDev {
     const float* C4f;
     const double* eoff;     // [natmtyp] per-atom energy offsets, or null
     double pen_dist, pen_scale;   // 2-body penalty (src/chimes_md.C:1747-1748 defaults)
+    int coulomb;            // Ewald sums with the charges qtype (electron units)
+    double qtype[10];       // charge of each atom type
 };
+
+// Ewald Coulomb forces, energy and virial of MD frames (ZCalc_Ewald, src/Ewald.C:28-426),
+// added to the raw (pre-normalisation) scalars; S holds md_ewald_scratch_bytes.
+size_t md_ewald_scratch_bytes(int nframes, int kmax_max);
+void launch_md_ewald(int nframes, int nreal, int kmax_max, const ModelDev& M, const MdDev& D, const FramesDev& F,
+                     void* S, double* Fo, double* So, cudaStream_t st);
 
 // Clusters grouped by key = frame * ntypes + type for the contraction kernels: the
 // order inside a group is not fixed (the forces are accumulated with atomics).

@@ -21,6 +21,13 @@
 
 namespace cg {
 
+// Largest Ewald k cut-off of a batch's frames (the k-space scratch is sized by it).
+static int md_ewald_kmax(const DeviceFrames& df) {
+    int km = 1;
+    for (const auto& b : df.box_host) km = std::max(km, b.ew_kmax);
+    return km;
+}
+
 void Session::md_setup(const double* x, int nx, int precision, bool offsets, double pen_dist, double pen_scale) {
     CK(cudaSetDevice(device_));
     const Model& m = model_;
@@ -72,8 +79,30 @@ void Session::md_setup(const double* x, int nx, int precision, bool offsets, dou
     t->dev.C4f = (const float*)up(C4f.data(), C4f.size() * sizeof(float));
     t->dev.eoff = nullptr;
     if (offsets) {
-        if (m.tot_all - m.tot_short != m.ctl.natmtyp) throw Error(2, "the model has no energy-offset columns");
-        t->dev.eoff = (const double*)up(x + m.tot_short, m.ctl.natmtyp * sizeof(double));
+        if (m.tot_all - m.tot_short - m.ncoul != m.ctl.natmtyp) throw Error(2, "the model has no energy-offset columns");
+        t->dev.eoff = (const double*)up(x + m.tot_short + m.ncoul, m.ctl.natmtyp * sizeof(double));
+    }
+    // FITCOUL: charges from the fitted products (chimes_md read_ff_params,
+    // src/chimes_md.C:2000-2080): q products in Stillinger units over ke, q_t =
+    // sign_t sqrt(|q_t q_t|), every pair's product within 1e-4 of q_i q_j
+    t->dev.coulomb = 0;
+    if (m.ncoul > 0) {
+        const double ke = 332.0637157615209;   // src/functions.h:40
+        const int nt = m.ctl.natmtyp;
+        if (nt > 10) throw Error(2, "Ewald MD supports up to 10 atom types");
+        for (int i = 0; i < nt; ++i) {
+            const double qq = x[m.tot_short + m.int_pair_map[i * nt + i]] / ke;
+            const std::string& sg = m.pairs[i].chrgsgn;
+            const double sign = sg.find('-') != std::string::npos ? -1.0 : 1.0;
+            t->dev.qtype[i] = std::sqrt(std::fabs(qq)) * sign;
+        }
+        for (int i = 0; i < nt; ++i)
+            for (int j = 0; j < nt; ++j) {
+                const double qq = x[m.tot_short + m.int_pair_map[i * nt + j]] / ke;
+                if (std::fabs(t->dev.qtype[i] * t->dev.qtype[j] - qq) > 1.0e-4)
+                    throw Error(2, "Inconsistent pair charges for pair: " + m.atom_types[i] + m.atom_types[j]);
+            }
+        t->dev.coulomb = 1;
     }
     t->dev.pen_dist = pen_dist;
     t->dev.pen_scale = pen_scale;
@@ -160,6 +189,11 @@ void Session::md_force(const DeviceFrames& df, double* Fo, double* So, MdCounts*
         cgd::launch_mdc(nbody, md_->precision, k == 0 ? M.order3 : M.order4, max_tiles, M, D, F, CS, B, Fo, So, st);
         L();
         CK(cudaGetLastError());
+    }
+    if (D.coulomb) {   // ZCalc_Ewald
+        const int km = md_ewald_kmax(df);
+        void* ews = S.get<unsigned char>(cgd::md_ewald_scratch_bytes(nf, km));
+        cgd::launch_md_ewald(nf, nreal, km, M, D, F, ews, Fo, So, st); L(3);
     }
     cgd::launch_md_finalize(nf, M, D, F, So, st); L();
     CK(cudaGetLastError());
@@ -337,6 +371,13 @@ void Session::md_force_lists(DeviceFrames& df, MdLists& L, double* Fo, double* S
         cgd::launch_mdc(3 + k, md_->precision, k == 0 ? M.order3 : M.order4, max_tiles, M, D, F, CS, L.B[k], Fo, So,
                         st);
         mark(k == 0 ? ST_FORCE3 : ST_FORCE4, false);
+    }
+    if (D.coulomb) {   // ZCalc_Ewald
+        const int km = md_ewald_kmax(df);
+        void* ews = nullptr;
+        CK(cudaMallocAsync(&ews, cgd::md_ewald_scratch_bytes(nf, km), st));
+        cgd::launch_md_ewald(nf, nreal, km, M, D, F, ews, Fo, So, st);
+        CK(cudaFreeAsync(ews, st));
     }
     cgd::launch_md_finalize(nf, M, D, F, So, st);
     CK(cudaGetLastError());
@@ -560,6 +601,11 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
         bd.lx = b.lx; bd.ly = b.ly; bd.lz = b.lz; bd.vol = b.vol;
         bd.is_ortho = b.is_ortho ? 1 : 0;
         set_small(bd, frame_is_small(m, b, false));
+        if (md_ && md_->dev.coulomb) {   // optimal_ewald_params for the request's cell
+            if (!b.is_ortho) throw Error(2, "the Ewald sums need an orthorhombic cell");
+            const EwaldParams ep = ewald_params(q.natoms, b);
+            bd.ew_alpha = ep.alpha; bd.ew_rc = ep.rc; bd.ew_kmax = ep.kmax;
+        }
     }
     std::vector<double> mv(mass_type, mass_type + nt), im(nt);
     for (int i = 0; i < nt; ++i) {

@@ -143,6 +143,60 @@ def make(name):
     print(name, "atoms", n, "cols", x.size, "force blocks", Fall.shape[0], "table rows", len(table))
 
 
+def make_coul(name="md_watercoul", steps=10, seed=33):
+    """Ewald MD: the FITCOUL water model (2B8 + 3B4 + charge products) with the
+    short-range coefficients fitted on the watercoul fixture's reference A and
+    consistent charges q_O = -0.82, q_H = +0.41 (products in Stillinger units, as
+    chimes_lsq.py writes them); chimes_md runs NVE from the fixture's first frame."""
+    src = os.path.join(HERE, "watercoul")
+    d = os.path.join(HERE, name)
+    os.makedirs(d, exist_ok=True)
+    fm = open(os.path.join(src, "fm_setup.in")).read()
+    open(os.path.join(d, "fm_setup.in"), "w").write(fm)
+    model = cg.Model(os.path.join(d, "fm_setup.in"))
+    ref = np.load(os.path.join(src, "ref.npz"))
+    A, b = ref["A"], ref["b"]
+    x = np.linalg.solve(A.T @ A + 1e-6 * np.abs(A).max() ** 2 * np.eye(A.shape[1]), A.T @ b)
+    names, masses = header_types(model)
+    ke = 332.0637157615209
+    q = {"O": -0.82, "H": 0.41}
+    ncoul, _ = model.charge_columns()
+    hdr = model.params_header().splitlines()
+    k = next(i for i, ln in enumerate(hdr) if ln.startswith("ATOM PAIRS:"))
+    short = model.ncols - ncoul
+    for p_ in range(ncoul):   # pair rows of the header: index, atom1, atom2
+        w = hdr[k + 3 + p_].split()
+        x[short + p_] = q[w[1]] * q[w[2]] * ke
+    n, types, xyz, cell = read_first_frame(os.path.join(src, "traj.xyzf"), names)
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((n, 3)) * np.sqrt(KB * 300.0 / masses[types])[:, None]
+    v -= (masses[types][:, None] * v).sum(0) / masses[types].sum()
+    dt = 0.2
+    with tempfile.TemporaryDirectory() as tmp:
+        open(os.path.join(tmp, "params.txt"), "w").write(model.params_txt(x, "! synthetic fit for MD fixtures\n!\n"))
+        with open(os.path.join(tmp, "input.xyzf"), "w") as f:
+            f.write(f"{n}\n{cell[0]:.10f} {cell[4]:.10f} {cell[8]:.10f}\n")
+            for j in range(n):
+                f.write(f"{names[types[j]]} {xyz[j, 0]:.10f} {xyz[j, 1]:.10f} {xyz[j, 2]:.10f} "
+                        f"{v[j, 0]:.16e} {v[j, 1]:.16e} {v[j, 2]:.16e}\n")
+        open(os.path.join(tmp, "run_md.in"), "w").write(RUN_MD.format(dt=dt, steps=steps))
+        p = subprocess.run([REF_MD, "run_md.in"], cwd=tmp, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"chimes_md failed for {name}:\n{p.stdout[-2000:]}")
+        _, _, xyz_in, _ = read_first_frame(os.path.join(tmp, "input.xyzf"), names)
+        Fall = np.loadtxt(os.path.join(tmp, "forceout.txt")).reshape(-1, n, 3)
+        table = []
+        out = p.stdout.split("Ktot/N", 1)[1].split("END SIMULATION", 1)[0]
+        for ln in out.splitlines():
+            w = ln.split()
+            if len(w) == 7 and w[0].isdigit():
+                table.append([float(t) for t in w])
+    vin = np.array([[float(t) for t in f"{v[j, 0]:.16e} {v[j, 1]:.16e} {v[j, 2]:.16e}".split()] for j in range(n)])
+    np.savez_compressed(os.path.join(d, "md_ref.npz"), x=x, types=types, xyz=xyz_in, cell=cell, v=vin,
+                        masses=masses, dt=dt, steps=steps, forces=Fall, table=np.array(table))
+    print(name, n, "atoms", Fall.shape, len(table))
+
+
 def write_inputs(tmp, model, names, d, consrnt, steps):
     n = len(d["types"])
     cell, xyz, v, types = d["cell"], d["xyz"], d["v"], d["types"]
@@ -182,8 +236,10 @@ def make_nvt(name="md_ch4b", steps=20):
 
 
 if __name__ == "__main__":
-    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt"]):
+    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "md_watercoul"]):
         if nm == "nvt":
             make_nvt()
+        elif nm == "md_watercoul":
+            make_coul()
         else:
             make(nm)

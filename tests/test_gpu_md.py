@@ -259,3 +259,42 @@ def test_md_nvt_matches_reference_run(cg, style):
         if style == "mtk":
             en = (ke_h[s] + So_h[s, 0] + c_h[s]) / n
             assert abs(en - tab[s, 7]) <= 5e-8 * max(1.0, abs(en)) + 1e-12, (s, en, tab[s, 7])
+
+
+def _md_coul_run(cg, steps):
+    torch = pytest.importorskip("torch")
+    fm, d = load_md("md_watercoul")
+    n = len(d["types"])
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.md_setup(d["x"])
+    fr = cg.Frames.from_arrays(model, [n], d["types"], d["xyz"], d["cell"][None]).independent()
+    F0, S0 = sess.md_force(fr)
+    dfr = sess.upload(fr)
+    v = torch.from_numpy(d["v"].reshape(-1).copy()).cuda()
+    Fd = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    So = torch.zeros((steps + 1, 11), dtype=torch.float64, device="cuda")
+    ke = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    sess.md_nve(dfr, d["masses"], float(d["dt"]), steps, v.data_ptr(), Fd.data_ptr(), So.data_ptr(), ke.data_ptr())
+    torch.cuda.synchronize()
+    return d, n, F0, Fd.cpu().numpy().reshape(n, 3), So.cpu().numpy(), ke.cpu().numpy()
+
+
+def test_md_coulomb_matches_reference_run(cg):
+    """Ewald MD (charges from a FITCOUL fit's products, ZCalc_Ewald) against the
+    reference chimes_md on 96 water atoms (tests/golden/md_watercoul): forces of step
+    0 and of the last step (1e-10 / 1e-8 of max|F|), Ktot/N, Vtot/N and P of every
+    step to the printed digits."""
+    fm, dd = load_md("md_watercoul")
+    steps = int(dd["steps"]) - 1
+    d, n, F0, Fl, So_h, ke_h = _md_coul_run(cg, steps)
+    assert close(F0, d["forces"][0], 1e-10)
+    assert close(Fl, d["forces"][steps], 1e-8)
+    V = abs(np.linalg.det(d["cell"].reshape(3, 3)))
+    tab = d["table"]
+    for s in range(steps + 1):
+        kn, vn = ke_h[s] / n, So_h[s, 0] / n
+        p = (So_h[s, 1] + 2.0 * ke_h[s] / (3.0 * V)) * GPA
+        assert abs(kn - tab[s, 2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, tab[s, 2])
+        assert abs(vn - tab[s, 3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, tab[s, 3])
+        assert abs(p - tab[s, 6]) <= 5e-9 * max(1.0, abs(p)) + 1e-12, (s, p, tab[s, 6])
