@@ -111,6 +111,7 @@ def lib():
         "cg_md_force": (ctypes.c_int, [vp, vp, dp, dp]),
         "cg_md_force_device": (ctypes.c_int, [vp, vp, vp, vp]),
         "cg_md_nve": (ctypes.c_int, [vp, vp, dp, ctypes.c_double, ctypes.c_int, vp, vp, vp, vp]),
+        "cg_frames_subtract_coulomb": (ctypes.c_int, [vp, vp]),
         "cg_md_nvt": (ctypes.c_int, [vp, vp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, vp, vp, vp, vp, vp]),
         "cg_dframes_positions": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_void_p), i64p]),
@@ -263,6 +264,11 @@ class Frames:
         h = ctypes.c_void_p()
         _check(lib().cg_frames_slice(self._h, int(first), int(count), ctypes.byref(h)))
         return Frames(h, self.model)
+
+    def subtract_coulomb(self, session):
+        """Fixed charges: subtract the Ewald forces from the force labels (in place)."""
+        _check(lib().cg_frames_subtract_coulomb(session._h, self._h))
+        return self
 
     def write_lsq_files(self, A, directory):
         """A.txt / b.txt / b-labeled.txt / natoms.txt / dim.txt for these frames (A: host FP64)."""

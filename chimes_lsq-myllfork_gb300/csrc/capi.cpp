@@ -449,6 +449,13 @@ int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
     });
 }
 
+int cg_frames_subtract_coulomb(cg_session* s, cg_frames* fr) {
+    return guarded([&] {
+        need(s && fr, "session/frames");
+        s->s->subtract_coulomb(fr->fb);
+    });
+}
+
 int cg_md_nvt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, int style,
               double temperature, double tau_fs, double* velocities, double* forces, double* scalars_steps,
               double* ke_steps, double* conserved_steps) {

@@ -103,6 +103,10 @@ void Session::md_setup(const double* x, int nx, int precision, bool offsets, dou
                     throw Error(2, "Inconsistent pair charges for pair: " + m.atom_types[i] + m.atom_types[j]);
             }
         t->dev.coulomb = 1;
+    } else if (m.ctl.use_partial_charges) {   // fixed charges (ATMCHRG), chimes_md.C:2024-2036
+        if (m.ctl.natmtyp > 10) throw Error(2, "Ewald MD supports up to 10 atom types");
+        for (int i = 0; i < m.ctl.natmtyp; ++i) t->dev.qtype[i] = m.pairs[i].chg1;
+        t->dev.coulomb = 1;
     }
     t->dev.pen_dist = pen_dist;
     t->dev.pen_scale = pen_scale;
@@ -422,6 +426,48 @@ void Session::md_force_step(DeviceFrames& df, MdListSet& LS, double* Fo, double*
         md_lists_build(df, md_skin_, LS.lists[LS.cur ^ 1], side_stream_);
         LS.next_ready = true;
         ++LS.early_builds;
+    }
+}
+
+void Session::subtract_coulomb(FrameBatch& fb) {
+    CK(cudaSetDevice(device_));
+    const Model& m = model_;
+    if (!m.ctl.use_partial_charges) return;
+    if (fb.nframes == 0) return;
+    if (m.ctl.natmtyp > 10) throw Error(2, "Ewald sums support up to 10 atom types");
+    cgd::MdDev D{};
+    D.coulomb = 1;
+    for (int i = 0; i < m.ctl.natmtyp; ++i) D.qtype[i] = m.pairs[i].chg1;   // ATOM_PAIRS[i].ATM1CHG
+    // the first frame's parameters for every frame (static alpha / r_cut / k_cut)
+    const cgd::BoxDev& b0 = fb.box[0];
+    if (!b0.is_ortho) throw Error(2, "the Ewald sums need an orthorhombic cell");
+    Box bx;
+    bx.ax = b0.h[0]; bx.by = b0.h[4]; bx.cz = b0.h[8];
+    const EwaldParams ep = ewald_params(fb.natoms[0], bx);
+    FrameBatch fe = fb;
+    for (auto& b : fe.box) {
+        if (!b.is_ortho) throw Error(2, "the Ewald sums need an orthorhombic cell");
+        b.ew_alpha = ep.alpha; b.ew_rc = ep.rc; b.ew_kmax = ep.kmax;
+    }
+    std::unique_ptr<DeviceFrames> df = upload(fe);
+    cudaStream_t st = stream_;
+    const int nf = df->nframes;
+    const int64_t n = df->natoms_total;
+    Scratch S(st);
+    double* Fo = S.get<double>(3 * n);
+    double* So = S.get<double>((size_t)nf * cgd::MD_NSCALAR);
+    void* ews = S.get<unsigned char>(cgd::md_ewald_scratch_bytes(nf, std::max(1, ep.kmax)));
+    CK(cudaMemsetAsync(Fo, 0, sizeof(double) * 3 * n, st));
+    CK(cudaMemsetAsync(So, 0, sizeof(double) * nf * cgd::MD_NSCALAR, st));
+    cgd::launch_frame_setup(df->dev, df->nghosts, st);
+    cgd::launch_md_ewald(nf, (int)n, std::max(1, ep.kmax), dm_->dev, D, df->dev, ews, Fo, So, st);
+    CK(cudaGetLastError());
+    std::vector<double> f(3 * n);
+    CK(cudaMemcpyAsync(f.data(), Fo, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int k = 0; k < fb.nframes; ++k) {   // FORCES -= ACCEL (force rows come first in each frame)
+        const int64_t r0 = fb.row_ofs[k], a0 = fb.atom_ofs[k];
+        for (int64_t q = 0; q < 3 * (int64_t)fb.natoms[k]; ++q) fb.b[r0 + q] -= f[3 * a0 + q];
     }
 }
 

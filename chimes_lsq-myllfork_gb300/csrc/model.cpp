@@ -662,7 +662,8 @@ Model load_model(const std::string& path) {
     if (c.wrap && c.nlayers > 0) c.wrap = false;
     if (c.fit_coul && (c.fit_stress || c.fit_stress_all || c.fit_ener))
         fail("FITCOUL with stress or energy rows: the reference prints no charge columns on those rows");
-    if (c.use_partial_charges) fail("fixed partial charges (Ewald subtraction) are outside this build's path");
+    if (c.use_partial_charges && (c.fit_stress || c.fit_stress_all || c.fit_ener))
+        fail("fixed charges with stress or energy rows: only the force labels are corrected (SubtractEwaldForces)");
     if (c.nlayers < 1) fail("NLAYERS must be >= 1 (ghost-atom images); NLAYERS 0 is not supported by this build");
     // main: src/chimes_lsq.C:198-248
     m.tot_snum = 0;

@@ -224,7 +224,7 @@ FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int firs
         bd.is_ortho = fr.box.is_ortho ? 1 : 0;
         bd.small = small ? 1 : 0;
         set_small(bd, small);
-        if (m.ncoul > 0) {   // ZCalc_Ewald_Deriv src/Ewald.C:518-550 (orthorhombic cells only)
+        if (m.ncoul > 0 || m.ctl.use_partial_charges) {   // optimal_ewald_params (orthorhombic cells only)
             if (!fr.box.is_ortho) throw Error(2, "the Ewald charge columns need an orthorhombic cell");
             const EwaldParams ep = ewald_params(fr.natoms, fr.box);
             bd.ew_alpha = ep.alpha; bd.ew_rc = ep.rc; bd.ew_kmax = ep.kmax;

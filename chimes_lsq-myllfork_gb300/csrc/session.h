@@ -233,6 +233,11 @@ class Session {
     // and v [natoms_total*3] (device) are advanced in place.  mass_type: host,
     // natmtyp masses.  So_steps [(nsteps+1)*nframes*MD_NSCALAR] and ke_steps
     // [(nsteps+1)*nframes] (device, may be null) receive step 0..nsteps.
+    // Fixed charges (FITCOUL false, ATMCHRG != 0): subtract each frame's Ewald
+    // forces from its force labels (SubtractEwaldForces src/Ewald.C:827-845, called
+    // by process_frame src/chimes_lsq.C:800-801), with the Ewald parameters of the
+    // run's first frame (ZCalc_Ewald keeps them in statics).
+    void subtract_coulomb(FrameBatch& fb);
     void md_nve(DeviceFrames& df, const double* mass_type, double dt, int nsteps, double* v, double* Fo,
                 double* So_steps, double* ke_steps);
     // The same loop with a thermostat (CONSRNT NVT-MTK HOOVER tau / NVT-BEREND tau);

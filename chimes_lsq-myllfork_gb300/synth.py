@@ -234,7 +234,7 @@ def write_xyzf(path, frames, species):
 
 
 def write_fm_setup(path, xyzf_name, nframes, species, masses, order2, order3, order4, smin, smax2, lam,
-                   smax3=None, smax4=None, fitstrs=None, fitener=False, nlayers=1, fitcoul=False):
+                   smax3=None, smax4=None, fitstrs=None, fitener=False, nlayers=1, fitcoul=False, charges=None):
     """fitcoul: fit the Ewald charge products (FITCOUL true, charge signs instead of
     charges, npairs-1 CHARGE CONSTRAINTS lines tying the products together)."""
     lines = ["####### CONTROL VARIABLES #######", "", "# TRJFILE #", f"\t{xyzf_name}", "# WRAPTRJ #", "\ttrue",
@@ -247,8 +247,8 @@ def write_fm_setup(path, xyzf_name, nframes, species, masses, order2, order3, or
     lines += ["# PAIRTYP #", f"\tCHEBYSHEV {order2} {order3} {order4}", "# CHBTYPE #", "\tMORSE", "",
               "####### TOPOLOGY VARIABLES #######", "", "# NATMTYP # ", f"\t{len(species)}", "",
               "# TYPEIDX #\t# ATM_TYP #\t# ATMCHRG #\t# ATMMASS #"]
-    for k, (s, m) in enumerate(zip(species, masses)):
-        chg = ("-" if k == 0 else "+") if fitcoul else "0.0"
+    for k, (s, m) in enumerate(zip(species, masses)):   # charges: fixed charges (Ewald subtraction)
+        chg = ("-" if k == 0 else "+") if fitcoul else (f"{charges[k]}" if charges else "0.0")
         lines.append(f"{k + 1}\t\t{s}\t\t{chg}\t\t{m}")
     lines += ["", "# PAIRIDX #\t# ATM_TY1 #\t# ATM_TY1 #\t# S_MINIM #\t# S_MAXIM #\t# S_DELTA #\t# MORSE_LAMBDA #"]
     k = 1
@@ -330,7 +330,7 @@ def make_workload(name, outdir, nframes=None, seed=1234, labels=True, **over):
     p = os.path.join(outdir, "fm_setup.in")
     write_fm_setup(p, "traj.xyzf", cfg["nframes"], species, masses, o2, o3, o4, cfg["smin"], s2, cfg["lam"],
                    smax3=s3, smax4=s4, fitstrs=cfg["fitstrs"], fitener=cfg["fitener"],
-                   fitcoul=cfg.get("fitcoul", False))
+                   fitcoul=cfg.get("fitcoul", False), charges=cfg.get("charges"))
     return p
 
 

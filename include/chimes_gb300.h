@@ -259,6 +259,13 @@ int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
  * conserved quantity (CONSERVED_QUANT: Q zeta^2 / 2 + N_DOF kB T s; 0 for
  * Berendsen): the run's Econs = kinetic + potential + this term. */
 enum { CG_NVT_MTK = 1, CG_NVT_BEREND = 2 };
+
+/* Fixed charges (FITCOUL false with non-zero ATMCHRG): subtract every frame's Ewald
+ * Coulomb forces from its force labels on the session's GPU (SubtractEwaldForces,
+ * src/Ewald.C:827-845, as process_frame does, src/chimes_lsq.C:800-801), with the
+ * Ewald parameters of the batch's first frame.  A no-op for other models; call it
+ * once on the batch cg_frames_read returned, before reading its labels. */
+int cg_frames_subtract_coulomb(cg_session* s, cg_frames* fr);
 int cg_md_nvt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, int style,
               double temperature, double tau_fs, double* velocities, double* forces, double* scalars_steps,
               double* ke_steps, double* conserved_steps);

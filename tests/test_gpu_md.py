@@ -298,3 +298,36 @@ def test_md_coulomb_matches_reference_run(cg):
         assert abs(kn - tab[s, 2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, tab[s, 2])
         assert abs(vn - tab[s, 3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, tab[s, 3])
         assert abs(p - tab[s, 6]) <= 5e-9 * max(1.0, abs(p)) + 1e-12, (s, p, tab[s, 6])
+
+
+def test_fixed_charge_labels_lose_the_ewald_forces(cg, tmp_path):
+    """Fixed charges (FITCOUL false, O -0.82 / H +0.41): cg_frames_subtract_coulomb
+    removes from each force label the Ewald force that the MD force call (pinned on
+    chimes_md by the Coulomb run above) gives the same frame with zero short-range
+    coefficients.  (The reference chimes_lsq built here faults on this path: its
+    ZCalc_Ewald writes PRESSURE_TENSORS_XYZ_ALL, which the LSQ frames never size.)"""
+    import importlib
+    synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
+    fm = synth.make_workload("water-2b", str(tmp_path), nframes=2, seed=17, nmol=32, L=9.86, order=(8, 0, 0),
+                             charges=[-0.82, 0.41], disp=0.1)
+    model = cg.Model(fm)
+    assert model.params_header().startswith("USECOUL: true")
+    sess = cg.Session(model, 0)
+    fr = cg.Frames.read(model)
+    raw = fr.labels().copy()
+    fr.subtract_coulomb(sess)
+    got = fr.labels()
+    sess.md_setup(np.zeros(model.ncols), penalty_scale=0.0)
+    names = ["O", "H"]
+    nat, types, xyz, cell = synth.frames_arrays(os.path.join(tmp_path, "traj.xyzf"), 2, names)[:4]
+    r0 = 0
+    a0 = 0
+    for k in range(2):
+        n = int(nat[k])
+        one = cg.Frames.from_arrays(model, [n], types[a0:a0 + n], xyz[a0:a0 + n], cell[k:k + 1]).independent()
+        F, _ = sess.md_force(one)
+        expect = raw[r0:r0 + 3 * n] - F.reshape(-1)
+        assert np.allclose(got[r0:r0 + 3 * n], expect, rtol=0, atol=1e-12 * np.abs(F).max())
+        assert np.abs(F).max() > 1.0   # the charges do act
+        r0 += 3 * n
+        a0 += n
