@@ -853,6 +853,7 @@ int oracle_sizes(const char* fm_setup, const char* xyzf, int nframes, int64_t* n
         Box box;
         std::vector<Frame> fr = xyzf ? read_xyzf(m, xyzf, nframes > 0 ? nframes : m.ctl.nframes, 0, box)
                                      : read_frames(m);
+        if (nframes > 0 && (size_t)nframes < fr.size()) fr.resize(nframes);   // the first nframes frames
         int64_t r = 0;
         for (size_t f = 0; f < fr.size(); ++f) r += frame_rows(m, (int)f, fr[f].natoms).total();
         *nrows = r;
@@ -873,6 +874,7 @@ int oracle_assemble(const char* fm_setup, const char* xyzf, int nframes, int fir
         Box box;
         std::vector<Frame> fr = xyzf ? read_xyzf(m, xyzf, nframes > 0 ? nframes : m.ctl.nframes, 0, box)
                                      : read_frames(m);
+        if (nframes > 0 && (size_t)nframes < fr.size()) fr.resize(nframes);   // the first nframes frames
         if (count <= 0) count = (int)fr.size() - first;
         std::vector<int64_t> ofs(count + 1, 0);
         std::vector<char> small(count, 0);
