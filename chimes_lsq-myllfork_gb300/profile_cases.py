@@ -2,7 +2,7 @@
 
     python chimes_lsq-myllfork_gb300/profile_cases.py gram [nframes]        # split-BF16 Gram of water-3b A
     python chimes_lsq-myllfork_gb300/profile_cases.py md NATOMS PRECISION   # MD force of one 4-body system
-    python chimes_lsq-myllfork_gb300/profile_cases.py assemble [nframes]    # FP64 A of water-3b frames
+    python chimes_lsq-myllfork_gb300/profile_cases.py assemble [nframes] [fp32]  # A of water-3b frames
     python chimes_lsq-myllfork_gb300/profile_cases.py serve NATOMS PRECISION NSTEPS  # one NVE request, stage times
 
 Each case runs its launch twice after the set-up, so `ncu -k regex:<kernel> -c 1`
@@ -33,8 +33,9 @@ def main(argv):
         nrows, _ = fr.rows()
         ncols = model.ncols
         dfr = sess.upload(fr)
-        prec = cg.CG_FP32 if case == "gram" else cg.CG_FP64
-        A = torch.empty((nrows, ncols), dtype=torch.float32 if case == "gram" else torch.float64, device="cuda")
+        fp32 = case == "gram" or (len(argv) > 2 and argv[2] == "fp32")
+        prec = cg.CG_FP32 if fp32 else cg.CG_FP64
+        A = torch.empty((nrows, ncols), dtype=torch.float32 if fp32 else torch.float64, device="cuda")
         for _ in range(1 if case == "gram" else 2):
             sess.assemble_device(dfr, prec, A.data_ptr(), ncols)
         if case == "gram":
