@@ -39,15 +39,17 @@ __device__ __forceinline__ void role_slots(int NB, int pi, int* I, int* O) {
     }
 }
 
-// Basis of the edge that maps to canonical slot s of cluster q: g, h (ord values each),
-// the edge's unit vector oriented first->second actual member, and stress factors.
+// Basis of the edge that maps to canonical slot s of cluster q: g, h (ord values each,
+// in the compute type T), the edge's vector oriented first->second actual member, and
+// its length.  The distance and cut-off are FP64 in both forms.
 struct SlotBasis {
     int e, ma, mb;
     double r, rab[3];
 };
 
+template <typename TC>
 __device__ void slot_basis(const ModelDev& M, const FramesDev& F, int NB, int f, int4 mem, int id, int T,
-                           int s, int ord, double* g, double* h, SlotBasis& sb) {
+                           int s, int ord, TC* g, TC* h, SlotBasis& sb) {
     const int np = NB == 3 ? 3 : 6;
     const int8_t* pm = (NB == 3 ? M.pidx3 : M.pidx4) + id * np;
     int e = 0;
@@ -65,7 +67,7 @@ __device__ void slot_basis(const ModelDev& M, const FramesDev& F, int NB, int f,
     const int pt = M.int_pair_map[typ[ga % N] * M.natmtyp + typ[gbm % N]];
     double fc, fd;
     fcut_eval(M, sb.r, CT.smax[s], fc, fd);
-    basis_gh(M, M.pairs[pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], sb.r, 0, ord, fc, fd, g, h, 1);
+    basis_gh_t<TC>(M, M.pairs[pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], sb.r, 0, ord, fc, fd, g, h, 1);
 }
 
 // ---------------------------------------------------------------- 2-body force rows
@@ -224,8 +226,8 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
     int* sCnt = reinterpret_cast<int*>(smem_raw + L.cnt);
     int* sQ = reinterpret_cast<int*>(smem_raw + L.q);
     int* sPi = reinterpret_cast<int*>(smem_raw + L.pi);
-    double* sGH = reinterpret_cast<double*>(smem_raw + L.gh);
-    double* sW = reinterpret_cast<double*>(smem_raw + L.w);
+    R* sGH = reinterpret_cast<R*>(smem_raw + L.gh);
+    R* sW = reinterpret_cast<R*>(smem_raw + L.w);
     R* sTab = reinterpret_cast<R*>(smem_raw + L.tab);
 
     const int gatom = blockIdx.x;
@@ -322,14 +324,14 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
                         int id = 0, w = 1;
                         for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
                         SlotBasis sb;
-                        double* g = sGH + ((size_t)c * NP + s) * 2 * ord;
-                        slot_basis(M, F, NBODY, f, mm, id, T, s, ord, g, g + ord, sb);
+                        R* g = sGH + ((size_t)c * NP + s) * 2 * ord;
+                        slot_basis<R>(M, F, NBODY, f, mm, id, T, s, ord, g, g + ord, sb);
                         const int m = sPi[c];
                         const double sg = (m == sb.ma) ? 1.0 : ((m == sb.mb) ? -1.0 : 0.0);
                         const double ir = sg / sb.r;
-                        const double wx = sb.rab[0] * ir, wy = sb.rab[1] * ir, wz = sb.rab[2] * ir;
-                        double* hw = sW + ((size_t)c * NP + s) * 3 * ord;   // h_s[n] * w_s,{x,y,z}
-                        const double* h = g + ord;
+                        const R wx = R(sb.rab[0] * ir), wy = R(sb.rab[1] * ir), wz = R(sb.rab[2] * ir);
+                        R* hw = sW + ((size_t)c * NP + s) * 3 * ord;   // h_s[n] * w_s,{x,y,z}
+                        const R* h = g + ord;
                         for (int n = 0; n < ord; ++n) { hw[n] = h[n] * wx; hw[ord + n] = h[n] * wy; hw[2 * ord + n] = h[n] * wz; }
                     }
                     __syncthreads();
@@ -337,28 +339,28 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
                     const int nzt = sizeI + sizeO;   // M entries (x,y,z written together) + Q entries
                     for (int t = threadIdx.x; t < nb * nzt; t += blockDim.x) {
                         const int c = t / nzt, z = t % nzt;
-                        const double* GH = sGH + (size_t)c * NP * 2 * ord;
-                        const double* HW = sW + (size_t)c * NP * 3 * ord;
+                        const R* GH = sGH + (size_t)c * NP * 2 * ord;
+                        const R* HW = sW + (size_t)c * NP * 3 * ord;
                         R* tab = sTab + (size_t)c * per;
                         if (z < sizeI) {
                             int pwr[3] = {0, 0, 0}, zz = z;
                             for (int u = 0; u < NI; ++u) { pwr[u] = zz % ord; zz /= ord; }
-                            double gs[3];
+                            R gs[3];
                             for (int u = 0; u < NI; ++u) gs[u] = GH[(size_t)I[u] * 2 * ord + pwr[u]];
-                            double other[3];   // product of the other incident slots' g
+                            R other[3];   // product of the other incident slots' g
                             if (NI == 2) { other[0] = gs[1]; other[1] = gs[0]; }
                             else { other[0] = gs[1] * gs[2]; other[1] = gs[0] * gs[2]; other[2] = gs[0] * gs[1]; }
-                            double mx = 0, my = 0, mz = 0;
+                            R mx = 0, my = 0, mz = 0;
                             for (int u = 0; u < NI; ++u) {
-                                const double* hw = HW + (size_t)I[u] * 3 * ord + pwr[u];
+                                const R* hw = HW + (size_t)I[u] * 3 * ord + pwr[u];
                                 mx += hw[0] * other[u]; my += hw[ord] * other[u]; mz += hw[2 * ord] * other[u];
                             }
-                            tab[z] = R(mx); tab[sizeI + z] = R(my); tab[2 * sizeI + z] = R(mz);
+                            tab[z] = mx; tab[sizeI + z] = my; tab[2 * sizeI + z] = mz;
                         } else {
                             int zz = z - sizeI;
-                            double prod = 1.0;
+                            R prod = R(1);
                             for (int u = 0; u < NO; ++u) { prod *= GH[(size_t)O[u] * 2 * ord + zz % ord]; zz /= ord; }
-                            tab[3 * sizeI + (z - sizeI)] = R(prod);
+                            tab[3 * sizeI + (z - sizeI)] = prod;
                         }
                     }
                     __syncthreads();
@@ -445,8 +447,8 @@ __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev 
     role_slots(NBODY, 0, S1, S2);
     const MbVirSmem L = mb_vir_smem(NBODY, ord, PPT * MB_THREADS, (int)sizeof(R));
     int* sQ = reinterpret_cast<int*>(smem_raw + L.q);
-    double* sGH = reinterpret_cast<double*>(smem_raw + L.gh);
-    double* sV = reinterpret_cast<double*>(smem_raw + L.v);
+    R* sGH = reinterpret_cast<R*>(smem_raw + L.gh);
+    R* sV = reinterpret_cast<R*>(smem_raw + L.v);
     R* sTab = reinterpret_cast<R*>(smem_raw + L.tab);
 
     int i1[PPT], i2[PPT];
@@ -476,12 +478,12 @@ __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev 
             int id = 0, w = 1;
             for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
             SlotBasis sb;
-            double* g = sGH + ((size_t)c * NP + s) * 2 * ord;
-            slot_basis(M, F, NBODY, f, mm, id, T, s, ord, g, g + ord, sb);
-            double* v = sV + ((size_t)c * NP + s) * 6;
+            R* g = sGH + ((size_t)c * NP + s) * 2 * ord;
+            slot_basis<R>(M, F, NBODY, f, mm, id, T, s, ord, g, g + ord, sb);
+            R* v = sV + ((size_t)c * NP + s) * 6;
             const double* x = sb.rab;
-            v[0] = x[0] * x[0] / sb.r; v[1] = x[1] * x[1] / sb.r; v[2] = x[2] * x[2] / sb.r;
-            v[3] = x[0] * x[1] / sb.r; v[4] = x[0] * x[2] / sb.r; v[5] = x[1] * x[2] / sb.r;
+            v[0] = R(x[0] * x[0] / sb.r); v[1] = R(x[1] * x[1] / sb.r); v[2] = R(x[2] * x[2] / sb.r);
+            v[3] = R(x[0] * x[1] / sb.r); v[4] = R(x[0] * x[2] / sb.r); v[5] = R(x[1] * x[2] / sb.r);
         }
         __syncthreads();
         for (int t = threadIdx.x; t < nb * (size1 + size2); t += blockDim.x) {
@@ -491,21 +493,21 @@ __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev 
             const int* S = first ? S1 : S2;
             const int ns = first ? N1 : N2;
             if (!first) z -= size1;
-            const double* GH = sGH + (size_t)c * NP * 2 * ord;
-            const double* V = sV + (size_t)c * NP * 6;
+            const R* GH = sGH + (size_t)c * NP * 2 * ord;
+            const R* V = sV + (size_t)c * NP * 6;
             int pwr[3] = {0, 0, 0}, zz = z;
             for (int u = 0; u < ns; ++u) { pwr[u] = zz % ord; zz /= ord; }
-            double q = 1.0, av[6] = {0, 0, 0, 0, 0, 0};
+            R q = R(1), av[6] = {0, 0, 0, 0, 0, 0};
             for (int u = 0; u < ns; ++u) q *= GH[(size_t)S[u] * 2 * ord + pwr[u]];
             for (int u = 0; u < ns; ++u) {
-                double prod = GH[(size_t)S[u] * 2 * ord + ord + pwr[u]];
+                R prod = GH[(size_t)S[u] * 2 * ord + ord + pwr[u]];
                 for (int v2 = 0; v2 < ns; ++v2) if (v2 != u) prod *= GH[(size_t)S[v2] * 2 * ord + pwr[v2]];
                 for (int k = 0; k < 6; ++k) av[k] += prod * V[S[u] * 6 + k];
             }
             R* tab = sTab + (size_t)c * per + (first ? 0 : 7 * size1);
             const int sz = first ? size1 : size2;
-            tab[z] = R(q);
-            for (int k = 0; k < 6; ++k) tab[(1 + k) * sz + z] = R(av[k]);
+            tab[z] = q;
+            for (int k = 0; k < 6; ++k) tab[(1 + k) * sz + z] = av[k];
         }
         __syncthreads();
         for (int c = 0; c < nb; ++c) {

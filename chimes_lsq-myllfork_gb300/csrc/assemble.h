@@ -30,8 +30,8 @@ __host__ __device__ inline MbForceSmem mb_force_smem(int nbody, int ord, int nke
     s.q = align16(s.cnt + (nkeys + 1) * sizeof(int));
     s.pi = align16(s.q + MB_CB * sizeof(int));
     s.gh = align16(s.pi + MB_CB * sizeof(int));
-    s.w = align16(s.gh + (size_t)MB_CB * np * 2 * ord * sizeof(double));
-    s.tab = align16(s.w + (size_t)MB_CB * np * 3 * ord * sizeof(double));
+    s.w = align16(s.gh + (size_t)MB_CB * np * 2 * ord * rsize);
+    s.tab = align16(s.w + (size_t)MB_CB * np * 3 * ord * rsize);
     size_t tab = (size_t)MB_CB * per;
     if ((size_t)max_allowed * 3 > tab) tab = (size_t)max_allowed * 3;
     s.total = align16(s.tab + tab * rsize);
@@ -50,8 +50,8 @@ __host__ __device__ inline MbVirSmem mb_vir_smem(int nbody, int ord, int pchunk,
     MbVirSmem s;
     s.q = 0;
     s.gh = align16(MB_CB * sizeof(int));
-    s.v = align16(s.gh + (size_t)MB_CB * np * 2 * ord * sizeof(double));
-    s.tab = align16(s.v + (size_t)MB_CB * np * 6 * sizeof(double));
+    s.v = align16(s.gh + (size_t)MB_CB * np * 2 * ord * rsize);
+    s.tab = align16(s.v + (size_t)MB_CB * np * 6 * rsize);
     size_t tab = (size_t)MB_CB * per;
     if ((size_t)pchunk * 7 > tab) tab = (size_t)pchunk * 7;
     s.total = align16(s.tab + tab * rsize);

@@ -62,6 +62,60 @@ __device__ __forceinline__ void basis_gh(const ModelDev& M, double lambda, doubl
     }
 }
 
+// basis_gh with the recursion in the compute type T: the argument x, dx/dr and the
+// out-of-range factors are formed in FP64 (one exp per edge), the per-power
+// recursion and products in T.  For T = double this is basis_gh itself.
+template <typename T>
+__device__ __forceinline__ void basis_gh_t(const ModelDev& M, double lambda, double xavg, double xdiff, double smin,
+                                           double r, int n0, int count, double fc, double fd, T* g, T* h,
+                                           int stride) {
+    if constexpr (sizeof(T) == 8) {
+        basis_gh(M, lambda, xavg, xdiff, smin, r, n0, count, fc, fd, g, h, stride);
+    } else {
+        const bool out = r < smin;
+        const double rr = out ? smin : r;
+        double xd, ex = 0.0;
+        const double ixd = 1.0 / xdiff;
+        if (M.trans == 0) { ex = exp(-rr / lambda); xd = (ex - xavg) * ixd; }
+        else if (M.trans == 1) { xd = (1.0 / rr - xavg) * ixd; }
+        else { xd = (rr - xavg) * ixd; }
+        double dxdr_d;
+        if (M.trans == 0) dxdr_d = -ex / lambda * ixd;
+        else if (M.trans == 1) dxdr_d = -ixd / (rr * rr);
+        else dxdr_d = ixd;
+        dxdr_d *= M.deriv_const;
+        const bool zero_d = out && M.fix == 1;
+        double damp_d = 1.0, shift_d = 0.0;
+        if (out && M.fix == 0) { damp_d = exp((r - smin) / M.smooth); shift_d = M.smooth * (damp_d - 1.0); }
+        const T x = T(xd), dxdr = T(dxdr_d), damp = T(damp_d), shift = T(shift_d);
+        const T lin = T((out && M.fix == 2) ? (r - smin) : 0.0);
+        const T tfc = T(fc), tfd = T(fd);
+        T t_prev = T(1), t_cur = x, u_prev2 = T(0), u_prev = T(1);
+        const int n1 = n0 + count;
+        for (int n = 0; n < n1; ++n) {
+            T tn, un_1;
+            if (n == 0) { tn = T(1); un_1 = T(0); }
+            else if (n == 1) { tn = x; un_1 = T(1); }
+            else {
+                tn = T(2) * x * t_cur - t_prev;
+                t_prev = t_cur; t_cur = tn;
+                const T un = (n - 1 == 1) ? T(2) * x : T(2) * x * u_prev - u_prev2;
+                u_prev2 = u_prev; u_prev = un;
+                un_1 = un;
+            }
+            T td = (n == 0 || zero_d) ? T(0) : T(n) * dxdr * un_1;
+            if (out) {
+                if (M.fix == 0) { tn += shift * td; td *= damp; }
+                else if (M.fix == 2) tn += td * lin;
+            }
+            if (n >= n0) {
+                g[(n - n0) * stride] = tfc * tn;
+                h[(n - n0) * stride] = tfc * td + tfd * tn;
+            }
+        }
+    }
+}
+
 // FCUT::get_fcut src/Fcut.C:17-72
 __device__ __forceinline__ void fcut_eval(const ModelDev& M, double r, double rmax, double& f, double& fd) {
     if (M.fcut == 0) {
