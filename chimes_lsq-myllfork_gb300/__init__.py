@@ -70,6 +70,7 @@ def lib():
         "cg_model_params_text": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t,
                                                 ctypes.POINTER(ctypes.c_size_t)]),
         "cg_frames_read": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int, pp]),
+        "cg_frames_read_ranks": (ctypes.c_int, [vp, ctypes.c_int, pp]),
         "cg_frames_create": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, pp]),
         "cg_frames_free": (None, [vp]),
         "cg_frames_rows": (ctypes.c_int, [vp, i64p, i64p]),
@@ -231,8 +232,15 @@ class Frames:
         self.model = model
 
     @classmethod
-    def read(cls, model, xyzf_path=None, nframes=0):
+    def read(cls, model, xyzf_path=None, nframes=0, nprocs=None):
+        """The model's trajectory (or nframes of xyzf_path).  nprocs: the frames and
+        output order of `chimes_lsq` run on that many ranks (SKPFRMS, SPLITFI)."""
         h = ctypes.c_void_p()
+        if nprocs is not None:
+            if xyzf_path is not None or nframes:
+                raise ValueError("nprocs reads the model's own trajectory")
+            _check(lib().cg_frames_read_ranks(model._h, int(nprocs), ctypes.byref(h)))
+            return cls(h, model)
         p = None if xyzf_path is None else os.fspath(xyzf_path).encode()
         _check(lib().cg_frames_read(model._h, p, int(nframes), ctypes.byref(h)))
         return cls(h, model)
@@ -271,9 +279,13 @@ class Frames:
         return self
 
     def write_lsq_files(self, A, directory):
-        """A.txt / b.txt / b-labeled.txt / natoms.txt / dim.txt for these frames (A: host FP64)."""
-        A = np.ascontiguousarray(A, dtype=np.float64)
-        _check(lib().cg_write_lsq_files(self.model._h, self._h, _ptr(A), A.shape[1], os.fspath(directory).encode()))
+        """A.txt / b.txt / b-labeled.txt / natoms.txt / dim.txt for these frames (A: host
+        FP64; None writes all but the A files).  SPLITFI models: A.%04d.txt / dim.%04d.txt."""
+        lda = 0
+        if A is not None:
+            A = np.ascontiguousarray(A, dtype=np.float64)
+            lda = A.shape[1]
+        _check(lib().cg_write_lsq_files(self.model._h, self._h, _ptr(A), lda, os.fspath(directory).encode()))
 
     def independent(self):
         """Each frame decides the small-cell convention alone (MD systems)."""

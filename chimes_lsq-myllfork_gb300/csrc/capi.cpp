@@ -150,7 +150,7 @@ int cg_frames_read(const cg_model* h, const char* path, int nframes, cg_frames**
         need(h && out, "model/out");
         std::vector<cg::Frame> frames;
         if (!path && nframes <= 0) {
-            frames = cg::read_frames(h->m);
+            frames = cg::read_frames(h->m, 1);
         } else {
             std::string p = path ? std::string(path) : h->m.ctl.infile.at(0);
             if (!path && !p.empty() && p[0] != '/') p = h->m.dir + "/" + p;
@@ -159,6 +159,16 @@ int cg_frames_read(const cg_model* h, const char* path, int nframes, cg_frames**
         }
         std::unique_ptr<cg_frames> f(new cg_frames());
         f->fb = cg::make_batch(h->m, frames, 0);
+        *out = f.release();
+    });
+}
+
+int cg_frames_read_ranks(const cg_model* h, int nprocs, cg_frames** out) {
+    return guarded([&] {
+        need(h && out && nprocs >= 1, "model/out/nprocs");
+        std::vector<cg::Frame> frames = cg::read_frames(h->m, nprocs);
+        std::unique_ptr<cg_frames> f(new cg_frames());
+        f->fb = cg::make_batch(h->m, frames, 0, nprocs);
         *out = f.release();
     });
 }
@@ -213,8 +223,8 @@ int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms) {
 
 int cg_write_lsq_files(const cg_model* h, const cg_frames* fr, const double* A, int64_t lda, const char* dir) {
     return guarded([&] {
-        need(h && fr && A && dir, "model/frames/A/dir");
-        need(lda >= h->m.tot_all, "lda");
+        need(h && fr && dir, "model/frames/dir");
+        need(!A || lda >= h->m.tot_all, "lda");
         cg::write_lsq_files(h->m, fr->fb, A, lda, dir);
     });
 }

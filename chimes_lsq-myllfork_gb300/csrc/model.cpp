@@ -1116,6 +1116,7 @@ std::vector<Frame> read_xyzf(const Model& m, const std::string& path, int nframe
     for (int f = 0; f < nframes; ++f) {
         const int fi = first_index + f;
         Frame fr;
+        fr.index = fi;
         if (!(in >> fr.natoms)) throw Error(2, "unexpected end of trajectory at frame " + std::to_string(fi));
         std::string header;
         std::getline(in, header);
@@ -1173,7 +1174,28 @@ std::vector<Frame> read_xyzf(const Model& m, const std::string& path, int nframe
     return out;
 }
 
-std::vector<Frame> read_frames(const Model& m) {
+std::vector<std::vector<int>> rank_frames(const Controls& c, int nprocs) {
+    if (nprocs < 1) throw Error(1, "the rank count must be at least 1");
+    std::vector<std::vector<int>> out(nprocs);
+    const int n = c.nframes;
+    for (int r = 0; r < nprocs; ++r) {
+        if (c.skip_frames >= 1) {
+            for (int i = 0; i < n; ++i)
+                if ((i + r) % nprocs == 0 && ((i + r) / nprocs) % c.skip_frames == 0) out[r].push_back(i);
+            continue;
+        }
+        if (n <= 0) continue;
+        const int used = nprocs <= n ? nprocs : n;
+        int beg = (int)std::ceil((double)r * n / used), end;
+        if (r > n) { beg = n + 1; end = n - 1; }
+        else if (r == used - 1) end = n - 1;
+        else end = std::min((int)std::ceil((double)(r + 1) * n / used) - 1, n - 1);
+        for (int i = beg; i <= end; ++i) out[r].push_back(i);
+    }
+    return out;
+}
+
+std::vector<Frame> read_frames(const Model& m, int nprocs) {
     // NFRAMES frames in file order (chimes_lsq.C:263-300: the next file opens when
     // a file's INFILE_FRAMES are used up); one SYSTEM box carries across files
     const Controls& c = m.ctl;
@@ -1190,7 +1212,12 @@ std::vector<Frame> read_frames(const Model& m) {
         done += n;
     }
     if (done < c.nframes) throw Error(2, "the trajectory files hold fewer than NFRAMES frames");
-    return all;
+    if (nprocs == 1 && c.skip_frames <= 0) return all;
+    std::vector<Frame> out;
+    const std::vector<std::vector<int>> sched = rank_frames(c, nprocs);
+    for (int r = 0; r < nprocs; ++r)
+        for (int i : sched[r]) { out.push_back(all[i]); out.back().rank = r; }
+    return out;
 }
 
 RowLayout frame_rows(const Model& m, int fi, int natoms) {

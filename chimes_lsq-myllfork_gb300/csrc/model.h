@@ -168,10 +168,19 @@ struct Frame {
     double stress_off[3] = {0, 0, 0};    // xy xz yz (GPa, as read)
     double energy = 0.0;
     int file = 0;                     // index of the TRJFILE the frame came from (label flags)
+    int index = -1;                   // frame number in the trajectory (NSTRESS / NENER cut-offs)
+    int rank = 0;                     // chimes_lsq rank that writes the frame (output order, SPLITFI)
 };
 
-// Read all NFRAMES frames of the model's trajectory file(s).
-std::vector<Frame> read_frames(const Model& m);
+// Frames that each of nprocs chimes_lsq ranks processes, in rank order: contiguous
+// blocks (divide_atoms, src/functions.C:182-222) or, with SKPFRMS n >= 1, frame i on
+// rank r when (i + r) % nprocs == 0 and ((i + r) / nprocs) % n == 0
+// (src/chimes_lsq.C:305-317).  The ranks' files are concatenated in rank order.
+std::vector<std::vector<int>> rank_frames(const Controls& c, int nprocs);
+
+// Read the NFRAMES frames of the model's trajectory file(s) and keep the ones
+// chimes_lsq on nprocs ranks would process, in the order of its output files.
+std::vector<Frame> read_frames(const Model& m, int nprocs = 1);
 // Read frames from one stream (exposed for tests and the C ABI).
 std::vector<Frame> read_xyzf(const Model& m, const std::string& path, int nframes, int first_index,
                              Box& persistent_box);

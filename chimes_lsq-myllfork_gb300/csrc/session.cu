@@ -166,6 +166,7 @@ FrameBatch slice_batch(const FrameBatch& fb, int first, int count) {
     FrameBatch o;
     o.nframes = count;
     o.first_index = fb.first_index + first;
+    o.nprocs = fb.nprocs;
     o.atom_ofs.push_back(0); o.ghost_ofs.push_back(0); o.row_ofs.push_back(0);
     const int64_t nimg = fb.natoms.empty() ? 1 : (fb.ghost_ofs[1] - fb.ghost_ofs[0]) / std::max(1, fb.natoms[0]);
     for (int k = first; k < first + count; ++k) {
@@ -176,6 +177,7 @@ FrameBatch slice_batch(const FrameBatch& fb, int first, int count) {
         o.box.push_back(fb.box[k]);
         o.small_self.push_back(fb.small_self[k]);
         o.file.push_back(k < (int)fb.file.size() ? fb.file[k] : 0);
+        o.rank.push_back(k < (int)fb.rank.size() ? fb.rank[k] : 0);
         o.atom_ofs.push_back(o.atom_ofs.back() + n);
         o.ghost_ofs.push_back(o.ghost_ofs.back() + nimg * n);
         const int64_t rows = fb.row_ofs[k + 1] - fb.row_ofs[k];
@@ -194,17 +196,20 @@ void make_independent(FrameBatch& fb) {
     for (int k = 0; k < fb.nframes; ++k) set_small(fb.box[k], fb.small_self[k] != 0);
 }
 
-FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int first_index) {
+FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int first_index, int nprocs) {
     FrameBatch fb;
     fb.nframes = (int)frames.size();
     fb.first_index = first_index;
+    fb.nprocs = nprocs;
     const int L = m.ctl.nlayers;
     const int nimg = (2 * L + 1) * (2 * L + 1) * (2 * L + 1);
     fb.atom_ofs.push_back(0); fb.ghost_ofs.push_back(0); fb.row_ofs.push_back(0);
     bool small = false;
     for (int k = 0; k < fb.nframes; ++k) {
         const Frame& fr = frames[k];
-        const int fi = first_index + k;
+        const int fi = fr.index >= 0 ? fr.index : first_index + k;
+        if (fr.rank < 0 || fr.rank >= nprocs) throw Error(1, "frame rank outside the run's rank count");
+        if (k > 0 && fr.rank != frames[k - 1].rank) small = false;   // each rank has its own neighbour lists
         if (fr.natoms <= 0) throw Error(2, "frame with no atoms");
         if (fr.natoms > 8191) throw Error(2, "frames above 8191 atoms are not supported on the device");
         RowLayout rl = frame_rows(m, fi, fr.natoms);
@@ -217,6 +222,7 @@ FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int firs
         small = frame_is_small(m, fr.box, small);
         fb.small_self.push_back(frame_is_small(m, fr.box, false) ? 1 : 0);
         fb.file.push_back(fr.file);
+        fb.rank.push_back(fr.rank);
         cgd::BoxDev bd;
         std::memset(&bd, 0, sizeof(bd));
         for (int q = 0; q < 9; ++q) { bd.h[q] = fr.box.hmat[q]; bd.inv[q] = fr.box.invr[q]; }

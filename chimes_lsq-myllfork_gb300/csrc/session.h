@@ -39,10 +39,14 @@ struct FrameBatch {
     std::vector<double> b;        // labels in A row order (src/A_Matrix.C:294-553)
     std::vector<char> small_self; // each frame's own small-cell test (no carry-over)
     std::vector<int> file;        // trajectory file of each frame (b-labeled.txt flags)
+    std::vector<int> rank;        // chimes_lsq rank whose output files hold the frame
+    int nprocs = 1;               // ranks of that emulated run
     int64_t nrows = 0, natoms_total = 0, nghosts = 0;
 };
 
-FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int first_index);
+// Frames carry their trajectory index (NSTRESS / NENER) when they have one, else
+// first_index + position; nprocs is the rank count of an emulated chimes_lsq run.
+FrameBatch make_batch(const Model& m, const std::vector<Frame>& frames, int first_index, int nprocs = 1);
 // The small-cell convention is sticky along a trajectory (the fit reads frames in
 // sequence); independent configurations (MD systems) each decide it alone.
 void make_independent(FrameBatch& fb);

@@ -4,7 +4,9 @@
 #include "textio.h"
 
 #include <cstdio>
+#include <algorithm>
 #include <fstream>
+#include <memory>
 #include <sstream>
 #include <vector>
 
@@ -32,77 +34,122 @@ struct Out {
 // FITCOUL: force rows carry the charge columns after the short-range ones, and the
 // charge-constraint rows follow the last frame ("0.0 " short-range, then the values).
 // natoms.txt has the frame's atom count per row; dim.txt "columns rows".
+// Frames of an emulated multi-rank run are written in rank order (the reference
+// concatenates its per-rank files); with SPLITFI the A rows stay in A.%04d.txt per
+// rank with data and dim.%04d.txt holds "columns first-row last-row total".
+// A == nullptr writes the label files and dimensions only.
 void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int64_t lda, const std::string& dir,
                      bool with_constraints) {
     const int C = m.tot_short;
     const int nener = m.tot_all - m.tot_short - m.ncoul;
     const bool do_ener = nener > 0;
-    Out fa(dir + "/A.txt"), fbv(dir + "/b.txt"), fbl(dir + "/b-labeled.txt"), fna(dir + "/natoms.txt");
-    int64_t row = 0;
+    const int nprocs = std::max(1, fb.nprocs);
+    const bool split = m.ctl.split_files;
+    auto rank_of = [&](int f) { return f < (int)fb.rank.size() ? fb.rank[f] : 0; };
+    for (int f = 1; f < fb.nframes; ++f)
+        if (rank_of(f) < rank_of(f - 1)) throw Error(1, "frames are not in rank order");
+    const bool constraints = with_constraints && !m.charge_constraints.empty();
+    // rows per rank; the constraint rows go to the first rank without data when the
+    // files stay split, else to the last rank (A_MAT::PRINT_CONSTRAINTS :570-604)
+    std::vector<int64_t> count(nprocs, 0);
+    for (int f = 0; f < fb.nframes; ++f) count[rank_of(f)] += fb.row_ofs[f + 1] - fb.row_ofs[f];
+    int print_rank = nprocs - 1;
+    if (split)
+        for (int r = 0; r < nprocs; ++r) if (count[r] == 0) { print_rank = r; break; }
+    if (constraints) count[print_rank] += (int64_t)m.charge_constraints.size();
+    Out fbv(dir + "/b.txt"), fbl(dir + "/b-labeled.txt"), fna(dir + "/natoms.txt");
+    std::unique_ptr<Out> fa;
+    if (A && !split) fa.reset(new Out(dir + "/A.txt"));
     auto flag = [&](const std::vector<std::string>& v, int f) -> const char* {   // INFILE_*_FLAGS[my_file]
         const int k = f < (int)fb.file.size() ? fb.file[f] : 0;
         return k < (int)v.size() ? v[k].c_str() : "";
     };
-    for (int f = 0; f < fb.nframes; ++f) {
-        const int N = fb.natoms[f];
-        const int64_t a0 = fb.atom_ofs[f];
-        std::vector<int> count(m.ctl.natmtyp, 0);
-        for (int a = 0; a < N; ++a) count[fb.type[a0 + a]]++;
-        auto tail = [&](bool energy) {
-            if (do_ener)
-                for (int t = 0; t < m.ctl.natmtyp; ++t) {
-                    if (energy) std::fprintf(fa.f, " %d", count[t]);
-                    else fa.s(" 0.0");
+    int64_t total = 0;
+    for (int r = 0; r < nprocs; ++r) total += count[r];
+    int64_t start = 0;
+    int f = 0;
+    for (int r = 0; r < nprocs; ++r) {
+        char name[64];
+        if (A && split && count[r] > 0) {
+            std::snprintf(name, sizeof(name), "/A.%04d.txt", r);
+            fa.reset(new Out(dir + name));
+        }
+        for (; f < fb.nframes && rank_of(f) == r; ++f) {
+            const int N = fb.natoms[f];
+            const int64_t a0 = fb.atom_ofs[f];
+            std::vector<int> natyp(m.ctl.natmtyp, 0);
+            for (int a = 0; a < N; ++a) natyp[fb.type[a0 + a]]++;
+            auto row_out = [&](int64_t r_, int ncols, const char* sep, bool energy) {
+                if (fa) {
+                    const double* Ar = A + r_ * lda;
+                    for (int c = 0; c < ncols; ++c) { fa->num(Ar[c]); fa->s(sep); }
+                    if (do_ener)
+                        for (int t = 0; t < m.ctl.natmtyp; ++t) {
+                            if (energy) std::fprintf(fa->f, " %d", natyp[t]);
+                            else fa->s(" 0.0");
+                        }
+                    fa->s("\n");
                 }
-            std::fprintf(fna.f, "%d\n", N);
-            fa.s("\n");
-        };
-        const int64_t r0 = fb.row_ofs[f];
-        for (int a = 0; a < N; ++a) {
-            for (int q = 0; q < 3; ++q, ++row) {
-                const double* Ar = A + (r0 + 3 * a + q) * lda;
-                for (int c = 0; c < C + m.ncoul; ++c) { fa.num(Ar[c]); fa.s("   "); }   // + charge columns
-                tail(false);
-                const double bv = fb.b[r0 + 3 * a + q];
-                fbv.num(bv); fbv.s("\n");
-                fbl.s(flag(m.ctl.force_flags, f)); fbl.s(m.atom_types[fb.type[a0 + a]].c_str()); fbl.s(" ");
-                fbl.lab(bv); fbl.s("\n");
+                std::fprintf(fna.f, "%d\n", N);
+            };
+            const int64_t r0 = fb.row_ofs[f];
+            for (int a = 0; a < N; ++a) {
+                for (int q = 0; q < 3; ++q) {
+                    row_out(r0 + 3 * a + q, C + m.ncoul, "   ", false);   // + charge columns
+                    const double bv = fb.b[r0 + 3 * a + q];
+                    fbv.num(bv); fbv.s("\n");
+                    fbl.s(flag(m.ctl.force_flags, f)); fbl.s(m.atom_types[fb.type[a0 + a]].c_str()); fbl.s(" ");
+                    fbl.lab(bv); fbl.s("\n");
+                }
+            }
+            const int srows = fb.stress_rows[f], erows = fb.energy_rows[f];
+            static const char* l3[3] = {"s_xx ", "s_yy ", "s_zz "};
+            static const char* l9[9] = {"s_xx ", "s_xy ", "s_xz ", "s_yx ", "s_yy ", "s_yz ", "s_zx ", "s_zy ", "s_zz "};
+            for (int k = 0; k < srows; ++k) {
+                const int64_t rr = r0 + 3 * N + k;
+                row_out(rr, C, " ", false);
+                fbv.num(fb.b[rr]); fbv.s("\n");
+                fbl.s(flag(m.ctl.stress_flags, f)); fbl.s(srows == 3 ? l3[k] : l9[k]); fbl.lab(fb.b[rr]); fbl.s("\n");
+            }
+            for (int k = 0; k < erows; ++k) {
+                const int64_t rr = r0 + 3 * N + srows + k;
+                row_out(rr, C, " ", true);
+                fbv.num(fb.b[rr]); fbv.s("\n");
+                fbl.s(flag(m.ctl.energy_flags, f)); fbl.s("+1 "); fbl.lab(fb.b[rr]); fbl.s("\n");
             }
         }
-        const int srows = fb.stress_rows[f], erows = fb.energy_rows[f];
-        static const char* l3[3] = {"s_xx ", "s_yy ", "s_zz "};
-        static const char* l9[9] = {"s_xx ", "s_xy ", "s_xz ", "s_yx ", "s_yy ", "s_yz ", "s_zx ", "s_zy ", "s_zz "};
-        for (int k = 0; k < srows; ++k, ++row) {
-            const int64_t r = r0 + 3 * N + k;
-            const double* Ar = A + r * lda;
-            for (int c = 0; c < C; ++c) { fa.num(Ar[c]); fa.s(" "); }
-            tail(false);
-            fbv.num(fb.b[r]); fbv.s("\n");
-            fbl.s(flag(m.ctl.stress_flags, f)); fbl.s(srows == 3 ? l3[k] : l9[k]); fbl.lab(fb.b[r]); fbl.s("\n");
+        if (constraints && r == print_rank) {   // A_MAT::PRINT_CONSTRAINTS src/A_Matrix.C:606-623
+            if (A && split && !fa) {
+                std::snprintf(name, sizeof(name), "/A.%04d.txt", r);
+                fa.reset(new Out(dir + name));
+            }
+            const int np = (int)m.pairs.size();
+            for (const ChargeConstraint& cc : m.charge_constraints) {
+                if (fa) {
+                    for (int c = 0; c < C; ++c) fa->s("0.0 ");
+                    for (int j = 0; j < np; ++j)
+                        for (size_t k = 0; k < cc.pair.size(); ++k)
+                            if (cc.pair[k] == j) { fa->num(cc.value[k]); fa->s(" "); }
+                    fa->s("\n");
+                }
+                fbv.num(cc.force); fbv.s("\n");
+            }
         }
-        for (int k = 0; k < erows; ++k, ++row) {
-            const int64_t r = r0 + 3 * N + srows + k;
-            const double* Ar = A + r * lda;
-            for (int c = 0; c < C; ++c) { fa.num(Ar[c]); fa.s(" "); }
-            tail(true);
-            fbv.num(fb.b[r]); fbv.s("\n");
-            fbl.s(flag(m.ctl.energy_flags, f)); fbl.s("+1 "); fbl.lab(fb.b[r]); fbl.s("\n");
+        if (split) {
+            fa.reset();
+            if (count[r] > 0) {   // CLEANUP_FILES src/A_Matrix.C:681-704: columns, first row, last row, total
+                std::snprintf(name, sizeof(name), "/dim.%04d.txt", r);
+                Out fd(dir + name);
+                std::fprintf(fd.f, "%d %lld %lld %lld\n", m.tot_all, (long long)start,
+                             (long long)(start + count[r] - 1), (long long)total);
+            }
         }
+        start += count[r];
     }
-    if (with_constraints && !m.charge_constraints.empty()) {   // A_MAT::PRINT_CONSTRAINTS src/A_Matrix.C:606-623
-        const int np = (int)m.pairs.size();
-        for (const ChargeConstraint& cc : m.charge_constraints) {
-            for (int c = 0; c < C; ++c) fa.s("0.0 ");
-            for (int j = 0; j < np; ++j)
-                for (size_t k = 0; k < cc.pair.size(); ++k)
-                    if (cc.pair[k] == j) { fa.num(cc.value[k]); fa.s(" "); }
-            fa.s("\n");
-            fbv.num(cc.force); fbv.s("\n");
-            ++row;
-        }
+    if (!split) {
+        Out fd(dir + "/dim.txt");
+        std::fprintf(fd.f, "%d %lld\n", m.tot_all, (long long)total);
     }
-    Out fd(dir + "/dim.txt");
-    std::fprintf(fd.f, "%d %lld\n", m.tot_all, (long long)row);
 }
 
 // Coefficients from params.txt text: the 2-body blocks ("%3d %21.13e" lines after

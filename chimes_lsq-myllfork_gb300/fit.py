@@ -47,6 +47,8 @@ def main(argv=None):
     ap.add_argument("--write-a", action="store_true", help="also write A.txt, b.txt, ... (slow for large A)")
     ap.add_argument("--out", default=None, help="output directory (default: the fm_setup.in directory)")
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--ranks", type=int, default=1,
+                    help="order the frames and text files as `srun -n RANKS chimes_lsq` would (SKPFRMS, SPLITFI)")
     args = ap.parse_args(argv)
 
     import numpy as np
@@ -57,7 +59,7 @@ def main(argv=None):
     model = cg.Model(args.fm_setup)
     open(os.path.join(out, "params.header"), "w").write(model.params_header())
     open(os.path.join(out, "ff_groups.map"), "w").write(model.ff_groups_map())
-    frames = cg.Frames.read(model)
+    frames = cg.Frames.read(model, nprocs=args.ranks)
     torch.cuda.set_device(args.device)
     sess = cg.Session(model, args.device)
     C = model.ncols

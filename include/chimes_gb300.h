@@ -73,6 +73,15 @@ int cg_model_params_read(const cg_model* m, const char* params_txt, double* x, i
  * nframes <= 0: NFRAMES).  Replaces FRAME::READ_XYZF (src/ClassDefs.C:2411-2683). */
 int cg_frames_read(const cg_model* m, const char* xyzf_path, int nframes, cg_frames** out);
 
+/* The model's trajectory as `srun -n nprocs chimes_lsq` processes it: the frames of
+ * each rank in rank order (contiguous blocks, divide_atoms src/functions.C:182-222,
+ * or SKPFRMS round-robin with skipping, src/chimes_lsq.C:305-317), each frame keeping
+ * its trajectory index for NSTRESS / NENER.  cg_write_lsq_files then writes the
+ * files that run leaves (rank-ordered b.txt / b-labeled.txt / natoms.txt; with
+ * SPLITFI, A.%04d.txt and dim.%04d.txt per rank).  nprocs = 1 is cg_frames_read of
+ * the model's TRJFILE with SKPFRMS applied. */
+int cg_frames_read_ranks(const cg_model* m, int nprocs, cg_frames** out);
+
 /* Build frames from arrays (no text parsing).  Per frame f: natoms[f] atoms with
  * types (index into the TYPEIDX order) and xyz (A), forces (Hartree/Bohr, as in
  * .xyzf), cell[9*f..] = the 9 cell-vector components ax ay az bx by bz cx cy cz,
@@ -90,7 +99,9 @@ int cg_frames_rows(const cg_frames* fr, int64_t* nrows, int64_t* natoms);
  * dir, with A (host, row-major, lda >= columns) as assembled for them: the files of
  * `chimes_lsq fm_setup.in` (A_MAT::PRINT_FRAME / CLEANUP_FILES,
  * src/A_Matrix.C:210-720; %.16e, three spaces after force-row entries, one after
- * stress / energy entries). */
+ * stress / energy entries).  A NULL writes every file but the A files.  SPLITFI
+ * models write A.%04d.txt / dim.%04d.txt per rank of the batch's emulated run
+ * (CLEANUP_FILES src/A_Matrix.C:626-720). */
 int cg_write_lsq_files(const cg_model* m, const cg_frames* fr, const double* A, int64_t lda, const char* dir);
 /* (FITCOUL models: A holds the frames' rows; the charge-constraint rows are appended
  * to A.txt and b.txt after them, as the reference writes them.) */

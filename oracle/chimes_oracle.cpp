@@ -842,6 +842,10 @@ thread_local std::string g_err;
 
 }  // namespace
 
+// Frame number in the trajectory (NSTRESS / NENER): the reader's index, which SKPFRMS
+// keeps for the frames it selects (src/chimes_lsq.C:305-322 passes i on).
+static int traj_index(const std::vector<Frame>& fr, int k) { return fr[k].index >= 0 ? fr[k].index : k; }
+
 extern "C" {
 
 const char* oracle_last_error() { return g_err.c_str(); }
@@ -855,7 +859,7 @@ int oracle_sizes(const char* fm_setup, const char* xyzf, int nframes, int64_t* n
                                      : read_frames(m);
         if (nframes > 0 && (size_t)nframes < fr.size()) fr.resize(nframes);   // the first nframes frames
         int64_t r = 0;
-        for (size_t f = 0; f < fr.size(); ++f) r += frame_rows(m, (int)f, fr[f].natoms).total();
+        for (size_t f = 0; f < fr.size(); ++f) r += frame_rows(m, traj_index(fr, (int)f), fr[f].natoms).total();
         *nrows = r;
         *ncols = m.tot_all;
         return 0;
@@ -883,12 +887,13 @@ int oracle_assemble(const char* fm_setup, const char* xyzf, int nframes, int fir
             sm = frame_is_small(m, fr[k].box, sm);
             if (k >= first) small[k - first] = sm;
         }
-        for (int k = 0; k < count; ++k) ofs[k + 1] = ofs[k] + frame_rows(m, first + k, fr[first + k].natoms).total();
+        for (int k = 0; k < count; ++k)
+            ofs[k + 1] = ofs[k] + frame_rows(m, traj_index(fr, first + k), fr[first + k].natoms).total();
         std::string err;
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
         for (int k = 0; k < count; ++k) {
             try {
-                frame_rows_out(m, fr[first + k], first + k, small[k], A + ofs[k] * lda, lda, b + ofs[k]);
+                frame_rows_out(m, fr[first + k], traj_index(fr, first + k), small[k], A + ofs[k] * lda, lda, b + ofs[k]);
             } catch (const std::exception& e) {
 #pragma omp critical
                 err = e.what();

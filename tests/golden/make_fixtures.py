@@ -38,7 +38,12 @@ FIXTURES = {
                                    disp=0.1), 2, 15),
     # two trajectory files of different sizes behind TRJFILE MULTI, label flags on the second
     "multifile": ("multi", {}, 3, 16),
+    # SKPFRMS 2 over 5 frames (frames 0, 2, 4 kept) with stress rows for the first 3
+    # trajectory frames only (FITSTRS FIRSTALL 3): the cut-off counts trajectory frames
+    "skipframes": ("water-3b", dict(nmol=24, L=8.96, order=(8, 4, 0), fitstrs="FIRSTALL 3", fitener=True), 5, 18),
 }
+
+SKIP = {"skipframes": 2}
 
 
 def make_multifile(d):
@@ -68,6 +73,12 @@ def make(name):
         inputs = make_multifile(d)
     else:
         synth.make_workload(wl, d, nframes=nframes, seed=seed, **over)
+    if name in SKIP:
+        fm = open(os.path.join(d, "fm_setup.in")).read()
+        key = f"# NFRAMES #\n\t{nframes}\n"
+        assert key in fm
+        fm = fm.replace(key, key + f"# SKPFRMS #\n\t{SKIP[name]}\n")
+        open(os.path.join(d, "fm_setup.in"), "w").write(fm)
     with tempfile.TemporaryDirectory() as tmp:
         shutil.copy(os.path.join(d, "fm_setup.in"), tmp)
         for f in inputs:
