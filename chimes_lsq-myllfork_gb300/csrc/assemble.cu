@@ -19,6 +19,7 @@
 //  * Powers that PARAM_INDICES maps to one column (permutations of identical
 //    atoms) are contiguous; they are summed in shared memory before the store.
 // g_s[n] = fcut_s T_n(x_s), h_s[n] = d g_s[n] / dr_s.
+#include <algorithm>
 #include <cstdio>
 #include "assemble.h"
 #include "basis.cuh"
@@ -47,15 +48,21 @@ struct SlotBasis {
     double r, rab[3];
 };
 
-template <typename TC>
-__device__ void slot_basis(const ModelDev& M, const FramesDev& F, int NB, int f, int4 mem, int id, int T,
-                           int s, int ord, TC* g, TC* h, SlotBasis& sb) {
+// The edge of cluster id that maps to canonical slot s, and its two members.
+__device__ __forceinline__ int slot_edge(const ModelDev& M, int NB, int id, int s, int& a, int& b) {
     const int np = NB == 3 ? 3 : 6;
     const int8_t* pm = (NB == 3 ? M.pidx3 : M.pidx4) + id * np;
     int e = 0;
     for (int k = 0; k < np; ++k) if (pm[k] == s) e = k;
-    int a, b;
     edge_members(NB, e, a, b);
+    return e;
+}
+
+template <typename TC>
+__device__ void slot_basis(const ModelDev& M, const FramesDev& F, int NB, int f, int4 mem, int id, int T,
+                           int s, int ord, TC* g, TC* h, SlotBasis& sb) {
+    int a, b;
+    const int e = slot_edge(M, NB, id, s, a, b);
     const int N = F.natoms[f];
     const int64_t gb = F.ghost_ofs[f];
     const int ga = member(mem, a), gbm = member(mem, b);
@@ -68,6 +75,38 @@ __device__ void slot_basis(const ModelDev& M, const FramesDev& F, int NB, int f,
     double fc, fd;
     fcut_eval(M, sb.r, CT.smax[s], fc, fd);
     basis_gh_t<TC>(M, M.pairs[pt].lambda, CT.xavg[s], CT.xdiff[s], CT.smin[s], sb.r, 0, ord, fc, fd, g, h, 1);
+}
+
+// ---------------------------------------------------------------- per-cluster slot bases
+// One thread per (cluster, slot) of the batch: g, h, r and r_ab of the slot's edge,
+// [cluster][slot][2 ord + 4].  The force kernel visits every cluster once per member
+// atom and the stress/energy kernel once more; with these tables the basis is
+// evaluated once per cluster.
+template <int NBODY, typename R>
+__global__ void k_cluster_basis(ModelDev M, FramesDev F, ClusterSet CS, int64_t nq, R* __restrict__ out) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    const int ord = NBODY == 3 ? M.order3 : M.order4;
+    const int stride = 2 * ord + 4;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq * NP; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = t / NP;
+        const int s = (int)(t % NP);
+        int lo = 0, hi = F.nframes - 1;   // frame of cluster q: last f with its first cluster <= q
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (CS.ofs[F.atom_ofs[mid]] <= q) lo = mid; else hi = mid - 1;
+        }
+        const int f = lo;
+        const int N = F.natoms[f];
+        const int* typ = F.type + F.atom_ofs[f];
+        const int4 mm = CS.m[q];
+        int id = 0, w = 1;
+        for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
+        R* o = out + t * stride;
+        SlotBasis sb;
+        slot_basis<R>(M, F, NBODY, f, mm, id, CS.type[q], s, ord, o, o + ord, sb);
+        o[2 * ord] = R(sb.r);
+        o[2 * ord + 1] = R(sb.rab[0]); o[2 * ord + 2] = R(sb.rab[1]); o[2 * ord + 3] = R(sb.rab[2]);
+    }
 }
 
 // ---------------------------------------------------------------- 2-body force rows
@@ -201,7 +240,8 @@ __global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t ld
 // tuple of the largest cluster type, so the accumulators stay in registers.
 template <int NBODY, typename R, int PPT>
 __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
-                                                         const int64_t* key_frame_ofs, R* A, int64_t lda) {
+                                                         const int64_t* key_frame_ofs, const R* __restrict__ pre,
+                                                         R* A, int64_t lda) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
     constexpr int NI = NBODY - 1;
     constexpr int NO = NP - NI;
@@ -226,6 +266,7 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
     int* sCnt = reinterpret_cast<int*>(smem_raw + L.cnt);
     int* sQ = reinterpret_cast<int*>(smem_raw + L.q);
     int* sPi = reinterpret_cast<int*>(smem_raw + L.pi);
+    int* sSg = reinterpret_cast<int*>(smem_raw + L.sg);   // owner's sign on each slot's edge: +1, -1, 0
     R* sGH = reinterpret_cast<R*>(smem_raw + L.gh);
     R* sW = reinterpret_cast<R*>(smem_raw + L.w);
     R* sTab = reinterpret_cast<R*>(smem_raw + L.tab);
@@ -315,9 +356,34 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
                     if (threadIdx.x < nb) {
                         const int v = sEnt[sOrd[b0 + threadIdx.x]];
                         sQ[threadIdx.x] = v >> 2; sPi[threadIdx.x] = v & 3;
+                        if (pre) {
+                            const int4 mm = CS.m[qbase + (v >> 2)];
+                            int id = 0, w = 1;
+                            for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
+                            for (int s = 0; s < NP; ++s) {
+                                int ea, eb;
+                                slot_edge(M, NBODY, id, s, ea, eb);
+                                sSg[threadIdx.x * NP + s] = ((v & 3) == ea) ? 1 : (((v & 3) == eb) ? -1 : 0);
+                            }
+                        }
                     }
                     __syncthreads();
                     // (1) per (cluster, slot): basis and the owner's weight vector
+                    if (pre) {   // bases of the cluster tables, one thread per (cluster, slot, power)
+                        const int stride = 2 * ord + 4;
+                        for (int t = threadIdx.x; t < nb * NP * ord; t += blockDim.x) {
+                            const int c = t / (NP * ord), rem = t % (NP * ord), s = rem / ord, n = rem % ord;
+                            const R* src = pre + ((size_t)(qbase + sQ[c]) * NP + s) * stride;
+                            const double ir = (double)sSg[c * NP + s] / (double)src[2 * ord];
+                            const R wx = R(src[2 * ord + 1] * ir), wy = R(src[2 * ord + 2] * ir),
+                                    wz = R(src[2 * ord + 3] * ir);
+                            R* g = sGH + ((size_t)c * NP + s) * 2 * ord;
+                            const R gn = src[n], hn = src[ord + n];
+                            g[n] = gn; g[ord + n] = hn;
+                            R* hw = sW + ((size_t)c * NP + s) * 3 * ord;
+                            hw[n] = hn * wx; hw[ord + n] = hn * wy; hw[2 * ord + n] = hn * wz;
+                        }
+                    } else
                     for (int t = threadIdx.x; t < nb * NP; t += blockDim.x) {
                         const int c = t / NP, s = t % NP;
                         const int4 mm = CS.m[qbase + sQ[c]];
@@ -411,7 +477,8 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
 // k_virial_reduce adds the chunks in order and writes the rows.
 template <int NBODY, typename R>
 __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets bytype,
-                                                          const int64_t* key_frame_ofs, int ncomp, R* part,
+                                                          const int64_t* key_frame_ofs, int ncomp,
+                                                          const R* __restrict__ pre, R* part,
                                                           int ntrue_max, int nchunks_max) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
     constexpr int N1 = NBODY - 1;
@@ -472,6 +539,22 @@ __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev 
         const int nb = (int)min((int64_t)MB_CB, c1 - b0);
         if (threadIdx.x < nb) sQ[threadIdx.x] = bytype.val[b0 + threadIdx.x];
         __syncthreads();
+        if (pre) {   // bases of the cluster tables, one thread per (cluster, slot, power)
+            const int stride = 2 * ord + 4;
+            for (int t = threadIdx.x; t < nb * NP * ord; t += blockDim.x) {
+                const int c = t / (NP * ord), rem = t % (NP * ord), s = rem / ord, n = rem % ord;
+                const R* src = pre + ((size_t)(qbase + sQ[c]) * NP + s) * stride;
+                R* g = sGH + ((size_t)c * NP + s) * 2 * ord;
+                g[n] = src[n]; g[ord + n] = src[ord + n];
+                if (n == 0) {
+                    const double r = (double)src[2 * ord];
+                    const double x[3] = {(double)src[2 * ord + 1], (double)src[2 * ord + 2], (double)src[2 * ord + 3]};
+                    R* v = sV + ((size_t)c * NP + s) * 6;
+                    v[0] = R(x[0] * x[0] / r); v[1] = R(x[1] * x[1] / r); v[2] = R(x[2] * x[2] / r);
+                    v[3] = R(x[0] * x[1] / r); v[4] = R(x[0] * x[2] / r); v[5] = R(x[1] * x[2] / r);
+                }
+            }
+        } else
         for (int t = threadIdx.x; t < nb * NP; t += blockDim.x) {
             const int c = t / NP, s = t % NP;
             const int4 mm = CS.m[qbase + sQ[c]];
@@ -637,56 +720,76 @@ void launch_virial2(int prec, int nframes, const ModelDev& M, const FramesDev& F
     }
 }
 
+size_t cluster_basis_count(int nbody, int ord, int64_t nclusters) {
+    return (size_t)nclusters * (nbody == 3 ? 3 : 6) * (2 * ord + 4);
+}
+
+void launch_cluster_basis(int nbody, int prec, int64_t nq, const ModelDev& M, const FramesDev& F,
+                          const ClusterSet& CS, void* basis, cudaStream_t st) {
+    const int64_t n = nq * (nbody == 3 ? 3 : 6);
+    if (n == 0) return;
+    const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 64);
+    if (nbody == 3 && prec == 0) k_cluster_basis<3, double><<<blocks, 256, 0, st>>>(M, F, CS, nq, (double*)basis);
+    else if (nbody == 3) k_cluster_basis<3, float><<<blocks, 256, 0, st>>>(M, F, CS, nq, (float*)basis);
+    else if (prec == 0) k_cluster_basis<4, double><<<blocks, 256, 0, st>>>(M, F, CS, nq, (double*)basis);
+    else k_cluster_basis<4, float><<<blocks, 256, 0, st>>>(M, F, CS, nq, (float*)basis);
+}
+
 template <int NBD, typename R>
 static void force_mb_ppt(int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS,
-                         const Buckets& inc, const int64_t* kfo, R* A, int64_t lda, cudaStream_t st) {
+                         const Buckets& inc, const int64_t* kfo, const R* pre, R* A, int64_t lda, cudaStream_t st) {
     if (ppt <= 1) {
         set_smem(k_force_mb<NBD, R, 1>, smem);
-        k_force_mb<NBD, R, 1><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, A, lda);
+        k_force_mb<NBD, R, 1><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
     } else if (ppt <= 2) {
         set_smem(k_force_mb<NBD, R, 2>, smem);
-        k_force_mb<NBD, R, 2><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, A, lda);
+        k_force_mb<NBD, R, 2><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
     } else {
         set_smem(k_force_mb<NBD, R, 8>, smem);
-        k_force_mb<NBD, R, 8><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, A, lda);
+        k_force_mb<NBD, R, 8><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
     }
 }
 
 void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,
-                     const ClusterSet& CS, const Buckets& inc, const int64_t* kfo, void* A, int64_t lda,
-                     cudaStream_t st) {
-    if (nbody == 3 && prec == 0) force_mb_ppt<3, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (double*)A, lda, st);
-    else if (nbody == 3) force_mb_ppt<3, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (float*)A, lda, st);
-    else if (prec == 0) force_mb_ppt<4, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (double*)A, lda, st);
-    else force_mb_ppt<4, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (float*)A, lda, st);
+                     const ClusterSet& CS, const Buckets& inc, const int64_t* kfo, const void* pre, void* A,
+                     int64_t lda, cudaStream_t st) {
+    if (nbody == 3 && prec == 0)
+        force_mb_ppt<3, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (const double*)pre, (double*)A, lda, st);
+    else if (nbody == 3)
+        force_mb_ppt<3, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st);
+    else if (prec == 0)
+        force_mb_ppt<4, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (const double*)pre, (double*)A, lda, st);
+    else
+        force_mb_ppt<4, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st);
 }
 
 void launch_virial_mb(int nbody, int prec, int nframes, int ntypes, int nzchunk, int nchunks_max, int ntrue_max,
                       size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
-                      const int64_t* kfo, int ncomp, void* part, void* A, int64_t lda, cudaStream_t st) {
+                      const int64_t* kfo, int ncomp, const void* pre, void* part, void* A, int64_t lda,
+                      cudaStream_t st) {
     dim3 grid(nframes * ntypes, nzchunk, nchunks_max);
     const unsigned rgrid = (unsigned)(nframes * ntypes);
     if (nbody == 3 && prec == 0) {
         set_smem(k_virial_mb<3, double>, smem);
-        k_virial_mb<3, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (double*)part, ntrue_max,
+        k_virial_mb<3, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (const double*)pre, (double*)part, ntrue_max,
                                                                 nchunks_max);
         k_virial_reduce<3, double><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const double*)part, ntrue_max, nchunks_max,
                                                           (double*)A, lda);
     } else if (nbody == 3) {
         set_smem(k_virial_mb<3, float>, smem);
-        k_virial_mb<3, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (float*)part, ntrue_max,
+        k_virial_mb<3, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (const float*)pre, (float*)part, ntrue_max,
                                                                nchunks_max);
         k_virial_reduce<3, float><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const float*)part, ntrue_max, nchunks_max,
                                                          (float*)A, lda);
     } else if (prec == 0) {
         set_smem(k_virial_mb<4, double>, smem);
-        k_virial_mb<4, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (double*)part, ntrue_max,
+        k_virial_mb<4, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (const double*)pre, (double*)part, ntrue_max,
                                                                 nchunks_max);
         k_virial_reduce<4, double><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const double*)part, ntrue_max, nchunks_max,
                                                           (double*)A, lda);
     } else {
         set_smem(k_virial_mb<4, float>, smem);
-        k_virial_mb<4, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (float*)part, ntrue_max,
+        k_virial_mb<4, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (const float*)pre, (float*)part, ntrue_max,
                                                                nchunks_max);
         k_virial_reduce<4, float><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const float*)part, ntrue_max, nchunks_max,
                                                          (float*)A, lda);

@@ -14,7 +14,7 @@ constexpr int F2_THREADS = 128;     // 2-body kernels
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 struct MbForceSmem {
-    size_t ent, key, ord, cnt, q, pi, gh, w, tab, total;
+    size_t ent, key, ord, cnt, q, pi, sg, gh, w, tab, total;
 };
 __host__ __device__ inline MbForceSmem mb_force_smem(int nbody, int ord, int nkeys, int max_allowed, int rsize) {
     const int np = nbody == 3 ? 3 : 6, ni = nbody - 1, no = np - ni;
@@ -29,7 +29,8 @@ __host__ __device__ inline MbForceSmem mb_force_smem(int nbody, int ord, int nke
     s.cnt = align16(s.ord + MB_MAX_ENT * sizeof(int));
     s.q = align16(s.cnt + (nkeys + 1) * sizeof(int));
     s.pi = align16(s.q + MB_CB * sizeof(int));
-    s.gh = align16(s.pi + MB_CB * sizeof(int));
+    s.sg = align16(s.pi + MB_CB * sizeof(int));
+    s.gh = align16(s.sg + MB_CB * 6 * sizeof(int));
     s.w = align16(s.gh + (size_t)MB_CB * np * 2 * ord * rsize);
     s.tab = align16(s.w + (size_t)MB_CB * np * 3 * ord * rsize);
     size_t tab = (size_t)MB_CB * per;
@@ -83,14 +84,21 @@ void launch_force2(int prec, int nreal, const ModelDev& M, const FramesDev& F, c
                    const Buckets& inc, const int64_t* key_frame_ofs, void* A, int64_t lda, cudaStream_t st);
 void launch_virial2(int prec, int nframes, const ModelDev& M, const FramesDev& F, const NeighDev& NB, void* A,
                     int64_t lda, cudaStream_t st);
+// Slot bases of every cluster, once per cluster: [cluster][slot][2 ord + 4] values in
+// the form's type (g, h, r, r_ab), read by the force and stress/energy kernels.
+size_t cluster_basis_count(int nbody, int ord, int64_t nclusters);
+void launch_cluster_basis(int nbody, int prec, int64_t nclusters, const ModelDev& M, const FramesDev& F,
+                          const ClusterSet& CS, void* basis, cudaStream_t st);
+// pre: the cluster bases above, or nullptr to evaluate them in the kernel.
 void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,
-                     const ClusterSet& CS, const Buckets& inc, const int64_t* key_frame_ofs, void* A, int64_t lda,
-                     cudaStream_t st);
+                     const ClusterSet& CS, const Buckets& inc, const int64_t* key_frame_ofs, const void* pre,
+                     void* A, int64_t lda, cudaStream_t st);
 // Stress/energy rows: nchunks_max cluster chunks of VIR_CLUSTERS per (frame, type);
 // part holds nframes*ntypes*nchunks_max*7*ntrue_max partial sums (R).
 void launch_virial_mb(int nbody, int prec, int nframes, int ntypes, int nzchunk, int nchunks_max, int ntrue_max,
                       size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
-                      const int64_t* key_frame_ofs, int ncomp, void* part, void* A, int64_t lda, cudaStream_t st);
+                      const int64_t* key_frame_ofs, int ncomp, const void* pre, void* part, void* A, int64_t lda,
+                      cudaStream_t st);
 void launch_max_bucket(const int64_t* key_ofs, const int64_t* key_frame_ofs, int nframes, int ntypes, int* out,
                        cudaStream_t st);
 void launch_energy_cols(int prec, int nframes, const ModelDev& M, const FramesDev& F, void* A, int64_t lda,

@@ -416,6 +416,10 @@ std::unique_ptr<DeviceFrames> Session::upload(const FrameBatch& fb) {
 }
 
 namespace {
+// Largest per-cluster basis table (bytes) an assembly call allocates; bigger
+// batches evaluate the bases inside the force and stress kernels instead.
+constexpr size_t kClusterBasisMax = size_t(16) << 30;
+
 // Scratch of the no-allocation entry point: one fixed array per device that loads
 // this library, held until the process exits.  Host code must not use the symbol
 // as an address; noalloc_scratch() obtains the device address once per device.
@@ -590,7 +594,16 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
         cgd::MbForceSmem Lf = cgd::mb_force_smem(nbody, ord, ntypes * 4, max_allowed, rsize);
         if (Lf.total > 227 * 1024) throw Error(2, "cluster order too large for the device force kernel");
         mark(nbody == 3 ? ST_FORCE3 : ST_FORCE4, true);
-        cgd::launch_force_mb(nbody, prec, pp, nreal, Lf.total, M, F, CS, inc, kfo_atoms, A, lda, st); L();
+        // slot bases once per cluster (the force kernel meets each cluster once per
+        // member, the stress kernel once more); evaluated in place when the fixed
+        // no-allocation scratch is in use or the table would pass kClusterBasisMax
+        void* pre = nullptr;
+        const size_t nbasis = cgd::cluster_basis_count(nbody, ord, nq);
+        if (!S.base && nbasis * rsize <= kClusterBasisMax) {
+            pre = prec == 0 ? (void*)S.get<double>(nbasis) : (void*)S.get<float>(nbasis);
+            cgd::launch_cluster_basis(nbody, prec, nq, M, F, CS, pre, st); L();
+        }
+        cgd::launch_force_mb(nbody, prec, pp, nreal, Lf.total, M, F, CS, inc, kfo_atoms, pre, A, lda, st); L();
         mark(nbody == 3 ? ST_FORCE3 : ST_FORCE4, false);
         CK(cudaGetLastError());
         if (virial) {
@@ -616,7 +629,7 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
                                    : (void*)S.get<float>((size_t)nf * ntypes * nch * 7 * ntrue_max);
             mark(nbody == 3 ? ST_VIRIAL3 : ST_VIRIAL4, true);
             cgd::launch_virial_mb(nbody, prec, nf, ntypes, std::min(maxz, cgd::MAXCHUNK), nch, ntrue_max, V.total, M, F,
-                                  CS, byt, kfo_types, ncomp, part, A, lda, st); L(2);
+                                  CS, byt, kfo_types, ncomp, pre, part, A, lda, st); L(2);
             mark(nbody == 3 ? ST_VIRIAL3 : ST_VIRIAL4, false);
             CK(cudaGetLastError());
         }
