@@ -171,9 +171,12 @@ __global__ void k_force2(ModelDev M, FramesDev F, NeighDev NB, Buckets inc, cons
     for (int c = 0; c < MAXC; ++c) {
         const int col = threadIdx.x + c * blockDim.x;
         if (col >= ncol) break;
-        A[(row + 0) * lda + col] = acc[c][0];
-        A[(row + 1) * lda + col] = acc[c][1];
-        A[(row + 2) * lda + col] = acc[c][2];
+        const int base = M.pairs[col / ord].col;   // HIERARC: excluded pairs have no columns
+        if (base < 0) continue;
+        const int oc = base + col % ord;
+        A[(row + 0) * lda + oc] = acc[c][0];
+        A[(row + 1) * lda + oc] = acc[c][1];
+        A[(row + 2) * lda + oc] = acc[c][2];
     }
 }
 
@@ -231,7 +234,8 @@ __global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t ld
     for (int c = 0; c < MAXC; ++c) {
         const int col = threadIdx.x + c * blockDim.x;
         if (col >= ncol) break;
-        write_virial_rows(F, f, col, acc[c], inv_vol, A, lda);
+        const int base = M.pairs[col / ord].col;   // HIERARC: excluded pairs have no columns
+        if (base >= 0) write_virial_rows(F, f, base + col % ord, acc[c], inv_vol, A, lda);
     }
 }
 
@@ -374,9 +378,8 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
                         for (int t = threadIdx.x; t < nb * NP * ord; t += blockDim.x) {
                             const int c = t / (NP * ord), rem = t % (NP * ord), s = rem / ord, n = rem % ord;
                             const R* src = pre + ((size_t)(qbase + sQ[c]) * NP + s) * stride;
-                            const double ir = (double)sSg[c * NP + s] / (double)src[2 * ord];
-                            const R wx = R(src[2 * ord + 1] * ir), wy = R(src[2 * ord + 2] * ir),
-                                    wz = R(src[2 * ord + 3] * ir);
+                            const R ir = R(sSg[c * NP + s]) / src[2 * ord];   // sign / r in the form's type
+                            const R wx = src[2 * ord + 1] * ir, wy = src[2 * ord + 2] * ir, wz = src[2 * ord + 3] * ir;
                             R* g = sGH + ((size_t)c * NP + s) * 2 * ord;
                             const R gn = src[n], hn = src[ord + n];
                             g[n] = gn; g[ord + n] = hn;
@@ -546,12 +549,12 @@ __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev 
                 const R* src = pre + ((size_t)(qbase + sQ[c]) * NP + s) * stride;
                 R* g = sGH + ((size_t)c * NP + s) * 2 * ord;
                 g[n] = src[n]; g[ord + n] = src[ord + n];
-                if (n == 0) {
-                    const double r = (double)src[2 * ord];
-                    const double x[3] = {(double)src[2 * ord + 1], (double)src[2 * ord + 2], (double)src[2 * ord + 3]};
+                if (n == 0) {   // r_a r_b / r in the form's type
+                    const R r = src[2 * ord];
+                    const R x[3] = {src[2 * ord + 1], src[2 * ord + 2], src[2 * ord + 3]};
                     R* v = sV + ((size_t)c * NP + s) * 6;
-                    v[0] = R(x[0] * x[0] / r); v[1] = R(x[1] * x[1] / r); v[2] = R(x[2] * x[2] / r);
-                    v[3] = R(x[0] * x[1] / r); v[4] = R(x[0] * x[2] / r); v[5] = R(x[1] * x[2] / r);
+                    v[0] = x[0] * x[0] / r; v[1] = x[1] * x[1] / r; v[2] = x[2] * x[2] / r;
+                    v[3] = x[0] * x[1] / r; v[4] = x[0] * x[2] / r; v[5] = x[1] * x[2] / r;
                 }
             }
         } else
@@ -671,6 +674,7 @@ __global__ void k_max_bucket(const int64_t* key_ofs, const int64_t* key_frame_of
 // ---------------------------------------------------------------- energy offset columns
 // One column per atom type holding that type's atom count on energy rows
 // (A_MAT::add_col_of_ones src/A_Matrix.C:155-175); force and stress rows keep 0.
+// HIERARC-excluded types have no column.
 __global__ void k_energy_cols(ModelDev M, FramesDev F, void* A, int64_t lda, int is_double) {
     const int f = blockIdx.x;
     if (F.energy_rows[f] == 0 || M.fit_ener_cols == 0) return;
@@ -678,10 +682,11 @@ __global__ void k_energy_cols(ModelDev M, FramesDev F, void* A, int64_t lda, int
     const int* typ = F.type + F.atom_ofs[f];
     const int64_t row = F.row_ofs[f] + 3 * (int64_t)N + F.stress_rows[f];
     for (int t = threadIdx.x; t < M.fit_ener_cols; t += blockDim.x) {
+        if (M.ener_col[t] < 0) continue;   // HIERARC EXCLUDE 1B: no column
         int count = 0;
         for (int k = 0; k < N; ++k) count += typ[k] == t;
         for (int rr = 0; rr < F.energy_rows[f]; ++rr) {
-            const int64_t idx = (row + rr) * lda + M.tot_short + M.ncoul + t;
+            const int64_t idx = (row + rr) * lda + M.tot_short + M.ncoul + M.ener_col[t];
             if (is_double) reinterpret_cast<double*>(A)[idx] = (double)count;
             else reinterpret_cast<float*>(A)[idx] = (float)count;
         }

@@ -19,6 +19,7 @@ constexpr int MAXCHUNK = 16;   // power chunks of one cluster type in the stress
 // ---------------------------------------------------------------- model tables
 struct PairDev {               // one 2-body pair type
     double smin, smax, lambda, xavg, xdiff;
+    int col;                   // first A column of its 2-body block, -1 when HIERARC excludes it
 };
 
 struct ClusterTypeDev {        // one triplet / quadruplet type
@@ -39,7 +40,8 @@ struct ModelDev {
     int ntypes3, ntypes4;
     int n2b, tot_short, tot_all;         // column counts
     int col3, col4;                      // first 3B / 4B column
-    int fit_ener_cols;                   // number of energy-offset columns (0 or natmtyp)
+    int fit_ener_cols;                   // atom types scanned for energy-offset columns (0 or natmtyp)
+    int ener_col[10];                    // energy-offset column of each type after tot_short + ncoul; -1 excluded
     int ncoul;                           // FITCOUL charge columns (one per pair type), after tot_short
     const int* int_pair_map;             // natmtyp^2
     const PairDev* pairs;

@@ -47,9 +47,12 @@ void Session::md_setup(const double* x, int nx, int precision, bool offsets, dou
         if (bytes) CK(cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice));
         return p;
     };
-    // 2-body: x[pt * order2 + n] multiplies T_{n+1} (src/chimes_lsq.py:462-477 layout)
-    std::vector<double> c2((size_t)m.pairs.size() * o2);
-    for (size_t i = 0; i < c2.size(); ++i) c2[i] = x[i];
+    // 2-body: x[col_pt + n] multiplies T_{n+1} (src/chimes_lsq.py:462-477 layout);
+    // pair types a HIERARC fit excluded keep zero coefficients, as its params.txt prints
+    std::vector<double> c2((size_t)m.pairs.size() * o2, 0.0);
+    for (size_t pt = 0; pt < m.pairs.size(); ++pt)
+        if (m.pairs[pt].col >= 0)
+            for (int n = 0; n < o2; ++n) c2[pt * o2 + n] = x[m.pairs[pt].col + n];
     t->dev.c2 = (const double*)up(c2.data(), c2.size() * sizeof(double));
     // dense cluster tensors: C[type][p_0..p_{n-1}] = x[col_type + PARAM_INDICES[q]]
     auto dense = [&](const ClusterList& cl, int np, int ord, int col0, std::vector<double>& out) {
@@ -78,9 +81,12 @@ void Session::md_setup(const double* x, int nx, int precision, bool offsets, dou
     t->dev.C3f = (const float*)up(C3f.data(), C3f.size() * sizeof(float));
     t->dev.C4f = (const float*)up(C4f.data(), C4f.size() * sizeof(float));
     t->dev.eoff = nullptr;
-    if (offsets) {
-        if (m.tot_all - m.tot_short - m.ncoul != m.ctl.natmtyp) throw Error(2, "the model has no energy-offset columns");
-        t->dev.eoff = (const double*)up(x + m.tot_short + m.ncoul, m.ctl.natmtyp * sizeof(double));
+    if (offsets) {   // HIERARC-excluded types have offset 0
+        if (!m.ctl.fit_ener) throw Error(2, "the model has no energy-offset columns");
+        std::vector<double> eo(m.ctl.natmtyp, 0.0);
+        for (int ty = 0; ty < m.ctl.natmtyp; ++ty)
+            if (m.ener_col[ty] >= 0) eo[ty] = x[m.tot_short + m.ncoul + m.ener_col[ty]];
+        t->dev.eoff = (const double*)up(eo.data(), eo.size() * sizeof(double));
     }
     // FITCOUL: charges from the fitted products (chimes_md read_ff_params,
     // src/chimes_md.C:2000-2080): q products in Stillinger units over ke, q_t =

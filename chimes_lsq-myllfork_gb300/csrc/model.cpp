@@ -585,7 +585,30 @@ static void parse_topology(const Listing& L, Model& m) {
             break;
         }
     };
-    if (c.hierarchical) fail("HIERARC (hierarchical 1B/2B exclusion) is not supported by this build");
+    // HIERARC: EXCLUDE 1B / 2B INTERACTION lists (INPUT::PARSE_TOPOLOGY_EXCLUDE
+    // src/input.C:753-842): atom type names, and pair names matched in either order
+    if (c.hierarchical) {
+        for (size_t i = 0; i < N; ++i) {
+            if (L.size(i) < 4 || L.at(i, 0) + " " + L.at(i, 1) + " " + L.at(i, 2) != "EXCLUDE 1B INTERACTION:") continue;
+            const int nex = to_int(L.at(i, 3));
+            for (int j = 1; j <= nex; ++j)
+                for (int k = 0; k < c.natmtyp; ++k)
+                    if (L.at(i + j, 0) == m.atom_types[k]) m.excl1b.push_back(m.atom_type_idx[k]);
+            break;
+        }
+        for (size_t i = 0; i < N; ++i) {
+            if (L.size(i) < 4 || L.at(i, 0) + " " + L.at(i, 1) + " " + L.at(i, 2) != "EXCLUDE 2B INTERACTION:") continue;
+            const int nex = to_int(L.at(i, 3));
+            for (int j = 1; j <= nex; ++j)
+                for (size_t k = 0; k < m.pairs.size(); ++k) {
+                    const PairType& p = m.pairs[k];
+                    if ((p.atm1 == L.at(i + j, 0) && p.atm2 == L.at(i + j, 1)) ||
+                        (p.atm1 == L.at(i + j, 1) && p.atm2 == L.at(i + j, 0)))
+                        m.excl2b.push_back((int)k);
+                }
+            break;
+        }
+    }
     read_exclude("EXCLUDE 3B INTERACTION:", m.trips.exclude, 3);
     read_exclude("EXCLUDE 4B INTERACTION:", m.quads.exclude, 4);
     // PAIRIDX src/input.C:1044-1102
@@ -666,10 +689,15 @@ Model load_model(const std::string& path) {
         fail("fixed charges with stress or energy rows: only the force labels are corrected (SubtractEwaldForces)");
     if (c.nlayers < 1) fail("NLAYERS must be >= 1 (ghost-atom images); NLAYERS 0 is not supported by this build");
     // main: src/chimes_lsq.C:198-248
+    // 2-body blocks in pair order without the HIERARC-excluded ones (A_MAT::skip_2b
+    // src/A_Matrix.C:192-208 drops them when PRINT_FRAME writes a row)
     m.tot_snum = 0;
-    for (auto& p : m.pairs) {
+    for (size_t k = 0; k < m.pairs.size(); ++k) {
+        PairType& p = m.pairs[k];
         p.snum = c.cheby_order; p.snum3 = c.cheby3; p.snum4 = c.cheby4; p.trans = c.trans;
-        m.tot_snum += p.snum;
+        const bool ex = std::find(m.excl2b.begin(), m.excl2b.end(), (int)k) != m.excl2b.end();
+        p.col = ex ? -1 : m.tot_snum;
+        if (!ex) m.tot_snum += p.snum;
     }
     for (auto& p : m.pairs) set_cheby_params(p.smin, p.smax, p.lambda, p.trans, p.xmin, p.xmax, p.xdiff, p.xavg);
     m.deriv_const = (m.pairs[0].range_high - m.pairs[0].range_low) / 2.0;
@@ -682,7 +710,14 @@ Model load_model(const std::string& path) {
     if (c.use4) for (auto& ct : m.quads.vec) m.num4 += ct.n_true;
     m.tot_short = m.tot_snum + m.num3 + m.num4;
     m.ncoul = c.fit_coul ? (int)m.pairs.size() : 0;
-    m.tot_all = m.tot_short + m.ncoul + (c.fit_ener ? c.natmtyp : 0);
+    if (m.ncoul > 0 && !m.excl2b.empty()) fail("HIERARC 2-body exclusion with FITCOUL: the solver script refuses it");
+    // energy-offset columns: one per atom type not excluded (A_MAT::add_col_of_ones
+    // src/A_Matrix.C:155-175)
+    int nen = 0;
+    m.ener_col.assign(c.natmtyp, -1);
+    for (int t = 0; t < c.natmtyp; ++t)
+        if (std::find(m.excl1b.begin(), m.excl1b.end(), t) == m.excl1b.end()) m.ener_col[t] = nen++;
+    m.tot_all = m.tot_short + m.ncoul + (c.fit_ener ? nen : 0);
     // JOB_CONTROL::LSQ_SETUP src/ClassDefs.C:2761-2785
     if ((c.fit_stress || c.fit_stress_all) && c.nstress == -1) c.nstress = c.nframes;
     if (c.fit_ener && c.nener == -1) c.nener = c.nframes;
@@ -758,8 +793,14 @@ std::string params_header_text(const Model& m) {   // print_param_header src/chi
     h << "FITCOUL: " << (c.fit_coul ? "true" : "false") << std::endl;
     h << "USE3BCH: " << (c.use3 ? "true" : "false") << std::endl;
     h << "USE4BCH: " << (c.use4 ? "true" : "false") << std::endl;
-    h << "EXCLD1B: false" << std::endl;
-    h << "EXCLD2B: false" << std::endl;
+    auto excl = [&](const char* tag, const std::vector<int>& v) {
+        h << tag;
+        if (v.empty()) h << "false";
+        else for (int i : v) h << i << " ";
+        h << std::endl;
+    };
+    excl("EXCLD1B: ", m.excl1b);
+    excl("EXCLD2B: ", m.excl2b);
     const PairType& p0 = m.pairs[0];
     h << std::endl << "PAIRTYP: " << c.ff_type << " ";
     h << " " << p0.snum << " " << p0.snum3 << " " << p0.snum4 << " " << p0.range_low << " " << p0.range_high << std::endl;
@@ -856,10 +897,18 @@ std::string params_txt_text(const Model& m, const double* x, int nx, const std::
     };
     size_t trip_line = 0, quad_line = 0;
     int ntrips = 0, nquads = 0;
+    std::vector<int> excl1b, excl2b;   // EXCLD1B / EXCLD2B header lines (src/chimes_lsq.py:335-348)
     for (size_t i = 0; i < hf.size(); ++i) {
         o << hf[i] << "\n";
         const auto t = ws_split(hf[i]);
         bool done = false;
+        for (int w = 0; w < 2; ++w) {
+            if (hf[i].find(w == 0 ? "EXCLD2B" : "EXCLD1B") == std::string::npos) continue;
+            std::vector<int>& ex = w == 0 ? excl2b : excl1b;
+            ex.clear();
+            if (!(t.size() == 2 && t[1] == "false"))
+                for (size_t k = 1; k < t.size(); ++k) ex.push_back(std::stoi(t[k]));
+        }
         if (t.size() > 3 && t[2] == "TRIPLETS:") {
             ntrips = std::stoi(t[3]);
             trip_line = i;
@@ -908,8 +957,12 @@ std::string params_txt_text(const Model& m, const double* x, int nx, const std::
     for (int i = 0; i < npairs; ++i) {
         const auto a = tok(pairs_line + 2 + i + 1);
         o << "PAIRTYPE PARAMS: " << i << " " << at(a, 1) << " " << at(a, 2) << "\n\n";
-        for (int j = 0; j < snum; ++j) o << fmt("%3d %21.13e", j, x[eff * snum + j]) << "\n";
-        ++eff;
+        if (std::find(excl2b.begin(), excl2b.end(), i) != excl2b.end()) {   // excluded: zeros
+            for (int j = 0; j < snum; ++j) o << fmt("%3d %21.13e", j, 0.0) << "\n";
+        } else {
+            for (int j = 0; j < snum; ++j) o << fmt("%3d %21.13e", j, x[eff * snum + j]) << "\n";
+            ++eff;
+        }
         if (fit_coul) {
             const int col = npairs * snum + snum3 + snum4 + i;
             if (col >= nx) throw Error(2, "params.header names a charge coefficient out of range");
@@ -964,10 +1017,15 @@ std::string params_txt_text(const Model& m, const double* x, int nx, const std::
     for (const auto& l : split_lines(ff_groups_map_text(m))) o << l << "\n";
     o << "\n";
     const int total = eff * snum + counted3 + counted4 + counted_coul;
-    if (total != nx && nx != total + ntypes) throw Error(2, "error in counting parameters");
-    if (nx == total + ntypes) {
+    const int n_offsets = ntypes - (int)excl1b.size();
+    if (total != nx && nx != total + n_offsets) throw Error(2, "error in counting parameters");
+    if (nx == total + n_offsets) {
         o << "NO ENERGY OFFSETS:  " << ntypes << "\n";
-        for (int i = 0; i < ntypes; ++i) o << fmt("ENERGY OFFSET %d %21.13e", i + 1, x[total + i]) << "\n";
+        int e = 0;
+        for (int i = 0; i < ntypes; ++i) {
+            const bool ex = std::find(excl1b.begin(), excl1b.end(), i) != excl1b.end();
+            o << fmt("ENERGY OFFSET %d %21.13e", i + 1, ex ? 0.0 : x[total + e++]) << "\n";
+        }
     }
     o << "ENDFILE\n";
     return o.str();

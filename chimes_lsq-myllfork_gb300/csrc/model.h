@@ -39,6 +39,7 @@ struct PairType {
     double range_low = -1, range_high = 1;
     int snum = 0, snum3 = 0, snum4 = 0;
     int trans = TRANS_NONE;
+    int col = 0;                      // first A column of its 2-body block; -1 when HIERARC excludes it
 };
 
 struct ClusterType {
@@ -111,6 +112,10 @@ struct Model {
     ClusterList trips, quads;
     int tot_snum = 0, num3 = 0, num4 = 0, tot_short = 0, tot_all = 0;
     int ncoul = 0;                                   // FITCOUL: one q_i q_j column per pair type
+    // HIERARC: atom types whose energy-offset column and pair types whose 2-body
+    // columns the A matrix leaves out (EXCLUDE 1B / 2B INTERACTION, in input order)
+    std::vector<int> excl1b, excl2b;
+    std::vector<int> ener_col;                       // energy-offset column of each type (-1 excluded)
     std::vector<ChargeConstraint> charge_constraints;
     double max_cutoff_2b = 0, max_cutoff_3b = 0, max_cutoff_4b = 0;
     double deriv_const = 1.0;

@@ -135,10 +135,12 @@ DeviceModel::DeviceModel(const Model& m, int vir_pchunk) {
     d.n2b = m.tot_snum; d.tot_short = m.tot_short; d.tot_all = m.tot_all;
     d.col3 = m.tot_snum; d.col4 = m.tot_snum + m.num3;
     d.fit_ener_cols = c.fit_ener ? c.natmtyp : 0;
+    if (c.natmtyp > 10) throw Error(2, "more than 10 atom types");
+    for (int t = 0; t < 10; ++t) d.ener_col[t] = t < c.natmtyp ? m.ener_col[t] : -1;
     d.ncoul = m.ncoul;
     d.int_pair_map = dev_upload(allocs, m.int_pair_map.data(), m.int_pair_map.size());
     std::vector<cgd::PairDev> pv;
-    for (const auto& p : m.pairs) pv.push_back({p.smin, p.smax, p.lambda, p.xavg, p.xdiff});
+    for (const auto& p : m.pairs) pv.push_back({p.smin, p.smax, p.lambda, p.xavg, p.xdiff, p.col});
     d.pairs = dev_upload(allocs, pv.data(), pv.size());
     if (c.use3)
         upload_list(m, m.trips, 3, d.col3, vir_pchunk, *this, &d.int_map3, &d.pidx3, &d.rev3, &d.types3, &d.pow3,

@@ -85,6 +85,7 @@ void write_lsq_files(const Model& m, const FrameBatch& fb, const double* A, int6
                     for (int c = 0; c < ncols; ++c) { fa->num(Ar[c]); fa->s(sep); }
                     if (do_ener)
                         for (int t = 0; t < m.ctl.natmtyp; ++t) {
+                            if (m.ener_col[t] < 0) continue;   // HIERARC EXCLUDE 1B
                             if (energy) std::fprintf(fa->f, " %d", natyp[t]);
                             else fa->s(" 0.0");
                         }
@@ -196,7 +197,9 @@ std::vector<double> params_txt_coefficients(const Model& m, const std::string& t
             continue;
         }
         if (t.size() >= 4 && t[0] == "ENERGY" && t[1] == "OFFSET") {
-            put(m.tot_short + m.ncoul + std::stoi(t[2]) - 1, std::stod(t[3]));
+            const int ty = std::stoi(t[2]) - 1;   // HIERARC-excluded types print 0 and have no column
+            if (ty < 0 || ty >= (int)m.ener_col.size()) throw Error(2, "params.txt names an unknown atom type");
+            if (m.ener_col[ty] >= 0) put(m.tot_short + m.ncoul + m.ener_col[ty], std::stod(t[3]));
             continue;
         }
         if (section == 2 && pair >= 0 && m.ncoul > 0 && t.size() == 4 && t[1] == "x" && t[0].rfind("q_", 0) == 0) {
@@ -205,7 +208,8 @@ std::vector<double> params_txt_coefficients(const Model& m, const std::string& t
         }
         if (section == 2 && pair >= 0 && t.size() == 2 && snum > 0 && t[0].find_first_not_of("0123456789") == std::string::npos) {
             const int k = std::stoi(t[0]);
-            if (k < snum) put(pair * snum + k, std::stod(t[1]));
+            if (pair >= (int)m.pairs.size()) throw Error(2, "params.txt names an unknown pair type");
+            if (k < snum && m.pairs[pair].col >= 0) put(m.pairs[pair].col + k, std::stod(t[1]));
             continue;
         }
         if ((section == 3 || section == 4) && ctype >= 0 && ctype < (int)cl->vec.size()) {

@@ -276,6 +276,17 @@ struct Basis {
     }
 };
 
+// Columns of the reference's FORCES / STRESSES arrays: every pair type's 2-body block
+// (TOT_SHORT_RANGE); PRINT_FRAME leaves out the HIERARC-excluded ones (skip_2b,
+// src/A_Matrix.C:192-208, 240-530) and add_col_of_ones the excluded types' offsets.
+int full_2b(const Model& m) { return (int)m.pairs.size() * m.ctl.cheby_order; }
+int full_short(const Model& m) { return full_2b(m) + m.num3 + m.num4; }
+int printed_col(const Model& m, int c) {   // -1 when skip_2b drops column c
+    if (c >= full_2b(m)) return c - full_2b(m) + m.tot_snum;
+    const int base = m.pairs[c / m.ctl.cheby_order].col;
+    return base < 0 ? -1 : base + c % m.ctl.cheby_order;
+}
+
 struct Acc {   // A_MAT::FORCES / STRESSES / FRAME_ENERGIES of one frame
     int C;
     std::vector<double> F;   // [atom][col][3]
@@ -357,7 +368,7 @@ void deriv_3b(const Model& m, const OFrame& fr, const Lists& L, Acc& A, bool fs,
                 double fc[3], fd[3];
                 for (int e = 0; e < 3; ++e)
                     B.polys(pts[e], T[e].data(), D[e].data(), rl[e], ct.xdiff[pi[e]], ct.xavg[pi[e]], ord, ct.smin[pi[e]]);
-                int vstart = m.tot_snum;
+                int vstart = full_2b(m);
                 for (int t = 0; t < T3; ++t) vstart += cl.vec[t].n_true;
                 for (int e = 0; e < 3; ++e) B.fcut(fc[e], fd[e], rl[e], ct.smax[pi[e]]);
                 int f2 = fr.parent[a2], f3 = fr.parent[a3];
@@ -424,7 +435,7 @@ void deriv_4b(const Model& m, const OFrame& fr, const Lists& L, Acc& A, bool fs,
                     if (!ok) continue;
                     for (int e = 0; e < 6; ++e)
                         B.polys(pts[e], T[e].data(), D[e].data(), rl[e], ct.xdiff[pm[e]], ct.xavg[pm[e]], ord, ct.smin[pm[e]]);
-                    int vstart = m.tot_snum + m.num3;
+                    int vstart = full_2b(m) + m.num3;
                     for (int t = 0; t < Q; ++t) vstart += cl.vec[t].n_true;
                     double fc[6], fd[6];
                     for (int e = 0; e < 6; ++e) B.fcut(fc[e], fd[e], rl[e], ct.smax[pm[e]]);
@@ -580,26 +591,32 @@ void frame_rows_out(const Model& m, const Frame& fr, int fi, bool small, double*
     Lists L = neighbours(m, of, small, m.ncoul > 0 ? ep.rc : 0.0);
     RowLayout rl = frame_rows(m, fi, fr.natoms);
     const bool fs = rl.stress_rows == 3, fsa = rl.stress_rows == 9, fe = rl.energy_rows > 0;
-    Acc A(fr.natoms, m.tot_short);
+    const int CF = full_short(m);
+    Acc A(fr.natoms, CF);
     if (m.ctl.cheby_order > 0) deriv_2b(m, of, L, A, fs, fsa, fe);
     if (m.ctl.use3) deriv_3b(m, of, L, A, fs, fsa, fe);
     if (m.ctl.use4) deriv_4b(m, of, L, A, fs, fsa, fe);
     const double iv = 1.0 / fr.box.vol;
     if (fs || fsa)
-        for (int c = 0; c < m.tot_short; ++c)
+        for (int c = 0; c < CF; ++c)
             for (int k = 0; k < 6; ++k) A.S[(size_t)c * 6 + k] *= iv;
     int64_t row = 0;
     auto put = [&](int64_t r, int c, double v) { out[r * lda + c] = v; };
+    auto put_short = [&](int64_t r, int c, double v) {   // full column c -> printed column
+        const int pc = printed_col(m, c);
+        if (pc >= 0) out[r * lda + pc] = v;
+    };
     std::vector<int> count(m.ctl.natmtyp, 0);
     for (int a = 0; a < fr.natoms; ++a) count[fr.type[a]]++;
-    const int nener = m.tot_all - m.tot_short - m.ncoul;
+    const int nener = m.ctl.fit_ener ? m.ctl.natmtyp : 0;   // types scanned; excluded ones print nothing
+    auto ecol = [&](int t) { return m.ener_col[t]; };
     std::vector<double> Q;
     if (m.ncoul > 0) ewald_deriv(m, of, fr, L, ep, Q);
     for (int a = 0; a < fr.natoms; ++a)
         for (int x = 0; x < 3; ++x, ++row) {
-            for (int c = 0; c < m.tot_short; ++c) put(row, c, A.f(a, c)[x]);
+            for (int c = 0; c < CF; ++c) put_short(row, c, A.f(a, c)[x]);
             for (int p = 0; p < m.ncoul; ++p) put(row, m.tot_short + p, Q[((size_t)p * fr.natoms + a) * 3 + x]);
-            for (int t = 0; t < nener; ++t) put(row, m.tot_short + m.ncoul + t, 0.0);
+            for (int t = 0; t < nener; ++t) if (ecol(t) >= 0) put(row, m.tot_short + m.ncoul + ecol(t), 0.0);
             b[row] = fr.force[3 * a + x];
         }
     if (rl.stress_rows) {
@@ -610,14 +627,14 @@ void frame_rows_out(const Model& m, const Frame& fr, int fi, bool small, double*
         const double xy = fr.stress_off[0], xz = fr.stress_off[1], yz = fr.stress_off[2];
         const double bd3[3] = {xx, yy, zz}, b9[9] = {xx, xy, xz, xy, yy, yz, xz, yz, zz};
         for (int k = 0; k < rl.stress_rows; ++k, ++row) {
-            for (int c = 0; c < m.tot_short; ++c) put(row, c, A.S[(size_t)c * 6 + idx[k]]);
-            for (int t = 0; t < nener; ++t) put(row, m.tot_short + t, 0.0);
+            for (int c = 0; c < CF; ++c) put_short(row, c, A.S[(size_t)c * 6 + idx[k]]);
+            for (int t = 0; t < nener; ++t) if (ecol(t) >= 0) put(row, m.tot_short + ecol(t), 0.0);
             b[row] = (fs ? bd3[k] : b9[k]) / GPA;
         }
     }
     for (int k = 0; k < rl.energy_rows; ++k, ++row) {
-        for (int c = 0; c < m.tot_short; ++c) put(row, c, A.E[c]);
-        for (int t = 0; t < nener; ++t) put(row, m.tot_short + t, (double)count[t]);
+        for (int c = 0; c < CF; ++c) put_short(row, c, A.E[c]);
+        for (int t = 0; t < nener; ++t) if (ecol(t) >= 0) put(row, m.tot_short + ecol(t), (double)count[t]);
         b[row] = fr.energy;
     }
 }
@@ -655,7 +672,7 @@ void md_force_2b(const Model& m, const OFrame& fr, const Lists& L, const double*
             B.fcut(fc, fd, r, p.smax);
             int fa2 = fr.parent[a2];
             for (int i = 0; i < p.snum; ++i) {
-                double coeff = perm * x[pt * p.snum + i];
+                double coeff = p.col < 0 ? 0.0 : perm * x[p.col + i];   // HIERARC-excluded pairs: 0
                 o.E += coeff * fc * Tn[i + 1];
                 double deriv = fc * Tnd[i + 1] + fd * Tn[i + 1];
                 o.P -= coeff * deriv * r;
@@ -806,7 +823,8 @@ void md_force_frame(const Model& m, const Frame& fr, bool small, const double* x
     MdOut o;
     o.F.assign(fr.natoms, V3{0, 0, 0});
     if (offsets)
-        for (int a = 0; a < fr.natoms; ++a) o.E += x[m.tot_short + fr.type[a]];
+        for (int a = 0; a < fr.natoms; ++a)
+            if (m.ener_col[fr.type[a]] >= 0) o.E += x[m.tot_short + m.ncoul + m.ener_col[fr.type[a]]];
     if (m.ctl.cheby_order > 0) md_force_2b(m, of, L, x, pd, ps, o);
     if (m.ctl.use3) md_force_3b(m, of, L, x, o);
     if (m.ctl.use4) md_force_4b(m, of, L, x, o);

@@ -35,7 +35,7 @@ def fixture_dir(name):
     return os.path.join(GOLDEN, name)
 
 
-FIXTURES = ["water2b", "water3b", "ch4b", "small4b", "watercoul", "multifile", "skipframes"]
+FIXTURES = ["water2b", "water3b", "ch4b", "small4b", "watercoul", "multifile", "skipframes", "hierarc"]
 
 
 def frame_part(model, ref):

@@ -21,6 +21,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
 REF = os.path.join(ROOT, "oracle", "_ref", "chimes_lsq")
+REF_PY = "/root/reference/src/chimes_lsq.py"   # the reference's solver script (read in place)
 
 # name -> (workload, overrides, nframes, seed)
 FIXTURES = {
@@ -41,9 +42,12 @@ FIXTURES = {
     # SKPFRMS 2 over 5 frames (frames 0, 2, 4 kept) with stress rows for the first 3
     # trajectory frames only (FITSTRS FIRSTALL 3): the cut-off counts trajectory frames
     "skipframes": ("water-3b", dict(nmol=24, L=8.96, order=(8, 4, 0), fitstrs="FIRSTALL 3", fitener=True), 5, 18),
+    # HIERARC: the O-H 2-body block and the H energy offset left out of A
+    "hierarc": ("water-3b", dict(nmol=24, L=8.96, order=(8, 4, 0), fitstrs="ALL", fitener=True), 2, 19),
 }
 
 SKIP = {"skipframes": 2}
+HIER = {"hierarc": ("EXCLUDE 1B INTERACTION: 1\nH\n\nEXCLUDE 2B INTERACTION: 1\nO H\n")}
 
 
 def make_multifile(d):
@@ -79,6 +83,13 @@ def make(name):
         assert key in fm
         fm = fm.replace(key, key + f"# SKPFRMS #\n\t{SKIP[name]}\n")
         open(os.path.join(d, "fm_setup.in"), "w").write(fm)
+    if name in HIER:
+        fm = open(os.path.join(d, "fm_setup.in")).read()
+        key = f"# NFRAMES #\n\t{nframes}\n"
+        assert key in fm and "# ENDFILE #" in fm
+        fm = fm.replace(key, key + "# HIERARC #\n\ttrue\n")
+        fm = fm.replace("# ENDFILE #", HIER[name] + "\n# ENDFILE #")
+        open(os.path.join(d, "fm_setup.in"), "w").write(fm)
     with tempfile.TemporaryDirectory() as tmp:
         shutil.copy(os.path.join(d, "fm_setup.in"), tmp)
         for f in inputs:
@@ -90,6 +101,11 @@ def make(name):
             shutil.copy(os.path.join(tmp, f), os.path.join(d, f))
         if wl == "multi":   # the labels file carries the per-file flags
             shutil.copy(os.path.join(tmp, "b-labeled.txt"), os.path.join(d, "b-labeled.txt"))
+        if name in HIER:   # the reference's solver script on that A: params.txt with the exclusions
+            out = subprocess.run([sys.executable, REF_PY, "--test_suite", "true"], cwd=tmp, check=True,
+                                 capture_output=True, text=True).stdout
+            open(os.path.join(d, "params.txt"), "w").write(out)
+            shutil.copy(os.path.join(tmp, "test_suite_params.txt"), os.path.join(d, "test_suite_params.txt"))
     np.savez_compressed(os.path.join(d, "ref.npz"), A=A, b=b)
     print(name, A.shape)
 

@@ -395,3 +395,24 @@ def test_split_files_hold_each_ranks_rows(cg, tmp_path):
     assert open(whole_dir / "dim.txt").read() == f"{ms.ncols} {total}\n"
     for f in ("b.txt", "b-labeled.txt", "natoms.txt"):
         assert open(split_dir / f).read() == open(whole_dir / f).read()
+
+
+def test_hierarchical_params_txt_matches_reference_script(cg):
+    """HIERARC fixture (O-H 2-body block and the H energy offset excluded): params.txt
+    from the reference solver script's coefficients is byte-identical to the one the
+    script printed (zeros for the excluded pair and offset), and reads back to them."""
+    d = fixture_dir("hierarc")
+    m = cg.Model(os.path.join(d, "fm_setup.in"))
+    cols = m.columns()
+    ref = np.load(os.path.join(d, "ref.npz"))
+    assert m.ncols == ref["A"].shape[1] == cols["n2b"] + cols["n3b"] + cols["n4b"] + cols["nener"]
+    assert cols["n2b"] == 2 * 8 and cols["nener"] == 1
+    gold = open(os.path.join(d, "params.txt")).read()
+    lines = gold.splitlines(True)
+    k = 0
+    while k < len(lines) and lines[k].startswith("!"):
+        k += 1
+    x = np.array([float(ln.split()[1]) for ln in open(os.path.join(d, "test_suite_params.txt")) if ln.strip()])
+    assert x.size == m.ncols
+    assert m.params_txt(x, "".join(lines[:k])) == gold
+    assert np.array_equal(m.params_read(gold), x)

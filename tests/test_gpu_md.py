@@ -331,3 +331,25 @@ def test_fixed_charge_labels_lose_the_ewald_forces(cg, tmp_path):
         assert np.abs(F).max() > 1.0   # the charges do act
         r0 += 3 * n
         a0 += n
+
+
+def test_hierarchical_md_force_equals_design_matrix(cg):
+    """HIERARC fixture: with the reference solver's coefficients (zeros for the
+    excluded O-H pair and H offset in its params.txt), the MD force read from that
+    params.txt equals A x over the compacted columns, force and energy rows."""
+    d = os.path.join(GOLDEN, "hierarc")
+    model = cg.Model(os.path.join(d, "fm_setup.in"))
+    x = model.params_read(open(os.path.join(d, "params.txt")).read())
+    fr = cg.Frames.read(model)
+    sess = cg.Session(model, 0)
+    A = sess.assemble(fr, cg.CG_FP64)
+    ref = np.load(os.path.join(d, "ref.npz"))
+    colmax = np.abs(ref["A"]).max(axis=0)
+    assert np.all(np.abs(A - ref["A"]) <= 1e-12 * np.abs(ref["A"]) + 1e-12 * colmax[None, :])
+    sess.md_setup(x, energy_offsets=True, penalty_scale=0.0)
+    y = A @ x
+    natoms = 72   # 24 molecules; frame 0's rows: 216 force, 9 stress, 3 energy
+    fr0 = cg.Frames.read(model, nframes=1).independent()
+    F, S = sess.md_force(fr0)
+    assert close(F.reshape(-1), y[:3 * natoms], 1e-10)
+    assert abs(y[3 * natoms + 9] - S[0, 0]) <= 1e-10 * abs(S[0, 0])
