@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libchimes_gb300.so")
 CG_FP64 = 0
 CG_FP32 = 1
 CG_NVT_MTK, CG_NVT_BEREND = 1, 2
+CG_NPT_BEREND, CG_NPT_BEREND_ANISO, CG_NPT_MTK = 3, 4, 5
 MD_ENERGY_OFFSETS = 1
 MD_NSCALAR = 11   # energy, PRESSURE_XYZ/3V, virial tensor/V (3x3 row-major)
 
@@ -115,6 +116,8 @@ def lib():
         "cg_frames_subtract_coulomb": (ctypes.c_int, [vp, vp]),
         "cg_md_nvt": (ctypes.c_int, [vp, vp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, vp, vp, vp, vp, vp]),
+        "cg_md_npt": (ctypes.c_int, [vp, vp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_double, vp, vp, vp, vp, vp, vp]),
         "cg_dframes_positions": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_void_p), i64p]),
         "cg_dframes_read_positions": (ctypes.c_int, [vp, dp]),
         "cg_md_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
@@ -517,6 +520,15 @@ class Session:
                                float(tau_fs), ctypes.c_void_p(int(v_ptr)), ctypes.c_void_p(int(forces_ptr)),
                                ctypes.c_void_p(int(scalars_ptr) or None), ctypes.c_void_p(int(ke_ptr) or None),
                                ctypes.c_void_p(int(cons_ptr) or None)))
+
+    def md_npt(self, dframes, masses, dt_fs, nsteps, style, temperature, tau_fs, pressure_gpa, tau_baro_fs, v_ptr,
+               forces_ptr, scalars_ptr=0, ke_ptr=0, cons_ptr=0, vol_ptr=0):
+        """nsteps NPT steps (cg_md_npt; style CG_NPT_BEREND, CG_NPT_BEREND_ANISO or CG_NPT_MTK)."""
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        opt = [ctypes.c_void_p(int(p) or None) for p in (scalars_ptr, ke_ptr, cons_ptr, vol_ptr)]
+        _check(lib().cg_md_npt(self._h, dframes._h, _ptr(m), float(dt_fs), int(nsteps), int(style), float(temperature),
+                               float(tau_fs), float(pressure_gpa), float(tau_baro_fs), ctypes.c_void_p(int(v_ptr)),
+                               ctypes.c_void_p(int(forces_ptr)), *opt))
 
     def md_serve(self, requests, masses, dt_fs=0.2, hbm_budget=150e9, max_batch_atoms=1 << 16,
                  max_batch_frames=1024, want_step_ms=True):

@@ -483,6 +483,25 @@ int cg_md_nvt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
     });
 }
 
+int cg_md_npt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, int style,
+              double temperature, double tau_fs, double pressure_gpa, double tau_baro_fs, double* velocities,
+              double* forces, double* scalars_steps, double* ke_steps, double* conserved_steps,
+              double* volume_steps) {
+    return guarded([&] {
+        need(s && d && mass && velocities && forces, "session/frames/mass/velocities/forces");
+        need(dt_fs > 0.0 && nsteps >= 0, "dt/nsteps");
+        need(style == CG_NPT_BEREND || style == CG_NPT_BEREND_ANISO || style == CG_NPT_MTK, "barostat style");
+        cg::MdThermostat th;
+        th.style = style;   // 3, 4, 5 as MdThermostat numbers them
+        th.temperature = temperature;
+        th.tau_fs = tau_fs;
+        th.pressure_gpa = pressure_gpa;
+        th.tau_baro_fs = tau_baro_fs;
+        s->s->md_run(*d->d, mass, dt_fs / 48.888, nsteps, th, velocities, forces, scalars_steps, ke_steps,
+                     conserved_steps, volume_steps);
+    });
+}
+
 int cg_md_serve(cg_session* s, int nreq, const cg_md_request* req, const double* mass, double dt_fs,
                 double hbm_budget_bytes, int64_t max_batch_atoms, int max_batch_frames, cg_md_result* results,
                 double* step_ms, int64_t* batch_steps) {

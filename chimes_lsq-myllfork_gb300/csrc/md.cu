@@ -844,11 +844,8 @@ __global__ void k_md_kick(FramesDev F, const double* Fo, const double* inv_mass_
 }
 
 // ------------------------------------------------------------------ thermostats
-// Per-frame thermostat state th[f * MD_TH_STRIDE + ...]: zeta (THERM_VELOC), its
-// force (THERM_FORCE), position (THERM_POSIT), inertia Q, N_DOF kB T, the kinetic
-// energy of the step's incoming velocities, zeta0 / force0 of the step.
+// Per-frame state th[f * MD_TH_STRIDE + TH_*] (md.h);
 // CONSTRAINT::UPDATE_COORDS / UPDATE_VELOCS_HALF_1 / _2, src/ClassDefs.C:867-1352.
-enum { TH_ZETA = 0, TH_FORCE, TH_POSIT, TH_Q, TH_NDOFKT, TH_KCUR, TH_ZETA0, TH_FORCE0 };
 
 __device__ __forceinline__ double block_sum(double v, double* red) {
     v = warp_sum(v);
@@ -1091,15 +1088,242 @@ void launch_md_berend(int nframes, const FramesDev& F, const double* mass_type, 
     if (nframes > 0) k_md_berend<<<nframes, 256, 0, st>>>(F, mass_type, v, dt, tau, T0, kb, ke, bad);
 }
 
-__global__ void k_md_conserved(int nframes, const double* th, int mtk, double* out) {
+// CONSTRAINT::CONSERVED_QUANT src/ClassDefs.C:1481-1511.
+__global__ void k_md_conserved(int nframes, const double* th, int mode, double p0, const BoxDev* box, double* out) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nframes) return;
     const double* t = th + (size_t)f * MD_TH_STRIDE;
-    out[f] = mtk ? 0.5 * t[TH_ZETA] * t[TH_ZETA] * t[TH_Q] + t[TH_NDOFKT] * t[TH_POSIT] : 0.0;
+    if (mode == 1) {
+        out[f] = 0.5 * t[TH_ZETA] * t[TH_ZETA] * t[TH_Q] + t[TH_NDOFKT] * t[TH_POSIT];
+    } else if (mode == 2) {
+        const double tke = 0.5 * t[TH_ZETA] * t[TH_ZETA] * t[TH_Q];
+        const double bke = 0.5 * t[TH_BVEL] * t[TH_BVEL] * t[TH_W];
+        const double tpe = t[TH_NDOF1KT] * t[TH_POSIT];
+        const double bpe = p0 * box[f].vol;
+        out[f] = tke + tpe + bke + bpe;
+    } else {
+        out[f] = 0.0;
+    }
 }
 
-void launch_md_conserved(int nframes, const double* th, int mtk, double* out, cudaStream_t st) {
-    if (nframes > 0) k_md_conserved<<<(nframes + 127) / 128, 128, 0, st>>>(nframes, th, mtk, out);
+void launch_md_conserved(int nframes, const double* th, int mode, double p0, const BoxDev* box, double* out,
+                         cudaStream_t st) {
+    if (nframes > 0) k_md_conserved<<<(nframes + 127) / 128, 128, 0, st>>>(nframes, th, mode, p0, box, out);
+}
+
+// ------------------------------------------------------------------ barostats
+// An orthorhombic cell scaled by (sx, sy, sz): H, H^-1, lengths, volume (BOX::UPDATE_CELL
+// for CELL_AX / BY / CZ only; the neighbour convention of the frame is kept).
+__device__ void box_scale(BoxDev& B, double sx, double sy, double sz) {
+    B.h[0] *= sx; B.h[4] *= sy; B.h[8] *= sz;
+    B.inv[0] = 1.0 / B.h[0]; B.inv[4] = 1.0 / B.h[4]; B.inv[8] = 1.0 / B.h[8];
+    B.lx = B.h[0]; B.ly = B.h[4]; B.lz = B.h[8];
+    B.vol = B.h[0] * B.h[4] * B.h[8];
+}
+
+// NPT-BEREND (-ANISO), CONSTRAINT::UPDATE_COORDS src/ClassDefs.C:883-1001 with the plain
+// first velocity half: K of v(t), x += v dt + a dt^2 / 2, v += a dt / 2, then
+// mu = (1 - dt / kp (P0 - P))^(1/3) with P = PRESSURE_XYZ + 2 K / (3 V) (or the tensor
+// diagonal + 2 K / (3 V) per axis), x *= mu and the cell *= mu.
+__global__ void k_md_npt_berend(FramesDev F, BoxDev* box, const double* mass_type, double* x, double* v,
+                                const double* a, double dt, const double* so_prev, double p0, double kp, int aniso,
+                                int* bad) {
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    double k = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        k += 0.5 * mass_type[F.type[aofs + i / 3]] * v[g] * v[g];
+    }
+    k = block_sum(k, red);
+    BoxDev& B = box[f];
+    const double v0 = B.vol;
+    const double* so = so_prev + (size_t)f * MD_NSCALAR;
+    double mu[3];
+    bool ok = true;
+    if (!aniso) {
+        const double P = so[1] + 2.0 * k / (3.0 * v0);
+        const double fac = 1.0 - dt / kp * (p0 - P);
+        ok = fac >= 0.0;
+        mu[0] = mu[1] = mu[2] = pow(fac, 1.0 / 3.0);
+    } else {
+        for (int d = 0; d < 3; ++d) {
+            const double pd = so[2 + 4 * d] + 2.0 / 3.0 * k / v0;
+            const double fac = 1.0 - dt / kp * (p0 - pd);
+            ok = ok && fac >= 0.0;
+            mu[d] = pow(fac, 1.0 / 3.0);
+        }
+    }
+    if (!ok) {   // the reference stops: negative Berendsen scaling factor
+        if (threadIdx.x == 0) atomicExch(bad, 1);
+        return;
+    }
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        double xi = x[g];
+        xi += v[g] * dt + 0.5 * a[g] * dt * dt;
+        v[g] = v[g] + 0.5 * a[g] * dt;
+        x[g] = xi * mu[i % 3];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) box_scale(B, mu[0], mu[1], mu[2]);
+}
+
+// NPT-MTK first half (one block per frame): the state shift of UPDATE_COORDS, K of
+// v(t); x += v dt + a dt^2/2 - zeta0 v dt^2/2; the thermostat position; barostat
+// position eps = eps0 + veps0 dt + dt^2/2 (Feps0 / W - veps0 zeta0), scale
+// s = exp(eps - eps0); x -= dt^2/2 (2 + 3/N_DOF) veps0 v, then x = s (x - com) + com and
+// the cell *= s; v_iter = (v + a dt/2 - zeta0 v dt/2 - (2 + 3/N_DOF) veps0 v dt/2) s.
+__global__ void k_md_nptmtk_half1(FramesDev F, BoxDev* box, const double* mass_type, double* x, double* v,
+                                  const double* a, double dt, double* th) {
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    double* t = th + (size_t)f * MD_TH_STRIDE;
+    double k = 0.0, mt = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const double m = mass_type[F.type[aofs + i / 3]];
+        k += 0.5 * m * v[g] * v[g];
+        if (i % 3 == 0) mt += m;
+    }
+    k = block_sum(k, red);
+    mt = block_sum(mt, red);
+    const double z0 = t[TH_ZETA], f0 = t[TH_FORCE];
+    const double bp0 = t[TH_BPOS], bv0 = t[TH_BVEL], bf0 = t[TH_BFORCE], W = t[TH_W];
+    const double cdof = 2.0 + 3.0 / t[TH_NDOF];
+    const double bpT = bp0 + bv0 * dt + 0.5 * dt * dt * bf0 / W - 0.5 * dt * dt * bv0 * z0;
+    const double sc = exp(bpT - bp0);
+    // drift and thermostat, then the centre of mass of those positions
+    double cm[3] = {0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const double vi = v[g], ai = a[g];
+        double xi = x[g] + (vi * dt + 0.5 * ai * dt * dt);
+        xi -= 0.5 * z0 * vi * dt * dt;
+        x[g] = xi;
+        cm[i % 3] += mass_type[F.type[aofs + i / 3]] * xi;
+    }
+    double com[3];
+    for (int d = 0; d < 3; ++d) com[d] = block_sum(cm[d], red) / mt;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const double vi = v[g], ai = a[g];
+        double xi = x[g];
+        xi -= 0.5 * dt * dt * cdof * bv0 * vi;
+        x[g] = sc * (xi - com[i % 3]) + com[i % 3];
+        double vn = vi + 0.5 * ai * dt;
+        vn -= 0.5 * z0 * vi * dt;
+        vn -= 0.5 * cdof * bv0 * vi * dt;
+        v[g] = vn * sc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        t[TH_KCUR] = k;
+        t[TH_ZETA0] = z0;
+        t[TH_FORCE0] = f0;
+        t[TH_BVEL0] = bv0;
+        t[TH_BFORCE0] = bf0;
+        t[TH_POSIT] = t[TH_POSIT] + z0 * dt + 0.5 * dt * dt * f0;
+        t[TH_BPOS] = bpT;
+        t[TH_SCALE] = sc;
+        box_scale(box[f], sc, sc, sc);
+        t[TH_VOL] = box[f].vol;
+    }
+}
+
+// NPT-MTK second half (one block per frame), UPDATE_VELOCS_HALF_2 src/ClassDefs.C:1262-1419:
+// u = v_iter + a dt/2; initial guess from K(v(t)); then 10 rounds of v = u / s,
+// K = K(u) / s^2, barostat force 3/N_DOF 2K + 3 V (P + 2K/(3V) - P0), thermostat
+// force (2K + W veps^2 - (N_DOF+1) kB T) / Q, zeta, veps and s; v keeps the last
+// round's u / s.
+__global__ void k_md_nptmtk_half2(FramesDev F, const double* Fo, const double* inv_mass_type,
+                                  const double* mass_type, const double* so, double p0, double* acc, double* v,
+                                  double dt, double* th, double* ke) {
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    double* t = th + (size_t)f * MD_TH_STRIDE;
+    double ku = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const int ty = F.type[aofs + i / 3];
+        const double ai = Fo[g] * inv_mass_type[ty];
+        acc[g] = ai;
+        const double u = v[g] + 0.5 * ai * dt;
+        v[g] = u;
+        ku += 0.5 * mass_type[ty] * u * u;
+    }
+    ku = block_sum(ku, red);
+    const double Q = t[TH_Q], W = t[TH_W], ndof = t[TH_NDOF], n1kt = t[TH_NDOF1KT];
+    const double z0 = t[TH_ZETA0], f0 = t[TH_FORCE0], bv0 = t[TH_BVEL0], bf0 = t[TH_BFORCE0];
+    const double VT = t[TH_VOL], P = so[(size_t)f * MD_NSCALAR + 1];
+    const double cdof = 2.0 + 3.0 / ndof;
+    double K = t[TH_KCUR];
+    double dP = P + 2.0 * K / (3.0 * VT) - p0;
+    double bfT = 3.0 / ndof * 2.0 * K + 3.0 * VT * dP;
+    double tfT = (2.0 * K + W * bv0 * bv0 - n1kt) / Q;
+    double zT = z0 + (f0 + tfT) * 0.5 * dt;
+    double bvT = bv0 + 0.5 * dt * (bf0 / W - bv0 * z0 + bfT / W - bv0 * zT);
+    double s = 1.0 + 0.5 * dt * (zT + cdof * bvT);
+    double s_used = s;
+    for (int itr = 0; itr < 10; ++itr) {
+        s_used = s;
+        K = ku / (s_used * s_used);
+        dP = P + 2.0 * K / (3.0 * VT) - p0;
+        bfT = 3.0 / ndof * 2.0 * K + 3.0 * VT * dP;
+        tfT = (2.0 * K + W * bvT * bvT - n1kt) / Q;
+        zT = z0 + (f0 + tfT) * 0.5 * dt;
+        bvT = bv0 + 0.5 * dt * (bf0 / W - bv0 * z0 + bfT / W - bvT * zT);
+        s = 1.0 + 0.5 * dt * (zT + cdof * bvT);
+    }
+    double k = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        const double vn = v[g] / s_used;
+        v[g] = vn;
+        k += 0.5 * mass_type[F.type[aofs + i / 3]] * vn * vn;
+    }
+    k = block_sum(k, red);
+    if (threadIdx.x == 0) {
+        t[TH_ZETA] = zT;
+        t[TH_FORCE] = tfT;
+        t[TH_BVEL] = bvT;
+        t[TH_BFORCE] = bfT;
+        if (ke) ke[f] = k;
+    }
+}
+
+__global__ void k_md_volume(int nframes, const BoxDev* box, double* out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < nframes) out[f] = box[f].vol;
+}
+
+void launch_md_npt_berend(int nframes, const FramesDev& F, BoxDev* box, const double* mass_type, double* x,
+                          double* v, const double* acc, double dt, const double* so_prev, double p0, double kp,
+                          int aniso, int* bad, cudaStream_t st) {
+    if (nframes > 0)
+        k_md_npt_berend<<<nframes, 256, 0, st>>>(F, box, mass_type, x, v, acc, dt, so_prev, p0, kp, aniso, bad);
+}
+
+void launch_md_nptmtk_half1(int nframes, const FramesDev& F, BoxDev* box, const double* mass_type, double* x,
+                            double* v, const double* acc, double dt, double* th, cudaStream_t st) {
+    if (nframes > 0) k_md_nptmtk_half1<<<nframes, 256, 0, st>>>(F, box, mass_type, x, v, acc, dt, th);
+}
+
+void launch_md_nptmtk_half2(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
+                            const double* mass_type, const double* so, double p0, double* acc, double* v, double dt,
+                            double* th, double* ke, cudaStream_t st) {
+    if (nframes > 0)
+        k_md_nptmtk_half2<<<nframes, 256, 0, st>>>(F, Fo, inv_mass_type, mass_type, so, p0, acc, v, dt, th, ke);
+}
+
+void launch_md_volume(int nframes, const BoxDev* box, double* out, cudaStream_t st) {
+    if (nframes > 0) k_md_volume<<<(nframes + 127) / 128, 128, 0, st>>>(nframes, box, out);
 }
 
 }  // namespace cgd

@@ -79,8 +79,35 @@ void launch_md_drift(int64_t natoms, const FramesDev& F, const unsigned char* fi
 void launch_md_kick(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
                     const double* mass_type, double* acc, double* v, double dt, int half, const unsigned char* first,
                     double* ke, cudaStream_t st);
-// Thermostats (NVT-MTK, NVT-BEREND): per-frame state of MD_TH_STRIDE doubles.
-constexpr int MD_TH_STRIDE = 8;
+// Thermostats and barostats (NVT-MTK, NVT-BEREND, NPT-BEREND(-ANISO), NPT-MTK):
+// per-frame state of MD_TH_STRIDE doubles, CONSTRAINT's members
+// (src/ClassDefs.C:479-520): thermostat velocity zeta, force, position, inertia Q,
+// N_DOF kB T, the kinetic energy of the step's incoming velocities, zeta / force at
+// the step's start; barostat position, velocity, force, inertia W and their values
+// at the step's start, the volume after the step's coordinate update and the
+// barostat's box scale.
+enum {
+    TH_ZETA = 0, TH_FORCE, TH_POSIT, TH_Q, TH_NDOFKT, TH_KCUR, TH_ZETA0, TH_FORCE0,
+    TH_BPOS, TH_BVEL, TH_BFORCE, TH_W, TH_BVEL0, TH_BFORCE0, TH_VOL, TH_NDOF, TH_NDOF1KT, TH_SCALE
+};
+constexpr int MD_TH_STRIDE = 18;
+// NPT-BEREND / NPT-BEREND-ANISO coordinate step (one block per frame): drift and
+// half kick, then x and the orthorhombic cell scaled by (1 - dt/kp (P0 - P))^(1/3)
+// with P from so_prev (the last force call's PRESSURE_XYZ or tensor diagonal) plus
+// the kinetic term of v(t).  box is the frames' device cell array.
+void launch_md_npt_berend(int nframes, const FramesDev& F, BoxDev* box, const double* mass_type, double* x,
+                          double* v, const double* acc, double dt, const double* so_prev, double p0, double kp,
+                          int aniso, int* bad, cudaStream_t st);
+// NPT-MTK (Martyna, Tobias, Klein 1994 as CONSTRAINT does it): coordinates,
+// thermostat and barostat positions, cell scale and the first velocity half; then
+// the second half with the 10-step fixed point of thermostat and barostat velocity.
+void launch_md_nptmtk_half1(int nframes, const FramesDev& F, BoxDev* box, const double* mass_type, double* x,
+                            double* v, const double* acc, double dt, double* th, cudaStream_t st);
+void launch_md_nptmtk_half2(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
+                            const double* mass_type, const double* so, double p0, double* acc, double* v, double dt,
+                            double* th, double* ke, cudaStream_t st);
+// Volume of each frame's cell into out[f].
+void launch_md_volume(int nframes, const BoxDev* box, double* out, cudaStream_t st);
 void launch_md_mtk_half1(int nframes, const FramesDev& F, const double* mass_type, double* x, double* v,
                          const double* acc, double dt, double* th, cudaStream_t st);
 void launch_md_mtk_half2(int nframes, const FramesDev& F, const double* Fo, const double* inv_mass_type,
@@ -88,6 +115,8 @@ void launch_md_mtk_half2(int nframes, const FramesDev& F, const double* Fo, cons
                          cudaStream_t st);
 void launch_md_berend(int nframes, const FramesDev& F, const double* mass_type, double* v, double dt, double tau,
                       double T0, double kb, double* ke, int* bad, cudaStream_t st);
-void launch_md_conserved(int nframes, const double* th, int mtk, double* out, cudaStream_t st);
+// Conserved-quantity term per frame: mode 1 NVT-MTK, 2 NPT-MTK (with p0 V), 0 none.
+void launch_md_conserved(int nframes, const double* th, int mode, double p0, const BoxDev* box, double* out,
+                         cudaStream_t st);
 
 }  // namespace cgd

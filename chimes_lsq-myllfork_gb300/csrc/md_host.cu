@@ -483,7 +483,7 @@ void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int n
 }
 
 void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int nsteps, const MdThermostat& th, double* v,
-                     double* Fo, double* So_steps, double* ke_steps, double* cons_steps) {
+                     double* Fo, double* So_steps, double* ke_steps, double* cons_steps, double* vol_steps) {
     CK(cudaSetDevice(device_));
     if (!md_) throw Error(1, "MD coefficients are not set (cg_md_setup)");
     if (nsteps < 0) throw Error(1, "negative step count");
@@ -506,17 +506,31 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
     const cgd::FramesDev& F = df.dev;
     // thermostat state per frame (CONSTRAINT::INITIALIZE src/ClassDefs.C:525-585):
     // N_DOF = 3N - 3, Q = N_DOF kB T tau^2 / Tfs^2 (tau in fs), Berendsen tau / Tfs
-    const double kb = 0.0019872067, tfs = 48.888;   // src/functions.h:43-44
+    const double kb = 0.0019872067, tfs = 48.888, gpa = 6.9476955;   // src/functions.h:43-45
     double* thd = nullptr;
     int* bad = nullptr;
+    const bool baro = th.style >= 3;
+    if (th.style < 0 || th.style > 5) throw Error(1, "unknown thermostat / barostat style");
+    if (baro) {   // src/chimes_md.C:556-563: orthorhombic cells only
+        if (!(th.tau_baro_fs > 0.0)) throw Error(1, "the barostat needs a positive time constant");
+        for (const auto& b : df.box_host)
+            if (!b.is_ortho) throw Error(2, "NPT-BEREND, NPT-BEREND-ANISO and NPT-MTK need orthorhombic cells");
+        if (md_->dev.coulomb) throw Error(2, "NPT with Ewald charges is not supported by this build");
+    }
+    const double p0 = th.pressure_gpa / gpa;
     if (th.style != 0) {
         if (!(th.temperature > 0.0) || !(th.tau_fs > 0.0))
             throw Error(1, "the thermostat needs a positive temperature and time constant");
         std::vector<double> h((size_t)nf * cgd::MD_TH_STRIDE, 0.0);
         for (int f = 0; f < nf; ++f) {
             const double ndof = 3.0 * df.natoms_host.at(f) - 3.0;
-            h[(size_t)f * cgd::MD_TH_STRIDE + 3] = ndof * kb * th.temperature * th.tau_fs * th.tau_fs / tfs / tfs;
-            h[(size_t)f * cgd::MD_TH_STRIDE + 4] = ndof * kb * th.temperature;
+            double* t = &h[(size_t)f * cgd::MD_TH_STRIDE];
+            t[cgd::TH_Q] = ndof * kb * th.temperature * th.tau_fs * th.tau_fs / tfs / tfs;
+            t[cgd::TH_NDOFKT] = ndof * kb * th.temperature;
+            t[cgd::TH_W] = (ndof + 3.0) * kb * th.temperature * th.tau_baro_fs * th.tau_baro_fs / tfs / tfs;
+            t[cgd::TH_NDOF] = ndof;
+            t[cgd::TH_NDOF1KT] = (ndof + 1.0) * kb * th.temperature;
+            t[cgd::TH_SCALE] = 1.0;
         }
         thd = S.get<double>(h.size());
         bad = S.get<int>(1);
@@ -524,13 +538,20 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
         CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
     }
     MdListSet lists;
+    cgd::BoxDev* dbox = const_cast<cgd::BoxDev*>(F.box);   // the barostats rescale the cells in place
+    const double* so_prev = nullptr;
     for (int step = 0; step <= nsteps; ++step) {
         if (step > 0) {   // UPDATE_COORDS + VELOCS_HALF_1
             if (th.style == 1) cgd::launch_md_mtk_half1(nf, F, dm, df.xyz, v, acc, dt, thd, st);
+            else if (th.style == 3 || th.style == 4)
+                cgd::launch_md_npt_berend(nf, F, dbox, dm, df.xyz, v, acc, dt, so_prev, p0, th.tau_baro_fs / tfs,
+                                          th.style == 4, bad, st);
+            else if (th.style == 5) cgd::launch_md_nptmtk_half1(nf, F, dbox, dm, df.xyz, v, acc, dt, thd, st);
             else cgd::launch_md_drift(n, F, nullptr, df.xyz, v, acc, dt, st);
         }
         double* sout = So_steps ? So_steps + (size_t)step * nf * cgd::MD_NSCALAR : so;
-        if (md_skin_ > 0.0) {
+        so_prev = sout;
+        if (md_skin_ > 0.0 && !baro) {   // a changing cell rebuilds every step
             md_force_step(df, lists, Fo, sout);
         } else {
             md_force(df, Fo, sout, nullptr);
@@ -538,22 +559,31 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
         double* ke = ke_steps ? ke_steps + (size_t)step * nf : nullptr;
         if (th.style == 1 && step > 0) {   // a = F/m, VELOCS_HALF_2 with the MTK iteration
             cgd::launch_md_mtk_half2(nf, F, Fo, dim, dm, acc, v, dt, thd, ke, st);
+        } else if (th.style == 5 && step > 0) {   // with the barostat
+            cgd::launch_md_nptmtk_half2(nf, F, Fo, dim, dm, sout, p0, acc, v, dt, thd, ke, st);
         } else {
             cgd::launch_md_kick(nf, F, Fo, dim, dm, acc, v, dt, step > 0 ? 1 : 0, nullptr, ke, st);
-            if (th.style == 2 && step > 0)
+            if ((th.style == 2 || th.style == 3 || th.style == 4) && step > 0)
                 cgd::launch_md_berend(nf, F, dm, v, dt, th.tau_fs / tfs, th.temperature, kb, ke, bad, st);
         }
-        if (cons_steps && thd) {   // CONSERVED_QUANT: Q zeta^2 / 2 + N_DOF kB T posit (NVT-MTK)
-            cgd::launch_md_conserved(nf, thd, th.style == 1, cons_steps + (size_t)step * nf, st);
+        if (cons_steps && thd) {   // CONSERVED_QUANT (NVT-MTK, NPT-MTK)
+            cgd::launch_md_conserved(nf, thd, th.style == 1 ? 1 : (th.style == 5 ? 2 : 0), p0, F.box,
+                                     cons_steps + (size_t)step * nf, st);
         }
+        if (vol_steps) cgd::launch_md_volume(nf, F.box, vol_steps + (size_t)step * nf, st);
         CK(cudaGetLastError());
+    }
+    if (baro) {   // keep the host copy of the cells current
+        CK(cudaMemcpyAsync(df.box_host.data(), F.box, df.box_host.size() * sizeof(cgd::BoxDev),
+                           cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
     }
     if (bad) {
         int hb = 0;
         CK(cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        if (hb) throw Error(2, "Berendsen temperature scale became negative: decrease the time step or increase the "
-                               "thermostat time");
+        if (hb) throw Error(2, "a Berendsen scale factor became negative: decrease the time step or increase the "
+                               "thermostat / barostat time");
     }
 }
 

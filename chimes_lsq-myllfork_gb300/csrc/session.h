@@ -126,9 +126,12 @@ struct MdListSet {
 
 // Thermostat of an MD run: style 0 NVE, 1 NVT-MTK (Nose-Hoover chain of one, MTK
 // integration), 2 NVT-BEREND; temperature in K, time constant in fs.
+// style: 0 NVE, 1 NVT-MTK, 2 NVT-BEREND, 3 NPT-BEREND, 4 NPT-BEREND-ANISO, 5 NPT-MTK
+// (CONSTRAINT::INITIALIZE src/ClassDefs.C:527-585); pressure in GPa, time constants in fs.
 struct MdThermostat {
     int style = 0;
     double temperature = 0.0, tau_fs = 0.0;
+    double pressure_gpa = 0.0, tau_baro_fs = 0.0;
 };
 
 // One MD request of the serving loop (host arrays owned by the caller).
@@ -248,7 +251,7 @@ class Session {
     // cons_steps ((nsteps+1) * nframes, device, may be null) receives the
     // thermostat's conserved-quantity term (NVT-MTK).
     void md_run(DeviceFrames& df, const double* mass_type, double dt, int nsteps, const MdThermostat& th, double* v,
-                double* Fo, double* So_steps, double* ke_steps, double* cons_steps);
+                double* Fo, double* So_steps, double* ke_steps, double* cons_steps, double* vol_steps = nullptr);
     // Continuous-batching serving loop: requests are admitted on arrival while the
     // batch has room (atoms, frames, memory budget), every batched step advances all
     // admitted requests by one velocity-Verlet step, finished requests leave at once.

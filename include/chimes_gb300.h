@@ -281,6 +281,23 @@ int cg_md_nvt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
               double temperature, double tau_fs, double* velocities, double* forces, double* scalars_steps,
               double* ke_steps, double* conserved_steps);
 
+/* NPT runs on uploaded frames (orthorhombic cells; the cells on the device change
+ * with the run): CG_NPT_BEREND = `CONSRNT NPT-BEREND tau tau_baro` (Berendsen
+ * velocity and isotropic position/cell scaling), CG_NPT_BEREND_ANISO = per-axis cell
+ * scaling from the pressure tensor's diagonal, CG_NPT_MTK = `NPT-MTK HOOVER tau
+ * tau_baro` (Martyna-Tobias-Klein thermostat and barostat with the reference's
+ * 10-step velocity iteration).  Replaces CONSTRAINT::UPDATE_COORDS /
+ * UPDATE_VELOCS_HALF_1 / _2 for those styles (src/ClassDefs.C:867-1424).
+ * pressure in GPa (PRESSUR), time constants in fs; conserved_steps as cg_md_nvt
+ * (NPT-MTK: thermostat and barostat energies + P V; 0 for Berendsen);
+ * volume_steps ((nsteps+1) * nframes, device, may be NULL) receives each frame's
+ * cell volume after each step. */
+enum { CG_NPT_BEREND = 3, CG_NPT_BEREND_ANISO = 4, CG_NPT_MTK = 5 };
+int cg_md_npt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, int nsteps, int style,
+              double temperature, double tau_fs, double pressure_gpa, double tau_baro_fs, double* velocities,
+              double* forces, double* scalars_steps, double* ke_steps, double* conserved_steps,
+              double* volume_steps);
+
 /* Continuous-batching MD serving (no counterpart in the reference, whose chimes_md
  * runs one system).  Each request runs nsteps velocity-Verlet NVE steps (step 0
  * evaluates forces only, as chimes_md's first step) from its own positions and

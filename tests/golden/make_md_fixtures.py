@@ -235,9 +235,44 @@ def make_nvt(name="md_ch4b", steps=20):
     print(name, "nvt", {k: v.shape for k, v in out.items()})
 
 
+def make_npt(name="md_ch4b", steps=20, pressure=1.0):
+    """CONSRNT NPT-BEREND 50 100, NPT-BEREND-ANISO 50 100 and NPT-MTK HOOVER 10 100 at
+    PRESSUR 1 GPa: the reference's per-step table (step, time, K/N, V/N, E/N, T, P,
+    volume) and forces."""
+    d = np.load(os.path.join(HERE, name, "md_ref.npz"))
+    model = cg.Model(os.path.join(HERE, name, "fm_setup.in"))
+    names, _ = header_types(model)
+    n = len(d["types"])
+    out = {}
+    for key, consrnt in (("berend", "NPT-BEREND 50 100"), ("aniso", "NPT-BEREND-ANISO 50 100"),
+                         ("mtk", "NPT-MTK HOOVER 10 100")):
+        with tempfile.TemporaryDirectory() as tmp:
+            write_inputs(tmp, model, names, d, consrnt, steps)
+            run = open(os.path.join(tmp, "run_md.in")).read()
+            run = run.replace("# TEMPERA #\n\t300.0\n", f"# TEMPERA #\n\t300.0\n# PRESSUR #\n\t{pressure}\n")
+            open(os.path.join(tmp, "run_md.in"), "w").write(run)
+            p = subprocess.run([REF_MD, "run_md.in"], cwd=tmp, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                               text=True)
+            if p.returncode != 0:
+                raise RuntimeError(f"chimes_md failed ({consrnt}):\n{p.stdout[-2000:]}")
+            table = []
+            body = p.stdout.split("Ktot/N", 1)[1].split("END SIMULATION", 1)[0]
+            for ln in body.splitlines():
+                w = ln.split()
+                if len(w) == 8 and w[0].isdigit():
+                    table.append([float(t) for t in w])
+            out[f"table_{key}"] = np.array(table)
+            out[f"forces_{key}"] = np.loadtxt(os.path.join(tmp, "forceout.txt")).reshape(-1, n, 3)
+    np.savez_compressed(os.path.join(HERE, name, "md_npt.npz"), steps=steps, tau=10.0, tau_berend=50.0,
+                        tau_baro=100.0, temperature=300.0, pressure=pressure, **out)
+    print(name, "npt", {k: v.shape for k, v in out.items()})
+
+
 if __name__ == "__main__":
-    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "md_watercoul"]):
-        if nm == "nvt":
+    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "md_watercoul"]):
+        if nm == "npt":
+            make_npt()
+        elif nm == "nvt":
             make_nvt()
         elif nm == "md_watercoul":
             make_coul()

@@ -353,3 +353,41 @@ def test_hierarchical_md_force_equals_design_matrix(cg):
     F, S = sess.md_force(fr0)
     assert close(F.reshape(-1), y[:3 * natoms], 1e-10)
     assert abs(y[3 * natoms + 9] - S[0, 0]) <= 1e-10 * abs(S[0, 0])
+
+
+@pytest.mark.parametrize("style", ["berend", "aniso", "mtk"])
+def test_md_npt_matches_reference_run(cg, style):
+    """CONSRNT NPT-BEREND 50 100, NPT-BEREND-ANISO 50 100 and NPT-MTK HOOVER 10 100 at
+    1 GPa against the reference chimes_md on the 4-body fixture
+    (tests/golden/md_ch4b/md_npt.npz, 20 steps): per-step Ktot/N, Vtot/N, P and the
+    cell volume to the printed digits, and the last step's forces (1e-8)."""
+    torch = pytest.importorskip("torch")
+    fm, d = load_md("md_ch4b")
+    t = np.load(os.path.join(GOLDEN, "md_ch4b", "md_npt.npz"))
+    tab = t[f"table_{style}"]
+    n = len(d["types"])
+    steps = int(t["steps"]) - 1
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.md_setup(d["x"], energy_offsets=True)
+    fr = cg.Frames.from_arrays(model, [n], d["types"], d["xyz"], d["cell"][None]).independent()
+    dfr = sess.upload(fr)
+    v = torch.from_numpy(d["v"].reshape(-1).copy()).cuda()
+    Fd = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    So = torch.zeros((steps + 1, 11), dtype=torch.float64, device="cuda")
+    ke = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    vol = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    st = {"berend": cg.CG_NPT_BEREND, "aniso": cg.CG_NPT_BEREND_ANISO, "mtk": cg.CG_NPT_MTK}[style]
+    tau = float(t["tau"] if style == "mtk" else t["tau_berend"])
+    sess.md_npt(dfr, d["masses"], float(d["dt"]), steps, st, float(t["temperature"]), tau, float(t["pressure"]),
+                float(t["tau_baro"]), v.data_ptr(), Fd.data_ptr(), So.data_ptr(), ke.data_ptr(), 0, vol.data_ptr())
+    torch.cuda.synchronize()
+    So_h, ke_h, V_h = So.cpu().numpy(), ke.cpu().numpy(), vol.cpu().numpy()
+    assert close(Fd.cpu().numpy().reshape(n, 3), t[f"forces_{style}"][steps], 1e-8)
+    for s in range(steps + 1):
+        kn, vn = ke_h[s] / n, So_h[s, 0] / n
+        p = (So_h[s, 1] + 2.0 * ke_h[s] / (3.0 * V_h[s])) * GPA
+        assert abs(kn - tab[s, 2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, tab[s, 2])
+        assert abs(vn - tab[s, 3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, tab[s, 3])
+        assert abs(p - tab[s, 6]) <= 5e-9 * max(1.0, abs(p)) + 1e-12, (s, p, tab[s, 6])
+        assert abs(V_h[s] - tab[s, 7]) <= 5e-8 * tab[s, 7], (s, V_h[s], tab[s, 7])
