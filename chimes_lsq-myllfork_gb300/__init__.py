@@ -26,6 +26,7 @@ CG_FP64 = 0
 CG_FP32 = 1
 CG_NVT_MTK, CG_NVT_BEREND = 1, 2
 CG_NPT_BEREND, CG_NPT_BEREND_ANISO, CG_NPT_MTK = 3, 4, 5
+CG_TRAJ_GEN, CG_TRAJ_XYZ, CG_TRAJ_LAMMPSTRJ = 1, 2, 3
 MD_ENERGY_OFFSETS = 1
 MD_NSCALAR = 11   # energy, PRESSURE_XYZ/3V, virial tensor/V (3x3 row-major)
 
@@ -118,6 +119,15 @@ def lib():
                                      ctypes.c_double, vp, vp, vp, vp, vp]),
         "cg_md_npt": (ctypes.c_int, [vp, vp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_double, ctypes.c_double, vp, vp, vp, vp, vp, vp]),
+        "cg_md_write_traj": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp, vp, vp,
+                                            vp]),
+        "cg_md_write_xyzv": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int, vp, vp, vp, vp, ctypes.c_int]),
+        "cg_md_write_restart": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, vp, vp, vp, vp, vp,
+                                               ctypes.c_int, ctypes.c_double, vp, ctypes.c_int]),
+        "cg_md_read_restart": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int, vp, vp, vp, vp, vp,
+                                              ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), vp, vp]),
+        "cg_md_resume": (ctypes.c_int, [vp, ctypes.c_int, vp]),
         "cg_dframes_positions": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_void_p), i64p]),
         "cg_dframes_read_positions": (ctypes.c_int, [vp, dp]),
         "cg_md_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
@@ -208,6 +218,36 @@ class Model:
 
     def ff_groups_map(self):
         return self._text(lib().cg_model_map_text)
+
+    def md_write_traj(self, fmt, path, frame_index, step, dt_fs, temperature, types, xyz, v, cell, wrap=False):
+        """One trajectory frame (cg_md_write_traj; fmt CG_TRAJ_GEN / _XYZ / _LAMMPSTRJ)."""
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        c = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        _check(lib().cg_md_write_traj(self._h, int(fmt), os.fspath(path).encode(), int(frame_index), int(step),
+                                      float(dt_fs), float(temperature), int(bool(wrap)), len(t), _ptr(t), _ptr(x),
+                                      _ptr(vv), _ptr(c)))
+
+    def md_write_xyzv(self, path, types, xyz, v, cell, wrap=False):
+        """output.xyz of a run (cg_md_write_xyzv)."""
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        vv = np.ascontiguousarray(v, dtype=np.float64)
+        c = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        _check(lib().cg_md_write_xyzv(self._h, os.fspath(path).encode(), len(t), _ptr(t), _ptr(x), _ptr(vv), _ptr(c),
+                                      int(bool(wrap))))
+
+    def md_read_restart(self, path, natoms):
+        """restart.xyzv -> dict(types, xyz, v, acc, cell, step, padding, constraint[29], avg[7])."""
+        n = int(natoms)
+        t = np.zeros(n, dtype=np.int32)
+        x, v, a = (np.zeros((n, 3)) for _ in range(3))
+        c, c29, avg = np.zeros(9), np.zeros(29), np.zeros(7)
+        step, pad = ctypes.c_int(), ctypes.c_double()
+        _check(lib().cg_md_read_restart(self._h, os.fspath(path).encode(), n, _ptr(t), _ptr(x), _ptr(v), _ptr(a),
+                                        _ptr(c), ctypes.byref(step), ctypes.byref(pad), _ptr(c29), _ptr(avg)))
+        return dict(types=t, xyz=x, v=v, acc=a, cell=c, step=step.value, padding=pad.value, constraint=c29, avg=avg)
 
     def params_read(self, text):
         """Coefficient vector of a params.txt text written for this model."""
@@ -529,6 +569,21 @@ class Session:
         _check(lib().cg_md_npt(self._h, dframes._h, _ptr(m), float(dt_fs), int(nsteps), int(style), float(temperature),
                                float(tau_fs), float(pressure_gpa), float(tau_baro_fs), ctypes.c_void_p(int(v_ptr)),
                                ctypes.c_void_p(int(forces_ptr)), *opt))
+
+    def md_write_restart(self, frame, path, types, xyz, v, acc, cell, step, rcut_padding, avg7=None, wrap=False):
+        """restart.xyzv of one frame after the last MD run (cg_md_write_restart)."""
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        x, vv, a = (np.ascontiguousarray(z, dtype=np.float64) for z in (xyz, v, acc))
+        c = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        av = None if avg7 is None else np.ascontiguousarray(avg7, dtype=np.float64)
+        _check(lib().cg_md_write_restart(self._h, int(frame), os.fspath(path).encode(), len(t), _ptr(t), _ptr(x),
+                                         _ptr(vv), _ptr(a), _ptr(c), int(step), float(rcut_padding), _ptr(av),
+                                         int(bool(wrap))))
+
+    def md_resume(self, constraint29):
+        """The next md_nvt / md_npt starts from these CONSTRAINT values ([nframes, 29])."""
+        c = np.ascontiguousarray(constraint29, dtype=np.float64).reshape(-1, 29)
+        _check(lib().cg_md_resume(self._h, c.shape[0], _ptr(c)))
 
     def md_serve(self, requests, masses, dt_fs=0.2, hbm_budget=150e9, max_batch_atoms=1 << 16,
                  max_batch_frames=1024, want_step_ms=True):

@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libchimes_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["geom.cu", "assemble.cu", "ewald.cu", "session.cu", "gram.cu", "solve.cu", "md.cu", "md_host.cu", "lars.cu"]
-CPP_SOURCES = ["model.cpp", "capi.cpp", "textio.cpp"]
+CPP_SOURCES = ["model.cpp", "capi.cpp", "textio.cpp", "mdio.cpp"]
 
 
 def _nvcc():

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -11,6 +12,7 @@
 #include "model.h"
 #include "session.h"
 #include "textio.h"
+#include "mdio.h"
 
 struct cg_model {
     cg::Model m;
@@ -499,6 +501,63 @@ int cg_md_npt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
         th.tau_baro_fs = tau_baro_fs;
         s->s->md_run(*d->d, mass, dt_fs / 48.888, nsteps, th, velocities, forces, scalars_steps, ke_steps,
                      conserved_steps, volume_steps);
+    });
+}
+
+int cg_md_write_traj(const cg_model* h, int format, const char* path, int frame_index, int step, double dt_fs,
+                     double temperature, int wrap, int natoms, const int* types, const double* xyz,
+                     const double* velocities, const double* cell) {
+    return guarded([&] {
+        need(h && path && types && xyz && cell && natoms >= 0 && frame_index >= 0, "model/path/arrays");
+        need(format == CG_TRAJ_GEN || format == CG_TRAJ_XYZ || format == CG_TRAJ_LAMMPSTRJ, "trajectory format");
+        cg::MdConfig c{natoms, types, xyz, velocities, cell};
+        cg::write_traj_frame(h->m, (cg::TrajFormat)format, path, frame_index, step, dt_fs, temperature, wrap != 0, c);
+    });
+}
+
+int cg_md_write_xyzv(const cg_model* h, const char* path, int natoms, const int* types, const double* xyz,
+                     const double* velocities, const double* cell, int wrap) {
+    return guarded([&] {
+        need(h && path && types && xyz && velocities && cell && natoms >= 0, "model/path/arrays");
+        cg::MdConfig c{natoms, types, xyz, velocities, cell};
+        cg::write_xyzv(h->m, path, c, wrap != 0, nullptr, 0, 0.0, nullptr, nullptr);
+    });
+}
+
+int cg_md_write_restart(cg_session* s, int frame, const char* path, int natoms, const int* types, const double* xyz,
+                        const double* velocities, const double* accel, const double* cell, int step,
+                        double rcut_padding, const double* avg7, int wrap) {
+    return guarded([&] {
+        need(s && path && types && xyz && velocities && accel && cell && natoms >= 0, "session/path/arrays");
+        const std::vector<double> c29 = s->s->md_restart_fields(frame);
+        cg::MdConfig c{natoms, types, xyz, velocities, cell};
+        cg::write_xyzv(s->s->model(), path, c, wrap != 0, accel, step + 1, rcut_padding, c29.data(), avg7);
+    });
+}
+
+int cg_md_read_restart(const cg_model* h, const char* path, int natoms, int* types, double* xyz,
+                       double* velocities, double* accel, double* cell, int* step, double* rcut_padding,
+                       double* constraint29, double* avg7) {
+    return guarded([&] {
+        need(h && path, "model/path");
+        cg::MdRestart r = cg::read_restart(h->m, path);
+        need((int)r.types.size() == natoms, "natoms (does not match the restart file)");
+        if (types) std::copy(r.types.begin(), r.types.end(), types);
+        if (xyz) std::copy(r.xyz.begin(), r.xyz.end(), xyz);
+        if (velocities) std::copy(r.v.begin(), r.v.end(), velocities);
+        if (accel) std::copy(r.acc.begin(), r.acc.end(), accel);
+        if (cell) std::copy(r.cell, r.cell + 9, cell);
+        if (step) *step = r.step;
+        if (rcut_padding) *rcut_padding = r.rcut_padding;
+        if (constraint29) std::copy(r.constraint, r.constraint + cg::RESTART_CONSTRAINT_FIELDS, constraint29);
+        if (avg7) std::copy(r.avg, r.avg + cg::RESTART_AVG_FIELDS, avg7);
+    });
+}
+
+int cg_md_resume(cg_session* s, int nframes, const double* constraint29) {
+    return guarded([&] {
+        need(s && nframes >= 0, "session/nframes");
+        s->s->md_resume(nframes, constraint29);
     });
 }
 

@@ -888,6 +888,7 @@ __global__ void k_md_mtk_half1(FramesDev F, const double* mass_type, double* x, 
         t[TH_KCUR] = k;
         t[TH_ZETA0] = z0;
         t[TH_FORCE0] = f0;
+        t[TH_POSIT0] = t[TH_POSIT];
         t[TH_POSIT] = t[TH_POSIT] + z0 * dt + 0.5 * dt * dt * f0;
     }
 }
@@ -932,6 +933,7 @@ __global__ void k_md_mtk_half2(FramesDev F, const double* Fo, const double* inv_
     if (threadIdx.x == 0) {
         t[TH_ZETA] = zT;
         t[TH_FORCE] = fT;
+        t[TH_VSCALE] = s;
         if (ke) ke[f] = k;
     }
 }
@@ -1227,9 +1229,12 @@ __global__ void k_md_nptmtk_half1(FramesDev F, BoxDev* box, const double* mass_t
         t[TH_FORCE0] = f0;
         t[TH_BVEL0] = bv0;
         t[TH_BFORCE0] = bf0;
+        t[TH_POSIT0] = t[TH_POSIT];
         t[TH_POSIT] = t[TH_POSIT] + z0 * dt + 0.5 * dt * dt * f0;
+        t[TH_BPOS0] = bp0;
         t[TH_BPOS] = bpT;
         t[TH_SCALE] = sc;
+        t[TH_VOL0] = t[TH_VOL];
         box_scale(box[f], sc, sc, sc);
         t[TH_VOL] = box[f].vol;
     }
@@ -1294,6 +1299,7 @@ __global__ void k_md_nptmtk_half2(FramesDev F, const double* Fo, const double* i
         t[TH_FORCE] = tfT;
         t[TH_BVEL] = bvT;
         t[TH_BFORCE] = bfT;
+        t[TH_VSCALE] = s;
         if (ke) ke[f] = k;
     }
 }

@@ -482,6 +482,34 @@ void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int n
     md_run(df, mass_type, dt, nsteps, MdThermostat{}, v, Fo, So_steps, ke_steps, nullptr);
 }
 
+std::vector<double> Session::md_restart_fields(int frame) const {
+    const int nf = (int)(md_state_.size() / cgd::MD_TH_STRIDE);
+    if (frame < 0 || frame >= nf) throw Error(1, "no MD run state for that frame");
+    const double* t = &md_state_[(size_t)frame * cgd::MD_TH_STRIDE];
+    const double tfs = 48.888;   // src/functions.h:44
+    const MdThermostat& th = md_last_th_;
+    std::vector<double> r(29, 0.0);
+    r[0] = t[cgd::TH_POSIT]; r[1] = t[cgd::TH_ZETA]; r[2] = t[cgd::TH_FORCE]; r[3] = t[cgd::TH_Q];
+    r[4] = t[cgd::TH_POSIT0]; r[5] = t[cgd::TH_FORCE0]; r[6] = t[cgd::TH_ZETA0];
+    r[7] = t[cgd::TH_BPOS]; r[8] = t[cgd::TH_BVEL]; r[9] = t[cgd::TH_BFORCE]; r[10] = t[cgd::TH_W];
+    r[11] = t[cgd::TH_BPOS0]; r[12] = t[cgd::TH_BFORCE0]; r[13] = t[cgd::TH_BVEL0];
+    r[14] = t[cgd::TH_SCALE]; r[15] = t[cgd::TH_VOL0]; r[16] = t[cgd::TH_VOL];
+    r[17] = 1.0;                                   // BEREND_MU
+    r[21] = th.tau_baro_fs / tfs;                  // BEREND_KP
+    r[22] = 1.0;                                   // BEREND_ETA
+    r[23] = th.tau_fs / tfs;                       // BEREND_TAU
+    r[24] = th.tau_fs; r[25] = th.tau_baro_fs;     // TIME, TIME_BARO
+    r[26] = t[cgd::TH_NDOF];
+    r[27] = t[cgd::TH_VSCALE];
+    r[28] = t[cgd::TH_KCUR];
+    return r;
+}
+
+void Session::md_resume(int nframes, const double* c29) {
+    if (nframes < 0 || (nframes > 0 && !c29)) throw Error(1, "resume state arrays");
+    md_resume_.assign(c29, c29 + (size_t)nframes * 29);
+}
+
 void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int nsteps, const MdThermostat& th, double* v,
                      double* Fo, double* So_steps, double* ke_steps, double* cons_steps, double* vol_steps) {
     CK(cudaSetDevice(device_));
@@ -531,6 +559,20 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
             t[cgd::TH_NDOF] = ndof;
             t[cgd::TH_NDOF1KT] = (ndof + 1.0) * kb * th.temperature;
             t[cgd::TH_SCALE] = 1.0;
+            t[cgd::TH_VSCALE] = 1.0;
+        }
+        if (!md_resume_.empty()) {   // CONSTRAINT::READ: the restart file's values
+            if (md_resume_.size() != (size_t)nf * 29) throw Error(1, "resume state was given for another frame count");
+            for (int f = 0; f < nf; ++f) {
+                const double* r = &md_resume_[(size_t)f * 29];
+                double* t = &h[(size_t)f * cgd::MD_TH_STRIDE];
+                t[cgd::TH_POSIT] = r[0]; t[cgd::TH_ZETA] = r[1]; t[cgd::TH_FORCE] = r[2]; t[cgd::TH_Q] = r[3];
+                t[cgd::TH_POSIT0] = r[4]; t[cgd::TH_FORCE0] = r[5]; t[cgd::TH_ZETA0] = r[6];
+                t[cgd::TH_BPOS] = r[7]; t[cgd::TH_BVEL] = r[8]; t[cgd::TH_BFORCE] = r[9]; t[cgd::TH_W] = r[10];
+                t[cgd::TH_BPOS0] = r[11]; t[cgd::TH_BFORCE0] = r[12]; t[cgd::TH_BVEL0] = r[13];
+                t[cgd::TH_SCALE] = r[14]; t[cgd::TH_VOL0] = r[15]; t[cgd::TH_VOL] = r[16];
+                t[cgd::TH_VSCALE] = r[27];
+            }
         }
         thd = S.get<double>(h.size());
         bad = S.get<int>(1);
@@ -573,6 +615,20 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
         if (vol_steps) cgd::launch_md_volume(nf, F.box, vol_steps + (size_t)step * nf, st);
         CK(cudaGetLastError());
     }
+    md_resume_.clear();
+    md_last_th_ = th;
+    md_state_.assign((size_t)nf * cgd::MD_TH_STRIDE, 0.0);
+    if (thd) {
+        CK(cudaMemcpyAsync(md_state_.data(), thd, md_state_.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    } else {   // NVE: the constraint holds only its degrees of freedom
+        for (int f = 0; f < nf; ++f) {
+            double* t = &md_state_[(size_t)f * cgd::MD_TH_STRIDE];
+            t[cgd::TH_NDOF] = 3.0 * df.natoms_host.at(f) - 3.0;
+            t[cgd::TH_SCALE] = 1.0;
+            t[cgd::TH_VSCALE] = 1.0;
+        }
+    }
+    CK(cudaStreamSynchronize(st));
     if (baro) {   // keep the host copy of the cells current
         CK(cudaMemcpyAsync(df.box_host.data(), F.box, df.box_host.size() * sizeof(cgd::BoxDev),
                            cudaMemcpyDeviceToHost, st));

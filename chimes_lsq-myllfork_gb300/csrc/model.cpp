@@ -1147,7 +1147,7 @@ void Box::update_cell() {   // BOX::UPDATE_CELL src/ClassDefs.C:1940-1971 (and t
 }
 
 // BOX::WRAP_ATOM src/ClassDefs.C:2075-2119 (in place)
-static void wrap_atom(const Box& b, double* x) {
+void wrap_atom(const Box& b, double* x) {
     if (b.is_ortho) {
         int wx = (int)std::floor(x[0] / b.lx), wy = (int)std::floor(x[1] / b.ly), wz = (int)std::floor(x[2] / b.lz);
         x[0] = x[0] - wx * b.lx; x[1] = x[1] - wy * b.ly; x[2] = x[2] - wz * b.lz;

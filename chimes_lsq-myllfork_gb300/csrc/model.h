@@ -163,6 +163,9 @@ struct Box {
 
 EwaldParams ewald_params(int natoms, const Box& box);
 
+// BOX::WRAP_ATOM (src/ClassDefs.C:2064-2119): x moved into the primary cell.
+void wrap_atom(const Box& b, double* x);
+
 struct Frame {
     int natoms = 0;
     std::vector<int> type;            // index into Model::atom_types

@@ -234,6 +234,15 @@ class Session {
     double md_lists_disp2(const DeviceFrames& df, MdLists& L);   // largest squared displacement
     // One step's forces through a list set (rebuilds, look-ahead builds, switch).
     void md_force_step(DeviceFrames& df, MdListSet& LS, double* Fo, double* So);
+    // Thermostat / barostat state of frame `frame` after the last md_run as CONSTRAINT's
+    // 29 restart values (CONSTRAINT::WRITE order, src/ClassDefs.C:790-827); values a
+    // device run does not track (the last Berendsen scale factors, KIN_ENER) hold what
+    // a fresh CONSTRAINT holds.
+    std::vector<double> md_restart_fields(int frame) const;
+    // The next md_run starts every frame from these restart values (nframes x 29,
+    // CONSTRAINT::READ): thermostat and barostat positions, velocities, forces and
+    // inertias.
+    void md_resume(int nframes, const double* constraint29);
     double md_skin() const { return md_skin_; }
     void set_md_skin(double s) { md_skin_ = s >= 0.0 ? s : 0.0; }
     // nsteps velocity-Verlet steps (NVE) of every frame of the batch; df's positions
@@ -287,6 +296,9 @@ class Session {
     std::unique_ptr<MdTables> md_;
     int gram_ctas_per_sm_ = 4;
     double md_skin_ = 0.5;   // Angstrom; 0: enumerate every step
+    std::vector<double> md_state_;   // last md_run: nframes * MD_TH_STRIDE
+    MdThermostat md_last_th_;
+    std::vector<double> md_resume_;  // next md_run's starting restart values (nframes * 29)
 };
 
 }  // namespace cg

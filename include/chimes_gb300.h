@@ -298,6 +298,40 @@ int cg_md_npt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
               double* forces, double* scalars_steps, double* ke_steps, double* conserved_steps,
               double* volume_steps);
 
+/* ---- MD output files (host arrays; xyz in A, velocities and accelerations in the
+ * MD's internal units as cg_md_* use them, cell = ax ay az bx by bz cx cy cz).
+ * One trajectory frame in the format of `# TRAJEXT #` GEN / XYZ / LAMMPSTRJ
+ * (WRITE_TRAJ::PRINT_FRAME_*, src/io_styles.C:322-423); frame_index 0 starts the
+ * file, later frames append with the number format the reference's stream has by
+ * then.  step is the MD step (printed as step + 1), temperature in K (GEN header),
+ * wrap = `# WRPCRDS #`. */
+enum { CG_TRAJ_GEN = 1, CG_TRAJ_XYZ = 2, CG_TRAJ_LAMMPSTRJ = 3 };
+int cg_md_write_traj(const cg_model* m, int format, const char* path, int frame_index, int step, double dt_fs,
+                     double temperature, int wrap, int natoms, const int* types, const double* xyz,
+                     const double* velocities, const double* cell);
+
+/* output.xyz of a run (write_xyzv, src/chimes_md.C:1207-1296, restart false). */
+int cg_md_write_xyzv(const cg_model* m, const char* path, int natoms, const int* types, const double* xyz,
+                     const double* velocities, const double* cell, int wrap);
+
+/* restart.xyzv of frame `frame` after the session's last MD run: positions,
+ * velocities, accelerations, step + 1, the neighbour padding, CONSTRAINT's 29 values
+ * (CONSTRAINT::WRITE, from the run's thermostat / barostat state) and THERMO_AVG's 7
+ * sums (avg7, may be NULL for zeros). */
+int cg_md_write_restart(cg_session* s, int frame, const char* path, int natoms, const int* types, const double* xyz,
+                        const double* velocities, const double* accel, const double* cell, int step,
+                        double rcut_padding, const double* avg7, int wrap);
+
+/* Read a restart.xyzv (read_restart_params, src/chimes_md.C:1298-1400): natoms must
+ * match the file; constraint29 / avg7 receive its CONSTRAINT and THERMO_AVG blocks. */
+int cg_md_read_restart(const cg_model* m, const char* path, int natoms, int* types, double* xyz,
+                       double* velocities, double* accel, double* cell, int* step, double* rcut_padding,
+                       double* constraint29, double* avg7);
+
+/* The session's next cg_md_nvt / cg_md_npt run starts each of its nframes frames
+ * from these CONSTRAINT values (nframes x 29, as cg_md_read_restart returns them). */
+int cg_md_resume(cg_session* s, int nframes, const double* constraint29);
+
 /* Continuous-batching MD serving (no counterpart in the reference, whose chimes_md
  * runs one system).  Each request runs nsteps velocity-Verlet NVE steps (step 0
  * evaluates forces only, as chimes_md's first step) from its own positions and

@@ -13,6 +13,7 @@ NVT-BEREND 50 runs of 20 steps on the same inputs.
 """
 import importlib
 import os
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -268,9 +269,50 @@ def make_npt(name="md_ch4b", steps=20, pressure=1.0):
     print(name, "npt", {k: v.shape for k, v in out.items()})
 
 
+def make_traj(name="md_ch4b", steps=6):
+    """The reference's MD output files for a 6-step NVE run with FRQDFTB 1 and FRQRSTR 3:
+    traj.gen / traj.xyz / traj.lammpstrj (TRAJEXT GEN, XYZ, LAMMPSTRJ), output.xyz,
+    restart.xyzv (after step 6) and restart.bak (after step 3); and an NVT-MTK HOOVER 10
+    run's restart.bak with its per-step table, to resume from."""
+    d = np.load(os.path.join(HERE, name, "md_ref.npz"))
+    model = cg.Model(os.path.join(HERE, name, "fm_setup.in"))
+    names, _ = header_types(model)
+    out = os.path.join(HERE, name, "traj")
+    os.makedirs(out, exist_ok=True)
+    tables = {}
+    for ext, consrnt in (("GEN", "NVE"), ("XYZ", "NVE"), ("LAMMPSTRJ", "NVE"), ("GEN", "NVT-MTK HOOVER 10")):
+        with tempfile.TemporaryDirectory() as tmp:
+            write_inputs(tmp, model, names, d, consrnt, steps)
+            run = open(os.path.join(tmp, "run_md.in")).read()
+            run = run.replace("# FRQDFTB #\n\t1000\n", f"# FRQDFTB #\n\t1\n# TRAJEXT #\n\t{ext}\n# FRQRSTR #\n\t3\n")
+            open(os.path.join(tmp, "run_md.in"), "w").write(run)
+            p = subprocess.run([REF_MD, "run_md.in"], cwd=tmp, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                               text=True)
+            if p.returncode != 0:
+                raise RuntimeError(f"chimes_md failed ({ext}, {consrnt}):\n{p.stdout[-2000:]}")
+            if consrnt == "NVE":
+                shutil.copy(os.path.join(tmp, "traj." + ext.lower()), out)
+                if ext == "GEN":
+                    for f in ("output.xyz", "restart.xyzv", "restart.bak"):
+                        shutil.copy(os.path.join(tmp, f), out)
+            else:
+                shutil.copy(os.path.join(tmp, "restart.bak"), os.path.join(out, "nvt_restart.bak"))
+                table = []
+                body = p.stdout.split("Ktot/N", 1)[1].split("END SIMULATION", 1)[0]
+                for ln in body.splitlines():
+                    w = ln.split()
+                    if len(w) == 8 and w[0].isdigit():
+                        table.append([float(t) for t in w])
+                tables["table_nvt"] = np.array(table)
+    np.savez_compressed(os.path.join(out, "tables.npz"), steps=steps, tau=10.0, temperature=300.0, **tables)
+    print(name, "traj", sorted(os.listdir(out)))
+
+
 if __name__ == "__main__":
-    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "md_watercoul"]):
-        if nm == "npt":
+    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "traj", "md_watercoul"]):
+        if nm == "traj":
+            make_traj()
+        elif nm == "npt":
             make_npt()
         elif nm == "nvt":
             make_nvt()

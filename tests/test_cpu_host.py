@@ -416,3 +416,20 @@ def test_hierarchical_params_txt_matches_reference_script(cg):
     assert x.size == m.ncols
     assert m.params_txt(x, "".join(lines[:k])) == gold
     assert np.array_equal(m.params_read(gold), x)
+
+
+# ---------------------------------------------------------------- MD output files
+TRAJ = os.path.join(GOLDEN, "md_ch4b", "traj")
+
+
+def test_md_restart_reader_and_output_xyz_match_reference(cg, tmp_path):
+    """The reference's restart.xyzv after a 6-step NVE run read back; written as
+    output.xyz it is byte-identical to the run's own output.xyz (same state)."""
+    m = cg.Model(os.path.join(GOLDEN, "md_ch4b", "fm_setup.in"))
+    r = m.md_read_restart(os.path.join(TRAJ, "restart.xyzv"), 40)
+    assert r["step"] == 6 and r["cell"][0] == r["cell"][4] == r["cell"][8] > 7.0
+    assert r["constraint"][26] == 117.0   # N_DOF = 3 * 40 - 3
+    m.md_write_xyzv(tmp_path / "output.xyz", r["types"], r["xyz"], r["v"], r["cell"])
+    assert open(tmp_path / "output.xyz").read() == open(os.path.join(TRAJ, "output.xyz")).read()
+    with pytest.raises(cg.ChimesError):
+        m.md_read_restart(os.path.join(TRAJ, "restart.xyzv"), 41)

@@ -391,3 +391,92 @@ def test_md_npt_matches_reference_run(cg, style):
         assert abs(vn - tab[s, 3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, tab[s, 3])
         assert abs(p - tab[s, 6]) <= 5e-9 * max(1.0, abs(p)) + 1e-12, (s, p, tab[s, 6])
         assert abs(V_h[s] - tab[s, 7]) <= 5e-8 * tab[s, 7], (s, V_h[s], tab[s, 7])
+
+
+# ---------------------------------------------------------------- MD output files and restart
+TRAJ = os.path.join(GOLDEN, "md_ch4b", "traj")
+KB = 0.0019872067
+
+
+def _nve_steps(cg, torch, nsteps):
+    """The 4-body fixture run one NVE step per call: positions, velocities, forces and
+    kinetic energy after each step (step 0 = the initial state)."""
+    fm, d = load_md("md_ch4b")
+    n = len(d["types"])
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.md_setup(d["x"], energy_offsets=True)
+    fr = cg.Frames.from_arrays(model, [n], d["types"], d["xyz"], d["cell"][None]).independent()
+    dfr = sess.upload(fr)
+    v = torch.from_numpy(d["v"].reshape(-1).copy()).cuda()
+    Fd = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    ke = torch.zeros(2, dtype=torch.float64, device="cuda")
+    states = []
+    for s in range(nsteps + 1):
+        sess.md_nve(dfr, d["masses"], float(d["dt"]), 0 if s == 0 else 1, v.data_ptr(), Fd.data_ptr(), 0,
+                    ke.data_ptr())
+        torch.cuda.synchronize()
+        xs = dfr.read_positions()
+        k = float(ke.cpu().numpy()[0 if s == 0 else 1])
+        states.append(dict(xyz=xs.reshape(n, 3), v=v.cpu().numpy().reshape(n, 3), f=Fd.cpu().numpy().reshape(n, 3),
+                           ke=k))
+    return model, sess, d, n, states
+
+
+def test_md_trajectory_files_match_reference(cg, tmp_path):
+    """traj.gen / traj.xyz / traj.lammpstrj of a 6-step NVE run (FRQDFTB 1) written from
+    the device run are byte-identical to the reference chimes_md's."""
+    torch = pytest.importorskip("torch")
+    model, sess, d, n, states = _nve_steps(cg, torch, 5)
+    tfs = 48.888
+    for fmt, name in ((cg.CG_TRAJ_GEN, "traj.gen"), (cg.CG_TRAJ_XYZ, "traj.xyz"),
+                      (cg.CG_TRAJ_LAMMPSTRJ, "traj.lammpstrj")):
+        out = tmp_path / name
+        for s, st in enumerate(states):
+            T = 2.0 * st["ke"] / ((3 * n - 3) * KB)
+            model.md_write_traj(fmt, out, s, s, float(d["dt"]), T, d["types"], st["xyz"], st["v"], d["cell"])
+        assert open(out).read() == open(os.path.join(TRAJ, name)).read(), name
+
+
+def test_md_restart_written_and_resumed_like_reference(cg, tmp_path):
+    """restart.xyzv after the 6-step NVE run matches the reference's numerically (step
+    line, cell, positions, velocities, accelerations, N_DOF); and an NVT-MTK run resumed
+    from the reference's restart file after its third step continues that run's table
+    (Ktot/N, Vtot/N, Econs/N) to the printed digits."""
+    torch = pytest.importorskip("torch")
+    model, sess, d, n, states = _nve_steps(cg, torch, 5)
+    last = states[-1]
+    masses = np.asarray(d["masses"])[np.asarray(d["types"])]
+    acc = last["f"] / masses[:, None]
+    sess.md_write_restart(0, tmp_path / "restart.xyzv", d["types"], last["xyz"], last["v"], acc, d["cell"], 5,
+                          float(model.md_read_restart(os.path.join(TRAJ, "restart.xyzv"), n)["padding"]))
+    ours = model.md_read_restart(tmp_path / "restart.xyzv", n)
+    ref = model.md_read_restart(os.path.join(TRAJ, "restart.xyzv"), n)
+    assert ours["step"] == ref["step"] == 6
+    assert np.array_equal(ours["types"], ref["types"]) and np.allclose(ours["cell"], ref["cell"], rtol=1e-14)
+    for k in ("xyz", "v", "acc"):
+        assert close(ours[k], ref[k], 1e-9), k
+    assert ours["constraint"][26] == ref["constraint"][26]
+    # resume an NVT-MTK run from the reference's restart file
+    r = model.md_read_restart(os.path.join(TRAJ, "nvt_restart.bak"), n)
+    tab = np.load(os.path.join(TRAJ, "tables.npz"))
+    rows = tab["table_nvt"]
+    fr = cg.Frames.from_arrays(model, [n], r["types"], r["xyz"], r["cell"][None]).independent()
+    dfr = sess.upload(fr)
+    v = torch.from_numpy(r["v"].reshape(-1).copy()).cuda()
+    Fd = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    steps = len(rows) - r["step"]
+    So = torch.zeros((steps + 1, 11), dtype=torch.float64, device="cuda")
+    ke = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    cons = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    sess.md_resume(r["constraint"][None])
+    sess.md_nvt(dfr, d["masses"], float(d["dt"]), steps, cg.CG_NVT_MTK, float(tab["temperature"]), float(tab["tau"]),
+                v.data_ptr(), Fd.data_ptr(), So.data_ptr(), ke.data_ptr(), cons.data_ptr())
+    torch.cuda.synchronize()
+    So_h, ke_h, c_h = So.cpu().numpy(), ke.cpu().numpy(), cons.cpu().numpy()
+    for s in range(steps + 1):
+        row = rows[r["step"] - 1 + s]
+        kn, vn, en = ke_h[s] / n, So_h[s, 0] / n, (ke_h[s] + So_h[s, 0] + c_h[s]) / n
+        assert abs(kn - row[2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, row[2])
+        assert abs(vn - row[3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, row[3])
+        assert abs(en - row[7]) <= 5e-8 * max(1.0, abs(en)) + 1e-12, (s, en, row[7])
