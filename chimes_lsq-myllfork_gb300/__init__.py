@@ -98,6 +98,8 @@ def lib():
         "cg_last_error": (ctypes.c_char_p, []),
         "cg_gram": (ctypes.c_int, [vp, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, vp, ctypes.c_int,
                                    vp, vp]),
+        "cg_gram_weighted": (ctypes.c_int, [vp, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, vp, vp,
+                                            ctypes.c_int, vp, vp]),
         "cg_gram_finish": (ctypes.c_int, [vp, vp, ctypes.c_int]),
         "cg_solve": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_double, vp, ctypes.c_int64, ctypes.c_int64, vp,
                                     ctypes.c_int, vp, vp]),
@@ -474,8 +476,15 @@ class Session:
                                                 ctypes.c_void_p(int(a_device_ptr)), int(lda)))
 
     # ---------------------------------------------------------------- normal equations
-    def gram(self, a_precision, a_ptr, lda, nrows, ncols, b_ptr, mode, g_ptr, h_ptr):
-        """Accumulate G += A^T A (upper triangle), h += A^T b on the device (cg_gram)."""
+    def gram(self, a_precision, a_ptr, lda, nrows, ncols, b_ptr, mode, g_ptr, h_ptr, w_ptr=0):
+        """Accumulate G += A^T A (upper triangle), h += A^T b on the device (cg_gram);
+        with w_ptr (device row weights) the weighted rows w A, w b (cg_gram_weighted)."""
+        if w_ptr:
+            _check(lib().cg_gram_weighted(self._h, int(a_precision), ctypes.c_void_p(int(a_ptr)),
+                                          ctypes.c_int64(int(lda)), ctypes.c_int64(int(nrows)), int(ncols),
+                                          ctypes.c_void_p(int(b_ptr)), ctypes.c_void_p(int(w_ptr)), int(mode),
+                                          ctypes.c_void_p(int(g_ptr)), ctypes.c_void_p(int(h_ptr))))
+            return
         _check(lib().cg_gram(self._h, int(a_precision), ctypes.c_void_p(int(a_ptr)), ctypes.c_int64(int(lda)),
                              ctypes.c_int64(int(nrows)), int(ncols), ctypes.c_void_p(int(b_ptr)), int(mode),
                              ctypes.c_void_p(int(g_ptr)), ctypes.c_void_p(int(h_ptr))))

@@ -338,6 +338,16 @@ int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplet
     });
 }
 
+int cg_gram_weighted(cg_session* s, int a_precision, const void* A, int64_t lda, int64_t nrows, int ncols,
+                     const double* b, const double* w, int mode, double* G, double* h) {
+    return guarded([&] {
+        need(s && A && b && w && G && h && ncols > 0 && lda >= ncols && nrows >= 0, "gram arguments");
+        need(a_precision == CG_FP64 || a_precision == CG_FP32, "precision");
+        need(mode == CG_GRAM_FP64 || mode == CG_GRAM_BF16X3, "gram mode");
+        s->s->gram(a_precision, A, lda, nrows, ncols, b, mode, G, h, w);
+    });
+}
+
 int cg_gram(cg_session* s, int a_precision, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b,
             int mode, double* G, double* h) {
     return guarded([&] {

@@ -661,10 +661,37 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
 }
 
 // ------------------------------------------------------------------ normal equations
+namespace {
+// Row weights of a weighted fit (chimes_lsq.py --weights, src/chimes_lsq.py:140-149:
+// A[i][j] * w[i], b[i] * w[i]): the weighted copy of one row block.
+template <typename T>
+__global__ void k_weight_rows(const T* A, int64_t lda, int64_t nrows, int ncols, const double* b, const double* w,
+                              T* out, double* wb) {
+    const int64_t r = blockIdx.x;
+    if (r >= nrows) return;
+    const double wr = w[r];
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) out[r * lda + c] = T(A[r * lda + c] * wr);
+    if (threadIdx.x == 0) wb[r] = b[r] * wr;
+}
+}  // namespace
+
 void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
-                   double* G, double* h) {
+                   double* G, double* h, const double* w) {
     CK(cudaSetDevice(device_));
     Scratch S(stream_);
+    if (w && nrows > 0) {   // G += (W A)^T (W A), h += (W A)^T (W b) on a weighted copy of the block
+        const size_t esz = prec_in == 0 ? sizeof(double) : sizeof(float);
+        void* wa = S.get<unsigned char>((size_t)nrows * lda * esz);
+        double* wb = S.get<double>(nrows);
+        const unsigned blocks = (unsigned)nrows;
+        if (prec_in == 0)
+            k_weight_rows<double><<<blocks, 256, 0, stream_>>>((const double*)A, lda, nrows, ncols, b, w, (double*)wa, wb);
+        else
+            k_weight_rows<float><<<blocks, 256, 0, stream_>>>((const float*)A, lda, nrows, ncols, b, w, (float*)wa, wb);
+        CK(cudaGetLastError());
+        A = wa;
+        b = wb;
+    }
     int* d_err = S.get<int>(1);
     CK(cudaMemsetAsync(d_err, 0, sizeof(int), stream_));
     void* planes = nullptr;

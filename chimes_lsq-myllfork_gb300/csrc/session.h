@@ -195,7 +195,7 @@ class Session {
 
     // Normal equations (gram.cu / solve.cu) on the session stream.
     void gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode, double* G,
-              double* h);
+              double* h, const double* w = nullptr);
     void gram_finish(double* G, int ncols);
     // x = (G + ridge I)^-1 h, then `iters` preconditioned-CG steps on A^T A x = A^T b
     // (A may be null when iters == 0).  info: [rnorm, gnorm, ridge used].

@@ -47,6 +47,8 @@ def main(argv=None):
     ap.add_argument("--write-a", action="store_true", help="also write A.txt, b.txt, ... (slow for large A)")
     ap.add_argument("--out", default=None, help="output directory (default: the fm_setup.in directory)")
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--weights", default=None,
+                    help="row weights, one per A row (chimes_lsq.py --weights): rows of A and b are multiplied by them")
     ap.add_argument("--ranks", type=int, default=1,
                     help="order the frames and text files as `srun -n RANKS chimes_lsq` would (SKPFRMS, SPLITFI)")
     args = ap.parse_args(argv)
@@ -75,6 +77,14 @@ def main(argv=None):
     keep64 = fits and (not mixed or (args.algorithm == "ridge" and args.refine > 0))
     A64_all = torch.empty((nrows, C), dtype=torch.float64, device="cuda") if keep64 else None
     b_all = torch.empty(nrows, dtype=torch.float64, device="cuda")
+    w_all = None   # row weights (src/chimes_lsq.py:71-149)
+    if args.weights:
+        wh = np.atleast_1d(np.loadtxt(args.weights, dtype=np.float64))
+        if wh.shape[0] != nrows:
+            raise SystemExit("Wrong number of lines in WEIGHTS file")
+        w_all = torch.from_numpy(wh).cuda()
+    wp = (lambda r: w_all[r:].data_ptr()) if w_all is not None else (lambda r: 0)
+    wcol = (lambda r, n: w_all[r:r + n, None]) if w_all is not None else (lambda r, n: 1.0)
     colsum = torch.zeros(C, dtype=torch.float64, device="cuda")   # A^T 1 (DLARS --normalize)
     r0 = 0
     for blk in blocks:
@@ -84,22 +94,23 @@ def main(argv=None):
         if mixed:
             A32 = torch.empty((n, C), dtype=torch.float32, device="cuda")
             sess.assemble_device(dfr, cg.CG_FP32, A32.data_ptr(), C)
-            sess.gram(1, A32.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 1, G.data_ptr(), h.data_ptr())
-            colsum += A32.sum(0, dtype=torch.float64)
+            sess.gram(1, A32.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 1, G.data_ptr(), h.data_ptr(), wp(r0))
+            colsum += (A32.double() * wcol(r0, n)).sum(0)
             del A32
         if keep64 or not mixed:
             dst = A64_all[r0:r0 + n] if keep64 else torch.empty((n, C), dtype=torch.float64, device="cuda")
             sess.assemble_device(dfr, cg.CG_FP64, dst.data_ptr(), C)
             if not mixed:
-                sess.gram(0, dst.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr())
-                colsum += dst.sum(0)
+                sess.gram(0, dst.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr(), wp(r0))
+                colsum += (dst * wcol(r0, n)).sum(0)
             del dst
         r0 += n
     if Acon.shape[0]:   # the constraint rows join the normal equations like any row block
         dAc = torch.from_numpy(Acon).cuda()
         b_all[r0:] = torch.from_numpy(bcon)
-        sess.gram(0, dAc.data_ptr(), C, Acon.shape[0], C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr())
-        colsum += dAc.sum(0)
+        sess.gram(0, dAc.data_ptr(), C, Acon.shape[0], C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr(),
+                  wp(r0))
+        colsum += (dAc * wcol(r0, Acon.shape[0])).sum(0)
         if keep64:
             A64_all[r0:] = dAc
     sess.gram_finish(G.data_ptr(), C)
@@ -108,8 +119,12 @@ def main(argv=None):
              f"! Number of equations            =  {nrows}"]
     if args.algorithm == "ridge":
         iters = args.refine if (mixed and keep64) else 0
-        sess.solve(G.data_ptr(), h.data_ptr(), C, args.alpha, A64_all.data_ptr() if iters else 0, C, nrows,
-                   b_all.data_ptr() if iters else 0, iters, x.data_ptr())
+        Ar, br = A64_all, b_all   # the refinement's residuals are those of the weighted rows
+        if iters and w_all is not None:
+            Ar, br = A64_all * w_all[:, None], b_all * w_all
+        sess.solve(G.data_ptr(), h.data_ptr(), C, args.alpha, Ar.data_ptr() if iters else 0, C, nrows,
+                   br.data_ptr() if iters else 0, iters, x.data_ptr())
+        del Ar, br
         lines += ["! ridge regression used", "! Ridge alpha = %11.4e" % args.alpha]
         if mixed:
             lines += [f"! split-BF16 tensor-core Gram, FP64 Cholesky, {iters} FP64-product CG iterations"]
@@ -118,8 +133,9 @@ def main(argv=None):
         lines += ["! LARS implementation of LASSO used", "! LASSO alpha = %11.4e" % args.alpha]
     else:   # fit_dlars src/chimes_lsq.py:714-790
         lasso = args.algorithm == "dlasso"
-        btb = float(b_all @ b_all)
-        bsum = float(b_all.sum())
+        bw = b_all * w_all if w_all is not None else b_all
+        btb = float(bw @ bw)
+        bsum = float(bw.sum())
         sess.dlars(G.data_ptr(), h.data_ptr(), C, nrows, btb, args.alpha, lasso, x.data_ptr(),
                    colsum_ptr=colsum.data_ptr() if args.normalize else 0, bsum=bsum)
         lines += ["! DLARS code for %s used" % ("LASSO" if lasso else "LARS"), "! DLARS alpha = %10.4e" % args.alpha,
@@ -149,7 +165,10 @@ def main(argv=None):
     lines += ["! RMS force error                = %11.4e" % math.sqrt(Z / nrows),
               "! max abs variable               = %11.4e" % float(np.abs(xh).max()),
               f"! number of fitting vars         =  {nvars}",
-              "! Bayesian Information Criterion = %11.4e" % bic, "!"]
+              "! Bayesian Information Criterion = %11.4e" % bic]
+    if args.weights:
+        lines += ["! Using weighting file:             " + args.weights]
+    lines += ["!"]
     with open(os.path.join(out, "force.txt"), "w") as f:
         f.write("".join("%13.6e\n" % v for v in y))
     open(os.path.join(out, "params.txt"), "w").write(model.params_txt(xh, "\n".join(lines) + "\n"))

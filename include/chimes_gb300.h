@@ -172,6 +172,12 @@ int cg_gram(cg_session* s, int a_precision, const void* A, int64_t lda, int64_t 
             int mode, double* G, double* h);
 int cg_gram_finish(cg_session* s, double* G, int ncols);
 
+/* cg_gram with row weights w (device, nrows): G += (W A)^T (W A), h += (W A)^T (W b),
+ * W = diag(w), as chimes_lsq.py --weights scales the rows of A and b
+ * (src/chimes_lsq.py:140-149). */
+int cg_gram_weighted(cg_session* s, int a_precision, const void* A, int64_t lda, int64_t nrows, int ncols,
+                     const double* b, const double* w, int mode, double* G, double* h);
+
 /* Ridge least squares (A^T A + ridge I) x = A^T b.  First x = (G + r I)^-1 h by FP64
  * Cholesky with r = ridge (r grows tenfold, at most 8 times, while G + r I is not
  * positive definite, as a mixed-precision G can be), then `iters` iterations of

@@ -47,3 +47,26 @@ def test_fit_lassolars_matches_sklearn(cg, tmp_path):
     A = np.loadtxt(tmp_path / "out" / "A.txt", ndmin=2)
     d = np.load(os.path.join(GOLDEN, "ch4b", "ref.npz"))
     assert A.shape[0] == d["A"].shape[0]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fit_with_row_weights_matches_weighted_normal_equations(cg, tmp_path, precision):
+    """--weights (chimes_lsq.py multiplies the rows of A and b by them): the ridge
+    coefficients solve (A^T W^2 A + alpha I) x = A^T W^2 b on the reference's A, and
+    force.txt stays the unweighted A x."""
+    d = np.load(os.path.join(GOLDEN, "water2b", "ref.npz"))
+    A, b = d["A"], d["b"]
+    w = np.random.default_rng(21).uniform(0.5, 2.0, A.shape[0])
+    np.savetxt(tmp_path / "weights.dat", w)
+    Aw, bw = A * w[:, None], b * w
+    ref = np.linalg.solve(Aw.T @ Aw + 1e-3 * np.eye(A.shape[1]), Aw.T @ bw)
+    x, y = _run(tmp_path, "water2b", "--algorithm", "ridge", "--alpha", "1e-3", "--precision", precision,
+                "--refine", "60", "--weights", str(tmp_path / "weights.dat"))
+    tol = 1e-9 if precision == "fp64" else 1e-8
+    assert np.linalg.norm(x - ref) <= tol * np.linalg.norm(ref)
+    f = np.loadtxt(tmp_path / "out" / "force.txt")
+    assert np.allclose(f, A @ ref, rtol=2e-6, atol=2e-6 * np.abs(f).max())
+    assert "! Using weighting file:" in open(tmp_path / "out" / "params.txt").read()
+    np.savetxt(tmp_path / "short.dat", w[:-1])
+    with pytest.raises(SystemExit):
+        _run(tmp_path, "water2b", "--weights", str(tmp_path / "short.dat"))
