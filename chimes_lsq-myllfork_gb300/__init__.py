@@ -130,6 +130,7 @@ def lib():
         "cg_md_read_restart": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_int, vp, vp, vp, vp, vp,
                                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), vp, vp]),
         "cg_md_resume": (ctypes.c_int, [vp, ctypes.c_int, vp]),
+        "cg_md_numerical": (ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
         "cg_dframes_positions": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_void_p), i64p]),
         "cg_dframes_read_positions": (ctypes.c_int, [vp, dp]),
         "cg_md_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
@@ -588,6 +589,18 @@ class Session:
         _check(lib().cg_md_write_restart(self._h, int(frame), os.fspath(path).encode(), len(t), _ptr(t), _ptr(x),
                                          _ptr(vv), _ptr(a), _ptr(c), int(step), float(rcut_padding), _ptr(av),
                                          int(bool(wrap))))
+
+    def md_numerical_pressure(self, frames):
+        """-dU/dV of each frame (cg_md_numerical what=0), kcal/mol/A^3."""
+        out = np.zeros(frames.nframes)
+        _check(lib().cg_md_numerical(self._h, frames._h, 0, _ptr(out)))
+        return out
+
+    def md_numerical_stress(self, frames):
+        """Finite-difference stress tensor of each frame ([nframes, 3, 3], cg_md_numerical what=1)."""
+        out = np.zeros((frames.nframes, 3, 3))
+        _check(lib().cg_md_numerical(self._h, frames._h, 1, _ptr(out)))
+        return out
 
     def md_resume(self, constraint29):
         """The next md_nvt / md_npt starts from these CONSTRAINT values ([nframes, 29])."""

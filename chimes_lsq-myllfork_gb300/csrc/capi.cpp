@@ -514,6 +514,13 @@ int cg_md_npt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
     });
 }
 
+int cg_md_numerical(cg_session* s, const cg_frames* fr, int what, double* out) {
+    return guarded([&] {
+        need(s && fr && out && (what == 0 || what == 1), "session/frames/out/what");
+        s->s->md_numerical(fr->fb, what == 1, out);
+    });
+}
+
 int cg_md_write_traj(const cg_model* h, int format, const char* path, int frame_index, int step, double dt_fs,
                      double temperature, int wrap, int natoms, const int* types, const double* xyz,
                      const double* velocities, const double* cell) {

@@ -482,6 +482,95 @@ void Session::md_nve(DeviceFrames& df, const double* mass_type, double dt, int n
     md_run(df, mass_type, dt, nsteps, MdThermostat{}, v, Fo, So_steps, ke_steps, nullptr);
 }
 
+void Session::md_numerical(const FrameBatch& fb, bool stress, double* out) {
+    CK(cudaSetDevice(device_));
+    if (!md_) throw Error(1, "MD coefficients are not set (cg_md_setup)");
+    const double eps = 1.0e-4;
+    const int nrep = stress ? 12 : 2;   // (t0 >= t1) components x (+, -), or (expand, contract)
+    std::vector<Frame> reps;
+    std::vector<double> vols;
+    reps.reserve((size_t)fb.nframes * nrep);
+    for (int k = 0; k < fb.nframes; ++k) {
+        const cgd::BoxDev& B = fb.box[k];
+        const double* H = B.h;   // columns a, b, c
+        const int n = fb.natoms[k];
+        const int64_t a0 = fb.atom_ofs[k];
+        auto make = [&](const double L[3][3], bool by_factor, double f) {
+            Frame r;
+            r.natoms = n;
+            r.type.assign(fb.type.begin() + a0, fb.type.begin() + a0 + n);
+            r.xyz.resize(3 * (size_t)n);
+            for (int i = 0; i < n; ++i) {
+                const double* x = &fb.xyz[3 * (a0 + i)];
+                double* y = &r.xyz[3 * (size_t)i];
+                if (by_factor) {   // BOX::SCALE_BY_FACTOR: to cell coordinates, back with f H
+                    const double* I = B.inv;
+                    const double s0 = I[0] * x[0] + I[1] * x[1] + I[2] * x[2];
+                    const double s1 = I[3] * x[0] + I[4] * x[1] + I[5] * x[2];
+                    const double s2 = I[6] * x[0] + I[7] * x[1] + I[8] * x[2];
+                    for (int q = 0; q < 3; ++q)
+                        y[q] = f * H[3 * q] * s0 + f * H[3 * q + 1] * s1 + f * H[3 * q + 2] * s2;
+                } else {   // BOX::SCALE_BY_MATRIX: x' = L x
+                    for (int q = 0; q < 3; ++q) y[q] = L[q][0] * x[0] + L[q][1] * x[1] + L[q][2] * x[2];
+                }
+            }
+            double cv[3][3] = {{H[0], H[3], H[6]}, {H[1], H[4], H[7]}, {H[2], H[5], H[8]}};   // a, b, c
+            double nv[3][3];
+            for (int v = 0; v < 3; ++v)
+                for (int q = 0; q < 3; ++q)
+                    nv[v][q] = by_factor ? cv[v][q] * f : cv[v][0] * L[q][0] + cv[v][1] * L[q][1] + cv[v][2] * L[q][2];
+            Box& bx = r.box;
+            bx.ax = nv[0][0]; bx.ay = nv[0][1]; bx.az = nv[0][2];
+            bx.bx = nv[1][0]; bx.by = nv[1][1]; bx.bz = nv[1][2];
+            bx.cx = nv[2][0]; bx.cy = nv[2][1]; bx.cz = nv[2][2];
+            bx.update_cell();
+            vols.push_back(bx.vol);
+            r.force.assign(3 * (size_t)n, 0.0);
+            reps.push_back(std::move(r));
+        };
+        const double I3[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        if (!stress) {
+            make(I3, true, 1.0 + eps);
+            make(I3, true, 1.0 - eps);
+        } else {
+            for (int t0 = 0; t0 < 3; ++t0)
+                for (int t1 = 0; t1 <= t0; ++t1)
+                    for (int sgn = 0; sgn < 2; ++sgn) {
+                        double L[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+                        L[t0][t1] += eps;
+                        if (sgn) L[t0][t1] -= 2.0 * eps;
+                        make(L, false, 1.0);
+                    }
+        }
+    }
+    FrameBatch rb = make_batch(model_, reps, 0);
+    make_independent(rb);
+    std::unique_ptr<DeviceFrames> d = upload(rb);
+    const size_t nF = (size_t)rb.natoms_total * 3, nS = (size_t)rb.nframes * cgd::MD_NSCALAR;
+    Scratch S(stream_);
+    double* dF = S.get<double>(nF + nS);
+    md_force(*d, dF, dF + nF, nullptr);
+    std::vector<double> so(nS);
+    CK(cudaMemcpyAsync(so.data(), dF + nF, nS * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    auto E = [&](int r) { return so[(size_t)r * cgd::MD_NSCALAR]; };
+    for (int k = 0; k < fb.nframes; ++k) {
+        const int r0 = k * nrep;
+        if (!stress) {   // -(U(1-e) - U(1+e)) / (V(1-e) - V(1+e))
+            out[k] = -1.0 * (E(r0 + 1) - E(r0)) / (vols[r0 + 1] - vols[r0]);
+            continue;
+        }
+        const double v0 = fb.box[k].vol;
+        int r = r0;
+        for (int t0 = 0; t0 < 3; ++t0)
+            for (int t1 = 0; t1 <= t0; ++t1, r += 2) {
+                const double pe1 = E(r) / (2.0 * eps * v0), pe2 = E(r + 1) / (2.0 * eps * v0);
+                out[(size_t)k * 9 + t0 * 3 + t1] = pe2 - pe1;
+                out[(size_t)k * 9 + t1 * 3 + t0] = pe2 - pe1;
+            }
+    }
+}
+
 std::vector<double> Session::md_restart_fields(int frame) const {
     const int nf = (int)(md_state_.size() / cgd::MD_TH_STRIDE);
     if (frame < 0 || frame >= nf) throw Error(1, "no MD run state for that frame");

@@ -243,6 +243,12 @@ class Session {
     // CONSTRAINT::READ): thermostat and barostat positions, velocities, forces and
     // inertias.
     void md_resume(int nframes, const double* constraint29);
+    // Finite-difference pressure / stress of each frame (PRSCALC / STRSCALC NUMERICAL,
+    // numerical_pressure and numerical_stress_all src/functions.C:402-628): the
+    // strained replicas of every frame (cell and coordinates scaled by 1 +- 1e-4, or by
+    // I +- 1e-4 e_i e_j) evaluated as one batch.  out: one PRESSURE_XYZ per frame
+    // (stress false) or nine PRESSURE_TENSORS_XYZ_ALL entries per frame (row-major).
+    void md_numerical(const FrameBatch& fb, bool stress, double* out);
     double md_skin() const { return md_skin_; }
     void set_md_skin(double s) { md_skin_ = s >= 0.0 ? s : 0.0; }
     // nsteps velocity-Verlet steps (NVE) of every frame of the batch; df's positions

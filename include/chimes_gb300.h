@@ -304,6 +304,14 @@ int cg_md_npt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
               double* forces, double* scalars_steps, double* ke_steps, double* conserved_steps,
               double* volume_steps);
 
+/* Finite-difference configurational pressure (what = 0: one PRESSURE_XYZ per frame,
+ * PRSCALC NUMERICAL) or stress tensor (what = 1: nine PRESSURE_TENSORS_XYZ_ALL values
+ * per frame, STRSCALC NUMERICAL) of host frames with the session's MD coefficients:
+ * -dU/dV from cells scaled by 1 +- 1e-4, and (U(I - e E_ij) - U(I + e E_ij)) / (2 e V)
+ * (numerical_pressure / numerical_stress_all, src/functions.C:402-628), every strained
+ * replica of every frame evaluated in one batched force call. */
+int cg_md_numerical(cg_session* s, const cg_frames* fr, int what, double* out);
+
 /* ---- MD output files (host arrays; xyz in A, velocities and accelerations in the
  * MD's internal units as cg_md_* use them, cell = ax ay az bx by bz cx cy cz).
  * One trajectory frame in the format of `# TRAJEXT #` GEN / XYZ / LAMMPSTRJ

@@ -308,10 +308,39 @@ def make_traj(name="md_ch4b", steps=6):
     print(name, "traj", sorted(os.listdir(out)))
 
 
+def make_numpress(name="md_ch4b", steps=6):
+    """A 6-step NVE run with PRSCALC NUMERICAL: the reference's per-step table, whose P
+    column is the finite-difference pressure plus the kinetic term."""
+    d = np.load(os.path.join(HERE, name, "md_ref.npz"))
+    model = cg.Model(os.path.join(HERE, name, "fm_setup.in"))
+    names, _ = header_types(model)
+    with tempfile.TemporaryDirectory() as tmp:
+        write_inputs(tmp, model, names, d, "NVE", steps)
+        run = open(os.path.join(tmp, "run_md.in")).read()
+        run = run.replace("# PRSCALC #\n\tANALYTICAL\n", "# PRSCALC #\n\tNUMERICAL\n")
+        assert "NUMERICAL" in run
+        open(os.path.join(tmp, "run_md.in"), "w").write(run)
+        p = subprocess.run([REF_MD, "run_md.in"], cwd=tmp, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"chimes_md failed (numerical pressure):\n{p.stdout[-2000:]}")
+        table = []
+        body = p.stdout.split("Ktot/N", 1)[1].split("END SIMULATION", 1)[0]
+        for ln in body.splitlines():
+            w = ln.split()
+            if len(w) == 7 and w[0].isdigit():
+                table.append([float(t) for t in w])
+    out = os.path.join(HERE, name, "traj")
+    os.makedirs(out, exist_ok=True)
+    np.savez_compressed(os.path.join(out, "numpress.npz"), steps=steps, table=np.array(table))
+    print(name, "numpress", np.array(table).shape)
+
+
 if __name__ == "__main__":
-    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "traj", "md_watercoul"]):
+    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "traj", "numpress", "md_watercoul"]):
         if nm == "traj":
             make_traj()
+        elif nm == "numpress":
+            make_numpress()
         elif nm == "npt":
             make_npt()
         elif nm == "nvt":

@@ -480,3 +480,27 @@ def test_md_restart_written_and_resumed_like_reference(cg, tmp_path):
         assert abs(kn - row[2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, row[2])
         assert abs(vn - row[3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, row[3])
         assert abs(en - row[7]) <= 5e-8 * max(1.0, abs(en)) + 1e-12, (s, en, row[7])
+
+
+def test_md_numerical_pressure_and_stress(cg):
+    """PRSCALC NUMERICAL: the finite-difference pressure of each step of a 6-step NVE
+    run (all strained replicas of all steps in one batched force call) plus the kinetic
+    term matches the reference chimes_md's printed P; the finite-difference stress
+    tensor (STRSCALC NUMERICAL) agrees with the analytic virial tensor to the O(eps^2)
+    truncation of the central difference."""
+    torch = pytest.importorskip("torch")
+    model, sess, d, n, states = _nve_steps(cg, torch, 5)
+    tab = np.load(os.path.join(TRAJ, "numpress.npz"))["table"]
+    k = len(states)
+    fr = cg.Frames.from_arrays(model, [n] * k, np.tile(d["types"], k), np.concatenate([s["xyz"] for s in states]),
+                               np.tile(d["cell"], (k, 1))).independent()
+    P = sess.md_numerical_pressure(fr)
+    V = abs(np.linalg.det(d["cell"].reshape(3, 3)))
+    for s, st in enumerate(states):
+        p = (P[s] + 2.0 * st["ke"] / (3.0 * V)) * GPA
+        assert abs(p - tab[s, 6]) <= 2e-8 * max(1.0, abs(p)), (s, p, tab[s, 6])
+    S = sess.md_numerical_stress(fr)
+    F, So = sess.md_force(fr)
+    for s in range(k):
+        an = So[s, 2:11].reshape(3, 3)
+        assert np.abs(S[s] - an).max() <= 1e-6 * np.abs(an).max(), (s, S[s], an)
