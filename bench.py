@@ -527,7 +527,10 @@ def main():
         step()
     stages = sess.stage_times()
     sess.profile(False)
-    dom = max(stages, key=lambda k: stages[k][0])
+    # the 3-body force stage (k_cluster_basis + k_force_mb) writes 99% of A's bytes; the
+    # stress/energy stage of similar length writes 1%, so the HBM roofline is the force
+    # stage's (both are FP64-pipe bound in the FP64 form: see fp64 / fp64_virial)
+    dom = "force_3b" if "force_3b" in stages else max(stages, key=lambda k: stages[k][0])
     dom_ms = stages[dom][0] / max(1, stages[dom][1])
     cols = model.columns()
     frames_n = args.frames
@@ -542,14 +545,29 @@ def main():
     hbm_peak, peak_kind = peaks()
     algo_bytes = bytes_by_stage.get(dom, nrows * ncols * esz)
     achieved = algo_bytes / (dom_ms / 1000.0) / 1e9
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
-                "note": "FP64 kernels are FP64-pipe bound; see fp64 below"}
+    # DRAM bytes (read + write) of the stage's kernels per frame, from one ncu capture of
+    # `profile_cases.py assemble 40` (FP64; profiles/k_force_mb_traffic_water3b_40frames.md),
+    # scaled to this launch's frames
+    traffic_per_frame = {("force_3b", 8): (406343168 + 218856704 + 18518272 + 327047680) / 40.0,
+                         ("virial_3b", 8): (410388736 + 14920704) / 40.0}
+    tpf = traffic_per_frame.get((dom, esz)) if WORKLOAD == "water-3b" else None
+    roofline = {"bound": "hbm", "kernel": dom + (" (k_cluster_basis + k_force_mb<3>)" if dom == "force_3b" else ""),
+                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": None if tpf is None else tpf * frames_n,
+                "traffic_note": None if tpf is None else "ncu dram bytes of a 40-frame capture scaled per frame",
+                "peak_source": peak_kind,
+                "note": "the FP64 kernels are FP64-pipe bound (89% of the FP64 pipe in k_force_mb); see fp64"}
     fp64 = None
     if dom in flops_by_stage:
         tf = flops_by_stage[dom] / (dom_ms / 1000.0) / 1e12
         fp64 = {"kernel": dom, "achieved_tflops": tf, "nominal_peak_tflops": 1.25, "frac_nominal": tf / 1.25,
                 "flops_per_launch": flops_by_stage[dom]}
+    fp64_virial = None
+    if "virial_3b" in stages:
+        vms = stages["virial_3b"][0] / max(1, stages["virial_3b"][1])
+        tf = flops_by_stage["virial_3b"] / (vms / 1000.0) / 1e12
+        fp64_virial = {"kernel": "virial_3b (k_virial_mb<3>)", "ms": vms, "achieved_tflops": tf,
+                       "frac_nominal": tf / 1.25, "flops_per_launch": flops_by_stage["virial_3b"]}
 
     # end to end through the C ABI with host buffers
     host = torch.empty((nrows, ncols), dtype=A.dtype, pin_memory=True)
@@ -599,7 +617,7 @@ def main():
             "config": {"workload": WORKLOAD, "desc": WORKLOAD_DESC, "rows_per_step": nrows, "cols": ncols,
                        "l2": "each step writes 1.5 GB of A (> 129 MB L2); no flush needed",
                        "parallelism": f"frames sharded, {world} rank(s), no collective"},
-            "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "fp64": fp64,
+            "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "fp64": fp64, "fp64_virial": fp64_virial,
             "stages_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in stages.items() if v[1]},
             "work": counts, "cpu_baseline": cpu, "gram": gram, "roofline_gram": gram_roof, "md": md, "fit4b": fit4b, "batched": batched,
         }
