@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libchimes_gb300.so")
 
 CG_FP64 = 0
 CG_FP32 = 1
-CG_NVT_MTK, CG_NVT_BEREND = 1, 2
+CG_NVT_MTK, CG_NVT_BEREND, CG_NVT_SCALE = 1, 2, 6
 CG_NPT_BEREND, CG_NPT_BEREND_ANISO, CG_NPT_MTK = 3, 4, 5
 CG_TRAJ_GEN, CG_TRAJ_XYZ, CG_TRAJ_LAMMPSTRJ = 1, 2, 3
 MD_ENERGY_OFFSETS = 1

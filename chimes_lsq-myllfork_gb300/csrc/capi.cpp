@@ -484,10 +484,10 @@ int cg_md_nvt(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
     return guarded([&] {
         need(s && d && mass && velocities && forces, "session/frames/mass/velocities/forces");
         need(dt_fs > 0.0 && nsteps >= 0, "dt/nsteps");
-        need(style == CG_NVT_MTK || style == CG_NVT_BEREND, "thermostat style");
+        need(style == CG_NVT_MTK || style == CG_NVT_BEREND || style == CG_NVT_SCALE, "thermostat style");
         const double Tfs = 48.888;   // internal time unit in fs (src/functions.h:44)
         cg::MdThermostat th;
-        th.style = style == CG_NVT_MTK ? 1 : 2;
+        th.style = style == CG_NVT_MTK ? 1 : (style == CG_NVT_BEREND ? 2 : 6);
         th.temperature = temperature;
         th.tau_fs = tau_fs;
         s->s->md_run(*d->d, mass, dt_fs / Tfs, nsteps, th, velocities, forces, scalars_steps, ke_steps,

@@ -1304,6 +1304,36 @@ __global__ void k_md_nptmtk_half2(FramesDev F, const double* Fo, const double* i
     }
 }
 
+__global__ void k_md_vscale(FramesDev F, const double* mass_type, double* v, double* th, int step, int freq,
+                            double T0, double kb) {
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    const int N = F.natoms[f];
+    const int64_t aofs = F.atom_ofs[f];
+    double* t = th + (size_t)f * MD_TH_STRIDE;
+    double k = 0.0;
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const int64_t g = 3 * aofs + i;
+        k += 0.5 * mass_type[F.type[aofs + i / 3]] * v[g] * v[g];
+    }
+    k = block_sum(k, red);
+    const double T = 2.0 * k / (t[TH_NDOF] * kb);
+    if ((step + 1) % freq != 0) {
+        if (threadIdx.x == 0) t[TH_TAVG] += T;
+        return;
+    }
+    double avg = t[TH_TAVG] + T;
+    avg /= freq;
+    const double s = sqrt(T0 / avg);
+    for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) v[3 * aofs + i] *= s;
+    if (threadIdx.x == 0) t[TH_TAVG] = 0.0;
+}
+
+void launch_md_vscale(int nframes, const FramesDev& F, const double* mass_type, double* v, double* th, int step,
+                      int freq, double T0, double kb, cudaStream_t st) {
+    if (nframes > 0) k_md_vscale<<<nframes, 256, 0, st>>>(F, mass_type, v, th, step, freq, T0, kb);
+}
+
 __global__ void k_md_volume(int nframes, const BoxDev* box, double* out) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f < nframes) out[f] = box[f].vol;

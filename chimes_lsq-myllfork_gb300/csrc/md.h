@@ -89,9 +89,14 @@ void launch_md_kick(int nframes, const FramesDev& F, const double* Fo, const dou
 enum {
     TH_ZETA = 0, TH_FORCE, TH_POSIT, TH_Q, TH_NDOFKT, TH_KCUR, TH_ZETA0, TH_FORCE0,
     TH_BPOS, TH_BVEL, TH_BFORCE, TH_W, TH_BVEL0, TH_BFORCE0, TH_VOL, TH_NDOF, TH_NDOF1KT, TH_SCALE,
-    TH_POSIT0, TH_BPOS0, TH_VOL0, TH_VSCALE
+    TH_POSIT0, TH_BPOS0, TH_VOL0, TH_VSCALE, TH_TAVG
 };
-constexpr int MD_TH_STRIDE = 22;
+constexpr int MD_TH_STRIDE = 23;
+// NVT-SCALE (src/chimes_md.C:1086-1094, CONSTRAINT::SCALE_VELOCITIES
+// src/ClassDefs.C:1447-1469): after step `step`, the temperature of v joins a running
+// sum; every freq-th step v *= sqrt(T0 / mean) and the sum restarts.
+void launch_md_vscale(int nframes, const FramesDev& F, const double* mass_type, double* v, double* th, int step,
+                      int freq, double T0, double kb, cudaStream_t st);
 // NPT-BEREND / NPT-BEREND-ANISO coordinate step (one block per frame): drift and
 // half kick, then x and the orthorhombic cell scaled by (1 - dt/kp (P0 - P))^(1/3)
 // with P from so_prev (the last force call's PRESSURE_XYZ or tensor diagonal) plus

@@ -626,8 +626,11 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
     const double kb = 0.0019872067, tfs = 48.888, gpa = 6.9476955;   // src/functions.h:43-45
     double* thd = nullptr;
     int* bad = nullptr;
-    const bool baro = th.style >= 3;
-    if (th.style < 0 || th.style > 5) throw Error(1, "unknown thermostat / barostat style");
+    const bool baro = th.style >= 3 && th.style <= 5;
+    if (th.style < 0 || th.style > 6) throw Error(1, "unknown thermostat / barostat style");
+    const int scale_freq = th.style == 6 ? (int)th.tau_fs : 0;   // NVT-SCALE: steps between rescalings
+    if (th.style == 6 && (scale_freq < 1 || (double)scale_freq != th.tau_fs))
+        throw Error(1, "NVT-SCALE needs a whole number of steps between rescalings");
     if (baro) {   // src/chimes_md.C:556-563: orthorhombic cells only
         if (!(th.tau_baro_fs > 0.0)) throw Error(1, "the barostat needs a positive time constant");
         for (const auto& b : df.box_host)
@@ -697,6 +700,7 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
             if ((th.style == 2 || th.style == 3 || th.style == 4) && step > 0)
                 cgd::launch_md_berend(nf, F, dm, v, dt, th.tau_fs / tfs, th.temperature, kb, ke, bad, st);
         }
+        if (th.style == 6) cgd::launch_md_vscale(nf, F, dm, v, thd, step, scale_freq, th.temperature, kb, st);
         if (cons_steps && thd) {   // CONSERVED_QUANT (NVT-MTK, NPT-MTK)
             cgd::launch_md_conserved(nf, thd, th.style == 1 ? 1 : (th.style == 5 ? 2 : 0), p0, F.box,
                                      cons_steps + (size_t)step * nf, st);

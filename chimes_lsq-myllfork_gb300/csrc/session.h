@@ -126,8 +126,9 @@ struct MdListSet {
 
 // Thermostat of an MD run: style 0 NVE, 1 NVT-MTK (Nose-Hoover chain of one, MTK
 // integration), 2 NVT-BEREND; temperature in K, time constant in fs.
-// style: 0 NVE, 1 NVT-MTK, 2 NVT-BEREND, 3 NPT-BEREND, 4 NPT-BEREND-ANISO, 5 NPT-MTK
-// (CONSTRAINT::INITIALIZE src/ClassDefs.C:527-585); pressure in GPa, time constants in fs.
+// style: 0 NVE, 1 NVT-MTK, 2 NVT-BEREND, 3 NPT-BEREND, 4 NPT-BEREND-ANISO, 5 NPT-MTK,
+// 6 NVT-SCALE (CONSTRAINT::INITIALIZE src/ClassDefs.C:527-585); pressure in GPa, time
+// constants in fs (NVT-SCALE: tau_fs holds the steps between rescalings).
 struct MdThermostat {
     int style = 0;
     double temperature = 0.0, tau_fs = 0.0;

@@ -275,7 +275,10 @@ int cg_md_nve(cg_session* s, cg_dframes* d, const double* mass, double dt_fs, in
  * ((nsteps+1) * nframes, device, may be NULL) receives the thermostat's part of the
  * conserved quantity (CONSERVED_QUANT: Q zeta^2 / 2 + N_DOF kB T s; 0 for
  * Berendsen): the run's Econs = kinetic + potential + this term. */
-enum { CG_NVT_MTK = 1, CG_NVT_BEREND = 2 };
+enum { CG_NVT_MTK = 1, CG_NVT_BEREND = 2, CG_NVT_SCALE = 6 };
+/* CG_NVT_SCALE = `CONSRNT NVT-SCALE n`: every n-th step the velocities are scaled by
+ * sqrt(T / mean temperature of the last n steps) (CONSTRAINT::SCALE_VELOCITIES,
+ * src/ClassDefs.C:1447-1469); tau_fs carries n. */
 
 /* Fixed charges (FITCOUL false with non-zero ATMCHRG): subtract every frame's Ewald
  * Coulomb forces from its force labels on the session's GPU (SubtractEwaldForces,

@@ -308,6 +308,29 @@ def make_traj(name="md_ch4b", steps=6):
     print(name, "traj", sorted(os.listdir(out)))
 
 
+def make_scale(name="md_ch4b", steps=8, freq=3):
+    """CONSRNT NVT-SCALE 3 for 8 steps: the reference's per-step table."""
+    d = np.load(os.path.join(HERE, name, "md_ref.npz"))
+    model = cg.Model(os.path.join(HERE, name, "fm_setup.in"))
+    names, _ = header_types(model)
+    with tempfile.TemporaryDirectory() as tmp:
+        write_inputs(tmp, model, names, d, f"NVT-SCALE {freq}", steps)
+        p = subprocess.run([REF_MD, "run_md.in"], cwd=tmp, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"chimes_md failed (NVT-SCALE):\n{p.stdout[-2000:]}")
+        table = []
+        body = p.stdout.split("Ktot/N", 1)[1].split("END SIMULATION", 1)[0]
+        for ln in body.splitlines():
+            w = ln.split()
+            if len(w) == 7 and w[0].isdigit():
+                table.append([float(t) for t in w])
+    out = os.path.join(HERE, name, "traj")
+    os.makedirs(out, exist_ok=True)
+    np.savez_compressed(os.path.join(out, "nvt_scale.npz"), steps=steps, freq=freq, temperature=300.0,
+                        table=np.array(table))
+    print(name, "nvt-scale", np.array(table).shape)
+
+
 def make_numpress(name="md_ch4b", steps=6):
     """A 6-step NVE run with PRSCALC NUMERICAL: the reference's per-step table, whose P
     column is the finite-difference pressure plus the kinetic term."""
@@ -336,11 +359,13 @@ def make_numpress(name="md_ch4b", steps=6):
 
 
 if __name__ == "__main__":
-    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "traj", "numpress", "md_watercoul"]):
+    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "traj", "numpress", "scale", "md_watercoul"]):
         if nm == "traj":
             make_traj()
         elif nm == "numpress":
             make_numpress()
+        elif nm == "scale":
+            make_scale()
         elif nm == "npt":
             make_npt()
         elif nm == "nvt":

@@ -504,3 +504,31 @@ def test_md_numerical_pressure_and_stress(cg):
     for s in range(k):
         an = So[s, 2:11].reshape(3, 3)
         assert np.abs(S[s] - an).max() <= 1e-6 * np.abs(an).max(), (s, S[s], an)
+
+
+def test_md_nvt_scale_matches_reference_run(cg):
+    """CONSRNT NVT-SCALE 3 against the reference chimes_md (8 steps): per-step Ktot/N and
+    Vtot/N to the printed digits across the rescalings after steps 3 and 6."""
+    torch = pytest.importorskip("torch")
+    fm, d = load_md("md_ch4b")
+    t = np.load(os.path.join(TRAJ, "nvt_scale.npz"))
+    tab = t["table"]
+    n = len(d["types"])
+    steps = int(t["steps"]) - 1
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.md_setup(d["x"], energy_offsets=True)
+    fr = cg.Frames.from_arrays(model, [n], d["types"], d["xyz"], d["cell"][None]).independent()
+    dfr = sess.upload(fr)
+    v = torch.from_numpy(d["v"].reshape(-1).copy()).cuda()
+    Fd = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    So = torch.zeros((steps + 1, 11), dtype=torch.float64, device="cuda")
+    ke = torch.zeros(steps + 1, dtype=torch.float64, device="cuda")
+    sess.md_nvt(dfr, d["masses"], float(d["dt"]), steps, cg.CG_NVT_SCALE, float(t["temperature"]), float(t["freq"]),
+                v.data_ptr(), Fd.data_ptr(), So.data_ptr(), ke.data_ptr())
+    torch.cuda.synchronize()
+    So_h, ke_h = So.cpu().numpy(), ke.cpu().numpy()
+    for s in range(steps + 1):
+        kn, vn = ke_h[s] / n, So_h[s, 0] / n
+        assert abs(kn - tab[s, 2]) <= 5e-8 * max(1.0, abs(kn)) + 1e-12, (s, kn, tab[s, 2])
+        assert abs(vn - tab[s, 3]) <= 5e-8 * max(1.0, abs(vn)) + 1e-12, (s, vn, tab[s, 3])
