@@ -131,6 +131,7 @@ def lib():
                                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), vp, vp]),
         "cg_md_resume": (ctypes.c_int, [vp, ctypes.c_int, vp]),
         "cg_md_numerical": (ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
+        "cg_md_velocities": (ctypes.c_int, [ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, vp]),
         "cg_dframes_positions": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_void_p), i64p]),
         "cg_dframes_read_positions": (ctypes.c_int, [vp, dp]),
         "cg_md_last_counts": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
@@ -163,6 +164,15 @@ def _check(rc):
 
 def _ptr(a):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def md_velocities(mass, temperature=0.0, seed=12357, v=None):
+    """Initial velocities ([natoms, 3], internal units): drawn as `# VELINIT # GEN` does
+    when v is None, else v as read; the centre-of-mass velocity removed (cg_md_velocities)."""
+    m = np.ascontiguousarray(mass, dtype=np.float64)
+    out = np.zeros((len(m), 3)) if v is None else np.array(v, dtype=np.float64).reshape(len(m), 3)
+    _check(lib().cg_md_velocities(len(m), _ptr(m), 1 if v is None else 0, int(seed), float(temperature), _ptr(out)))
+    return out
 
 
 class Model:

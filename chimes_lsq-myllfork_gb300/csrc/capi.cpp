@@ -571,6 +571,13 @@ int cg_md_read_restart(const cg_model* h, const char* path, int natoms, int* typ
     });
 }
 
+int cg_md_velocities(int natoms, const double* mass, int generate, int seed, double temperature, double* v) {
+    return guarded([&] {
+        need(natoms >= 0 && (natoms == 0 || (mass && v)), "natoms/mass/v");
+        cg::md_velocities(natoms, mass, generate != 0, seed, temperature, v);
+    });
+}
+
 int cg_md_resume(cg_session* s, int nframes, const double* constraint29) {
     return guarded([&] {
         need(s && nframes >= 0, "session/nframes");

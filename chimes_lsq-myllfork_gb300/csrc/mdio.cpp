@@ -3,6 +3,7 @@
 // and read_restart_params src/chimes_md.C:1207-1400).
 #include "mdio.h"
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -181,6 +182,36 @@ MdRestart read_restart(const Model& m, const std::string& path) {
     for (int k = 0; k < RESTART_CONSTRAINT_FIELDS; ++k) r.constraint[k] = next("constraint block");
     for (int k = 0; k < RESTART_AVG_FIELDS; ++k) r.avg[k] = next("average block");
     return r;
+}
+
+void md_velocities(int natoms, const double* mass, bool generate, int seed, double temperature, double* v) {
+    if (natoms < 0 || (natoms > 0 && (!mass || !v))) throw Error(1, "velocity arrays");
+    const double kb = 0.0019872067;   // src/functions.h:43
+    if (generate) {
+        std::srand((unsigned)seed);
+        int counter = 0;
+        for (int a = 0; a < natoms; ++a) {
+            if (!(mass[a] > 0.0)) throw Error(1, "atom masses must be positive");
+            const double sigma = std::sqrt(temperature * kb / mass[a]);
+            for (int q = 0; q < 3; ++q, ++counter) {
+                const double x1 = double(std::rand()) / double(RAND_MAX);
+                const double x2 = double(std::rand()) / double(RAND_MAX);
+                double y1 = std::sqrt(-2.0 * std::log(x1)) * std::cos(2.0 * M_PI * x2);
+                double y2 = std::sqrt(-2.0 * std::log(x1)) * std::sin(2.0 * M_PI * x2);
+                y1 *= sigma;
+                y2 *= sigma;
+                v[3 * a + q] = counter % 2 == 0 ? y2 : y1;
+            }
+        }
+    }
+    double p[3] = {0.0, 0.0, 0.0}, mt = 0.0;
+    for (int a = 0; a < natoms; ++a) {
+        for (int q = 0; q < 3; ++q) p[q] += mass[a] * v[3 * a + q];
+        mt += mass[a];
+    }
+    if (mt > 0.0)
+        for (int a = 0; a < natoms; ++a)
+            for (int q = 0; q < 3; ++q) v[3 * a + q] -= p[q] / mt;
 }
 
 }  // namespace cg

@@ -49,4 +49,11 @@ struct MdRestart {
 };
 MdRestart read_restart(const Model& m, const std::string& path);
 
+// Initial velocities (internal units) of natoms atoms with masses mass[i]:
+// generate = VELINIT GEN (CONSTRAINT::INIT_VEL src/ClassDefs.C:617-713: C rand()
+// seeded with `seed`, a Box-Muller pair per component whose sine and cosine halves
+// alternate, sigma = sqrt(T kB / m)); then, as for read velocities, the mass-weighted
+// centre-of-mass velocity is removed (CONSTRAINT::CHECK_VEL src/ClassDefs.C:715-788).
+void md_velocities(int natoms, const double* mass, bool generate, int seed, double temperature, double* v);
+
 }  // namespace cg

@@ -345,6 +345,12 @@ int cg_md_read_restart(const cg_model* m, const char* path, int natoms, int* typ
                        double* velocities, double* accel, double* cell, int* step, double* rcut_padding,
                        double* constraint29, double* avg7);
 
+/* Initial velocities of one system (internal units, [natoms][3]; mass per atom, amu):
+ * generate != 0 draws them as `# VELINIT # GEN` does (C rand() seeded with `seed`,
+ * Box-Muller, T in K), generate = 0 keeps v as read; either way the centre-of-mass
+ * velocity is then removed (CONSTRAINT::INIT_VEL / CHECK_VEL, src/ClassDefs.C:617-788). */
+int cg_md_velocities(int natoms, const double* mass, int generate, int seed, double temperature, double* v);
+
 /* The session's next cg_md_nvt / cg_md_npt run starts each of its nframes frames
  * from these CONSTRAINT values (nframes x 29, as cg_md_read_restart returns them). */
 int cg_md_resume(cg_session* s, int nframes, const double* constraint29);

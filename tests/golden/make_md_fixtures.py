@@ -331,6 +331,28 @@ def make_scale(name="md_ch4b", steps=8, freq=3):
     print(name, "nvt-scale", np.array(table).shape)
 
 
+def make_velgen(name="md_ch4b", steps=2, seed=4321):
+    """VELINIT GEN with RNDSEED 4321 and PRNTVEL every step: the reference's
+    velocout.txt, whose first block holds the generated velocities after the
+    centre-of-mass correction."""
+    d = np.load(os.path.join(HERE, name, "md_ref.npz"))
+    model = cg.Model(os.path.join(HERE, name, "fm_setup.in"))
+    names, _ = header_types(model)
+    with tempfile.TemporaryDirectory() as tmp:
+        write_inputs(tmp, model, names, d, "NVE", steps)
+        run = open(os.path.join(tmp, "run_md.in")).read()
+        run = run.replace("# VELINIT #\n\tREAD\n", "# VELINIT #\n\tGEN\n# PRNTVEL #\n\ttrue 1\n")
+        run = run.replace("# RNDSEED #\n\t12357\n", f"# RNDSEED #\n\t{seed}\n")
+        assert "GEN" in run and str(seed) in run
+        open(os.path.join(tmp, "run_md.in"), "w").write(run)
+        p = subprocess.run([REF_MD, "run_md.in"], cwd=tmp, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"chimes_md failed (VELINIT GEN):\n{p.stdout[-2000:]}")
+        out = os.path.join(HERE, name, "traj")
+        shutil.copy(os.path.join(tmp, "velocout.txt"), os.path.join(out, "velgen_velocout.txt"))
+    print(name, "velgen")
+
+
 def make_numpress(name="md_ch4b", steps=6):
     """A 6-step NVE run with PRSCALC NUMERICAL: the reference's per-step table, whose P
     column is the finite-difference pressure plus the kinetic term."""
@@ -359,13 +381,15 @@ def make_numpress(name="md_ch4b", steps=6):
 
 
 if __name__ == "__main__":
-    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "traj", "numpress", "scale", "md_watercoul"]):
+    for nm in (sys.argv[1:] or list(MD_FIXTURES) + ["nvt", "npt", "traj", "numpress", "scale", "velgen", "md_watercoul"]):
         if nm == "traj":
             make_traj()
         elif nm == "numpress":
             make_numpress()
         elif nm == "scale":
             make_scale()
+        elif nm == "velgen":
+            make_velgen()
         elif nm == "npt":
             make_npt()
         elif nm == "nvt":

@@ -433,3 +433,19 @@ def test_md_restart_reader_and_output_xyz_match_reference(cg, tmp_path):
     assert open(tmp_path / "output.xyz").read() == open(os.path.join(TRAJ, "output.xyz")).read()
     with pytest.raises(cg.ChimesError):
         m.md_read_restart(os.path.join(TRAJ, "restart.xyzv"), 41)
+
+
+def test_md_generated_velocities_match_reference(cg):
+    """VELINIT GEN (RNDSEED 4321, 300 K) with the centre-of-mass correction: the
+    velocities as the reference chimes_md printed them (velocout.txt, %13.6e) for the
+    40-atom fixture."""
+    d = np.load(os.path.join(GOLDEN, "md_ch4b", "md_ref.npz"))
+    masses = np.asarray(d["masses"])[np.asarray(d["types"])]
+    v = cg.md_velocities(masses, 300.0, 4321)
+    lines = open(os.path.join(TRAJ, "velgen_velocout.txt")).read().splitlines()[:120]
+    assert ["%13.6e" % x for x in v.reshape(-1)] == lines
+    p = (masses[:, None] * v).sum(0)
+    assert np.abs(p).max() <= 1e-12 * np.abs(masses[:, None] * v).sum()
+    # read velocities keep their values apart from the centre-of-mass shift
+    w = cg.md_velocities(masses, v=v + 0.25)
+    assert np.allclose(w, v, rtol=0, atol=1e-12)
