@@ -245,8 +245,11 @@ def md_bench(cg, local):
                        f"({model.ncols} coefficients, seeded), {nsteps} NVE steps at 0.2 fs each",
            "unit": "atom-steps/s"}
     sel = (sizes >= 768) & (sizes <= 1280)
+    # throughput-oriented batches (16k atoms), a latency-oriented FP32 batch cap, and the
+    # plain one-request-at-a-time FP64 loop
     for name, prec, cap, frames_cap, sub in (("batched_fp64", 0, 16384, 1024, None),
                                              ("batched_fp32", 1, 16384, 1024, None),
+                                             ("batched_fp32_cap4096", 1, 4096, 1024, None),
                                              ("one_at_a_time_fp64", 0, 1 << 16, 1, 6)):
         sess = cg.Session(model, local)
         sess.md_setup(x, precision=prec)
