@@ -274,13 +274,13 @@ def write_fm_setup(path, xyzf_name, nframes, species, masses, order2, order3, or
 
 # ---------------------------------------------------------------- workloads
 WORKLOADS = {
-    # configs[0]: plain 2-body, forces only
+    # water-2b: plain 2-body, forces only (64 molecules, 10 frames)
     "water-2b": dict(kind="water", nmol=64, L=12.42, nframes=10, disp=0.0, order=(12, 0, 0), smin=0.8,
                      smax=(5.0, None, None), lam=1.4, fitstrs=None, fitener=False),
-    # configs[1]: 2B 16 @ 5.0, 3B 8 @ 4.0, forces + energy + full stress
+    # water-3b: 2B 16 @ 5.0, 3B 8 @ 4.0, forces + energy + full stress (128 molecules, 200 frames)
     "water-3b": dict(kind="water", nmol=128, L=15.65, nframes=200, disp=0.1, order=(16, 8, 0), smin=0.8,
                      smax=(5.0, 4.0, None), lam=1.4, fitstrs="ALL", fitener=True),
-    # configs[2]: C/H/N/O triclinic, 2B 16 / 3B 8 / 4B 4 at 5.0 / 4.0 / 3.5
+    # chno-4b: C/H/N/O triclinic, 2B 16 / 3B 8 / 4B 4 at 5.0 / 4.0 / 3.5 (256 atoms)
     "chno-4b": dict(kind="chno", natoms=256, nframes=1000, order=(16, 8, 4), smin=0.8, smax=(5.0, 4.0, 3.5),
                     lam=1.4, fitstrs="ALL", fitener=True, triclinic=True),
 }

@@ -25,9 +25,9 @@ REF_PY = "/root/reference/src/chimes_lsq.py"   # the reference's solver script (
 
 # name -> (workload, overrides, nframes, seed)
 FIXTURES = {
-    # 2-body water, forces only (configs[0] basis)
+    # 2-body water, forces only (the water-2b basis)
     "water2b": ("water-2b", {}, 2, 11),
-    # 2B16 + 3B8 water with full stress and energy rows (configs[1] basis), 32 molecules
+    # 2B16 + 3B8 water with full stress and energy rows (the water-3b basis), 32 molecules
     "water3b": ("water-3b", dict(nmol=32, L=9.86), 1, 12),
     # C/H triclinic with 2B8 / 3B4 / 4B3, stress and energy rows
     "ch4b": ("chno-4b", dict(natoms=40, order=(8, 4, 3), triclinic=False, density=0.1, species2=True), 2, 13),
