@@ -1,7 +1,7 @@
 // Normal equations of the fit: G = A^T A and h = A^T b, streamed over row blocks.
 //
 // The reference solves the least-squares problem with a truncated SVD of the full
-// A in numpy (src/chimes_lsq.py:169-214); this build forms the Gram instead, the
+// A in numpy (src/chimes_lsq.py:169-214); this library forms the Gram instead, the
 // path's only dense contraction and its only tensor-core work:
 //  * mixed form: A is split into two BF16 planes (hi = bf16(a), lo = bf16(a - hi)),
 //    stored transposed (K = rows contiguous), and G += hi^T hi + hi^T lo + lo^T hi on

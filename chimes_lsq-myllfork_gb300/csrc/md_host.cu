@@ -635,7 +635,7 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
         if (!(th.tau_baro_fs > 0.0)) throw Error(1, "the barostat needs a positive time constant");
         for (const auto& b : df.box_host)
             if (!b.is_ortho) throw Error(2, "NPT-BEREND, NPT-BEREND-ANISO and NPT-MTK need orthorhombic cells");
-        if (md_->dev.coulomb) throw Error(2, "NPT with Ewald charges is not supported by this build");
+        if (md_->dev.coulomb) throw Error(2, "NPT with Ewald charges is not supported by this library");
     }
     const double p0 = th.pressure_gpa / gpa;
     if (th.style != 0) {

@@ -687,7 +687,7 @@ Model load_model(const std::string& path) {
         fail("FITCOUL with stress or energy rows: the reference prints no charge columns on those rows");
     if (c.use_partial_charges && (c.fit_stress || c.fit_stress_all || c.fit_ener))
         fail("fixed charges with stress or energy rows: only the force labels are corrected (SubtractEwaldForces)");
-    if (c.nlayers < 1) fail("NLAYERS must be >= 1 (ghost-atom images); NLAYERS 0 is not supported by this build");
+    if (c.nlayers < 1) fail("NLAYERS must be >= 1 (ghost-atom images); NLAYERS 0 is not supported by this library");
     // main: src/chimes_lsq.C:198-248
     // 2-body blocks in pair order without the HIERARC-excluded ones (A_MAT::skip_2b
     // src/A_Matrix.C:192-208 drops them when PRINT_FRAME writes a row)
