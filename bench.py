@@ -592,6 +592,29 @@ def main():
         sess.assemble_device(dfr, cg.CG_FP64, A64.data_ptr(), ncols) if esz != 8 else None
         torch.cuda.synchronize()
         gram, gram_roof = gram_bench(cg, sess, model, A64, b, max(3, args.steps // 2), torch)
+    # the mixed-precision form of the same step: FP32 assembly + split-BF16 Gram, against
+    # the plain FP64 assembly + FP64 Gram (the spec comparison on this workload)
+    mixed = None
+    if rank == 0 and not args.no_gram and esz == 8 and gram is not None:
+        A32 = torch.empty((nrows, ncols), dtype=torch.float32, device="cuda")
+        for _ in range(3):
+            sess.assemble_device(dfr, cg.CG_FP32, A32.data_ptr(), ncols)
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            sess.assemble_device(dfr, cg.CG_FP32, A32.data_ptr(), ncols)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = f0.elapsed_time(f1) / args.steps
+        plain = ms / args.steps + gram["fp64_ms"]
+        mix = ms32 + gram["bf16x3_ms"]
+        mixed = {"assembly_fp32_rows_per_s": nrows / (ms32 / 1000.0), "assembly_fp32_ms": ms32,
+                 "plain_assembly_plus_gram_ms": plain, "mixed_assembly_plus_gram_ms": mix,
+                 "speedup_mixed_vs_plain": plain / mix,
+                 "note": "FP32 A within 2e-5 of each column's scale; ridge coefficients of the mixed Gram "
+                         "(FP64-refined) vs FP64 in gram.solve"}
+        del A32
     md = None
     if rank == 0 and not args.no_md:
         del A
@@ -620,7 +643,7 @@ def main():
             "config": {"workload": WORKLOAD, "desc": WORKLOAD_DESC, "rows_per_step": nrows, "cols": ncols,
                        "l2": "each step writes 1.5 GB of A (> 129 MB L2); no flush needed",
                        "parallelism": f"frames sharded, {world} rank(s), no collective"},
-            "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "fp64": fp64, "fp64_virial": fp64_virial,
+            "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "fp64": fp64, "fp64_virial": fp64_virial, "mixed_form": mixed,
             "stages_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in stages.items() if v[1]},
             "work": counts, "cpu_baseline": cpu, "gram": gram, "roofline_gram": gram_roof, "md": md, "fit4b": fit4b, "batched": batched,
         }
