@@ -143,13 +143,13 @@ __global__ void k_force2(ModelDev M, FramesDev F, NeighDev NB, Buckets inc, cons
             double fc, fd;
             fcut_eval(M, r, P.smax, fc, fd);
             const double ir = sgn * B.perm2 / r;
-            const double ux = NB.rab2[3 * p] * ir, uy = NB.rab2[3 * p + 1] * ir, uz = NB.rab2[3 * p + 2] * ir;
+            const R ux = R(NB.rab2[3 * p] * ir), uy = R(NB.rab2[3 * p + 1] * ir), uz = R(NB.rab2[3 * p + 2] * ir);
             R* d = sD + (size_t)threadIdx.x * 3 * ord;
-            // h_n (n = 1..ord) into the x slot, then spread to y and z
-            basis_gh(M, P.lambda, P.xavg, P.xdiff, P.smin, r, 1, ord, fc, fd, d + 1, d, 3);
+            // h_n (n = 1..ord) into the x slot, then spread to y and z (recursion in R)
+            basis_gh_t<R>(M, P.lambda, P.xavg, P.xdiff, P.smin, r, 1, ord, fc, fd, d + 1, d, 3);
             for (int n = 0; n < ord; ++n) {
-                const double t = (double)d[3 * n];
-                d[3 * n] = R(t * ux); d[3 * n + 1] = R(t * uy); d[3 * n + 2] = R(t * uz);
+                const R t = d[3 * n];
+                d[3 * n] = t * ux; d[3 * n + 1] = t * uy; d[3 * n + 2] = t * uz;
             }
             sPt[threadIdx.x] = pt;
         }
@@ -207,11 +207,17 @@ __global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t ld
             double fc, fd;
             fcut_eval(M, r, P.smax, fc, fd);
             R* gh = sGH + (size_t)threadIdx.x * 2 * ord;
-            basis_gh(M, P.lambda, P.xavg, P.xdiff, P.smin, r, 1, ord, B.perm2 * fc, B.perm2 * fd, gh, gh + 1, 2);
+            basis_gh_t<R>(M, P.lambda, P.xavg, P.xdiff, P.smin, r, 1, ord, B.perm2 * fc, B.perm2 * fd, gh, gh + 1, 2);
             const double* x = NB.rab2 + 3 * p;
             R* v = sV + (size_t)threadIdx.x * 6;
-            v[0] = R(x[0] * x[0] / r); v[1] = R(x[1] * x[1] / r); v[2] = R(x[2] * x[2] / r);
-            v[3] = R(x[0] * x[1] / r); v[4] = R(x[0] * x[2] / r); v[5] = R(x[1] * x[2] / r);
+            if constexpr (sizeof(R) == 8) {
+                v[0] = x[0] * x[0] / r; v[1] = x[1] * x[1] / r; v[2] = x[2] * x[2] / r;
+                v[3] = x[0] * x[1] / r; v[4] = x[0] * x[2] / r; v[5] = x[1] * x[2] / r;
+            } else {   // r_a r_b / r in FP32
+                const R xf[3] = {R(x[0]), R(x[1]), R(x[2])}, rf = R(r);
+                v[0] = xf[0] * xf[0] / rf; v[1] = xf[1] * xf[1] / rf; v[2] = xf[2] * xf[2] / rf;
+                v[3] = xf[0] * xf[1] / rf; v[4] = xf[0] * xf[2] / rf; v[5] = xf[1] * xf[2] / rf;
+            }
             sPt[threadIdx.x] = pt;
         }
         __syncthreads();
