@@ -113,9 +113,48 @@ __global__ void __launch_bounds__(32 * NEIGH_WARPS) k_neigh(ModelDev M, FramesDe
     const int per = ((G + nw - 1) / nw + 31) & ~31;
     const int g0 = w * per, g1 = min(G, g0 + per);
     const unsigned lt = (1u << lane) - 1u;
+    // bounding box of the frame's real atoms (the first N ghosts); image k of the
+    // layers is that box shifted by one lattice translation, so an image whose box lies
+    // beyond the search radius of atom i holds none of its neighbours and is skipped
+    // (the lists keep their ghost order: only chunks without neighbours are passed over)
+    const float4* c32 = reinterpret_cast<const float4*>(F.cart32) + gbase;
+    float bmin[3] = {3.0e38f, 3.0e38f, 3.0e38f}, bmax[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    for (int a = lane; a < N; a += 32) {
+        const float4 c = c32[a];
+        bmin[0] = fminf(bmin[0], c.x); bmin[1] = fminf(bmin[1], c.y); bmin[2] = fminf(bmin[2], c.z);
+        bmax[0] = fmaxf(bmax[0], c.x); bmax[1] = fmaxf(bmax[1], c.y); bmax[2] = fmaxf(bmax[2], c.z);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int d = 0; d < 3; ++d) {
+            bmin[d] = fminf(bmin[d], __shfl_xor_sync(0xffffffffu, bmin[d], o));
+            bmax[d] = fmaxf(bmax[d], __shfl_xor_sync(0xffffffffu, bmax[d], o));
+        }
+    const float reach = pre + 0.05f;   // float rounding of the images' positions stays far below 0.05 A
+    const float4 c0 = c32[0];
+    auto image_far = [&](int k) {
+        const float4 ck = c32[(int64_t)k * N];
+        const float s[3] = {ck.x - c0.x, ck.y - c0.y, ck.z - c0.z};
+        const float p[3] = {ci.x, ci.y, ci.z};
+        float d2 = 0.0f;
+        for (int d = 0; d < 3; ++d) {
+            const float lo = bmin[d] + s[d], hi = bmax[d] + s[d];
+            const float e = p[d] < lo ? lo - p[d] : (p[d] > hi ? p[d] - hi : 0.0f);
+            d2 += e * e;
+        }
+        return d2 > reach * reach;
+    };
     auto sweep = [&](bool write, int64_t o2, int64_t o3, int64_t o4, int& c2, int& c3, int& c4) {
-        for (int base = g0; base < g1; base += 32) {
+        int kseen = -1;
+        bool kfar = false;
+        for (int base = g0; base < g1;) {
+            const int k = base / N;
+            if (k != kseen) { kseen = k; kfar = image_far(k); }
+            if (kfar) {   // warp-uniform: the rest of image k has no neighbour of atom i
+                base = min(g1, (k + 1) * N);
+                continue;
+            }
             const int g = base + lane;
+            base += 32;
             bool in2 = false, in3 = false, in4 = false;
             double r = 0, rab[3] = {0, 0, 0};
             int pt = 0;
