@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
 // grid: x = frame * ntypes + type, y = group-aligned power chunk, z = cluster chunk.
 // Each CTA sums VIR_CLUSTERS clusters and stores its column partials (7 comps);
 // k_virial_reduce adds the chunks in order and writes the rows.
-template <int NBODY, typename R>
+template <int NBODY, typename R, int PPT>
 __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets bytype,
                                                           const int64_t* key_frame_ofs, int ncomp,
                                                           const R* __restrict__ pre, R* part,
@@ -492,7 +492,6 @@ __global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev 
     constexpr int NP = NBODY == 3 ? 3 : 6;
     constexpr int N1 = NBODY - 1;
     constexpr int N2 = NP - N1;
-    constexpr int PPT = VIR_PPT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
     const int f = blockIdx.x / ntypes;
@@ -774,37 +773,46 @@ void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const
         force_mb_ppt<4, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st);
 }
 
-void launch_virial_mb(int nbody, int prec, int nframes, int ntypes, int nzchunk, int nchunks_max, int ntrue_max,
-                      size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
-                      const int64_t* kfo, int ncomp, const void* pre, void* part, void* A, int64_t lda,
-                      cudaStream_t st) {
+template <int NBD, typename R, int PPT>
+static void virial_mb_ppt(dim3 grid, unsigned rgrid, size_t smem, const ModelDev& M, const FramesDev& F,
+                          const ClusterSet& CS, const Buckets& byt, const int64_t* kfo, int ncomp, const R* pre,
+                          R* part, int ntrue_max, int nchunks_max, R* A, int64_t lda, cudaStream_t st) {
+    set_smem(k_virial_mb<NBD, R, PPT>, smem);
+    k_virial_mb<NBD, R, PPT><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, pre, part, ntrue_max,
+                                                              nchunks_max);
+    k_virial_reduce<NBD, R><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, part, ntrue_max, nchunks_max, A, lda);
+}
+
+template <int NBD, typename R>
+static void virial_mb_typed(int ppt, dim3 grid, unsigned rgrid, size_t smem, const ModelDev& M, const FramesDev& F,
+                            const ClusterSet& CS, const Buckets& byt, const int64_t* kfo, int ncomp, const void* pre,
+                            void* part, int ntrue_max, int nchunks_max, void* A, int64_t lda, cudaStream_t st) {
+    if (ppt == 1)
+        virial_mb_ppt<NBD, R, 1>(grid, rgrid, smem, M, F, CS, byt, kfo, ncomp, (const R*)pre, (R*)part, ntrue_max,
+                                 nchunks_max, (R*)A, lda, st);
+    else
+        virial_mb_ppt<NBD, R, VIR_PPT>(grid, rgrid, smem, M, F, CS, byt, kfo, ncomp, (const R*)pre, (R*)part,
+                                       ntrue_max, nchunks_max, (R*)A, lda, st);
+}
+
+void launch_virial_mb(int nbody, int prec, int ppt, int nframes, int ntypes, int nzchunk, int nchunks_max,
+                      int ntrue_max, size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS,
+                      const Buckets& byt, const int64_t* kfo, int ncomp, const void* pre, void* part, void* A,
+                      int64_t lda, cudaStream_t st) {
     dim3 grid(nframes * ntypes, nzchunk, nchunks_max);
     const unsigned rgrid = (unsigned)(nframes * ntypes);
-    if (nbody == 3 && prec == 0) {
-        set_smem(k_virial_mb<3, double>, smem);
-        k_virial_mb<3, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (const double*)pre, (double*)part, ntrue_max,
-                                                                nchunks_max);
-        k_virial_reduce<3, double><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const double*)part, ntrue_max, nchunks_max,
-                                                          (double*)A, lda);
-    } else if (nbody == 3) {
-        set_smem(k_virial_mb<3, float>, smem);
-        k_virial_mb<3, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (const float*)pre, (float*)part, ntrue_max,
-                                                               nchunks_max);
-        k_virial_reduce<3, float><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const float*)part, ntrue_max, nchunks_max,
-                                                         (float*)A, lda);
-    } else if (prec == 0) {
-        set_smem(k_virial_mb<4, double>, smem);
-        k_virial_mb<4, double><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (const double*)pre, (double*)part, ntrue_max,
-                                                                nchunks_max);
-        k_virial_reduce<4, double><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const double*)part, ntrue_max, nchunks_max,
-                                                          (double*)A, lda);
-    } else {
-        set_smem(k_virial_mb<4, float>, smem);
-        k_virial_mb<4, float><<<grid, MB_THREADS, smem, st>>>(M, F, CS, byt, kfo, ncomp, (const float*)pre, (float*)part, ntrue_max,
-                                                               nchunks_max);
-        k_virial_reduce<4, float><<<rgrid, 256, 0, st>>>(M, F, byt, kfo, (const float*)part, ntrue_max, nchunks_max,
-                                                         (float*)A, lda);
-    }
+    if (nbody == 3 && prec == 0)
+        virial_mb_typed<3, double>(ppt, grid, rgrid, smem, M, F, CS, byt, kfo, ncomp, pre, part, ntrue_max,
+                                   nchunks_max, A, lda, st);
+    else if (nbody == 3)
+        virial_mb_typed<3, float>(ppt, grid, rgrid, smem, M, F, CS, byt, kfo, ncomp, pre, part, ntrue_max,
+                                  nchunks_max, A, lda, st);
+    else if (prec == 0)
+        virial_mb_typed<4, double>(ppt, grid, rgrid, smem, M, F, CS, byt, kfo, ncomp, pre, part, ntrue_max,
+                                   nchunks_max, A, lda, st);
+    else
+        virial_mb_typed<4, float>(ppt, grid, rgrid, smem, M, F, CS, byt, kfo, ncomp, pre, part, ntrue_max,
+                                  nchunks_max, A, lda, st);
 }
 
 void launch_max_bucket(const int64_t* key_ofs, const int64_t* kfo, int nframes, int ntypes, int* out,

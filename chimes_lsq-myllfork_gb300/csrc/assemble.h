@@ -95,10 +95,12 @@ void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const
                      void* A, int64_t lda, cudaStream_t st);
 // Stress/energy rows: nchunks_max cluster chunks of VIR_CLUSTERS per (frame, type);
 // part holds nframes*ntypes*nchunks_max*7*ntrue_max partial sums (R).
-void launch_virial_mb(int nbody, int prec, int nframes, int ntypes, int nzchunk, int nchunks_max, int ntrue_max,
-                      size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS, const Buckets& byt,
-                      const int64_t* key_frame_ofs, int ncomp, const void* pre, void* part, void* A, int64_t lda,
-                      cudaStream_t st);
+// ppt: powers per thread, 1 when every cluster type has at most MB_THREADS allowed
+// powers (fewer registers, more CTAs per SM), else VIR_PPT.
+void launch_virial_mb(int nbody, int prec, int ppt, int nframes, int ntypes, int nzchunk, int nchunks_max,
+                      int ntrue_max, size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS,
+                      const Buckets& byt, const int64_t* key_frame_ofs, int ncomp, const void* pre, void* part,
+                      void* A, int64_t lda, cudaStream_t st);
 void launch_max_bucket(const int64_t* key_ofs, const int64_t* key_frame_ofs, int nframes, int ntypes, int* out,
                        cudaStream_t st);
 void launch_energy_cols(int prec, int nframes, const ModelDev& M, const FramesDev& F, void* A, int64_t lda,

@@ -630,7 +630,8 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
             void* part = prec == 0 ? (void*)S.get<double>((size_t)nf * ntypes * nch * 7 * ntrue_max)
                                    : (void*)S.get<float>((size_t)nf * ntypes * nch * 7 * ntrue_max);
             mark(nbody == 3 ? ST_VIRIAL3 : ST_VIRIAL4, true);
-            cgd::launch_virial_mb(nbody, prec, nf, ntypes, std::min(maxz, cgd::MAXCHUNK), nch, ntrue_max, V.total, M, F,
+            const int vppt = max_allowed <= cgd::MB_THREADS ? 1 : cgd::VIR_PPT;
+            cgd::launch_virial_mb(nbody, prec, vppt, nf, ntypes, std::min(maxz, cgd::MAXCHUNK), nch, ntrue_max, V.total, M, F,
                                   CS, byt, kfo_types, ncomp, pre, part, A, lda, st); L(2);
             mark(nbody == 3 ? ST_VIRIAL3 : ST_VIRIAL4, false);
             CK(cudaGetLastError());
