@@ -255,6 +255,7 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
     constexpr int NP = NBODY == 3 ? 3 : 6;
     constexpr int NI = NBODY - 1;
     constexpr int NO = NP - NI;
+    constexpr int CB = mb_force_cb((int)sizeof(R));
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ord = NBODY == 3 ? M.order3 : M.order4;
     const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
@@ -361,8 +362,8 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
                         idxI[k] = ii; idxO[k] = oo;
                     }
                 }
-                for (int b0 = rb; b0 < re; b0 += MB_CB) {
-                    const int nb = min(MB_CB, re - b0);
+                for (int b0 = rb; b0 < re; b0 += CB) {
+                    const int nb = min(CB, re - b0);
                     if (threadIdx.x < nb) {
                         const int v = sEnt[sOrd[b0 + threadIdx.x]];
                         sQ[threadIdx.x] = v >> 2; sPi[threadIdx.x] = v & 3;

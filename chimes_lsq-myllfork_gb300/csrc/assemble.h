@@ -6,6 +6,9 @@ namespace cgd {
 
 constexpr int MB_THREADS = 512;     // threads of the many-body kernels
 constexpr int MB_CB = 16;           // clusters staged per shared-memory batch
+// clusters per batch of the force kernel: twice as many in the FP32 form, whose
+// tables take half the shared memory (half the batch barriers per owner atom)
+__host__ __device__ constexpr int mb_force_cb(int rsize) { return rsize == 4 ? 32 : 16; }
 constexpr int MB_MAX_ENT = 1024;    // owner incidences handled per pass
 constexpr int VIR_PPT = 4;          // powers per thread in the stress/energy kernel
 constexpr int VIR_CLUSTERS = 512;   // clusters per CTA in the stress/energy kernel
@@ -28,12 +31,13 @@ __host__ __device__ inline MbForceSmem mb_force_smem(int nbody, int ord, int nke
     s.ord = align16(s.key + MB_MAX_ENT * sizeof(int));
     s.cnt = align16(s.ord + MB_MAX_ENT * sizeof(int));
     s.q = align16(s.cnt + (nkeys + 1) * sizeof(int));
-    s.pi = align16(s.q + MB_CB * sizeof(int));
-    s.sg = align16(s.pi + MB_CB * sizeof(int));
-    s.gh = align16(s.sg + MB_CB * 6 * sizeof(int));
-    s.w = align16(s.gh + (size_t)MB_CB * np * 2 * ord * rsize);
-    s.tab = align16(s.w + (size_t)MB_CB * np * 3 * ord * rsize);
-    size_t tab = (size_t)MB_CB * per;
+    const int cb = mb_force_cb(rsize);
+    s.pi = align16(s.q + cb * sizeof(int));
+    s.sg = align16(s.pi + cb * sizeof(int));
+    s.gh = align16(s.sg + cb * 6 * sizeof(int));
+    s.w = align16(s.gh + (size_t)cb * np * 2 * ord * rsize);
+    s.tab = align16(s.w + (size_t)cb * np * 3 * ord * rsize);
+    size_t tab = (size_t)cb * per;
     if ((size_t)max_allowed * 3 > tab) tab = (size_t)max_allowed * 3;
     s.total = align16(s.tab + tab * rsize);
     return s;
