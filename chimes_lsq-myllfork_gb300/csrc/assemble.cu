@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(Mod
 // Each CTA sums VIR_CLUSTERS clusters and stores its column partials (7 comps);
 // k_virial_reduce adds the chunks in order and writes the rows.
 template <int NBODY, typename R, int PPT>
-__global__ void __launch_bounds__(MB_THREADS) k_virial_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets bytype,
+__global__ void __launch_bounds__(MB_THREADS, (PPT == 1 && sizeof(R) == 4) ? 2 : 1) k_virial_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets bytype,
                                                           const int64_t* key_frame_ofs, int ncomp,
                                                           const R* __restrict__ pre, R* part,
                                                           int ntrue_max, int nchunks_max) {
