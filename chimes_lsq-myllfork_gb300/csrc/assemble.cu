@@ -249,7 +249,7 @@ __global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t ld
 // One CTA per real (owner) atom.  PPT powers per thread cover every allowed power
 // tuple of the largest cluster type, so the accumulators stay in registers.
 template <int NBODY, typename R, int PPT>
-__global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? 2 : 1) k_force_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
+__global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? (sizeof(R) == 4 ? 3 : 2) : 1) k_force_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
                                                          const int64_t* key_frame_ofs, const R* __restrict__ pre,
                                                          R* A, int64_t lda) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
