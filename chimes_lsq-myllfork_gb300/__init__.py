@@ -103,6 +103,11 @@ def lib():
         "cg_gram_finish": (ctypes.c_int, [vp, vp, ctypes.c_int]),
         "cg_solve": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_double, vp, ctypes.c_int64, ctypes.c_int64, vp,
                                     ctypes.c_int, vp, vp]),
+        "cg_solve_streamed": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, vp, vp, vp,
+                                             ctypes.c_int64, vp, vp, ctypes.c_int, ctypes.c_double, vp, vp]),
+        "cg_fp64_fma_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
+        "cg_md_serve_memory": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_double)]),
         "cg_batch_fit_create": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int64, vp, vp, pp]),
         "cg_batch_fit_launch": (ctypes.c_int, [vp, vp]),
         "cg_batch_fit_nodes": (ctypes.c_int, [vp, i64p]),
@@ -154,7 +159,7 @@ class MdRequest(ctypes.Structure):
 
 class MdResult(ctypes.Structure):
     _fields_ = [("admitted", ctypes.c_double), ("finished", ctypes.c_double), ("step_ms_sum", ctypes.c_double),
-                ("step_ms_max", ctypes.c_double)]
+                ("step_ms_max", ctypes.c_double), ("reserved_bytes", ctypes.c_double)]
 
 
 def _check(rc):
@@ -512,6 +517,35 @@ class Session:
                               ctypes.c_void_p(int(x_ptr)), info))
         return info[0], info[1], info[2]
 
+    def solve_streamed(self, g_ptr, h_ptr, ncols, ridge, dframes, label_ptrs, x_ptr, weight_ptrs=None, extra=None,
+                       max_iters=50, tol=1e-12):
+        """The mixed form's ridge solve without a stored FP64 A (cg_solve_streamed):
+        FP64 Cholesky of G + ridge I, then CG passes that assemble every uploaded
+        block again in FP64.  extra: (A_ptr, nrows, b_ptr, w_ptr or 0) of rows outside
+        the frames (device).  Returns dict(iters, rel_update, rnorm0, rnorm, ridge)."""
+        n = len(dframes)
+        blocks = (ctypes.c_void_p * max(n, 1))(*[d._h.value if isinstance(d._h, ctypes.c_void_p) else d._h
+                                                 for d in dframes])
+        labels = (ctypes.c_void_p * max(n, 1))(*[int(p) for p in label_ptrs])
+        weights = None
+        if weight_ptrs is not None:
+            weights = ctypes.cast((ctypes.c_void_p * max(n, 1))(*[int(p) for p in weight_ptrs]), ctypes.c_void_p)
+        ea, er, eb, ew = extra if extra is not None else (0, 0, 0, 0)
+        info = (ctypes.c_double * 5)()
+        _check(lib().cg_solve_streamed(self._h, ctypes.c_void_p(int(g_ptr)), ctypes.c_void_p(int(h_ptr)), int(ncols),
+                                       ctypes.c_double(ridge), n, ctypes.cast(blocks, ctypes.c_void_p),
+                                       ctypes.cast(labels, ctypes.c_void_p), weights,
+                                       ctypes.c_void_p(int(ea) or None), ctypes.c_int64(int(er)),
+                                       ctypes.c_void_p(int(eb) or None), ctypes.c_void_p(int(ew) or None),
+                                       int(max_iters), ctypes.c_double(tol), ctypes.c_void_p(int(x_ptr)), info))
+        return {"iters": int(info[0]), "rel_update": info[1], "rnorm0": info[2], "rnorm": info[3], "ridge": info[4]}
+
+    def fp64_fma_rate(self):
+        """Measured FP64 FMA rate of the session's GPU (TFLOP/s)."""
+        v = ctypes.c_double()
+        _check(lib().cg_fp64_fma_rate(self._h, ctypes.byref(v)))
+        return v.value
+
     def tune(self, key, value):
         _check(lib().cg_session_tune(self._h, key.encode(), int(value)))
 
@@ -643,9 +677,17 @@ class Session:
         _check(lib().cg_md_serve(self._h, len(requests), ctypes.cast(arr, ctypes.c_void_p), _ptr(m), float(dt_fs),
                                  float(hbm_budget), int(max_batch_atoms), int(max_batch_frames),
                                  ctypes.cast(res, ctypes.c_void_p), _ptr(step_ms), ctypes.byref(nb)))
-        r = np.array([(x.admitted, x.finished, x.step_ms_sum, x.step_ms_max) for x in res],
-                     dtype=[("admitted", "f8"), ("finished", "f8"), ("step_ms_sum", "f8"), ("step_ms_max", "f8")])
+        r = np.array([(x.admitted, x.finished, x.step_ms_sum, x.step_ms_max, x.reserved_bytes) for x in res],
+                     dtype=[("admitted", "f8"), ("finished", "f8"), ("step_ms_sum", "f8"), ("step_ms_max", "f8"),
+                            ("reserved_bytes", "f8")])
         return outs, r, step_ms, nb.value
+
+    def md_serve_memory(self, max_batch_atoms=1 << 16, max_batch_frames=1024):
+        """(arena bytes, reserved bytes per atom) of md_serve for these capacities."""
+        a, p = ctypes.c_double(), ctypes.c_double()
+        _check(lib().cg_md_serve_memory(self._h, int(max_batch_atoms), int(max_batch_frames), ctypes.byref(a),
+                                        ctypes.byref(p)))
+        return a.value, p.value
 
     def md_last_counts(self):
         v = [ctypes.c_int64() for _ in range(4)]

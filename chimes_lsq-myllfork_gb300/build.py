@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libchimes_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["geom.cu", "assemble.cu", "ewald.cu", "session.cu", "gram.cu", "solve.cu", "md.cu", "md_host.cu", "lars.cu"]
+CU_SOURCES = ["geom.cu", "assemble.cu", "ewald.cu", "session.cu", "gram.cu", "dense64.cu", "solve.cu", "md.cu", "md_host.cu", "lars.cu"]
 CPP_SOURCES = ["model.cpp", "capi.cpp", "textio.cpp", "mdio.cpp"]
 
 
@@ -79,7 +79,7 @@ def build(verbose=False, force=False):
                 if verbose and out.strip():
                     print(out)
     if force or jobs or not os.path.exists(LIB):
-        _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart", "-lcublas"])
+        _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])
     return LIB
 
 

@@ -8,6 +8,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "model.h"
 #include "session.h"
@@ -374,6 +375,37 @@ int cg_solve(cg_session* s, const double* G, const double* h, int ncols, double 
     });
 }
 
+int cg_solve_streamed(cg_session* s, const double* G, const double* h, int ncols, double ridge, int nblocks,
+                      cg_dframes* const* blocks, const double* const* labels, const double* const* weights,
+                      const double* extra_A, int64_t extra_rows, const double* extra_b, const double* extra_w,
+                      int max_iters, double tol, double* x, double* info) {
+    return guarded([&] {
+        need(s && G && h && x && ncols > 0 && nblocks >= 0 && max_iters >= 0 && tol >= 0.0, "solve arguments");
+        need(nblocks == 0 || (blocks && labels), "blocks/labels");
+        need(extra_rows >= 0 && (extra_rows == 0 || (extra_A && extra_b)), "extra rows");
+        std::vector<const cg::DeviceFrames*> bl;
+        std::vector<const double*> lb, wt;
+        for (int k = 0; k < nblocks; ++k) {
+            need(blocks[k] && labels[k], "block/labels entry");
+            bl.push_back(blocks[k]->d.get());
+            lb.push_back(labels[k]);
+            if (weights) {
+                need(weights[k] != nullptr, "weights entry");
+                wt.push_back(weights[k]);
+            }
+        }
+        s->s->solve_streamed(G, h, ncols, ridge, bl, lb, wt, extra_A, extra_rows, extra_b, extra_w, max_iters, tol, x,
+                             info);
+    });
+}
+
+int cg_fp64_fma_rate(cg_session* s, double* tflops) {
+    return guarded([&] {
+        need(s && tflops, "session/tflops");
+        *tflops = s->s->fp64_fma_tflops();
+    });
+}
+
 int cg_lars(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter,
             double* x, double* info) {
     return guarded([&] {
@@ -607,8 +639,17 @@ int cg_md_serve(cg_session* s, int nreq, const cg_md_request* req, const double*
         for (int r = 0; r < nreq; ++r) {
             results[r].admitted = out[r].admitted; results[r].finished = out[r].finished;
             results[r].step_ms_sum = out[r].step_ms_sum; results[r].step_ms_max = out[r].step_ms_max;
+            results[r].reserved_bytes = out[r].reserved_bytes;
         }
         if (batch_steps) *batch_steps = nb;
+    });
+}
+
+int cg_md_serve_memory(cg_session* s, int64_t max_batch_atoms, int max_batch_frames, double* arena_bytes,
+                       double* bytes_per_atom) {
+    return guarded([&] {
+        need(s && max_batch_atoms > 0 && max_batch_frames > 0, "session/limits");
+        s->s->md_serve_memory(max_batch_atoms, max_batch_frames, arena_bytes, bytes_per_atom);
     });
 }
 

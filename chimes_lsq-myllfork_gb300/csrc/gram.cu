@@ -9,21 +9,24 @@
 //    128-byte swizzle through a 3-stage mbarrier pipeline; one thread issues the
 //    MMAs; four warps drain TMEM with tcgen05.ld and add the split-K partial tile
 //    into an FP64 G.
-//  * plain form: FP64 G by the library SYRK (cuBLAS), a plain GEMM.
-//  * h = A^T b is an FP64 matrix-vector product (memory bound) in both forms.
+//  * plain form: FP64 G by this library's register-blocked FP64 SYRK (dense64.cu),
+//    which runs at the FP64 FMA rate of the GPU.
+//  * h = A^T b is an FP64 matrix-vector product (plain form) or is fused into the
+//    BF16 split pass (mixed form).
 // Every wait on an mbarrier is bounded (about one second); on time-out the kernel
 // records an error code, skips its stores, frees its TMEM and returns.
-#include <cublas_v2.h>
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
 #include <stdexcept>
 #include <string>
 
+#include "dense64.h"
 #include "gram.h"
 
 namespace cgd {
@@ -42,7 +45,7 @@ constexpr long long GB_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
 // two floats) is formed exactly by an FMA, added by an error-free two-sum, and the
 // pair renormalised after every tile, so the sum carries about 44 significant bits
 // while the FP64 pipe (a small fraction of the FP32 rate on this GPU) stays idle.
-// partial[blockIdx.x][c] = the block's sum, combined in order by k_atb_reduce.
+// partial[blockIdx.x][c] = the block's sum, combined in order by k_split_reduce.
 constexpr int SPA_K = 128, SPA_C = 32, SPA_THREADS = 256;
 struct FloatFloat {
     float hi = 0.f, lo = 0.f;
@@ -151,51 +154,9 @@ __global__ void __launch_bounds__(SPA_THREADS, 4) k_split_atb(const T* __restric
     }
 }
 
-// h[c] += sum_r A[r][c] b[r] in FP64: partial[y][c] over row slices y, then an
-// ordered sum over y, so the result is reproducible.  A block walks its slice's
-// rows with its threads across the columns (whole rows read contiguously), four
-// columns per thread and four rows per step.
-constexpr int ATB_SLICES = 1024;
-constexpr int ATB_THREADS = 256;
-__global__ void __launch_bounds__(ATB_THREADS) k_atb_partial(const double* __restrict__ A, int64_t lda, int64_t nr,
-                                                             int ncols, const double* __restrict__ b,
-                                                             double* __restrict__ partial) {
-    const int64_t per = (nr + gridDim.y - 1) / gridDim.y;
-    const int64_t r0 = (int64_t)blockIdx.y * per, r1 = min(nr, r0 + per);
-    for (int c0 = 0; c0 < ncols; c0 += 4 * ATB_THREADS) {
-        double s[4] = {0, 0, 0, 0};
-        int cc[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) cc[u] = c0 + u * ATB_THREADS + threadIdx.x;
-        int64_t r = r0;
-        for (; r + 4 <= r1; r += 4) {   // 16 loads in flight per thread
-            double v[4][4];
-            double br[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                br[q] = b[r + q];
-                const double* row = A + (r + q) * lda;
-#pragma unroll
-                for (int u = 0; u < 4; ++u) v[q][u] = cc[u] < ncols ? row[cc[u]] : 0.0;
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-#pragma unroll
-                for (int u = 0; u < 4; ++u) s[u] = fma(v[q][u], br[q], s[u]);
-        }
-        for (; r < r1; ++r) {
-            const double br = b[r];
-            const double* row = A + r * lda;
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (cc[u] < ncols) s[u] = fma(row[cc[u]], br, s[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (cc[u] < ncols) partial[(int64_t)blockIdx.y * ncols + cc[u]] = s[u];
-    }
-}
-__global__ void k_atb_reduce(const double* __restrict__ partial, int nslices, int ncols, double* __restrict__ h) {
+// h[c] += sum over y of partial[y][c] (the split pass's per-block column sums), in
+// a fixed order so that h is reproducible.
+__global__ void k_split_reduce(const double* __restrict__ partial, int nslices, int ncols, double* __restrict__ h) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncols) return;
     double s = 0.0;
@@ -304,6 +265,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
     bool ok = true;
 
     if (warp == 0 && lane == 0 && nk > 0) {   // producer
+        int issued = 0;
         for (int it = 0; it < nk && ok; ++it) {
             const int s = it % GB_STAGES;
             const uint32_t ph = (uint32_t)(it / GB_STAGES) & 1u;
@@ -315,10 +277,14 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             tma_load_2d(st + GB_TILE_BYTES, &map_lo, &full[s], x, ti * GB_M);
             tma_load_2d(st + 2 * GB_TILE_BYTES, &map_hi, &full[s], x, tj * GB_N);
             tma_load_2d(st + 3 * GB_TILE_BYTES, &map_lo, &full[s], x, tj * GB_N);
+            ++issued;
         }
-        // drain: wait for the copies still in flight before the CTA may exit
+        // drain after a time-out: the last load issued into each stage completes the
+        // full-barrier phase (it / GB_STAGES) & 1; wait (bounded) for it so that no
+        // copy still writes this CTA's shared memory when it exits
         if (!ok)
-            for (int s = 0; s < GB_STAGES; ++s) mbar_try_wait(&full[s], 0);
+            for (int it = issued - 1; it >= 0 && it >= issued - GB_STAGES; --it)
+                mbar_wait(&full[it % GB_STAGES], (uint32_t)(it / GB_STAGES) & 1u, err, 4);
     } else if (warp == 1 && lane == 0 && nk > 0) {   // MMA issuer
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GB_N >> 3) << 17) |
                                ((uint32_t)(GB_M >> 4) << 24);
@@ -420,6 +386,19 @@ static CUtensorMap plane_map(void* base, int64_t kpad, int64_t cpad) {
     return m;
 }
 
+// Streaming multiprocessors of the current device (cached per device).
+static int device_sms() {
+    static thread_local int dev_cached = -1, cached = 0;
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev != dev_cached) {
+        ck(cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        cached = std::max(1, cached);
+        dev_cached = dev;
+    }
+    return cached;
+}
+
 // Blocks of k_split_atb<T> resident on the current device at once (cached per device).
 template <typename T>
 static int split_atb_resident() {
@@ -444,33 +423,22 @@ size_t gram_plane_bytes(int64_t nrows_block, int ncols) {
 }
 
 void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
-                     double* G, double* h, void* planes, size_t planes_bytes, int* d_err, void* cublas,
-                     cudaStream_t st, const std::function<void(int, bool)>& mark, int ctas_per_sm) {
+                     double* G, double* h, void* planes, size_t planes_bytes, int* d_err, cudaStream_t st, const std::function<void(int, bool)>& mark, int ctas_per_sm) {
     if (nrows <= 0) return;
     // stage ids (session.h): ST_GRAM_ATB 11, ST_GRAM_SPLIT 12, ST_GRAM_TC 13, ST_GRAM_SYRK 14
     enum { S_ATB = 11, S_SPLIT = 12, S_TC = 13, S_SYRK = 14 };
-    if (mode == 0) {   // h += A^T b (FP64), reproducible
+    if (mode == 0) {   // h += A^T b (FP64, reproducible), then the FP64 SYRK of the block
         if (prec_in != 0) throw std::runtime_error("the FP64 Gram needs an FP64 A");
-        const int ns = (int)std::min<int64_t>(nrows, cgd::ATB_SLICES);
         double* partial = nullptr;
-        ck(cudaMallocAsync((void**)&partial, sizeof(double) * ns * ncols, st), "atb scratch");
+        ck(cudaMallocAsync((void**)&partial, sizeof(double) * atb_partial_doubles(nrows, ncols), st), "atb scratch");
         mark(S_ATB, true);
-        cgd::k_atb_partial<<<dim3(1, ns), cgd::ATB_THREADS, 0, st>>>((const double*)A, lda, nrows, ncols, b, partial);
-        cgd::k_atb_reduce<<<(ncols + 127) / 128, 128, 0, st>>>(partial, ns, ncols, h);
+        gemv_cols64((const double*)A, lda, nrows, ncols, b, h, partial, st);
         mark(S_ATB, false);
-        ck(cudaGetLastError(), "k_atb");
         ck(cudaFreeAsync(partial, st), "atb scratch free");
-        // FP64 library SYRK (upper triangle of the row-major G)
-        cublasHandle_t hnd = (cublasHandle_t)cublas;
-        cublasSetStream(hnd, st);
-        const double one = 1.0;
-        // row-major A (nrows x ncols) is column-major X = A^T (ncols x nrows); G = X X^T.
         mark(S_SYRK, true);
-        cublasStatus_t s = cublasDsyrk(hnd, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, ncols, (int)nrows, &one,
-                                       (const double*)A, (int)lda, &one, G, ncols);
+        syrk_tn((const double*)A, lda, nrows, ncols, 1.0, G, ncols, st);
         mark(S_SYRK, false);
-        if (s != CUBLAS_STATUS_SUCCESS) throw std::runtime_error("cublasDsyrk failed");
-        return;   // lower triangle of column-major G == upper triangle of row-major G
+        return;
     }
     // split-BF16 3-term on tcgen05, in row blocks that fit the plane buffer
     const int64_t cpad = (ncols + cgd::GB_M - 1) / cgd::GB_M * cgd::GB_M;
@@ -510,13 +478,13 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         mark(S_SPLIT, false);
         ck(cudaGetLastError(), "k_split_atb");
         mark(S_ATB, true);
-        cgd::k_atb_reduce<<<(ncols + 127) / 128, 128, 0, st>>>(partial, gxb, ncols, h);
+        cgd::k_split_reduce<<<(ncols + 127) / 128, 128, 0, st>>>(partial, gxb, ncols, h);
         mark(S_ATB, false);
-        ck(cudaGetLastError(), "k_atb_reduce");
+        ck(cudaGetLastError(), "k_split_reduce");
         CUtensorMap mhi = plane_map(hi, kpad, cpad), mlo = plane_map(lo, kpad, cpad);
-        // K slices: about ctas_per_sm CTAs per SM in total (152 SMs)
+        // K slices: about ctas_per_sm CTAs per SM in total
         const int64_t ksteps = kpad / cgd::GB_K;
-        const int64_t target = 152 * (int64_t)std::max(1, ctas_per_sm);
+        const int64_t target = (int64_t)device_sms() * std::max(1, ctas_per_sm);
         int64_t nslice = std::max<int64_t>(1, std::min<int64_t>(ksteps, (target + npairs - 1) / npairs));
         const int64_t kslice = (ksteps + nslice - 1) / nslice * cgd::GB_K;
         nslice = (kpad + kslice - 1) / kslice;

@@ -1,4 +1,4 @@
-// Normal equations and their FP64 solve (see gram.cu and solve.cu).
+// Normal equations and their FP64 solve (see gram.cu, solve.cu and dense64.cu).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -12,37 +12,50 @@ namespace cg {
 size_t gram_plane_bytes(int64_t nrows_block, int ncols);
 
 // G (row-major ncols x ncols FP64, upper triangle) += A^T A and h += A^T b for the
-// device A block (row-major, lda; prec_in 0 = FP64, 1 = FP32).  mode 0: FP64 library
-// SYRK; mode 1: split-BF16 3-product Gram on tcgen05 (planes: scratch of at least
-// gram_plane_bytes(64, ncols) bytes; larger buffers take larger row blocks).
+// device A block (row-major, lda; prec_in 0 = FP64, 1 = FP32).  mode 0: FP64 SYRK
+// (dense64.cu); mode 1: split-BF16 3-product Gram on tcgen05 (planes: scratch of at
+// least gram_plane_bytes(64, ncols) bytes; larger buffers take larger row blocks).
 // mark(stage, begin) brackets the A^T b, split, tensor and FP64 SYRK launches
 // (stage ids of session.h) for the optional CUDA-event timing.
 // ctas_per_sm: target CTAs per SM when the K dimension is sliced (tunable).
 void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
-                     double* G, double* h, void* planes, size_t planes_bytes, int* d_err, void* cublas,
-                     cudaStream_t st, const std::function<void(int, bool)>& mark, int ctas_per_sm = 4);
+                     double* G, double* h, void* planes, size_t planes_bytes, int* d_err, cudaStream_t st,
+                     const std::function<void(int, bool)>& mark, int ctas_per_sm = 4);
 // Copy the upper triangle of G to the lower one.
 void gram_symmetrize(double* G, int n, bool from_upper, cudaStream_t st);
 
-// In-place Cholesky G = L L^T (lower, row-major storage of a symmetric matrix).
-// Returns false when a pivot is not positive.
-bool cholesky(double* G, int n, int* d_info, void* cublas, cudaStream_t st);
-// x = G^-1 h with the factor from cholesky().
-void cholesky_solve(const double* L, int n, const double* h, double* x, void* cublas, cudaStream_t st);
-// r = b - A x (FP64 A, row-major lda) and g = A^T r; returns ||r||_2 and ||g||_2.
-void residual(const double* A, int64_t lda, int64_t nrows, int ncols, const double* b, const double* x, double* r,
-              double* g, double* rnorm, double* gnorm, void* cublas, cudaStream_t st);
+// L = Cholesky factor of G + r I (n x n, L: device n*n doubles, column-major lower in
+// the symmetric storage) with r = ridge, grown tenfold at most 8 times while G + r I
+// is not positive definite.  Returns the r used, or -1 when every attempt failed.
+double factor_ridge(const double* G, int n, double ridge, double* L, int* d_info, cudaStream_t st);
+
+// The FP64 products of a least-squares problem with rows A (never stored whole by
+// the streamed form): apply(p, q): q = A^T (A p); residual(x, r): r = A^T (b - A x).
+// Row weights, when present, enter both as A^T W^2 (...).
+struct Fp64Operator {
+    std::function<void(const double* p, double* q)> apply;
+    std::function<void(const double* x, double* r)> residual;
+};
+struct PcgStats {
+    int iters = 0;
+    double rel_update = 0.0;   // |alpha| ||p|| / ||x|| of the last step
+    double rnorm0 = 0.0, rnorm = 0.0;   // ||A^T (b - A x) - ridge x|| before and after (recursive)
+};
+// Preconditioned CG on (A^T A + ridge I) x = A^T b from x (device, updated), with
+// M = L L^T (factor_ridge); stops after max_iters steps or when the relative update
+// falls to tol.
+PcgStats pcg_ridge(const double* L, int n, double ridge, const Fp64Operator& op, double* x, int max_iters,
+                   double tol, cudaStream_t st);
 
 // LARS with the lasso modification on G (full symmetric, FP64, device) and h:
 // coefficients into x (device); info: [steps, active variables, final C / n].
 // mode 0: scikit-learn LassoLars; mode 1 / 2: the reference's DLARS `lars` /
 // `lasso` (needs btb = b^T b; info[2] is then the objective of the last vertex).
 void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
-                double* info, void* cublas, cudaStream_t st, int mode = 0, double btb = 0.0);
+                double* info, cudaStream_t st, int mode = 0, double btb = 0.0);
 // DLARS with --normalize: columns centred and scaled, b centred (colsum = A^T 1 on
 // the device, bsum = sum b), coefficients returned in unscaled units.
 void dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int n, int64_t nsamples,
-                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, void* cublas,
-                      cudaStream_t st);
+                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, cudaStream_t st);
 
 }  // namespace cg

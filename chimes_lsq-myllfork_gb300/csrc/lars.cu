@@ -9,18 +9,20 @@
 //
 // Device state: correlations c = h - G w, coefficients, the active list and the
 // lower Cholesky factor of G_AA (row-major, leading dimension kmax).  Per step:
-// the largest inactive |c| (block reduction), the factor's new row (cuBLAS DTRSV
-// on the stored factor, then one small kernel), the equiangular direction (two
-// DTRSV), a = sum_k w_k G[active_k, :] over contiguous rows of G, the step length
+// the largest inactive |c| (block reduction), the factor's new row (a triangular
+// solve on the stored factor, dense64.cu, then one small kernel), the equiangular
+// direction (two triangular solves), a = sum_k w_k G[active_k, :] over contiguous rows of G, the step length
 // (block reductions over inactive crossings and active zero crossings), and on a
 // zero crossing the deletion of the variable from the factor by Givens rotations.
-#include <cublas_v2.h>
 
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
 #include <string>
 #include <vector>
+
+#include "dense64.h"
+#include "gram.h"
 
 namespace cgd {
 
@@ -250,14 +252,11 @@ namespace cg {
 static void ckl(cudaError_t e, const char* w) {
     if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error in ") + w + ": " + cudaGetErrorString(e));
 }
-static void cbl(cublasStatus_t s, const char* w) {
-    if (s != CUBLAS_STATUS_SUCCESS) throw std::runtime_error(std::string("cuBLAS error in ") + w);
-}
 
 // Returns [steps, active variables, final C / n]; x (device, n values) receives
 // the coefficients.  G: full symmetric FP64 (row-major), h: X^T y (device).
 void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
-                double* info, void* cublas, cudaStream_t st, int mode, double btb) {
+                double* info, cudaStream_t st, int mode, double btb) {
     // mode 0: scikit-learn LassoLars (exact landing on C/n = alpha).  mode 1 / 2: the
     // reference's DLARS `lars` / `lasso` (contrib/dlars/src/dlars.C): the variable
     // named by the last step enters, C = max |c| over every variable, lasso
@@ -266,8 +265,6 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
     // previous vertex's by more than 1e-10, returning that vertex (the driver,
     // :376-420).
     const bool dl = mode != 0, dlasso = mode == 2;
-    cublasHandle_t hb = (cublasHandle_t)cublas;
-    cbl(cublasSetStream(hb, st), "setStream");
     const int kmax = (int)std::min<int64_t>(n, std::max<int64_t>(nsamples, 1));
     std::vector<void*> mem;
     auto get = [&](size_t bytes) {
@@ -335,10 +332,9 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
                     ckl(cudaStreamSynchronize(st), "sync");
                     d2 = gjj;
                 } else {
-                    // L l = G[A, j]: the stored row-major lower factor is column-major upper U = L^T
+                    // L l = G[A, j] with the row-major lower factor L(i, j) = L[i * kmax + j]
                     cgd::k_lars_gather<<<(na + tb - 1) / tb, tb, 0, st>>>(G, n, dact, na, j, sv);
-                    cbl(cublasDtrsv(hb, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, na, L, kmax, sv, 1),
-                        "trsv add");
+                    trsv64(L, kmax, 1, na, true, sv, st);
                     cgd::k_lars_dot_rest<<<1, cgd::LARS_THREADS, 0, st>>>(sv, na, gjj, scal);
                     ckl(cudaMemcpyAsync(&d2, scal, sizeof(double), cudaMemcpyDeviceToHost, st), "d2");
                     ckl(cudaStreamSynchronize(st), "sync");
@@ -365,8 +361,8 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
             // equiangular direction: L L^T w = s, w *= AA
             cgd::k_lars_signs<<<(na + tb - 1) / tb, tb, 0, st>>>(c, dact, na, sv);
             ckl(cudaMemcpyAsync(w, sv, sizeof(double) * na, cudaMemcpyDeviceToDevice, st), "w = s");
-            cbl(cublasDtrsv(hb, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, na, L, kmax, w, 1), "trsv 1");
-            cbl(cublasDtrsv(hb, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, na, L, kmax, w, 1), "trsv 2");
+            trsv64(L, kmax, 1, na, true, w, st);    // L y = s
+            trsv64(L, 1, kmax, na, false, w, st);   // L^T w = y
             cgd::k_lars_scale<<<1, cgd::LARS_THREADS, 0, st>>>(sv, w, na, scal + 1);
             cgd::k_lars_direction<<<(n + tb - 1) / tb, tb, 0, st>>>(G, n, dact, w, na, a);
             double AA = 0.0;
@@ -425,8 +421,7 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
 }
 
 void dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int n, int64_t nsamples,
-                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, void* cublas,
-                      cudaStream_t st) {
+                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, cudaStream_t st) {
     double *Gc = nullptr, *hc = nullptr, *sigma = nullptr;
     int* bad = nullptr;
     ckl(cudaMallocAsync((void**)&Gc, sizeof(double) * (size_t)n * n, st), "normalised G");
@@ -447,7 +442,7 @@ void dlars_normalized(const double* G, const double* h, const double* colsum, do
         const int64_t nn = (int64_t)n * n;
         cgd::k_dlars_center<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(G, h, colsum, sigma, n, N, ybar, Gc, hc);
         ckl(cudaGetLastError(), "normalise");
-        lars_lasso(Gc, hc, n, nsamples, lambda, max_iter, x, info, cublas, st, lasso ? 2 : 1, btb - N * ybar * ybar);
+        lars_lasso(Gc, hc, n, nsamples, lambda, max_iter, x, info, st, lasso ? 2 : 1, btb - N * ybar * ybar);
         cgd::k_dlars_unscale<<<(n + 255) / 256, 256, 0, st>>>(x, sigma, n);
         ckl(cudaGetLastError(), "unscale");
     } catch (...) {

@@ -742,6 +742,14 @@ void Session::md_run(DeviceFrames& df, const double* mass_type, double dt, int n
 namespace cg {
 namespace {
 
+// Device bytes of one serving arena (the arrays ServeArena::init allocates).
+size_t arena_bytes(int64_t atoms, int frames, int nimg) {
+    auto r = [](size_t n, size_t esz) { return std::max<size_t>(n, 1) * esz; };
+    return r(frames, 4) + 3 * r(frames + 1, 8) + 2 * r(frames, 4) + r(frames, sizeof(cgd::BoxDev)) + r(atoms, 4) +
+           4 * r(3 * atoms, 8) + r((size_t)frames * cgd::MD_NSCALAR, 8) + r(3 * atoms * nimg, 8) +
+           r(4 * atoms * nimg, 4) + r(frames, 1);
+}
+
 // Device arrays of one batch composition, sized for the largest batch.
 struct ServeArena {
     std::vector<void*> allocs;
@@ -800,6 +808,13 @@ double now_s(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
+void Session::md_serve_memory(int64_t max_batch_atoms, int max_batch_frames, double* arena, double* per_atom) const {
+    const int L = model_.ctl.nlayers;
+    const int nimg = (2 * L + 1) * (2 * L + 1) * (2 * L + 1);
+    if (arena) *arena = 2.0 * (double)arena_bytes(max_batch_atoms, std::max(1, max_batch_frames), nimg);
+    if (per_atom) *per_atom = 2.0 * serve_list_per_atom_;
+}
+
 int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_type, const MdServeOptions& opt,
                           MdResult* res, double* step_ms) {
     CK(cudaSetDevice(device_));
@@ -846,6 +861,21 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
     cudaStream_t st = stream_;
     const int64_t cap_atoms = opt.max_batch_atoms;
     const int cap_frames = std::max(1, opt.max_batch_frames);
+    // Device memory: the two arenas (fixed, allocated below) plus the neighbour /
+    // cluster lists of the running composition, which grow with its atoms.  A request
+    // of n atoms reserves 2 * list_per_atom * n bytes (the current lists and the set
+    // built ahead of need); list_per_atom starts from a prior and is replaced by the
+    // lists' measured allocation per atom after every build (never shrinking).
+    const double fixed = 2.0 * (double)arena_bytes(cap_atoms, cap_frames, nimg);
+    if (fixed > opt.hbm_budget)
+        throw Error(1, "hbm_budget of " + std::to_string((long long)opt.hbm_budget) + " bytes is below the " +
+                           std::to_string((long long)fixed) + " bytes of the serving arenas for max_batch_atoms");
+    auto need = [&](int64_t atoms) { return 2.0 * serve_list_per_atom_ * (double)atoms; };
+    for (int r = 0; r < nreq; ++r)
+        if (fixed + need(req[r].natoms) > opt.hbm_budget)
+            throw Error(1, "request " + std::to_string(r) + " alone needs more device memory (" +
+                               std::to_string((long long)(fixed + need(req[r].natoms))) +
+                               " bytes with the arenas) than hbm_budget allows");
     ServeArena arena[2];
     arena[0].init(cap_atoms, cap_frames, nimg);
     arena[1].init(cap_atoms, cap_frames, nimg);
@@ -866,14 +896,13 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
     std::vector<int> order(nreq);
     for (int r = 0; r < nreq; ++r) order[r] = r;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return req[a].arrival < req[b].arrival; });
-    const double per_atom_bytes = 12288.0, per_req_bytes = 65536.0;   // resident estimate per request
     std::vector<int> active, steps_done(nreq, 0);
     std::vector<int64_t> pos(nreq, -1);      // atom offset of each active request in the current arena
     std::vector<char> first(nreq, 0);
     int cur = 0, next_pending = 0, finished = 0;
     int64_t active_atoms = 0, nbatch = 0;
     MdListSet lists;   // skin lists of the current composition
-    double mem = 0.0;
+    int64_t builds_seen = 0;
     bool changed = false;
     const auto t0 = std::chrono::steady_clock::now();
     while (finished < nreq) {
@@ -881,16 +910,20 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
         double t = now_s(t0);
         while (next_pending < nreq) {
             const MdRequest& q = req[order[next_pending]];
-            const double need = per_atom_bytes * q.natoms + per_req_bytes;
-            if (q.arrival > t || active_atoms + q.natoms > cap_atoms || (int)active.size() >= cap_frames ||
-                mem + need > opt.hbm_budget)
+            if (q.arrival > t || active_atoms + q.natoms > cap_atoms || (int)active.size() >= cap_frames) break;
+            if (fixed + need(active_atoms + q.natoms) > opt.hbm_budget) {
+                if (active.empty())   // the measured list size leaves no room for it even alone
+                    throw Error(4, "request " + std::to_string(order[next_pending]) +
+                                       " needs more device memory than hbm_budget allows (measured list size " +
+                                       std::to_string((long long)serve_list_per_atom_) + " bytes per atom)");
                 break;
+            }
             const int r = order[next_pending++];
             active.push_back(r);
             active_atoms += q.natoms;
-            mem += need;
             first[r] = 1;
             res[r].admitted = t;
+            res[r].reserved_bytes = need(q.natoms);
             changed = true;
         }
         if (active.empty()) {
@@ -964,6 +997,14 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
         CK(cudaStreamSynchronize(st));
         const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - s0).count();
         ++nbatch;
+        // list bytes per atom measured on the lists just built (grow-only buffers)
+        const int64_t nbuilds = lists.lists[0].builds + lists.lists[1].builds;
+        if (nbuilds != builds_seen && active_atoms > 0) {
+            builds_seen = nbuilds;
+            size_t bytes = 0;
+            for (size_t c : lists.current().caps) bytes += c;
+            serve_list_per_atom_ = std::max(serve_list_per_atom_, (double)bytes / (double)active_atoms);
+        }
         // bookkeeping, retire finished requests
         std::vector<int> keep;
         keep.reserve(active.size());
@@ -977,7 +1018,6 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
                     CK(cudaMemcpyAsync(req[r].xyz_out, C.xyz + 3 * pos[r], 3 * req[r].natoms * sizeof(double),
                                        cudaMemcpyDeviceToHost, st));
                 active_atoms -= req[r].natoms;
-                mem -= per_atom_bytes * req[r].natoms + per_req_bytes;
                 ++finished;
                 changed = true;
             } else {

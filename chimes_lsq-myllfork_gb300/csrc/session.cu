@@ -6,9 +6,8 @@
 #include <mutex>
 #include <numeric>
 
-#include <cublas_v2.h>
-
 #include "../../include/chimes_gb300.h"
+#include "dense64.h"
 #include "gram.h"
 #include "assemble.h"
 #include "kernels.h"
@@ -361,18 +360,16 @@ void Session::reset_stage_totals() {
 // ------------------------------------------------------------------ session
 Session::Session(const Model& m, int device) : model_(m), device_(device) {
     CK(cudaSetDevice(device));
-    CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    // A blocking stream: work the caller queued on the legacy default stream (for
+    // example the zeroing of G by a framework) completes before the session's next
+    // launch, and the other way round.
+    CK(cudaStreamCreateWithFlags(&stream_, cudaStreamDefault));
     dm_.reset(new DeviceModel(model_, cgd::VIR_PPT * cgd::MB_THREADS));
-    cublasHandle_t h = nullptr;
-    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) throw Error(3, "cublasCreate failed");
-    cublasSetStream(h, stream_);
-    cublas_ = h;
 }
 
 Session::~Session() {
     for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : event_pool_) cudaEventDestroy(e);
-    if (cublas_) cublasDestroy((cublasHandle_t)cublas_);
     md_.reset();
     dm_.reset();
     if (side_event_) cudaEventDestroy(side_event_);
@@ -704,7 +701,7 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
         planes = S.get<unsigned char>(pbytes);
     }
     try {
-        gram_accumulate(prec_in, A, lda, nrows, ncols, b, mode, G, h, planes, pbytes, d_err, cublas_, stream_,
+        gram_accumulate(prec_in, A, lda, nrows, ncols, b, mode, G, h, planes, pbytes, d_err, stream_,
                         [this](int stage, bool begin) { mark(stage, begin); }, gram_ctas_per_sm_);
     } catch (const std::runtime_error& e) {
         throw Error(3, e.what());
@@ -719,7 +716,7 @@ void Session::lars(const double* G, const double* h, int ncols, int64_t nsamples
                    double* x, double* info, int mode, double btb) {
     CK(cudaSetDevice(device_));
     try {
-        lars_lasso(G, h, ncols, nsamples, alpha, max_iter, x, info, cublas_, stream_, mode, btb);
+        lars_lasso(G, h, ncols, nsamples, alpha, max_iter, x, info, stream_, mode, btb);
     } catch (const std::runtime_error& e) {
         throw Error(3, e.what());
     }
@@ -730,8 +727,7 @@ void Session::dlars_normalized(const double* G, const double* h, const double* c
                                double* info) {
     CK(cudaSetDevice(device_));
     try {
-        cg::dlars_normalized(G, h, colsum, bsum, ncols, nsamples, btb, lambda, lasso, max_iter, x, info, cublas_,
-                             stream_);
+        cg::dlars_normalized(G, h, colsum, bsum, ncols, nsamples, btb, lambda, lasso, max_iter, x, info, stream_);
     } catch (const std::runtime_error& e) {
         throw Error(2, e.what());
     }
@@ -742,77 +738,96 @@ void Session::gram_finish(double* G, int ncols) {
     gram_symmetrize(G, ncols, true, stream_);
 }
 
-__global__ void k_add_diag(double* G, int n, double v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) G[(int64_t)i * n + i] += v;
-}
-
 void Session::solve(const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda,
                     int64_t nrows, const double* b, int iters, double* x, double* info) {
     CK(cudaSetDevice(device_));
     Scratch S(stream_);
     double* L = S.get<double>((size_t)ncols * ncols);
     int* d_info = S.get<int>(1);
-    cublasHandle_t hb = (cublasHandle_t)cublas_;
     try {
-        // Cholesky of G + ridge I; the ridge grows tenfold (up to 8 times) until the
-        // factorisation succeeds (a mixed-precision G can be indefinite at tiny ridges).
-        double used = ridge;
-        bool ok = false;
-        for (int attempt = 0; attempt < 9 && !ok; ++attempt) {
-            CK(cudaMemcpyAsync(L, G, sizeof(double) * ncols * ncols, cudaMemcpyDeviceToDevice, stream_));
-            if (used != 0.0) k_add_diag<<<(ncols + 255) / 256, 256, 0, stream_>>>(L, ncols, used);
-            ok = cholesky(L, ncols, d_info, cublas_, stream_);
-            if (!ok) used = used > 0.0 ? used * 10.0 : 1e-12;
-        }
-        if (!ok) throw Error(2, "the normal-equations matrix is not positive definite even with a ridge");
-        cholesky_solve(L, ncols, h, x, cublas_, stream_);
-        double rn = 0, gn = 0;
+        const double used = factor_ridge(G, ncols, ridge, L, d_info, stream_);
+        if (used < 0.0) throw Error(2, "the normal-equations matrix is not positive definite even with a ridge");
+        cholesky_solve64(L, ncols, h, x, stream_);
+        PcgStats ps;
         if (iters > 0 && A && b) {
-            // preconditioned CG on the FP64 ridge normal equations (A^T A + ridge I) x = A^T b,
-            // products through A; preconditioner (L L^T)^-1 from the (possibly mixed-precision,
-            // possibly more strongly ridged) Gram factor
-            double* r = S.get<double>(ncols);   // normal-equation residual
-            double* z = S.get<double>(ncols);
-            double* pv = S.get<double>(ncols);
-            double* q = S.get<double>(ncols);
+            // preconditioned CG on the FP64 ridge system with products through the resident A
             double* t = S.get<double>(nrows);
-            const double one = 1.0, zero = 0.0, mridge = -ridge;
-            cublasSetStream(hb, stream_);
-            cublasSetPointerMode(hb, CUBLAS_POINTER_MODE_HOST);
-            residual(A, lda, nrows, ncols, b, x, t, r, &rn, &gn, cublas_, stream_);
-            if (ridge != 0.0) cublasDaxpy(hb, ncols, &mridge, x, 1, r, 1);
-            cholesky_solve(L, ncols, r, z, cublas_, stream_);
-            CK(cudaMemcpyAsync(pv, z, sizeof(double) * ncols, cudaMemcpyDeviceToDevice, stream_));
-            double rz = 0;
-            cublasDdot(hb, ncols, r, 1, z, 1, &rz);
-            for (int it = 0; it < iters && rz > 0.0; ++it) {
-                // q = A^T (A p) + ridge p
-                cublasDgemv(hb, CUBLAS_OP_T, ncols, (int)nrows, &one, A, (int)lda, pv, 1, &zero, t, 1);
-                cublasDgemv(hb, CUBLAS_OP_N, ncols, (int)nrows, &one, A, (int)lda, t, 1, &zero, q, 1);
-                if (ridge != 0.0) cublasDaxpy(hb, ncols, &ridge, pv, 1, q, 1);
-                double pq = 0;
-                cublasDdot(hb, ncols, pv, 1, q, 1, &pq);
-                if (!(pq > 0.0)) break;
-                const double alpha = rz / pq, malpha = -alpha;
-                cublasDaxpy(hb, ncols, &alpha, pv, 1, x, 1);
-                cublasDaxpy(hb, ncols, &malpha, q, 1, r, 1);
-                cholesky_solve(L, ncols, r, z, cublas_, stream_);
-                double rz_new = 0;
-                cublasDdot(hb, ncols, r, 1, z, 1, &rz_new);
-                const double beta = rz_new / rz;
-                cublasDscal(hb, ncols, &beta, pv, 1);
-                cublasDaxpy(hb, ncols, &one, z, 1, pv, 1);
-                rz = rz_new;
-            }
-            residual(A, lda, nrows, ncols, b, x, t, r, &rn, &gn, cublas_, stream_);
-            if (ridge != 0.0) {
-                cublasDaxpy(hb, ncols, &mridge, x, 1, r, 1);
-                cublasDnrm2(hb, ncols, r, 1, &gn);
-            }
+            double* partial = S.get<double>(atb_partial_doubles(nrows, ncols));
+            Fp64Operator op;
+            op.apply = [&](const double* p, double* q) {
+                gemv_rows64(A, lda, nrows, ncols, p, nullptr, nullptr, t, stream_);
+                CK(cudaMemsetAsync(q, 0, sizeof(double) * ncols, stream_));
+                gemv_cols64(A, lda, nrows, ncols, t, q, partial, stream_);
+            };
+            op.residual = [&](const double* xv, double* r) {
+                gemv_rows64(A, lda, nrows, ncols, xv, b, nullptr, t, stream_);
+                CK(cudaMemsetAsync(r, 0, sizeof(double) * ncols, stream_));
+                gemv_cols64(A, lda, nrows, ncols, t, r, partial, stream_);
+            };
+            ps = pcg_ridge(L, ncols, ridge, op, x, iters, 1e-15, stream_);
         }
         CK(cudaStreamSynchronize(stream_));
-        if (info) { info[0] = rn; info[1] = gn; info[2] = used; }
+        if (info) { info[0] = ps.rnorm0; info[1] = ps.rnorm; info[2] = used; }
+    } catch (const std::runtime_error& e) {
+        if (dynamic_cast<const Error*>(&e)) throw;
+        throw Error(3, e.what());
+    }
+}
+
+double Session::fp64_fma_tflops() {
+    CK(cudaSetDevice(device_));
+    try {
+        return cg::fp64_fma_tflops(stream_);
+    } catch (const std::runtime_error& e) {
+        throw Error(3, e.what());
+    }
+}
+
+void Session::solve_streamed(const double* G, const double* h, int ncols, double ridge,
+                             const std::vector<const DeviceFrames*>& blocks, const std::vector<const double*>& labels,
+                             const std::vector<const double*>& weights, const double* extra_A, int64_t extra_rows,
+                             const double* extra_b, const double* extra_w, int max_iters, double tol, double* x,
+                             double* info) {
+    CK(cudaSetDevice(device_));
+    if (blocks.size() != labels.size() || (!weights.empty() && weights.size() != blocks.size()))
+        throw Error(1, "blocks, labels and weights differ in number");
+    if (ncols != model_.tot_all) throw Error(1, "ncols is not the model's column count");
+    Scratch S(stream_);
+    double* L = S.get<double>((size_t)ncols * ncols);
+    int* d_info = S.get<int>(1);
+    int64_t maxrows = std::max<int64_t>(1, extra_rows);
+    for (const DeviceFrames* d : blocks) maxrows = std::max<int64_t>(maxrows, d->nrows);
+    double* Ablk = S.get<double>((size_t)maxrows * ncols);   // one FP64 row block at a time
+    double* t = S.get<double>(maxrows);
+    double* partial = S.get<double>(atb_partial_doubles(maxrows, ncols));
+    try {
+        const double used = factor_ridge(G, ncols, ridge, L, d_info, stream_);
+        if (used < 0.0) throw Error(2, "the normal-equations matrix is not positive definite even with a ridge");
+        cholesky_solve64(L, ncols, h, x, stream_);
+        // one pass over every row block: FP64 assembly, t = (b -) A v, (t *= w^2), out += A^T t
+        auto pass = [&](const double* v, bool resid, double* out) {
+            CK(cudaMemsetAsync(out, 0, sizeof(double) * ncols, stream_));
+            for (size_t k = 0; k < blocks.size(); ++k) {
+                const DeviceFrames& d = *blocks[k];
+                if (d.nrows == 0) continue;
+                assemble(d, 0, Ablk, ncols, nullptr);
+                gemv_rows64(Ablk, ncols, d.nrows, ncols, v, resid ? labels[k] : nullptr,
+                            weights.empty() ? nullptr : weights[k], t, stream_);
+                gemv_cols64(Ablk, ncols, d.nrows, ncols, t, out, partial, stream_);
+            }
+            if (extra_rows > 0) {
+                gemv_rows64(extra_A, ncols, extra_rows, ncols, v, resid ? extra_b : nullptr, extra_w, t, stream_);
+                gemv_cols64(extra_A, ncols, extra_rows, ncols, t, out, partial, stream_);
+            }
+        };
+        Fp64Operator op;
+        op.apply = [&](const double* p, double* q) { pass(p, false, q); };
+        op.residual = [&](const double* xv, double* r) { pass(xv, true, r); };
+        const PcgStats ps = pcg_ridge(L, ncols, ridge, op, x, max_iters, tol, stream_);
+        CK(cudaStreamSynchronize(stream_));
+        if (info) {
+            info[0] = ps.iters; info[1] = ps.rel_update; info[2] = ps.rnorm0; info[3] = ps.rnorm; info[4] = used;
+        }
     } catch (const std::runtime_error& e) {
         if (dynamic_cast<const Error*>(&e)) throw;
         throw Error(3, e.what());
@@ -859,7 +874,7 @@ std::unique_ptr<BatchFit> Session::batch_fit_graph(const std::vector<const Devic
             run(*blocks[k], precision, Abuf, lda, nullptr, S, &plans[k], nullptr);
             void* planes = S.get<unsigned char>(pbytes);
             gram_accumulate(precision, Abuf, lda, blocks[k]->nrows, ncols, labels[k], 1, G, h, planes, pbytes,
-                            bf->d_err, cublas_, stream_, [](int, bool) {}, gram_ctas_per_sm_);
+                            bf->d_err, stream_, [](int, bool) {}, gram_ctas_per_sm_);
         }
     } catch (...) {
         cudaGraph_t g = nullptr;

@@ -148,6 +148,7 @@ struct MdRequest {
 struct MdResult {
     double admitted = 0, finished = 0;    // seconds after the start of the run
     double step_ms_sum = 0, step_ms_max = 0;
+    double reserved_bytes = 0;            // device memory reserved for it at admission
 };
 struct MdServeOptions {
     double dt = 0;                        // internal time units
@@ -202,7 +203,19 @@ class Session {
     // (A may be null when iters == 0).  info: [rnorm, gnorm, ridge used].
     void solve(const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda, int64_t nrows,
                const double* b, int iters, double* x, double* info);
-    void* cublas() const { return cublas_; }
+    // The mixed form's solve without a stored FP64 A: x = (G + r I)^-1 h (FP64
+    // Cholesky), then preconditioned CG on the FP64 ridge system whose products
+    // A^T (A p) and residual A^T (b - A x) are formed block by block from FP64 rows
+    // assembled again for each pass (labels[k], weights[k]: block k's b and row
+    // weights on the device; weights may be empty).  extra_A (device, row-major,
+    // extra_rows x ncols, may be null) joins as one more block (charge-constraint
+    // rows).  Stops after max_iters passes or when the relative update reaches tol.
+    // info: [iterations, last relative update, initial and final residual norm, r].
+    void solve_streamed(const double* G, const double* h, int ncols, double ridge,
+                        const std::vector<const DeviceFrames*>& blocks, const std::vector<const double*>& labels,
+                        const std::vector<const double*>& weights, const double* extra_A, int64_t extra_rows,
+                        const double* extra_b, const double* extra_w, int max_iters, double tol, double* x,
+                        double* info);
     // Sizing pass of a batch (a full assembly into A) recording its list sizes.
     RunPlan plan(const DeviceFrames& df, int precision, void* A, int64_t lda);
     // Capture the assembly of every block into Abuf (lda) and the split-BF16 Gram
@@ -214,6 +227,8 @@ class Session {
     void batch_fit_launch(BatchFit& bf);
     void set_gram_ctas_per_sm(int v) { gram_ctas_per_sm_ = v > 0 ? v : 4; }
     int gram_ctas_per_sm() const { return gram_ctas_per_sm_; }
+    // Measured FP64 FMA rate of the session's GPU in TFLOP/s (dense64.cu).
+    double fp64_fma_tflops();
     // LARS-lasso on the normal equations (lars.cu).
     void lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter, double* x,
               double* info, int mode = 0, double btb = 0.0);
@@ -275,6 +290,10 @@ class Session {
     // = largest nsteps.  Returns the number of batched steps.
     int64_t md_serve(const std::vector<MdRequest>& req, const double* mass_type, const MdServeOptions& opt,
                      MdResult* res, double* step_ms);
+    // Device memory of the serving loop: the fixed bytes of its two arenas for these
+    // capacities, and the bytes a request reserves per atom (list estimate; measured
+    // by the last serving run of this session, a prior before any).
+    void md_serve_memory(int64_t max_batch_atoms, int max_batch_frames, double* arena, double* per_atom) const;
 
     // Stage timing (CUDA events on the session stream).
     void set_profiling(bool on) { profiling_ = on; }
@@ -298,11 +317,11 @@ class Session {
     cudaStream_t stream_ = nullptr;
     cudaStream_t side_stream_ = nullptr;   // look-ahead MD list builds
     cudaEvent_t side_event_ = nullptr;
-    void* cublas_ = nullptr;
     std::unique_ptr<DeviceModel> dm_;
     std::unique_ptr<MdTables> md_;
     int gram_ctas_per_sm_ = 4;
     double md_skin_ = 0.5;   // Angstrom; 0: enumerate every step
+    double serve_list_per_atom_ = 6144.0;   // list bytes per atom (measured by md_serve)
     std::vector<double> md_state_;   // last md_run: nframes * MD_TH_STRIDE
     MdThermostat md_last_th_;
     std::vector<double> md_resume_;  // next md_run's starting restart values (nframes * 29)

@@ -9,10 +9,11 @@ Writes params.header, ff_groups.map, params.txt and force.txt (and, with
 --write-a, A.txt / b.txt / b-labeled.txt / natoms.txt / dim.txt) in the reference's
 formats.  The design matrix is assembled on the GPU in blocks of frames and folded
 into the normal equations G = A^T A, h = A^T b:
-  fp64   FP64 assembly, FP64 library Gram, FP64 Cholesky (ridge) or LARS;
+  fp64   FP64 assembly, FP64 SYRK Gram, FP64 Cholesky (ridge) or LARS;
   mixed  FP32 assembly, split-BF16 tensor-core Gram; ridge is then refined by
-         conjugate gradients with FP64 products through an FP64 A (--refine N
-         iterations, when the FP64 A fits on the device).
+         preconditioned conjugate gradients on the FP64 system, each pass
+         assembling the row blocks again in FP64 (no FP64 A is stored; at most
+         --refine passes, stopping once the relative update is below --tol).
 ridge solves (A^T A + alpha I) x = A^T b (scikit-learn Ridge(alpha,
 fit_intercept=False), the reference's --algorithm ridge); lassolars follows the
 LARS-lasso path to (1/2n)||b - A x||^2 + alpha ||x||_1 (the reference's
@@ -41,7 +42,9 @@ def main(argv=None):
     ap.add_argument("--alpha", type=float, default=1.0e-3)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--block-frames", type=int, default=64)
-    ap.add_argument("--refine", type=int, default=50, help="CG iterations of the mixed ridge solve")
+    ap.add_argument("--refine", type=int, default=50, help="most CG passes of the mixed ridge solve")
+    ap.add_argument("--tol", type=float, default=1e-11,
+                    help="mixed ridge solve: stop once the relative size of a CG update is below this")
     ap.add_argument("--normalize", action="store_true",
                     help="dlars / dlasso: centre and scale the columns and centre b (DLARS --normalize=y)")
     ap.add_argument("--write-a", action="store_true", help="also write A.txt, b.txt, ... (slow for large A)")
@@ -74,7 +77,7 @@ def main(argv=None):
     nfr_rows = sum(b.nrows for b in blocks)
     nrows = nfr_rows + Acon.shape[0]
     fits = nrows * C * 8 < 0.5 * torch.cuda.mem_get_info()[0]
-    keep64 = fits and (not mixed or (args.algorithm == "ridge" and args.refine > 0))
+    keep64 = fits and not mixed   # the plain form keeps its FP64 A for force.txt when it fits
     A64_all = torch.empty((nrows, C), dtype=torch.float64, device="cuda") if keep64 else None
     b_all = torch.empty(nrows, dtype=torch.float64, device="cuda")
     w_all = None   # row weights (src/chimes_lsq.py:71-149)
@@ -86,10 +89,15 @@ def main(argv=None):
     wp = (lambda r: w_all[r:].data_ptr()) if w_all is not None else (lambda r: 0)
     wcol = (lambda r, n: w_all[r:r + n, None]) if w_all is not None else (lambda r, n: 1.0)
     colsum = torch.zeros(C, dtype=torch.float64, device="cuda")   # A^T 1 (DLARS --normalize)
+    dfrs, lab_ptrs, w_ptrs = [], [], []   # the mixed form's blocks, kept for the FP64 refinement
     r0 = 0
     for blk in blocks:
         dfr = sess.upload(blk)
         n = blk.nrows
+        if mixed:
+            dfrs.append(dfr)
+            lab_ptrs.append(b_all[r0:].data_ptr())
+            w_ptrs.append(w_all[r0:].data_ptr() if w_all is not None else 0)
         b_all[r0:r0 + n] = torch.from_numpy(blk.labels())
         if mixed:
             A32 = torch.empty((n, C), dtype=torch.float32, device="cuda")
@@ -97,14 +105,14 @@ def main(argv=None):
             sess.gram(1, A32.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 1, G.data_ptr(), h.data_ptr(), wp(r0))
             colsum += (A32.double() * wcol(r0, n)).sum(0)
             del A32
-        if keep64 or not mixed:
+        else:
             dst = A64_all[r0:r0 + n] if keep64 else torch.empty((n, C), dtype=torch.float64, device="cuda")
             sess.assemble_device(dfr, cg.CG_FP64, dst.data_ptr(), C)
-            if not mixed:
-                sess.gram(0, dst.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr(), wp(r0))
-                colsum += (dst * wcol(r0, n)).sum(0)
+            sess.gram(0, dst.data_ptr(), C, n, C, b_all[r0:].data_ptr(), 0, G.data_ptr(), h.data_ptr(), wp(r0))
+            colsum += (dst * wcol(r0, n)).sum(0)
             del dst
         r0 += n
+    dAc = None
     if Acon.shape[0]:   # the constraint rows join the normal equations like any row block
         dAc = torch.from_numpy(Acon).cuda()
         b_all[r0:] = torch.from_numpy(bcon)
@@ -118,16 +126,22 @@ def main(argv=None):
     lines = [f"! Date  {datetime.date.today()}", "!", f"! Number of variables            =  {C}",
              f"! Number of equations            =  {nrows}"]
     if args.algorithm == "ridge":
-        iters = args.refine if (mixed and keep64) else 0
-        Ar, br = A64_all, b_all   # the refinement's residuals are those of the weighted rows
-        if iters and w_all is not None:
-            Ar, br = A64_all * w_all[:, None], b_all * w_all
-        sess.solve(G.data_ptr(), h.data_ptr(), C, args.alpha, Ar.data_ptr() if iters else 0, C, nrows,
-                   br.data_ptr() if iters else 0, iters, x.data_ptr())
-        del Ar, br
+        if mixed and args.refine > 0:
+            extra = None
+            if dAc is not None:
+                extra = (dAc.data_ptr(), Acon.shape[0], b_all[r0:].data_ptr(),
+                         w_all[r0:].data_ptr() if w_all is not None else 0)
+            info = sess.solve_streamed(G.data_ptr(), h.data_ptr(), C, args.alpha, dfrs, lab_ptrs, x.data_ptr(),
+                                       weight_ptrs=w_ptrs if w_all is not None else None, extra=extra,
+                                       max_iters=args.refine, tol=args.tol)
+            iters = info["iters"]
+        else:
+            sess.solve(G.data_ptr(), h.data_ptr(), C, args.alpha, 0, C, 0, 0, 0, x.data_ptr())
+            iters = 0
         lines += ["! ridge regression used", "! Ridge alpha = %11.4e" % args.alpha]
         if mixed:
-            lines += [f"! split-BF16 tensor-core Gram, FP64 Cholesky, {iters} FP64-product CG iterations"]
+            lines += [f"! split-BF16 tensor-core Gram, FP64 Cholesky, {iters} FP64 CG passes "
+                      f"over FP64 row blocks assembled again"]
     elif args.algorithm == "lassolars":
         sess.lars(G.data_ptr(), h.data_ptr(), C, nrows, args.alpha, x.data_ptr())
         lines += ["! LARS implementation of LASSO used", "! LASSO alpha = %11.4e" % args.alpha]

@@ -286,8 +286,28 @@ WORKLOADS = {
 }
 
 
-def make_workload(name, outdir, nframes=None, seed=1234, labels=True, **over):
-    """Write <outdir>/fm_setup.in and <outdir>/traj.xyzf; returns the fm_setup.in path."""
+def _chno_labels_many(args):
+    return [chno_labels(*a) for a in args]
+
+
+def _labels_parallel(jobs, workers):
+    """chno_labels of every (xyz, types, cell) job, in a pool of `workers` fresh
+    interpreters (spawn: safe beside an initialised CUDA context); same values as
+    the serial loop, since each frame's labels depend on that frame alone."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    chunks = [jobs[i::workers] for i in range(workers)]
+    with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        parts = list(ex.map(_chno_labels_many, chunks))
+    out = [None] * len(jobs)
+    for i, part in enumerate(parts):
+        out[i::workers] = part
+    return out
+
+
+def make_workload(name, outdir, nframes=None, seed=1234, labels=True, workers=1, **over):
+    """Write <outdir>/fm_setup.in and <outdir>/traj.xyzf; returns the fm_setup.in path.
+    workers > 1 computes the C/H/N/O labels in that many processes."""
     cfg = dict(WORKLOADS[name])
     cfg.update(over)
     if nframes is not None:
@@ -310,6 +330,7 @@ def make_workload(name, outdir, nframes=None, seed=1234, labels=True, **over):
         if cfg.get("species2"):
             species, masses = species[:2], masses[:2]
         sizes = cfg.get("sizes")
+        geo = []
         for k in range(cfg["nframes"]):
             n = int(sizes[k]) if sizes is not None else cfg["natoms"]
             if cfg.get("triclinic", False):
@@ -318,10 +339,14 @@ def make_workload(name, outdir, nframes=None, seed=1234, labels=True, **over):
                 L = (n / cfg.get("density", 0.1)) ** (1.0 / 3.0)
                 cell = np.diag([L, L, L])
             xyz, types = chno_frame(rng, n, cell, ntypes=len(species))
-            if labels:
-                E, F, S = chno_labels(xyz, types, cell)
-            else:
-                E, F, S = 0.0, np.zeros_like(xyz), np.zeros(6)
+            geo.append((xyz, types, cell))
+        if not labels:
+            lab = [(0.0, np.zeros_like(g[0]), np.zeros(6)) for g in geo]
+        elif workers > 1 and len(geo) > 1:
+            lab = _labels_parallel(geo, min(workers, len(geo)))
+        else:
+            lab = [chno_labels(*g) for g in geo]
+        for (xyz, types, cell), (E, F, S) in zip(geo, lab):
             frames.append(dict(xyz=xyz, types=types, cell=cell, forces=F,
                                stress=S if cfg["fitstrs"] else None, energy=E if cfg["fitener"] else None))
     write_xyzf(os.path.join(outdir, "traj.xyzf"), frames, species)

@@ -151,7 +151,9 @@ int cg_assemble_device(cg_session* s, const cg_dframes* d, int precision, void* 
  * CG_NOALLOC_SCRATCH_BYTES compiled into the library, and calls no cudaMalloc,
  * cudaMallocAsync or cudaFree.  The caller still provides the uploaded frames and the
  * output A (device, row-major, lda >= ntotal).  Inputs whose work lists do not fit
- * are rejected with status 4 and a message naming the capacity.  The array exists
+ * are rejected with status 4 and a message naming the capacity; the earlier stages of
+ * such a call have already run, so the contents of A after a status-4 return are
+ * unspecified (neither zeroed nor complete).  The array exists
  * once per GPU that loads the library and stays allocated until the process exits.
  * The first call on a device looks up the array's device address (make that first
  * call before any stream capture).  Every call on a device shares the array and
@@ -163,7 +165,7 @@ int cg_assemble_device_noalloc(cg_session* s, const cg_dframes* d, int precision
 /* Normal equations of the fit (replaces the SVD of chimes_lsq.py, src/chimes_lsq.py:169-214).
  * cg_gram accumulates G += A^T A (row-major ncols x ncols FP64, upper triangle until
  * cg_gram_finish mirrors it) and h += A^T b for a device A block (row-major, lda,
- * a_precision CG_FP64 or CG_FP32).  mode CG_GRAM_FP64: FP64 library SYRK (FP64 A);
+ * a_precision CG_FP64 or CG_FP32).  mode CG_GRAM_FP64: FP64 SYRK on the CUDA cores (FP64 A);
  * CG_GRAM_BF16X3: A split into BF16 hi/lo planes, G from hi.hi + hi.lo + lo.hi on the
  * tensor cores with FP32 accumulation.  The caller zeroes G and h before the first
  * block.  All pointers are device pointers. */
@@ -188,6 +190,32 @@ int cg_gram_weighted(cg_session* s, int a_precision, const void* A, int64_t lda,
  * and the r of the factorisation. */
 int cg_solve(cg_session* s, const double* G, const double* h, int ncols, double ridge, const double* A, int64_t lda,
              int64_t nrows, const double* b, int iters, double* x, double* info);
+
+/* The mixed form's ridge solve without a stored FP64 A (replaces the solve of
+ * src/chimes_lsq.py:169-214 for a tensor-core Gram).  G, h: the normal equations of
+ * the fit (device; typically the split-BF16 Gram of an FP32-assembled A).  First
+ * x = (G + r I)^-1 h by FP64 Cholesky (r = ridge, grown as in cg_solve), then
+ * preconditioned conjugate gradients on the FP64 system (A^T A + ridge I) x = A^T b:
+ * every pass re-assembles each of the nblocks uploaded row blocks in FP64 into one
+ * block-sized device buffer and folds it into A^T (A p) (or A^T (b - A x)), so no
+ * FP64 A is ever stored whole.  labels[k] (device, block k's rows): b; weights
+ * (NULL, or device row weights per block): rows enter as W A, W b
+ * (src/chimes_lsq.py:140-149).  extra_A (device, row-major, extra_rows x ncols, may
+ * be NULL with extra_rows 0), extra_b, extra_w (may be NULL): rows outside the
+ * frames (FITCOUL charge constraints).  Stops after max_iters passes or once the
+ * relative size of the last update |alpha| ||p|| / ||x|| falls to tol.  info (host, 5
+ * doubles, may be NULL): passes made, last relative update, initial and final norm
+ * of A^T (b - A x) - ridge x, and the r of the factorisation.  x: device, ncols. */
+int cg_solve_streamed(cg_session* s, const double* G, const double* h, int ncols, double ridge, int nblocks,
+                      cg_dframes* const* blocks, const double* const* labels, const double* const* weights,
+                      const double* extra_A, int64_t extra_rows, const double* extra_b, const double* extra_w,
+                      int max_iters, double tol, double* x, double* info);
+
+/* FP64 fused multiply-add rate of the session's GPU in TFLOP/s (2 flops per FMA),
+ * measured by a kernel of independent FMA chains on every SM (no counterpart in the
+ * reference; the denominator of the FP64 roofline fractions).  Changes no device
+ * setting. */
+int cg_fp64_fma_rate(cg_session* s, double* tflops);
 
 /* LARS with the lasso modification (the reference's `--algorithm lassolars`,
  * scikit-learn LassoLars with fit_intercept=False, src/chimes_lsq.py:248-263; the
@@ -360,12 +388,18 @@ int cg_md_resume(cg_session* s, int nframes, const double* constraint29);
  * evaluates forces only, as chimes_md's first step) from its own positions and
  * velocities; it is admitted once its arrival time (seconds after the call starts)
  * has passed and the batch has room -- at most max_batch_atoms atoms and
- * max_batch_frames requests, and hbm_budget_bytes of estimated resident memory --
- * and every batched step advances all admitted requests together; a request leaves
- * the batch as soon as it finishes and its final positions are copied to xyz_out.
+ * max_batch_frames requests, and device memory within hbm_budget_bytes: the two
+ * serving arenas (fixed for these capacities) plus, per admitted request, its atoms
+ * times the list bytes per atom (cg_md_serve_memory; the lists' measured allocation
+ * after every build replaces the prior) -- and every batched step advances all
+ * admitted requests together; a request leaves the batch as soon as it finishes and
+ * its final positions are copied to xyz_out.  A budget below the arenas, or a request
+ * that cannot fit even alone, is refused (status 1 before any step, status 4 if the
+ * measured list size rules it out later) instead of waiting forever.
  * results[r]: admission / finish times (seconds), sum and maximum of its step times
- * (ms).  step_ms (may be NULL): nreq * max(nsteps) wall times (ms) of the batched
- * step that advanced request r at step s.  *batch_steps: number of batched steps. */
+ * (ms), bytes reserved for it at admission.  step_ms (may be NULL): nreq *
+ * max(nsteps) wall times (ms) of the batched step that advanced request r at step s.
+ * *batch_steps: number of batched steps. */
 typedef struct {
     int natoms, nsteps;
     double arrival;
@@ -376,11 +410,18 @@ typedef struct {
     double* xyz_out;
 } cg_md_request;
 typedef struct {
-    double admitted, finished, step_ms_sum, step_ms_max;
+    double admitted, finished, step_ms_sum, step_ms_max, reserved_bytes;
 } cg_md_result;
 int cg_md_serve(cg_session* s, int nreq, const cg_md_request* req, const double* mass, double dt_fs,
                 double hbm_budget_bytes, int64_t max_batch_atoms, int max_batch_frames, cg_md_result* results,
                 double* step_ms, int64_t* batch_steps);
+
+/* Device memory of cg_md_serve for these capacities: arena_bytes = the two serving
+ * arenas, bytes_per_atom = what an admitted request reserves per atom (the session's
+ * last measured list size, or the prior before its first serving run).  Either output
+ * may be NULL. */
+int cg_md_serve_memory(cg_session* s, int64_t max_batch_atoms, int max_batch_frames, double* arena_bytes,
+                       double* bytes_per_atom);
 
 /* Device pointer to the positions of uploaded frames (3 per atom), and a copy of
  * them into host memory. */

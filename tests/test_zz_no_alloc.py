@@ -20,13 +20,18 @@ from conftest import fixture_dir
 pytestmark = pytest.mark.gpu
 
 
-def _close(A, R):
+def _close(A, R, prec):
+    """FP64: 1e-12 of the entry and of its column's scale; FP32: 2e-5 of the column's
+    scale (the tolerances of the assembly parity tests)."""
     colmax = np.abs(R).max(axis=0)
-    return bool(np.all(np.abs(A - R) <= 1e-12 * np.abs(R) + 1e-12 * colmax[None, :]))
+    if prec == 0:
+        return bool(np.all(np.abs(A - R) <= 1e-12 * np.abs(R) + 1e-12 * colmax[None, :]))
+    return bool(np.all(np.abs(A - R) <= 2e-5 * (colmax[None, :] + 1e-300)))
 
 
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "fp32"])
 @pytest.mark.parametrize("name", ["water3b", "ch4b"])
-def test_noalloc_matches_device_entry_point(cg, name):
+def test_noalloc_matches_device_entry_point(cg, name, prec):
     torch = pytest.importorskip("torch")
     lib = cg.lib()
     model = cg.Model(os.path.join(fixture_dir(name), "fm_setup.in"))
@@ -34,16 +39,17 @@ def test_noalloc_matches_device_entry_point(cg, name):
     sess = cg.Session(model, 0)
     dfr = sess.upload(frames)
     nrows, ncols = frames.nrows, model.ncols
-    ref = torch.empty((nrows, ncols), dtype=torch.float64, device="cuda")
-    sess.assemble_device(dfr, cg.CG_FP64, ref.data_ptr(), ncols)
+    dt = torch.float64 if prec == cg.CG_FP64 else torch.float32
+    ref = torch.empty((nrows, ncols), dtype=dt, device="cuda")
+    sess.assemble_device(dfr, prec, ref.data_ptr(), ncols)
     torch.cuda.synchronize()
-    R = ref.cpu().numpy()
+    R = ref.double().cpu().numpy()
     for _ in range(2):
-        out = torch.full((nrows, ncols), float("nan"), dtype=torch.float64, device="cuda")
-        rc = lib.cg_assemble_device_noalloc(sess._h, dfr._h, cg.CG_FP64, ctypes.c_void_p(out.data_ptr()), ncols)
+        out = torch.full((nrows, ncols), float("nan"), dtype=dt, device="cuda")
+        rc = lib.cg_assemble_device_noalloc(sess._h, dfr._h, prec, ctypes.c_void_p(out.data_ptr()), ncols)
         assert rc == 0, lib.cg_last_error().decode()
         torch.cuda.synchronize()
-        assert _close(out.cpu().numpy(), R)
+        assert _close(out.double().cpu().numpy(), R, prec)
 
 
 def test_noalloc_rejects_oversize_input(cg, tmp_path):
