@@ -103,8 +103,14 @@ def lib():
         "cg_gram_finish": (ctypes.c_int, [vp, vp, ctypes.c_int]),
         "cg_solve": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_double, vp, ctypes.c_int64, ctypes.c_int64, vp,
                                     ctypes.c_int, vp, vp]),
+        "cg_assemble_stream": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]),
         "cg_solve_streamed": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, vp, vp, vp,
                                              ctypes.c_int64, vp, vp, ctypes.c_int, ctypes.c_double, vp, vp]),
+        "cg_cholesky": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_double, vp, ctypes.POINTER(ctypes.c_double)]),
+        "cg_cholesky_solve": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, vp]),
+        "cg_refine_streamed": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, vp, vp, vp,
+                                              ctypes.c_int64, vp, vp, ctypes.c_int, ctypes.c_double, vp, vp]),
+        "cg_predict_streamed": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
         "cg_fp64_fma_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
         "cg_md_serve_memory": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double)]),
@@ -149,6 +155,10 @@ def lib():
         fn.argtypes = args
     _lib = L
     return L
+
+
+ROWS_SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                             ctypes.c_int64)
 
 
 class MdRequest(ctypes.Structure):
@@ -457,6 +467,29 @@ class Session:
         _check(lib().cg_assemble(self._h, frames._h, int(precision), _ptr(out), out.shape[1]))
         return out
 
+    def assemble_stream(self, frames, precision, sink, block_frames=0):
+        """cg_assemble_stream: sink(first_row, A_block) is called with each row block
+        (a numpy view of pinned host memory, valid during the call); a truthy return
+        stops the assembly."""
+        ncols = self.model.ncols
+        dt = np.float64 if precision == CG_FP64 else np.float32
+        err = []
+
+        def cb(user, first, nrows, ptr, lda):
+            try:
+                buf = (ctypes.c_char * (int(nrows) * int(lda) * np.dtype(dt).itemsize)).from_address(ptr)
+                view = np.frombuffer(buf, dtype=dt).reshape(int(nrows), int(lda))[:, :ncols]
+                return 1 if sink(int(first), view) else 0
+            except Exception as e:   # noqa: BLE001  (reported after the call)
+                err.append(e)
+                return 1
+        cfn = ROWS_SINK(cb)
+        rc = lib().cg_assemble_stream(self._h, frames._h, int(precision), int(block_frames),
+                                      ctypes.cast(cfn, ctypes.c_void_p), None)
+        if err:
+            raise err[0]
+        _check(rc)
+
     def upload(self, frames):
         h = ctypes.c_void_p()
         _check(lib().cg_frames_upload(self._h, frames._h, ctypes.byref(h)))
@@ -539,6 +572,42 @@ class Session:
                                        ctypes.c_void_p(int(eb) or None), ctypes.c_void_p(int(ew) or None),
                                        int(max_iters), ctypes.c_double(tol), ctypes.c_void_p(int(x_ptr)), info))
         return {"iters": int(info[0]), "rel_update": info[1], "rnorm0": info[2], "rnorm": info[3], "ridge": info[4]}
+
+    @staticmethod
+    def _blocks(dframes, ptrs=None):
+        n = len(dframes)
+        b = (ctypes.c_void_p * max(n, 1))(*[d._h.value if isinstance(d._h, ctypes.c_void_p) else d._h
+                                            for d in dframes])
+        return b
+
+    def cholesky(self, g_ptr, ncols, ridge, l_ptr):
+        """cg_cholesky: L <- factor of G + r I; returns r."""
+        r = ctypes.c_double()
+        _check(lib().cg_cholesky(self._h, ctypes.c_void_p(int(g_ptr)), int(ncols), ctypes.c_double(ridge),
+                                 ctypes.c_void_p(int(l_ptr)), ctypes.byref(r)))
+        return r.value
+
+    def cholesky_solve(self, l_ptr, ncols, h_ptr, x_ptr):
+        _check(lib().cg_cholesky_solve(self._h, ctypes.c_void_p(int(l_ptr)), int(ncols), ctypes.c_void_p(int(h_ptr)),
+                                       ctypes.c_void_p(int(x_ptr))))
+
+    def refine_streamed(self, l_ptr, ncols, ridge, dframes, label_ptrs, x_ptr, max_iters=50, tol=1e-12):
+        """cg_refine_streamed from the x at x_ptr; returns dict(iters, rel_update, rnorm0, rnorm)."""
+        n = len(dframes)
+        blocks = self._blocks(dframes)
+        labels = (ctypes.c_void_p * max(n, 1))(*[int(p) for p in label_ptrs])
+        info = (ctypes.c_double * 4)()
+        _check(lib().cg_refine_streamed(self._h, ctypes.c_void_p(int(l_ptr)), int(ncols), ctypes.c_double(ridge), n,
+                                        ctypes.cast(blocks, ctypes.c_void_p), ctypes.cast(labels, ctypes.c_void_p),
+                                        None, None, ctypes.c_int64(0), None, None, int(max_iters),
+                                        ctypes.c_double(tol), ctypes.c_void_p(int(x_ptr)), info))
+        return {"iters": int(info[0]), "rel_update": info[1], "rnorm0": info[2], "rnorm": info[3]}
+
+    def predict_streamed(self, dframes, x_ptr, y_ptr):
+        """cg_predict_streamed: y = A x over the blocks' rows (device pointers)."""
+        blocks = self._blocks(dframes)
+        _check(lib().cg_predict_streamed(self._h, len(dframes), ctypes.cast(blocks, ctypes.c_void_p),
+                                         ctypes.c_void_p(int(x_ptr)), ctypes.c_void_p(int(y_ptr))))
 
     def fp64_fma_rate(self):
         """Measured FP64 FMA rate of the session's GPU (TFLOP/s)."""

@@ -303,27 +303,53 @@ int cg_assemble_device_noalloc(cg_session* s, const cg_dframes* d, int precision
     });
 }
 
+// Frames per block of a streamed assembly: about 1 GiB of A per block, at least one
+// frame, and at least two blocks when the batch has two frames (so copies overlap).
+static int auto_block_frames(const cg::FrameBatch& fb, int64_t lda, size_t rsz) {
+    if (fb.nframes <= 1) return 1;
+    const double bytes_per_frame = (double)fb.nrows / fb.nframes * (double)lda * (double)rsz;
+    int bf = (int)std::max(1.0, (double)(1u << 30) / std::max(1.0, bytes_per_frame));
+    return std::max(1, std::min(bf, (fb.nframes + 1) / 2));
+}
+
 int cg_assemble(cg_session* s, const cg_frames* fr, int precision, void* A, int64_t lda) {
     return guarded([&] {
         need(s && fr && A, "session/frames/A");
         need(precision == CG_FP64 || precision == CG_FP32, "precision");
         const size_t rsz = precision == CG_FP64 ? 8 : 4;
-        std::unique_ptr<cg::DeviceFrames> d = s->s->upload(fr->fb);
-        void* dA = nullptr;
-        const size_t bytes = (size_t)std::max<int64_t>(1, fr->fb.nrows) * lda * rsz;
-        cg::cuda_check(cudaMallocAsync(&dA, bytes, s->s->stream()), "cudaMallocAsync(A)");
-        try {
-            s->s->assemble(*d, precision, dA, lda, &s->last);
-            cg::cuda_check(cudaMemcpyAsync(A, dA, (size_t)fr->fb.nrows * lda * rsz, cudaMemcpyDeviceToHost,
-                                           s->s->stream()),
-                           "cudaMemcpyAsync(A)");
-            cg::cuda_check(cudaFreeAsync(dA, s->s->stream()), "cudaFreeAsync(A)");
-            cg::cuda_check(cudaStreamSynchronize(s->s->stream()), "cudaStreamSynchronize");
-        } catch (...) {
-            cudaFreeAsync(dA, s->s->stream());
-            cudaStreamSynchronize(s->s->stream());
-            throw;
+        char* base = static_cast<char*>(A);
+        s->s->assemble_to_host(
+            fr->fb, precision, auto_block_frames(fr->fb, lda, rsz), lda,
+            [&](int64_t first, int64_t) -> void* { return base + (size_t)first * lda * rsz; },
+            [](int64_t, int64_t, const void*) { return true; }, &s->last);
+    });
+}
+
+int cg_assemble_stream(cg_session* s, const cg_frames* fr, int precision, int block_frames, cg_rows_sink sink,
+                       void* user) {
+    return guarded([&] {
+        need(s && fr && sink, "session/frames/sink");
+        need(precision == CG_FP64 || precision == CG_FP32, "precision");
+        need(block_frames >= 0, "block_frames");
+        const size_t rsz = precision == CG_FP64 ? 8 : 4;
+        const int64_t lda = s->s->model().tot_all;
+        const int bf = block_frames > 0 ? block_frames : auto_block_frames(fr->fb, lda, rsz);
+        int64_t maxrows = 1;
+        for (int f0 = 0; f0 < fr->fb.nframes; f0 += bf) {
+            const int f1 = std::min(fr->fb.nframes, f0 + bf);
+            maxrows = std::max<int64_t>(maxrows, fr->fb.row_ofs[f1] - fr->fb.row_ofs[f0]);
         }
+        const size_t bytes = (size_t)maxrows * lda * rsz;
+        void* H[2] = {s->s->pinned(0, bytes), s->s->pinned(1, bytes)};
+        int next = 0, rc = 0;
+        s->s->assemble_to_host(
+            fr->fb, precision, bf, lda, [&](int64_t, int64_t) -> void* { return H[next++ % 2]; },
+            [&](int64_t first, int64_t nrows, const void* host) {
+                rc = sink(user, first, nrows, host, lda);
+                return rc == 0;
+            },
+            &s->last);
+        if (rc != 0) throw cg::Error(1, "the row sink stopped the assembly (returned " + std::to_string(rc) + ")");
     });
 }
 
@@ -396,6 +422,61 @@ int cg_solve_streamed(cg_session* s, const double* G, const double* h, int ncols
         }
         s->s->solve_streamed(G, h, ncols, ridge, bl, lb, wt, extra_A, extra_rows, extra_b, extra_w, max_iters, tol, x,
                              info);
+    });
+}
+
+static std::vector<const cg::DeviceFrames*> block_list(int nblocks, cg_dframes* const* blocks) {
+    need(nblocks == 0 || blocks, "blocks");
+    std::vector<const cg::DeviceFrames*> bl;
+    for (int k = 0; k < nblocks; ++k) {
+        need(blocks[k] != nullptr, "block entry");
+        bl.push_back(blocks[k]->d.get());
+    }
+    return bl;
+}
+
+int cg_cholesky(cg_session* s, const double* G, int ncols, double ridge, double* L, double* ridge_used) {
+    return guarded([&] {
+        need(s && G && L && ncols > 0, "cholesky arguments");
+        const double r = s->s->factor(G, ncols, ridge, L);
+        if (ridge_used) *ridge_used = r;
+    });
+}
+
+int cg_cholesky_solve(cg_session* s, const double* L, int ncols, const double* h, double* x) {
+    return guarded([&] {
+        need(s && L && h && x && ncols > 0, "cholesky_solve arguments");
+        s->s->factor_solve(L, ncols, h, x);
+    });
+}
+
+int cg_refine_streamed(cg_session* s, const double* L, int ncols, double ridge, int nblocks,
+                       cg_dframes* const* blocks, const double* const* labels, const double* const* weights,
+                       const double* extra_A, int64_t extra_rows, const double* extra_b, const double* extra_w,
+                       int max_iters, double tol, double* x, double* info) {
+    return guarded([&] {
+        need(s && L && x && ncols > 0 && nblocks >= 0 && max_iters >= 0 && tol >= 0.0, "refine arguments");
+        need(nblocks == 0 || labels, "labels");
+        need(extra_rows >= 0 && (extra_rows == 0 || (extra_A && extra_b)), "extra rows");
+        std::vector<const cg::DeviceFrames*> bl = block_list(nblocks, blocks);
+        std::vector<const double*> lb, wt;
+        for (int k = 0; k < nblocks; ++k) {
+            need(labels[k] != nullptr, "labels entry");
+            lb.push_back(labels[k]);
+            if (weights) {
+                need(weights[k] != nullptr, "weights entry");
+                wt.push_back(weights[k]);
+            }
+        }
+        s->s->refine_streamed(L, ncols, ridge, bl, lb, wt, extra_A, extra_rows, extra_b, extra_w, max_iters, tol, x,
+                              info);
+    });
+}
+
+int cg_predict_streamed(cg_session* s, int nblocks, cg_dframes* const* blocks, const double* x, double* y) {
+    return guarded([&] {
+        need(s && x && y && nblocks >= 0, "predict arguments");
+        s->s->predict_streamed(block_list(nblocks, blocks), x, y);
     });
 }
 

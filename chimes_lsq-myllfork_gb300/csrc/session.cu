@@ -374,6 +374,8 @@ Session::~Session() {
     dm_.reset();
     if (side_event_) cudaEventDestroy(side_event_);
     if (side_stream_) cudaStreamDestroy(side_stream_);
+    if (copy_stream_) cudaStreamDestroy(copy_stream_);
+    for (void* p : pinned_) if (p) cudaFreeHost(p);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -454,6 +456,94 @@ void Session::assemble(const DeviceFrames& df, int precision, void* A, int64_t l
     CK(cudaSetDevice(device_));
     Scratch S(stream_);
     run(df, precision, A, lda, stats, S, nullptr, nullptr);
+}
+
+void* Session::pinned(int i, size_t bytes) {
+    if (i < 0 || i > 1) throw Error(1, "pinned staging index");
+    if (pinned_bytes_[i] < bytes) {
+        if (pinned_[i]) CK(cudaFreeHost(pinned_[i]));
+        pinned_[i] = nullptr;
+        pinned_bytes_[i] = 0;
+        CK(cudaMallocHost(&pinned_[i], bytes));
+        pinned_bytes_[i] = bytes;
+    }
+    return pinned_[i];
+}
+
+int64_t Session::assemble_to_host(const FrameBatch& fb, int precision, int block_frames, int64_t ldh,
+                                  const std::function<void*(int64_t, int64_t)>& dest,
+                                  const std::function<bool(int64_t, int64_t, const void*)>& done,
+                                  AssembleStats* stats) {
+    CK(cudaSetDevice(device_));
+    const int nf = fb.nframes;
+    if (nf == 0) return 0;
+    const int bf = std::max(1, std::min(block_frames, nf));
+    const int nblk = (nf + bf - 1) / bf;
+    const size_t rsz = precision == 0 ? sizeof(double) : sizeof(float);
+    if (ldh < model_.tot_all) throw Error(1, "host lda smaller than the number of A columns");
+    if (!copy_stream_) CK(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+    // every block's frames on the device first (positions and boxes are small)
+    std::vector<std::unique_ptr<DeviceFrames>> dev(nblk);
+    int64_t maxrows = 1;
+    for (int k = 0; k < nblk; ++k) {
+        dev[k] = upload(slice_batch(fb, k * bf, std::min(bf, nf - k * bf)));
+        maxrows = std::max<int64_t>(maxrows, dev[k]->nrows);
+    }
+    struct Res {
+        void* dA[2] = {nullptr, nullptr};
+        cudaEvent_t asm_done[2] = {nullptr, nullptr}, copy_done[2] = {nullptr, nullptr};
+        ~Res() {
+            for (int i = 0; i < 2; ++i) {
+                if (dA[i]) cudaFree(dA[i]);
+                if (asm_done[i]) cudaEventDestroy(asm_done[i]);
+                if (copy_done[i]) cudaEventDestroy(copy_done[i]);
+            }
+        }
+    } R;
+    const int64_t lda = model_.tot_all;
+    for (int i = 0; i < 2 && i < nblk; ++i) CK(cudaMalloc(&R.dA[i], (size_t)maxrows * lda * rsz));
+    for (int i = 0; i < 2; ++i) {
+        CK(cudaEventCreateWithFlags(&R.asm_done[i], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&R.copy_done[i], cudaEventDisableTiming));
+    }
+    std::vector<int64_t> first(nblk + 1, 0);
+    for (int k = 0; k < nblk; ++k) first[k + 1] = first[k] + dev[k]->nrows;
+    std::vector<void*> hdst(nblk, nullptr);
+    AssembleStats total, one;
+    auto finish = [&](int k) {   // block k's copy has been issued: wait for it, hand it over
+        CK(cudaEventSynchronize(R.copy_done[k % 2]));
+        return done(first[k], dev[k]->nrows, hdst[k]);
+    };
+    bool go = true;
+    for (int k = 0; k < nblk && go; ++k) {
+        const int b = k % 2;
+        if (k >= 2) CK(cudaStreamWaitEvent(stream_, R.copy_done[b], 0));   // buffer b is free again
+        assemble(*dev[k], precision, R.dA[b], lda, stats ? &one : nullptr);
+        if (stats) {
+            total.pairs2 += one.pairs2; total.list3 += one.list3; total.list4 += one.list4;
+            total.triplets += one.triplets; total.quads += one.quads;
+            total.power_evals3 += one.power_evals3; total.power_evals4 += one.power_evals4;
+            total.launches += one.launches;
+        }
+        CK(cudaEventRecord(R.asm_done[b], stream_));
+        CK(cudaStreamWaitEvent(copy_stream_, R.asm_done[b], 0));
+        hdst[k] = dest(first[k], dev[k]->nrows);
+        if (!hdst[k]) throw Error(1, "no host destination for a row block");
+        if (ldh == lda) {
+            CK(cudaMemcpyAsync(hdst[k], R.dA[b], (size_t)dev[k]->nrows * lda * rsz, cudaMemcpyDeviceToHost,
+                               copy_stream_));
+        } else {
+            CK(cudaMemcpy2DAsync(hdst[k], (size_t)ldh * rsz, R.dA[b], (size_t)lda * rsz, (size_t)lda * rsz,
+                                 (size_t)dev[k]->nrows, cudaMemcpyDeviceToHost, copy_stream_));
+        }
+        CK(cudaEventRecord(R.copy_done[b], copy_stream_));
+        if (k >= 1) go = finish(k - 1);
+    }
+    if (go) finish(nblk - 1);
+    CK(cudaStreamSynchronize(copy_stream_));
+    CK(cudaStreamSynchronize(stream_));
+    if (stats) *stats = total;
+    return first[nblk];
 }
 
 void Session::assemble_noalloc(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats) {
@@ -783,51 +873,120 @@ double Session::fp64_fma_tflops() {
     }
 }
 
+double Session::factor(const double* G, int ncols, double ridge, double* L) {
+    CK(cudaSetDevice(device_));
+    Scratch S(stream_);
+    int* d_info = S.get<int>(1);
+    try {
+        const double used = factor_ridge(G, ncols, ridge, L, d_info, stream_);
+        if (used < 0.0) throw Error(2, "the normal-equations matrix is not positive definite even with a ridge");
+        return used;
+    } catch (const std::runtime_error& e) {
+        if (dynamic_cast<const Error*>(&e)) throw;
+        throw Error(3, e.what());
+    }
+}
+
+void Session::factor_solve(const double* L, int ncols, const double* h, double* x) {
+    CK(cudaSetDevice(device_));
+    try {
+        cholesky_solve64(L, ncols, h, x, stream_);
+        CK(cudaStreamSynchronize(stream_));
+    } catch (const std::runtime_error& e) {
+        if (dynamic_cast<const Error*>(&e)) throw;
+        throw Error(3, e.what());
+    }
+}
+
+namespace {
+// One pass over every row block: FP64 assembly into Ablk, t = (b -) A v (t *= w^2),
+// then out += A^T t, or (predict) t copied to y at the block's rows.
+struct StreamRows {
+    Session& se;
+    int ncols;
+    const std::vector<const DeviceFrames*>& blocks;
+    const std::vector<const double*>& labels;
+    const std::vector<const double*>& weights;
+    const double *extra_A, *extra_b, *extra_w;
+    int64_t extra_rows;
+    double *Ablk, *t, *partial;
+    void pass(const double* v, bool resid, double* out, cudaStream_t st) {
+        CK(cudaMemsetAsync(out, 0, sizeof(double) * ncols, st));
+        for (size_t k = 0; k < blocks.size(); ++k) {
+            const DeviceFrames& d = *blocks[k];
+            if (d.nrows == 0) continue;
+            se.assemble(d, 0, Ablk, ncols, nullptr);
+            gemv_rows64(Ablk, ncols, d.nrows, ncols, v, resid ? labels[k] : nullptr,
+                        weights.empty() ? nullptr : weights[k], t, st);
+            gemv_cols64(Ablk, ncols, d.nrows, ncols, t, out, partial, st);
+        }
+        if (extra_rows > 0) {
+            gemv_rows64(extra_A, ncols, extra_rows, ncols, v, resid ? extra_b : nullptr, extra_w, t, st);
+            gemv_cols64(extra_A, ncols, extra_rows, ncols, t, out, partial, st);
+        }
+    }
+};
+}  // namespace
+
+void Session::refine_streamed(const double* L, int ncols, double ridge, const std::vector<const DeviceFrames*>& blocks,
+                              const std::vector<const double*>& labels, const std::vector<const double*>& weights,
+                              const double* extra_A, int64_t extra_rows, const double* extra_b, const double* extra_w,
+                              int max_iters, double tol, double* x, double* info) {
+    CK(cudaSetDevice(device_));
+    if (blocks.size() != labels.size() || (!weights.empty() && weights.size() != blocks.size()))
+        throw Error(1, "blocks, labels and weights differ in number");
+    if (ncols != model_.tot_all) throw Error(1, "ncols is not the model's column count");
+    Scratch S(stream_);
+    int64_t maxrows = std::max<int64_t>(1, extra_rows);
+    for (const DeviceFrames* d : blocks) maxrows = std::max<int64_t>(maxrows, d->nrows);
+    StreamRows R{*this, ncols, blocks, labels, weights, extra_A, extra_b, extra_w, extra_rows,
+                 S.get<double>((size_t)maxrows * ncols), S.get<double>(maxrows),
+                 S.get<double>(atb_partial_doubles(maxrows, ncols))};
+    try {
+        Fp64Operator op;
+        op.apply = [&](const double* p, double* q) { R.pass(p, false, q, stream_); };
+        op.residual = [&](const double* xv, double* r) { R.pass(xv, true, r, stream_); };
+        const PcgStats ps = pcg_ridge(L, ncols, ridge, op, x, max_iters, tol, stream_);
+        CK(cudaStreamSynchronize(stream_));
+        if (info) { info[0] = ps.iters; info[1] = ps.rel_update; info[2] = ps.rnorm0; info[3] = ps.rnorm; }
+    } catch (const std::runtime_error& e) {
+        if (dynamic_cast<const Error*>(&e)) throw;
+        throw Error(3, e.what());
+    }
+}
+
 void Session::solve_streamed(const double* G, const double* h, int ncols, double ridge,
                              const std::vector<const DeviceFrames*>& blocks, const std::vector<const double*>& labels,
                              const std::vector<const double*>& weights, const double* extra_A, int64_t extra_rows,
                              const double* extra_b, const double* extra_w, int max_iters, double tol, double* x,
                              double* info) {
     CK(cudaSetDevice(device_));
-    if (blocks.size() != labels.size() || (!weights.empty() && weights.size() != blocks.size()))
-        throw Error(1, "blocks, labels and weights differ in number");
-    if (ncols != model_.tot_all) throw Error(1, "ncols is not the model's column count");
     Scratch S(stream_);
     double* L = S.get<double>((size_t)ncols * ncols);
-    int* d_info = S.get<int>(1);
-    int64_t maxrows = std::max<int64_t>(1, extra_rows);
+    const double used = factor(G, ncols, ridge, L);
+    factor_solve(L, ncols, h, x);
+    double in[4] = {0, 0, 0, 0};
+    refine_streamed(L, ncols, ridge, blocks, labels, weights, extra_A, extra_rows, extra_b, extra_w, max_iters, tol, x,
+                    in);
+    if (info) { for (int k = 0; k < 4; ++k) info[k] = in[k]; info[4] = used; }
+}
+
+void Session::predict_streamed(const std::vector<const DeviceFrames*>& blocks, const double* x, double* y) {
+    CK(cudaSetDevice(device_));
+    const int ncols = model_.tot_all;
+    Scratch S(stream_);
+    int64_t maxrows = 1;
     for (const DeviceFrames* d : blocks) maxrows = std::max<int64_t>(maxrows, d->nrows);
-    double* Ablk = S.get<double>((size_t)maxrows * ncols);   // one FP64 row block at a time
-    double* t = S.get<double>(maxrows);
-    double* partial = S.get<double>(atb_partial_doubles(maxrows, ncols));
+    double* Ablk = S.get<double>((size_t)maxrows * ncols);
     try {
-        const double used = factor_ridge(G, ncols, ridge, L, d_info, stream_);
-        if (used < 0.0) throw Error(2, "the normal-equations matrix is not positive definite even with a ridge");
-        cholesky_solve64(L, ncols, h, x, stream_);
-        // one pass over every row block: FP64 assembly, t = (b -) A v, (t *= w^2), out += A^T t
-        auto pass = [&](const double* v, bool resid, double* out) {
-            CK(cudaMemsetAsync(out, 0, sizeof(double) * ncols, stream_));
-            for (size_t k = 0; k < blocks.size(); ++k) {
-                const DeviceFrames& d = *blocks[k];
-                if (d.nrows == 0) continue;
-                assemble(d, 0, Ablk, ncols, nullptr);
-                gemv_rows64(Ablk, ncols, d.nrows, ncols, v, resid ? labels[k] : nullptr,
-                            weights.empty() ? nullptr : weights[k], t, stream_);
-                gemv_cols64(Ablk, ncols, d.nrows, ncols, t, out, partial, stream_);
-            }
-            if (extra_rows > 0) {
-                gemv_rows64(extra_A, ncols, extra_rows, ncols, v, resid ? extra_b : nullptr, extra_w, t, stream_);
-                gemv_cols64(extra_A, ncols, extra_rows, ncols, t, out, partial, stream_);
-            }
-        };
-        Fp64Operator op;
-        op.apply = [&](const double* p, double* q) { pass(p, false, q); };
-        op.residual = [&](const double* xv, double* r) { pass(xv, true, r); };
-        const PcgStats ps = pcg_ridge(L, ncols, ridge, op, x, max_iters, tol, stream_);
-        CK(cudaStreamSynchronize(stream_));
-        if (info) {
-            info[0] = ps.iters; info[1] = ps.rel_update; info[2] = ps.rnorm0; info[3] = ps.rnorm; info[4] = used;
+        int64_t r0 = 0;
+        for (const DeviceFrames* d : blocks) {
+            if (d->nrows == 0) continue;
+            assemble(*d, 0, Ablk, ncols, nullptr);
+            gemv_rows64(Ablk, ncols, d->nrows, ncols, x, nullptr, nullptr, y + r0, stream_);
+            r0 += d->nrows;
         }
+        CK(cudaStreamSynchronize(stream_));
     } catch (const std::runtime_error& e) {
         if (dynamic_cast<const Error*>(&e)) throw;
         throw Error(3, e.what());

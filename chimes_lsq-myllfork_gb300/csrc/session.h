@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -191,6 +192,18 @@ class Session {
     std::unique_ptr<DeviceFrames> upload(const FrameBatch& fb);
     // A (device pointer, row-major, lda >= tot_all) receives the batch's rows.
     void assemble(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats);
+    // A host batch assembled in blocks of block_frames frames into host memory: block
+    // k is assembled on the session stream while block k-1 is copied to the host on
+    // a copy stream.  dest(first_row, nrows) names the host destination of a block
+    // (row-major, lda = ldh); done(first_row, nrows, host) is called once its copy has
+    // landed (before the destination of block k+1 is reused) and may return false
+    // to stop.  Returns the rows assembled.
+    int64_t assemble_to_host(const FrameBatch& fb, int precision, int block_frames, int64_t ldh,
+                             const std::function<void*(int64_t, int64_t)>& dest,
+                             const std::function<bool(int64_t, int64_t, const void*)>& done, AssembleStats* stats);
+    // Pinned host staging buffer i (0 or 1) of at least `bytes`, kept and grown across
+    // calls (streamed assemblies), freed with the session.
+    void* pinned(int i, size_t bytes);
     // Same pipeline with every per-call device buffer taken from a fixed static
     // device array (no cudaMalloc / cudaMallocAsync / cudaFree in the call).
     void assemble_noalloc(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats);
@@ -216,6 +229,18 @@ class Session {
                         const std::vector<const double*>& weights, const double* extra_A, int64_t extra_rows,
                         const double* extra_b, const double* extra_w, int max_iters, double tol, double* x,
                         double* info);
+    // Its pieces: L = FP64 Cholesky factor of G + r I (returns r; L: ncols^2 device
+    // doubles), x = (L L^T)^-1 h, and the CG passes from a given x (info: iterations,
+    // last relative update, initial and final residual norm).
+    double factor(const double* G, int ncols, double ridge, double* L);
+    void factor_solve(const double* L, int ncols, const double* h, double* x);
+    void refine_streamed(const double* L, int ncols, double ridge, const std::vector<const DeviceFrames*>& blocks,
+                         const std::vector<const double*>& labels, const std::vector<const double*>& weights,
+                         const double* extra_A, int64_t extra_rows, const double* extra_b, const double* extra_w,
+                         int max_iters, double tol, double* x, double* info);
+    // y = A x for every row of the blocks (in block order), from FP64 rows assembled
+    // block by block (chimes_lsq.py's force.txt without a stored A).
+    void predict_streamed(const std::vector<const DeviceFrames*>& blocks, const double* x, double* y);
     // Sizing pass of a batch (a full assembly into A) recording its list sizes.
     RunPlan plan(const DeviceFrames& df, int precision, void* A, int64_t lda);
     // Capture the assembly of every block into Abuf (lda) and the split-BF16 Gram
@@ -316,6 +341,9 @@ class Session {
     int device_;
     cudaStream_t stream_ = nullptr;
     cudaStream_t side_stream_ = nullptr;   // look-ahead MD list builds
+    cudaStream_t copy_stream_ = nullptr;   // device-to-host copies of streamed assemblies
+    void* pinned_[2] = {nullptr, nullptr};
+    size_t pinned_bytes_[2] = {0, 0};
     cudaEvent_t side_event_ = nullptr;
     std::unique_ptr<DeviceModel> dm_;
     std::unique_ptr<MdTables> md_;

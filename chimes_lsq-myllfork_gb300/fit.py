@@ -89,15 +89,14 @@ def main(argv=None):
     wp = (lambda r: w_all[r:].data_ptr()) if w_all is not None else (lambda r: 0)
     wcol = (lambda r, n: w_all[r:r + n, None]) if w_all is not None else (lambda r, n: 1.0)
     colsum = torch.zeros(C, dtype=torch.float64, device="cuda")   # A^T 1 (DLARS --normalize)
-    dfrs, lab_ptrs, w_ptrs = [], [], []   # the mixed form's blocks, kept for the FP64 refinement
+    dfrs, lab_ptrs, w_ptrs = [], [], []   # the blocks on the device (FP64 refinement, force.txt)
     r0 = 0
     for blk in blocks:
         dfr = sess.upload(blk)
         n = blk.nrows
-        if mixed:
-            dfrs.append(dfr)
-            lab_ptrs.append(b_all[r0:].data_ptr())
-            w_ptrs.append(w_all[r0:].data_ptr() if w_all is not None else 0)
+        dfrs.append(dfr)
+        lab_ptrs.append(b_all[r0:].data_ptr())
+        w_ptrs.append(w_all[r0:].data_ptr() if w_all is not None else 0)
         b_all[r0:r0 + n] = torch.from_numpy(blk.labels())
         if mixed:
             A32 = torch.empty((n, C), dtype=torch.float32, device="cuda")
@@ -160,16 +159,10 @@ def main(argv=None):
     # predicted labels y = A x (force.txt) and the fit statistics
     if keep64:
         y = (A64_all @ x).cpu().numpy()
-    else:
-        ys = []
-        for blk in blocks:
-            dfr = sess.upload(blk)
-            A = torch.empty((blk.nrows, C), dtype=torch.float64, device="cuda")
-            sess.assemble_device(dfr, cg.CG_FP64, A.data_ptr(), C)
-            ys.append((A @ x).cpu().numpy())
-            del A
-        ys.append(Acon @ xh)
-        y = np.concatenate(ys)
+    else:   # FP64 rows assembled block by block (no stored A)
+        yd = torch.empty(max(nfr_rows, 1), dtype=torch.float64, device="cuda")
+        sess.predict_streamed(dfrs, x.data_ptr(), yd.data_ptr())
+        y = np.concatenate([yd[:nfr_rows].cpu().numpy(), Acon @ xh])
     b = b_all.cpu().numpy()
     if args.normalize and args.algorithm in ("dlars", "dlasso"):   # print_unshifted_mu: the centring comes back
         y = y - float((colsum @ x).item()) / nrows + float(b.sum()) / nrows

@@ -131,10 +131,26 @@ void* cg_session_stream(cg_session* s);
 
 /* Assemble the full A matrix of the frames into HOST memory A (row-major,
  * nrows x lda, lda >= ntotal) in CG_FP64 (double) or CG_FP32 (float).  Host->device
- * copies of the coordinates and the device->host copy of A happen inside.
+ * copies of the coordinates and the device->host copies of A happen inside: the
+ * frames are assembled in blocks, each block's copy overlapping the next block's
+ * assembly (pinned host memory lets the copies run asynchronously).
  * Replaces the per-frame loop process_frame -> ZCalc_Deriv -> Deriv_2B/3B/4B
  * (src/chimes_lsq.C:292-328, 718-823; src/functions.C:755-804; src/Cheby.C:709-1729). */
 int cg_assemble(cg_session* s, const cg_frames* fr, int precision, void* A, int64_t lda);
+
+/* Streamed assembly into host memory without a host buffer for the whole A: the
+ * frames are assembled in blocks of block_frames frames (0: about 1 GiB of A per
+ * block), block k on the GPU while block k-1 is copied to pinned host memory, and
+ * sink(user, first_row, nrows, A_block, lda) is called on the calling thread with each
+ * block in row order (A_block: nrows x lda values of the requested precision, valid
+ * until the sink returns; lda = the model's column count).  A non-zero return from
+ * the sink stops the assembly (status 1).  cg_assemble uses the same pipeline with
+ * the caller's buffer as the destination.  This is the shape of chimes_lsq's frame
+ * loop that prints A.txt as it goes (src/chimes_lsq.C:292-328, A_MAT::PRINT_FRAME
+ * src/A_Matrix.C:210-567), for A matrices larger than host memory. */
+typedef int (*cg_rows_sink)(void* user, int64_t first_row, int64_t nrows, const void* A_block, int64_t lda);
+int cg_assemble_stream(cg_session* s, const cg_frames* fr, int precision, int block_frames, cg_rows_sink sink,
+                       void* user);
 
 /* Device-resident variant: upload the frames once, then assemble into a DEVICE
  * buffer A.  cg_assemble_device is asynchronous on the session stream. */
@@ -210,6 +226,25 @@ int cg_solve_streamed(cg_session* s, const double* G, const double* h, int ncols
                       cg_dframes* const* blocks, const double* const* labels, const double* const* weights,
                       const double* extra_A, int64_t extra_rows, const double* extra_b, const double* extra_w,
                       int max_iters, double tol, double* x, double* info);
+
+/* The pieces of cg_solve_streamed, for callers that keep the factor: cg_cholesky
+ * writes the FP64 Cholesky factor of G + r I into L (device, ncols * ncols doubles;
+ * its column-major lower triangle; r = ridge grown as in cg_solve, returned in
+ * *ridge_used, which may be NULL); cg_cholesky_solve: x = (L L^T)^-1 h;
+ * cg_refine_streamed: the conjugate-gradient passes of cg_solve_streamed from the
+ * caller's x (device, updated in place), preconditioned by L; info (4 doubles, may
+ * be NULL): passes, last relative update, initial and final residual norm. */
+int cg_cholesky(cg_session* s, const double* G, int ncols, double ridge, double* L, double* ridge_used);
+int cg_cholesky_solve(cg_session* s, const double* L, int ncols, const double* h, double* x);
+int cg_refine_streamed(cg_session* s, const double* L, int ncols, double ridge, int nblocks,
+                       cg_dframes* const* blocks, const double* const* labels, const double* const* weights,
+                       const double* extra_A, int64_t extra_rows, const double* extra_b, const double* extra_w,
+                       int max_iters, double tol, double* x, double* info);
+
+/* Predicted labels y = A x (device, one value per row of the blocks in order) from
+ * FP64 rows assembled block by block: force.txt of chimes_lsq.py
+ * (src/chimes_lsq.py:284-296) without a stored A. */
+int cg_predict_streamed(cg_session* s, int nblocks, cg_dframes* const* blocks, const double* x, double* y);
 
 /* FP64 fused multiply-add rate of the session's GPU in TFLOP/s (2 flops per FMA),
  * measured by a kernel of independent FMA chains on every SM (no counterpart in the

@@ -1,9 +1,12 @@
 """Small, fixed workloads for profiling single kernels under ncu.
 
-    python chimes_lsq-myllfork_gb300/profile_cases.py gram [nframes]        # split-BF16 Gram of water-3b A
-    python chimes_lsq-myllfork_gb300/profile_cases.py md NATOMS PRECISION   # MD force of one 4-body system
-    python chimes_lsq-myllfork_gb300/profile_cases.py assemble [nframes] [fp32]  # A of water-3b frames
-    python chimes_lsq-myllfork_gb300/profile_cases.py serve NATOMS PRECISION NSTEPS  # one NVE request, stage times
+    python profile_cases.py gram [nframes]        # split-BF16 Gram of water-3b A
+    python profile_cases.py md NATOMS PRECISION   # MD force of one 4-body system
+    python profile_cases.py assemble [nframes] [fp32]  # A of water-3b frames
+    python profile_cases.py assemble4b [nframes] [fp32]  # A of 256-atom C/H/N/O 4-body frames
+    python profile_cases.py gram4b [rows]         # split-BF16 Gram of a 4-body FP32 A (51,209 columns)
+    python profile_cases.py syrk [rows] [cols]    # FP64 SYRK Gram of a random A
+    python profile_cases.py serve NATOMS PRECISION NSTEPS  # one NVE request, stage times
 
 Each case runs its launch twice after the set-up, so `ncu -k regex:<kernel> -c 1`
 captures a warm launch; the synthetic inputs are seeded.
@@ -14,7 +17,7 @@ import sys
 import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, HERE)
 
 
 def main(argv):
@@ -46,6 +49,47 @@ def main(argv):
                 sess.gram(1, A.data_ptr(), ncols, nrows, ncols, b.data_ptr(), 1, G.data_ptr(), h.data_ptr())
         torch.cuda.synchronize()
         print("ok", case, nrows, ncols)
+        return
+    if case in ("assemble4b", "gram4b"):
+        nframes = int(argv[1]) if len(argv) > 1 and case == "assemble4b" else 4
+        fm = synth.make_workload("chno-4b", tmp, nframes=nframes, seed=2024, labels=case == "gram4b")
+        model = cg.Model(fm)
+        fr = cg.Frames.read(model)
+        sess = cg.Session(model, 0)
+        nrows, _ = fr.rows()
+        ncols = model.ncols
+        dfr = sess.upload(fr)
+        fp32 = case == "gram4b" or (len(argv) > 2 and argv[2] == "fp32")
+        prec = cg.CG_FP32 if fp32 else cg.CG_FP64
+        A = torch.empty((nrows, ncols), dtype=torch.float32 if fp32 else torch.float64, device="cuda")
+        for _ in range(1 if case == "gram4b" else 2):
+            sess.assemble_device(dfr, prec, A.data_ptr(), ncols)
+        if case == "gram4b":   # rows: repeat the frames' rows up to the requested K
+            rows = int(argv[1]) if len(argv) > 1 else 8192
+            reps = (rows + nrows - 1) // nrows
+            Ar = A.repeat(reps, 1)[:rows].contiguous()
+            b = torch.from_numpy(np.tile(fr.labels(), reps)[:rows].copy()).cuda()
+            G = torch.zeros((ncols, ncols), dtype=torch.float64, device="cuda")
+            h = torch.zeros(ncols, dtype=torch.float64, device="cuda")
+            for _ in range(2):
+                sess.gram(1, Ar.data_ptr(), ncols, rows, ncols, b.data_ptr(), 1, G.data_ptr(), h.data_ptr())
+        torch.cuda.synchronize()
+        print("ok", case, nrows, ncols)
+        return
+    if case == "syrk":
+        rows = int(argv[1]) if len(argv) > 1 else 8192
+        cols = int(argv[2]) if len(argv) > 2 else 8192
+        fm = synth.make_workload("water-2b", tmp, nframes=1, seed=3)
+        sess = cg.Session(cg.Model(fm), 0)
+        A = torch.randn(rows, cols, dtype=torch.float64, device="cuda")
+        b = torch.randn(rows, dtype=torch.float64, device="cuda")
+        G = torch.zeros((cols, cols), dtype=torch.float64, device="cuda")
+        h = torch.zeros(cols, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for _ in range(2):
+            sess.gram(0, A.data_ptr(), cols, rows, cols, b.data_ptr(), 0, G.data_ptr(), h.data_ptr())
+        torch.cuda.synchronize()
+        print("ok", case, rows, cols)
         return
     n = int(argv[1]) if len(argv) > 1 else 1024
     prec = int(argv[2]) if len(argv) > 2 else 0

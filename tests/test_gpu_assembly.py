@@ -127,3 +127,28 @@ def test_arrays_path_equals_text_path(cg, session_for):
     fa = cg.Frames.from_arrays(model, nat, typ, xyz, cell, frc, st, en)
     ft = cg.Frames.read(model)
     assert np.array_equal(sess.assemble(fa), sess.assemble(ft))
+
+
+def test_streamed_host_assembly_equals_device_assembly(cg, session_for, tmp_path_factory):
+    """cg_assemble_stream (row blocks to pinned host memory while the next block
+    assembles) and cg_assemble (the same pipeline into the caller's buffer) give the
+    device assembly's A bit for bit; a sink that asks to stop ends the call with
+    status 1."""
+    torch = pytest.importorskip("torch")
+    fm = _workload(tmp_path_factory, cg, "water-3b", 7, 505)
+    model, sess = session_for(fm)
+    frames = cg.Frames.read(model)
+    dfr = sess.upload(frames)
+    dA = torch.empty((frames.nrows, model.ncols), dtype=torch.float64, device="cuda")
+    sess.assemble_device(dfr, cg.CG_FP64, dA.data_ptr(), model.ncols)
+    torch.cuda.synchronize()
+    R = dA.cpu().numpy()
+    got = []
+    sess.assemble_stream(frames, cg.CG_FP64, lambda first, blk: got.append((first, blk.copy())) and False,
+                         block_frames=2)
+    assert [g[0] for g in got] == sorted(g[0] for g in got) and len(got) == 4
+    assert np.array_equal(np.concatenate([g[1] for g in got]), R)
+    assert np.array_equal(sess.assemble(frames, cg.CG_FP64), R)
+    with pytest.raises(cg.ChimesError) as e:
+        sess.assemble_stream(frames, cg.CG_FP64, lambda first, blk: True, block_frames=3)
+    assert e.value.code == 1
