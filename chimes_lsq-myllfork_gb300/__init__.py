@@ -67,6 +67,7 @@ def lib():
         "cg_model_charge_columns": (ctypes.c_int, [vp, ip, ip]),
         "cg_model_constraint_rows": (ctypes.c_int, [vp, dp, ctypes.c_int64, dp]),
         "cg_model_sizes": (ctypes.c_int, [vp, ip, ip]),
+        "cg_model_row_layout": (ctypes.c_int, [vp, ip, ip]),
         "cg_model_header_text": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "cg_model_map_text": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "cg_model_params_text": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t,

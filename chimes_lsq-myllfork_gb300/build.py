@@ -80,7 +80,26 @@ def build(verbose=False, force=False):
                     print(out)
     if force or jobs or not os.path.exists(LIB):
         _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"])
+    build_native_checks(force)
     return LIB
+
+
+def build_native_checks(force=False):
+    """The test programs that call the library through include/ alone: a C caller of
+    chimes_gb300.h and a C++ caller of the ZCalc / ZCalc_Deriv drop-ins
+    (tests/native/*), linked against the in-tree library."""
+    root = os.path.dirname(HERE)
+    inc = os.path.join(root, "include")
+    src = os.path.join(root, "tests", "native")
+    for name, comp, extra in (("capi_check.c", "gcc", ["-std=c11"]), ("zcalc_check.cpp", "g++", ["-std=c++17"])):
+        s = os.path.join(src, name)
+        if not os.path.exists(s):
+            continue
+        out = os.path.join(OUT, os.path.splitext(name)[0])
+        deps = [s, LIB] + [os.path.join(inc, f) for f in os.listdir(inc)]
+        if force or _stale(out, deps):
+            _run([comp, "-O2"] + extra + ["-I" + inc, s, "-o", out, "-L" + OUT, "-lchimes_gb300",
+                                          "-Wl,-rpath," + OUT])
 
 
 if __name__ == "__main__":

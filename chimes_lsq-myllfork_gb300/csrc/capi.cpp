@@ -100,6 +100,15 @@ int cg_model_constraint_rows(const cg_model* h, double* A, int64_t lda, double* 
     });
 }
 
+int cg_model_row_layout(const cg_model* h, int* stress_rows, int* energy_rows) {
+    return guarded([&] {
+        need(h, "model");
+        const cg::Controls& c = h->m.ctl;
+        if (stress_rows) *stress_rows = c.fit_stress_all ? 9 : (c.fit_stress ? 3 : 0);
+        if (energy_rows) *energy_rows = c.fit_ener ? 3 : 0;
+    });
+}
+
 int cg_model_sizes(const cg_model* h, int* nframes, int* natmtyp) {
     return guarded([&] {
         need(h, "model");

@@ -47,6 +47,12 @@ int cg_model_charge_columns(const cg_model* m, int* ncoul, int* nconstraints);
  * (row-major, lda >= total columns) and their b values. */
 int cg_model_constraint_rows(const cg_model* m, double* A, int64_t lda, double* b);
 
+/* Rows a frame contributes after its 3 * natoms force rows, for frames below
+ * NSTRESS / NENER: stress rows (0, 3 with FITSTRS true / FIRST: xx yy zz, 9 with ALL /
+ * FIRSTALL: xx xy xz xy yy yz xz yz zz) and energy rows (0, or 3 identical rows with
+ * FITENER) -- the row layout of A_MAT::PRINT_FRAME (src/A_Matrix.C:309-553). */
+int cg_model_row_layout(const cg_model* m, int* stress_rows, int* energy_rows);
+
 /* Number of frames (NFRAMES) and atom types (NATMTYP) of the model. */
 int cg_model_sizes(const cg_model* m, int* nframes, int* natmtyp);
 

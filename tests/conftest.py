@@ -35,7 +35,8 @@ def fixture_dir(name):
     return os.path.join(GOLDEN, name)
 
 
-FIXTURES = ["water2b", "water3b", "ch4b", "small4b", "watercoul", "multifile", "skipframes", "hierarc"]
+FIXTURES = ["water2b", "water3b", "ch4b", "small4b", "watercoul", "multifile", "skipframes", "hierarc", "tersoff",
+            "invr", "notrans", "specific", "exclude", "chebyfix_zero", "chebyfix_const", "chebyfix_smooth"]
 
 
 def frame_part(model, ref):

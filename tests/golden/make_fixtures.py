@@ -21,7 +21,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
 REF = os.path.join(ROOT, "oracle", "_ref", "chimes_lsq")
-REF_PY = "/root/reference/src/chimes_lsq.py"   # the reference's solver script (read in place)
+REF_DIR = os.environ.get("CHIMES_REF_DIR", "/root/reference")
+REF_PY = os.path.join(REF_DIR, "src", "chimes_lsq.py")   # the reference's solver script (read in place)
 
 # name -> (workload, overrides, nframes, seed)
 FIXTURES = {
@@ -44,6 +45,48 @@ FIXTURES = {
     "skipframes": ("water-3b", dict(nmol=24, L=8.96, order=(8, 4, 0), fitstrs="FIRSTALL 3", fitener=True), 5, 18),
     # HIERARC: the O-H 2-body block and the H energy offset left out of A
     "hierarc": ("water-3b", dict(nmol=24, L=8.96, order=(8, 4, 0), fitstrs="ALL", fitener=True), 2, 19),
+}
+
+# The input branches of the remaining fm_setup.in options, each a C/H 4-body system
+# (or water for the inverse-r transform) with one option changed; the cut-off
+# blocks use the reference's syntax (src/input.C:690-874, 1207-1282, src/Fcut.C:40-65).
+CH4B = dict(order=(6, 3, 2), triclinic=False, density=0.1, species2=True)
+FIXTURES.update({
+    # TERSOFF smooth cut-off with offset 0.5, a cell wide enough for the ordered lists
+    "tersoff": ("chno-4b", dict(CH4B, natoms=120), 1, 21),
+    # inverse-r Chebyshev transform (water, 2-body + 3-body)
+    "invr": ("water-3b", dict(nmol=24, L=8.96, order=(8, 4, 0), fitstrs="ALL", fitener=True), 1, 22),
+    # no transform (x = r)
+    "notrans": ("chno-4b", dict(CH4B, natoms=60), 1, 23),
+    # per-cluster-type S_MAXIM and S_MINIM of 3- and 4-body types (SPECIAL ... SPECIFIC)
+    "specific": ("chno-4b", dict(CH4B, natoms=120), 1, 24),
+    # 3- and 4-body cluster types left out of A (EXCLUDE 3B / 4B INTERACTION)
+    "exclude": ("chno-4b", dict(CH4B, natoms=60), 1, 25),
+    # below-s_min variants of the 3/4-body basis (CHEBYFIX), with inner cut-offs raised
+    # to 1.3 A so that pairs at 0.9-1.3 A fall below them
+    "chebyfix_zero": ("chno-4b", dict(CH4B, natoms=60), 1, 26),
+    "chebyfix_const": ("chno-4b", dict(CH4B, natoms=60), 1, 27),
+    "chebyfix_smooth": ("chno-4b", dict(CH4B, natoms=60), 1, 28),
+})
+RAISE_SMIN = "\nSPECIAL 3B S_MINIM: ALL 1.3\n\nSPECIAL 4B S_MINIM: ALL 1.3\n"
+PATCH = {   # name -> [(old, new), ...] applied to the generated fm_setup.in
+    "tersoff": [("\tCUBIC", "\tTERSOFF 0.5")],
+    "invr": [("\tMORSE", "\tINVRSE_R")],
+    "notrans": [("\tMORSE", "\tNONE")],
+    "specific": [("SPECIAL 3B S_MAXIM: ALL 4.0",
+                  "SPECIAL 3B S_MAXIM: SPECIFIC 2\nCCCCCC CC CC CC 4.2 4.2 4.2\nCCCHCH CC CH CH 3.9 3.6 3.6\n\n"
+                  "SPECIAL 3B S_MINIM: SPECIFIC 1\nCHCHHH CH CH HH 1.1 1.1 1.2"),
+                 ("SPECIAL 4B S_MAXIM: ALL 3.5",
+                  "SPECIAL 4B S_MAXIM: SPECIFIC 2\nCCCCCCCCCCCC CC CC CC CC CC CC 3.6 3.6 3.6 3.6 3.6 3.6\n"
+                  "CCCCCHCCCHCH CC CC CH CC CH CH 3.4 3.4 3.1 3.4 3.1 3.1")],
+    "exclude": [("# ENDFILE #", "EXCLUDE 3B INTERACTION: 1\nC C H\n\nEXCLUDE 4B INTERACTION: 2\nC C C H\n"
+                                "H H H H\n\n# ENDFILE #")],
+    "chebyfix_zero": [("# PAIRTYP #", "# CHEBYFIX #\n\tZERO_DERIV\n# PAIRTYP #"),
+                      ("# FCUTTYP #", RAISE_SMIN + "\n# FCUTTYP #")],
+    "chebyfix_const": [("# PAIRTYP #", "# CHEBYFIX #\n\tCONSTANT_DERIV\n# PAIRTYP #"),
+                       ("# FCUTTYP #", RAISE_SMIN + "\n# FCUTTYP #")],
+    "chebyfix_smooth": [("# PAIRTYP #", "# CHEBYFIX #\n\tSMOOTH 0.02\n# PAIRTYP #"),
+                        ("# FCUTTYP #", RAISE_SMIN + "\n# FCUTTYP #")],
 }
 
 SKIP = {"skipframes": 2}
@@ -82,6 +125,12 @@ def make(name):
         key = f"# NFRAMES #\n\t{nframes}\n"
         assert key in fm
         fm = fm.replace(key, key + f"# SKPFRMS #\n\t{SKIP[name]}\n")
+        open(os.path.join(d, "fm_setup.in"), "w").write(fm)
+    if name in PATCH:
+        fm = open(os.path.join(d, "fm_setup.in")).read()
+        for a, b in PATCH[name]:
+            assert a in fm, (name, a)
+            fm = fm.replace(a, b, 1)
         open(os.path.join(d, "fm_setup.in"), "w").write(fm)
     if name in HIER:
         fm = open(os.path.join(d, "fm_setup.in")).read()

@@ -27,7 +27,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 cg = importlib.import_module("chimes_lsq-myllfork_gb300")
 REF = os.path.join(ROOT, "oracle", "_ref", "chimes_lsq")
-CASE = "/root/reference/test_suite-lsq/lsq2"
+CASE = os.path.join(os.environ.get("CHIMES_REF_DIR", "/root/reference"), "test_suite-lsq", "lsq2")
 
 
 def main():
