@@ -230,9 +230,13 @@ def fit_bench(cg, sess, model, blocks, dblocks, asm64_s, timer, torch, args):
     t_cs = timer(lambda: sess.cholesky_solve(L.data_ptr(), C, h.data_ptr(), x.data_ptr()))
     x_direct = x.clone()
     lab_ptrs = [l.data_ptr() for l in labels]
+    sess.profile(True)
     t0 = time.perf_counter()
     info = sess.refine_streamed(L.data_ptr(), C, lam, dblocks, lab_ptrs, x.data_ptr(), max_iters=40, tol=1e-10)
     t_ref = time.perf_counter() - t0
+    rst = sess.stage_times()
+    sess.profile(False)
+    ref_stages = {k: v[0] / 1e3 for k, v in rst.items() if v[1]}
     x_mixed = x.clone()
     info_c = sess.refine_streamed(L.data_ptr(), C, lam, dblocks, lab_ptrs, x.data_ptr(), max_iters=30, tol=1e-14)
     x_conv = x.clone()
@@ -272,7 +276,7 @@ def fit_bench(cg, sess, model, blocks, dblocks, asm64_s, timer, torch, args):
         "rows": R, "cols": C, "ridge": lam, "ridge_rule": "1e-6 * max_i (A^T A)_ii",
         "mixed": {"assembly_fp32_s": t_asm32, "gram_bf16x3_s": t_gram, "cholesky_fp64_s": t_chol,
                   "cholesky_solve_s": t_cs, "refine_fp64_s": t_ref, "refine_passes": info["iters"],
-                  "refine_last_rel_update": info["rel_update"], "total_s": mixed,
+                  "refine_last_rel_update": info["rel_update"], "refine_stages_s": ref_stages, "total_s": mixed,
                   "rows_per_s_assembly_plus_gram": R / (t_asm32 + t_gram)},
         "plain": {"assembly_fp64_s": asm64_s, "gram_fp64_s": t_gram64,
                   "gram_fp64_timing": f"FP64 SYRK of {K} rows x all {C} columns, {len(reps)} repeats "

@@ -365,20 +365,22 @@ __global__ void k_add_diag(double* G, int n, double v) {
 }
 
 // ---------------------------------------------------------------- FP64 FMA rate
-// Eight independent FMA chains per thread; the result is stored so that the chains
-// are not removed.
+// CH independent FMA chains per thread (enough in flight to cover the FP64 pipe's
+// latency at the occupancy the launch gets); the result is stored so that the
+// chains are not removed.
+template <int CH>
 __global__ void __launch_bounds__(256) k_fp64_fma(double* out, int iters, double seed) {
-    double x[8];
+    double x[CH];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) x[k] = seed + 1e-9 * (threadIdx.x + 37 * k);
+    for (int k = 0; k < CH; ++k) x[k] = seed + 1e-9 * (threadIdx.x + 37 * k);
     const double mul = 0.9999999999, add = 1e-12;
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], mul, add);
+        for (int k = 0; k < CH; ++k) x[k] = fma(x[k], mul, add);
     }
     double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) s += x[k];
+    for (int k = 0; k < CH; ++k) s += x[k];
     out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
@@ -516,30 +518,38 @@ void add_diag64(double* G, int n, double v, cudaStream_t st) {
 }
 
 double fp64_fma_tflops(cudaStream_t st) {
-    const int blocks = sm_count() * 8, threads = 256, iters = 1 << 15;
+    // the best of a few chain counts and occupancies; flops = 2 per FMA
+    const int threads = 256, iters = 1 << 13;
+    const int sms = sm_count();
     double* out = nullptr;
-    ckd(cudaMallocAsync((void**)&out, sizeof(double) * blocks * threads, st), "peak scratch");
+    ckd(cudaMallocAsync((void**)&out, sizeof(double) * sms * 8 * threads, st), "peak scratch");
     cudaEvent_t e0, e1;
     ckd(cudaEventCreate(&e0), "event");
     ckd(cudaEventCreate(&e1), "event");
-    cgd::k_fp64_fma<<<blocks, threads, 0, st>>>(out, iters, 1.0);   // warm-up (clocks settle)
-    float best = 1e30f;
-    for (int rep = 0; rep < 5; ++rep) {
-        ckd(cudaEventRecord(e0, st), "record");
-        cgd::k_fp64_fma<<<blocks, threads, 0, st>>>(out, iters, 1.0 + rep);
-        ckd(cudaEventRecord(e1, st), "record");
-        ckd(cudaEventSynchronize(e1), "sync");
-        float ms = 0.f;
-        ckd(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
-        best = std::min(best, ms);
-    }
-    ckd(cudaGetLastError(), "k_fp64_fma");
+    double best = 0.0;
+    auto run = [&](auto kernel, int chains, int blocks_per_sm) {
+        const int blocks = sms * blocks_per_sm;
+        kernel<<<blocks, threads, 0, st>>>(out, iters, 1.0);   // warm-up (clocks settle)
+        for (int rep = 0; rep < 3; ++rep) {
+            ckd(cudaEventRecord(e0, st), "record");
+            kernel<<<blocks, threads, 0, st>>>(out, iters, 1.0 + rep);
+            ckd(cudaEventRecord(e1, st), "record");
+            ckd(cudaEventSynchronize(e1), "sync");
+            float ms = 0.f;
+            ckd(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            best = std::max(best, 2.0 * chains * iters * (double)blocks * threads / (ms * 1e-3) / 1e12);
+        }
+        ckd(cudaGetLastError(), "k_fp64_fma");
+    };
+    run(cgd::k_fp64_fma<8>, 8, 8);
+    run(cgd::k_fp64_fma<16>, 16, 4);
+    run(cgd::k_fp64_fma<32>, 32, 4);
+    run(cgd::k_fp64_fma<32>, 32, 2);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ckd(cudaFreeAsync(out, st), "peak scratch free");
     ckd(cudaStreamSynchronize(st), "sync");
-    const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
-    return flops / (best * 1e-3) / 1e12;
+    return best;
 }
 
 }  // namespace cg

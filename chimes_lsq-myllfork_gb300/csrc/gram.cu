@@ -226,6 +226,40 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                  : "memory");
 }
 
+// Tile pair (ti <= tj) of CTA t.  The upper triangle is walked in super-tiles of
+// GB_GROUP x GB_GROUP tile pairs (super-tile pairs by rows, tiles inside column by
+// column), so that the CTAs resident at one time -- about one super-tile -- read
+// GB_GROUP row tiles and GB_GROUP column tiles between them, which stay in L2, instead
+// of one row tile and a different column tile each.
+constexpr int GB_GROUP = 12;
+__device__ __forceinline__ void grouped_pair(int t, int ntile, int& ti, int& tj) {
+    const int G = GB_GROUP;
+    const int nsup = (ntile + G - 1) / G;
+    int SI = 0;
+    for (; SI < nsup; ++SI) {
+        const int r = min(G, ntile - SI * G);
+        const int cnt = r * (r + 1) / 2 + r * max(0, ntile - (SI + 1) * G);
+        if (t < cnt) break;
+        t -= cnt;
+    }
+    const int r = min(G, ntile - SI * G);
+    const int dcnt = r * (r + 1) / 2;
+    if (t < dcnt) {   // the diagonal super-tile, upper triangle by rows
+        int li = 0;
+        while (t >= r - li) { t -= r - li; ++li; }
+        ti = SI * G + li;
+        tj = ti + t;
+        return;
+    }
+    t -= dcnt;
+    for (int SJ = SI + 1; SJ < nsup; ++SJ) {
+        const int c = min(G, ntile - SJ * G);
+        if (t < r * c) { ti = SI * G + t % r; tj = SJ * G + t / r; return; }
+        t -= r * c;
+    }
+    ti = tj = 0;   // not reached for t < ntile (ntile + 1) / 2
+}
+
 // ---------------------------------------------------------------- tcgen05 Gram tile
 // grid.x: upper-triangular tile pair (i <= j), grid.y: K slice.
 __global__ void __launch_bounds__(GB_THREADS, 1)
@@ -238,10 +272,8 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
     uint64_t* done = empty + GB_STAGES;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
 
-    // tile pair from the linear upper-triangle index
-    int t = blockIdx.x, ti = 0;
-    while (t >= ntile - ti) { t -= ntile - ti; ++ti; }
-    const int tj = ti + t;
+    int ti = 0, tj = 0;
+    grouped_pair((int)blockIdx.x, ntile, ti, tj);
     const int64_t kb = (int64_t)blockIdx.y * kslice;
     const int64_t ke = min(kpad, kb + kslice);
     const int nk = (int)((ke - kb) / GB_K);

@@ -35,6 +35,7 @@ double factor_ridge(const double* G, int n, double ridge, double* L, int* d_info
 struct Fp64Operator {
     std::function<void(const double* p, double* q)> apply;
     std::function<void(const double* x, double* r)> residual;
+    std::function<void(bool begin)> mark;   // brackets the preconditioner solves (optional timing)
 };
 struct PcgStats {
     int iters = 0;

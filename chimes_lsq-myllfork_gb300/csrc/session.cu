@@ -314,7 +314,8 @@ static_assert(ST_GRAM_ATB == 11 && ST_GRAM_SPLIT == 12 && ST_GRAM_TC == 13 && ST
 
 const char* stage_name(int s) {
     static const char* names[ST_COUNT] = {"frame_setup", "neighbour_lists", "clusters", "buckets", "force_2b",
-                                          "virial_2b", "force_3b", "virial_3b", "force_4b", "virial_4b", "other", "gram_atb", "gram_split", "gram_tensor", "gram_fp64_syrk"};
+                                          "virial_2b", "force_3b", "virial_3b", "force_4b", "virial_4b", "other", "gram_atb", "gram_split", "gram_tensor", "gram_fp64_syrk",
+                                          "refine_products", "refine_preconditioner"};
     return s >= 0 && s < ST_COUNT ? names[s] : "?";
 }
 
@@ -916,9 +917,11 @@ struct StreamRows {
             const DeviceFrames& d = *blocks[k];
             if (d.nrows == 0) continue;
             se.assemble(d, 0, Ablk, ncols, nullptr);
+            se.mark(ST_REFINE_PRODUCTS, true);
             gemv_rows64(Ablk, ncols, d.nrows, ncols, v, resid ? labels[k] : nullptr,
                         weights.empty() ? nullptr : weights[k], t, st);
             gemv_cols64(Ablk, ncols, d.nrows, ncols, t, out, partial, st);
+            se.mark(ST_REFINE_PRODUCTS, false);
         }
         if (extra_rows > 0) {
             gemv_rows64(extra_A, ncols, extra_rows, ncols, v, resid ? extra_b : nullptr, extra_w, t, st);
@@ -946,6 +949,7 @@ void Session::refine_streamed(const double* L, int ncols, double ridge, const st
         Fp64Operator op;
         op.apply = [&](const double* p, double* q) { R.pass(p, false, q, stream_); };
         op.residual = [&](const double* xv, double* r) { R.pass(xv, true, r, stream_); };
+        op.mark = [this](bool begin) { mark(ST_REFINE_PRECOND, begin); };
         const PcgStats ps = pcg_ridge(L, ncols, ridge, op, x, max_iters, tol, stream_);
         CK(cudaStreamSynchronize(stream_));
         if (info) { info[0] = ps.iters; info[1] = ps.rel_update; info[2] = ps.rnorm0; info[3] = ps.rnorm; }

@@ -179,7 +179,8 @@ struct BatchFit {
 // Pipeline stages timed with CUDA events when profiling is on.
 enum Stage {
     ST_SETUP = 0, ST_NEIGH, ST_CLUSTERS, ST_BUCKET, ST_FORCE2, ST_VIRIAL2, ST_FORCE3, ST_VIRIAL3, ST_FORCE4,
-    ST_VIRIAL4, ST_OTHER, ST_GRAM_ATB, ST_GRAM_SPLIT, ST_GRAM_TC, ST_GRAM_SYRK, ST_COUNT
+    ST_VIRIAL4, ST_OTHER, ST_GRAM_ATB, ST_GRAM_SPLIT, ST_GRAM_TC, ST_GRAM_SYRK, ST_REFINE_PRODUCTS,
+    ST_REFINE_PRECOND, ST_COUNT
 };
 const char* stage_name(int s);
 

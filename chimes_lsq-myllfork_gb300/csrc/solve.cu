@@ -57,6 +57,11 @@ double factor_ridge(const double* G, int n, double ridge, double* L, int* d_info
 
 PcgStats pcg_ridge(const double* L, int n, double ridge, const Fp64Operator& op, double* x, int max_iters,
                    double tol, cudaStream_t st) {
+    auto precond = [&](const double* r, double* z) {
+        if (op.mark) op.mark(true);
+        cholesky_solve64(L, n, r, z, st);
+        if (op.mark) op.mark(false);
+    };
     PcgStats out;
     DevVec r(n, st), z(n, st), p(n, st), q(n, st), sc(1, st);
     // r = A^T (b - A x) - ridge x
@@ -65,7 +70,7 @@ PcgStats pcg_ridge(const double* L, int n, double ridge, const Fp64Operator& op,
     out.rnorm0 = std::sqrt(host_dot(r.p, r.p, n, sc.p, st));
     out.rnorm = out.rnorm0;
     if (max_iters <= 0 || out.rnorm0 == 0.0) return out;
-    cholesky_solve64(L, n, r.p, z.p, st);
+    precond(r.p, z.p);
     cks(cudaMemcpyAsync(p.p, z.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st), "p = z");
     double rz = host_dot(r.p, z.p, n, sc.p, st);
     for (int it = 0; it < max_iters && rz > 0.0; ++it) {
@@ -80,7 +85,7 @@ PcgStats pcg_ridge(const double* L, int n, double ridge, const Fp64Operator& op,
         // relative size of this update: |alpha| ||p|| / ||x||
         const double pp = host_dot(p.p, p.p, n, sc.p, st), xx = host_dot(x, x, n, sc.p, st);
         out.rel_update = xx > 0.0 ? std::fabs(alpha) * std::sqrt(pp / xx) : 0.0;
-        cholesky_solve64(L, n, r.p, z.p, st);
+        precond(r.p, z.p);
         const double rz_new = host_dot(r.p, z.p, n, sc.p, st);
         if (out.rel_update <= tol) { rz = rz_new; break; }
         axpby64(n, 1.0, z.p, rz_new / rz, p.p, st);   // p = z + beta p

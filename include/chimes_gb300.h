@@ -296,7 +296,7 @@ int cg_session_last_launches(const cg_session* s, int64_t* launches);
  * stage of every assembly (on its own stream).  cg_session_stage_times waits for them
  * and returns accumulated milliseconds and call counts for the CG_NSTAGES stages
  * named by cg_stage_name; cg_session_profile(s, 1) also clears the totals. */
-#define CG_NSTAGES 15
+#define CG_NSTAGES 17
 int cg_session_profile(cg_session* s, int enable);
 int cg_session_stage_times(cg_session* s, double* ms, int64_t* calls);
 const char* cg_stage_name(int stage);
