@@ -177,20 +177,28 @@ __device__ __forceinline__ double tget(const double* M, int64_t si, int64_t sj, 
     return M[i * si + j * sj];
 }
 
-__device__ void trsv_block_warp(const double* M, int64_t si, int64_t sj, int b0, int bl, bool lower, double* xs,
-                                int lane) {
+// The bl x bl diagonal block at b0 (bl <= 32), staged by every thread of the CTA into
+// tb (32 x 33) so that warp 0's substitution below reads shared memory only.
+__device__ void trsv_stage_block(const double* M, int64_t si, int64_t sj, int b0, int bl, double (*tb)[33]) {
+    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
+        const int i = si == 1 ? t % 32 : t / 32, j = si == 1 ? t / 32 : t % 32;   // contiguous index fastest
+        tb[i][j] = (i < bl && j < bl) ? tget(M, si, sj, b0 + i, b0 + j) : 0.0;
+    }
+}
+
+__device__ void trsv_block_warp(const double (*tb)[33], int b0, int bl, bool lower, double* xs, int lane) {
     double v = lane < bl ? xs[b0 + lane] : 0.0;
     if (lower) {
         for (int k = 0; k < bl; ++k) {
-            if (lane == k) v = v / tget(M, si, sj, b0 + k, b0 + k);
+            if (lane == k) v = v / tb[k][k];
             const double xk = __shfl_sync(0xffffffffu, v, k);
-            if (lane > k && lane < bl) v = fma(-tget(M, si, sj, b0 + lane, b0 + k), xk, v);
+            if (lane > k && lane < bl) v = fma(-tb[lane][k], xk, v);
         }
     } else {
         for (int k = bl - 1; k >= 0; --k) {
-            if (lane == k) v = v / tget(M, si, sj, b0 + k, b0 + k);
+            if (lane == k) v = v / tb[k][k];
             const double xk = __shfl_sync(0xffffffffu, v, k);
-            if (lane < k) v = fma(-tget(M, si, sj, b0 + lane, b0 + k), xk, v);
+            if (lane < k) v = fma(-tb[lane][k], xk, v);
         }
     }
     if (lane < bl) xs[b0 + lane] = v;
@@ -219,14 +227,16 @@ __device__ void trsv_update_cta(const double* M, int64_t si, int64_t sj, int b0,
 __global__ void __launch_bounds__(TS_THREADS) k_trsv_small(const double* __restrict__ M, int64_t si, int64_t sj,
                                                            int n, int lower, double* __restrict__ x) {
     extern __shared__ double xs[];
+    __shared__ double tb[32][33];
     for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = x[i];
-    __syncthreads();
     const int nb = (n + 31) / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int bb = 0; bb < nb; ++bb) {
         const int b = lower ? bb : nb - 1 - bb;
         const int b0 = b * 32, bl = min(32, n - b0);
-        if (warp == 0) trsv_block_warp(M, si, sj, b0, bl, lower != 0, xs, lane);
+        trsv_stage_block(M, si, sj, b0, bl, tb);
+        __syncthreads();
+        if (warp == 0) trsv_block_warp(tb, b0, bl, lower != 0, xs, lane);
         __syncthreads();
         if (lower) trsv_update_cta(M, si, sj, b0, bl, b0 + bl, n, xs);
         else trsv_update_cta(M, si, sj, b0, bl, 0, b0, xs);

@@ -35,6 +35,8 @@ constexpr int GB_M = 128, GB_N = 128, GB_K = 64, GB_STAGES = 3, GB_THREADS = 128
 constexpr uint32_t GB_TILE_BYTES = GB_M * GB_K * 2;         // one 128x64 bf16 operand tile (16 KB)
 constexpr uint32_t GB_STAGE_BYTES = 4 * GB_TILE_BYTES;      // A_hi, A_lo, B_hi, B_lo
 constexpr long long GB_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
+constexpr int GB_EPI_LD = GB_N + 1;                         // epilogue staging row (floats)
+static_assert(4 * 32 * GB_EPI_LD * 4 <= (int)(GB_STAGES * GB_STAGE_BYTES), "epilogue staging fits the stages");
 
 // ---------------------------------------------------------------- split + transpose
 // planes[p][c][k] (bf16, k contiguous) for rows [r0, r0+nr) of A (row-major, lda),
@@ -345,7 +347,10 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
     if (have) have = mbar_wait(done, 0, err, 3);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (have && *err == 0) {
-        const int row = ti * GB_M + warp * 32 + lane;
+        // The accumulator rows of this warp (TMEM lanes warp*32 ..) pass through a
+        // private slice of the (now idle) stage memory, so that every atomic
+        // instruction then adds 32 consecutive columns of one row of G.
+        float* stile = reinterpret_cast<float*>(smem) + (size_t)warp * 32 * GB_EPI_LD;
 #pragma unroll 1
         for (int c0 = 0; c0 < GB_N; c0 += 32) {
             uint32_t v[32];
@@ -360,13 +365,20 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                   "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row < ncols) {
 #pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    const int col = tj * GB_N + c0 + c;
-                    if (col < ncols && (ti != tj || col >= row))
-                        atomicAdd(&G[(int64_t)row * ncols + col], (double)__uint_as_float(v[c]));
-                }
+            for (int c = 0; c < 32; ++c) stile[lane * GB_EPI_LD + c0 + c] = __uint_as_float(v[c]);
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int r = 0; r < 32; ++r) {
+            const int row = ti * GB_M + warp * 32 + r;
+            if (row >= ncols) break;
+            double* grow = G + (int64_t)row * ncols;
+#pragma unroll
+            for (int j = 0; j < GB_N / 32; ++j) {
+                const int col = tj * GB_N + j * 32 + lane;
+                if (col < ncols && (ti != tj || col >= row))
+                    atomicAdd(grow + col, (double)stile[r * GB_EPI_LD + j * 32 + lane]);
             }
         }
     }

@@ -787,7 +787,9 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
     size_t pbytes = 0;
     if (mode == 1) {
         const int64_t cpad = (ncols + 127) / 128 * 128;
-        int64_t rb = std::min<int64_t>(nrows, std::max<int64_t>(64, (int64_t)(1ull << 30) / (4 * cpad)));
+        // planes for up to 8 GiB of rows: the whole block of a large-column fit in one
+        // tensor-core launch (each launch re-walks every tile pair)
+        int64_t rb = std::min<int64_t>(nrows, std::max<int64_t>(64, (int64_t)(8ull << 30) / (4 * cpad)));
         pbytes = gram_plane_bytes(rb, ncols);
         planes = S.get<unsigned char>(pbytes);
     }
@@ -1028,7 +1030,7 @@ std::unique_ptr<BatchFit> Session::batch_fit_graph(const std::vector<const Devic
     int64_t maxrows = 1;
     for (const DeviceFrames* d : blocks) maxrows = std::max<int64_t>(maxrows, d->nrows);
     const int64_t cpad = (ncols + 127) / 128 * 128;
-    const int64_t rb = std::min<int64_t>(maxrows, std::max<int64_t>(64, (int64_t)(1ull << 30) / (4 * cpad)));
+    const int64_t rb = std::min<int64_t>(maxrows, std::max<int64_t>(64, (int64_t)(8ull << 30) / (4 * cpad)));
     const size_t pbytes = gram_plane_bytes(rb, ncols);
     CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
     try {

@@ -6,6 +6,7 @@
     python profile_cases.py assemble4b [nframes] [fp32]  # A of 256-atom C/H/N/O 4-body frames
     python profile_cases.py gram4b [rows]         # split-BF16 Gram of a 4-body FP32 A (51,209 columns)
     python profile_cases.py syrk [rows] [cols]    # FP64 SYRK Gram of a random A
+    python profile_cases.py gramrand [rows] [cols]  # split-BF16 Gram of a random FP32 A
     python profile_cases.py serve NATOMS PRECISION NSTEPS  # one NVE request, stage times
 
 Each case runs its launch twice after the set-up, so `ncu -k regex:<kernel> -c 1`
@@ -75,6 +76,21 @@ def main(argv):
                 sess.gram(1, Ar.data_ptr(), ncols, rows, ncols, b.data_ptr(), 1, G.data_ptr(), h.data_ptr())
         torch.cuda.synchronize()
         print("ok", case, nrows, ncols)
+        return
+    if case == "gramrand":
+        rows = int(argv[1]) if len(argv) > 1 else 16384
+        cols = int(argv[2]) if len(argv) > 2 else 8192
+        fm = synth.make_workload("water-2b", tmp, nframes=1, seed=3)
+        sess = cg.Session(cg.Model(fm), 0)
+        A = torch.randn(rows, cols, dtype=torch.float32, device="cuda")
+        b = torch.randn(rows, dtype=torch.float64, device="cuda")
+        G = torch.zeros((cols, cols), dtype=torch.float64, device="cuda")
+        h = torch.zeros(cols, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for _ in range(2):
+            sess.gram(1, A.data_ptr(), cols, rows, cols, b.data_ptr(), 1, G.data_ptr(), h.data_ptr())
+        torch.cuda.synchronize()
+        print("ok", case, rows, cols)
         return
     if case == "syrk":
         rows = int(argv[1]) if len(argv) > 1 else 8192
