@@ -123,6 +123,9 @@ def lib():
         "cg_lars": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_int, vp, vp]),
         "cg_dlars": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_int, vp, ctypes.c_double, ctypes.c_int, vp, vp]),
+        "cg_dlars_ex": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int, vp, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_char_p, ctypes.c_char_p, vp, vp]),
         "cg_md_setup": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double]),
         "cg_md_force": (ctypes.c_int, [vp, vp, dp, dp]),
@@ -639,15 +642,18 @@ class Session:
         return int(info[0]), int(info[1]), info[2]
 
     def dlars(self, g_ptr, h_ptr, ncols, nsamples, btb, lam, lasso, x_ptr, max_iter=10000000, colsum_ptr=0,
-              bsum=0.0):
-        """The reference's DLARS (lars / lasso) on the normal equations (cg_dlars);
-        colsum_ptr (device A^T 1) and bsum select --normalize=y.  Returns
+              bsum=0.0, max_norm=0.0, restart_in=None, restart_out=None):
+        """The reference's DLARS (lars / lasso) on the normal equations (cg_dlars_ex);
+        colsum_ptr (device A^T 1) and bsum select --normalize=y; max_iter, max_norm,
+        restart_in / restart_out as its --iterations, --max_norm, --restart.  Returns
         (iterations, active, objective of the last vertex)."""
         info = (ctypes.c_double * 3)()
-        _check(lib().cg_dlars(self._h, ctypes.c_void_p(int(g_ptr)), ctypes.c_void_p(int(h_ptr)), int(ncols),
-                              int(nsamples), float(btb), float(lam), 1 if lasso else 0,
-                              ctypes.c_void_p(int(colsum_ptr) or None), float(bsum), int(max_iter),
-                              ctypes.c_void_p(int(x_ptr)), info))
+        enc = lambda p: os.fspath(p).encode() if p else None
+        _check(lib().cg_dlars_ex(self._h, ctypes.c_void_p(int(g_ptr)), ctypes.c_void_p(int(h_ptr)), int(ncols),
+                                 int(nsamples), float(btb), float(lam), 1 if lasso else 0,
+                                 ctypes.c_void_p(int(colsum_ptr) or None), float(bsum), int(max_iter),
+                                 float(max_norm), enc(restart_in), enc(restart_out), ctypes.c_void_p(int(x_ptr)),
+                                 info))
         return int(info[0]), int(info[1]), info[2]
 
     # ---------------------------------------------------------------- MD force

@@ -515,6 +515,21 @@ int cg_dlars(cg_session* s, const double* G, const double* h, int ncols, int64_t
     });
 }
 
+int cg_dlars_ex(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double btb,
+                double lambda, int lasso, const double* colsum, double bsum, int max_iter, double max_norm,
+                const char* restart_in, const char* restart_out, double* x, double* info) {
+    return guarded([&] {
+        need(s && G && h && x && ncols > 0 && nsamples > 0 && lambda >= 0.0 && max_iter > 0, "dlars arguments");
+        const double mn = max_norm > 0.0 ? max_norm : 1.0e50;
+        if (colsum)
+            s->s->dlars_normalized(G, h, colsum, bsum, ncols, nsamples, btb, lambda, lasso, max_iter, x, info, mn,
+                                   restart_in, restart_out);
+        else
+            s->s->lars(G, h, ncols, nsamples, lambda, max_iter, x, info, lasso ? 2 : 1, btb, mn, restart_in,
+                       restart_out);
+    });
+}
+
 int cg_session_last_launches(const cg_session* s, int64_t* launches) {
     return guarded([&] {
         need(s && launches, "session/launches");
@@ -812,6 +827,8 @@ int cg_session_tune(cg_session* s, const char* key, int value) {
         const std::string k(key);
         if (k == "gram_ctas_per_sm") s->s->set_gram_ctas_per_sm(value);
         else if (k == "md_skin_milli") s->s->set_md_skin(value * 1e-3);
+        else if (k == "gram_rows_per_launch") s->s->set_gram_rows_per_launch(value);
+        else if (k == "refine_cache_mb") s->s->set_refine_cache_bytes(value < 0 ? -1 : (int64_t)value << 20);
         else throw cg::Error(1, "unknown tuning key: " + k);
     });
 }

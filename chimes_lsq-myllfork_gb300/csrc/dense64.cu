@@ -218,6 +218,7 @@ __device__ void trsv_update_cta(const double* M, int64_t si, int64_t sj, int b0,
     } else {         // columns contiguous along i (or general): a thread per row
         for (int i = r0 + (int)threadIdx.x; i < r1; i += blockDim.x) {
             double p = 0.0;
+#pragma unroll 8   // eight independent loads in flight per thread
             for (int c = 0; c < bl; ++c) p = fma(tget(M, si, sj, i, b0 + c), xs[b0 + c], p);
             xs[i] -= p;
         }
@@ -264,9 +265,15 @@ __global__ void __launch_bounds__(256) k_trsv_update(const double* __restrict__ 
         }
     } else {
         for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
-            double p = 0.0;
-            for (int c = 0; c < bl; ++c) p = fma(tget(M, si, sj, i, b0 + c), xb[c], p);
-            x[i] -= p;
+            double p0 = 0.0, p1 = 0.0;
+            int c = 0;
+#pragma unroll 8   // sixteen independent loads in flight per thread
+            for (; c + 1 < bl; c += 2) {
+                p0 = fma(tget(M, si, sj, i, b0 + c), xb[c], p0);
+                p1 = fma(tget(M, si, sj, i, b0 + c + 1), xb[c + 1], p1);
+            }
+            if (c < bl) p0 = fma(tget(M, si, sj, i, b0 + c), xb[c], p0);
+            x[i] -= p0 + p1;
         }
     }
 }

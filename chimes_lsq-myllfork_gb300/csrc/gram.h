@@ -52,11 +52,18 @@ PcgStats pcg_ridge(const double* L, int n, double ridge, const Fp64Operator& op,
 // coefficients into x (device); info: [steps, active variables, final C / n].
 // mode 0: scikit-learn LassoLars; mode 1 / 2: the reference's DLARS `lars` /
 // `lasso` (needs btb = b^T b; info[2] is then the objective of the last vertex).
+// DLARS only (mode 1 / 2): max_norm stops once ||x||_1 after a step exceeds it and
+// returns the vertex before that step (the driver's --max_norm); restart_out (may be
+// null) receives the walk's state every ten iterations and restart_in (may be null)
+// resumes a walk from such a file (the driver's --restart).
 void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
-                double* info, cudaStream_t st, int mode = 0, double btb = 0.0);
+                double* info, cudaStream_t st, int mode = 0, double btb = 0.0, double max_norm = 1.0e50,
+                const char* restart_in = nullptr, const char* restart_out = nullptr);
 // DLARS with --normalize: columns centred and scaled, b centred (colsum = A^T 1 on
 // the device, bsum = sum b), coefficients returned in unscaled units.
 void dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int n, int64_t nsamples,
-                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, cudaStream_t st);
+                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, cudaStream_t st,
+                      double max_norm = 1.0e50, const char* restart_in = nullptr,
+                      const char* restart_out = nullptr);
 
 }  // namespace cg

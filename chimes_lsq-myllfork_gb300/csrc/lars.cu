@@ -16,6 +16,8 @@
 // zero crossing the deletion of the variable from the factor by Givens rotations.
 
 #include <algorithm>
+#include <cstdio>
+#include <fstream>
 #include <cmath>
 #include <stdexcept>
 #include <string>
@@ -182,6 +184,32 @@ __global__ void k_lars_objective(const double* x, const double* h, const double*
     }
 }
 
+// ||x||_1 (single block; out[0])
+__global__ void k_lars_l1(const double* x, int n, double* out) {
+    __shared__ double s1[32];
+    double l1 = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) l1 += fabs(x[j]);
+    for (int o = 16; o > 0; o >>= 1) l1 += __shfl_down_sync(0xffffffffu, l1, o);
+    if ((threadIdx.x & 31) == 0) s1[threadIdx.x >> 5] = l1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double L1 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) L1 += s1[w];
+        out[0] = L1;
+    }
+}
+
+// c = h - G x (a warp per row of the symmetric G): the correlations of a restarted path
+__global__ void k_lars_corr(const double* G, const double* h, const double* x, int n, double* c) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= n) return;
+    double sacc = 0.0;
+    for (int j = lane; j < n; j += 32) sacc = fma(G[i * n + j], x[j], sacc);
+    for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+    if (lane == 0) c[i] = h[i] - sacc;
+}
+
 // DLARS --normalize on the normal equations (Matrix::normalize, Vector::normalize
 // contrib/dlars/src/Matrix.h:614-660, Vector.h:140-150): columns centred on their
 // means mu = colsum / n and scaled to unit norm sigma_j = sqrt(G_jj - n mu_j^2), b
@@ -253,10 +281,73 @@ static void ckl(cudaError_t e, const char* w) {
     if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error in ") + w + ": " + cudaGetErrorString(e));
 }
 
+namespace {
+// The walk's state at the top of an iteration (the DLARS restart file).
+struct LarsState {
+    int steps = 0, next_add = -1;
+    bool drop = false;
+    double last_obj = 1.0e50;
+    std::vector<double> x;        // n coefficients
+    std::vector<int> active;      // in entry order
+    std::vector<int> exclude;     // left out as dependent on the active set
+};
+
+void write_state(const std::string& path, const LarsState& S, double lambda, int mode) {
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) throw std::runtime_error("cannot write the DLARS restart file " + path);
+    std::fprintf(f, "DLARS restart\nIteration %d\nObjective %.17e\nLambda %.17e\nLasso %d\nNextAdd %d\nDrop %d\n",
+                 S.steps, S.last_obj, lambda, mode == 2 ? 1 : 0, S.next_add, S.drop ? 1 : 0);
+    int nz = 0;
+    for (double v : S.x) nz += v != 0.0;
+    std::fprintf(f, "Beta %zu %d\n", S.x.size(), nz);
+    for (size_t j = 0; j < S.x.size(); ++j)
+        if (S.x[j] != 0.0) std::fprintf(f, "%zu %.17e\n", j, S.x[j]);
+    std::fprintf(f, "Active %zu\n", S.active.size());
+    for (int j : S.active) std::fprintf(f, "%d\n", j);
+    std::fprintf(f, "Exclude %zu\n", S.exclude.size());
+    for (int j : S.exclude) std::fprintf(f, "%d\n", j);
+    std::fclose(f);
+}
+
+LarsState read_state(const std::string& path, int n, double lambda, int mode) {
+    std::ifstream in(path);
+    if (!in) throw std::runtime_error("cannot open the DLARS restart file " + path);
+    LarsState S;
+    std::string tag, w;
+    double lam = 0.0;
+    int lasso = 0, drop = 0;
+    size_t dim = 0, nz = 0, na = 0, ne = 0;
+    in >> w >> w;   // "DLARS restart"
+    in >> tag >> S.steps >> tag >> S.last_obj >> tag >> lam >> tag >> lasso >> tag >> S.next_add >> tag >> drop;
+    S.drop = drop != 0;
+    in >> tag >> dim >> nz;
+    if (!in || tag != "Beta" || (int)dim != n) throw std::runtime_error("DLARS restart file does not match the problem");
+    if (lasso != (mode == 2 ? 1 : 0) || lam != lambda)
+        throw std::runtime_error("DLARS restart file was written for another algorithm or lambda");
+    S.x.assign(n, 0.0);
+    for (size_t k = 0; k < nz; ++k) {
+        size_t j;
+        double v;
+        in >> j >> v;
+        if (j >= (size_t)n) throw std::runtime_error("DLARS restart file: coefficient index out of range");
+        S.x[j] = v;
+    }
+    in >> tag >> na;
+    for (size_t k = 0; k < na; ++k) { int j; in >> j; S.active.push_back(j); }
+    in >> tag >> ne;
+    for (size_t k = 0; k < ne; ++k) { int j; in >> j; S.exclude.push_back(j); }
+    if (!in) throw std::runtime_error("DLARS restart file is truncated");
+    for (int j : S.active) if (j < 0 || j >= n) throw std::runtime_error("DLARS restart file: bad active index");
+    for (int j : S.exclude) if (j < 0 || j >= n) throw std::runtime_error("DLARS restart file: bad excluded index");
+    return S;
+}
+}  // namespace
+
 // Returns [steps, active variables, final C / n]; x (device, n values) receives
 // the coefficients.  G: full symmetric FP64 (row-major), h: X^T y (device).
 void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, double alpha, int max_iter, double* x,
-                double* info, cudaStream_t st, int mode, double btb) {
+                double* info, cudaStream_t st, int mode, double btb, double max_norm, const char* restart_in,
+                const char* restart_out) {
     // mode 0: scikit-learn LassoLars (exact landing on C/n = alpha).  mode 1 / 2: the
     // reference's DLARS `lars` / `lasso` (contrib/dlars/src/dlars.C): the variable
     // named by the last step enters, C = max |c| over every variable, lasso
@@ -282,6 +373,7 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
         double* w = (double*)get(sizeof(double) * kmax);
         double* sv = (double*)get(sizeof(double) * kmax);
         double* scal = (double*)get(sizeof(double) * 4);
+        double* xprev = (double*)get(sizeof(double) * n);   // the vertex before a step (max_norm)
         cgd::ArgMax* am = (cgd::ArgMax*)get(sizeof(cgd::ArgMax));
         cgd::MinPos* mp = (cgd::MinPos*)get(sizeof(cgd::MinPos) * 2);
         ckl(cudaMemcpyAsync(c, h, sizeof(double) * n, cudaMemcpyDeviceToDevice, st), "c = h");
@@ -293,6 +385,7 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
         double C = 0.0;
         bool drop = false;
         int dropped = -1, steps = 0, next_add = -1;
+        bool resumed = false, stopped_max_norm = false, stopped_objective = false;
         double last_obj = 1.0e50, obj = 0.0;
         // C = max |h|
         cgd::k_lars_argmax<<<1, cgd::LARS_THREADS, 0, st>>>(c, flag, n, am);
@@ -301,6 +394,52 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
         ckl(cudaStreamSynchronize(st), "sync");
         C = hm.v;
         const int tb = 256;
+        // the active-set factor's new row for variable j (entering as number na);
+        // returns d2, the new diagonal squared (dependent when below 1e-13 G_jj)
+        auto factor_row = [&](int j, int na, double& gjj) {
+            ckl(cudaMemcpyAsync(&gjj, G + (size_t)j * n + j, sizeof(double), cudaMemcpyDeviceToHost, st), "Gjj");
+            double d2 = 0.0;
+            if (na == 0) {
+                ckl(cudaStreamSynchronize(st), "sync");
+                d2 = gjj;
+            } else {
+                // L l = G[A, j] with the row-major lower factor L(i, j) = L[i * kmax + j]
+                cgd::k_lars_gather<<<(na + tb - 1) / tb, tb, 0, st>>>(G, n, dact, na, j, sv);
+                trsv64(L, kmax, 1, na, true, sv, st);
+                cgd::k_lars_dot_rest<<<1, cgd::LARS_THREADS, 0, st>>>(sv, na, gjj, scal);
+                ckl(cudaMemcpyAsync(&d2, scal, sizeof(double), cudaMemcpyDeviceToHost, st), "d2");
+                ckl(cudaStreamSynchronize(st), "sync");
+            }
+            return d2;
+        };
+        if (dl && restart_in && *restart_in) {   // resume a walk from its restart file
+            LarsState R = read_state(restart_in, n, alpha, mode);
+            ckl(cudaMemcpyAsync(x, R.x.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st), "restart x");
+            cgd::k_lars_corr<<<(n + 7) / 8, 256, 0, st>>>(G, h, x, n, c);
+            const int one = 1, two = 2;
+            for (int j : R.exclude) {
+                hflag[j] = 2;
+                ckl(cudaMemcpyAsync(flag + j, &two, sizeof(int), cudaMemcpyHostToDevice, st), "flag");
+            }
+            for (int j : R.active) {   // the factor of G_AA, one row per active variable in entry order
+                const int na = (int)active.size();
+                if (na >= kmax) throw std::runtime_error("DLARS restart file: more active variables than rows");
+                double gjj = 0.0;
+                const double d2 = factor_row(j, na, gjj);
+                if (!(d2 > 0.0)) throw std::runtime_error("DLARS restart file: active set is not independent");
+                cgd::k_lars_put_row<<<(na + 1 + tb - 1) / tb, tb, 0, st>>>(L, kmax, na, sv, d2);
+                active.push_back(j);
+                hflag[j] = 1;
+                ckl(cudaMemcpyAsync(flag + j, &one, sizeof(int), cudaMemcpyHostToDevice, st), "flag");
+                ckl(cudaMemcpyAsync(dact + na, &active.back(), sizeof(int), cudaMemcpyHostToDevice, st), "active");
+                ckl(cudaStreamSynchronize(st), "sync");
+            }
+            steps = R.steps;
+            next_add = R.next_add;
+            drop = R.drop;
+            last_obj = R.last_obj;
+            resumed = true;
+        }
         while (steps < max_iter && (dl || C > target)) {
             if (dl) {
                 if ((int)active.size() >= n) break;   // no more iterations possible
@@ -310,9 +449,24 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
                 ckl(cudaMemcpyAsync(&obj, scal + 2, sizeof(double), cudaMemcpyDeviceToHost, st), "objective");
                 ckl(cudaMemcpyAsync(&hm, am, sizeof(hm), cudaMemcpyDeviceToHost, st), "C");
                 ckl(cudaStreamSynchronize(st), "sync");
-                if (obj > last_obj + 1.0e-10) break;   // this vertex is the answer
-                last_obj = obj;
+                if (resumed) {   // the restart file holds this vertex's objective already
+                    resumed = false;
+                } else {
+                    if (obj > last_obj + 1.0e-10) { stopped_objective = true; break; }   // this vertex is the answer
+                    last_obj = obj;
+                }
                 C = hm.v;
+                if (restart_out && *restart_out && steps > 0 && steps % 10 == 0) {
+                    // the state every ten iterations, as the reference's DLARS::print_restart
+                    LarsState W;
+                    W.steps = steps; W.next_add = next_add; W.drop = drop; W.last_obj = last_obj;
+                    W.x.resize(n);
+                    ckl(cudaMemcpyAsync(W.x.data(), x, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "x");
+                    ckl(cudaStreamSynchronize(st), "sync");
+                    W.active = active;
+                    for (int j = 0; j < n; ++j) if (hflag[j] == 2) W.exclude.push_back(j);
+                    write_state(restart_out, W, alpha, mode);
+                }
             }
             if (!drop) {
                 if (dl && next_add >= 0) {
@@ -326,19 +480,7 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
                 const int j = hm.i;
                 const int na = (int)active.size();
                 double gjj = 0.0;
-                ckl(cudaMemcpyAsync(&gjj, G + (size_t)j * n + j, sizeof(double), cudaMemcpyDeviceToHost, st), "Gjj");
-                double d2 = 0.0;
-                if (na == 0) {
-                    ckl(cudaStreamSynchronize(st), "sync");
-                    d2 = gjj;
-                } else {
-                    // L l = G[A, j] with the row-major lower factor L(i, j) = L[i * kmax + j]
-                    cgd::k_lars_gather<<<(na + tb - 1) / tb, tb, 0, st>>>(G, n, dact, na, j, sv);
-                    trsv64(L, kmax, 1, na, true, sv, st);
-                    cgd::k_lars_dot_rest<<<1, cgd::LARS_THREADS, 0, st>>>(sv, na, gjj, scal);
-                    ckl(cudaMemcpyAsync(&d2, scal, sizeof(double), cudaMemcpyDeviceToHost, st), "d2");
-                    ckl(cudaStreamSynchronize(st), "sync");
-                }
+                const double d2 = factor_row(j, na, gjj);
                 const int one = 1, two = 2;
                 if (!(d2 > 1e-13 * gjj) || na >= kmax) {   // dependent on the active set: leave it out
                     hflag[j] = 2;
@@ -389,6 +531,8 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
                 kz = -1;
                 last = true;
             }
+            if (dl && max_norm < 1.0e49)
+                ckl(cudaMemcpyAsync(xprev, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st), "x before the step");
             cgd::k_lars_update<<<(std::max(n, na) + tb - 1) / tb, tb, 0, st>>>(x, c, a, dact, w, na, n, gamma);
             if (!dl) C -= gamma * AA;
             ++steps;
@@ -408,10 +552,28 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
                 dropped = var;
                 ckl(cudaStreamSynchronize(st), "sync");
             }
+            if (dl && max_norm < 1.0e49) {   // the driver's --max_norm: keep the vertex before this step
+                cgd::k_lars_l1<<<1, cgd::LARS_THREADS, 0, st>>>(x, n, scal + 3);
+                double l1 = 0.0;
+                ckl(cudaMemcpyAsync(&l1, scal + 3, sizeof(double), cudaMemcpyDeviceToHost, st), "l1");
+                ckl(cudaStreamSynchronize(st), "sync");
+                if (l1 > max_norm) {
+                    ckl(cudaMemcpyAsync(x, xprev, sizeof(double) * n, cudaMemcpyDeviceToDevice, st), "revert");
+                    stopped_max_norm = true;
+                    break;
+                }
+            }
             ckl(cudaGetLastError(), "lars step");
         }
         ckl(cudaStreamSynchronize(st), "sync");
-        if (info) { info[0] = steps; info[1] = (double)active.size(); info[2] = dl ? last_obj : C / (double)nsamples; }
+        // iterations as the reference's driver counts them: it takes the step of the
+        // iteration that finds the objective risen before it stops (dlars.C:365-381)
+        if (info) {
+            info[0] = steps + (stopped_objective ? 1 : 0);
+            info[1] = (double)active.size();
+            info[2] = dl ? last_obj : C / (double)nsamples;
+        }
+        (void)stopped_max_norm;
     } catch (...) {
         for (void* p : mem) cudaFreeAsync(p, st);
         cudaStreamSynchronize(st);
@@ -421,7 +583,8 @@ void lars_lasso(const double* G, const double* h, int n, int64_t nsamples, doubl
 }
 
 void dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int n, int64_t nsamples,
-                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, cudaStream_t st) {
+                      double btb, double lambda, int lasso, int max_iter, double* x, double* info, cudaStream_t st,
+                      double max_norm, const char* restart_in, const char* restart_out) {
     double *Gc = nullptr, *hc = nullptr, *sigma = nullptr;
     int* bad = nullptr;
     ckl(cudaMallocAsync((void**)&Gc, sizeof(double) * (size_t)n * n, st), "normalised G");
@@ -442,7 +605,8 @@ void dlars_normalized(const double* G, const double* h, const double* colsum, do
         const int64_t nn = (int64_t)n * n;
         cgd::k_dlars_center<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(G, h, colsum, sigma, n, N, ybar, Gc, hc);
         ckl(cudaGetLastError(), "normalise");
-        lars_lasso(Gc, hc, n, nsamples, lambda, max_iter, x, info, st, lasso ? 2 : 1, btb - N * ybar * ybar);
+        lars_lasso(Gc, hc, n, nsamples, lambda, max_iter, x, info, st, lasso ? 2 : 1, btb - N * ybar * ybar, max_norm,
+                   restart_in, restart_out);
         cgd::k_dlars_unscale<<<(n + 255) / 256, 256, 0, st>>>(x, sigma, n);
         ckl(cudaGetLastError(), "unscale");
     } catch (...) {

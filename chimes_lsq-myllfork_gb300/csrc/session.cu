@@ -764,6 +764,12 @@ __global__ void k_weight_rows(const T* A, int64_t lda, int64_t nrows, int ncols,
 }
 }  // namespace
 
+int64_t Session::gram_plane_rows(int64_t nrows, int ncols) const {
+    const int64_t cpad = (ncols + 127) / 128 * 128;
+    const int64_t rows = gram_rows_per_launch_ > 0 ? gram_rows_per_launch_ : (int64_t)(1ull << 30) / (4 * cpad);
+    return std::min<int64_t>(nrows, std::max<int64_t>(64, rows));
+}
+
 void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
                    double* G, double* h, const double* w) {
     CK(cudaSetDevice(device_));
@@ -786,10 +792,7 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
     void* planes = nullptr;
     size_t pbytes = 0;
     if (mode == 1) {
-        const int64_t cpad = (ncols + 127) / 128 * 128;
-        // planes for up to 8 GiB of rows: the whole block of a large-column fit in one
-        // tensor-core launch (each launch re-walks every tile pair)
-        int64_t rb = std::min<int64_t>(nrows, std::max<int64_t>(64, (int64_t)(8ull << 30) / (4 * cpad)));
+        const int64_t rb = gram_plane_rows(nrows, ncols);
         pbytes = gram_plane_bytes(rb, ncols);
         planes = S.get<unsigned char>(pbytes);
     }
@@ -806,10 +809,12 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
 }
 
 void Session::lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter,
-                   double* x, double* info, int mode, double btb) {
+                   double* x, double* info, int mode, double btb, double max_norm, const char* restart_in,
+                   const char* restart_out) {
     CK(cudaSetDevice(device_));
     try {
-        lars_lasso(G, h, ncols, nsamples, alpha, max_iter, x, info, stream_, mode, btb);
+        lars_lasso(G, h, ncols, nsamples, alpha, max_iter, x, info, stream_, mode, btb, max_norm, restart_in,
+                   restart_out);
     } catch (const std::runtime_error& e) {
         throw Error(3, e.what());
     }
@@ -817,10 +822,11 @@ void Session::lars(const double* G, const double* h, int ncols, int64_t nsamples
 
 void Session::dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int ncols,
                                int64_t nsamples, double btb, double lambda, int lasso, int max_iter, double* x,
-                               double* info) {
+                               double* info, double max_norm, const char* restart_in, const char* restart_out) {
     CK(cudaSetDevice(device_));
     try {
-        cg::dlars_normalized(G, h, colsum, bsum, ncols, nsamples, btb, lambda, lasso, max_iter, x, info, stream_);
+        cg::dlars_normalized(G, h, colsum, bsum, ncols, nsamples, btb, lambda, lasso, max_iter, x, info, stream_,
+                             max_norm, restart_in, restart_out);
     } catch (const std::runtime_error& e) {
         throw Error(2, e.what());
     }
@@ -902,8 +908,10 @@ void Session::factor_solve(const double* L, int ncols, const double* h, double* 
 }
 
 namespace {
-// One pass over every row block: FP64 assembly into Ablk, t = (b -) A v (t *= w^2),
-// then out += A^T t, or (predict) t copied to y at the block's rows.
+// One pass over every row block: the block's FP64 rows (assembled again into Ablk,
+// or kept from an earlier pass in `kept`), t = (b -) A v (t *= w^2), then
+// out += A^T t.  Blocks are kept resident while the cache budget allows, so that
+// later passes assemble only the others.
 struct StreamRows {
     Session& se;
     int ncols;
@@ -913,16 +921,38 @@ struct StreamRows {
     const double *extra_A, *extra_b, *extra_w;
     int64_t extra_rows;
     double *Ablk, *t, *partial;
+    int64_t cache_left = 0;            // bytes still allowed for kept blocks
+    std::vector<double*> kept;         // per block: resident FP64 rows, or null
+    ~StreamRows() { for (double* p : kept) if (p) cudaFree(p); }
+    const double* rows_of(size_t k, cudaStream_t st) {
+        const DeviceFrames& d = *blocks[k];
+        if (kept.size() < blocks.size()) kept.resize(blocks.size(), nullptr);
+        if (kept[k]) return kept[k];
+        const int64_t bytes = d.nrows * (int64_t)ncols * (int64_t)sizeof(double);
+        if (bytes <= cache_left) {
+            double* p = nullptr;
+            if (cudaMalloc(&p, (size_t)bytes) == cudaSuccess) {
+                se.assemble(d, 0, p, ncols, nullptr);
+                kept[k] = p;
+                cache_left -= bytes;
+                return p;
+            }
+            cudaGetLastError();   // out of memory: assemble into the block buffer instead
+            cache_left = 0;
+        }
+        se.assemble(d, 0, Ablk, ncols, nullptr);
+        return Ablk;
+    }
     void pass(const double* v, bool resid, double* out, cudaStream_t st) {
         CK(cudaMemsetAsync(out, 0, sizeof(double) * ncols, st));
         for (size_t k = 0; k < blocks.size(); ++k) {
             const DeviceFrames& d = *blocks[k];
             if (d.nrows == 0) continue;
-            se.assemble(d, 0, Ablk, ncols, nullptr);
+            const double* Ak = rows_of(k, st);
             se.mark(ST_REFINE_PRODUCTS, true);
-            gemv_rows64(Ablk, ncols, d.nrows, ncols, v, resid ? labels[k] : nullptr,
+            gemv_rows64(Ak, ncols, d.nrows, ncols, v, resid ? labels[k] : nullptr,
                         weights.empty() ? nullptr : weights[k], t, st);
-            gemv_cols64(Ablk, ncols, d.nrows, ncols, t, out, partial, st);
+            gemv_cols64(Ak, ncols, d.nrows, ncols, t, out, partial, st);
             se.mark(ST_REFINE_PRODUCTS, false);
         }
         if (extra_rows > 0) {
@@ -947,6 +977,15 @@ void Session::refine_streamed(const double* L, int ncols, double ridge, const st
     StreamRows R{*this, ncols, blocks, labels, weights, extra_A, extra_b, extra_w, extra_rows,
                  S.get<double>((size_t)maxrows * ncols), S.get<double>(maxrows),
                  S.get<double>(atb_partial_doubles(maxrows, ncols))};
+    if (refine_cache_bytes_ < 0) {   // what is free now, less a margin for the assembly's own work lists
+        size_t fr = 0, tot = 0;
+        CK(cudaStreamSynchronize(stream_));
+        CK(cudaMemGetInfo(&fr, &tot));
+        const int64_t margin = (int64_t)(tot / 10) + 3 * (int64_t)maxrows * ncols * (int64_t)sizeof(double);
+        R.cache_left = std::max<int64_t>(0, (int64_t)fr - margin);
+    } else {
+        R.cache_left = refine_cache_bytes_;
+    }
     try {
         Fp64Operator op;
         op.apply = [&](const double* p, double* q) { R.pass(p, false, q, stream_); };
@@ -1029,8 +1068,7 @@ std::unique_ptr<BatchFit> Session::batch_fit_graph(const std::vector<const Devic
     const int ncols = m.tot_all;
     int64_t maxrows = 1;
     for (const DeviceFrames* d : blocks) maxrows = std::max<int64_t>(maxrows, d->nrows);
-    const int64_t cpad = (ncols + 127) / 128 * 128;
-    const int64_t rb = std::min<int64_t>(maxrows, std::max<int64_t>(64, (int64_t)(8ull << 30) / (4 * cpad)));
+    const int64_t rb = gram_plane_rows(maxrows, ncols);
     const size_t pbytes = gram_plane_bytes(rb, ncols);
     CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
     try {

@@ -252,15 +252,25 @@ class Session {
                                               int64_t lda, double* G, double* h);
     void batch_fit_launch(BatchFit& bf);
     void set_gram_ctas_per_sm(int v) { gram_ctas_per_sm_ = v > 0 ? v : 4; }
+    // Rows of A per tensor-core Gram launch (0: the default of about 1 GiB of BF16
+    // planes).  Each launch sums its rows in FP32 before adding into the FP64 G, so
+    // the accumulation error grows with this length (diagonal entries linearly).
+    void set_gram_rows_per_launch(int64_t v) { gram_rows_per_launch_ = v > 0 ? v : 0; }
+    // Bytes of FP64 row blocks the streamed refinement may keep resident between
+    // passes (-1: what the device has free beyond a margin; 0: none).
+    void set_refine_cache_bytes(int64_t v) { refine_cache_bytes_ = v; }
     int gram_ctas_per_sm() const { return gram_ctas_per_sm_; }
     // Measured FP64 FMA rate of the session's GPU in TFLOP/s (dense64.cu).
     double fp64_fma_tflops();
     // LARS-lasso on the normal equations (lars.cu).
     void lars(const double* G, const double* h, int ncols, int64_t nsamples, double alpha, int max_iter, double* x,
-              double* info, int mode = 0, double btb = 0.0);
+              double* info, int mode = 0, double btb = 0.0, double max_norm = 1.0e50, const char* restart_in = nullptr,
+              const char* restart_out = nullptr);
     // DLARS with column normalisation (colsum = A^T 1 on the device, bsum = sum b).
     void dlars_normalized(const double* G, const double* h, const double* colsum, double bsum, int ncols,
-                          int64_t nsamples, double btb, double lambda, int lasso, int max_iter, double* x, double* info);
+                          int64_t nsamples, double btb, double lambda, int lasso, int max_iter, double* x, double* info,
+                          double max_norm = 1.0e50, const char* restart_in = nullptr,
+                          const char* restart_out = nullptr);
 
     // MD force (md.h / md_host.cu).  md_setup stores the coefficients x (one per A
     // column): offsets adds the per-atom-type energy offsets of an energy fit.
@@ -349,6 +359,9 @@ class Session {
     std::unique_ptr<DeviceModel> dm_;
     std::unique_ptr<MdTables> md_;
     int gram_ctas_per_sm_ = 4;
+    int64_t gram_rows_per_launch_ = 0;
+    int64_t refine_cache_bytes_ = -1;
+    int64_t gram_plane_rows(int64_t nrows, int ncols) const;
     double md_skin_ = 0.5;   // Angstrom; 0: enumerate every step
     double serve_list_per_atom_ = 6144.0;   // list bytes per atom (measured by md_serve)
     std::vector<double> md_state_;   // last md_run: nframes * MD_TH_STRIDE

@@ -284,6 +284,21 @@ int cg_lars(cg_session* s, const double* G, const double* h, int ncols, int64_t 
 int cg_dlars(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double btb, double lambda,
              int lasso, const double* colsum, double bsum, int max_iter, double* x, double* info);
 
+/* cg_dlars with the reference DLARS driver's stopping and restart options
+ * (contrib/dlars/src/dlars.C:96-100, 356-420, DLARS::print_restart / restart
+ * :1543-2221): max_iter = --iterations; max_norm (> 0; 0 = none) = --max_norm: the
+ * walk stops once the L1 norm of the coefficients after a step exceeds it and returns
+ * the vertex before that step; restart_out (NULL = none) receives the walk's state
+ * every ten iterations (iteration count, objective, coefficients, active set in entry
+ * order, excluded variables, the variable named to enter next) and restart_in (NULL
+ * = none) resumes a walk from such a file -- the active-set Cholesky factor is rebuilt
+ * from G, so a resumed walk follows the uninterrupted one to rounding.  The file is
+ * this library's text format, not the reference's restart.txt.  With colsum the
+ * coefficients of the file are those of the normalised problem, as in the reference. */
+int cg_dlars_ex(cg_session* s, const double* G, const double* h, int ncols, int64_t nsamples, double btb,
+                double lambda, int lasso, const double* colsum, double bsum, int max_iter, double max_norm,
+                const char* restart_in, const char* restart_out, double* x, double* info);
+
 /* Work counters of the last assembly: accepted 2-body pairs, triplets, quadruplets,
  * and (cluster, allowed-power) evaluations of the 3- and 4-body terms. */
 int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplets, int64_t* quads,
@@ -492,7 +507,13 @@ void cg_batch_fit_free(cg_batch_fit* b);
  * chimes_lsq-myllfork_gb300/autotune.py): "gram_ctas_per_sm" (CTAs per SM the
  * tensor-core Gram aims for when it slices K; default 4); "md_skin_milli" (the
  * neighbour-list skin of cg_md_nve / cg_md_serve in 1e-3 A, default 500; 0 =
- * enumerate every step; lists are rebuilt when an atom has moved half the skin). */
+ * enumerate every step; lists are rebuilt when an atom has moved half the skin);
+ * "gram_rows_per_launch" (rows of A summed in FP32 per tensor-core Gram launch before
+ * they are added into the FP64 G; 0 = about 1 GiB of BF16 planes -- longer runs are
+ * faster but their FP32 sums lose accuracy, which costs refinement passes);
+ * "refine_cache_mb" (device memory the streamed refinement may fill with FP64 row
+ * blocks kept between passes, in MiB; -1 = what is free beyond a margin, the
+ * default; 0 = assemble every block on every pass). */
 int cg_session_tune(cg_session* s, const char* key, int value);
 
 const char* cg_last_error(void);

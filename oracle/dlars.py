@@ -26,9 +26,12 @@ normal equations (G, h, b^T b, n) are needed.
 import numpy as np
 
 
-def dlars(G, h, btb, n, lam, lasso, max_iter=10000000):
+def dlars(G, h, btb, n, lam, lasso, max_iter=10000000, max_norm=1.0e50):
     """Returns (beta, iterations, stop) for DLARS `--algorithm lars` (lasso False)
-    or `lasso` (lasso True) with `--lambda lam`, `--normalize n`."""
+    or `lasso` (lasso True) with `--lambda lam`, `--normalize n`, `--iterations
+    max_iter` and `--max_norm max_norm` (the driver stops once the L1 norm of the
+    coefficients after a step exceeds it and keeps the vertex before that step,
+    contrib/dlars/src/dlars.C:376-381)."""
     G = np.asarray(G, dtype=np.float64)
     h = np.asarray(h, dtype=np.float64)
     p = G.shape[0]
@@ -94,6 +97,9 @@ def dlars(G, h, btb, n, lam, lasso, max_iter=10000000):
             beta[A[remove_prop]] = 0.0
         c = c - g * a
         it += 1
+        if np.abs(beta).sum() > max_norm:
+            stop = "max norm"
+            break
         if obj > last_obj + 1.0e-10:
             stop = "objective increased"
             break
@@ -102,7 +108,7 @@ def dlars(G, h, btb, n, lam, lasso, max_iter=10000000):
     return last_beta, it, stop
 
 
-def dlars_normalized(G, h, colsum, bsum, btb, n, lam, lasso, max_iter=10000000):
+def dlars_normalized(G, h, colsum, bsum, btb, n, lam, lasso, max_iter=10000000, max_norm=1.0e50):
     """DLARS with --normalize=y (Matrix::normalize / Vector::normalize,
     contrib/dlars/src/Matrix.h:614-660, Vector.h:140-150; print_unscaled
     dlars.C:2073-2097): columns centred and scaled to unit norm, b centred;
@@ -115,5 +121,5 @@ def dlars_normalized(G, h, colsum, bsum, btb, n, lam, lasso, max_iter=10000000):
         raise ValueError("a column of A is constant: its normalisation scale is 0")
     Gc = (G - n * np.outer(mu, mu)) / np.outer(sig, sig)
     hc = (np.asarray(h) - ybar * np.asarray(colsum)) / sig
-    beta, it, stop = dlars(Gc, hc, btb - n * ybar * ybar, n, lam, lasso, max_iter)
+    beta, it, stop = dlars(Gc, hc, btb - n * ybar * ybar, n, lam, lasso, max_iter, max_norm)
     return beta / sig, it, stop

@@ -104,3 +104,27 @@ def test_oracle_dlars_normalized_matches_reference_lsq2_output():
     assert stop == "objective increased"
     assert np.array_equal(x != 0, ref != 0)
     assert np.abs(x - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def _dlars64():
+    import os
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "dlars64", "dlars64.npz"))
+    X, y = d["X"], d["y"]
+    return d, X.T @ X, X.T @ y, X.sum(0), float(y.sum()), float(y @ y), X.shape[0]
+
+
+@pytest.mark.parametrize("case", ["lars", "lasso", "maxnorm", "lambda", "iters"])
+def test_dlars_restatement_matches_reference_test_suite(case):
+    """The reference DLARS's own 64 x 32 test problem (contrib/dlars/tests, --normalize=y)
+    with its --algorithm, --max_norm=20, --lambda=5e-3 and --iterations=10 runs: the
+    final coefficients it printed (13 significant digits) and its iteration count."""
+    import dlars
+    d, G, h, colsum, bsum, btb, n = _dlars64()
+    lasso, lam, mn, its = d[case + "_params"]
+    x, it, stop = dlars.dlars_normalized(G, h, colsum, bsum, btb, n, lam, bool(lasso), int(its), mn)
+    mu = colsum / n
+    sig = np.sqrt(np.diag(G) - n * mu * mu)
+    ref = d[case + "_beta"]
+    assert np.abs(x * sig - ref).max() <= 1e-11 * np.abs(ref).max()
+    assert it == int(d[case + "_iterations"])
