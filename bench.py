@@ -326,7 +326,8 @@ def batched_bench(cg, local, nframes, timer, torch, eager_blocks=4, per_frame_sa
     choice, trials = autotune.tune_batch(cg, sess, frames, sizes, block_candidates=(16, 32, 64), sample_frames=64,
                                          repeats=1, torch=torch)
     tune_s = time.perf_counter() - t0
-    sess.tune("gram_ctas_per_sm", choice["gram_ctas_per_sm"])
+    for k in ("gram_ctas_per_sm", "force4_threads", "gram_rows_per_launch"):
+        sess.tune(k, choice[k])
     bf = choice["block_frames"]
     blocks = [frames.slice(f0, min(bf, nframes - f0)) for f0 in range(0, nframes, bf)]
     rows = sum(b.nrows for b in blocks)

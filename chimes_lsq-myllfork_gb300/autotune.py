@@ -2,11 +2,15 @@
 
 Tunes, on a sample of the batch's own frames, (a) the frames per row block (the
 A buffer a block is assembled into and the K extent of each tensor-core Gram
-launch) and (b) the CTAs per SM the Gram aims for when it slices K (which only
-matters when the column count is small).  Each candidate is built as the real
-graph (sizing pass, capture) and timed with CUDA events on the session stream
-over repeated launches; the fastest rows/s wins.  Choices are cached in a JSON
-file keyed by the column count and the sample's mean frame size.
+launch), (b) the CTAs per SM the Gram aims for when it slices K (which only
+matters when the column count is small), (c) the threads per CTA of the 4-body
+force-row kernel (512 or 1024: one CTA per SM either way, shared memory bound) and
+(d) the rows of A each tensor-core Gram launch sums in FP32 (longer is faster, but
+the FP32 sums lose accuracy; only lengths up to the accuracy limit are offered).
+Each candidate is built as the real graph (sizing pass, capture) and timed with
+CUDA events on the session stream over repeated launches; the fastest rows/s wins.
+Choices are cached in a JSON file keyed by the column count and the sample's mean
+frame size.
 """
 import json
 import os
@@ -18,7 +22,8 @@ def _key(ncols, mean_atoms):
 
 
 def tune_batch(cg, sess, frames, natoms, a_precision=1, block_candidates=(16, 32, 64), ctas_candidates=(4,),
-               sample_frames=64, repeats=2, cache=None, torch=None):
+               sample_frames=64, repeats=2, cache=None, torch=None, force4_candidates=(512, 1024),
+               gram_rows_candidates=(0,)):
     """Returns (best dict, all trials).  frames: a cg.Frames batch; natoms: its
     per-frame atom counts (for the cache key)."""
     import numpy as np
@@ -45,27 +50,32 @@ def tune_batch(cg, sess, frames, natoms, a_precision=1, block_candidates=(16, 32
         dfs = [sess.upload(b) for b in blocks]
         labels = [torch.from_numpy(b.labels()).cuda() for b in blocks]
         for ctas in ctas_candidates:
-            sess.tune("gram_ctas_per_sm", ctas)
-            t0 = time.perf_counter()
-            g = sess.batch_fit(dfs, [l.data_ptr() for l in labels], a_precision, A.data_ptr(), ncols, G.data_ptr(),
-                               h.data_ptr())
-            build_s = time.perf_counter() - t0
-            g.launch()   # warm
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(repeats):
-                g.launch()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / repeats
-            trials.append({"block_frames": bf, "gram_ctas_per_sm": ctas, "rows_per_s": rows / (ms / 1e3),
-                           "ms": ms, "graph_nodes": g.nodes, "build_s": build_s})
-            del g
+            for nt4 in force4_candidates:
+                for grl in gram_rows_candidates:
+                    sess.tune("gram_ctas_per_sm", ctas)
+                    sess.tune("force4_threads", nt4)
+                    sess.tune("gram_rows_per_launch", grl)
+                    t0 = time.perf_counter()
+                    g = sess.batch_fit(dfs, [l.data_ptr() for l in labels], a_precision, A.data_ptr(), ncols,
+                                       G.data_ptr(), h.data_ptr())
+                    build_s = time.perf_counter() - t0
+                    g.launch()   # warm
+                    torch.cuda.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    for _ in range(repeats):
+                        g.launch()
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    ms = e0.elapsed_time(e1) / repeats
+                    trials.append({"block_frames": bf, "gram_ctas_per_sm": ctas, "force4_threads": nt4,
+                                   "gram_rows_per_launch": grl, "rows_per_s": rows / (ms / 1e3), "ms": ms,
+                                   "graph_nodes": g.nodes, "build_s": build_s})
+                    del g
         del A, G, h, dfs, labels
         torch.cuda.empty_cache()
     best = max(trials, key=lambda t: t["rows_per_s"])
-    choice = {"block_frames": best["block_frames"], "gram_ctas_per_sm": best["gram_ctas_per_sm"]}
+    choice = {k: best[k] for k in ("block_frames", "gram_ctas_per_sm", "force4_threads", "gram_rows_per_launch")}
     if cache:
         data = json.load(open(cache)) if os.path.exists(cache) else {}
         data[key] = choice

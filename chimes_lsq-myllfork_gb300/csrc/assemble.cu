@@ -248,8 +248,10 @@ __global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t ld
 // ---------------------------------------------------------------- many-body force rows
 // One CTA per real (owner) atom.  PPT powers per thread cover every allowed power
 // tuple of the largest cluster type, so the accumulators stay in registers.
-template <int NBODY, typename R, int PPT>
-__global__ void __launch_bounds__(MB_THREADS, NBODY == 3 ? (sizeof(R) == 4 ? 3 : 2) : 1) k_force_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
+// NT threads per CTA: MB_THREADS, or twice that for the 4-body kernel, whose one CTA
+// per SM (shared-memory bound) then keeps 32 warps issuing instead of 16.
+template <int NBODY, typename R, int PPT, int NT = MB_THREADS>
+__global__ void __launch_bounds__(NT, NBODY == 3 ? (sizeof(R) == 4 ? 3 : 2) : 1) k_force_mb(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
                                                          const int64_t* key_frame_ofs, const R* __restrict__ pre,
                                                          R* A, int64_t lda) {
     constexpr int NP = NBODY == 3 ? 3 : 6;
@@ -748,13 +750,17 @@ void launch_cluster_basis(int nbody, int prec, int64_t nq, const ModelDev& M, co
 
 template <int NBD, typename R>
 static void force_mb_ppt(int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS,
-                         const Buckets& inc, const int64_t* kfo, const R* pre, R* A, int64_t lda, cudaStream_t st) {
+                         const Buckets& inc, const int64_t* kfo, const R* pre, R* A, int64_t lda, cudaStream_t st,
+                         int nt4) {
     if (ppt <= 1) {
         set_smem(k_force_mb<NBD, R, 1>, smem);
         k_force_mb<NBD, R, 1><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
     } else if (ppt <= 2) {
         set_smem(k_force_mb<NBD, R, 2>, smem);
         k_force_mb<NBD, R, 2><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
+    } else if (NBD == 4 && nt4 == 2 * MB_THREADS) {   // up to 8 powers per thread at MB_THREADS = 4 at twice the threads
+        set_smem(k_force_mb<NBD, R, 4, 2 * MB_THREADS>, smem);
+        k_force_mb<NBD, R, 4, 2 * MB_THREADS><<<nreal, 2 * MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
     } else {
         set_smem(k_force_mb<NBD, R, 8>, smem);
         k_force_mb<NBD, R, 8><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
@@ -763,15 +769,15 @@ static void force_mb_ppt(int ppt, int nreal, size_t smem, const ModelDev& M, con
 
 void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,
                      const ClusterSet& CS, const Buckets& inc, const int64_t* kfo, const void* pre, void* A,
-                     int64_t lda, cudaStream_t st) {
+                     int64_t lda, cudaStream_t st, int nt4) {
     if (nbody == 3 && prec == 0)
-        force_mb_ppt<3, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (const double*)pre, (double*)A, lda, st);
+        force_mb_ppt<3, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (const double*)pre, (double*)A, lda, st, nt4);
     else if (nbody == 3)
-        force_mb_ppt<3, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st);
+        force_mb_ppt<3, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st, nt4);
     else if (prec == 0)
-        force_mb_ppt<4, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (const double*)pre, (double*)A, lda, st);
+        force_mb_ppt<4, double>(ppt, nreal, smem, M, F, CS, inc, kfo, (const double*)pre, (double*)A, lda, st, nt4);
     else
-        force_mb_ppt<4, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st);
+        force_mb_ppt<4, float>(ppt, nreal, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st, nt4);
 }
 
 template <int NBD, typename R, int PPT>

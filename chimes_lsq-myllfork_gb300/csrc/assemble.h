@@ -93,10 +93,12 @@ void launch_virial2(int prec, int nframes, const ModelDev& M, const FramesDev& F
 size_t cluster_basis_count(int nbody, int ord, int64_t nclusters);
 void launch_cluster_basis(int nbody, int prec, int64_t nclusters, const ModelDev& M, const FramesDev& F,
                           const ClusterSet& CS, void* basis, cudaStream_t st);
-// pre: the cluster bases above, or nullptr to evaluate them in the kernel.
+// pre: the cluster bases above, or nullptr to evaluate them in the kernel.  nt4:
+// threads per CTA of the 4-body kernel when it needs more than two powers per thread
+// (MB_THREADS or 2 * MB_THREADS).
 void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,
                      const ClusterSet& CS, const Buckets& inc, const int64_t* key_frame_ofs, const void* pre,
-                     void* A, int64_t lda, cudaStream_t st);
+                     void* A, int64_t lda, cudaStream_t st, int nt4 = MB_THREADS);
 // Stress/energy rows: nchunks_max cluster chunks of VIR_CLUSTERS per (frame, type);
 // part holds nframes*ntypes*nchunks_max*7*ntrue_max partial sums (R).
 // ppt: powers per thread, 1 when every cluster type has at most MB_THREADS allowed

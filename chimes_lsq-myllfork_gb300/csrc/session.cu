@@ -693,7 +693,8 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
             pre = prec == 0 ? (void*)S.get<double>(nbasis) : (void*)S.get<float>(nbasis);
             cgd::launch_cluster_basis(nbody, prec, nq, M, F, CS, pre, st); L();
         }
-        cgd::launch_force_mb(nbody, prec, pp, nreal, Lf.total, M, F, CS, inc, kfo_atoms, pre, A, lda, st); L();
+        cgd::launch_force_mb(nbody, prec, pp, nreal, Lf.total, M, F, CS, inc, kfo_atoms, pre, A, lda, st,
+                             force4_threads_); L();
         mark(nbody == 3 ? ST_FORCE3 : ST_FORCE4, false);
         CK(cudaGetLastError());
         if (virial) {

@@ -259,6 +259,8 @@ class Session {
     // Bytes of FP64 row blocks the streamed refinement may keep resident between
     // passes (-1: what the device has free beyond a margin; 0: none).
     void set_refine_cache_bytes(int64_t v) { refine_cache_bytes_ = v; }
+    // Threads per CTA of the 4-body force kernel (512 or 1024).
+    void set_force4_threads(int v) { force4_threads_ = v == 1024 ? 1024 : 512; }
     int gram_ctas_per_sm() const { return gram_ctas_per_sm_; }
     // Measured FP64 FMA rate of the session's GPU in TFLOP/s (dense64.cu).
     double fp64_fma_tflops();
@@ -361,6 +363,7 @@ class Session {
     int gram_ctas_per_sm_ = 4;
     int64_t gram_rows_per_launch_ = 0;
     int64_t refine_cache_bytes_ = -1;
+    int force4_threads_ = 512;
     int64_t gram_plane_rows(int64_t nrows, int ncols) const;
     double md_skin_ = 0.5;   // Angstrom; 0: enumerate every step
     double serve_list_per_atom_ = 6144.0;   // list bytes per atom (measured by md_serve)

@@ -513,7 +513,8 @@ void cg_batch_fit_free(cg_batch_fit* b);
  * faster but their FP32 sums lose accuracy, which costs refinement passes);
  * "refine_cache_mb" (device memory the streamed refinement may fill with FP64 row
  * blocks kept between passes, in MiB; -1 = what is free beyond a margin, the
- * default; 0 = assemble every block on every pass). */
+ * default; 0 = assemble every block on every pass); "force4_threads" (threads per CTA
+ * of the 4-body force-row kernel, 512 or 1024). */
 int cg_session_tune(cg_session* s, const char* key, int value);
 
 const char* cg_last_error(void);

@@ -90,15 +90,23 @@ def test_water3b_matches_oracle(cg, oracle, session_for, tmp_path_factory):
     assert c["triplets"] > 0
 
 
-def test_chno4b_matches_oracle(cg, oracle, session_for, tmp_path_factory):
+@pytest.mark.parametrize("threads", [512, 1024])
+def test_chno4b_matches_oracle(cg, oracle, tmp_path_factory, threads):
+    """The full 4-body basis (3,861 allowed powers per quadruplet type) with either
+    launch shape of the 4-body force-row kernel."""
     fm = _workload(tmp_path_factory, cg, "chno-4b", 1, 202)
-    model, sess = session_for(fm)
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.tune("force4_threads", threads)
     frames = cg.Frames.read(model)
     A = sess.assemble(frames, cg.CG_FP64)
     O, _ = oracle.assemble(fm, nthreads=8)
     assert A.shape == O.shape == (780, 51209)
     ok, err = close_fp64(A, O)
     assert ok, f"max |gpu - oracle| = {err}"
+    A32 = sess.assemble(frames, cg.CG_FP32).astype(np.float64)
+    colmax = np.abs(O).max(axis=0) + 1e-300
+    assert (np.abs(A32 - O) / colmax[None, :]).max() < 2e-5
 
 
 def test_force_rows_sum_to_zero(cg, session_for, tmp_path_factory):
