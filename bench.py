@@ -577,7 +577,20 @@ def main():
     for _ in range(e2e_steps):
         sess.assemble_stream(frames, cg.CG_FP64, sink, block_frames=10)
     e2e_s = time.perf_counter() - t0
+    # the host link's device-to-host rate in this run (pinned destination), the
+    # ceiling of the streamed call
+    link = torch.empty(1 << 29, dtype=torch.float64, device="cuda")
+    pin = torch.empty(1 << 29, dtype=torch.float64, pin_memory=True)
+    pin.copy_(link, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        pin.copy_(link, non_blocking=True)
+    torch.cuda.synchronize()
+    link_gbs = 3 * link.numel() * 8 / (time.perf_counter() - t0) / 1e9
+    del link, pin
     e2e = {"value": world * nrows * e2e_steps / e2e_s, "unit": "rows/s", "steps": e2e_steps,
+           "d2h_link_gbs_measured": link_gbs, "d2h_gbs_achieved": nrows * C * 8 * e2e_steps / e2e_s / 1e9,
            "h2d_bytes_per_step": int(natoms * (3 * 8 + 4) + args.frames * (4 + 3 * 8 + 2 * 4 + 208)),
            "d2h_bytes_per_step": int(nrows * C * 8),
            "call": "cg_assemble_stream (FP64, blocks of 10 frames, pinned double buffer, no-op sink)"}

@@ -562,9 +562,29 @@ double fp64_fma_tflops(cudaStream_t st) {
     run(cgd::k_fp64_fma<16>, 16, 4);
     run(cgd::k_fp64_fma<32>, 32, 4);
     run(cgd::k_fp64_fma<32>, 32, 2);
+    ckd(cudaFreeAsync(out, st), "peak scratch free");
+    {   // and the register-blocked SYRK of this file on a 2048 x 4096 operand (FMA bound)
+        const int K = 2048, m = 4096;
+        double *X = nullptr, *C = nullptr;
+        ckd(cudaMallocAsync((void**)&X, sizeof(double) * K * m, st), "peak scratch");
+        ckd(cudaMallocAsync((void**)&C, sizeof(double) * m * m, st), "peak scratch");
+        ckd(cudaMemsetAsync(X, 0, sizeof(double) * K * m, st), "peak scratch");   // finite operands
+        ckd(cudaMemsetAsync(C, 0, sizeof(double) * m * m, st), "peak scratch");
+        syrk_tn(X, m, K, m, 1.0, C, m, st);   // warm-up
+        for (int rep = 0; rep < 3; ++rep) {
+            ckd(cudaEventRecord(e0, st), "record");
+            syrk_tn(X, m, K, m, 1.0, C, m, st);
+            ckd(cudaEventRecord(e1, st), "record");
+            ckd(cudaEventSynchronize(e1), "sync");
+            float ms = 0.f;
+            ckd(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            best = std::max(best, (double)K * m * (m + 1.0) / (ms * 1e-3) / 1e12);
+        }
+        ckd(cudaFreeAsync(X, st), "peak scratch free");
+        ckd(cudaFreeAsync(C, st), "peak scratch free");
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    ckd(cudaFreeAsync(out, st), "peak scratch free");
     ckd(cudaStreamSynchronize(st), "sync");
     return best;
 }

@@ -51,9 +51,10 @@ void axpby64(int n, double a, const double* x, double b, double* y, cudaStream_t
 // G[i][i] += v
 void add_diag64(double* G, int n, double v, cudaStream_t st);
 
-// Measured FP64 FMA rate of the current device (TFLOP/s, 2 flops per FMA): a kernel
-// of independent FMA chains on every SM, timed with CUDA events.  Changes no
-// device setting.
+// Measured FP64 FMA rate of the current device (TFLOP/s, 2 flops per FMA): the
+// better of a kernel of independent FMA chains on every SM and this file's
+// register-blocked SYRK on a 2048 x 4096 operand, timed with CUDA events.  Changes
+// no device setting.
 double fp64_fma_tflops(cudaStream_t st);
 
 }  // namespace cg
