@@ -312,12 +312,18 @@ int cg_assemble_device_noalloc(cg_session* s, const cg_dframes* d, int precision
     });
 }
 
-// Frames per block of a streamed assembly: about 1 GiB of A per block, at least one
-// frame, and at least two blocks when the batch has two frames (so copies overlap).
-static int auto_block_frames(const cg::FrameBatch& fb, int64_t lda, size_t rsz) {
+// Frames per block of a streamed assembly: about 8 GiB of A per block (smaller
+// blocks lose device efficiency to per-block list sizing), at most an eighth of the
+// device's free memory (two blocks are resident), at least one frame, and at least
+// two blocks when the batch has two frames (so copies overlap).
+static int auto_block_frames(int device, const cg::FrameBatch& fb, int64_t lda, size_t rsz) {
     if (fb.nframes <= 1) return 1;
+    size_t free_b = 0, total_b = 0;
+    cudaSetDevice(device);
+    double target = double(size_t(8) << 30);
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) target = std::min(target, (double)free_b / 8.0);
     const double bytes_per_frame = (double)fb.nrows / fb.nframes * (double)lda * (double)rsz;
-    int bf = (int)std::max(1.0, (double)(1u << 30) / std::max(1.0, bytes_per_frame));
+    int bf = (int)std::max(1.0, target / std::max(1.0, bytes_per_frame));
     return std::max(1, std::min(bf, (fb.nframes + 1) / 2));
 }
 
@@ -328,7 +334,7 @@ int cg_assemble(cg_session* s, const cg_frames* fr, int precision, void* A, int6
         const size_t rsz = precision == CG_FP64 ? 8 : 4;
         char* base = static_cast<char*>(A);
         s->s->assemble_to_host(
-            fr->fb, precision, auto_block_frames(fr->fb, lda, rsz), lda,
+            fr->fb, precision, auto_block_frames(s->s->device(), fr->fb, lda, rsz), lda,
             [&](int64_t first, int64_t) -> void* { return base + (size_t)first * lda * rsz; },
             [](int64_t, int64_t, const void*) { return true; }, &s->last);
     });
@@ -342,7 +348,7 @@ int cg_assemble_stream(cg_session* s, const cg_frames* fr, int precision, int bl
         need(block_frames >= 0, "block_frames");
         const size_t rsz = precision == CG_FP64 ? 8 : 4;
         const int64_t lda = s->s->model().tot_all;
-        const int bf = block_frames > 0 ? block_frames : auto_block_frames(fr->fb, lda, rsz);
+        const int bf = block_frames > 0 ? block_frames : auto_block_frames(s->s->device(), fr->fb, lda, rsz);
         int64_t maxrows = 1;
         for (int f0 = 0; f0 < fr->fb.nframes; f0 += bf) {
             const int f1 = std::min(fr->fb.nframes, f0 + bf);

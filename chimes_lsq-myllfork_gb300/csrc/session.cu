@@ -377,6 +377,7 @@ Session::~Session() {
     if (side_stream_) cudaStreamDestroy(side_stream_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
     for (void* p : pinned_) if (p) cudaFreeHost(p);
+    if (mailbox_host_) cudaFreeHost(mailbox_host_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -457,6 +458,46 @@ void Session::assemble(const DeviceFrames& df, int precision, void* A, int64_t l
     CK(cudaSetDevice(device_));
     Scratch S(stream_);
     run(df, precision, A, lda, stats, S, nullptr, nullptr);
+}
+
+namespace {
+constexpr int kMailboxBytes = 256;
+struct PeekList {
+    const void* src[4];
+    int bytes[4];
+    int n;
+};
+__global__ void k_peek(PeekList L, unsigned char* dst) {
+    int off = 0;
+    for (int i = 0; i < L.n; ++i) {
+        const unsigned char* s = static_cast<const unsigned char*>(L.src[i]);
+        for (int b = 0; b < L.bytes[i]; ++b) dst[off + b] = s[b];
+        off += L.bytes[i];
+    }
+}
+}  // namespace
+
+void Session::peek(cudaStream_t st, std::initializer_list<PeekItem> items) {
+    if (!mailbox_host_) {
+        CK(cudaHostAlloc((void**)&mailbox_host_, kMailboxBytes, cudaHostAllocMapped));
+        CK(cudaHostGetDevicePointer((void**)&mailbox_dev_, mailbox_host_, 0));
+    }
+    PeekList L{};
+    int total = 0;
+    for (const PeekItem& it : items) {
+        if (L.n == 4 || it.bytes < 0 || total + it.bytes > kMailboxBytes) throw Error(1, "peek list too large");
+        L.src[L.n] = it.dev;
+        L.bytes[L.n++] = it.bytes;
+        total += it.bytes;
+    }
+    k_peek<<<1, 1, 0, st>>>(L, mailbox_dev_);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    int off = 0;
+    for (const PeekItem& it : items) {
+        std::memcpy(it.host, mailbox_host_ + off, it.bytes);
+        off += it.bytes;
+    }
 }
 
 void* Session::pinned(int i, size_t bytes) {
@@ -587,10 +628,7 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
     if (plan_in) {   // sizes known from an earlier pass: no host synchronisation (capturable)
         for (int k = 0; k < 3; ++k) tot[k] = plan_in->tot[k];
     } else {
-        CK(cudaMemcpyAsync(&tot[0], NB.ofs2 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&tot[1], NB.ofs3 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&tot[2], NB.ofs4 + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        peek(st, {{&tot[0], NB.ofs2 + nreal, 8}, {&tot[1], NB.ofs3 + nreal, 8}, {&tot[2], NB.ofs4 + nreal, 8}});
     }
     if (plan_out) for (int k = 0; k < 3; ++k) plan_out->tot[k] = tot[k];
     NB.i2 = S.get<int>(tot[0]); NB.g2 = S.get<int>(tot[0]); NB.pt2 = S.get<int>(tot[0]);
@@ -614,8 +652,7 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
         if (plan_in) {
             n = plan_in->ncl[nbody - 3];
         } else {
-            CK(cudaMemcpyAsync(&n, CS.ofs + nreal, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
+            peek(st, {{&n, CS.ofs + nreal, 8}});
         }
         if (plan_out) plan_out->ncl[nbody - 3] = n;
         CS.m = S.get<int4>(n);
@@ -708,8 +745,7 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
             if (plan_in) {
                 hmax = plan_in->hmax[nbody - 3];
             } else {
-                CK(cudaMemcpyAsync(&hmax, d_max, sizeof(int), cudaMemcpyDeviceToHost, st));
-                CK(cudaStreamSynchronize(st));
+                peek(st, {{&hmax, d_max, 4}});
             }
             if (plan_out) plan_out->hmax[nbody - 3] = hmax;
             const int nch = std::max(1, (hmax + cgd::VIR_CLUSTERS - 1) / cgd::VIR_CLUSTERS);
@@ -741,8 +777,7 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
     }
     if (stats && !plan_in) {
         unsigned long long ev[2] = {0, 0};
-        CK(cudaMemcpyAsync(ev, d_evals, sizeof(ev), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        peek(st, {{ev, d_evals, (int)sizeof(ev)}});
         stats->pairs2 = tot[0]; stats->list3 = tot[1]; stats->list4 = tot[2];
         stats->triplets = n3; stats->quads = n4;
         stats->power_evals3 = (int64_t)ev[0]; stats->power_evals4 = (int64_t)ev[1];
@@ -804,8 +839,7 @@ void Session::gram(int prec_in, const void* A, int64_t lda, int64_t nrows, int n
         throw Error(3, e.what());
     }
     int herr = 0;
-    CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream_));
-    CK(cudaStreamSynchronize(stream_));
+    peek(stream_, {{&herr, d_err, 4}});
     if (herr) throw Error(3, "tensor-core Gram kernel timed out waiting on its pipeline (code " + std::to_string(herr) + ")");
 }
 

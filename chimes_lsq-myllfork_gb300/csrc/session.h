@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <functional>
+#include <initializer_list>
 #include <memory>
 #include <string>
 #include <vector>
@@ -262,6 +263,7 @@ class Session {
     // Threads per CTA of the 4-body force kernel (512 or 1024).
     void set_force4_threads(int v) { force4_threads_ = v == 1024 ? 1024 : 512; }
     int gram_ctas_per_sm() const { return gram_ctas_per_sm_; }
+    int device() const { return device_; }
     // Measured FP64 FMA rate of the session's GPU in TFLOP/s (dense64.cu).
     double fp64_fma_tflops();
     // LARS-lasso on the normal equations (lars.cu).
@@ -338,6 +340,12 @@ class Session {
     void stage_totals(double* ms, int64_t* calls);   // syncs pending events, accumulates, returns totals
     void reset_stage_totals();
     void mark(int stage, bool begin);
+    // Host reads of a few device bytes (sizes, error words) ordered on stream st: a
+    // one-thread kernel stores them into mapped pinned memory, then the host waits
+    // for st.  A copy-engine read would queue behind a large block copy on the copy
+    // stream and serialise the assembly with it.  At most 256 bytes per call.
+    struct PeekItem { void* host; const void* dev; int bytes; };
+    void peek(cudaStream_t st, std::initializer_list<PeekItem> items);
 
    private:
     void run(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats, struct Scratch& S,
@@ -357,6 +365,8 @@ class Session {
     cudaStream_t copy_stream_ = nullptr;   // device-to-host copies of streamed assemblies
     void* pinned_[2] = {nullptr, nullptr};
     size_t pinned_bytes_[2] = {0, 0};
+    unsigned char* mailbox_host_ = nullptr;   // mapped pinned bytes written by peek()
+    unsigned char* mailbox_dev_ = nullptr;
     cudaEvent_t side_event_ = nullptr;
     std::unique_ptr<DeviceModel> dm_;
     std::unique_ptr<MdTables> md_;
