@@ -5,15 +5,16 @@
 // path's only dense contraction and its only tensor-core work:
 //  * mixed form: A is split into two BF16 planes (hi = bf16(a), lo = bf16(a - hi)),
 //    stored transposed (K = rows contiguous), and G += hi^T hi + hi^T lo + lo^T hi on
-//    tcgen05 (kind::f16, FP32 accumulation in TMEM).  Operands arrive by TMA with
-//    128-byte swizzle through a 3-stage mbarrier pipeline; one thread issues the
-//    MMAs; four warps drain TMEM with tcgen05.ld and add the split-K partial tile
-//    into an FP64 G.
+//    tcgen05 (kind::f16, FP32 accumulation in TMEM).  A persistent CTA per SM walks
+//    the upper-triangle tile pairs: operands arrive by TMA with 128-byte swizzle
+//    through a 3-stage mbarrier ring, one thread issues the MMAs into one of two TMEM
+//    accumulators, and four epilogue warps drain the other with tcgen05.ld and add
+//    it into an FP64 G.
 //  * plain form: FP64 G by this library's register-blocked FP64 SYRK (dense64.cu),
 //    which runs at the FP64 FMA rate of the GPU.
 //  * h = A^T b is an FP64 matrix-vector product (plain form) or is fused into the
 //    BF16 split pass (mixed form).
-// Every wait on an mbarrier is bounded (about one second); on time-out the kernel
+// Every wait on an mbarrier is bounded (about two seconds); on time-out the kernel
 // records an error code, skips its stores, frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -31,12 +32,11 @@
 
 namespace cgd {
 
-constexpr int GB_M = 128, GB_N = 128, GB_K = 64, GB_STAGES = 3, GB_THREADS = 128;
+constexpr int GB_M = 128, GB_N = 128, GB_K = 64, GB_STAGES = 3, GB_THREADS = 192;
 constexpr uint32_t GB_TILE_BYTES = GB_M * GB_K * 2;         // one 128x64 bf16 operand tile (16 KB)
 constexpr uint32_t GB_STAGE_BYTES = 4 * GB_TILE_BYTES;      // A_hi, A_lo, B_hi, B_lo
 constexpr long long GB_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
-constexpr int GB_EPI_LD = GB_N + 1;                         // epilogue staging row (floats)
-static_assert(4 * 32 * GB_EPI_LD * 4 <= (int)(GB_STAGES * GB_STAGE_BYTES), "epilogue staging fits the stages");
+constexpr int GB_EPI_LD = 33;                               // epilogue staging row (floats)
 
 // ---------------------------------------------------------------- split + transpose
 // planes[p][c][k] (bf16, k contiguous) for rows [r0, r0+nr) of A (row-major, lda),
@@ -262,33 +262,65 @@ __device__ __forceinline__ void grouped_pair(int t, int ntile, int& ti, int& tj)
     ti = tj = 0;   // not reached for t < ntile (ntile + 1) / 2
 }
 
-// ---------------------------------------------------------------- tcgen05 Gram tile
-// grid.x: upper-triangular tile pair (i <= j), grid.y: K slice.
+// ---------------------------------------------------------------- tcgen05 Gram tiles
+// Persistent kernel, one CTA per SM.  A work unit is a (tile pair i <= j, K slice);
+// CTA b takes units b, b + gridDim.x, ... in grouped tile-pair order, so the units in
+// flight at one time stay close in the triangle.  Warp roles:
+//   warp 0      TMA producer: the four 128x64 operand tiles of each K step into a
+//               GB_STAGES-deep ring of stages (full / empty mbarriers);
+//   warp 1      MMA issuer: 12 tcgen05.mma per K step into one of two TMEM
+//               accumulators (128 columns each), committed to acc_full[buf];
+//   warps 2..5  epilogue: tcgen05.ld of the accumulator (TMEM lane quarter =
+//               warp % 4), staged 32 columns at a time through shared memory so that
+//               every FP64 atomic instruction adds 32 consecutive columns of a row of
+//               G, then acc_empty[buf] frees the accumulator.
+// With two accumulators the epilogue of one unit runs under the MMAs of the next, and
+// the ring keeps loading across unit boundaries.
+constexpr int GB_ACC = 2;
+struct GbSmem {
+    static constexpr uint32_t epi = GB_STAGES * GB_STAGE_BYTES;
+    static constexpr uint32_t bars = epi + 4 * 32 * GB_EPI_LD * 4;
+    static constexpr uint32_t nbars = 2 * GB_STAGES + 2 * GB_ACC + 1;
+    static constexpr uint32_t total = bars + nbars * 8 + 16;
+};
+static_assert(GbSmem::bars % 8 == 0, "mbarrier alignment");
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ int gb_unit(int u, int npairs, int ntile, int64_t kpad, int64_t kslice, int& ti, int& tj,
+                                       int64_t& kb) {
+    const int slice = u / npairs;
+    grouped_pair(u - slice * npairs, ntile, ti, tj);
+    kb = (int64_t)slice * kslice;
+    const int64_t ke = min(kpad, kb + kslice);
+    return ke > kb ? (int)((ke - kb) / GB_K) : 0;
+}
+
 __global__ void __launch_bounds__(GB_THREADS, 1)
     k_gram_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo, int ntile,
-              int64_t kpad, int64_t kslice, int ncols, double* __restrict__ G, int* __restrict__ err) {
+              int npairs, int nunits, int64_t kpad, int64_t kslice, int ncols, double* __restrict__ G,
+              int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + GB_STAGES * GB_STAGE_BYTES);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + GbSmem::bars);
     uint64_t* empty = full + GB_STAGES;
-    uint64_t* done = empty + GB_STAGES;
+    uint64_t* acc_full = empty + GB_STAGES;
+    uint64_t* acc_empty = acc_full + GB_ACC;
+    uint64_t* done = acc_empty + GB_ACC;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
-
-    int ti = 0, tj = 0;
-    grouped_pair((int)blockIdx.x, ntile, ti, tj);
-    const int64_t kb = (int64_t)blockIdx.y * kslice;
-    const int64_t ke = min(kpad, kb + kslice);
-    const int nk = (int)((ke - kb) / GB_K);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < GB_STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int b = 0; b < GB_ACC; ++b) { mbar_init(&acc_full[b], 1); mbar_init(&acc_empty[b], 4); }
         mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {   // TMEM: 128 lanes x 128 FP32 columns
+    if (warp == 0) {   // TMEM: 128 lanes x (2 x 128) FP32 columns
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(GB_N)
+                     "r"(GB_ACC * GB_N)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -296,96 +328,128 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    bool ok = true;
 
-    if (warp == 0 && lane == 0 && nk > 0) {   // producer
-        int issued = 0;
-        for (int it = 0; it < nk && ok; ++it) {
-            const int s = it % GB_STAGES;
-            const uint32_t ph = (uint32_t)(it / GB_STAGES) & 1u;
-            if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
-            unsigned char* st = smem + s * GB_STAGE_BYTES;
-            mbar_expect_tx(&full[s], GB_STAGE_BYTES);
-            const int x = (int)(kb + (int64_t)it * GB_K);
-            tma_load_2d(st, &map_hi, &full[s], x, ti * GB_M);
-            tma_load_2d(st + GB_TILE_BYTES, &map_lo, &full[s], x, ti * GB_M);
-            tma_load_2d(st + 2 * GB_TILE_BYTES, &map_hi, &full[s], x, tj * GB_N);
-            tma_load_2d(st + 3 * GB_TILE_BYTES, &map_lo, &full[s], x, tj * GB_N);
-            ++issued;
+    if (warp == 0) {
+        if (lane == 0) {   // producer
+            bool ok = true;
+            int64_t g = 0;   // K steps issued over all units
+            for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+                int ti, tj;
+                int64_t kb;
+                const int nk = gb_unit(u, npairs, ntile, kpad, kslice, ti, tj, kb);
+                for (int it = 0; it < nk; ++it, ++g) {
+                    const int s = (int)(g % GB_STAGES);
+                    const uint32_t ph = (uint32_t)(g / GB_STAGES) & 1u;
+                    if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                    unsigned char* st = smem + s * GB_STAGE_BYTES;
+                    mbar_expect_tx(&full[s], GB_STAGE_BYTES);
+                    const int x = (int)(kb + (int64_t)it * GB_K);
+                    tma_load_2d(st, &map_hi, &full[s], x, ti * GB_M);
+                    tma_load_2d(st + GB_TILE_BYTES, &map_lo, &full[s], x, ti * GB_M);
+                    tma_load_2d(st + 2 * GB_TILE_BYTES, &map_hi, &full[s], x, tj * GB_N);
+                    tma_load_2d(st + 3 * GB_TILE_BYTES, &map_lo, &full[s], x, tj * GB_N);
+                }
+            }
+            // drain after a time-out: the last load issued into each stage completes
+            // the full-barrier phase (g / GB_STAGES) & 1; wait (bounded) for it so that
+            // no copy still writes this CTA's shared memory when it exits
+            if (!ok)
+                for (int64_t q = g - 1; q >= 0 && q >= g - GB_STAGES; --q)
+                    mbar_wait(&full[q % GB_STAGES], (uint32_t)(q / GB_STAGES) & 1u, err, 4);
         }
-        // drain after a time-out: the last load issued into each stage completes the
-        // full-barrier phase (it / GB_STAGES) & 1; wait (bounded) for it so that no
-        // copy still writes this CTA's shared memory when it exits
-        if (!ok)
-            for (int it = issued - 1; it >= 0 && it >= issued - GB_STAGES; --it)
-                mbar_wait(&full[it % GB_STAGES], (uint32_t)(it / GB_STAGES) & 1u, err, 4);
-    } else if (warp == 1 && lane == 0 && nk > 0) {   // MMA issuer
-        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GB_N >> 3) << 17) |
-                               ((uint32_t)(GB_M >> 4) << 24);
-        for (int it = 0; it < nk && ok; ++it) {
-            const int s = it % GB_STAGES;
-            const uint32_t ph = (uint32_t)(it / GB_STAGES) & 1u;
-            if (!mbar_wait(&full[s], ph, err, 2)) { ok = false; break; }
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer
+            const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(GB_N >> 3) << 17) |
+                                   ((uint32_t)(GB_M >> 4) << 24);
+            bool ok = true;
+            int64_t g = 0;
+            int j = 0;   // units with K steps, in order (accumulator buffer j & 1)
+            for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+                int ti, tj;
+                int64_t kb;
+                const int nk = gb_unit(u, npairs, ntile, kpad, kslice, ti, tj, kb);
+                if (nk == 0) continue;
+                const int buf = j & 1;
+                if (!mbar_wait(&acc_empty[buf], ((uint32_t)(j >> 1) & 1u) ^ 1u, err, 5)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)(buf * GB_N);
+                for (int it = 0; it < nk; ++it, ++g) {
+                    const int s = (int)(g % GB_STAGES);
+                    const uint32_t ph = (uint32_t)(g / GB_STAGES) & 1u;
+                    if (!mbar_wait(&full[s], ph, err, 2)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    unsigned char* st = smem + s * GB_STAGE_BYTES;
+                    const uint64_t ahi = smem_desc(st), alo = smem_desc(st + GB_TILE_BYTES);
+                    const uint64_t bhi = smem_desc(st + 2 * GB_TILE_BYTES), blo = smem_desc(st + 3 * GB_TILE_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < GB_K / 16; ++kk) {
+                        const uint64_t adv = (uint64_t)((kk * 32) >> 4);   // 16 bf16 = 32 B along K
+                        umma_bf16(d, ahi + adv, bhi + adv, idesc, (it > 0 || kk > 0) ? 1u : 0u);
+                        umma_bf16(d, ahi + adv, blo + adv, idesc, 1u);
+                        umma_bf16(d, alo + adv, bhi + adv, idesc, 1u);
+                    }
+                    umma_commit(&empty[s]);
+                }
+                if (!ok) break;
+                umma_commit(&acc_full[buf]);
+                ++j;
+            }
+            // every MMA of this CTA has finished before TMEM is released
+            umma_commit(done);
+            mbar_wait(done, 0, err, 6);
+        }
+    } else {   // epilogue warps 2..5
+        const int q = warp & 3;   // TMEM lane quarter this warp may read
+        float* stile = reinterpret_cast<float*>(smem + GbSmem::epi) + (size_t)(warp - 2) * 32 * GB_EPI_LD;
+        int j = 0;
+        for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+            int ti, tj;
+            int64_t kb;
+            const int nk = gb_unit(u, npairs, ntile, kpad, kslice, ti, tj, kb);
+            if (nk == 0) continue;
+            const int buf = j & 1;
+            const bool got = mbar_wait(&acc_full[buf], (uint32_t)(j >> 1) & 1u, err, 3);
+            if (!__all_sync(0xffffffffu, got)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            unsigned char* st = smem + s * GB_STAGE_BYTES;
-            const uint64_t ahi = smem_desc(st), alo = smem_desc(st + GB_TILE_BYTES);
-            const uint64_t bhi = smem_desc(st + 2 * GB_TILE_BYTES), blo = smem_desc(st + 3 * GB_TILE_BYTES);
-#pragma unroll
-            for (int kk = 0; kk < GB_K / 16; ++kk) {
-                const uint64_t adv = (uint64_t)((kk * 32) >> 4);   // 16 bf16 = 32 B along K
-                umma_bf16(tmem, ahi + adv, bhi + adv, idesc, (it > 0 || kk > 0) ? 1u : 0u);
-                umma_bf16(tmem, ahi + adv, blo + adv, idesc, 1u);
-                umma_bf16(tmem, alo + adv, bhi + adv, idesc, 1u);
-            }
-            umma_commit(&empty[s]);
-        }
-        umma_commit(done);
-    }
-    __syncwarp();
-    // epilogue: all four warps (TMEM lane quarter = warp)
-    bool have = nk > 0;
-    if (have) have = mbar_wait(done, 0, err, 3);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (have && *err == 0) {
-        // The accumulator rows of this warp (TMEM lanes warp*32 ..) pass through a
-        // private slice of the (now idle) stage memory, so that every atomic
-        // instruction then adds 32 consecutive columns of one row of G.
-        float* stile = reinterpret_cast<float*>(smem) + (size_t)warp * 32 * GB_EPI_LD;
 #pragma unroll 1
-        for (int c0 = 0; c0 < GB_N; c0 += 32) {
-            uint32_t v[32];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            for (int c0 = 0; c0 < GB_N; c0 += 32) {
+                uint32_t v[32];
+                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * GB_N + c0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int c = 0; c < 32; ++c) stile[lane * GB_EPI_LD + c0 + c] = __uint_as_float(v[c]);
-        }
-        __syncwarp();
-#pragma unroll 1
-        for (int r = 0; r < 32; ++r) {
-            const int row = ti * GB_M + warp * 32 + r;
-            if (row >= ncols) break;
-            double* grow = G + (int64_t)row * ncols;
-#pragma unroll
-            for (int j = 0; j < GB_N / 32; ++j) {
-                const int col = tj * GB_N + j * 32 + lane;
-                if (col < ncols && (ti != tj || col >= row))
-                    atomicAdd(grow + col, (double)stile[r * GB_EPI_LD + j * 32 + lane]);
+                for (int c = 0; c < 32; ++c) stile[lane * GB_EPI_LD + c] = __uint_as_float(v[c]);
+                __syncwarp();
+                if (*err == 0) {
+                    const int col = tj * GB_N + c0 + lane;
+#pragma unroll 4
+                    for (int r = 0; r < 32; ++r) {
+                        const int row = ti * GB_M + q * 32 + r;
+                        if (row < ncols && col < ncols && (ti != tj || col >= row))
+                            atomicAdd(G + (int64_t)row * ncols + col, (double)stile[r * GB_EPI_LD + lane]);
+                    }
+                }
+                __syncwarp();
             }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[buf]);
+            ++j;
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GB_N) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GB_ACC * GB_N)
+                     : "memory");
     }
 }
 
@@ -490,7 +554,7 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
     if (rblock <= 0) throw std::runtime_error("Gram plane buffer too small");
     const int ntile = (int)(cpad / cgd::GB_M);
     const int npairs = ntile * (ntile + 1) / 2;
-    const size_t smem = (size_t)cgd::GB_STAGES * cgd::GB_STAGE_BYTES + 1024 + 256;
+    const size_t smem = (size_t)cgd::GbSmem::total + 1024;
     ck(cudaFuncSetAttribute(cgd::k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr");
     // split + A^T b: one wave of resident blocks over the column strips (a second,
     // partial wave would double the pass)
@@ -526,15 +590,28 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         mark(S_ATB, false);
         ck(cudaGetLastError(), "k_split_reduce");
         CUtensorMap mhi = plane_map(hi, kpad, cpad), mlo = plane_map(lo, kpad, cpad);
-        // K slices: about ctas_per_sm CTAs per SM in total
+        // K slices: the persistent grid (one CTA per SM) runs npairs * nslice units
+        // in waves; pick nslice (at most ctas_per_sm units per SM) minimising the K
+        // steps on the longest CTA's path, waves * ceil(ksteps / nslice), plus one
+        // step per wave for the unit switch.
         const int64_t ksteps = kpad / cgd::GB_K;
-        const int64_t target = (int64_t)device_sms() * std::max(1, ctas_per_sm);
-        int64_t nslice = std::max<int64_t>(1, std::min<int64_t>(ksteps, (target + npairs - 1) / npairs));
+        const int64_t sms = device_sms();
+        const int64_t smax = std::max<int64_t>(
+            1, std::min<int64_t>(ksteps, sms * std::max(1, ctas_per_sm) / std::max(1, npairs)));
+        int64_t nslice = 1, best = INT64_MAX;
+        for (int64_t sl = 1; sl <= smax; ++sl) {
+            const int64_t waves = (npairs * sl + sms - 1) / sms;
+            const int64_t cost = waves * ((ksteps + sl - 1) / sl + 1);
+            if (cost < best) { best = cost; nslice = sl; }
+        }
         const int64_t kslice = (ksteps + nslice - 1) / nslice * cgd::GB_K;
         nslice = (kpad + kslice - 1) / kslice;
+        const int64_t nunits = (int64_t)npairs * nslice;
+        if (nunits > INT32_MAX) throw std::runtime_error("too many Gram tiles");
+        const unsigned grid = (unsigned)std::min<int64_t>(nunits, device_sms());
         mark(S_TC, true);
-        cgd::k_gram_tc<<<dim3(npairs, (unsigned)nslice), cgd::GB_THREADS, smem, st>>>(mhi, mlo, ntile, kpad, kslice,
-                                                                                      ncols, G, d_err);
+        cgd::k_gram_tc<<<grid, cgd::GB_THREADS, smem, st>>>(mhi, mlo, ntile, npairs, (int)nunits, kpad, kslice, ncols,
+                                                            G, d_err);
         mark(S_TC, false);
         ck(cudaGetLastError(), "k_gram_tc");
     }

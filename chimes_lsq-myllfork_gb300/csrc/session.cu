@@ -359,6 +359,27 @@ void Session::reset_stage_totals() {
 }
 
 // ------------------------------------------------------------------ session
+cudaMemPool_t scratch_pool(int device) {
+    static std::mutex mu;
+    static std::vector<cudaMemPool_t> pools;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)pools.size() <= device) pools.resize(device + 1, nullptr);
+    if (!pools[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t pool = nullptr;
+        CK(cudaMemPoolCreate(&pool, &props));
+        uint64_t keep = uint64_t(32) << 30;
+        CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        pools[device] = pool;
+    }
+    return pools[device];
+}
+
+void scratch_pool_trim(int device) { CK(cudaMemPoolTrimTo(scratch_pool(device), 0)); }
+
 Session::Session(const Model& m, int device) : model_(m), device_(device) {
     CK(cudaSetDevice(device));
     // A blocking stream: work the caller queued on the legacy default stream (for
@@ -1015,6 +1036,7 @@ void Session::refine_streamed(const double* L, int ncols, double ridge, const st
     if (refine_cache_bytes_ < 0) {   // what is free now, less a margin for the assembly's own work lists
         size_t fr = 0, tot = 0;
         CK(cudaStreamSynchronize(stream_));
+        scratch_pool_trim(device_);
         CK(cudaMemGetInfo(&fr, &tot));
         const int64_t margin = (int64_t)(tot / 10) + 3 * (int64_t)maxrows * ncols * (int64_t)sizeof(double);
         R.cache_left = std::max<int64_t>(0, (int64_t)fr - margin);
