@@ -181,22 +181,27 @@ __global__ void k_force2(ModelDev M, FramesDev F, NeighDev NB, Buckets inc, cons
 }
 
 // ---------------------------------------------------------------- 2-body stress/energy rows
-// One CTA per frame; threads over the 2-body columns.  comps: 0 E, 1 xx, 2 yy, 3 zz, 4 xy, 5 xz, 6 yz.
-template <typename R>
-__global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t lda) {
+// grid: (frame, slice of the frame's pairs); threads over the 2-body columns.  Each
+// CTA sums its slice into per-column partials (comps: 0 E, 1 xx, 2 yy, 3 zz, 4 xy,
+// 5 xz, 6 yz); k_virial2_rows adds a frame's slices in slice order and writes the
+// rows, so the result does not depend on timing.  The slices spread a block's few
+// frames over every SM (the pairs' FP64 basis evaluations dominate this kernel).
+template <typename R, int MAXC>
+__global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, int nslice, R* __restrict__ part) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ord = M.order2;
     const int ncol = M.npairs * ord;
-    const int f = blockIdx.x;
+    const int f = blockIdx.x, sl = blockIdx.y;
     const int srows = F.stress_rows[f], erows = F.energy_rows[f];
     if (srows == 0 && erows == 0) return;
     R* sGH = reinterpret_cast<R*>(smem_raw);                      // [chunk][2*ord]
     R* sV = sGH + (size_t)blockDim.x * 2 * ord;                    // [chunk][6]
     int* sPt = reinterpret_cast<int*>(sV + (size_t)blockDim.x * 6);
     const BoxDev& B = F.box[f];
-    const int64_t p0 = NB.ofs2[F.atom_ofs[f]], p1 = NB.ofs2[F.atom_ofs[f + 1]];
-    constexpr int MAXC = 8;
-    R acc[MAXC][7];
+    const int64_t q0 = NB.ofs2[F.atom_ofs[f]], q1 = NB.ofs2[F.atom_ofs[f + 1]];
+    const int64_t len = (q1 - q0 + nslice - 1) / nslice;
+    const int64_t p0 = min(q1, q0 + (int64_t)sl * len), p1 = min(q1, p0 + len);
+    R acc[MAXC][7];   // MAXC columns per thread, unrolled so that acc stays in registers
     for (int c = 0; c < MAXC; ++c) for (int k = 0; k < 7; ++k) acc[c][k] = R(0);
     for (int64_t c0 = p0; c0 < p1; c0 += blockDim.x) {
         const int64_t p = c0 + threadIdx.x;
@@ -222,26 +227,49 @@ __global__ void k_virial2(ModelDev M, FramesDev F, NeighDev NB, R* A, int64_t ld
         }
         __syncthreads();
         const int cnt = (int)min((int64_t)blockDim.x, p1 - c0);
+#pragma unroll
         for (int c = 0; c < MAXC; ++c) {
             const int col = threadIdx.x + c * blockDim.x;
-            if (col >= ncol) break;
-            const int pt = col / ord, n = col % ord;
-            for (int k = 0; k < cnt; ++k) {
-                if (sPt[k] != pt) continue;
-                const R* gh = sGH + (size_t)k * 2 * ord + 2 * n;
-                const R* v = sV + (size_t)k * 6;
-                acc[c][0] += gh[0];
-                for (int q = 0; q < 6; ++q) acc[c][1 + q] -= gh[1] * v[q];
+            if (col < ncol) {
+                const int pt = col / ord, n = col % ord;
+                for (int k = 0; k < cnt; ++k) {
+                    if (sPt[k] != pt) continue;
+                    const R* gh = sGH + (size_t)k * 2 * ord + 2 * n;
+                    const R* v = sV + (size_t)k * 6;
+                    acc[c][0] += gh[0];
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) acc[c][1 + q] -= gh[1] * v[q];
+                }
             }
         }
         __syncthreads();
     }
-    const double inv_vol = 1.0 / B.vol;
+    R* o = part + ((int64_t)f * nslice + sl) * 7 * ncol;
+#pragma unroll
     for (int c = 0; c < MAXC; ++c) {
         const int col = threadIdx.x + c * blockDim.x;
-        if (col >= ncol) break;
+        if (col < ncol)
+#pragma unroll
+            for (int k = 0; k < 7; ++k) o[(int64_t)k * ncol + col] = acc[c][k];
+    }
+}
+
+template <typename R>
+__global__ void k_virial2_rows(ModelDev M, FramesDev F, int nslice, const R* __restrict__ part, R* A, int64_t lda) {
+    const int ord = M.order2;
+    const int ncol = M.npairs * ord;
+    const int f = blockIdx.x;
+    if (F.stress_rows[f] == 0 && F.energy_rows[f] == 0) return;
+    const double inv_vol = 1.0 / F.box[f].vol;
+    const R* o = part + (int64_t)f * nslice * 7 * ncol;
+    for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
         const int base = M.pairs[col / ord].col;   // HIERARC: excluded pairs have no columns
-        if (base >= 0) write_virial_rows(F, f, base + col % ord, acc[c], inv_vol, A, lda);
+        if (base < 0) continue;
+        R s[7];
+        for (int k = 0; k < 7; ++k) s[k] = R(0);
+        for (int sl = 0; sl < nslice; ++sl)
+            for (int k = 0; k < 7; ++k) s[k] += o[((int64_t)sl * 7 + k) * ncol + col];
+        write_virial_rows(F, f, base + col % ord, s, inv_vol, A, lda);
     }
 }
 
@@ -720,17 +748,39 @@ void launch_force2(int prec, int nreal, const ModelDev& M, const FramesDev& F, c
     }
 }
 
-void launch_virial2(int prec, int nframes, const ModelDev& M, const FramesDev& F, const NeighDev& NB, void* A,
-                    int64_t lda, cudaStream_t st) {
+int virial2_slices(int nframes, int64_t npairs, int sms) {
+    if (nframes <= 0) return 1;
+    const int64_t per_frame = npairs / nframes;
+    const int64_t want = (2 * (int64_t)sms + nframes - 1) / nframes;       // about two CTAs per SM
+    const int64_t most = std::max<int64_t>(1, per_frame / (2 * F2_THREADS));   // two chunks of pairs per slice
+    return (int)std::max<int64_t>(1, std::min<int64_t>({want, most, 64}));
+}
+
+template <typename R, int MAXC>
+static void virial2_launch(int nframes, int nslice, size_t sm, const ModelDev& M, const FramesDev& F,
+                           const NeighDev& NB, void* part, void* A, int64_t lda, cudaStream_t st) {
+    set_smem(k_virial2<R, MAXC>, sm);
+    k_virial2<R, MAXC><<<dim3((unsigned)nframes, (unsigned)nslice), F2_THREADS, sm, st>>>(M, F, NB, nslice, (R*)part);
+    k_virial2_rows<R><<<nframes, F2_THREADS, 0, st>>>(M, F, nslice, (const R*)part, (R*)A, lda);
+}
+
+template <typename R>
+static void virial2_dispatch(int maxc, int nframes, int nslice, size_t sm, const ModelDev& M, const FramesDev& F,
+                             const NeighDev& NB, void* part, void* A, int64_t lda, cudaStream_t st) {
+    if (maxc <= 1) virial2_launch<R, 1>(nframes, nslice, sm, M, F, NB, part, A, lda, st);
+    else if (maxc <= 2) virial2_launch<R, 2>(nframes, nslice, sm, M, F, NB, part, A, lda, st);
+    else if (maxc <= 4) virial2_launch<R, 4>(nframes, nslice, sm, M, F, NB, part, A, lda, st);
+    else virial2_launch<R, 8>(nframes, nslice, sm, M, F, NB, part, A, lda, st);
+}
+
+void launch_virial2(int prec, int nframes, int nslice, const ModelDev& M, const FramesDev& F, const NeighDev& NB,
+                    void* part, void* A, int64_t lda, cudaStream_t st) {
+    if (nframes <= 0) return;
     const size_t rs = prec == 0 ? 8 : 4;
     const size_t sm = (size_t)F2_THREADS * (2 * M.order2 + 6) * rs + F2_THREADS * sizeof(int);
-    if (prec == 0) {
-        set_smem(k_virial2<double>, sm);
-        k_virial2<double><<<nframes, F2_THREADS, sm, st>>>(M, F, NB, (double*)A, lda);
-    } else {
-        set_smem(k_virial2<float>, sm);
-        k_virial2<float><<<nframes, F2_THREADS, sm, st>>>(M, F, NB, (float*)A, lda);
-    }
+    const int maxc = (M.npairs * M.order2 + F2_THREADS - 1) / F2_THREADS;   // at most 8 (checked by the caller)
+    if (prec == 0) virial2_dispatch<double>(maxc, nframes, nslice, sm, M, F, NB, part, A, lda, st);
+    else virial2_dispatch<float>(maxc, nframes, nslice, sm, M, F, NB, part, A, lda, st);
 }
 
 size_t cluster_basis_count(int nbody, int ord, int64_t nclusters) {

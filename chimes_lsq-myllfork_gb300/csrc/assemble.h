@@ -86,8 +86,11 @@ __device__ __forceinline__ void write_virial_rows(const FramesDev& F, int f, int
 // Host launchers (kernels are defined in assemble.cu).  prec: 0 FP64, 1 FP32.
 void launch_force2(int prec, int nreal, const ModelDev& M, const FramesDev& F, const NeighDev& NB,
                    const Buckets& inc, const int64_t* key_frame_ofs, void* A, int64_t lda, cudaStream_t st);
-void launch_virial2(int prec, int nframes, const ModelDev& M, const FramesDev& F, const NeighDev& NB, void* A,
-                    int64_t lda, cudaStream_t st);
+// 2-body stress/energy rows in two launches: per-(frame, slice) partials into part
+// (nframes * nslice * 7 * 2-body columns values in the form's type), then the rows.
+int virial2_slices(int nframes, int64_t npairs, int sms);
+void launch_virial2(int prec, int nframes, int nslice, const ModelDev& M, const FramesDev& F, const NeighDev& NB,
+                    void* part, void* A, int64_t lda, cudaStream_t st);
 // Slot bases of every cluster, once per cluster: [cluster][slot][2 ord + 4] values in
 // the form's type (g, h, r, r_ab), read by the force and stress/energy kernels.
 size_t cluster_basis_count(int nbody, int ord, int64_t nclusters);

@@ -532,11 +532,15 @@ __global__ void k_quads(ModelDev M, FramesDev F, NeighDev NB, ClusterSet CS, int
 }
 
 // ---------------------------------------------------------------- bucketing
-// Stable counting sort of one frame's items by key, one CTA per frame.  Counting
-// and the scan are parallel; the fill walks the items in order, one warp, 32 at a
-// time, ranking equal keys with __match_any_sync so the result is deterministic.
-constexpr int BUCKET_THREADS = 256;
+// Stable counting sort of one frame's items by key, one CTA per frame.  The items
+// are split into contiguous ranges, one per warp (as many warps as the per-warp key
+// counts fit in shared memory); each warp counts the keys of its range, a scan turns
+// the counts into a start for every (key, warp), and each warp then places its range
+// in order, 32 items at a time, ranking equal keys with __match_any_sync.  Within a
+// key the items keep their order, so the result does not depend on timing.
+constexpr int BUCKET_THREADS = 512;
 constexpr int BUCKET_MAX_KEYS = 8192;
+constexpr int BUCKET_SMEM_INTS = 24576;   // per-warp key counts + key starts (96 KB)
 
 __device__ __forceinline__ void bucket_item(const BucketSpec& S, int N, int64_t base, int64_t t, int& key, int& val) {
     if (S.kind == 0) {
@@ -557,8 +561,8 @@ __device__ __forceinline__ void bucket_item(const BucketSpec& S, int N, int64_t 
     }
 }
 
-__global__ void k_bucket(FramesDev F, BucketSpec S, Buckets out) {
-    __shared__ int cnt[BUCKET_MAX_KEYS];
+__global__ void __launch_bounds__(BUCKET_THREADS) k_bucket(FramesDev F, BucketSpec S, Buckets out) {
+    extern __shared__ int bsm[];
     __shared__ int part[BUCKET_THREADS];
     const int f = blockIdx.x;
     const int N = F.natoms[f];
@@ -570,19 +574,34 @@ __global__ void k_bucket(FramesDev F, BucketSpec S, Buckets out) {
     const int64_t kbase = S.key_frame_ofs[f];
     const int K = (int)(S.key_frame_ofs[f + 1] - kbase - 1);
     const int64_t vbase = base * mult;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) cnt[k] = 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int W = max(1, min((int)(blockDim.x >> 5), (BUCKET_SMEM_INTS - K) / max(K, 1)));
+    int* cntw = bsm;            // [W][K]: counts, then starts
+    int* kst = bsm + W * K;     // [K]: totals, then starts
+    for (int k = threadIdx.x; k < W * K; k += blockDim.x) cntw[k] = 0;
     __syncthreads();
-    for (int64_t t = threadIdx.x; t < nitems; t += blockDim.x) {
-        int key, val;
-        bucket_item(S, N, base, t, key, val);
-        atomicAdd(&cnt[key], 1);
+    const int64_t chunk = (nitems + W - 1) / W;
+    const int64_t r0 = min(nitems, (int64_t)warp * chunk), r1 = min(nitems, r0 + chunk);
+    if (warp < W) {
+        for (int64_t t = r0 + lane; t < r1; t += 32) {
+            int key, val;
+            bucket_item(S, N, base, t, key, val);
+            atomicAdd(&cntw[warp * K + key], 1);
+        }
     }
     __syncthreads();
-    // exclusive scan of cnt[0..K)
+    // per key: starts of each warp's share relative to the key, and the key's total
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        int run = 0;
+        for (int w = 0; w < W; ++w) { const int v = cntw[w * K + k]; cntw[w * K + k] = run; run += v; }
+        kst[k] = run;
+    }
+    __syncthreads();
+    // exclusive scan of the key totals
     const int per = (K + blockDim.x - 1) / blockDim.x;
     const int k0 = threadIdx.x * per, k1 = min(K, k0 + per);
     int local = 0;
-    for (int k = k0; k < k1; ++k) local += cnt[k];
+    for (int k = k0; k < k1; ++k) local += kst[k];
     part[threadIdx.x] = local;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -591,14 +610,16 @@ __global__ void k_bucket(FramesDev F, BucketSpec S, Buckets out) {
     }
     __syncthreads();
     int run = part[threadIdx.x];
-    for (int k = k0; k < k1; ++k) { int v = cnt[k]; cnt[k] = run; out.key_ofs[kbase + k] = vbase + run; run += v; }
+    for (int k = k0; k < k1; ++k) { int v = kst[k]; kst[k] = run; out.key_ofs[kbase + k] = vbase + run; run += v; }
     if (threadIdx.x == 0) out.key_ofs[kbase + K] = vbase + nitems;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        for (int64_t c0 = 0; c0 < nitems; c0 += 32) {
+    for (int k = threadIdx.x; k < W * K; k += blockDim.x) cntw[k] += kst[k % K];
+    __syncthreads();
+    if (warp < W) {
+        int* cnt = cntw + warp * K;
+        for (int64_t c0 = r0; c0 < r1; c0 += 32) {
             int64_t t = c0 + lane;
-            bool act = t < nitems;
+            bool act = t < r1;
             int key = -1 - lane, val = 0;
             if (act) bucket_item(S, N, base, t, key, val);
             unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -655,7 +676,10 @@ void launch_clusters(int nbody, const ModelDev& M, const FramesDev& F, const Nei
     else k_quads<<<g, 256, 0, st>>>(M, F, NB, CS, fill, parts);
 }
 void launch_bucket(int nframes, const FramesDev& F, const BucketSpec& S, const Buckets& out, cudaStream_t st) {
-    if (nframes > 0) k_bucket<<<nframes, BUCKET_THREADS, 0, st>>>(F, S, out);
+    if (nframes <= 0) return;
+    const int smem = BUCKET_SMEM_INTS * (int)sizeof(int);
+    cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_bucket<<<nframes, BUCKET_THREADS, smem, st>>>(F, S, out);
 }
 
 }  // namespace cgd

@@ -386,6 +386,7 @@ Session::Session(const Model& m, int device) : model_(m), device_(device) {
     // example the zeroing of G by a framework) completes before the session's next
     // launch, and the other way round.
     CK(cudaStreamCreateWithFlags(&stream_, cudaStreamDefault));
+    CK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device));
     dm_.reset(new DeviceModel(model_, cgd::VIR_PPT * cgd::MB_THREADS));
 }
 
@@ -717,7 +718,9 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
         mark(ST_FORCE2, false);
         if (virial) {
             mark(ST_VIRIAL2, true);
-            cgd::launch_virial2(prec, nf, M, F, NB, A, lda, st); L();
+            const int nsl = cgd::virial2_slices(nf, tot[0], sms_);
+            void* part = S.get<double>((size_t)nf * nsl * 7 * ncol);
+            cgd::launch_virial2(prec, nf, nsl, M, F, NB, part, A, lda, st); L(2);
             mark(ST_VIRIAL2, false);
         }
         CK(cudaGetLastError());

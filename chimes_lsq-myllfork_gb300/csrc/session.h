@@ -360,6 +360,7 @@ class Session {
     cudaEvent_t open_event_ = nullptr;
     int open_stage_ = -1;
     int device_;
+    int sms_ = 1;   // streaming multiprocessors of the device
     cudaStream_t stream_ = nullptr;
     cudaStream_t side_stream_ = nullptr;   // look-ahead MD list builds
     cudaStream_t copy_stream_ = nullptr;   // device-to-host copies of streamed assemblies
