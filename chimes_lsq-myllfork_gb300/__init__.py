@@ -113,6 +113,11 @@ def lib():
                                               ctypes.c_int64, vp, vp, ctypes.c_int, ctypes.c_double, vp, vp]),
         "cg_predict_streamed": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, vp]),
         "cg_fp64_fma_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
+        "cg_md_server_start": (ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_void_p)]),
+        "cg_md_server_submit": (ctypes.c_int, [vp, vp, ctypes.POINTER(ctypes.c_int64)]),
+        "cg_md_server_poll": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int, vp, vp]),
+        "cg_md_server_stop": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_int64)]),
         "cg_md_serve_memory": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double)]),
         "cg_batch_fit_create": (ctypes.c_int, [vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int64, vp, vp, pp]),
@@ -441,6 +446,63 @@ class BatchFit:
         return v.value
 
 
+CG_PENDING = 5
+
+
+class MdServer:
+    """cg_md_server_*: a library thread runs the serving loop; submit() queues a
+    request (its arrays are copied), poll() returns None while it waits or runs, else
+    (final xyz [n,3], result record)."""
+
+    _RESULT = [("admitted", "f8"), ("finished", "f8"), ("step_ms_sum", "f8"), ("step_ms_max", "f8"),
+               ("reserved_bytes", "f8")]
+
+    def __init__(self, session, masses, dt_fs, hbm_budget, max_batch_atoms, max_batch_frames):
+        self._session = session   # kept alive while the server runs
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        h = ctypes.c_void_p()
+        _check(lib().cg_md_server_start(session._h, _ptr(m), float(dt_fs), float(hbm_budget), int(max_batch_atoms),
+                                        int(max_batch_frames), ctypes.byref(h)))
+        self._h = h
+        self._natoms = {}
+
+    def submit(self, types, xyz, cell, v, nsteps):
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        c = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        vv = np.ascontiguousarray(v, dtype=np.float64)
+        req = MdRequest(len(t), int(nsteps), 0.0, t.ctypes.data, x.ctypes.data, c.ctypes.data, vv.ctypes.data, None)
+        tk = ctypes.c_int64()
+        _check(lib().cg_md_server_submit(self._h, ctypes.byref(req), ctypes.byref(tk)))
+        self._natoms[tk.value] = len(t)
+        return tk.value
+
+    def poll(self, ticket, wait=False):
+        out = np.zeros((self._natoms[ticket], 3))
+        res = MdResult()
+        rc = lib().cg_md_server_poll(self._h, int(ticket), 1 if wait else 0, ctypes.byref(res), _ptr(out))
+        if rc == CG_PENDING:
+            return None
+        _check(rc)
+        r = np.array([(res.admitted, res.finished, res.step_ms_sum, res.step_ms_max, res.reserved_bytes)],
+                     dtype=self._RESULT)[0]
+        return out, r
+
+    def stop(self):
+        """Finishes every queued and running request; returns the batched steps run."""
+        if self._h is None:
+            return 0
+        nb = ctypes.c_int64()
+        h, self._h = self._h, None
+        _check(lib().cg_md_server_stop(h, ctypes.byref(nb)))
+        return nb.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None:
+            lib().cg_md_server_stop(self._h, None)
+            self._h = None
+
+
 class Session:
     """One GPU (device ordinal) with a CUDA stream, bound to a model."""
 
@@ -764,6 +826,12 @@ class Session:
         _check(lib().cg_md_serve_memory(self._h, int(max_batch_atoms), int(max_batch_frames), ctypes.byref(a),
                                         ctypes.byref(p)))
         return a.value, p.value
+
+    def md_server(self, masses, dt_fs=0.2, hbm_budget=150e9, max_batch_atoms=1 << 16, max_batch_frames=1024):
+        """Live continuous-batching server on this session (cg_md_server_start): submit
+        requests from any thread while it runs, poll their results, stop() at the end.
+        The session belongs to the server until stop()."""
+        return MdServer(self, masses, dt_fs, hbm_budget, max_batch_atoms, max_batch_frames)
 
     def md_last_counts(self):
         v = [ctypes.c_int64() for _ in range(4)]

@@ -12,6 +12,7 @@
 
 #include "model.h"
 #include "session.h"
+#include "md_server.h"
 #include "textio.h"
 #include "mdio.h"
 
@@ -25,6 +26,9 @@ struct cg_session {
     std::unique_ptr<cg::Session> s;
     cg::AssembleStats last;
     cg::MdCounts md_last;
+};
+struct cg_md_server {
+    std::unique_ptr<cg::MdServer> srv;
 };
 struct cg_batch_fit {
     std::unique_ptr<cg::BatchFit> b;
@@ -752,6 +756,56 @@ int cg_md_serve(cg_session* s, int nreq, const cg_md_request* req, const double*
             results[r].step_ms_sum = out[r].step_ms_sum; results[r].step_ms_max = out[r].step_ms_max;
             results[r].reserved_bytes = out[r].reserved_bytes;
         }
+        if (batch_steps) *batch_steps = nb;
+    });
+}
+
+int cg_md_server_start(cg_session* s, const double* mass, double dt_fs, double hbm_budget_bytes,
+                       int64_t max_batch_atoms, int max_batch_frames, cg_md_server** out) {
+    return guarded([&] {
+        need(s && mass && out, "session/mass/out");
+        need(dt_fs > 0.0 && max_batch_atoms > 0 && max_batch_frames > 0 && hbm_budget_bytes > 0.0, "limits");
+        cg::MdServeOptions opt;
+        opt.dt = dt_fs / 48.888;   // internal time unit in fs (src/functions.h:44)
+        opt.hbm_budget = hbm_budget_bytes;
+        opt.max_batch_atoms = max_batch_atoms;
+        opt.max_batch_frames = max_batch_frames;
+        std::unique_ptr<cg_md_server> h(new cg_md_server());
+        h->srv.reset(new cg::MdServer(*s->s, mass, opt));
+        *out = h.release();
+    });
+}
+
+int cg_md_server_submit(cg_md_server* srv, const cg_md_request* req, int64_t* ticket) {
+    return guarded([&] {
+        need(srv && req && ticket, "server/request/ticket");
+        cg::MdRequest q;
+        q.natoms = req->natoms; q.nsteps = req->nsteps; q.arrival = 0.0;
+        q.types = req->types; q.xyz = req->xyz; q.cell = req->cell; q.v = req->v; q.xyz_out = nullptr;
+        *ticket = srv->srv->submit(q);
+    });
+}
+
+int cg_md_server_poll(cg_md_server* srv, int64_t ticket, int wait, cg_md_result* result, double* xyz_out) {
+    int rc = 0;
+    const int g = guarded([&] {
+        need(srv, "server");
+        cg::MdResult r;
+        rc = srv->srv->poll(ticket, wait != 0, &r, xyz_out);
+        if (rc == 0 && result) {
+            result->admitted = r.admitted; result->finished = r.finished;
+            result->step_ms_sum = r.step_ms_sum; result->step_ms_max = r.step_ms_max;
+            result->reserved_bytes = r.reserved_bytes;
+        }
+    });
+    return g ? g : rc;
+}
+
+int cg_md_server_stop(cg_md_server* srv, int64_t* batch_steps) {
+    return guarded([&] {
+        need(srv, "server");
+        std::unique_ptr<cg_md_server> h(srv);   // freed on every path
+        const int64_t nb = h->srv->stop();
         if (batch_steps) *batch_steps = nb;
     });
 }

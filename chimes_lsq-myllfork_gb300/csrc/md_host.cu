@@ -18,6 +18,7 @@
 #include "md.h"
 #include "scratch.h"
 #include "session.h"
+#include "md_server.h"
 
 namespace cg {
 
@@ -815,44 +816,97 @@ void Session::md_serve_memory(int64_t max_batch_atoms, int max_batch_frames, dou
     if (per_atom) *per_atom = 2.0 * serve_list_per_atom_;
 }
 
+cgd::BoxDev Session::serve_check(const MdRequest& q, const MdServeOptions& opt, const std::string& who) const {
+    const Model& m = model_;
+    const int nt = m.ctl.natmtyp;
+    if (q.natoms <= 0 || q.nsteps <= 0 || !q.types || !q.xyz || !q.cell || !q.v)
+        throw Error(1, who + ": empty or incomplete");
+    if (q.natoms > opt.max_batch_atoms) throw Error(1, who + ": larger than the batch capacity");
+    if (q.natoms > 8191) throw Error(2, "frames above 8191 atoms are not supported on the device");
+    for (int a = 0; a < q.natoms; ++a)
+        if (q.types[a] < 0 || q.types[a] >= nt) throw Error(1, who + ": atom type index out of range");
+    Box b;
+    b.ax = q.cell[0]; b.ay = q.cell[1]; b.az = q.cell[2]; b.bx = q.cell[3]; b.by = q.cell[4]; b.bz = q.cell[5];
+    b.cx = q.cell[6]; b.cy = q.cell[7]; b.cz = q.cell[8];
+    b.update_cell();
+    if (b.ax <= 0.0 || b.by <= 0.0 || b.cz <= 0.0 || b.ay != 0.0 || b.az != 0.0 || b.bz != 0.0)
+        throw Error(2, "cell must be upper triangular with a positive diagonal");
+    cgd::BoxDev bd;
+    std::memset(&bd, 0, sizeof(bd));
+    for (int k = 0; k < 9; ++k) { bd.h[k] = b.hmat[k]; bd.inv[k] = b.invr[k]; }
+    bd.lx = b.lx; bd.ly = b.ly; bd.lz = b.lz; bd.vol = b.vol;
+    bd.is_ortho = b.is_ortho ? 1 : 0;
+    set_small(bd, frame_is_small(m, b, false));
+    if (md_ && md_->dev.coulomb) {   // optimal_ewald_params for the request's cell
+        if (!b.is_ortho) throw Error(2, "the Ewald sums need an orthorhombic cell");
+        const EwaldParams ep = ewald_params(q.natoms, b);
+        bd.ew_alpha = ep.alpha; bd.ew_rc = ep.rc; bd.ew_kmax = ep.kmax;
+    }
+    return bd;
+}
+
+double Session::serve_fixed_bytes(const MdServeOptions& opt) const {
+    const int L = model_.ctl.nlayers;
+    const int nimg = (2 * L + 1) * (2 * L + 1) * (2 * L + 1);
+    return 2.0 * (double)arena_bytes(opt.max_batch_atoms, std::max(1, opt.max_batch_frames), nimg);
+}
+
+namespace {
+// cg_md_serve's requests: a fixed list, offered in order of arrival time.
+struct ListSource : ServeSource {
+    const std::vector<MdRequest>& req;
+    MdResult* res;
+    std::vector<int> order;
+    size_t next_pending = 0;
+    ListSource(const std::vector<MdRequest>& r, MdResult* out) : req(r), res(out), order(r.size()) {
+        for (size_t k = 0; k < r.size(); ++k) order[k] = (int)k;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return req[a].arrival < req[b].arrival; });
+    }
+    int next(double now) override {
+        if (next_pending < order.size() && req[order[next_pending]].arrival <= now) return order[next_pending];
+        return -1;
+    }
+    void admitted() override { ++next_pending; }
+    const MdRequest& request(int id) override { return req[id]; }
+    bool wait(double now) override {
+        if (next_pending >= order.size()) return false;
+        const double w = req[order[next_pending]].arrival - now;
+        if (w > 0) std::this_thread::sleep_for(std::chrono::duration<double>(w));
+        return true;
+    }
+    void finished(int id, const MdResult& r) override { res[id] = r; }
+};
+}  // namespace
+
 int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_type, const MdServeOptions& opt,
                           MdResult* res, double* step_ms) {
     CK(cudaSetDevice(device_));
     if (!md_) throw Error(1, "MD coefficients are not set (cg_md_setup)");
+    const double fixed = serve_fixed_bytes(opt);
+    if (fixed > opt.hbm_budget)
+        throw Error(1, "hbm_budget of " + std::to_string((long long)opt.hbm_budget) + " bytes is below the " +
+                           std::to_string((long long)fixed) + " bytes of the serving arenas for max_batch_atoms");
+    int stride = 0;
+    for (size_t r = 0; r < req.size(); ++r) {
+        serve_check(req[r], opt, "request " + std::to_string(r));
+        stride = std::max(stride, req[r].nsteps);
+        if (fixed + serve_need_bytes(req[r].natoms) > opt.hbm_budget)
+            throw Error(1, "request " + std::to_string(r) + " alone needs more device memory (" +
+                               std::to_string((long long)(fixed + serve_need_bytes(req[r].natoms))) +
+                               " bytes with the arenas) than hbm_budget allows");
+    }
+    ListSource src(req, res);
+    return serve_loop(src, mass_type, opt, step_ms, stride);
+}
+
+int64_t Session::serve_loop(ServeSource& src, const double* mass_type, const MdServeOptions& opt, double* step_ms,
+                            int stride) {
+    CK(cudaSetDevice(device_));
+    if (!md_) throw Error(1, "MD coefficients are not set (cg_md_setup)");
     const Model& m = model_;
     const int nt = m.ctl.natmtyp;
-    const int nreq = (int)req.size();
     const int L = m.ctl.nlayers;
     const int nimg = (2 * L + 1) * (2 * L + 1) * (2 * L + 1);
-    int stride = 0;
-    std::vector<cgd::BoxDev> boxes(nreq);
-    for (int r = 0; r < nreq; ++r) {
-        const MdRequest& q = req[r];
-        if (q.natoms <= 0 || q.nsteps <= 0 || !q.types || !q.xyz || !q.cell || !q.v)
-            throw Error(1, "request " + std::to_string(r) + ": empty or incomplete");
-        if (q.natoms > opt.max_batch_atoms) throw Error(1, "request larger than the batch capacity");
-        if (q.natoms > 8191) throw Error(2, "frames above 8191 atoms are not supported on the device");
-        for (int a = 0; a < q.natoms; ++a)
-            if (q.types[a] < 0 || q.types[a] >= nt) throw Error(1, "atom type index out of range");
-        stride = std::max(stride, q.nsteps);
-        Box b;
-        b.ax = q.cell[0]; b.ay = q.cell[1]; b.az = q.cell[2]; b.bx = q.cell[3]; b.by = q.cell[4]; b.bz = q.cell[5];
-        b.cx = q.cell[6]; b.cy = q.cell[7]; b.cz = q.cell[8];
-        b.update_cell();
-        if (b.ax <= 0.0 || b.by <= 0.0 || b.cz <= 0.0 || b.ay != 0.0 || b.az != 0.0 || b.bz != 0.0)
-            throw Error(2, "cell must be upper triangular with a positive diagonal");
-        cgd::BoxDev& bd = boxes[r];
-        std::memset(&bd, 0, sizeof(bd));
-        for (int k = 0; k < 9; ++k) { bd.h[k] = b.hmat[k]; bd.inv[k] = b.invr[k]; }
-        bd.lx = b.lx; bd.ly = b.ly; bd.lz = b.lz; bd.vol = b.vol;
-        bd.is_ortho = b.is_ortho ? 1 : 0;
-        set_small(bd, frame_is_small(m, b, false));
-        if (md_ && md_->dev.coulomb) {   // optimal_ewald_params for the request's cell
-            if (!b.is_ortho) throw Error(2, "the Ewald sums need an orthorhombic cell");
-            const EwaldParams ep = ewald_params(q.natoms, b);
-            bd.ew_alpha = ep.alpha; bd.ew_rc = ep.rc; bd.ew_kmax = ep.kmax;
-        }
-    }
     std::vector<double> mv(mass_type, mass_type + nt), im(nt);
     for (int i = 0; i < nt; ++i) {
         if (!(mv[i] > 0.0)) throw Error(1, "atom masses must be positive");
@@ -866,16 +920,10 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
     // of n atoms reserves 2 * list_per_atom * n bytes (the current lists and the set
     // built ahead of need); list_per_atom starts from a prior and is replaced by the
     // lists' measured allocation per atom after every build (never shrinking).
-    const double fixed = 2.0 * (double)arena_bytes(cap_atoms, cap_frames, nimg);
+    const double fixed = serve_fixed_bytes(opt);
     if (fixed > opt.hbm_budget)
         throw Error(1, "hbm_budget of " + std::to_string((long long)opt.hbm_budget) + " bytes is below the " +
                            std::to_string((long long)fixed) + " bytes of the serving arenas for max_batch_atoms");
-    auto need = [&](int64_t atoms) { return 2.0 * serve_list_per_atom_ * (double)atoms; };
-    for (int r = 0; r < nreq; ++r)
-        if (fixed + need(req[r].natoms) > opt.hbm_budget)
-            throw Error(1, "request " + std::to_string(r) + " alone needs more device memory (" +
-                               std::to_string((long long)(fixed + need(req[r].natoms))) +
-                               " bytes with the arenas) than hbm_budget allows");
     ServeArena arena[2];
     arena[0].init(cap_atoms, cap_frames, nimg);
     arena[1].init(cap_atoms, cap_frames, nimg);
@@ -893,44 +941,49 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
     h_nat.reserve(cap_frames); h_aofs.reserve(cap_frames + 1); h_gofs.reserve(cap_frames + 1);
     h_box.reserve(cap_frames); h_first.reserve(cap_frames); h_type.reserve(cap_atoms);
 
-    std::vector<int> order(nreq);
-    for (int r = 0; r < nreq; ++r) order[r] = r;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return req[a].arrival < req[b].arrival; });
-    std::vector<int> active, steps_done(nreq, 0);
-    std::vector<int64_t> pos(nreq, -1);      // atom offset of each active request in the current arena
-    std::vector<char> first(nreq, 0);
-    int cur = 0, next_pending = 0, finished = 0;
+    // per-request state, by id
+    std::vector<int> steps_done;
+    std::vector<int64_t> pos;      // atom offset of each active request in the current arena
+    std::vector<char> first;
+    std::vector<MdResult> res;
+    std::vector<cgd::BoxDev> boxes;
+    auto grow = [&](int id) {
+        if ((int)steps_done.size() > id) return;
+        const size_t n = (size_t)id + 1;
+        steps_done.resize(n, 0); pos.resize(n, -1); first.resize(n, 0); res.resize(n); boxes.resize(n);
+    };
+    std::vector<int> active, done_now;
+    int cur = 0;
     int64_t active_atoms = 0, nbatch = 0;
     MdListSet lists;   // skin lists of the current composition
     int64_t builds_seen = 0;
     bool changed = false;
     const auto t0 = std::chrono::steady_clock::now();
-    while (finished < nreq) {
+    for (;;) {
         // admit every arrived request that fits
-        double t = now_s(t0);
-        while (next_pending < nreq) {
-            const MdRequest& q = req[order[next_pending]];
-            if (q.arrival > t || active_atoms + q.natoms > cap_atoms || (int)active.size() >= cap_frames) break;
-            if (fixed + need(active_atoms + q.natoms) > opt.hbm_budget) {
+        const double t = now_s(t0);
+        for (int id; (id = src.next(t)) >= 0;) {
+            const MdRequest& q = src.request(id);
+            if (active_atoms + q.natoms > cap_atoms || (int)active.size() >= cap_frames) break;
+            if (fixed + serve_need_bytes(active_atoms + q.natoms) > opt.hbm_budget) {
                 if (active.empty())   // the measured list size leaves no room for it even alone
-                    throw Error(4, "request " + std::to_string(order[next_pending]) +
+                    throw Error(4, "request " + std::to_string(id) +
                                        " needs more device memory than hbm_budget allows (measured list size " +
                                        std::to_string((long long)serve_list_per_atom_) + " bytes per atom)");
                 break;
             }
-            const int r = order[next_pending++];
-            active.push_back(r);
+            grow(id);
+            boxes[id] = serve_check(q, opt, "request " + std::to_string(id));
+            src.admitted();
+            active.push_back(id);
             active_atoms += q.natoms;
-            first[r] = 1;
-            res[r].admitted = t;
-            res[r].reserved_bytes = need(q.natoms);
+            first[id] = 1;
+            res[id].admitted = t;
+            res[id].reserved_bytes = serve_need_bytes(q.natoms);
             changed = true;
         }
         if (active.empty()) {
-            if (next_pending < nreq) {
-                const double wait = req[order[next_pending]].arrival - now_s(t0);
-                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
-            }
+            if (!src.wait(now_s(t0))) break;
             continue;
         }
         ServeArena& A = arena[cur];
@@ -942,13 +995,14 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
             h_aofs.p[0] = 0; h_gofs.p[0] = 0;
             for (int k = 0; k < nf; ++k) {
                 const int r = active[k];
-                const int n = req[r].natoms;
+                const MdRequest& q = src.request(r);
+                const int n = q.natoms;
                 h_nat.p[k] = n;
                 h_box.p[k] = boxes[r];
-                std::memcpy(h_type.p + ofs, req[r].types, n * sizeof(int));
+                std::memcpy(h_type.p + ofs, q.types, n * sizeof(int));
                 if (first[r]) {
-                    CK(cudaMemcpyAsync(B.xyz + 3 * ofs, req[r].xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
-                    CK(cudaMemcpyAsync(B.v + 3 * ofs, req[r].v, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+                    CK(cudaMemcpyAsync(B.xyz + 3 * ofs, q.xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+                    CK(cudaMemcpyAsync(B.v + 3 * ofs, q.v, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
                     CK(cudaMemsetAsync(B.acc + 3 * ofs, 0, 3 * n * sizeof(double), st));
                 } else {
                     const size_t bytes = 3 * n * sizeof(double);
@@ -1003,36 +1057,173 @@ int64_t Session::md_serve(const std::vector<MdRequest>& req, const double* mass_
             builds_seen = nbuilds;
             size_t bytes = 0;
             for (size_t c : lists.current().caps) bytes += c;
-            serve_list_per_atom_ = std::max(serve_list_per_atom_, (double)bytes / (double)active_atoms);
+            serve_list_per_atom_ = std::max((double)serve_list_per_atom_, (double)bytes / (double)active_atoms);
         }
         // bookkeeping, retire finished requests
         std::vector<int> keep;
         keep.reserve(active.size());
+        done_now.clear();
         for (int r : active) {
-            if (step_ms) step_ms[(size_t)r * stride + steps_done[r]] = ms;
+            const MdRequest& q = src.request(r);
+            if (step_ms && steps_done[r] < stride) step_ms[(size_t)r * stride + steps_done[r]] = ms;
             res[r].step_ms_sum += ms;
             res[r].step_ms_max = std::max(res[r].step_ms_max, ms);
             first[r] = 0;
-            if (++steps_done[r] == req[r].nsteps) {
-                if (req[r].xyz_out)
-                    CK(cudaMemcpyAsync(req[r].xyz_out, C.xyz + 3 * pos[r], 3 * req[r].natoms * sizeof(double),
+            if (++steps_done[r] == q.nsteps) {
+                if (q.xyz_out)
+                    CK(cudaMemcpyAsync(q.xyz_out, C.xyz + 3 * pos[r], 3 * q.natoms * sizeof(double),
                                        cudaMemcpyDeviceToHost, st));
-                active_atoms -= req[r].natoms;
-                ++finished;
+                active_atoms -= q.natoms;
+                done_now.push_back(r);
                 changed = true;
             } else {
                 keep.push_back(r);
             }
         }
-        if (changed) {
+        if (!done_now.empty()) {
             CK(cudaStreamSynchronize(st));
             const double tf = now_s(t0);
-            for (int r : active)
-                if (steps_done[r] == req[r].nsteps && res[r].finished == 0.0) res[r].finished = tf;
+            for (int r : done_now) {
+                res[r].finished = tf;
+                src.finished(r, res[r]);
+            }
         }
         active.swap(keep);
     }
     return nbatch;
+}
+
+// ---------------------------------------------------------------- live serving
+MdServer::MdServer(Session& s, const double* mass_type, const MdServeOptions& opt)
+    : s_(s), mass_(mass_type, mass_type + s.model().ctl.natmtyp), opt_(opt) {
+    const double fixed = s_.serve_fixed_bytes(opt_);
+    if (fixed > opt_.hbm_budget)
+        throw Error(1, "hbm_budget of " + std::to_string((long long)opt_.hbm_budget) + " bytes is below the " +
+                           std::to_string((long long)fixed) + " bytes of the serving arenas for max_batch_atoms");
+    for (double mv : mass_)
+        if (!(mv > 0.0)) throw Error(1, "atom masses must be positive");
+    th_ = std::thread([this] { run(); });
+}
+
+MdServer::~MdServer() {
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        stopping_ = true;
+    }
+    cv_.notify_all();
+    if (th_.joinable()) th_.join();
+}
+
+void MdServer::run() {
+    int code = 0;
+    std::string msg;
+    int64_t steps = 0;
+    try {
+        steps = s_.serve_loop(*this, mass_.data(), opt_, nullptr, 0);
+    } catch (const Error& e) {
+        code = e.code;
+        msg = e.what();
+    } catch (const std::bad_alloc&) {
+        code = 4;
+        msg = "out of host memory";
+    } catch (const std::exception& e) {
+        code = 3;
+        msg = e.what();
+    }
+    std::lock_guard<std::mutex> lk(mu_);
+    steps_ = steps;
+    err_code_ = code;
+    err_msg_ = msg;
+    ended_ = true;
+    cv_.notify_all();
+}
+
+int64_t MdServer::submit(const MdRequest& q) {
+    const double fixed = s_.serve_fixed_bytes(opt_);
+    s_.serve_check(q, opt_, "request");
+    if (fixed + s_.serve_need_bytes(q.natoms) > opt_.hbm_budget)
+        throw Error(1, "the request alone needs more device memory (" +
+                           std::to_string((long long)(fixed + s_.serve_need_bytes(q.natoms))) +
+                           " bytes with the arenas) than hbm_budget allows");
+    std::unique_lock<std::mutex> lk(mu_);
+    if (stopping_ || ended_) throw Error(1, "the server has stopped");
+    t_.emplace_back();
+    Ticket& k = t_.back();
+    k.types.assign(q.types, q.types + q.natoms);
+    k.xyz.assign(q.xyz, q.xyz + 3 * (size_t)q.natoms);
+    k.cell.assign(q.cell, q.cell + 9);
+    k.v.assign(q.v, q.v + 3 * (size_t)q.natoms);
+    k.out.assign(3 * (size_t)q.natoms, 0.0);
+    k.q.natoms = q.natoms;
+    k.q.nsteps = q.nsteps;
+    k.q.arrival = 0.0;
+    k.q.types = k.types.data();
+    k.q.xyz = k.xyz.data();
+    k.q.cell = k.cell.data();
+    k.q.v = k.v.data();
+    k.q.xyz_out = k.out.data();
+    const int64_t ticket = (int64_t)t_.size() - 1;
+    lk.unlock();
+    cv_.notify_all();
+    return ticket;
+}
+
+int MdServer::poll(int64_t ticket, bool wait, MdResult* r, double* xyz) {
+    std::unique_lock<std::mutex> lk(mu_);
+    if (ticket < 0 || ticket >= (int64_t)t_.size()) throw Error(1, "unknown ticket");
+    Ticket& k = t_[(size_t)ticket];
+    if (wait) cv_.wait(lk, [&] { return k.done || ended_; });
+    if (k.done) {
+        if (r) *r = k.res;
+        if (xyz) std::memcpy(xyz, k.out.data(), k.out.size() * sizeof(double));
+        return 0;
+    }
+    if (ended_) {
+        if (err_code_) throw Error(err_code_, "serving loop failed: " + err_msg_);
+        throw Error(1, "the server stopped before this request finished");
+    }
+    return CG_PENDING_STATUS;
+}
+
+int64_t MdServer::stop() {
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        stopping_ = true;
+    }
+    cv_.notify_all();
+    if (th_.joinable()) th_.join();
+    if (err_code_) throw Error(err_code_, "serving loop failed: " + err_msg_);
+    return steps_;
+}
+
+int MdServer::next(double) {
+    std::lock_guard<std::mutex> lk(mu_);
+    return next_ < t_.size() ? (int)next_ : -1;
+}
+
+void MdServer::admitted() {
+    std::lock_guard<std::mutex> lk(mu_);
+    ++next_;
+}
+
+const MdRequest& MdServer::request(int id) {
+    std::lock_guard<std::mutex> lk(mu_);
+    return t_[(size_t)id].q;   // deque elements do not move when the queue grows
+}
+
+bool MdServer::wait(double) {
+    std::unique_lock<std::mutex> lk(mu_);
+    cv_.wait(lk, [&] { return next_ < t_.size() || stopping_; });
+    return next_ < t_.size();
+}
+
+void MdServer::finished(int id, const MdResult& r) {
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        t_[(size_t)id].res = r;
+        t_[(size_t)id].done = true;
+    }
+    cv_.notify_all();
 }
 
 }  // namespace cg

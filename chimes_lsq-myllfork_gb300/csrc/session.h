@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <functional>
 #include <initializer_list>
 #include <memory>
@@ -157,6 +158,23 @@ struct MdServeOptions {
     double hbm_budget = 150e9;            // bytes of device memory requests may hold
     int64_t max_batch_atoms = 1 << 16;
     int max_batch_frames = 1024;
+};
+
+// Where the serving loop (Session::serve_loop) takes its requests from: the fixed
+// list of cg_md_serve, or the queue that cg_md_server_submit fills while the loop
+// runs.  Requests have dense ids 0, 1, 2, ... in the order the source offers them.
+struct ServeSource {
+    virtual ~ServeSource() = default;
+    // The next request to admit if it has arrived by `now` (seconds on the loop's
+    // clock), else -1.  The same id is offered again until admitted() is called.
+    virtual int next(double now) = 0;
+    virtual void admitted() = 0;
+    virtual const MdRequest& request(int id) = 0;
+    // Called when no request is running: waits until next() may offer one; false
+    // when no request will come any more.
+    virtual bool wait(double now) = 0;
+    // Request id has finished: its final positions are in its xyz_out.
+    virtual void finished(int id, const MdResult& r) = 0;
 };
 
 // Sizes of one batch's work lists, recorded by a sizing pass so that later passes
@@ -330,6 +348,16 @@ class Session {
     // = largest nsteps.  Returns the number of batched steps.
     int64_t md_serve(const std::vector<MdRequest>& req, const double* mass_type, const MdServeOptions& opt,
                      MdResult* res, double* step_ms);
+    // The loop itself, over any request source (step_ms as above, or null).
+    int64_t serve_loop(ServeSource& src, const double* mass_type, const MdServeOptions& opt, double* step_ms,
+                       int stride);
+    // Checks one serving request against the model and the loop's capacities (throws
+    // Error 1 / 2) and returns its device box.
+    cgd::BoxDev serve_check(const MdRequest& q, const MdServeOptions& opt, const std::string& who) const;
+    // Device memory of the loop's two arenas, and what a running request of `atoms`
+    // atoms reserves for its lists.
+    double serve_fixed_bytes(const MdServeOptions& opt) const;
+    double serve_need_bytes(int64_t atoms) const { return 2.0 * serve_list_per_atom_ * (double)atoms; }
     // Device memory of the serving loop: the fixed bytes of its two arenas for these
     // capacities, and the bytes a request reserves per atom (list estimate; measured
     // by the last serving run of this session, a prior before any).
@@ -377,7 +405,7 @@ class Session {
     int force4_threads_ = 512;
     int64_t gram_plane_rows(int64_t nrows, int ncols) const;
     double md_skin_ = 0.5;   // Angstrom; 0: enumerate every step
-    double serve_list_per_atom_ = 6144.0;   // list bytes per atom (measured by md_serve)
+    std::atomic<double> serve_list_per_atom_{6144.0};   // list bytes per atom (measured by the serving loop)
     std::vector<double> md_state_;   // last md_run: nframes * MD_TH_STRIDE
     MdThermostat md_last_th_;
     std::vector<double> md_resume_;  // next md_run's starting restart values (nframes * 29)

@@ -472,6 +472,31 @@ int cg_md_serve(cg_session* s, int nreq, const cg_md_request* req, const double*
                 double hbm_budget_bytes, int64_t max_batch_atoms, int max_batch_frames, cg_md_result* results,
                 double* step_ms, int64_t* batch_steps);
 
+/* Live form of cg_md_serve (no counterpart in the reference): a thread of the library
+ * runs the same batching loop on the session's GPU while the caller's threads submit
+ * requests as they arrive and collect results, so a request submitted while others
+ * are on the GPU joins the next batched step once the batch has room.  The session
+ * belongs to the server until cg_md_server_stop (make no other call on it meanwhile).
+ * Capacities and hbm_budget_bytes as in cg_md_serve; mass: one per atom type (amu). */
+typedef struct cg_md_server cg_md_server;
+int cg_md_server_start(cg_session* s, const double* mass, double dt_fs, double hbm_budget_bytes,
+                       int64_t max_batch_atoms, int max_batch_frames, cg_md_server** out);
+/* Queue one request (arrival = now: req->arrival and req->xyz_out are not read); its
+ * inputs are copied before the call returns.  *ticket identifies it in
+ * cg_md_server_poll.  Status 1 / 2 for a request that can never run: bad input, more
+ * atoms than max_batch_atoms, more device memory than hbm_budget_bytes alone. */
+int cg_md_server_submit(cg_md_server* srv, const cg_md_request* req, int64_t* ticket);
+/* Status of a ticket: 0 once the request finished (result and, when xyz_out is not
+ * NULL, its final positions, 3 per atom), CG_PENDING while it waits or runs (wait = 0),
+ * or, with wait != 0, blocks until it finishes.  A failure of the serving loop (status
+ * 3 or 4) is returned by every later poll and by cg_md_server_stop. */
+#define CG_PENDING 5
+int cg_md_server_poll(cg_md_server* srv, int64_t ticket, int wait, cg_md_result* result, double* xyz_out);
+/* Stop taking requests, finish every queued and running one, end the thread and free
+ * the server (also when a status is returned).  *batch_steps (may be NULL): batched
+ * steps run. */
+int cg_md_server_stop(cg_md_server* srv, int64_t* batch_steps);
+
 /* Device memory of cg_md_serve for these capacities: arena_bytes = the two serving
  * arenas, bytes_per_atom = what an admitted request reserves per atom (the session's
  * last measured list size, or the prior before its first serving run).  Either output

@@ -81,3 +81,41 @@ def test_serving_refuses_budgets_it_cannot_meet(cg, tmp_path):
         with pytest.raises(cg.ChimesError) as e:
             sess.md_serve(reqs, MASSES, dt_fs=0.2, hbm_budget=budget, max_batch_atoms=512, max_batch_frames=4)
         assert e.value.code == 1
+
+
+def test_live_server_same_as_alone(cg, tmp_path):
+    """cg_md_server_*: a client thread submits requests at intervals while earlier
+    ones are on the GPU; every result equals the same request run alone through
+    cg_md_serve (FP32 form, 1e-8 A), requests overlap in batched steps, a request too
+    large for the batch is refused at submission, and poll reports unfinished tickets
+    as pending."""
+    import threading
+    import time
+    model, x, reqs = _requests(cg, tmp_path, [1024, 700, 1100, 900, 300], (16, 8, 4), 321, 12, 0.0)
+    sess = cg.Session(model, 0)
+    sess.md_setup(x, precision=cg.CG_FP32)
+    alone, _, _, _ = sess.md_serve(reqs, MASSES, dt_fs=0.2, max_batch_frames=1)
+    srv = sess.md_server(MASSES, dt_fs=0.2, max_batch_atoms=4096, max_batch_frames=4)
+    tickets = []
+    with pytest.raises(RuntimeError):
+        srv.submit(np.zeros(5000, dtype=np.int32), np.zeros((5000, 3)), reqs[0]["cell"], np.zeros((5000, 3)), 1)
+
+    def client():
+        for q in reqs:
+            tickets.append(srv.submit(q["types"], q["xyz"], q["cell"], q["v"], q["nsteps"]))
+            time.sleep(0.002)
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    pending_seen = any(srv.poll(t) is None for t in tickets)
+    outs = [srv.poll(t, wait=True) for t in tickets]
+    nb = srv.stop()
+    worst = max(float(np.abs(o[0] - a).max()) for o, a in zip(outs, alone))
+    overlap = sum(1 for i in range(len(outs)) for j in range(i + 1, len(outs))
+                  if outs[i][1]["admitted"] < outs[j][1]["finished"] and outs[j][1]["admitted"] < outs[i][1]["finished"])
+    print(f"\nlive server: {nb} batched steps for {len(reqs)} requests of 12 steps; overlapping pairs {overlap}; "
+          f"largest |server - alone| = {worst:.3e} A; pending seen {pending_seen}", flush=True)
+    assert worst <= 1e-8
+    assert overlap > 0 and nb < 12 * len(reqs)
+    assert all(o[1]["finished"] >= o[1]["admitted"] for o in outs)
