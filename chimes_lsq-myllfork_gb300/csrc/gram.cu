@@ -6,10 +6,10 @@
 //  * mixed form: A is split into two BF16 planes (hi = bf16(a), lo = bf16(a - hi)),
 //    stored transposed (K = rows contiguous), and G += hi^T hi + hi^T lo + lo^T hi on
 //    tcgen05 (kind::f16, FP32 accumulation in TMEM).  A persistent CTA per SM walks
-//    the upper-triangle tile pairs: operands arrive by TMA with 128-byte swizzle
-//    through a 3-stage mbarrier ring, one thread issues the MMAs into one of two TMEM
-//    accumulators, and four epilogue warps drain the other with tcgen05.ld and add
-//    it into an FP64 G.
+//    the 128 x 256 (or, for small Grams, 128 x 128) tiles that reach the upper
+//    triangle: operands arrive by TMA with 128-byte swizzle through a 192 KB mbarrier
+//    ring, one thread issues the MMAs into one of two TMEM accumulators, and four
+//    epilogue warps drain the other with tcgen05.ld and add it into an FP64 G.
 //  * plain form: FP64 G by this library's register-blocked FP64 SYRK (dense64.cu),
 //    which runs at the FP64 FMA rate of the GPU.
 //  * h = A^T b is an FP64 matrix-vector product (plain form) or is fused into the
@@ -26,15 +26,15 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <utility>
 
 #include "dense64.h"
 #include "gram.h"
 
 namespace cgd {
 
-constexpr int GB_M = 128, GB_N = 128, GB_K = 64, GB_STAGES = 3, GB_THREADS = 192;
-constexpr uint32_t GB_TILE_BYTES = GB_M * GB_K * 2;         // one 128x64 bf16 operand tile (16 KB)
-constexpr uint32_t GB_STAGE_BYTES = 4 * GB_TILE_BYTES;      // A_hi, A_lo, B_hi, B_lo
+constexpr int GB_M = 128, GB_K = 64, GB_THREADS = 192;
+constexpr uint32_t GB_TILE_A = GB_M * GB_K * 2;             // one 128x64 bf16 row-tile operand (16 KB)
 constexpr long long GB_WAIT_CYCLES = 4000000000LL;          // ~2 s at 2 GHz
 constexpr int GB_EPI_LD = 33;                               // epilogue staging row (floats)
 
@@ -228,83 +228,104 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                  : "memory");
 }
 
-// Tile pair (ti <= tj) of CTA t.  The upper triangle is walked in super-tiles of
-// GB_GROUP x GB_GROUP tile pairs (super-tile pairs by rows, tiles inside column by
-// column), so that the CTAs resident at one time -- about one super-tile -- read
-// GB_GROUP row tiles and GB_GROUP column tiles between them, which stay in L2, instead
-// of one row tile and a different column tile each.
-constexpr int GB_GROUP = 12;
-__device__ __forceinline__ void grouped_pair(int t, int ntile, int& ti, int& tj) {
-    const int G = GB_GROUP;
-    const int nsup = (ntile + G - 1) / G;
-    int SI = 0;
-    for (; SI < nsup; ++SI) {
-        const int r = min(G, ntile - SI * G);
-        const int cnt = r * (r + 1) / 2 + r * max(0, ntile - (SI + 1) * G);
-        if (t < cnt) break;
-        t -= cnt;
+// Tile pair t of the Gram's upper triangle: ti indexes 128-row tiles, tj column
+// tiles of Q x 128 columns, and a pair is kept when its tile reaches the upper
+// triangle (tj >= ti / Q).  Pairs are walked in super-tiles of GB_GR row tiles x
+// GB_GR / Q column tiles (the same 1536 rows and columns), super-tiles of one
+// super-row in column order, tiles inside a super-tile column by column: the ~150
+// units in flight at one time read about 12 row tiles and 12 / Q column tiles between
+// them, which stay in L2.
+constexpr int GB_GR = 12;
+template <int Q>
+__device__ __forceinline__ void grouped_pair(int t, int nti, int ntj, int& ti, int& tj) {
+    constexpr int GB_GC = GB_GR / Q;
+    const int nsr = (nti + GB_GR - 1) / GB_GR;
+    for (int SI = 0; SI < nsr; ++SI) {
+        const int r0 = SI * GB_GR, r1 = min(nti, r0 + GB_GR), r = r1 - r0;
+        const int c0 = SI * GB_GC, c1 = min(ntj, c0 + GB_GC);
+        if (c0 >= ntj) break;
+        int diag = 0;
+        for (int i = r0; i < r1; ++i) diag += max(0, c1 - max(c0, i / Q));
+        if (t < diag) {   // the diagonal super-tile, by rows
+            for (int i = r0; i < r1; ++i) {
+                const int lo = max(c0, i / Q), cnt = max(0, c1 - lo);
+                if (t < cnt) { ti = i; tj = lo + t; return; }
+                t -= cnt;
+            }
+        }
+        t -= diag;
+        const int off = r * max(0, ntj - c1);
+        if (t < off) {    // full super-tiles to the right, column by column
+            const int SJ = SI + 1 + t / (r * GB_GC), tt = t % (r * GB_GC);
+            ti = r0 + tt % r;
+            tj = SJ * GB_GC + tt / r;
+            return;
+        }
+        t -= off;
     }
-    const int r = min(G, ntile - SI * G);
-    const int dcnt = r * (r + 1) / 2;
-    if (t < dcnt) {   // the diagonal super-tile, upper triangle by rows
-        int li = 0;
-        while (t >= r - li) { t -= r - li; ++li; }
-        ti = SI * G + li;
-        tj = ti + t;
-        return;
-    }
-    t -= dcnt;
-    for (int SJ = SI + 1; SJ < nsup; ++SJ) {
-        const int c = min(G, ntile - SJ * G);
-        if (t < r * c) { ti = SI * G + t % r; tj = SJ * G + t / r; return; }
-        t -= r * c;
-    }
-    ti = tj = 0;   // not reached for t < ntile (ntile + 1) / 2
+    ti = tj = 0;   // not reached for t < the pair count
 }
 
 // ---------------------------------------------------------------- tcgen05 Gram tiles
 // Persistent kernel, one CTA per SM.  A work unit is a (tile pair i <= j, K slice);
 // CTA b takes units b, b + gridDim.x, ... in grouped tile-pair order, so the units in
 // flight at one time stay close in the triangle.  Warp roles:
-//   warp 0      TMA producer: the four 128x64 operand tiles of each K step into a
-//               GB_STAGES-deep ring of stages (full / empty mbarriers);
-//   warp 1      MMA issuer: 12 tcgen05.mma per K step into one of two TMEM
-//               accumulators (128 columns each), committed to acc_full[buf];
+//   warp 0      TMA producer: the hi / lo 128x64 row-tile and BNx64 column-tile
+//               operands of each K step into a GB_STAGES-deep ring of stages
+//               (full / empty mbarriers);
+//   warp 1      MMA issuer: 12 tcgen05.mma (M 128, N BN, K 16) per K step into one
+//               of two TMEM accumulators (BN columns each), committed to acc_full[buf];
 //   warps 2..5  epilogue: tcgen05.ld of the accumulator (TMEM lane quarter =
 //               warp % 4), staged 32 columns at a time through shared memory so that
 //               every FP64 atomic instruction adds 32 consecutive columns of a row of
 //               G, then acc_empty[buf] frees the accumulator.
 // With two accumulators the epilogue of one unit runs under the MMAs of the next, and
 // the ring keeps loading across unit boundaries.
+// BN: columns of a column tile (256 for large Grams; 128 when the triangle has too
+// few tiles to fill the GPU without slicing K, where the wider tile's longer K
+// slices lose their L2 reuse).  Both forms hold 192 KB of operand stages.
 constexpr int GB_ACC = 2;
-struct GbSmem {
-    static constexpr uint32_t epi = GB_STAGES * GB_STAGE_BYTES;
+template <int BN>
+struct GbCfg {
+    static constexpr int N = BN;
+    static constexpr int Q = BN / GB_M;
+    static constexpr int STAGES = BN == 256 ? 2 : 3;
+    static constexpr uint32_t TILE_B = BN * GB_K * 2;
+    static constexpr uint32_t STAGE_BYTES = 2 * GB_TILE_A + 2 * TILE_B;   // A_hi, A_lo, B_hi, B_lo
+    static constexpr uint32_t epi = STAGES * STAGE_BYTES;
     static constexpr uint32_t bars = epi + 4 * 32 * GB_EPI_LD * 4;
-    static constexpr uint32_t nbars = 2 * GB_STAGES + 2 * GB_ACC + 1;
+    static constexpr uint32_t nbars = 2 * STAGES + 2 * GB_ACC + 1;
     static constexpr uint32_t total = bars + nbars * 8 + 16;
+    static_assert(bars % 8 == 0, "mbarrier alignment");
+    static_assert(total + 1024 <= 227 * 1024, "shared memory per CTA");
 };
-static_assert(GbSmem::bars % 8 == 0, "mbarrier alignment");
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-__device__ __forceinline__ int gb_unit(int u, int npairs, int ntile, int64_t kpad, int64_t kslice, int& ti, int& tj,
-                                       int64_t& kb) {
+template <int Q>
+__device__ __forceinline__ int gb_unit(int u, int npairs, int nti, int ntj, int64_t kpad, int64_t kslice, int& ti,
+                                       int& tj, int64_t& kb) {
     const int slice = u / npairs;
-    grouped_pair(u - slice * npairs, ntile, ti, tj);
+    grouped_pair<Q>(u - slice * npairs, nti, ntj, ti, tj);
     kb = (int64_t)slice * kslice;
     const int64_t ke = min(kpad, kb + kslice);
     return ke > kb ? (int)((ke - kb) / GB_K) : 0;
 }
 
+template <int BN>
 __global__ void __launch_bounds__(GB_THREADS, 1)
-    k_gram_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo, int ntile,
-              int npairs, int nunits, int64_t kpad, int64_t kslice, int ncols, double* __restrict__ G,
+    k_gram_tc(const __grid_constant__ CUtensorMap map_hi_a, const __grid_constant__ CUtensorMap map_lo_a,
+              const __grid_constant__ CUtensorMap map_hi_b, const __grid_constant__ CUtensorMap map_lo_b, int nti,
+              int ntj, int npairs, int nunits, int64_t kpad, int64_t kslice, int ncols, double* __restrict__ G,
               int* __restrict__ err) {
+    using Cfg = GbCfg<BN>;
+    constexpr int GB_N = Cfg::N, GB_STAGES = Cfg::STAGES;
+    constexpr uint32_t GB_TILE_B = Cfg::TILE_B, GB_STAGE_BYTES = Cfg::STAGE_BYTES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + GbSmem::bars);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cfg::bars);
     uint64_t* empty = full + GB_STAGES;
     uint64_t* acc_full = empty + GB_STAGES;
     uint64_t* acc_empty = acc_full + GB_ACC;
@@ -336,18 +357,20 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
                 int ti, tj;
                 int64_t kb;
-                const int nk = gb_unit(u, npairs, ntile, kpad, kslice, ti, tj, kb);
+                const int nk = gb_unit<Cfg::Q>(u, npairs, nti, ntj, kpad, kslice, ti, tj, kb);
                 for (int it = 0; it < nk; ++it, ++g) {
                     const int s = (int)(g % GB_STAGES);
                     const uint32_t ph = (uint32_t)(g / GB_STAGES) & 1u;
                     if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
                     unsigned char* st = smem + s * GB_STAGE_BYTES;
+                    // a column tile reaching past the padded column count reads zeros
+                    // (out-of-range rows of a TMA load are filled and still counted)
                     mbar_expect_tx(&full[s], GB_STAGE_BYTES);
                     const int x = (int)(kb + (int64_t)it * GB_K);
-                    tma_load_2d(st, &map_hi, &full[s], x, ti * GB_M);
-                    tma_load_2d(st + GB_TILE_BYTES, &map_lo, &full[s], x, ti * GB_M);
-                    tma_load_2d(st + 2 * GB_TILE_BYTES, &map_hi, &full[s], x, tj * GB_N);
-                    tma_load_2d(st + 3 * GB_TILE_BYTES, &map_lo, &full[s], x, tj * GB_N);
+                    tma_load_2d(st, &map_hi_a, &full[s], x, ti * GB_M);
+                    tma_load_2d(st + GB_TILE_A, &map_lo_a, &full[s], x, ti * GB_M);
+                    tma_load_2d(st + 2 * GB_TILE_A, &map_hi_b, &full[s], x, tj * GB_N);
+                    tma_load_2d(st + 2 * GB_TILE_A + GB_TILE_B, &map_lo_b, &full[s], x, tj * GB_N);
                 }
             }
             // drain after a time-out: the last load issued into each stage completes
@@ -367,7 +390,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
                 int ti, tj;
                 int64_t kb;
-                const int nk = gb_unit(u, npairs, ntile, kpad, kslice, ti, tj, kb);
+                const int nk = gb_unit<Cfg::Q>(u, npairs, nti, ntj, kpad, kslice, ti, tj, kb);
                 if (nk == 0) continue;
                 const int buf = j & 1;
                 if (!mbar_wait(&acc_empty[buf], ((uint32_t)(j >> 1) & 1u) ^ 1u, err, 5)) { ok = false; break; }
@@ -379,8 +402,8 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                     if (!mbar_wait(&full[s], ph, err, 2)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     unsigned char* st = smem + s * GB_STAGE_BYTES;
-                    const uint64_t ahi = smem_desc(st), alo = smem_desc(st + GB_TILE_BYTES);
-                    const uint64_t bhi = smem_desc(st + 2 * GB_TILE_BYTES), blo = smem_desc(st + 3 * GB_TILE_BYTES);
+                    const uint64_t ahi = smem_desc(st), alo = smem_desc(st + GB_TILE_A);
+                    const uint64_t bhi = smem_desc(st + 2 * GB_TILE_A), blo = smem_desc(st + 2 * GB_TILE_A + GB_TILE_B);
 #pragma unroll
                     for (int kk = 0; kk < GB_K / 16; ++kk) {
                         const uint64_t adv = (uint64_t)((kk * 32) >> 4);   // 16 bf16 = 32 B along K
@@ -400,12 +423,12 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
         }
     } else {   // epilogue warps 2..5
         const int q = warp & 3;   // TMEM lane quarter this warp may read
-        float* stile = reinterpret_cast<float*>(smem + GbSmem::epi) + (size_t)(warp - 2) * 32 * GB_EPI_LD;
+        float* stile = reinterpret_cast<float*>(smem + Cfg::epi) + (size_t)(warp - 2) * 32 * GB_EPI_LD;
         int j = 0;
         for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
             int ti, tj;
             int64_t kb;
-            const int nk = gb_unit(u, npairs, ntile, kpad, kslice, ti, tj, kb);
+            const int nk = gb_unit<Cfg::Q>(u, npairs, nti, ntj, kpad, kslice, ti, tj, kb);
             if (nk == 0) continue;
             const int buf = j & 1;
             const bool got = mbar_wait(&acc_full[buf], (uint32_t)(j >> 1) & 1u, err, 3);
@@ -433,7 +456,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 #pragma unroll 4
                     for (int r = 0; r < 32; ++r) {
                         const int row = ti * GB_M + q * 32 + r;
-                        if (row < ncols && col < ncols && (ti != tj || col >= row))
+                        if (row < ncols && col < ncols && col >= row)
                             atomicAdd(G + (int64_t)row * ncols + col, (double)stile[r * GB_EPI_LD + lane]);
                     }
                 }
@@ -481,11 +504,11 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-static CUtensorMap plane_map(void* base, int64_t kpad, int64_t cpad) {
+static CUtensorMap plane_map(void* base, int64_t kpad, int64_t cpad, int box_rows) {
     CUtensorMap m;
     cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)cpad};
     cuuint64_t strides[1] = {(cuuint64_t)(kpad * 2)};
-    cuuint32_t box[2] = {cgd::GB_K, cgd::GB_M};
+    cuuint32_t box[2] = {cgd::GB_K, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -552,10 +575,25 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
     const int64_t cpad = (ncols + cgd::GB_M - 1) / cgd::GB_M * cgd::GB_M;
     int64_t rblock = (int64_t)(planes_bytes / (size_t)(2 * cpad * 2)) / cgd::GB_K * cgd::GB_K;
     if (rblock <= 0) throw std::runtime_error("Gram plane buffer too small");
-    const int ntile = (int)(cpad / cgd::GB_M);
-    const int npairs = ntile * (ntile + 1) / 2;
-    const size_t smem = (size_t)cgd::GbSmem::total + 1024;
-    ck(cudaFuncSetAttribute(cgd::k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr");
+    // column tiles of 256 when the triangle has at least two tiles per SM of those,
+    // else of 128 (tiles that reach the upper triangle: tj >= ti / q)
+    const int nti = (int)(cpad / cgd::GB_M);   // 128-row tiles
+    auto pair_count = [&](int q) {
+        const int ntj = (int)((ncols + q * cgd::GB_M - 1) / (q * cgd::GB_M));
+        int n = 0;
+        for (int tj = 0; tj < ntj; ++tj) n += std::min(nti, q * tj + q);
+        return std::make_pair(ntj, n);
+    };
+    const int q = pair_count(2).second >= 2 * device_sms() ? 2 : 1;
+    const int bn = q * cgd::GB_M;
+    const int ntj = pair_count(q).first, npairs = pair_count(q).second;
+    const size_t smem = (size_t)(q == 2 ? cgd::GbCfg<256>::total : cgd::GbCfg<128>::total) + 1024;
+    if (q == 2)
+        ck(cudaFuncSetAttribute(cgd::k_gram_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+           "smem attr");
+    else
+        ck(cudaFuncSetAttribute(cgd::k_gram_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+           "smem attr");
     // split + A^T b: one wave of resident blocks over the column strips (a second,
     // partial wave would double the pass)
     const int nstrip = (int)(cpad / cgd::SPA_C);
@@ -589,7 +627,8 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         cgd::k_split_reduce<<<(ncols + 127) / 128, 128, 0, st>>>(partial, gxb, ncols, h);
         mark(S_ATB, false);
         ck(cudaGetLastError(), "k_split_reduce");
-        CUtensorMap mhi = plane_map(hi, kpad, cpad), mlo = plane_map(lo, kpad, cpad);
+        CUtensorMap mhi_a = plane_map(hi, kpad, cpad, cgd::GB_M), mlo_a = plane_map(lo, kpad, cpad, cgd::GB_M);
+        CUtensorMap mhi_b = plane_map(hi, kpad, cpad, bn), mlo_b = plane_map(lo, kpad, cpad, bn);
         // K slices: the persistent grid (one CTA per SM) runs npairs * nslice units
         // in waves; pick nslice (at most ctas_per_sm units per SM) minimising the K
         // steps on the longest CTA's path, waves * ceil(ksteps / nslice), plus one
@@ -610,8 +649,12 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         if (nunits > INT32_MAX) throw std::runtime_error("too many Gram tiles");
         const unsigned grid = (unsigned)std::min<int64_t>(nunits, device_sms());
         mark(S_TC, true);
-        cgd::k_gram_tc<<<grid, cgd::GB_THREADS, smem, st>>>(mhi, mlo, ntile, npairs, (int)nunits, kpad, kslice, ncols,
-                                                            G, d_err);
+        if (q == 2)
+            cgd::k_gram_tc<256><<<grid, cgd::GB_THREADS, smem, st>>>(mhi_a, mlo_a, mhi_b, mlo_b, nti, ntj, npairs,
+                                                                     (int)nunits, kpad, kslice, ncols, G, d_err);
+        else
+            cgd::k_gram_tc<128><<<grid, cgd::GB_THREADS, smem, st>>>(mhi_a, mlo_a, mhi_b, mlo_b, nti, ntj, npairs,
+                                                                     (int)nunits, kpad, kslice, ncols, G, d_err);
         mark(S_TC, false);
         ck(cudaGetLastError(), "k_gram_tc");
     }
