@@ -633,12 +633,15 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
         // in waves; pick nslice (at most ctas_per_sm units per SM) minimising the K
         // steps on the longest CTA's path, waves * ceil(ksteps / nslice), plus one
         // step per wave for the unit switch.
+        // With the wide tile a unit spans at most 128 K steps: over longer ranges the
+        // CTAs drift apart along K and the operand tiles they share leave L2.
         const int64_t ksteps = kpad / cgd::GB_K;
         const int64_t sms = device_sms();
+        const int64_t smin = q == 2 ? std::max<int64_t>(1, (ksteps + 127) / 128) : 1;
         const int64_t smax = std::max<int64_t>(
-            1, std::min<int64_t>(ksteps, sms * std::max(1, ctas_per_sm) / std::max(1, npairs)));
-        int64_t nslice = 1, best = INT64_MAX;
-        for (int64_t sl = 1; sl <= smax; ++sl) {
+            smin, std::min<int64_t>(ksteps, sms * std::max(1, ctas_per_sm) / std::max(1, npairs)));
+        int64_t nslice = smin, best = INT64_MAX;
+        for (int64_t sl = smin; sl <= smax; ++sl) {
             const int64_t waves = (npairs * sl + sms - 1) / sms;
             const int64_t cost = waves * ((ksteps + sl - 1) / sl + 1);
             if (cost < best) { best = cost; nslice = sl; }
