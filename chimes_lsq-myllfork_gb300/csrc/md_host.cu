@@ -365,24 +365,46 @@ void Session::md_force_lists(DeviceFrames& df, MdLists& L, double* Fo, double* S
     mark(ST_SETUP, true);
     cgd::launch_frame_setup(F, df.nghosts, st);
     mark(ST_SETUP, false);
+    // The 2-body, 3-body and 4-body parts add into Fo / So with atomics and are
+    // otherwise independent: the many-body parts run on two side streams beside the
+    // 2-body kernel (a frame of ~1000 atoms gives each contraction only a few warps
+    // per SM).  Stage timing keeps them in order on the session stream.
+    const bool fork = !profiling_;
+    if (fork && !md_side_[0]) {
+        for (int k = 0; k < 2; ++k) {
+            CK(cudaStreamCreateWithFlags(&md_side_[k], cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&md_join_[k], cudaEventDisableTiming));
+        }
+        CK(cudaEventCreateWithFlags(&md_fork_, cudaEventDisableTiming));
+    }
+    if (fork) CK(cudaEventRecord(md_fork_, st));
     mark(ST_FORCE2, true);
     cgd::launch_md2(M, D, F, L.NB, Fo, So, st, md_->precision);
     mark(ST_FORCE2, false);
+    bool joined[2] = {false, false};
     for (int k = 0; k < 2; ++k) {
         const int64_t n = L.ncl[k];
         if (n == 0 || !L.tstep[k]) continue;
+        cudaStream_t sk = fork ? md_side_[k] : st;
+        if (fork) CK(cudaStreamWaitEvent(sk, md_fork_, 0));
         cgd::ClusterSet CS = L.CS[k];
         mark(ST_BUCKET, true);
-        cgd::launch_md_filter(3 + k, M, F, CS, L.cfo[k], n, L.tstep[k], st);
+        cgd::launch_md_filter(3 + k, M, F, CS, L.cfo[k], n, L.tstep[k], sk);
         CS.type = L.tstep[k];
-        cgd::launch_md_bucket(n, nf, L.cfo[k], L.tstep[k], L.B[k], st);
+        cgd::launch_md_bucket(n, nf, L.cfo[k], L.tstep[k], L.B[k], sk);
         mark(ST_BUCKET, false);
         const int64_t max_tiles = (n + cgd::MDC_TILE - 1) / cgd::MDC_TILE + L.B[k].nkeys;
         mark(k == 0 ? ST_FORCE3 : ST_FORCE4, true);
         cgd::launch_mdc(3 + k, md_->precision, k == 0 ? M.order3 : M.order4, max_tiles, M, D, F, CS, L.B[k], Fo, So,
-                        st);
+                        sk);
         mark(k == 0 ? ST_FORCE3 : ST_FORCE4, false);
+        if (fork) {
+            CK(cudaEventRecord(md_join_[k], sk));
+            joined[k] = true;
+        }
     }
+    for (int k = 0; k < 2; ++k)
+        if (joined[k]) CK(cudaStreamWaitEvent(st, md_join_[k], 0));
     if (D.coulomb) {   // ZCalc_Ewald
         const int km = md_ewald_kmax(df);
         void* ews = nullptr;

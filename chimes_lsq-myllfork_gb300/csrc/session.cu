@@ -396,6 +396,11 @@ Session::~Session() {
     md_.reset();
     dm_.reset();
     if (side_event_) cudaEventDestroy(side_event_);
+    for (int k = 0; k < 2; ++k) {
+        if (md_side_[k]) cudaStreamDestroy(md_side_[k]);
+        if (md_join_[k]) cudaEventDestroy(md_join_[k]);
+    }
+    if (md_fork_) cudaEventDestroy(md_fork_);
     if (side_stream_) cudaStreamDestroy(side_stream_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
     for (void* p : pinned_) if (p) cudaFreeHost(p);

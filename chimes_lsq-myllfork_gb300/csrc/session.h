@@ -397,6 +397,8 @@ class Session {
     unsigned char* mailbox_host_ = nullptr;   // mapped pinned bytes written by peek()
     unsigned char* mailbox_dev_ = nullptr;
     cudaEvent_t side_event_ = nullptr;
+    cudaStream_t md_side_[2] = {nullptr, nullptr};   // many-body MD force parts beside the 2-body kernel
+    cudaEvent_t md_fork_ = nullptr, md_join_[2] = {nullptr, nullptr};
     std::unique_ptr<DeviceModel> dm_;
     std::unique_ptr<MdTables> md_;
     int gram_ctas_per_sm_ = 4;
