@@ -1046,7 +1046,9 @@ void Session::refine_streamed(const double* L, int ncols, double ridge, const st
         CK(cudaStreamSynchronize(stream_));
         scratch_pool_trim(device_);
         CK(cudaMemGetInfo(&fr, &tot));
-        const int64_t margin = (int64_t)(tot / 10) + 3 * (int64_t)maxrows * ncols * (int64_t)sizeof(double);
+        // margin: a sixteenth of the device plus one more row block, far above the
+        // work lists of one block's assembly (a few GB for 50 four-body frames)
+        const int64_t margin = (int64_t)(tot / 16) + (int64_t)maxrows * ncols * (int64_t)sizeof(double);
         R.cache_left = std::max<int64_t>(0, (int64_t)fr - margin);
     } else {
         R.cache_left = refine_cache_bytes_;
