@@ -13,6 +13,7 @@
 #include <string>
 
 #include "dense64.h"
+#include "gram.h"
 
 namespace cgd {
 
@@ -439,8 +440,16 @@ void syrk_tn(const double* X, int64_t ldx, int64_t K, int m, double alpha, doubl
     ckd(cudaGetLastError(), "k_syrk_tn");
 }
 
-bool cholesky64(double* G, int n, int* d_info, cudaStream_t st) {
+bool cholesky64(double* G, int n, int* d_info, cudaStream_t st, bool tensor_updates) {
     ckd(cudaMemsetAsync(d_info, 0, sizeof(int), st), "info");
+    // trailing updates of full 128-wide panels by exact BF16 digit products on the
+    // tensor cores (syrk_update_ozaki); the FP64 SYRK otherwise
+    void* oz = nullptr;
+    const bool use_oz = tensor_updates && cgd::CH_NB == 128 && n > cgd::CH_NB;
+    if (use_oz) {
+        ckd(cudaMallocAsync(&oz, ozaki_scratch_bytes(n), st), "Ozaki scratch");
+        ckd(cudaMemsetAsync(oz, 0, sizeof(int), st), "Ozaki error word");
+    }
     const size_t smem_potrf = (size_t)cgd::CH_NB * cgd::CH_NB * sizeof(double);
     const size_t smem_trsm = ((size_t)cgd::CH_NB * cgd::CH_NB + (size_t)cgd::TR_R * cgd::TR_PLD + cgd::CH_NB) *
                              sizeof(double);
@@ -456,13 +465,23 @@ bool cholesky64(double* G, int n, int* d_info, cudaStream_t st) {
             const size_t sm = ((size_t)kb * kb + (size_t)cgd::TR_R * cgd::TR_PLD + kb) * sizeof(double);
             cgd::k_trsm_panel<<<(m + cgd::TR_R - 1) / cgd::TR_R, cgd::TR_THREADS, sm, st>>>(G, n, k, kb, m);
             // trailing update: A22 -= P P^T (P: rows k+kb.., columns k..k+kb, column-major)
-            syrk_tn(G + (int64_t)k * n + (k + kb), n, kb, m, -1.0, G + (int64_t)(k + kb) * n + (k + kb), n, st);
+            if (use_oz && kb == 128)
+                syrk_update_ozaki(G + (int64_t)k * n + (k + kb), n, kb, m, -1.0, G + (int64_t)(k + kb) * n + (k + kb),
+                                  n, oz, st);
+            else
+                syrk_tn(G + (int64_t)k * n + (k + kb), n, kb, m, -1.0, G + (int64_t)(k + kb) * n + (k + kb), n, st);
         }
         ckd(cudaGetLastError(), "cholesky step");
     }
-    int info = 0;
+    int info = 0, oz_err = 0;
     ckd(cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, st), "info");
+    if (use_oz) {
+        ckd(cudaMemcpyAsync(&oz_err, oz, sizeof(int), cudaMemcpyDeviceToHost, st), "Ozaki error word");
+        ckd(cudaFreeAsync(oz, st), "Ozaki scratch");
+    }
     ckd(cudaStreamSynchronize(st), "cholesky");
+    if (oz_err) throw std::runtime_error("Cholesky trailing update timed out on its pipeline (code " +
+                                         std::to_string(oz_err) + ")");
     return info == 0;
 }
 

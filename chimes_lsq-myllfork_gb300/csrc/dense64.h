@@ -22,7 +22,7 @@ void syrk_tn(const double* X, int64_t ldx, int64_t K, int m, double alpha, doubl
 // blocks are factorised in shared memory, the panel below by substitution against
 // the block, the trailing matrix by syrk_tn.  Returns false when a pivot is not
 // positive (d_info: device int, first bad column + 1).
-bool cholesky64(double* G, int n, int* d_info, cudaStream_t st);
+bool cholesky64(double* G, int n, int* d_info, cudaStream_t st, bool tensor_updates = false);
 
 // In-place triangular solve T x = b (x holds b on entry) with T(i, j) = M[i*si + j*sj]
 // lower (forward substitution) or upper (backward substitution), n x n.

@@ -476,6 +476,252 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
     }
 }
 
+// ---------------------------------------------------------------- FP64 SYRK update by exact BF16 slices
+// C (upper triangle) += alpha X^T X for a panel X of K <= 128 rows, the trailing
+// update of the blocked Cholesky, computed with FP64 accuracy on the tensor cores
+// (the Ozaki scheme: Ozaki, Ogita, Oishi and Rump, Numer. Algorithms 59, 2012).  Each
+// column i of X is scaled by a power of two s_i (|X / s_i| < 1) and split into OZ_S
+// signed digits, x / s_i = sum_a d_a 128^-(a+1) + r with |d_0| <= 128, |d_a| <= 64,
+// |r| < 2^-57, each an integer that BF16 holds exactly.  A digit product summed over
+// K = 128 stays below 2^21 and the sum over the pairs (a, b) of one diagonal a + b = D
+// below 2^23, so the FP32 tensor-core accumulator of each diagonal is exact; the pairs
+// with a + b >= OZ_S are dropped (below 2^-56 of the leading term), and the
+// epilogue packs sum_D S_D 128^-(D+2) into one 53-bit integer (scaled by s_i s_j).
+constexpr int OZ_S = 8;            // digits per element (57 bits)
+constexpr int OZ_K = 128;          // panel width (K, zero padded)
+constexpr int OZ_M = 128, OZ_N = 64;
+constexpr int OZ_THREADS = 128;
+constexpr int OZ_LD = 33;          // epilogue staging row (doubles)
+struct OzSmem {
+    static constexpr uint32_t b = 0;                                          // OZ_S slices x 2 K halves x 8 KB
+    static constexpr uint32_t a = b + OZ_S * 2 * (OZ_N * 128);                // 2 slots x 2 K halves x 16 KB
+    static constexpr uint32_t stage = a + 2 * 2 * (OZ_M * 128);               // 4 warps x 32 x OZ_LD doubles
+    static constexpr uint32_t bars = stage + 4 * 32 * OZ_LD * 8;
+    static constexpr uint32_t total = bars + 6 * 8 + 16;
+};
+static_assert(OzSmem::bars % 8 == 0, "mbarrier alignment");
+static_assert(OzSmem::total + 1024 <= 227 * 1024, "shared memory per CTA");
+
+// Digit planes P[a][i][k] (bf16, k contiguous, a < OZ_S, i < mpad, k < OZ_K) and
+// scale exponents ex[i] (column i scaled by 2^-ex[i]) of the columns of X (K x m,
+// row-major, ldx).  Block: 32 columns.
+__global__ void __launch_bounds__(256) k_oz_slice(const double* __restrict__ X, int64_t ldx, int K, int m, int mpad,
+                                                  __nv_bfloat16* __restrict__ P, int* __restrict__ ex) {
+    __shared__ double tile[OZ_K][33];
+    __shared__ double scs[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i0 = blockIdx.x * 32;
+    for (int k = w; k < OZ_K; k += 8) {
+        const int i = i0 + lane;
+        tile[k][lane] = (k < K && i < m) ? X[(int64_t)k * ldx + i] : 0.0;
+    }
+    __syncthreads();
+    for (int c = w; c < 32; c += 8) {   // column maximum -> power-of-two scale
+        double mx = 0.0;
+        for (int k = lane; k < OZ_K; k += 32) mx = fmax(mx, fabs(tile[k][c]));
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) {
+            int e = 0;
+            if (mx > 0.0) frexp(mx, &e);
+            scs[c] = ldexp(1.0, e);
+            if (i0 + c < mpad) ex[i0 + c] = e;
+        }
+    }
+    __syncthreads();
+    for (int c = w; c < 32; c += 8) {
+        const int i = i0 + c;
+        if (i >= mpad) continue;
+        const double inv = 1.0 / scs[c];   // a power of two: exact
+        for (int h = 0; h < OZ_K; h += 64) {
+            const int k = h + 2 * lane;
+            double y0 = tile[k][c] * inv, y1 = tile[k + 1][c] * inv;
+#pragma unroll
+            for (int a = 0; a < OZ_S; ++a) {
+                const double t0 = y0 * 128.0, t1 = y1 * 128.0;
+                const double d0 = rint(t0), d1 = rint(t1);
+                y0 = t0 - d0;
+                y1 = t1 - d1;
+                const __nv_bfloat162 v = __floats2bfloat162_rn((float)d0, (float)d1);
+                *reinterpret_cast<__nv_bfloat162*>(P + ((int64_t)a * mpad + i) * OZ_K + k) = v;
+            }
+        }
+    }
+}
+
+// Tile u of the upper triangle in 128-row x 64-column tiles (ti, tj), kept when
+// tj >= 2 ti: row ti holds ntj - 2 ti tiles and f(ti) = ti (ntj + 1 - ti) precede it.
+__device__ __forceinline__ void oz_tile(int u, int ntj, int& ti, int& tj) {
+    const double b = ntj + 1.0;
+    int t = (int)floor((b - sqrt(fmax(0.0, b * b - 4.0 * (double)u))) * 0.5);
+    while (t > 0 && (int64_t)t * (ntj + 1 - t) > u) --t;
+    while ((int64_t)(t + 1) * (ntj - t) <= u) ++t;
+    ti = t;
+    tj = 2 * t + (u - t * (ntj + 1 - t));
+}
+
+// One CTA per tile: the tile's OZ_S column-slice operands stay in shared memory, its
+// OZ_S row-slice operands stream through two slots; one thread issues the digit-pair
+// MMAs (M 128, N 64, K 16) into OZ_S TMEM accumulators (diagonal D at columns D x 64:
+// all of TMEM), then four warps combine the diagonals in FP64 and add the tile into C.
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    k_oz_syrk(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+              const int* __restrict__ ex, int m, int mpad, int ntj, double alpha, double* __restrict__ C,
+              int64_t ldc, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* bfull = reinterpret_cast<uint64_t*>(smem + OzSmem::bars);
+    uint64_t* afull = bfull + 1;     // [2]
+    uint64_t* aempty = afull + 2;    // [2]
+    uint64_t* done = aempty + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int ti, tj;
+    oz_tile((int)blockIdx.x, ntj, ti, tj);
+
+    if (threadIdx.x == 0) {
+        mbar_init(bfull, 1);
+        for (int s = 0; s < 2; ++s) { mbar_init(&afull[s], 1); mbar_init(&aempty[s], 1); }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(OZ_S * OZ_N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (threadIdx.x == 0) {   // producer
+        bool ok = true;
+        int issued = 0;   // row-slice loads issued
+        mbar_expect_tx(bfull, OZ_S * 2 * OZ_N * 128);
+        for (int b = 0; b < OZ_S; ++b)
+            for (int h = 0; h < 2; ++h)
+                tma_load_2d(smem + OzSmem::b + (b * 2 + h) * (OZ_N * 128), &map_b, bfull, h * 64,
+                            b * mpad + tj * OZ_N);
+        for (int a = 0; a < OZ_S && ok; ++a) {
+            const int s = a & 1;
+            if (a >= 2 && !mbar_wait(&aempty[s], (uint32_t)((a >> 1) - 1) & 1u, err, 11)) { ok = false; break; }
+            mbar_expect_tx(&afull[s], 2 * OZ_M * 128);
+            for (int h = 0; h < 2; ++h)
+                tma_load_2d(smem + OzSmem::a + (s * 2 + h) * (OZ_M * 128), &map_a, &afull[s], h * 64,
+                            a * mpad + ti * OZ_M);
+            ++issued;
+        }
+        // every issued copy lands before the CTA can exit, on every path (the last
+        // copy into each slot completes that slot's latest full-barrier phase)
+        mbar_wait(bfull, 0, err, 14);
+        for (int a = issued - 1; a >= 0 && a >= issued - 2; --a)
+            mbar_wait(&afull[a & 1], (uint32_t)(a >> 1) & 1u, err, 14);
+    } else if (warp >= 2) {   // while the MMAs run: the tile's rows of C into L2 (4 lines of 128 B each)
+        for (int t = threadIdx.x - 64; t < OZ_M * 4; t += 64) {
+            const int row = ti * OZ_M + t / 4, col = tj * OZ_N + (t % 4) * 16;
+            if (row < m && col < m)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(C + (int64_t)row * ldc + col));
+        }
+    } else if (threadIdx.x == 32) {   // MMA issuer
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
+                               ((uint32_t)(OZ_M >> 4) << 24);
+        bool ok = mbar_wait(bfull, 0, err, 12);
+        for (int a = 0; a < OZ_S && ok; ++a) {
+            const int s = a & 1;
+            if (!mbar_wait(&afull[s], (uint32_t)(a >> 1) & 1u, err, 13)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int b = 0; a + b < OZ_S; ++b) {
+                const uint32_t d = tmem + (uint32_t)((a + b) * OZ_N);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const uint64_t da = smem_desc(smem + OzSmem::a + (s * 2 + h) * (OZ_M * 128));
+                    const uint64_t db = smem_desc(smem + OzSmem::b + (b * 2 + h) * (OZ_N * 128));
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint64_t adv = (uint64_t)((kk * 32) >> 4);
+                        umma_bf16(d, da + adv, db + adv, idesc, (a > 0 || h > 0 || kk > 0) ? 1u : 0u);
+                    }
+                }
+            }
+            umma_commit(&aempty[s]);
+        }
+        umma_commit(done);
+    }
+    __syncwarp();
+    // epilogue: all four warps (TMEM lane quarter = warp)
+    const bool have = mbar_wait(done, 0, err, 15);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (__all_sync(0xffffffffu, have) && *err == 0) {
+        // The diagonal sums S_D are exact integers below 2^23 (in FP32 registers).  The
+        // element is sum_D S_D 2^(-7D-14) = V 2^-54 with the integer
+        //   V = sum_{D<6} S_D 2^(40-7D) + round((S_6 2^7 + S_7) / 2^9),   |V| < 2^62,
+        // so one conversion (rounding to 53 bits, as FP64 arithmetic would) and one FMA
+        // per element remain in FP64; the rounded tail moves V by at most 2^-55.
+        double* stg = reinterpret_cast<double*>(smem + OzSmem::stage) + (size_t)warp * 32 * OZ_LD;
+        const int row0 = ti * OZ_M + warp * 32;
+#pragma unroll 1
+        for (int c0 = 0; c0 < OZ_N; c0 += 32) {
+            long long hi[32], lo[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) hi[c] = lo[c] = 0;
+#pragma unroll 1
+            for (int D = 0; D < OZ_S; ++D) {
+                uint32_t v[32];
+                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(D * OZ_N + c0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const int sh = D < 6 ? 40 - 7 * D : (D == 6 ? 7 : 0);
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    const long long sd = (long long)__float2int_rz(__uint_as_float(v[c])) << sh;
+                    if (D < 6) hi[c] += sd; else lo[c] += sd;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+                stg[lane * OZ_LD + c] = (double)(hi[c] + ((lo[c] + 256) >> 9));
+            __syncwarp();
+            const int col = tj * OZ_N + c0 + lane;
+            const int ecol = col < m ? ex[col] : 0;
+            const int erow = row0 + lane < m ? ex[row0 + lane] : 0;   // row r's exponent from lane r
+            double cold[32];   // all 32 reads in flight before the first write
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                const int row = row0 + r;
+                cold[r] = (row < m && col < m && col >= row) ? C[(int64_t)row * ldc + col] : 0.0;
+            }
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                const int row = row0 + r;
+                const int e = __shfl_sync(0xffffffffu, erow, r) + ecol - 54;
+                if (row < m && col < m && col >= row) {
+                    // alpha 2^(e_row + e_col - 54): a power of two times alpha
+                    const double f = (e > -1000 && e < 1000)
+                                         ? alpha * __longlong_as_double((long long)(1023 + e) << 52)
+                                         : ldexp(alpha, e);
+                    C[(int64_t)row * ldc + col] = fma(f, stg[r * OZ_LD + lane], cold[r]);
+                }
+            }
+            __syncwarp();
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_S * OZ_N)
+                     : "memory");
+    }
+}
+
 }  // namespace cgd
 
 // ================================================================ host side
@@ -663,6 +909,38 @@ void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int
     }
     ck(cudaFreeAsync(partial, st), "atb scratch free");
     if (bsplit) ck(cudaFreeAsync(bsplit, st), "b split scratch free");
+}
+
+size_t ozaki_scratch_bytes(int m_max) {
+    const size_t mpad = (size_t)(std::max(m_max, 1) + 127) / 128 * 128;
+    return 256 + (mpad * sizeof(double) + 255) / 256 * 256 + (size_t)cgd::OZ_S * mpad * cgd::OZ_K * 2;
+}
+
+void syrk_update_ozaki(const double* X, int64_t ldx, int K, int m, double alpha, double* C, int64_t ldc,
+                       void* scratch, cudaStream_t st) {
+    if (m <= 0 || K <= 0) return;
+    if (K > cgd::OZ_K) throw std::runtime_error("syrk_update_ozaki: panel wider than 128");
+    const int mpad = (m + 127) / 128 * 128;
+    int* d_err = static_cast<int*>(scratch);
+    int* ex = reinterpret_cast<int*>(static_cast<char*>(scratch) + 256);
+    __nv_bfloat16* P = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(scratch) + 256 +
+                                                        ((size_t)mpad * sizeof(double) + 255) / 256 * 256);
+    cgd::k_oz_slice<<<mpad / 32, 256, 0, st>>>(X, ldx, K, m, mpad, P, ex);
+    ck(cudaGetLastError(), "k_oz_slice");
+    const CUtensorMap ma = plane_map(P, cgd::OZ_K, (int64_t)cgd::OZ_S * mpad, cgd::OZ_M);
+    const CUtensorMap mb = plane_map(P, cgd::OZ_K, (int64_t)cgd::OZ_S * mpad, cgd::OZ_N);
+    const int ntj = (m + cgd::OZ_N - 1) / cgd::OZ_N, rows = (ntj + 1) / 2;
+    const int64_t ntiles = (int64_t)rows * (ntj + 1 - rows);
+    const size_t smem = (size_t)cgd::OzSmem::total + 1024;
+    static thread_local int attr_dev = -1;
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (attr_dev != dev) {
+        ck(cudaFuncSetAttribute(cgd::k_oz_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr");
+        attr_dev = dev;
+    }
+    cgd::k_oz_syrk<<<(unsigned)ntiles, cgd::OZ_THREADS, smem, st>>>(ma, mb, ex, m, mpad, ntj, alpha, C, ldc, d_err);
+    ck(cudaGetLastError(), "k_oz_syrk");
 }
 
 void gram_symmetrize(double* G, int n, bool from_upper, cudaStream_t st) {

@@ -21,13 +21,22 @@ size_t gram_plane_bytes(int64_t nrows_block, int ncols);
 void gram_accumulate(int prec_in, const void* A, int64_t lda, int64_t nrows, int ncols, const double* b, int mode,
                      double* G, double* h, void* planes, size_t planes_bytes, int* d_err, cudaStream_t st,
                      const std::function<void(int, bool)>& mark, int ctas_per_sm = 4);
+// C (row-major ldc, upper triangle) += alpha X^T X for X of K <= 128 rows x m columns
+// (row-major ldx), with FP64 accuracy from exact BF16 digit products on the tensor
+// cores (gram.cu).  scratch: ozaki_scratch_bytes(m) bytes (its first int is the
+// kernel's error word, zeroed by the caller before the first call).
+size_t ozaki_scratch_bytes(int m_max);
+void syrk_update_ozaki(const double* X, int64_t ldx, int K, int m, double alpha, double* C, int64_t ldc,
+                       void* scratch, cudaStream_t st);
 // Copy the upper triangle of G to the lower one.
 void gram_symmetrize(double* G, int n, bool from_upper, cudaStream_t st);
 
 // L = Cholesky factor of G + r I (n x n, L: device n*n doubles, column-major lower in
 // the symmetric storage) with r = ridge, grown tenfold at most 8 times while G + r I
 // is not positive definite.  Returns the r used, or -1 when every attempt failed.
-double factor_ridge(const double* G, int n, double ridge, double* L, int* d_info, cudaStream_t st);
+// tensor_updates: trailing updates by syrk_update_ozaki (else the FP64 SYRK).
+double factor_ridge(const double* G, int n, double ridge, double* L, int* d_info, cudaStream_t st,
+                    bool tensor_updates = true);
 
 // The FP64 products of a least-squares problem with rows A (never stored whole by
 // the streamed form): apply(p, q): q = A^T (A p); residual(x, r): r = A^T (b - A x).

@@ -908,7 +908,7 @@ void Session::solve(const double* G, const double* h, int ncols, double ridge, c
     double* L = S.get<double>((size_t)ncols * ncols);
     int* d_info = S.get<int>(1);
     try {
-        const double used = factor_ridge(G, ncols, ridge, L, d_info, stream_);
+        const double used = factor_ridge(G, ncols, ridge, L, d_info, stream_, chol_tensor_);
         if (used < 0.0) throw Error(2, "the normal-equations matrix is not positive definite even with a ridge");
         cholesky_solve64(L, ncols, h, x, stream_);
         PcgStats ps;
@@ -951,7 +951,7 @@ double Session::factor(const double* G, int ncols, double ridge, double* L) {
     Scratch S(stream_);
     int* d_info = S.get<int>(1);
     try {
-        const double used = factor_ridge(G, ncols, ridge, L, d_info, stream_);
+        const double used = factor_ridge(G, ncols, ridge, L, d_info, stream_, chol_tensor_);
         if (used < 0.0) throw Error(2, "the normal-equations matrix is not positive definite even with a ridge");
         return used;
     } catch (const std::runtime_error& e) {

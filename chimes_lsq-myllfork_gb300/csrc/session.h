@@ -280,6 +280,9 @@ class Session {
     void set_refine_cache_bytes(int64_t v) { refine_cache_bytes_ = v; }
     // Threads per CTA of the 4-body force kernel (512 or 1024).
     void set_force4_threads(int v) { force4_threads_ = v == 1024 ? 1024 : 512; }
+    // Cholesky trailing updates by exact BF16 digit products on the tensor cores
+    // (FP64-accurate) or by the FP64 SYRK.
+    void set_cholesky_tensor_updates(bool v) { chol_tensor_ = v; }
     int gram_ctas_per_sm() const { return gram_ctas_per_sm_; }
     int device() const { return device_; }
     // Measured FP64 FMA rate of the session's GPU in TFLOP/s (dense64.cu).
@@ -405,6 +408,7 @@ class Session {
     int64_t gram_rows_per_launch_ = 0;
     int64_t refine_cache_bytes_ = -1;
     int force4_threads_ = 512;
+    bool chol_tensor_ = true;
     int64_t gram_plane_rows(int64_t nrows, int ncols) const;
     double md_skin_ = 0.5;   // Angstrom; 0: enumerate every step
     std::atomic<double> serve_list_per_atom_{6144.0};   // list bytes per atom (measured by the serving loop)

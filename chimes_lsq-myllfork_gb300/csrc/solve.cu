@@ -42,14 +42,15 @@ double host_dot(const double* x, const double* y, int n, double* dscal, cudaStre
 }
 }  // namespace
 
-double factor_ridge(const double* G, int n, double ridge, double* L, int* d_info, cudaStream_t st) {
+double factor_ridge(const double* G, int n, double ridge, double* L, int* d_info, cudaStream_t st,
+                    bool tensor_updates) {
     // The ridge grows tenfold (at most 8 times) until the factorisation succeeds: a
     // mixed-precision G can be indefinite at tiny ridges.
     double used = ridge;
     for (int attempt = 0; attempt < 9; ++attempt) {
         cks(cudaMemcpyAsync(L, G, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, st), "L = G");
         add_diag64(L, n, used, st);
-        if (cholesky64(L, n, d_info, st)) return used;
+        if (cholesky64(L, n, d_info, st, tensor_updates)) return used;
         used = used > 0.0 ? used * 10.0 : 1e-12;
     }
     return -1.0;

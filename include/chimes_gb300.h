@@ -539,7 +539,9 @@ void cg_batch_fit_free(cg_batch_fit* b);
  * "refine_cache_mb" (device memory the streamed refinement may fill with FP64 row
  * blocks kept between passes, in MiB; -1 = what is free beyond a margin, the
  * default; 0 = assemble every block on every pass); "force4_threads" (threads per CTA
- * of the 4-body force-row kernel, 512 or 1024). */
+ * of the 4-body force-row kernel, 512 or 1024); "cholesky_tensor_updates" (1, the
+ * default: the blocked Cholesky's trailing updates from exact BF16 digit products on
+ * the tensor cores, FP64-accurate; 0: the FP64 SYRK). */
 int cg_session_tune(cg_session* s, const char* key, int value);
 
 const char* cg_last_error(void);
