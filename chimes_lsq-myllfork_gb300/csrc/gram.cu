@@ -490,14 +490,15 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 constexpr int OZ_S = 8;            // digits per element (57 bits)
 constexpr int OZ_K = 128;          // panel width (K, zero padded)
 constexpr int OZ_M = 128, OZ_N = 64;
-constexpr int OZ_THREADS = 128;
+constexpr int OZ_THREADS = 192;    // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr int OZ_LD = 33;          // epilogue staging row (doubles)
+constexpr int OZ_NBARS = 9;        // bfull, bempty, afull[2], aempty[2], tfull, tempty, done
 struct OzSmem {
     static constexpr uint32_t b = 0;                                          // OZ_S slices x 2 K halves x 8 KB
     static constexpr uint32_t a = b + OZ_S * 2 * (OZ_N * 128);                // 2 slots x 2 K halves x 16 KB
     static constexpr uint32_t stage = a + 2 * 2 * (OZ_M * 128);               // 4 warps x 32 x OZ_LD doubles
     static constexpr uint32_t bars = stage + 4 * 32 * OZ_LD * 8;
-    static constexpr uint32_t total = bars + 6 * 8 + 16;
+    static constexpr uint32_t total = bars + OZ_NBARS * 8 + 16;
 };
 static_assert(OzSmem::bars % 8 == 0, "mbarrier alignment");
 static_assert(OzSmem::total + 1024 <= 227 * 1024, "shared memory per CTA");
@@ -559,28 +560,36 @@ __device__ __forceinline__ void oz_tile(int u, int ntj, int& ti, int& tj) {
     tj = 2 * t + (u - t * (ntj + 1 - t));
 }
 
-// One CTA per tile: the tile's OZ_S column-slice operands stay in shared memory, its
-// OZ_S row-slice operands stream through two slots; one thread issues the digit-pair
+// Persistent: one CTA per SM walks the tiles u = b, b + grid, ...  Warp 0 (TMA) loads a
+// tile's OZ_S column-slice operands into one buffer once the previous tile's MMAs have
+// read it, and its row-slice operands through two slots; warp 1 issues the digit-pair
 // MMAs (M 128, N 64, K 16) into OZ_S TMEM accumulators (diagonal D at columns D x 64:
-// all of TMEM), then four warps combine the diagonals in FP64 and add the tile into C.
+// all of TMEM) once the epilogue has drained the previous tile; warps 2..5 (TMEM lane
+// quarter = warp % 4) combine the diagonals, add the tile into C and prefetch the next
+// tile's rows of C into L2.  The next tile's operands arrive while this tile's
+// epilogue runs.
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_oz_syrk(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-              const int* __restrict__ ex, int m, int mpad, int ntj, double alpha, double* __restrict__ C,
+              const int* __restrict__ ex, int m, int mpad, int ntj, int ntiles, double alpha, double* __restrict__ C,
               int64_t ldc, int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t* bfull = reinterpret_cast<uint64_t*>(smem + OzSmem::bars);
-    uint64_t* afull = bfull + 1;     // [2]
-    uint64_t* aempty = afull + 2;    // [2]
-    uint64_t* done = aempty + 2;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    uint64_t* bempty = bfull + 1;
+    uint64_t* afull = bfull + 2;     // [2]
+    uint64_t* aempty = bfull + 4;    // [2]
+    uint64_t* tfull = bfull + 6;
+    uint64_t* tempty = bfull + 7;
+    uint64_t* done = bfull + 8;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bfull + OZ_NBARS);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int ti, tj;
-    oz_tile((int)blockIdx.x, ntj, ti, tj);
 
     if (threadIdx.x == 0) {
         mbar_init(bfull, 1);
+        mbar_init(bempty, 1);
         for (int s = 0; s < 2; ++s) { mbar_init(&afull[s], 1); mbar_init(&aempty[s], 1); }
+        mbar_init(tfull, 1);
+        mbar_init(tempty, 4);
         mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -595,123 +604,159 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    if (threadIdx.x == 0) {   // producer
-        bool ok = true;
-        int issued = 0;   // row-slice loads issued
-        mbar_expect_tx(bfull, OZ_S * 2 * OZ_N * 128);
-        for (int b = 0; b < OZ_S; ++b)
-            for (int h = 0; h < 2; ++h)
-                tma_load_2d(smem + OzSmem::b + (b * 2 + h) * (OZ_N * 128), &map_b, bfull, h * 64,
-                            b * mpad + tj * OZ_N);
-        for (int a = 0; a < OZ_S && ok; ++a) {
-            const int s = a & 1;
-            if (a >= 2 && !mbar_wait(&aempty[s], (uint32_t)((a >> 1) - 1) & 1u, err, 11)) { ok = false; break; }
-            mbar_expect_tx(&afull[s], 2 * OZ_M * 128);
-            for (int h = 0; h < 2; ++h)
-                tma_load_2d(smem + OzSmem::a + (s * 2 + h) * (OZ_M * 128), &map_a, &afull[s], h * 64,
-                            a * mpad + ti * OZ_M);
-            ++issued;
+    if (warp == 0) {
+        if (lane == 0) {   // producer
+            bool ok = true;
+            int64_t g = 0;   // row slices issued over all tiles
+            int nb = 0;      // column-slice sets issued
+            int64_t last[2] = {-1, -1};
+            for (int u = blockIdx.x; u < ntiles && ok; u += gridDim.x) {
+                int ti, tj;
+                oz_tile(u, ntj, ti, tj);
+                if (nb > 0 && !mbar_wait(bempty, (uint32_t)(nb - 1) & 1u, err, 21)) { ok = false; break; }
+                mbar_expect_tx(bfull, OZ_S * 2 * OZ_N * 128);
+                for (int b = 0; b < OZ_S; ++b)
+                    for (int h = 0; h < 2; ++h)
+                        tma_load_2d(smem + OzSmem::b + (b * 2 + h) * (OZ_N * 128), &map_b, bfull, h * 64,
+                                    b * mpad + tj * OZ_N);
+                ++nb;
+                for (int a = 0; a < OZ_S; ++a, ++g) {
+                    const int s = (int)(g & 1);
+                    if (g >= 2 && !mbar_wait(&aempty[s], (uint32_t)((g >> 1) - 1) & 1u, err, 22)) { ok = false; break; }
+                    mbar_expect_tx(&afull[s], 2 * OZ_M * 128);
+                    for (int h = 0; h < 2; ++h)
+                        tma_load_2d(smem + OzSmem::a + (s * 2 + h) * (OZ_M * 128), &map_a, &afull[s], h * 64,
+                                    a * mpad + ti * OZ_M);
+                    last[s] = g;
+                }
+            }
+            // every issued copy lands before the CTA can exit, on every path (the last
+            // copy into a buffer completes that buffer's latest full-barrier phase)
+            if (nb > 0) mbar_wait(bfull, (uint32_t)(nb - 1) & 1u, err, 24);
+            for (int s = 0; s < 2; ++s)
+                if (last[s] >= 0) mbar_wait(&afull[s], (uint32_t)(last[s] >> 1) & 1u, err, 24);
         }
-        // every issued copy lands before the CTA can exit, on every path (the last
-        // copy into each slot completes that slot's latest full-barrier phase)
-        mbar_wait(bfull, 0, err, 14);
-        for (int a = issued - 1; a >= 0 && a >= issued - 2; --a)
-            mbar_wait(&afull[a & 1], (uint32_t)(a >> 1) & 1u, err, 14);
-    } else if (warp >= 2) {   // while the MMAs run: the tile's rows of C into L2 (4 lines of 128 B each)
-        for (int t = threadIdx.x - 64; t < OZ_M * 4; t += 64) {
-            const int row = ti * OZ_M + t / 4, col = tj * OZ_N + (t % 4) * 16;
-            if (row < m && col < m)
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(C + (int64_t)row * ldc + col));
-        }
-    } else if (threadIdx.x == 32) {   // MMA issuer
-        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
-                               ((uint32_t)(OZ_M >> 4) << 24);
-        bool ok = mbar_wait(bfull, 0, err, 12);
-        for (int a = 0; a < OZ_S && ok; ++a) {
-            const int s = a & 1;
-            if (!mbar_wait(&afull[s], (uint32_t)(a >> 1) & 1u, err, 13)) { ok = false; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int b = 0; a + b < OZ_S; ++b) {
-                const uint32_t d = tmem + (uint32_t)((a + b) * OZ_N);
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer
+            const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
+                                   ((uint32_t)(OZ_M >> 4) << 24);
+            bool ok = true;
+            int64_t g = 0;
+            int j = 0;
+            for (int u = blockIdx.x; u < ntiles && ok; u += gridDim.x, ++j) {
+                if (j > 0 && !mbar_wait(tempty, (uint32_t)(j - 1) & 1u, err, 25)) { ok = false; break; }
+                if (!mbar_wait(bfull, (uint32_t)j & 1u, err, 26)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                for (int a = 0; a < OZ_S; ++a, ++g) {
+                    const int s = (int)(g & 1);
+                    if (!mbar_wait(&afull[s], (uint32_t)(g >> 1) & 1u, err, 27)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    for (int b = 0; a + b < OZ_S; ++b) {
+                        const uint32_t d = tmem + (uint32_t)((a + b) * OZ_N);
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const uint64_t da = smem_desc(smem + OzSmem::a + (s * 2 + h) * (OZ_M * 128));
-                    const uint64_t db = smem_desc(smem + OzSmem::b + (b * 2 + h) * (OZ_N * 128));
+                        for (int h = 0; h < 2; ++h) {
+                            const uint64_t da = smem_desc(smem + OzSmem::a + (s * 2 + h) * (OZ_M * 128));
+                            const uint64_t db = smem_desc(smem + OzSmem::b + (b * 2 + h) * (OZ_N * 128));
 #pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) {
-                        const uint64_t adv = (uint64_t)((kk * 32) >> 4);
-                        umma_bf16(d, da + adv, db + adv, idesc, (a > 0 || h > 0 || kk > 0) ? 1u : 0u);
+                            for (int kk = 0; kk < 4; ++kk) {
+                                const uint64_t adv = (uint64_t)((kk * 32) >> 4);
+                                umma_bf16(d, da + adv, db + adv, idesc, (a > 0 || h > 0 || kk > 0) ? 1u : 0u);
+                            }
+                        }
                     }
+                    umma_commit(&aempty[s]);
                 }
+                if (!ok) break;
+                umma_commit(bempty);
+                umma_commit(tfull);
             }
-            umma_commit(&aempty[s]);
+            // every MMA of this CTA has finished before TMEM is released
+            umma_commit(done);
+            mbar_wait(done, 0, err, 29);
         }
-        umma_commit(done);
-    }
-    __syncwarp();
-    // epilogue: all four warps (TMEM lane quarter = warp)
-    const bool have = mbar_wait(done, 0, err, 15);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (__all_sync(0xffffffffu, have) && *err == 0) {
-        // The diagonal sums S_D are exact integers below 2^23 (in FP32 registers).  The
-        // element is sum_D S_D 2^(-7D-14) = V 2^-54 with the integer
-        //   V = sum_{D<6} S_D 2^(40-7D) + round((S_6 2^7 + S_7) / 2^9),   |V| < 2^62,
-        // so one conversion (rounding to 53 bits, as FP64 arithmetic would) and one FMA
-        // per element remain in FP64; the rounded tail moves V by at most 2^-55.
-        double* stg = reinterpret_cast<double*>(smem + OzSmem::stage) + (size_t)warp * 32 * OZ_LD;
-        const int row0 = ti * OZ_M + warp * 32;
+    } else {   // epilogue warps 2..5
+        const int q = warp & 3;   // TMEM lane quarter this warp may read
+        double* stg = reinterpret_cast<double*>(smem + OzSmem::stage) + (size_t)(warp - 2) * 32 * OZ_LD;
+        auto prefetch_c = [&](int u) {   // the tile's rows of C into L2: 4 lines of 128 B per row
+            int ti, tj;
+            oz_tile(u, ntj, ti, tj);
+            for (int t = threadIdx.x - 64; t < OZ_M * 4; t += 128) {
+                const int row = ti * OZ_M + t / 4, col = tj * OZ_N + (t % 4) * 16;
+                if (row < m && col < m) asm volatile("prefetch.global.L2 [%0];" ::"l"(C + (int64_t)row * ldc + col));
+            }
+        };
+        if ((int)blockIdx.x < ntiles) prefetch_c(blockIdx.x);
+        int j = 0;
+        for (int u = blockIdx.x; u < ntiles; u += gridDim.x, ++j) {
+            int ti, tj;
+            oz_tile(u, ntj, ti, tj);
+            const bool got = mbar_wait(tfull, (uint32_t)j & 1u, err, 28);
+            if (!__all_sync(0xffffffffu, got)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (*err == 0) {
+                // The diagonal sums S_D are exact integers below 2^23 (in FP32 registers).
+                // The element is sum_D S_D 2^(-7D-14) = V 2^-54 with the integer
+                //   V = sum_{D<6} S_D 2^(40-7D) + round((S_6 2^7 + S_7) / 2^9),   |V| < 2^62,
+                // so one conversion (rounding to 53 bits, as FP64 arithmetic would) and one
+                // FMA per element remain in FP64; the rounded tail moves V by at most 2^-55.
+                const int row0 = ti * OZ_M + q * 32;
 #pragma unroll 1
-        for (int c0 = 0; c0 < OZ_N; c0 += 32) {
-            long long hi[32], lo[32];
+                for (int c0 = 0; c0 < OZ_N; c0 += 32) {
+                    long long hi[32], lo[32];
 #pragma unroll
-            for (int c = 0; c < 32; ++c) hi[c] = lo[c] = 0;
+                    for (int c = 0; c < 32; ++c) hi[c] = lo[c] = 0;
 #pragma unroll 1
-            for (int D = 0; D < OZ_S; ++D) {
-                uint32_t v[32];
-                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(D * OZ_N + c0);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                    : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                const int sh = D < 6 ? 40 - 7 * D : (D == 6 ? 7 : 0);
+                    for (int D = 0; D < OZ_S; ++D) {
+                        uint32_t v[32];
+                        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(D * OZ_N + c0);
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                            "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                              "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+                              "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+                              "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                            : "r"(taddr));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        const int sh = D < 6 ? 40 - 7 * D : (D == 6 ? 7 : 0);
 #pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    const long long sd = (long long)__float2int_rz(__uint_as_float(v[c])) << sh;
-                    if (D < 6) hi[c] += sd; else lo[c] += sd;
+                        for (int c = 0; c < 32; ++c) {
+                            const long long sd = (long long)__float2int_rz(__uint_as_float(v[c])) << sh;
+                            if (D < 6) hi[c] += sd; else lo[c] += sd;
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) stg[lane * OZ_LD + c] = (double)(hi[c] + ((lo[c] + 256) >> 9));
+                    __syncwarp();
+                    const int col = tj * OZ_N + c0 + lane;
+                    const int ecol = col < m ? ex[col] : 0;
+                    const int erow = row0 + lane < m ? ex[row0 + lane] : 0;   // row r's exponent from lane r
+                    double cold[32];   // all 32 reads in flight before the first write
+#pragma unroll
+                    for (int r = 0; r < 32; ++r) {
+                        const int row = row0 + r;
+                        cold[r] = (row < m && col < m && col >= row) ? C[(int64_t)row * ldc + col] : 0.0;
+                    }
+#pragma unroll
+                    for (int r = 0; r < 32; ++r) {
+                        const int row = row0 + r;
+                        const int e = __shfl_sync(0xffffffffu, erow, r) + ecol - 54;
+                        if (row < m && col < m && col >= row) {
+                            // alpha 2^(e_row + e_col - 54): a power of two times alpha
+                            const double f = (e > -1000 && e < 1000)
+                                                 ? alpha * __longlong_as_double((long long)(1023 + e) << 52)
+                                                 : ldexp(alpha, e);
+                            C[(int64_t)row * ldc + col] = fma(f, stg[r * OZ_LD + lane], cold[r]);
+                        }
+                    }
+                    __syncwarp();
                 }
             }
-#pragma unroll
-            for (int c = 0; c < 32; ++c)
-                stg[lane * OZ_LD + c] = (double)(hi[c] + ((lo[c] + 256) >> 9));
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
-            const int col = tj * OZ_N + c0 + lane;
-            const int ecol = col < m ? ex[col] : 0;
-            const int erow = row0 + lane < m ? ex[row0 + lane] : 0;   // row r's exponent from lane r
-            double cold[32];   // all 32 reads in flight before the first write
-#pragma unroll
-            for (int r = 0; r < 32; ++r) {
-                const int row = row0 + r;
-                cold[r] = (row < m && col < m && col >= row) ? C[(int64_t)row * ldc + col] : 0.0;
-            }
-#pragma unroll
-            for (int r = 0; r < 32; ++r) {
-                const int row = row0 + r;
-                const int e = __shfl_sync(0xffffffffu, erow, r) + ecol - 54;
-                if (row < m && col < m && col >= row) {
-                    // alpha 2^(e_row + e_col - 54): a power of two times alpha
-                    const double f = (e > -1000 && e < 1000)
-                                         ? alpha * __longlong_as_double((long long)(1023 + e) << 52)
-                                         : ldexp(alpha, e);
-                    C[(int64_t)row * ldc + col] = fma(f, stg[r * OZ_LD + lane], cold[r]);
-                }
-            }
-            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty);
+            if (u + (int)gridDim.x < ntiles) prefetch_c(u + gridDim.x);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -939,7 +984,9 @@ void syrk_update_ozaki(const double* X, int64_t ldx, int K, int m, double alpha,
         ck(cudaFuncSetAttribute(cgd::k_oz_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr");
         attr_dev = dev;
     }
-    cgd::k_oz_syrk<<<(unsigned)ntiles, cgd::OZ_THREADS, smem, st>>>(ma, mb, ex, m, mpad, ntj, alpha, C, ldc, d_err);
+    if (ntiles > INT32_MAX) throw std::runtime_error("syrk_update_ozaki: too many tiles");
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, device_sms());
+    cgd::k_oz_syrk<<<grid, cgd::OZ_THREADS, smem, st>>>(ma, mb, ex, m, mpad, ntj, (int)ntiles, alpha, C, ldc, d_err);
     ck(cudaGetLastError(), "k_oz_syrk");
 }
 
