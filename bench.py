@@ -617,11 +617,22 @@ def main():
     def sink(first, blk):
         sink_rows[0] += blk.shape[0]
         return False
-    sess.assemble_stream(frames, cg.CG_FP64, sink, block_frames=E2E_BLOCK_FRAMES)   # warm (pinned staging allocated)
+    # two untimed calls: the first allocates the pinned staging; copies into freshly
+    # registered host memory run slower for a while on these hosts
+    for _ in range(2):
+        sess.assemble_stream(frames, cg.CG_FP64, sink, block_frames=E2E_BLOCK_FRAMES)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         sess.assemble_stream(frames, cg.CG_FP64, sink, block_frames=E2E_BLOCK_FRAMES)
     e2e_s = time.perf_counter() - t0
+    # one more streamed call with stage timing: the device time of the block copies
+    # (copy stream) beside the assembly stages, against the call's wall time
+    sess.profile(True)
+    t1 = time.perf_counter()
+    sess.assemble_stream(frames, cg.CG_FP64, sink, block_frames=E2E_BLOCK_FRAMES)
+    diag_wall = time.perf_counter() - t1
+    diag = {k: v[0] for k, v in sess.stage_times().items() if v[1]}
+    sess.profile(False)
     # the host link's device-to-host rate in this run (pinned destination), the
     # ceiling of the streamed call
     link = torch.empty(1 << 29, dtype=torch.float64, device="cuda")
@@ -638,7 +649,11 @@ def main():
            "d2h_link_gbs_measured": link_gbs, "d2h_gbs_achieved": nrows * C * 8 * e2e_steps / e2e_s / 1e9,
            "h2d_bytes_per_step": int(natoms * (3 * 8 + 4) + args.frames * (4 + 3 * 8 + 2 * 4 + 208)),
            "d2h_bytes_per_step": int(nrows * C * 8),
-           "call": f"cg_assemble_stream (FP64, blocks of {E2E_BLOCK_FRAMES} frames, pinned double buffer, no-op sink)"}
+           "call": f"cg_assemble_stream (FP64, blocks of {E2E_BLOCK_FRAMES} frames, pinned double buffer, no-op sink)",
+           "profiled_call": {"wall_s": diag_wall, "host_copies_s": diag.get("host_copies", 0.0) / 1e3,
+                             "copy_gbs_device": nrows * C * 8 / (diag["host_copies"] / 1e3) / 1e9
+                             if diag.get("host_copies") else None,
+                             "assembly_stages_s": sum(v for k, v in diag.items() if k != "host_copies") / 1e3}}
 
     fit = None
     if rank == 0 and not args.no_fit:

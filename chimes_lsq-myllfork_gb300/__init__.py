@@ -566,7 +566,7 @@ class Session:
         _check(lib().cg_assemble_device(self._h, dframes._h, int(precision), ctypes.c_void_p(int(a_device_ptr)),
                                         int(lda)))
 
-    NSTAGES = 17
+    NSTAGES = 18
 
     def profile(self, enable=True):
         """Turn per-stage CUDA-event timing on/off (clears the totals)."""

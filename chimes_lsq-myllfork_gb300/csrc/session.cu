@@ -1,7 +1,10 @@
 // Host orchestration of the design-matrix path (see session.h).
 #include "session.h"
 
+#include <sys/mman.h>
+
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <numeric>
@@ -315,7 +318,7 @@ static_assert(ST_GRAM_ATB == 11 && ST_GRAM_SPLIT == 12 && ST_GRAM_TC == 13 && ST
 const char* stage_name(int s) {
     static const char* names[ST_COUNT] = {"frame_setup", "neighbour_lists", "clusters", "buckets", "force_2b",
                                           "virial_2b", "force_3b", "virial_3b", "force_4b", "virial_4b", "other", "gram_atb", "gram_split", "gram_tensor", "gram_fp64_syrk",
-                                          "refine_products", "refine_preconditioner"};
+                                          "refine_products", "refine_preconditioner", "host_copies"};
     return s >= 0 && s < ST_COUNT ? names[s] : "?";
 }
 
@@ -390,6 +393,42 @@ Session::Session(const Model& m, int device) : model_(m), device_(device) {
     dm_.reset(new DeviceModel(model_, cgd::VIR_PPT * cgd::MB_THREADS));
 }
 
+namespace {
+// Host staging for device-to-host row blocks: memory aligned to 512 MiB, advised for
+// transparent huge pages and faulted in before it is registered with CUDA, so that a
+// block's copy meets few page mappings.  Multi-GB cudaMallocHost buffers on these hosts
+// took some copies at 60-140 GB/s where such memory held the link's 193 GB/s.
+// Falls back to cudaMallocHost (registered = false) when registration fails.
+void* staging_alloc(size_t bytes, bool& registered) {
+    constexpr size_t kAlign = size_t(512) << 20;
+    const size_t sz = (bytes + kAlign - 1) / kAlign * kAlign;
+    registered = false;
+    void* p = std::aligned_alloc(kAlign, sz);
+    if (p) {
+        madvise(p, sz, MADV_HUGEPAGE);
+        for (size_t o = 0; o < sz; o += 4096) static_cast<volatile char*>(p)[o] = 0;
+        if (cudaHostRegister(p, sz, cudaHostRegisterDefault) == cudaSuccess) {
+            registered = true;
+            return p;
+        }
+        cudaGetLastError();   // clear the failed registration
+        std::free(p);
+    }
+    void* q = nullptr;
+    CK(cudaMallocHost(&q, bytes));
+    return q;
+}
+void staging_free(void* p, bool registered) {
+    if (!p) return;
+    if (registered) {
+        cudaHostUnregister(p);
+        std::free(p);
+    } else {
+        cudaFreeHost(p);
+    }
+}
+}  // namespace
+
 Session::~Session() {
     for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : event_pool_) cudaEventDestroy(e);
@@ -403,7 +442,7 @@ Session::~Session() {
     if (md_fork_) cudaEventDestroy(md_fork_);
     if (side_stream_) cudaStreamDestroy(side_stream_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
-    for (void* p : pinned_) if (p) cudaFreeHost(p);
+    for (int i = 0; i < 2; ++i) staging_free(pinned_[i], pinned_reg_[i]);
     if (mailbox_host_) cudaFreeHost(mailbox_host_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -530,10 +569,10 @@ void Session::peek(cudaStream_t st, std::initializer_list<PeekItem> items) {
 void* Session::pinned(int i, size_t bytes) {
     if (i < 0 || i > 1) throw Error(1, "pinned staging index");
     if (pinned_bytes_[i] < bytes) {
-        if (pinned_[i]) CK(cudaFreeHost(pinned_[i]));
+        staging_free(pinned_[i], pinned_reg_[i]);
         pinned_[i] = nullptr;
         pinned_bytes_[i] = 0;
-        CK(cudaMallocHost(&pinned_[i], bytes));
+        pinned_[i] = staging_alloc(bytes, pinned_reg_[i]);
         pinned_bytes_[i] = bytes;
     }
     return pinned_[i];
@@ -561,11 +600,14 @@ int64_t Session::assemble_to_host(const FrameBatch& fb, int precision, int block
     struct Res {
         void* dA[2] = {nullptr, nullptr};
         cudaEvent_t asm_done[2] = {nullptr, nullptr}, copy_done[2] = {nullptr, nullptr};
+        cudaEvent_t copy_t0[2] = {nullptr, nullptr}, copy_t1[2] = {nullptr, nullptr};   // profiling only
         ~Res() {
             for (int i = 0; i < 2; ++i) {
                 if (dA[i]) cudaFree(dA[i]);
                 if (asm_done[i]) cudaEventDestroy(asm_done[i]);
                 if (copy_done[i]) cudaEventDestroy(copy_done[i]);
+                if (copy_t0[i]) cudaEventDestroy(copy_t0[i]);
+                if (copy_t1[i]) cudaEventDestroy(copy_t1[i]);
             }
         }
     } R;
@@ -574,6 +616,10 @@ int64_t Session::assemble_to_host(const FrameBatch& fb, int precision, int block
     for (int i = 0; i < 2; ++i) {
         CK(cudaEventCreateWithFlags(&R.asm_done[i], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&R.copy_done[i], cudaEventDisableTiming));
+        if (profiling_) {   // the device time of each block's copy to the host (stage host_copies)
+            CK(cudaEventCreate(&R.copy_t0[i]));
+            CK(cudaEventCreate(&R.copy_t1[i]));
+        }
     }
     std::vector<int64_t> first(nblk + 1, 0);
     for (int k = 0; k < nblk; ++k) first[k + 1] = first[k] + dev[k]->nrows;
@@ -581,6 +627,12 @@ int64_t Session::assemble_to_host(const FrameBatch& fb, int precision, int block
     AssembleStats total, one;
     auto finish = [&](int k) {   // block k's copy has been issued: wait for it, hand it over
         CK(cudaEventSynchronize(R.copy_done[k % 2]));
+        if (profiling_) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, R.copy_t0[k % 2], R.copy_t1[k % 2]));
+            stage_ms_[ST_HOST_COPY] += ms;
+            ++stage_calls_[ST_HOST_COPY];
+        }
         return done(first[k], dev[k]->nrows, hdst[k]);
     };
     bool go = true;
@@ -598,6 +650,7 @@ int64_t Session::assemble_to_host(const FrameBatch& fb, int precision, int block
         CK(cudaStreamWaitEvent(copy_stream_, R.asm_done[b], 0));
         hdst[k] = dest(first[k], dev[k]->nrows);
         if (!hdst[k]) throw Error(1, "no host destination for a row block");
+        if (profiling_) CK(cudaEventRecord(R.copy_t0[b], copy_stream_));
         if (ldh == lda) {
             CK(cudaMemcpyAsync(hdst[k], R.dA[b], (size_t)dev[k]->nrows * lda * rsz, cudaMemcpyDeviceToHost,
                                copy_stream_));
@@ -605,6 +658,7 @@ int64_t Session::assemble_to_host(const FrameBatch& fb, int precision, int block
             CK(cudaMemcpy2DAsync(hdst[k], (size_t)ldh * rsz, R.dA[b], (size_t)lda * rsz, (size_t)lda * rsz,
                                  (size_t)dev[k]->nrows, cudaMemcpyDeviceToHost, copy_stream_));
         }
+        if (profiling_) CK(cudaEventRecord(R.copy_t1[b], copy_stream_));
         CK(cudaEventRecord(R.copy_done[b], copy_stream_));
         if (k >= 1) go = finish(k - 1);
     }

@@ -199,7 +199,7 @@ struct BatchFit {
 enum Stage {
     ST_SETUP = 0, ST_NEIGH, ST_CLUSTERS, ST_BUCKET, ST_FORCE2, ST_VIRIAL2, ST_FORCE3, ST_VIRIAL3, ST_FORCE4,
     ST_VIRIAL4, ST_OTHER, ST_GRAM_ATB, ST_GRAM_SPLIT, ST_GRAM_TC, ST_GRAM_SYRK, ST_REFINE_PRODUCTS,
-    ST_REFINE_PRECOND, ST_COUNT
+    ST_REFINE_PRECOND, ST_HOST_COPY, ST_COUNT
 };
 const char* stage_name(int s);
 
@@ -397,6 +397,7 @@ class Session {
     cudaStream_t copy_stream_ = nullptr;   // device-to-host copies of streamed assemblies
     void* pinned_[2] = {nullptr, nullptr};
     size_t pinned_bytes_[2] = {0, 0};
+    bool pinned_reg_[2] = {false, false};   // registered host memory (else cudaMallocHost)
     unsigned char* mailbox_host_ = nullptr;   // mapped pinned bytes written by peek()
     unsigned char* mailbox_dev_ = nullptr;
     cudaEvent_t side_event_ = nullptr;

@@ -308,10 +308,11 @@ int cg_session_last_counts(const cg_session* s, int64_t* pairs, int64_t* triplet
 int cg_session_last_launches(const cg_session* s, int64_t* launches);
 
 /* Per-stage GPU time: with profiling on, the session records CUDA events around each
- * stage of every assembly (on its own stream).  cg_session_stage_times waits for them
- * and returns accumulated milliseconds and call counts for the CG_NSTAGES stages
+ * stage of every assembly (on its own stream) and around each row block's copy to the
+ * host in the streamed calls (stage "host_copies").  cg_session_stage_times waits for
+ * them and returns accumulated milliseconds and call counts for the CG_NSTAGES stages
  * named by cg_stage_name; cg_session_profile(s, 1) also clears the totals. */
-#define CG_NSTAGES 17
+#define CG_NSTAGES 18
 int cg_session_profile(cg_session* s, int enable);
 int cg_session_stage_times(cg_session* s, double* ms, int64_t* calls);
 const char* cg_stage_name(int stage);
