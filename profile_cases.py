@@ -7,6 +7,7 @@
     python profile_cases.py gram4b [rows]         # split-BF16 Gram of a 4-body FP32 A (51,209 columns)
     python profile_cases.py syrk [rows] [cols]    # FP64 SYRK Gram of a random A
     python profile_cases.py gramrand [rows] [cols]  # split-BF16 Gram of a random FP32 A
+    python profile_cases.py cholesky [n] [tensor]   # blocked Cholesky of a random SPD matrix
     python profile_cases.py serve NATOMS PRECISION NSTEPS  # one NVE request, stage times
 
 Each case runs its launch twice after the set-up, so `ncu -k regex:<kernel> -c 1`
@@ -91,6 +92,22 @@ def main(argv):
             sess.gram(1, A.data_ptr(), cols, rows, cols, b.data_ptr(), 1, G.data_ptr(), h.data_ptr())
         torch.cuda.synchronize()
         print("ok", case, rows, cols)
+        return
+    if case == "cholesky":   # one factorisation; tensor = 1: tensor-core trailing updates
+        n = int(argv[1]) if len(argv) > 1 else 8192
+        tensor = int(argv[2]) if len(argv) > 2 else 1
+        fm = synth.make_workload("water-2b", tmp, nframes=1, seed=3)
+        sess = cg.Session(cg.Model(fm), 0)
+        gen = torch.Generator(device="cuda").manual_seed(11)
+        X = torch.randn(n + 256, n, dtype=torch.float64, device="cuda", generator=gen)
+        G = X.T @ X
+        del X
+        G += 1e-3 * torch.diag(torch.diagonal(G))
+        L = torch.empty_like(G)
+        sess.tune("cholesky_tensor_updates", tensor)
+        sess.cholesky(G.data_ptr(), n, 0.0, L.data_ptr())
+        torch.cuda.synchronize()
+        print("ok", case, n, tensor)
         return
     if case == "syrk":
         rows = int(argv[1]) if len(argv) > 1 else 8192
