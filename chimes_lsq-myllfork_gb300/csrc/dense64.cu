@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(TR_THREADS, 1) k_trsm_panel(double* __restrict
 // T(i, j) = M[i*si + j*sj].  One CTA solves the whole system when n fits its shared
 // memory: blocks of 32 in solve order, warp 0 substitutes within the block with
 // shuffles, then every warp updates the remaining right-hand sides.
-constexpr int TS_THREADS = 1024, TS_SMALL = 8192, TS_BLOCK = 128;
+constexpr int TS_THREADS = 1024, TS_SMALL = 1024, TS_BLOCK = 128;
 __device__ __forceinline__ double tget(const double* M, int64_t si, int64_t sj, int64_t i, int64_t j) {
     return M[i * si + j * sj];
 }
