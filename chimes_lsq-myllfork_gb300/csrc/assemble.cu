@@ -29,15 +29,8 @@ namespace cgd {
 // ---------------------------------------------------------------- slot tables
 // Canonical slot lists: incident slots of canonical position pi, and the rest.
 __device__ __forceinline__ void role_slots(int NB, int pi, int* I, int* O) {
-    if (NB == 3) {
-        const int ti[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-        const int to[3] = {2, 1, 0};
-        I[0] = ti[pi][0]; I[1] = ti[pi][1]; O[0] = to[pi];
-    } else {
-        const int ti[4][3] = {{0, 1, 2}, {0, 3, 4}, {1, 3, 5}, {2, 4, 5}};
-        const int to[4][3] = {{3, 4, 5}, {1, 2, 5}, {0, 2, 4}, {0, 1, 3}};
-        for (int k = 0; k < 3; ++k) { I[k] = ti[pi][k]; O[k] = to[pi][k]; }
-    }
+    for (int k = 0; k < NB - 1; ++k) I[k] = role_slot_in(NB, pi, k);
+    for (int k = 0; k < (NB == 3 ? 1 : 3); ++k) O[k] = role_slot_out(NB, pi, k);
 }
 
 // Basis of the edge that maps to canonical slot s of cluster q: g, h (ord values each,
@@ -273,6 +266,55 @@ __global__ void k_virial2_rows(ModelDev M, FramesDev F, int nslice, const R* __r
     }
 }
 
+// ---------------------------------------------------------------- owner incidence sort
+// The owner's incidences inc.val[c0 .. c0 + nent) (cluster << 2 | member) sorted
+// stably by key = cluster type * 4 + the owner's canonical role: sEnt[k] = entry k,
+// sKey[k] its key, sOrd the entries in key order, and sCnt[key] the end of each key's
+// run (its start is the previous key's end).  Every thread of the CTA calls it; the
+// first barrier keeps a previous pass's readers of sCnt ahead of the reset.
+template <int NBODY>
+__device__ void sort_incidences(const ClusterSet& CS, const Buckets& inc, const int8_t* revs, const int* typ, int N,
+                                int64_t qbase, int64_t c0, int nent, int nkeys, int* sEnt, int* sKey, int* sOrd,
+                                int* sCnt) {
+    const int lane = threadIdx.x & 31;
+    __syncthreads();
+    for (int k = threadIdx.x; k <= nkeys; k += blockDim.x) sCnt[k] = 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < nent; k += blockDim.x) {
+        const int v = inc.val[c0 + k];
+        const int q = v >> 2, m = v & 3;
+        const int4 mm = CS.m[qbase + q];
+        const int T = CS.type[qbase + q];
+        int id = 0, w = 1;
+        for (int t = 0; t < NBODY; ++t) { id += w * (typ[member(mm, t) % N] + 1); w *= 10; }
+        const int pi = revs[id * NBODY + m];
+        sEnt[k] = v;
+        sKey[k] = T * 4 + pi;
+        atomicAdd(&sCnt[T * 4 + pi + 1], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) for (int k = 1; k <= nkeys; ++k) sCnt[k] += sCnt[k - 1];
+    __syncthreads();
+    if (threadIdx.x < 32) {   // stable placement by (type, role), 32 entries at a time
+        for (int b = 0; b < nent; b += 32) {
+            const int k = b + lane;
+            const bool act = k < nent;
+            const int key = act ? sKey[k] : -1 - lane;
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            const int leader = __ffs(peers) - 1;
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            int st = 0;
+            if (act && lane == leader) st = sCnt[key];
+            st = __shfl_sync(0xffffffffu, st, leader);
+            if (act) sOrd[st + rank] = k;
+            __syncwarp();
+            if (act && lane == leader) sCnt[key] = st + __popc(peers);
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------- many-body force rows
 // One CTA per real (owner) atom.  PPT powers per thread cover every allowed power
 // tuple of the largest cluster type, so the accumulators stay in registers.
@@ -326,46 +368,10 @@ __global__ void __launch_bounds__(NT, NBODY == 3 ? (sizeof(R) == 4 ? 3 : 2) : 1)
     const int64_t qbase = CS.ofs[F.atom_ofs[f]];
     const int* typ = F.type + F.atom_ofs[f];
     const int64_t row = F.row_ofs[f] + 3 * (int64_t)a;
-    const int lane = threadIdx.x & 31;
 
     for (int64_t c0 = e0; c0 < e1; c0 += MB_MAX_ENT) {
         const int nent = (int)min((int64_t)MB_MAX_ENT, e1 - c0);
-        for (int k = threadIdx.x; k <= nkeys; k += blockDim.x) sCnt[k] = 0;
-        __syncthreads();
-        for (int k = threadIdx.x; k < nent; k += blockDim.x) {
-            const int v = inc.val[c0 + k];
-            const int q = v >> 2, m = v & 3;
-            const int4 mm = CS.m[qbase + q];
-            const int T = CS.type[qbase + q];
-            int id = 0, w = 1;
-            for (int t = 0; t < NBODY; ++t) { id += w * (typ[member(mm, t) % N] + 1); w *= 10; }
-            const int pi = revs[id * NBODY + m];
-            sEnt[k] = v;
-            sKey[k] = T * 4 + pi;
-            atomicAdd(&sCnt[T * 4 + pi + 1], 1);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) for (int k = 1; k <= nkeys; ++k) sCnt[k] += sCnt[k - 1];
-        __syncthreads();
-        if (threadIdx.x < 32) {   // stable placement by (type, role), 32 entries at a time
-            for (int b = 0; b < nent; b += 32) {
-                const int k = b + lane;
-                const bool act = k < nent;
-                const int key = act ? sKey[k] : -1 - lane;
-                const unsigned peers = __match_any_sync(0xffffffffu, key);
-                const int leader = __ffs(peers) - 1;
-                const int rank = __popc(peers & ((1u << lane) - 1u));
-                int st = 0;
-                if (act && lane == leader) st = sCnt[key];
-                st = __shfl_sync(0xffffffffu, st, leader);
-                if (act) sOrd[st + rank] = k;
-                __syncwarp();
-                if (act && lane == leader) sCnt[key] = st + __popc(peers);
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-        // sCnt[key] now holds the end of each key; starts are the previous key's end
+        sort_incidences<NBODY>(CS, inc, revs, typ, N, qbase, c0, nent, nkeys, sEnt, sKey, sOrd, sCnt);
         for (int T = 0; T < ntypes; ++T) {
             const int gbeg = T == 0 ? 0 : sCnt[T * 4 - 1], gend = sCnt[T * 4 + 3];
             if (gbeg == gend) continue;
@@ -506,6 +512,244 @@ __global__ void __launch_bounds__(NT, NBODY == 3 ? (sizeof(R) == 4 ? 3 : 2) : 1)
                 else { *a0 += R(sx * perm); *a1 += R(sy * perm); *a2 += R(sz * perm); }
             }
             __syncthreads();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- many-body force rows, range form
+// One CTA per owner atom, as k_force_mb, with the powers split differently: each
+// thread takes a contiguous range of S = ceil(n_allowed / NT) powers of a cluster
+// type.  The powers of one column are contiguous, so most columns fall to one thread
+// and are summed in its FMA chain; a column whose powers cross a range boundary is
+// finished by the thread holding its first power, which adds its neighbours' partial
+// sums from shared memory in thread order (so the result does not depend on timing).
+// The clusters of every owner role of a type are tabulated together, CB at a time,
+// and each thread reads each power's table entries for each role from offsN.  With no
+// per-power accumulator arrays two CTAs fit on an SM, and one CTA's table building
+// and barriers overlap the other's FMAs.  blockDim.x (at most rg_max_threads) is chosen
+// by the host (rg_threads).  The frame's PERM_SCALE is folded into the Q table.
+template <int NBODY, typename R>
+__global__ void __launch_bounds__(rg_max_threads((int)sizeof(R)), 2) k_force_rg(ModelDev M, FramesDev F, ClusterSet CS, Buckets inc,
+                                                    const int64_t* key_frame_ofs, const R* __restrict__ pre,
+                                                    R* A, int64_t lda) {
+    constexpr int NP = NBODY == 3 ? 3 : 6;
+    constexpr int NI = NBODY - 1;
+    constexpr int NO = NP - NI;
+    constexpr int CB = mb_force_cb((int)sizeof(R));
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ord = NBODY == 3 ? M.order3 : M.order4;
+    const int ntypes = NBODY == 3 ? M.ntypes3 : M.ntypes4;
+    const ClusterTypeDev* types = NBODY == 3 ? M.types3 : M.types4;
+    const int* grps = NBODY == 3 ? M.grp3 : M.grp4;
+    const int8_t* revs = NBODY == 3 ? M.rev3 : M.rev4;
+    const uint4* offs = NBODY == 3 ? M.offs3 : M.offs4;
+    const int* tcol = NBODY == 3 ? M.tcol3 : M.tcol4;
+    int sizeI = 1, sizeO = 1;
+    for (int k = 0; k < NI; ++k) sizeI *= ord;
+    for (int k = 0; k < NO; ++k) sizeO *= ord;
+    const int per = 3 * sizeI + sizeO;
+    const int nkeys = ntypes * 4;
+    const int NT = blockDim.x;
+    const MbRangeSmem L = mb_range_smem(NBODY, ord, nkeys, NT, (int)sizeof(R));
+    int* sEnt = reinterpret_cast<int*>(smem_raw + L.ent);
+    int* sKey = reinterpret_cast<int*>(smem_raw + L.key);
+    int* sOrd = reinterpret_cast<int*>(smem_raw + L.ord);
+    int* sCnt = reinterpret_cast<int*>(smem_raw + L.cnt);
+    int* sQ = reinterpret_cast<int*>(smem_raw + L.q);
+    int* sM = reinterpret_cast<int*>(smem_raw + L.m);        // owner's member index in each cluster
+    int* sRole = reinterpret_cast<int*>(smem_raw + L.role);  // owner's canonical role in each cluster
+    int* sSg = reinterpret_cast<int*>(smem_raw + L.sg);      // owner's sign on each slot's edge: +1, -1, 0
+    R* sGH = reinterpret_cast<R*>(smem_raw + L.gh);
+    R* sW = reinterpret_cast<R*>(smem_raw + L.w);
+    R* sTab = reinterpret_cast<R*>(smem_raw + L.tab);
+    R* sPart = reinterpret_cast<R*>(smem_raw + L.part);
+
+    const int gatom = blockIdx.x;
+    int lo = 0, hi = F.nframes - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (F.atom_ofs[mid] <= gatom) lo = mid; else hi = mid - 1; }
+    const int f = lo;
+    const int a = gatom - (int)F.atom_ofs[f];
+    const int N = F.natoms[f];
+    const BoxDev& B = F.box[f];
+    const double perm = NBODY == 3 ? B.perm3 : B.perm4;
+    const int64_t kb = key_frame_ofs[f];
+    const int64_t e0 = inc.key_ofs[kb + a], e1 = inc.key_ofs[kb + a + 1];
+    const bool single_pass = (e1 - e0) <= MB_MAX_ENT;
+    const int64_t qbase = CS.ofs[F.atom_ofs[f]];
+    const int* typ = F.type + F.atom_ofs[f];
+    R* const arow = A + (F.row_ofs[f] + 3 * (int64_t)a) * lda;
+    const int tid = threadIdx.x;
+
+    for (int64_t c0 = e0; c0 < e1; c0 += MB_MAX_ENT) {
+        const int nent = (int)min((int64_t)MB_MAX_ENT, e1 - c0);
+        sort_incidences<NBODY>(CS, inc, revs, typ, N, qbase, c0, nent, nkeys, sEnt, sKey, sOrd, sCnt);
+        for (int T = 0; T < ntypes; ++T) {
+            const int gbeg = T == 0 ? 0 : sCnt[T * 4 - 1], gend = sCnt[T * 4 + 3];
+            const ClusterTypeDev& CT = types[T];
+            const int n = CT.n_allowed;
+            if (gbeg == gend || n == 0) continue;
+            const int S = (n + NT - 1) / NT;                   // powers per thread
+            const int pb = min(n, tid * S), pe = min(n, pb + S);
+            const int tb = CT.pow_offset / NP;                 // the type's first power in offs / tcol
+            R* const acol = arow + CT.col_base;
+            // the thread's first column began in an earlier thread's range
+            const bool head = pb < pe && pb > 0 && tcol[tb + pb - 1] == tcol[tb + pb];
+            for (int ch0 = gbeg; ch0 < gend; ch0 += CB) {
+                const int nb = min(CB, gend - ch0);
+                const bool add = !single_pass || ch0 > gbeg;   // later chunks add to the rows
+                if (tid < nb) {
+                    const int k = sOrd[ch0 + tid];
+                    const int v = sEnt[k];
+                    sQ[tid] = v >> 2; sM[tid] = v & 3; sRole[tid] = sKey[k] & 3;
+                    if (pre) {
+                        const int4 mm = CS.m[qbase + (v >> 2)];
+                        int id = 0, w = 1;
+                        for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
+                        for (int s = 0; s < NP; ++s) {
+                            int ea, eb;
+                            slot_edge(M, NBODY, id, s, ea, eb);
+                            sSg[tid * NP + s] = ((v & 3) == ea) ? 1 : (((v & 3) == eb) ? -1 : 0);
+                        }
+                    }
+                }
+                __syncthreads();
+                // (1) per (cluster, slot): basis and the owner's weighted derivative
+                if (pre) {
+                    const int stride = 2 * ord + 4;
+                    for (int t = tid; t < nb * NP; t += NT) {
+                        const int c = t / NP, s = t % NP;
+                        const R* src = pre + ((size_t)(qbase + sQ[c]) * NP + s) * stride;
+                        const int sg = sSg[c * NP + s];
+                        const R ir = sg != 0 ? R(sg) / src[2 * ord] : R(0);   // sign / r in the form's type
+                        const R wx = src[2 * ord + 1] * ir, wy = src[2 * ord + 2] * ir, wz = src[2 * ord + 3] * ir;
+                        R* g = sGH + ((size_t)c * NP + s) * 2 * ord;
+                        R* hw = sW + ((size_t)c * NP + s) * 3 * ord;
+                        for (int j = 0; j < ord; ++j) {
+                            const R gn = src[j], hn = src[ord + j];
+                            g[j] = gn; g[ord + j] = hn;
+                            hw[j] = hn * wx; hw[ord + j] = hn * wy; hw[2 * ord + j] = hn * wz;
+                        }
+                    }
+                } else
+                for (int t = tid; t < nb * NP; t += NT) {
+                    const int c = t / NP, s = t % NP;
+                    const int4 mm = CS.m[qbase + sQ[c]];
+                    int id = 0, w = 1;
+                    for (int u = 0; u < NBODY; ++u) { id += w * (typ[member(mm, u) % N] + 1); w *= 10; }
+                    SlotBasis sb;
+                    R* g = sGH + ((size_t)c * NP + s) * 2 * ord;
+                    slot_basis<R>(M, F, NBODY, f, mm, id, T, s, ord, g, g + ord, sb);
+                    const int m = sM[c];
+                    const double sg = (m == sb.ma) ? 1.0 : ((m == sb.mb) ? -1.0 : 0.0);
+                    const double ir = sg / sb.r;
+                    const R wx = R(sb.rab[0] * ir), wy = R(sb.rab[1] * ir), wz = R(sb.rab[2] * ir);
+                    R* hw = sW + ((size_t)c * NP + s) * 3 * ord;
+                    const R* h = g + ord;
+                    for (int j = 0; j < ord; ++j) { hw[j] = h[j] * wx; hw[ord + j] = h[j] * wy; hw[2 * ord + j] = h[j] * wz; }
+                }
+                __syncthreads();
+                // (2) M_x,y,z over the incident-slot powers, Q (times PERM_SCALE) over
+                // the others, each cluster with its owner's role.  4-body M items cover
+                // one (p0, p1) pair and every p2:
+                //   M[p0,p1,p2] = (w0 h0 g1 + g0 w1 h1)[p0,p1] g2[p2] + (g0 g1)[p0,p1] w2 h2[p2]
+                const int nzm = NI == 3 ? ord * ord : sizeI;   // M items per cluster
+                const int nzt = nzm + sizeO;
+                for (int t = tid; t < nb * nzt; t += NT) {
+                    const int c = t / nzt, z = t % nzt;
+                    const int role = sRole[c];
+                    const R* GH = sGH + (size_t)c * NP * 2 * ord;
+                    const R* HW = sW + (size_t)c * NP * 3 * ord;
+                    R* tab = sTab + (size_t)c * per;
+                    if (z < nzm) {
+                        const int p0 = z % ord, p1 = z / ord % ord;
+                        const R* g0 = GH + (size_t)role_slot_in(NBODY, role, 0) * 2 * ord;
+                        const R* g1 = GH + (size_t)role_slot_in(NBODY, role, 1) * 2 * ord;
+                        const R* w0 = HW + (size_t)role_slot_in(NBODY, role, 0) * 3 * ord;
+                        const R* w1 = HW + (size_t)role_slot_in(NBODY, role, 1) * 3 * ord;
+                        if constexpr (NI == 2) {
+                            tab[z] = w0[p0] * g1[p1] + w1[p1] * g0[p0];
+                            tab[sizeI + z] = w0[ord + p0] * g1[p1] + w1[ord + p1] * g0[p0];
+                            tab[2 * sizeI + z] = w0[2 * ord + p0] * g1[p1] + w1[2 * ord + p1] * g0[p0];
+                        } else {
+                            const R* g2 = GH + (size_t)role_slot_in(NBODY, role, 2) * 2 * ord;
+                            const R* w2 = HW + (size_t)role_slot_in(NBODY, role, 2) * 3 * ord;
+                            const R a0 = g0[p0], a1 = g1[p1];
+                            const R gg = a0 * a1;
+                            const R bx = w0[p0] * a1 + a0 * w1[p1];
+                            const R by = w0[ord + p0] * a1 + a0 * w1[ord + p1];
+                            const R bz = w0[2 * ord + p0] * a1 + a0 * w1[2 * ord + p1];
+                            for (int p2 = 0; p2 < ord; ++p2) {
+                                const int zz = z + p2 * ord * ord;
+                                const R c2 = g2[p2];
+                                tab[zz] = bx * c2 + gg * w2[p2];
+                                tab[sizeI + zz] = by * c2 + gg * w2[ord + p2];
+                                tab[2 * sizeI + zz] = bz * c2 + gg * w2[2 * ord + p2];
+                            }
+                        }
+                    } else {
+                        int zz = z - nzm;
+                        R prod = R(perm);
+                        for (int u = 0; u < NO; ++u) {
+                            prod *= GH[(size_t)role_slot_out(NBODY, role, u) * 2 * ord + zz % ord];
+                            zz /= ord;
+                        }
+                        tab[3 * sizeI + (z - nzm)] = prod;
+                    }
+                }
+                __syncthreads();
+                // (3) the thread's powers: 3 FMAs per (power, cluster), summed per column
+                int rs[NBODY], re[NBODY];   // each role's clusters within the chunk
+#pragma unroll
+                for (int r = 0; r < NBODY; ++r) {
+                    const int key = T * 4 + r;
+                    rs[r] = max(key == 0 ? 0 : sCnt[key - 1], ch0) - ch0;
+                    re[r] = min(sCnt[key], ch0 + nb) - ch0;
+                }
+                auto put = [&](int col, R x, R y, R z) {
+                    R* p0 = acol + col;
+                    if (add) { p0[0] += x; p0[lda] += y; p0[2 * lda] += z; }
+                    else { p0[0] = x; p0[lda] = y; p0[2 * lda] = z; }
+                };
+                R ax = R(0), ay = R(0), az = R(0);
+                int pcol = -1;
+                bool first = true;   // still in the thread's first column
+                for (int p = pb; p < pe; ++p) {
+                    const int col = tcol[tb + p];
+                    if (p > pb && col != pcol) {   // column pcol ended at p - 1
+                        if (first && head) { sPart[3 * tid] = ax; sPart[3 * tid + 1] = ay; sPart[3 * tid + 2] = az; }
+                        else put(pcol, ax, ay, az);
+                        first = false;
+                        ax = ay = az = R(0);
+                    }
+                    pcol = col;
+                    const uint4 o4 = offs[tb + p];
+                    const uint32_t ow[4] = {o4.x, o4.y, o4.z, o4.w};
+#pragma unroll
+                    for (int r = 0; r < NBODY; ++r) {
+                        const int oM = (int)(ow[r] & 0xffffu), oQ = (int)(ow[r] >> 16);
+                        for (int c = rs[r]; c < re[r]; ++c) {
+                            const R* tab = sTab + (size_t)c * per;
+                            const R qv = tab[oQ];
+                            ax += tab[oM] * qv; ay += tab[sizeI + oM] * qv; az += tab[2 * sizeI + oM] * qv;
+                        }
+                    }
+                }
+                bool tail = false;   // the last column continues into later ranges
+                if (pb < pe) {
+                    const bool ends = pe == n || tcol[tb + pe] != pcol;
+                    if (first && head) { sPart[3 * tid] = ax; sPart[3 * tid + 1] = ay; sPart[3 * tid + 2] = az; }
+                    else if (ends) put(pcol, ax, ay, az);
+                    else tail = true;
+                }
+                __syncthreads();
+                if (tail) {   // add the later ranges' partials of this column in thread order
+                    const int last = (grps[CT.grp_offset + pcol + 1] - 1) / S;
+                    for (int t2 = tid + 1; t2 <= last; ++t2) {
+                        ax += sPart[3 * t2]; ay += sPart[3 * t2 + 1]; az += sPart[3 * t2 + 2];
+                    }
+                    put(pcol, ax, ay, az);
+                }
+            }
         }
     }
 }
@@ -815,6 +1059,42 @@ static void force_mb_ppt(int ppt, int nreal, size_t smem, const ModelDev& M, con
         set_smem(k_force_mb<NBD, R, 8>, smem);
         k_force_mb<NBD, R, 8><<<nreal, MB_THREADS, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
     }
+}
+
+template <int NBD, typename R>
+static void force_rg(int nreal, int nt, size_t smem, const ModelDev& M, const FramesDev& F, const ClusterSet& CS,
+                     const Buckets& inc, const int64_t* kfo, const R* pre, R* A, int64_t lda, cudaStream_t st) {
+    set_smem(k_force_rg<NBD, R>, smem);
+    k_force_rg<NBD, R><<<nreal, nt, smem, st>>>(M, F, CS, inc, kfo, pre, A, lda);
+}
+
+int rg_threads(const int* n_allowed, int ntypes, int rsize) {
+    const int mx = rg_max_threads(rsize);
+    if (rsize != 8) return mx;
+    int best = mx;
+    long long best_idle = -1;
+    for (int nt = mx; nt >= mx / 2; nt -= 32) {
+        long long idle = 0;
+        for (int t = 0; t < ntypes; ++t) {
+            const int n = n_allowed[t];
+            if (n > 0) idle += (long long)((n + nt - 1) / nt) * nt - n;
+        }
+        if (best_idle < 0 || idle < best_idle) { best_idle = idle; best = nt; }
+    }
+    return best;
+}
+
+void launch_force_rg(int nbody, int prec, int nreal, int nt, size_t smem, const ModelDev& M, const FramesDev& F,
+                     const ClusterSet& CS, const Buckets& inc, const int64_t* kfo, const void* pre, void* A,
+                     int64_t lda, cudaStream_t st) {
+    if (nbody == 3 && prec == 0)
+        force_rg<3, double>(nreal, nt, smem, M, F, CS, inc, kfo, (const double*)pre, (double*)A, lda, st);
+    else if (nbody == 3)
+        force_rg<3, float>(nreal, nt, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st);
+    else if (prec == 0)
+        force_rg<4, double>(nreal, nt, smem, M, F, CS, inc, kfo, (const double*)pre, (double*)A, lda, st);
+    else
+        force_rg<4, float>(nreal, nt, smem, M, F, CS, inc, kfo, (const float*)pre, (float*)A, lda, st);
 }
 
 void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,

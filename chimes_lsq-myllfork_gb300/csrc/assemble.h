@@ -43,6 +43,40 @@ __host__ __device__ inline MbForceSmem mb_force_smem(int nbody, int ord, int nke
     return s;
 }
 
+// Range form of the force kernel (k_force_rg): at most rg_max_threads threads, two CTAs
+// per SM (384 in FP64, where 80 registers a thread keep the FMA loop out of local
+// memory; 512 in FP32, whose shorter latency-bound loop gains from the extra warps).
+// Shared memory: the incidence sort, then per chunk of mb_force_cb clusters (of every
+// owner role) the slot bases, the owner-weighted derivatives and the M / Q tables,
+// and one partial column sum (3 values) per thread.
+__host__ __device__ constexpr int rg_max_threads(int rsize) { return rsize == 8 ? 384 : 512; }
+struct MbRangeSmem {
+    size_t ent, key, ord, cnt, q, m, role, sg, gh, w, tab, part, total;
+};
+__host__ __device__ inline MbRangeSmem mb_range_smem(int nbody, int ord, int nkeys, int nt, int rsize) {
+    const int np = nbody == 3 ? 3 : 6, ni = nbody - 1, no = np - ni;
+    int sizeI = 1, sizeO = 1;
+    for (int k = 0; k < ni; ++k) sizeI *= ord;
+    for (int k = 0; k < no; ++k) sizeO *= ord;
+    const size_t per = 3 * (size_t)sizeI + sizeO;
+    const int cb = mb_force_cb(rsize);
+    MbRangeSmem s;
+    s.ent = 0;
+    s.key = align16(s.ent + MB_MAX_ENT * sizeof(int));
+    s.ord = align16(s.key + MB_MAX_ENT * sizeof(int));
+    s.cnt = align16(s.ord + MB_MAX_ENT * sizeof(int));
+    s.q = align16(s.cnt + (nkeys + 1) * sizeof(int));
+    s.m = align16(s.q + cb * sizeof(int));
+    s.role = align16(s.m + cb * sizeof(int));
+    s.sg = align16(s.role + cb * sizeof(int));
+    s.gh = align16(s.sg + cb * 6 * sizeof(int));
+    s.w = align16(s.gh + (size_t)cb * np * 2 * ord * rsize);
+    s.tab = align16(s.w + (size_t)cb * np * 3 * ord * rsize);
+    s.part = align16(s.tab + (size_t)cb * per * rsize);
+    s.total = align16(s.part + (size_t)nt * 3 * rsize);
+    return s;
+}
+
 struct MbVirSmem {
     size_t q, gh, v, tab, total;
 };
@@ -102,6 +136,15 @@ void launch_cluster_basis(int nbody, int prec, int64_t nclusters, const ModelDev
 void launch_force_mb(int nbody, int prec, int ppt, int nreal, size_t smem, const ModelDev& M, const FramesDev& F,
                      const ClusterSet& CS, const Buckets& inc, const int64_t* key_frame_ofs, const void* pre,
                      void* A, int64_t lda, cudaStream_t st, int nt4 = MB_THREADS);
+// The same rows by the range form (k_force_rg) on nt threads per CTA;
+// smem = mb_range_smem(..., nt, ...).total.
+void launch_force_rg(int nbody, int prec, int nreal, int nt, size_t smem, const ModelDev& M, const FramesDev& F,
+                     const ClusterSet& CS, const Buckets& inc, const int64_t* key_frame_ofs, const void* pre,
+                     void* A, int64_t lda, cudaStream_t st);
+// Threads per CTA of k_force_rg.  FP64: the multiple of 32 in [max / 2, max] whose
+// ranges of ceil(n / threads) powers leave the fewest idle lanes (which still occupy
+// the FP64 pipe) over the cluster types' allowed-power counts; FP32: the maximum.
+int rg_threads(const int* n_allowed, int ntypes, int rsize);
 // Stress/energy rows: nchunks_max cluster chunks of VIR_CLUSTERS per (frame, type);
 // part holds nframes*ntypes*nchunks_max*7*ntrue_max partial sums (R).
 // ppt: powers per thread, 1 when every cluster type has at most MB_THREADS allowed

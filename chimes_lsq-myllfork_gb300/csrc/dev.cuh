@@ -57,7 +57,28 @@ struct ModelDev {
     const ClusterTypeDev* types4;
     const uint8_t* pow4;
     const int* grp4;
+    // Per allowed power (indexed pow_offset / nslots + p): for each canonical role pi
+    // of the owner, the power's entries in a cluster's force table (see k_force_rg):
+    // low 16 bits the M_x index, high 16 bits the Q index.  And the column of the
+    // power within its type (PARAM_INDICES).
+    const uint4* offs3;
+    const int* tcol3;
+    const uint4* offs4;
+    const int* tcol4;
 };
+
+// Canonical slots incident to the member at canonical position pi (nb - 1 of them,
+// k-th returned by role_slot_in) and the other slots (role_slot_out).  Edges of a
+// triplet: 0 = (0,1), 1 = (0,2), 2 = (1,2); of a quadruplet: 0 = (0,1), 1 = (0,2),
+// 2 = (0,3), 3 = (1,2), 4 = (1,3), 5 = (2,3).  Packed 4 bits per entry:
+//   3-body in  {0,1} {0,2} {1,2}                out {2} {1} {0}
+//   4-body in  {0,1,2} {0,3,4} {1,3,5} {2,4,5}  out {3,4,5} {1,2,5} {0,2,4} {0,1,3}
+__host__ __device__ constexpr int role_slot_in(int nb, int pi, int k) {
+    return nb == 3 ? (int)((0x212010ull >> (4 * (2 * pi + k))) & 15) : (int)((0x542531430210ull >> (4 * (3 * pi + k))) & 15);
+}
+__host__ __device__ constexpr int role_slot_out(int nb, int pi, int k) {
+    return nb == 3 ? (int)((0x012ull >> (4 * pi)) & 15) : (int)((0x310420521543ull >> (4 * (3 * pi + k))) & 15);
+}
 
 // ---------------------------------------------------------------- frame batch
 struct BoxDev {

@@ -44,9 +44,9 @@ static void rev_index(const ClusterType& ct, const int* types, int n, int8_t* ou
     }
 }
 
-static void upload_list(const Model& m, const ClusterList& cl, int nb, int col_base, int pchunk, DeviceModel& D,
+static void upload_list(const Model& m, const ClusterList& cl, int nb, int ord, int col_base, int pchunk, DeviceModel& D,
                         const int** int_map, const int8_t** pidx, const int8_t** rev, const cgd::ClusterTypeDev** types,
-                        const uint8_t** pows, const int** grps, int& max_allowed) {
+                        const uint8_t** pows, const int** grps, const uint4** offs, const int** tcols, int& max_allowed) {
     const int np = nb == 3 ? 3 : 6;
     const int dim = nb == 3 ? 1000 : 10000;
     std::vector<int> imap(dim, -1);
@@ -62,6 +62,10 @@ static void upload_list(const Model& m, const ClusterList& cl, int nb, int col_b
     std::vector<cgd::ClusterTypeDev> tv(cl.vec.size());
     std::vector<uint8_t> pw;
     std::vector<int> gp;
+    std::vector<uint4> of;      // force-table entries of each power for each owner role
+    std::vector<int> tc;        // column of each power within its type
+    int sizeI = 1;
+    for (int k = 0; k < nb - 1; ++k) sizeI *= ord;
     int col = col_base;
     max_allowed = 0;
     for (size_t t = 0; t < cl.vec.size(); ++t) {
@@ -77,6 +81,17 @@ static void upload_list(const Model& m, const ClusterList& cl, int nb, int col_b
         max_allowed = std::max(max_allowed, d.n_allowed);
         for (int p = 0; p < d.n_allowed; ++p)
             for (int s = 0; s < np; ++s) pw.push_back((uint8_t)ct.allowed_powers[p][s]);
+        for (int p = 0; p < d.n_allowed; ++p) {
+            uint32_t e[4] = {0, 0, 0, 0};
+            for (int pi = 0; pi < nb; ++pi) {
+                int ii = 0, oo = 0;
+                for (int k = nb - 2; k >= 0; --k) ii = ii * ord + ct.allowed_powers[p][cgd::role_slot_in(nb, pi, k)];
+                for (int k = np - nb; k >= 0; --k) oo = oo * ord + ct.allowed_powers[p][cgd::role_slot_out(nb, pi, k)];
+                e[pi] = (uint32_t)ii | ((uint32_t)(3 * sizeI + oo) << 16);
+            }
+            of.push_back(make_uint4(e[0], e[1], e[2], e[3]));
+            tc.push_back(ct.param_indices[p]);
+        }
         // column groups: PARAM_INDICES is non-decreasing with contiguous groups
         int c = 0;
         for (int p = 0; p < d.n_allowed; ++p) {
@@ -115,6 +130,9 @@ static void upload_list(const Model& m, const ClusterList& cl, int nb, int col_b
     *types = dev_upload(D.allocs, tv.data(), tv.size());
     *pows = dev_upload(D.allocs, pw.data(), pw.size());
     *grps = dev_upload(D.allocs, gp.data(), gp.size());
+    if (of.empty()) { of.push_back(make_uint4(0, 0, 0, 0)); tc.push_back(0); }
+    *offs = dev_upload(D.allocs, of.data(), of.size());
+    *tcols = dev_upload(D.allocs, tc.data(), tc.size());
 }
 
 DeviceModel::DeviceModel(const Model& m, int vir_pchunk) {
@@ -145,11 +163,11 @@ DeviceModel::DeviceModel(const Model& m, int vir_pchunk) {
     for (const auto& p : m.pairs) pv.push_back({p.smin, p.smax, p.lambda, p.xavg, p.xdiff, p.col});
     d.pairs = dev_upload(allocs, pv.data(), pv.size());
     if (c.use3)
-        upload_list(m, m.trips, 3, d.col3, vir_pchunk, *this, &d.int_map3, &d.pidx3, &d.rev3, &d.types3, &d.pow3,
-                    &d.grp3, max_allowed3);
+        upload_list(m, m.trips, 3, c.cheby3, d.col3, vir_pchunk, *this, &d.int_map3, &d.pidx3, &d.rev3, &d.types3,
+                    &d.pow3, &d.grp3, &d.offs3, &d.tcol3, max_allowed3);
     if (c.use4)
-        upload_list(m, m.quads, 4, d.col4, vir_pchunk, *this, &d.int_map4, &d.pidx4, &d.rev4, &d.types4, &d.pow4,
-                    &d.grp4, max_allowed4);
+        upload_list(m, m.quads, 4, c.cheby4, d.col4, vir_pchunk, *this, &d.int_map4, &d.pidx4, &d.rev4, &d.types4,
+                    &d.pow4, &d.grp4, &d.offs4, &d.tcol4, max_allowed4);
 }
 
 DeviceModel::~DeviceModel() {
@@ -799,10 +817,20 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
         cgd::launch_bucket(nf, F, spec2, byt, st); L();
         mark(ST_BUCKET, false);
         const int ppt = (max_allowed + cgd::MB_THREADS - 1) / cgd::MB_THREADS;
-        if (ppt > 8) throw Error(2, "too many allowed powers for the device force kernel");
         const int pp = ppt <= 1 ? 1 : (ppt <= 2 ? 2 : 8);
-        cgd::MbForceSmem Lf = cgd::mb_force_smem(nbody, ord, ntypes * 4, max_allowed, rsize);
-        if (Lf.total > 227 * 1024) throw Error(2, "cluster order too large for the device force kernel");
+        // range form in FP64, and in FP32 where a type has more powers than the per-power
+        // form has threads (with one power per thread that form fits three CTAs per SM)
+        const bool range = force_range_ == 2 || (force_range_ == 1 && (prec == 0 || ppt > 1));
+        int rg_nt = cgd::rg_max_threads(rsize);
+        if (range) {
+            std::vector<int> na;
+            for (const auto& ct : (nbody == 3 ? model.trips : model.quads).vec) na.push_back(ct.excluded ? 0 : ct.n_allowed);
+            rg_nt = cgd::rg_threads(na.data(), (int)na.size(), rsize);
+        }
+        const size_t force_smem = range ? cgd::mb_range_smem(nbody, ord, ntypes * 4, rg_nt, rsize).total
+                                        : cgd::mb_force_smem(nbody, ord, ntypes * 4, max_allowed, rsize).total;
+        if (!range && ppt > 8) throw Error(2, "too many allowed powers for the device force kernel");
+        if (force_smem > 227 * 1024) throw Error(2, "cluster order too large for the device force kernel");
         mark(nbody == 3 ? ST_FORCE3 : ST_FORCE4, true);
         // slot bases once per cluster (the force kernel meets each cluster once per
         // member, the stress kernel once more); evaluated in place when the fixed
@@ -813,8 +841,12 @@ void Session::run(const DeviceFrames& df, int precision, void* A, int64_t lda, A
             pre = prec == 0 ? (void*)S.get<double>(nbasis) : (void*)S.get<float>(nbasis);
             cgd::launch_cluster_basis(nbody, prec, nq, M, F, CS, pre, st); L();
         }
-        cgd::launch_force_mb(nbody, prec, pp, nreal, Lf.total, M, F, CS, inc, kfo_atoms, pre, A, lda, st,
-                             force4_threads_); L();
+        if (range)
+            cgd::launch_force_rg(nbody, prec, nreal, rg_nt, force_smem, M, F, CS, inc, kfo_atoms, pre, A, lda, st);
+        else
+            cgd::launch_force_mb(nbody, prec, pp, nreal, force_smem, M, F, CS, inc, kfo_atoms, pre, A, lda, st,
+                                 force4_threads_);
+        L();
         mark(nbody == 3 ? ST_FORCE3 : ST_FORCE4, false);
         CK(cudaGetLastError());
         if (virial) {

@@ -280,6 +280,9 @@ class Session {
     void set_refine_cache_bytes(int64_t v) { refine_cache_bytes_ = v; }
     // Threads per CTA of the 4-body force kernel (512 or 1024).
     void set_force4_threads(int v) { force4_threads_ = v == 1024 ? 1024 : 512; }
+    // many-body force rows: the range form (k_force_rg) never (0), where a cluster type
+    // has more allowed powers than MB_THREADS (1), or always (2); else k_force_mb
+    void set_force_range(int v) { force_range_ = v < 0 ? 0 : (v > 2 ? 2 : v); }
     // Cholesky trailing updates by exact BF16 digit products on the tensor cores
     // (FP64-accurate) or by the FP64 SYRK.
     void set_cholesky_tensor_updates(bool v) { chol_tensor_ = v; }
@@ -409,6 +412,7 @@ class Session {
     int64_t gram_rows_per_launch_ = 0;
     int64_t refine_cache_bytes_ = -1;
     int force4_threads_ = 512;
+    int force_range_ = 1;
     bool chol_tensor_ = true;
     int64_t gram_plane_rows(int64_t nrows, int ncols) const;
     double md_skin_ = 0.5;   // Angstrom; 0: enumerate every step

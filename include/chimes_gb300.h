@@ -539,8 +539,12 @@ void cg_batch_fit_free(cg_batch_fit* b);
  * faster but their FP32 sums lose accuracy, which costs refinement passes);
  * "refine_cache_mb" (device memory the streamed refinement may fill with FP64 row
  * blocks kept between passes, in MiB; -1 = what is free beyond a margin, the
- * default; 0 = assemble every block on every pass); "force4_threads" (threads per CTA
- * of the 4-body force-row kernel, 512 or 1024); "cholesky_tensor_updates" (1, the
+ * default; 0 = assemble every block on every pass); "force_range" (the many-body
+ * force rows by the range form, each thread summing a contiguous range of a cluster
+ * type's powers per column: 1, the default, where a type has more than 512 allowed
+ * powers; 2 always; 0 never -- one accumulator per power, summed per column in shared
+ * memory); "force4_threads" (threads per CTA of the 4-body force-row kernel when the
+ * range form is not used, 512 or 1024); "cholesky_tensor_updates" (1, the
  * default: the blocked Cholesky's trailing updates from exact BF16 digit products on
  * the tensor cores, FP64-accurate; 0: the FP64 SYRK). */
 int cg_session_tune(cg_session* s, const char* key, int value);

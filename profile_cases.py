@@ -9,6 +9,7 @@
     python profile_cases.py gramrand [rows] [cols]  # split-BF16 Gram of a random FP32 A
     python profile_cases.py cholesky [n] [tensor]   # blocked Cholesky of a random SPD matrix
     python profile_cases.py serve NATOMS PRECISION NSTEPS  # one NVE request, stage times
+    python profile_cases.py forms4b [nframes]     # both force-row forms: stage times, agreement
 
 Each case runs its launch twice after the set-up, so `ncu -k regex:<kernel> -c 1`
 captures a warm launch; the synthetic inputs are seeded.
@@ -50,6 +51,36 @@ def main(argv):
             for _ in range(2):
                 sess.gram(1, A.data_ptr(), ncols, nrows, ncols, b.data_ptr(), 1, G.data_ptr(), h.data_ptr())
         torch.cuda.synchronize()
+        print("ok", case, nrows, ncols)
+        return
+    if case == "forms4b":   # the range and per-power forms of the force rows, FP64 and FP32
+        nframes = int(argv[1]) if len(argv) > 1 else 50
+        fm = synth.make_workload("chno-4b", tmp, nframes=nframes, seed=2024, labels=False)
+        model = cg.Model(fm)
+        fr = cg.Frames.read(model)
+        sess = cg.Session(model, 0)
+        nrows, _ = fr.rows()
+        ncols = model.ncols
+        dfr = sess.upload(fr)
+        for prec, dt in ((cg.CG_FP64, torch.float64), (cg.CG_FP32, torch.float32)):
+            outs = {}
+            for form in (2, 0):
+                sess.tune("force_range", form)
+                A = torch.empty((nrows, ncols), dtype=dt, device="cuda")
+                sess.assemble_device(dfr, prec, A.data_ptr(), ncols)
+                sess.profile(True)
+                for _ in range(3):
+                    sess.assemble_device(dfr, prec, A.data_ptr(), ncols)
+                torch.cuda.synchronize()
+                st = sess.stage_times()
+                sess.profile(False)
+                outs[form] = A
+                ms = {k: round(v[0] / 3, 2) for k, v in st.items() if k.startswith(("force", "virial"))}
+                print(f"prec {prec} force_range {form} ms per assembly of {nframes} frames: {ms}", flush=True)
+            d = (outs[2].double() - outs[0].double()).abs().max().item()
+            print(f"prec {prec}: max |range - per-power| / max |A| = {d / outs[0].double().abs().max().item():.3e}",
+                  flush=True)
+            del outs
         print("ok", case, nrows, ncols)
         return
     if case in ("assemble4b", "gram4b"):

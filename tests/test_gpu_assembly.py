@@ -90,13 +90,14 @@ def test_water3b_matches_oracle(cg, oracle, session_for, tmp_path_factory):
     assert c["triplets"] > 0
 
 
-@pytest.mark.parametrize("threads", [512, 1024])
-def test_chno4b_matches_oracle(cg, oracle, tmp_path_factory, threads):
-    """The full 4-body basis (3,861 allowed powers per quadruplet type) with either
-    launch shape of the 4-body force-row kernel."""
+@pytest.mark.parametrize("form,threads", [(1, 512), (0, 512), (0, 1024)])
+def test_chno4b_matches_oracle(cg, oracle, tmp_path_factory, form, threads):
+    """The full 4-body basis (3,861 allowed powers per quadruplet type) with the range
+    form of the force-row kernel and both launch shapes of the per-power form."""
     fm = _workload(tmp_path_factory, cg, "chno-4b", 1, 202)
     model = cg.Model(fm)
     sess = cg.Session(model, 0)
+    sess.tune("force_range", form)
     sess.tune("force4_threads", threads)
     frames = cg.Frames.read(model)
     A = sess.assemble(frames, cg.CG_FP64)
@@ -107,6 +108,24 @@ def test_chno4b_matches_oracle(cg, oracle, tmp_path_factory, threads):
     A32 = sess.assemble(frames, cg.CG_FP32).astype(np.float64)
     colmax = np.abs(O).max(axis=0) + 1e-300
     assert (np.abs(A32 - O) / colmax[None, :]).max() < 2e-5
+
+
+@pytest.mark.parametrize("form", [2, 0])
+def test_dense_3body_matches_oracle(cg, oracle, tmp_path_factory, form):
+    """A 6 A 3-body cut-off in liquid water: each owner meets its triplet types far
+    more often than one shared-memory chunk holds, and more than one pass of
+    incidences (above 1024), so the force rows are added over chunks and passes."""
+    fm = _workload(tmp_path_factory, cg, "water-3b", 2, 303, smax=(5.0, 6.0, None))
+    model = cg.Model(fm)
+    sess = cg.Session(model, 0)
+    sess.tune("force_range", form)
+    frames = cg.Frames.read(model)
+    A = sess.assemble(frames, cg.CG_FP64)
+    c = sess.last_counts()
+    assert 3 * c["triplets"] > 1024 * 384 * 2, c   # more than 1024 incidences per owner on average
+    O, _ = oracle.assemble(fm, nthreads=8)
+    ok, err = close_fp64(A, O)
+    assert ok, f"max |gpu - oracle| = {err}"
 
 
 def test_force_rows_sum_to_zero(cg, session_for, tmp_path_factory):
