@@ -617,8 +617,8 @@ def main():
     def sink(first, blk):
         sink_rows[0] += blk.shape[0]
         return False
-    # two untimed calls: the first allocates the pinned staging; copies into freshly
-    # registered host memory run slower for a while on these hosts
+    # two untimed calls: the first allocates the pinned staging (two cudaMallocHost
+    # buffers of one block each) and the device blocks
     for _ in range(2):
         sess.assemble_stream(frames, cg.CG_FP64, sink, block_frames=E2E_BLOCK_FRAMES)
     t0 = time.perf_counter()

@@ -890,6 +890,7 @@ int cg_session_tune(cg_session* s, const char* key, int value) {
         else if (k == "gram_rows_per_launch") s->s->set_gram_rows_per_launch(value);
         else if (k == "force4_threads") s->s->set_force4_threads(value);
         else if (k == "force_range") s->s->set_force_range(value);
+        else if (k == "host_staging") s->s->set_host_staging(value);
         else if (k == "cholesky_tensor_updates") s->s->set_cholesky_tensor_updates(value != 0);
         else if (k == "refine_cache_mb") s->s->set_refine_cache_bytes(value < 0 ? -1 : (int64_t)value << 20);
         else throw cg::Error(1, "unknown tuning key: " + k);

@@ -412,16 +412,18 @@ Session::Session(const Model& m, int device) : model_(m), device_(device) {
 }
 
 namespace {
-// Host staging for device-to-host row blocks: memory aligned to 512 MiB, advised for
-// transparent huge pages and faulted in before it is registered with CUDA, so that a
-// block's copy meets few page mappings.  Multi-GB cudaMallocHost buffers on these hosts
-// took some copies at 60-140 GB/s where such memory held the link's 193 GB/s.
-// Falls back to cudaMallocHost (registered = false) when registration fails.
-void* staging_alloc(size_t bytes, bool& registered) {
+// Host staging for device-to-host row blocks: cudaMallocHost (registered = false), or,
+// with huge_pages, memory aligned to 512 MiB, advised for transparent huge pages and
+// faulted in before it is registered with CUDA (falling back to cudaMallocHost when
+// registration fails).  Measured in a process that had run device-resident assemblies
+// first: 8 GB blocks copied into cudaMallocHost memory at 168-186 GB/s from the first
+// call on, into the registered memory at 39-40 GB/s in the call that allocated it and
+// 159-175 GB/s after (the kernel granted huge pages for only 20-53% of one buffer).
+void* staging_alloc(size_t bytes, bool& registered, bool huge_pages) {
     constexpr size_t kAlign = size_t(512) << 20;
     const size_t sz = (bytes + kAlign - 1) / kAlign * kAlign;
     registered = false;
-    void* p = std::aligned_alloc(kAlign, sz);
+    void* p = huge_pages ? std::aligned_alloc(kAlign, sz) : nullptr;
     if (p) {
         madvise(p, sz, MADV_HUGEPAGE);
         for (size_t o = 0; o < sz; o += 4096) static_cast<volatile char*>(p)[o] = 0;
@@ -584,13 +586,25 @@ void Session::peek(cudaStream_t st, std::initializer_list<PeekItem> items) {
     }
 }
 
+void Session::set_host_staging(int kind) {
+    const bool huge = kind == 0;
+    if (huge == staging_huge_) return;
+    staging_huge_ = huge;
+    for (int i = 0; i < 2; ++i) {   // the next streamed call allocates the new kind
+        staging_free(pinned_[i], pinned_reg_[i]);
+        pinned_[i] = nullptr;
+        pinned_bytes_[i] = 0;
+        pinned_reg_[i] = false;
+    }
+}
+
 void* Session::pinned(int i, size_t bytes) {
     if (i < 0 || i > 1) throw Error(1, "pinned staging index");
     if (pinned_bytes_[i] < bytes) {
         staging_free(pinned_[i], pinned_reg_[i]);
         pinned_[i] = nullptr;
         pinned_bytes_[i] = 0;
-        pinned_[i] = staging_alloc(bytes, pinned_reg_[i]);
+        pinned_[i] = staging_alloc(bytes, pinned_reg_[i], staging_huge_);
         pinned_bytes_[i] = bytes;
     }
     return pinned_[i];

@@ -224,6 +224,9 @@ class Session {
     // Pinned host staging buffer i (0 or 1) of at least `bytes`, kept and grown across
     // calls (streamed assemblies), freed with the session.
     void* pinned(int i, size_t bytes);
+    // host staging of streamed row blocks: 0 = 512 MiB-aligned memory advised for huge
+    // pages and registered with CUDA, 1 = cudaMallocHost (the default)
+    void set_host_staging(int kind);
     // Same pipeline with every per-call device buffer taken from a fixed static
     // device array (no cudaMalloc / cudaMallocAsync / cudaFree in the call).
     void assemble_noalloc(const DeviceFrames& df, int precision, void* A, int64_t lda, AssembleStats* stats);
@@ -401,6 +404,7 @@ class Session {
     void* pinned_[2] = {nullptr, nullptr};
     size_t pinned_bytes_[2] = {0, 0};
     bool pinned_reg_[2] = {false, false};   // registered host memory (else cudaMallocHost)
+    bool staging_huge_ = false;             // staging from huge-page registered memory
     unsigned char* mailbox_host_ = nullptr;   // mapped pinned bytes written by peek()
     unsigned char* mailbox_dev_ = nullptr;
     cudaEvent_t side_event_ = nullptr;

@@ -543,7 +543,10 @@ void cg_batch_fit_free(cg_batch_fit* b);
  * force rows by the range form, each thread summing a contiguous range of a cluster
  * type's powers per column: 1, the default, where a type has more than 512 allowed
  * powers; 2 always; 0 never -- one accumulator per power, summed per column in shared
- * memory); "force4_threads" (threads per CTA of the 4-body force-row kernel when the
+ * memory); "host_staging" (the pinned host buffers of cg_assemble_stream: 1, the
+ * default, cudaMallocHost; 0, 512 MiB-aligned memory advised for transparent huge
+ * pages and registered with CUDA); "force4_threads" (threads per CTA of the 4-body
+ * force-row kernel when the
  * range form is not used, 512 or 1024); "cholesky_tensor_updates" (1, the
  * default: the blocked Cholesky's trailing updates from exact BF16 digit products on
  * the tensor cores, FP64-accurate; 0: the FP64 SYRK). */

@@ -179,3 +179,9 @@ def test_streamed_host_assembly_equals_device_assembly(cg, session_for, tmp_path
     with pytest.raises(cg.ChimesError) as e:
         sess.assemble_stream(frames, cg.CG_FP64, lambda first, blk: True, block_frames=3)
     assert e.value.code == 1
+    sess.tune("host_staging", 0)   # staging in huge-page memory registered with CUDA
+    got = []
+    sess.assemble_stream(frames, cg.CG_FP64, lambda first, blk: got.append((first, blk.copy())) and False,
+                         block_frames=2)
+    assert np.array_equal(np.concatenate([g[1] for g in got]), R)
+    sess.tune("host_staging", 1)
