@@ -3,8 +3,10 @@
 Tunes, on a sample of the batch's own frames, (a) the frames per row block (the
 A buffer a block is assembled into and the K extent of each tensor-core Gram
 launch), (b) the CTAs per SM the Gram aims for when it slices K (which only
-matters when the column count is small), (c) the threads per CTA of the 4-body
-force-row kernel (512 or 1024: one CTA per SM either way, shared memory bound) and
+matters when the column count is small), (c) the threads per CTA of the per-power
+4-body force-row kernel (512 or 1024: one CTA per SM either way, shared memory
+bound; it runs only when the session's "force_range" tunable is 0 -- by default the
+4-body rows use the range form, whose thread count the library picks itself) and
 (d) the rows of A each tensor-core Gram launch sums in FP32 (longer is faster, but
 the FP32 sums lose accuracy; only lengths up to the accuracy limit are offered).
 Each candidate is built as the real graph (sizing pass, capture) and timed with
