@@ -64,8 +64,10 @@ static void upload_list(const Model& m, const ClusterList& cl, int nb, int ord, 
     std::vector<int> gp;
     std::vector<uint4> of;      // force-table entries of each power for each owner role
     std::vector<int> tc;        // column of each power within its type
-    int sizeI = 1;
+    int sizeI = 1, sizeO = 1;
     for (int k = 0; k < nb - 1; ++k) sizeI *= ord;
+    for (int k = 0; k < np - nb + 1; ++k) sizeO *= ord;
+    if (3 * sizeI + sizeO > 65536) throw Error(2, "cluster order too large for the force-table offsets");
     int col = col_base;
     max_allowed = 0;
     for (size_t t = 0; t < cl.vec.size(); ++t) {
