@@ -2,8 +2,8 @@
 
     python profile_cases.py gram [nframes]        # split-BF16 Gram of water-3b A
     python profile_cases.py md NATOMS PRECISION   # MD force of one 4-body system
-    python profile_cases.py assemble [nframes] [fp32]  # A of water-3b frames
-    python profile_cases.py assemble4b [nframes] [fp32]  # A of 256-atom C/H/N/O 4-body frames
+    python profile_cases.py assemble [nframes] [fp32] [form=N]  # A of water-3b frames
+    python profile_cases.py assemble4b [nframes] [fp32] [form=N]  # A of 256-atom C/H/N/O 4-body frames
     python profile_cases.py gram4b [rows]         # split-BF16 Gram of a 4-body FP32 A (51,209 columns)
     python profile_cases.py syrk [rows] [cols]    # FP64 SYRK Gram of a random A
     python profile_cases.py gramrand [rows] [cols]  # split-BF16 Gram of a random FP32 A
@@ -12,7 +12,9 @@
     python profile_cases.py forms4b [nframes]     # both force-row forms: stage times, agreement
 
 Each case runs its launch twice after the set-up, so `ncu -k regex:<kernel> -c 1`
-captures a warm launch; the synthetic inputs are seeded.
+captures a warm launch; the synthetic inputs are seeded.  form=N sets the session's
+force_range tunable (0: the per-power force kernel k_force_mb, 2: the range form
+k_force_rg everywhere; default 1).
 """
 import importlib
 import os
@@ -28,6 +30,8 @@ def main(argv):
     synth = importlib.import_module("chimes_lsq-myllfork_gb300.synth")
     import numpy as np
     import torch
+    form = [int(a.split("=", 1)[1]) for a in argv if a.startswith("form=")]
+    argv = [a for a in argv if not a.startswith("form=")]
     case = argv[0] if argv else "md"
     tmp = tempfile.mkdtemp(prefix="chimes_prof_")
     if case in ("gram", "assemble"):
@@ -36,6 +40,8 @@ def main(argv):
         model = cg.Model(fm)
         fr = cg.Frames.read(model)
         sess = cg.Session(model, 0)
+        if form:
+            sess.tune("force_range", form[0])
         nrows, _ = fr.rows()
         ncols = model.ncols
         dfr = sess.upload(fr)
@@ -89,6 +95,8 @@ def main(argv):
         model = cg.Model(fm)
         fr = cg.Frames.read(model)
         sess = cg.Session(model, 0)
+        if form:
+            sess.tune("force_range", form[0])
         nrows, _ = fr.rows()
         ncols = model.ncols
         dfr = sess.upload(fr)
