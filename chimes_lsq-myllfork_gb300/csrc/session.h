@@ -283,8 +283,9 @@ class Session {
     void set_refine_cache_bytes(int64_t v) { refine_cache_bytes_ = v; }
     // Threads per CTA of the 4-body force kernel (512 or 1024).
     void set_force4_threads(int v) { force4_threads_ = v == 1024 ? 1024 : 512; }
-    // many-body force rows: the range form (k_force_rg) never (0), where a cluster type
-    // has more allowed powers than MB_THREADS (1), or always (2); else k_force_mb
+    // many-body force rows: the range form (k_force_rg) never (0); in FP64, and in FP32
+    // where a cluster type has more allowed powers than MB_THREADS (1, the default);
+    // or always (2); else the per-power form k_force_mb
     void set_force_range(int v) { force_range_ = v < 0 ? 0 : (v > 2 ? 2 : v); }
     // Cholesky trailing updates by exact BF16 digit products on the tensor cores
     // (FP64-accurate) or by the FP64 SYRK.

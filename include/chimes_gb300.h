@@ -541,9 +541,9 @@ void cg_batch_fit_free(cg_batch_fit* b);
  * blocks kept between passes, in MiB; -1 = what is free beyond a margin, the
  * default; 0 = assemble every block on every pass); "force_range" (the many-body
  * force rows by the range form, each thread summing a contiguous range of a cluster
- * type's powers per column: 1, the default, where a type has more than 512 allowed
- * powers; 2 always; 0 never -- one accumulator per power, summed per column in shared
- * memory); "host_staging" (the pinned host buffers of cg_assemble_stream: 1, the
+ * type's powers per column: 1, the default, in FP64 and, in FP32, where a type has
+ * more than 512 allowed powers; 2 always; 0 never -- one accumulator per power, summed
+ * per column in shared memory); "host_staging" (the pinned host buffers of cg_assemble_stream: 1, the
  * default, cudaMallocHost; 0, 512 MiB-aligned memory advised for transparent huge
  * pages and registered with CUDA); "force4_threads" (threads per CTA of the 4-body
  * force-row kernel when the
